@@ -1,0 +1,193 @@
+"""ctypes access to the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the
+checker; the product package never imports this module.
+
+Two libraries:
+  * liboracle.so      -- the plain-C restatement in oracle/sw4_oracle.c (always built
+                         by ``make -C oracle``; builds on x86_64 and aarch64 alike);
+  * _ref/libsw4ref.so -- the reference's own kernels compiled in place from the
+                         reference sources (``make -C oracle ref``), present only
+                         where the reference tree exists.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+
+
+def _dp(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous, (a.dtype, a.flags)
+    return a.ctypes.data_as(_D)
+
+
+def _ip(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(_I)
+
+
+def build(ref: bool = False) -> None:
+    """Build liboracle.so (and the reference kernels when asked and possible)."""
+    target = "ref" if ref else "all"
+    subprocess.run(["make", "-s", "-C", str(HERE), target], check=True)
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = HERE / "liboracle.so"
+        if not path.exists():
+            build()
+        _lib = C.CDLL(str(path))
+        _lib.sw4o_timefunc.restype = C.c_double
+        _lib.sw4o_timefunc_tt.restype = C.c_double
+    return _lib
+
+
+def ref_available() -> bool:
+    return (HERE / "_ref" / "libsw4ref.so").exists()
+
+
+def ref():
+    """The reference's own kernels, or None where they were not built."""
+    global _ref
+    if _ref is None and ref_available():
+        _ref = C.CDLL(str(HERE / "_ref" / "libsw4ref.so"))
+    return _ref
+
+
+# --------------------------------------------------------------------------
+# Thin wrappers.  `which` is "oracle" (the restatement) or "ref" (the reference).
+# Arrays are flat float64 numpy arrays in the layout selected by `soa`.
+# --------------------------------------------------------------------------
+def stencil_coefficients(which="oracle"):
+    acof = np.zeros(384)
+    ghcof = np.zeros(6)
+    bope = np.zeros(48)
+    sbop = np.zeros(5)
+    if which == "ref":
+        ref().sw4ref_stencil_coefficients(_dp(acof), _dp(ghcof), _dp(bope), _dp(sbop))
+    else:
+        lib().sw4o_stencil_coefficients(_dp(acof), _dp(ghcof), _dp(bope), _dp(sbop))
+    return acof, ghcof, bope, sbop
+
+
+def rhs4sg(soa, bounds, nk, onesided, lu, u, mu, la, h, strx, stry, strz, which="oracle"):
+    acof, ghcof, bope, _ = stencil_coefficients("oracle")
+    os_arr, os_p = _ip(onesided)
+    fn = ref().sw4ref_rhs4sg if which == "ref" else lib().sw4o_rhs4sg
+    fn(C.c_int(soa), *[C.c_int(b) for b in bounds], C.c_int(nk), os_p, _dp(acof), _dp(bope),
+       _dp(ghcof), _dp(lu), _dp(u), _dp(mu), _dp(la), C.c_double(h), _dp(strx), _dp(stry),
+       _dp(strz))
+
+
+def predfort(soa, bounds, up, u, um, lu, fo, rho, dt2, which="oracle"):
+    fn = ref().sw4ref_predfort if which == "ref" else lib().sw4o_predfort
+    fn(C.c_int(soa), *[C.c_int(b) for b in bounds], _dp(up), _dp(u), _dp(um), _dp(lu), _dp(fo),
+       _dp(rho), C.c_double(dt2))
+
+
+def corrfort(soa, bounds, up, lu, fo, rho, dt4, which="oracle"):
+    fn = ref().sw4ref_corrfort if which == "ref" else lib().sw4o_corrfort
+    fn(C.c_int(soa), *[C.c_int(b) for b in bounds], _dp(up), _dp(lu), _dp(fo), _dp(rho),
+       C.c_double(dt4))
+
+
+def dpdmtfort(bounds, up, u, um, u2, dt2i, which="oracle"):
+    fn = ref().sw4ref_dpdmtfort if which == "ref" else lib().sw4o_dpdmtfort
+    fn(*[C.c_int(b) for b in bounds], _dp(up), _dp(u), _dp(um), _dp(u2), C.c_double(dt2i))
+
+
+def addsgd(order, soa, bounds, up, u, um, rho, dc, st, co, beta, which="oracle"):
+    if which == "ref":
+        fn = ref().sw4ref_addsgd6 if order == 6 else ref().sw4ref_addsgd4
+    else:
+        fn = lib().sw4o_addsgd6 if order == 6 else lib().sw4o_addsgd4
+    fn(C.c_int(soa), *[C.c_int(b) for b in bounds], _dp(up), _dp(u), _dp(um), _dp(rho),
+       _dp(dc[0]), _dp(dc[1]), _dp(dc[2]), _dp(st[0]), _dp(st[1]), _dp(st[2]), _dp(co[0]),
+       _dp(co[1]), _dp(co[2]), C.c_double(beta))
+
+
+def boundary_windows(bounds, nxyz, bccnd):
+    wind = np.zeros(36, dtype=np.int32)
+    npts = np.zeros(6, dtype=np.int32)
+    bc, bcp = _ip(bccnd)
+    lib().sw4o_boundary_windows(*[C.c_int(b) for b in bounds], *[C.c_int(n) for n in nxyz], bcp,
+                                wind.ctypes.data_as(_I), npts.ctypes.data_as(_I))
+    return wind, npts
+
+
+def bcfortsg(soa, bounds, wind, nxyz, u, h, bccnd, sbop, mu, la, bforce, strx, stry,
+             which="oracle"):
+    w, wp = _ip(wind)
+    bc, bcp = _ip(bccnd)
+    bf = [None if b is None else np.ascontiguousarray(b, dtype=np.float64) for b in bforce]
+    if which == "ref":
+        # the reference kernel dereferences every forcing array it is given for
+        # sides with bccnd 1/2/0; hand it zero arrays of the window size where None
+        bf = [np.zeros(3 * max(1, _wsize(w, s))) if b is None else b for s, b in enumerate(bf)]
+        ref().sw4ref_bcfortsg(C.c_int(soa), *[C.c_int(b) for b in bounds], wp,
+                              *[C.c_int(n) for n in nxyz], _dp(u), C.c_double(h), bcp, _dp(sbop),
+                              _dp(mu), _dp(la), C.c_double(0.0), *[_dp(b) for b in bf],
+                              _dp(strx), _dp(stry))
+    else:
+        arr = (_D * 6)(*[(_dp(b) if b is not None else _D()) for b in bf])
+        lib().sw4o_bcfortsg(C.c_int(soa), *[C.c_int(b) for b in bounds], wp,
+                            *[C.c_int(n) for n in nxyz], _dp(u), C.c_double(h), bcp, _dp(sbop),
+                            _dp(mu), _dp(la), arr, _dp(strx), _dp(stry))
+
+
+def _wsize(w, s):
+    ww = w[6 * s:6 * s + 6]
+    return max(0, (ww[1] - ww[0] + 1) * (ww[3] - ww[2] + 1) * (ww[5] - ww[4] + 1))
+
+
+def supergrid_profile(first, last, h, xmin, left, right, x0, x1, width):
+    n = last - first + 1
+    dc, st, co = np.zeros(n), np.zeros(n), np.zeros(n)
+    lib().sw4o_supergrid_profile(C.c_int(first), C.c_int(last), C.c_double(h), C.c_double(xmin),
+                                 C.c_int(int(left)), C.c_int(int(right)), C.c_double(x0),
+                                 C.c_double(x1), C.c_double(width), _dp(dc), _dp(st), _dp(co))
+    return dc, st, co
+
+
+def timefunc(kind, freq, t, tt=False):
+    f = lib().sw4o_timefunc_tt if tt else lib().sw4o_timefunc
+    return f(C.c_int(kind), C.c_double(freq), C.c_double(t))
+
+
+class Problem(C.Structure):
+    """Mirror of sw4o_problem (oracle/sw4_oracle.h)."""
+    _fields_ = [("ib", C.c_int), ("ie", C.c_int), ("jb", C.c_int), ("je", C.c_int),
+                ("kb", C.c_int), ("ke", C.c_int), ("nx", C.c_int), ("ny", C.c_int),
+                ("nz", C.c_int), ("h", C.c_double), ("dt", C.c_double),
+                ("onesided", C.c_int * 6), ("bccnd", C.c_int * 6), ("wind", C.c_int * 36),
+                ("sg_beta", C.c_double), ("sg_order", C.c_int),
+                ("mu", _D), ("la", _D), ("rho", _D),
+                ("strx", _D), ("stry", _D), ("strz", _D), ("dcx", _D), ("dcy", _D),
+                ("dcz", _D), ("cox", _D), ("coy", _D), ("coz", _D),
+                ("nsrc", C.c_int), ("src_ijk", _I), ("src_amp", _D), ("src_freq", _D),
+                ("src_t0", _D), ("src_kind", _I)]
+
+
+def step(problem: Problem, soa, t, up, u, um, lu, f, uacc):
+    lib().sw4o_step(C.byref(problem), C.c_int(soa), C.c_double(t), _dp(up), _dp(u), _dp(um),
+                    _dp(lu), _dp(f), _dp(uacc))
+
+
+def set_threads(n: int) -> None:
+    os.environ["OMP_NUM_THREADS"] = str(n)

@@ -1,0 +1,216 @@
+// Test infrastructure only: C entry points onto the reference's OWN kernels,
+// compiled from the read-only reference sources into oracle/_ref/libsw4ref.so by
+// oracle/Makefile.  Nothing in the product links or loads this library; tests use
+// it to pin the oracle restatement (oracle/sw4_oracle.c) and bench.py may time it
+// as the CPU baseline when it has been built on the machine in question.
+//
+// The reference's pointwise, damping, boundary and metric kernels are non-virtual
+// member functions of class EW (src/EW.h:220-290).  Their bodies read at most the
+// member m_corder (src/ew-cfromfort.C:45, :75), so the shim calls them on a
+// zero-filled block the size of EW with only m_corder set: the full EW
+// constructor (src/EW.C:162) would parse an input deck and start MPI.
+#include <cstring>
+#include <new>
+#include "sw4.h"
+#include "EW.h"
+#include "SuperGrid.h"
+#include "time_functions.h"
+
+// Free functions compiled from src/rhs4sg.C, rhs4sg_rev.C, rhs4sgcurv.C and
+// rhs4sgcurv_rev.C; declarations as in src/EW.C:141-160.
+void rhs4sg_rev(int, int, int, int, int, int, int, int*, float_sw4*, float_sw4*, float_sw4*,
+                float_sw4*, float_sw4*, float_sw4*, float_sw4*, float_sw4, float_sw4*,
+                float_sw4*, float_sw4*);
+void rhs4sg(int, int, int, int, int, int, int, int*, float_sw4*, float_sw4*, float_sw4*,
+            float_sw4*, float_sw4*, float_sw4*, float_sw4*, float_sw4, float_sw4*, float_sw4*,
+            float_sw4*);
+void rhs4sgcurv_rev(int, int, int, int, int, int, float_sw4*, float_sw4*, float_sw4*,
+                    float_sw4*, float_sw4*, float_sw4*, int*, float_sw4*, float_sw4*,
+                    float_sw4*, float_sw4*, float_sw4*);
+void rhs4sgcurv(int, int, int, int, int, int, float_sw4*, float_sw4*, float_sw4*, float_sw4*,
+                float_sw4*, float_sw4*, int*, float_sw4*, float_sw4*, float_sw4*, float_sw4*,
+                float_sw4*);
+
+namespace {
+EW* kernel_host(int corder)
+{
+   static unsigned char storage[2][sizeof(EW)] __attribute__((aligned(64)));
+   unsigned char* s = storage[corder ? 1 : 0];
+   std::memset(s, 0, sizeof(EW));
+   EW* ew = reinterpret_cast<EW*>(s);
+   ew->m_corder = corder != 0;
+   return ew;
+}
+}  // namespace
+
+extern "C" {
+
+void sw4ref_stencil_coefficients(double* acof, double* ghcof, double* bope, double* sbop)
+{
+   kernel_host(1)->GetStencilCoefficients(acof, ghcof, bope, sbop);
+}
+
+void sw4ref_rhs4sg(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                   int nk, int* onesided, double* acof, double* bope, double* ghcof, double* lu,
+                   double* u, double* mu, double* la, double h, double* strx, double* stry,
+                   double* strz)
+{
+   if (soa)
+      rhs4sg_rev(ifirst, ilast, jfirst, jlast, kfirst, klast, nk, onesided, acof, bope, ghcof, lu,
+                 u, mu, la, h, strx, stry, strz);
+   else
+      rhs4sg(ifirst, ilast, jfirst, jlast, kfirst, klast, nk, onesided, acof, bope, ghcof, lu, u,
+             mu, la, h, strx, stry, strz);
+}
+
+void sw4ref_rhs4sgcurv(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst,
+                       int klast, double* u, double* mu, double* la, double* met, double* jac,
+                       double* lu, int* onesided, double* acof, double* bope, double* ghcof,
+                       double* strx, double* stry)
+{
+   if (soa)
+      rhs4sgcurv_rev(ifirst, ilast, jfirst, jlast, kfirst, klast, u, mu, la, met, jac, lu,
+                     onesided, acof, bope, ghcof, strx, stry);
+   else
+      rhs4sgcurv(ifirst, ilast, jfirst, jlast, kfirst, klast, u, mu, la, met, jac, lu, onesided,
+                 acof, bope, ghcof, strx, stry);
+}
+
+void sw4ref_predfort(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
+                     double* u, double* um, double* lu, double* fo, double* rho, double dt2)
+{
+   kernel_host(soa)->predfort(ib, ie, jb, je, kb, ke, up, u, um, lu, fo, rho, dt2);
+}
+
+void sw4ref_corrfort(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
+                     double* lu, double* fo, double* rho, double dt4)
+{
+   kernel_host(soa)->corrfort(ib, ie, jb, je, kb, ke, up, lu, fo, rho, dt4);
+}
+
+void sw4ref_dpdmtfort(int ib, int ie, int jb, int je, int kb, int ke, double* up, double* u,
+                      double* um, double* u2, double dt2i)
+{
+   kernel_host(1)->dpdmtfort(ib, ie, jb, je, kb, ke, up, u, um, u2, dt2i);
+}
+
+void sw4ref_addsgd4(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                    double* up, double* u, double* um, double* rho, double* dcx, double* dcy,
+                    double* dcz, double* strx, double* stry, double* strz, double* cox,
+                    double* coy, double* coz, double beta)
+{
+   EW* ew = kernel_host(soa);
+   if (soa)
+      ew->addsgd4fort_indrev(ifirst, ilast, jfirst, jlast, kfirst, klast, up, u, um, rho, dcx,
+                             dcy, dcz, strx, stry, strz, cox, coy, coz, beta);
+   else
+      ew->addsgd4fort(ifirst, ilast, jfirst, jlast, kfirst, klast, up, u, um, rho, dcx, dcy, dcz,
+                      strx, stry, strz, cox, coy, coz, beta);
+}
+
+void sw4ref_addsgd6(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                    double* up, double* u, double* um, double* rho, double* dcx, double* dcy,
+                    double* dcz, double* strx, double* stry, double* strz, double* cox,
+                    double* coy, double* coz, double beta)
+{
+   EW* ew = kernel_host(soa);
+   if (soa)
+      ew->addsgd6fort_indrev(ifirst, ilast, jfirst, jlast, kfirst, klast, up, u, um, rho, dcx,
+                             dcy, dcz, strx, stry, strz, cox, coy, coz, beta);
+   else
+      ew->addsgd6fort(ifirst, ilast, jfirst, jlast, kfirst, klast, up, u, um, rho, dcx, dcy, dcz,
+                      strx, stry, strz, cox, coy, coz, beta);
+}
+
+void sw4ref_addsgd4c(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst,
+                     int klast, double* up, double* u, double* um, double* rho, double* dcx,
+                     double* dcy, double* strx, double* stry, double* jac, double* cox,
+                     double* coy, double beta)
+{
+   EW* ew = kernel_host(soa);
+   if (soa)
+      ew->addsgd4cfort_indrev(ifirst, ilast, jfirst, jlast, kfirst, klast, up, u, um, rho, dcx,
+                              dcy, strx, stry, jac, cox, coy, beta);
+   else
+      ew->addsgd4cfort(ifirst, ilast, jfirst, jlast, kfirst, klast, up, u, um, rho, dcx, dcy,
+                       strx, stry, jac, cox, coy, beta);
+}
+
+void sw4ref_bcfortsg(int soa, int ib, int ie, int jb, int je, int kb, int ke, int* wind, int nx,
+                     int ny, int nz, double* u, double h, const int* bccnd_int, double* sbop,
+                     double* mu, double* la, double t, double* bf1, double* bf2, double* bf3,
+                     double* bf4, double* bf5, double* bf6, double* strx, double* stry)
+{
+   boundaryConditionType bccnd[6];
+   for (int s = 0; s < 6; s++) bccnd[s] = static_cast<boundaryConditionType>(bccnd_int[s]);
+   EW* ew = kernel_host(soa);
+   if (soa)
+      ew->bcfortsg_indrev(ib, ie, jb, je, kb, ke, wind, nx, ny, nz, u, h, bccnd, sbop, mu, la, t,
+                          bf1, bf2, bf3, bf4, bf5, bf6, 0.0, 0.0, 0.0, strx, stry);
+   else
+      ew->bcfortsg(ib, ie, jb, je, kb, ke, wind, nx, ny, nz, u, h, bccnd, sbop, mu, la, t, bf1,
+                   bf2, bf3, bf4, bf5, bf6, 0.0, 0.0, 0.0, strx, stry);
+}
+
+int sw4ref_metric(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* x, double* y,
+                  double* z, double* met, double* jac)
+{
+   EW* ew = kernel_host(soa);
+   if (soa) return ew->metric_rev(ib, ie, jb, je, kb, ke, x, y, z, met, jac);
+   return ew->metric(ib, ie, jb, je, kb, ke, x, y, z, met, jac);
+}
+
+void sw4ref_metricexgh(int soa, int ib, int ie, int jb, int je, int kb, int ke, int nz, double* x,
+                       double* y, double* z, double* met, double* jac, int order, double sb,
+                       double zmax, double amp, double xc, double yc, double xl, double yl)
+{
+   EW* ew = kernel_host(soa);
+   if (soa)
+      ew->metricexgh_rev(ib, ie, jb, je, kb, ke, nz, x, y, z, met, jac, order, sb, zmax, amp, xc,
+                         yc, xl, yl);
+   else
+      ew->metricexgh(ib, ie, jb, je, kb, ke, nz, x, y, z, met, jac, order, sb, zmax, amp, xc, yc,
+                     xl, yl);
+}
+
+void sw4ref_freesurfcurvisg(int soa, int ib, int ie, int jb, int je, int kb, int ke, int nz,
+                            int side, double* u, double* mu, double* la, double* met, double* sbop,
+                            double* forcing, double* strx, double* stry)
+{
+   EW* ew = kernel_host(soa);
+   if (soa)
+      ew->freesurfcurvisg_rev(ib, ie, jb, je, kb, ke, nz, side, u, mu, la, met, sbop, forcing,
+                              strx, stry);
+   else
+      ew->freesurfcurvisg(ib, ie, jb, je, kb, ke, nz, side, u, mu, la, met, sbop, forcing, strx,
+                          stry);
+}
+
+// Supergrid profiles through the reference class (src/SuperGrid.C:52-198), sampled
+// as in src/EW.C:4745-4781: x = (q-1)*h + xmin for q in [first,last].
+void sw4ref_supergrid_profile(int first, int last, double h, double xmin, int left, int right,
+                              double x0, double x1, double width, double* dc, double* str,
+                              double* corner)
+{
+   SuperGrid sg;
+   sg.define_taper(left != 0, x0, right != 0, x1, width);
+   for (int q = first; q <= last; q++) {
+      double x = (q - 1) * h + xmin;
+      dc[q - first] = sg.dampingCoeff(x);
+      str[q - first] = sg.stretching(x);
+      corner[q - first] = sg.cornerTaper(x);
+   }
+}
+
+// Source time functions (src/time_functions.C): kind 0 Gaussian, 1 C6SmoothBump.
+// par[0] is the underflow cut-off exponent the reference's Source sets (-700,
+// src/Source.C:2183-2187).
+double sw4ref_timefunc(int kind, double freq, double t, int tt)
+{
+   double par[2] = {-700.0, 0.0};
+   int ipar[1] = {0};
+   if (kind == 0) return tt ? Gaussian_tt(freq, t, par, 2, ipar, 1) : Gaussian(freq, t, par, 2, ipar, 1);
+   return tt ? C6SmoothBump_tt(freq, t, par, 2, ipar, 1) : C6SmoothBump(freq, t, par, 2, ipar, 1);
+}
+
+}  // extern "C"

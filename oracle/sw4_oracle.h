@@ -1,0 +1,118 @@
+/*
+ * CPU oracle for the sw4lite elastic time step -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference's CPU kernels for the hot path, used by
+ * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the checker.
+ * The product (sw4lite_gb300/) never links, loads or calls it.
+ *
+ * Parity pin: tests/test_oracle_pin.py compares every function here with the
+ * reference's own kernels compiled from the reference sources into
+ * oracle/_ref/libsw4ref.so (built by `make -C oracle ref` where the reference tree
+ * exists), and tests/golden/ holds fixtures generated from that library so the pin
+ * also travels to machines without the reference tree.
+ *
+ * Conventions follow the reference: inclusive, 1-based (Fortran-style) bounds
+ * [ib,ie]x[jb,je]x[kb,ke] that include 2 ghost points per side; i fastest.
+ * `soa` selects the component layout: soa=1 is the reference's "_rev/_indrev"
+ * layout u[c*npts + p] (src/rhs4sg_rev.C:60-62), soa=0 the AoS layout u[3*p + c]
+ * (src/rhs4sg.C:53).  All arithmetic is IEEE double.
+ */
+#ifndef SW4G_ORACLE_H
+#define SW4G_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* SBP coefficient tables, layout as src/ew-cfromfort.C:1487-1944. */
+void sw4o_stencil_coefficients(double acof[384], double ghcof[6], double bope[48], double sbop[5]);
+
+/* Lu = div(sigma(u)) / rho-less, 4th-order SBP (src/rhs4sg_rev.C:44, src/rhs4sg.C:38). */
+void sw4o_rhs4sg(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                 int nk, const int onesided[6], const double* acof, const double* bope,
+                 const double* ghcof, double* lu, const double* u, const double* mu,
+                 const double* la, double h, const double* strx, const double* stry,
+                 const double* strz);
+
+/* Pointwise time-level updates (src/ew-cfromfort.C:40-142). */
+void sw4o_predfort(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
+                   const double* u, const double* um, const double* lu, const double* fo,
+                   const double* rho, double dt2);
+void sw4o_corrfort(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
+                   const double* lu, const double* fo, const double* rho, double dt4);
+void sw4o_dpdmtfort(int ib, int ie, int jb, int je, int kb, int ke, const double* up,
+                    const double* u, const double* um, double* u2, double dt2i);
+
+/* Supergrid damping, 4th and 6th order (src/ew-cfromfort.C:748-1158). */
+void sw4o_addsgd4(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                  double* up, const double* u, const double* um, const double* rho,
+                  const double* dcx, const double* dcy, const double* dcz, const double* strx,
+                  const double* stry, const double* strz, const double* cox, const double* coy,
+                  const double* coz, double beta);
+void sw4o_addsgd6(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                  double* up, const double* u, const double* um, const double* rho,
+                  const double* dcx, const double* dcy, const double* dcz, const double* strx,
+                  const double* stry, const double* strz, const double* cox, const double* coy,
+                  const double* coz, double beta);
+
+/* Ghost-point closures (src/ew-cfromfort.C:205-746).  bccnd values are the
+ * reference's boundaryConditionType (0 free surface, 1 Dirichlet, 2 supergrid,
+ * 3 periodic, others: no-op).  bforce[s] may be NULL when side s has no forcing. */
+void sw4o_bcfortsg(int soa, int ib, int ie, int jb, int je, int kb, int ke, const int wind[36],
+                   int nx, int ny, int nz, double* u, double h, const int bccnd[6],
+                   const double sbop[5], const double* mu, const double* la,
+                   double* const bforce[6], const double* strx, const double* stry);
+
+/* Boundary windows (src/EW.C:3347-3444) for one grid with bounds and global sizes;
+ * writes wind[36] and npts[6]. */
+void sw4o_boundary_windows(int ib, int ie, int jb, int je, int kb, int ke, int nx, int ny,
+                           int nz, const int bccnd[6], int wind[36], int npts[6]);
+
+/* Supergrid 1-D profiles along one axis (src/SuperGrid.C:52-198 and the
+ * assignment loop src/EW.C:4745-4781): for index q in [first,last],
+ * x = (q-1)*h + xmin.  width = gp*h. */
+void sw4o_supergrid_profile(int first, int last, double h, double xmin, int left, int right,
+                            double x0, double x1, double width, double* dc, double* str,
+                            double* corner);
+
+/* Time functions used by grid-point sources (src/time_functions.C:284-319, :1637-1700). */
+double sw4o_timefunc(int kind, double freq, double t);     /* kind: 0 Gaussian, 1 C6SmoothBump */
+double sw4o_timefunc_tt(int kind, double freq, double t);
+
+/* Forcing: zero F then accumulate every grid-point source (src/EW.C:3085-3124). */
+void sw4o_force(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* f, int nsrc,
+                const int* src_ijk, const double* src_amp, const double* src_freq,
+                const double* src_t0, const int* src_kind, double t, int tt);
+
+/* One full time step for one Cartesian grid, in the reference CPU phase order
+ * (src/EW.C:2537-2756): Force, evalRHS, evalPredictor, enforceBC, Force_tt,
+ * evalDpDmInTime, evalRHS, evalCorrector, addSuperGridDamping, enforceBC.
+ * up receives the new level.  lu, f, uacc are caller-provided work arrays of
+ * 3*npts doubles.  Boundary forcing arrays are zero (no point-source-test
+ * Dirichlet data). */
+typedef struct {
+   int ib, ie, jb, je, kb, ke;
+   int nx, ny, nz;
+   double h, dt;
+   int onesided[6];
+   int bccnd[6];
+   int wind[36];
+   double sg_beta; /* supergrid damping coefficient; 0 disables damping */
+   int sg_order;   /* 4 or 6 */
+   const double *mu, *la, *rho;
+   const double *strx, *stry, *strz, *dcx, *dcy, *dcz, *cox, *coy, *coz;
+   int nsrc;
+   const int* src_ijk;
+   const double* src_amp;
+   const double* src_freq;
+   const double* src_t0;
+   const int* src_kind;
+} sw4o_problem;
+
+void sw4o_step(const sw4o_problem* p, int soa, double t, double* up, const double* u,
+               const double* um, double* lu, double* f, double* uacc);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
