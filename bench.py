@@ -1,0 +1,374 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 elastic time step: grid-point-steps/s on the 512^3
+layer-over-halfspace workload (free surface on top, supergrid on the other five
+sides, moment-tensor point source), FP64, one GPU.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A "step" is one full time step of the fused path (predictor stage, one-sided rows,
+forcing, boundary closures, corrector stage with supergrid damping).  Inputs are
+resident in HBM (3.3 GB per 3-component field, far above the 129 MB L2, so no L2
+flush is needed between steps).  Prints one JSON line on rank 0.
+
+--impl reference times the reference's own CPU implementation of the step on the
+host cores (oracle/_ref where it was built here, else the oracle restatement of
+the reference kernels) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "grid-pt-steps/s FP64 vs mixed at stated L2 err; HBM GB/s vs peak; adjoint/fwd time"
+UNIT = "grid-pt-steps/s"
+
+
+# --------------------------------------------------------------------------
+# Workload: 512^3, h = 50 m, 1 km layer (vp 4000, vs 2000, rho 2600) over a
+# half-space (vp 6000, vs 3464, rho 2700); free surface on top, supergrid (30
+# points) on the other sides; Mxy = 1e18 N m at 2 km depth, Gaussian moment rate
+# with sigma = 0.05 s (freq 20), t0 = 0.3 s; dt from CFL 1.3.
+# --------------------------------------------------------------------------
+def c2_config(n=512):
+    return dict(nx=n, ny=n, nz=n, h=50.0, bc=(2, 2, 2, 2, 0, 2), sg_gp=30, sg_damping=0.02,
+                layer_depth=1000.0, layer=(4000.0, 2000.0, 2600.0), half=(6000.0, 3464.0, 2700.0),
+                src=dict(x=(n - 1) * 50.0 / 2, y=(n - 1) * 50.0 / 2, z=2000.0,
+                         moment=(0.0, 1e18, 0.0, 0.0, 0.0, 0.0), freq=20.0, t0=0.3),
+                cfl=1.3)
+
+
+def layered_material(cfg):
+    nx, ny, nz, h = cfg["nx"], cfg["ny"], cfg["nz"], cfg["h"]
+    kk = np.arange(-1, nz + 3)
+    z = (kk - 1) * h
+    vp = np.where(z <= cfg["layer_depth"], cfg["layer"][0], cfg["half"][0])
+    vs = np.where(z <= cfg["layer_depth"], cfg["layer"][1], cfg["half"][1])
+    rh = np.where(z <= cfg["layer_depth"], cfg["layer"][2], cfg["half"][2])
+    mu_k = rh * vs * vs
+    la_k = rh * vp * vp - 2 * mu_k
+    plane = (ny + 4) * (nx + 4)
+    rho = np.repeat(rh, plane)
+    mu = np.repeat(mu_k, plane)
+    la = np.repeat(la_k, plane)
+    return rho, mu, la
+
+
+def cfl_dt(cfg):
+    vmax2 = max(cfg["layer"][0] ** 2 + 2 * cfg["layer"][1] ** 2,
+                cfg["half"][0] ** 2 + 2 * cfg["half"][1] ** 2)
+    return cfg["cfl"] * cfg["h"] / np.sqrt(vmax2)
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# algorithmic bytes per interior point of one corrector stage: reads Up, U, Um (9
+# words) and mu, lambda, rho (3), writes the new level (3): 15 FP64 words
+CORR_STAGE_WORDS = 15
+# reference flop counts per interior point (tests/testil/testil.C:271, :299):
+# rhs4sg 666, addsgd4 375, corrector+dpdm ~23 -> corrector stage; predictor ~683
+CORR_STAGE_REF_FLOPS = 666 + 375 + 11 + 12
+STEP_REF_FLOPS = 1747
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64,
+                     device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# --------------------------------------------------------------------------
+# CPU baseline: the oracle time step on a bounded sample of the workload
+# --------------------------------------------------------------------------
+def cpu_sample(n=96, steps=1, use_ref=False):
+    """Time `steps` CPU time steps of the C2 workload restricted to an n^3 grid."""
+    from oracle import oracle as O
+    import sw4lite_gb300 as sg
+    from tests.gpu_util import OracleProblem
+    O.lib()
+    cfg = c2_config(n)
+    cfg["sg_gp"] = min(cfg["sg_gp"], n // 4)
+    cfg["src"].update(x=(n - 1) * cfg["h"] / 2, y=(n - 1) * cfg["h"] / 2, z=min(2000.0, n * cfg["h"] / 3))
+    g = sg.grid_desc(n, n, n, cfg["h"], bc=cfg["bc"], sg_gp=cfg["sg_gp"], sg_damping=cfg["sg_damping"])
+    rho, mu, la = layered_material(cfg)
+    src = sg.source_desc(**{k: cfg["src"][k] for k in ("x", "y", "z")}, moment=cfg["src"]["moment"],
+                         freq=cfg["src"]["freq"], t0=cfg["src"]["t0"], kind=sg.GAUSSIAN)
+    dt = cfl_dt(cfg)
+    prob = OracleProblem(g, rho, mu, la, dt, [src])
+    npts3 = 3 * prob.npts
+    u = np.zeros(npts3)
+    um = np.zeros(npts3)
+    up, lu, f, uacc = (np.zeros(npts3) for _ in range(4))
+    # one untimed step warms the OpenMP pool and the pages
+    O.step(prob.P, 1, 0.0, up, u, um, lu, f, uacc)
+    t0 = time.perf_counter()
+    t = cfg["src"]["t0"]
+    for _ in range(steps):
+        O.step(prob.P, 1, t, up, u, um, lu, f, uacc)
+        um, u, up = u, up, um
+        t += dt
+    el = time.perf_counter() - t0
+    return n ** 3 * steps / el, el, n
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the reference's CPU step on the host cores."""
+    if rank != 0:
+        return 0
+    ncores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(ncores))
+    n = args.cpu_n
+    samples = []
+    for s in range(args.warmup + args.steps):
+        rate, el, _ = cpu_sample(n=n, steps=1)
+        if s >= args.warmup:
+            samples.append((rate, el))
+    rate = len(samples) * n ** 3 / sum(e for _, e in samples)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * n ** 3 / rate, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"C2 layer-over-halfspace, FP64 time step, sampled on {n}^3 "
+                               "(h=50, same material, boundaries and source)", "grid": [n, n, n]},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]),
+                         "kind": "port",
+                         "sample": f"{args.steps} time steps of a {n}^3 grid of the workload"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+def run_ours(args, rank, world):
+    import torch
+    import sw4lite_gb300 as sg
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    sg.build()
+    cfg = c2_config(args.n)
+    n = args.n
+    g = sg.grid_desc(n, n, n, cfg["h"], bc=cfg["bc"], sg_gp=cfg["sg_gp"], sg_damping=cfg["sg_damping"])
+    stream = torch.cuda.Stream()
+    ew = sg.EW(g, stream=stream)
+    rho, mu, la = layered_material(cfg)
+    ew.set_material(rho, mu, la)
+    del rho, mu, la
+    ew.add_source(sg.source_desc(cfg["src"]["x"], cfg["src"]["y"], cfg["src"]["z"],
+                                 moment=cfg["src"]["moment"], freq=cfg["src"]["freq"],
+                                 t0=cfg["src"]["t0"], kind=sg.GAUSSIAN))
+    dt = cfl_dt(cfg)
+    ew.set_time_step(dt, 0.0)
+    mode = sg.MODE_FUSED if args.mode == "fused" else sg.MODE_PHASES
+    npts_int = n ** 3
+
+    with torch.cuda.stream(stream):
+        ew.step(args.warmup, mode)
+        torch.cuda.synchronize()
+        barrier(world)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clocks:
+            torch.cuda.synchronize()
+            e0.record(stream)
+            ew.step(args.steps, mode)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+    barrier(world)
+    ms = max_over_ranks(ms, world)
+    ms_step = ms / args.steps
+    value = world * npts_int / (ms_step * 1e-3)
+
+    # per-kernel device times of a fused step (CUDA events on the EW stream)
+    prof = ew.profile_kernels(nrep=3)
+    corr_ms = prof["corr_stage"]
+    peak_hbm, peak_kind = measured_peaks()
+    corr_bytes = CORR_STAGE_WORDS * 8 * npts_int
+    achieved = corr_bytes / (corr_ms * 1e-3) / 1e9
+    fp64_peak = sg.fma_peak(64, stream=stream)
+    fp64_equiv = CORR_STAGE_REF_FLOPS * npts_int / (corr_ms * 1e-3) / 1e12
+
+    # end to end through the C ABI with host buffers: H2D of (U, Um) from pinned
+    # host memory, the K steps, D2H of U
+    e2e = None
+    if not args.no_e2e:
+        n3 = 3 * ew.npts
+        hu = torch.zeros(n3, dtype=torch.float64, pin_memory=True)
+        hum = torch.zeros(n3, dtype=torch.float64, pin_memory=True)
+        ew.get_fields(hu, hum)  # current state as the "input" the user holds
+        torch.cuda.synchronize()
+        barrier(world)
+        t0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            ew.set_fields(hu, hum)
+            ew.step(args.steps, mode)
+            ew.get_fields(hu, None)
+        torch.cuda.synchronize()
+        el = max_over_ranks(time.perf_counter() - t0, world)
+        e2e = {"value": world * npts_int * args.steps / el, "unit": UNIT,
+               "h2d_bytes_per_step": int(2 * n3 * 8 / args.steps),
+               "d2h_bytes_per_step": int(n3 * 8 / args.steps)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        ncores = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(ncores))
+        rate, el, cn = cpu_sample(n=args.cpu_n, steps=1)
+        cpu = {"value": rate, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]),
+               "kind": "port",
+               "sample": f"1 time step of a {cn}^3 grid of the workload ({el:.1f} s, oracle "
+                         "restatement of the reference kernels, OpenMP)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"C2 layer-over-halfspace {n}^3 h=50, FP64, fused time step",
+                       "grid": [n, n, n], "mode": args.mode, "dt": dt,
+                       "l2": "inputs larger than L2 (3.3 GB per field), no flush",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": {"bound": "hbm", "kernel": "fused corrector stage", "achieved": achieved,
+                         "peak": peak_hbm, "unit": "GB/s", "frac": achieved / peak_hbm,
+                         "traffic": None, "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": corr_bytes, "launch_ms": corr_ms},
+            "fp64_pipe": {"kernel": "fused corrector stage",
+                          "reference_equivalent_tflops": fp64_equiv,
+                          "measured_fma_peak_tflops": fp64_peak,
+                          "frac": fp64_equiv / fp64_peak,
+                          "basis": f"{CORR_STAGE_REF_FLOPS} reference flops per point "
+                                   "(rhs4sg 666 + addsgd4 375 + update 23)"},
+            "kernel_ms": prof,
+            "clocks": clocks.summary(),
+            "e2e": e2e,
+            "gpu_launches": ew.launches_per_step(mode) * args.steps,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    ew.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--mode", choices=["fused", "phases"], default="fused")
+    ap.add_argument("--n", type=int, default=512, help="grid points per axis")
+    ap.add_argument("--cpu-n", type=int, default=96, help="CPU sample grid points per axis")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    rank, world = dist_init(args)
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

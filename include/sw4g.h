@@ -1,0 +1,192 @@
+/*
+ * sw4g -- C ABI of the GB300 (sm_103a) elastic-wave time step.
+ *
+ * Drop-in boundary for the Scheme, Supergrid, BC-phys and Forcing phases of
+ * sw4lite's time loop.  Conventions are the reference's:
+ *   - inclusive, 1-based (Fortran-style) array bounds ifirst..ilast etc. that
+ *     include 2 ghost points per side, i fastest;
+ *   - `soa` selects the component layout of 3-component fields: 1 is the
+ *     reference's corder=1 layout u[c*npts + p] (the *_rev / *_indrev kernels),
+ *     0 the AoS layout u[3*p + c];
+ *   - all field pointers are DEVICE pointers owned by the caller unless a
+ *     function says otherwise; small tables (wind, bccnd, onesided, sbop) are
+ *     host pointers;
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream); every call only
+ *     enqueues work on it, never synchronises the host and never allocates.
+ * Every function returns an sw4g_status (0 = success); none aborts or exits,
+ * where the reference would CHECK_ERROR -> exit(0) or MPI_Abort.
+ */
+#ifndef SW4G_H
+#define SW4G_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+   SW4G_OK = 0,
+   SW4G_BAD_ARGUMENT = 1,
+   SW4G_CUDA_ERROR = 2,
+   SW4G_NAN_DETECTED = 3,
+   SW4G_NOT_SUPPORTED = 4,
+   SW4G_TIMEOUT = 5
+} sw4g_status;
+
+/* Library version string. */
+const char* sw4g_version(void);
+/* Human-readable text for a status code. */
+const char* sw4g_status_string(int status);
+
+/* SBP operator tables (host arrays), layout of EW::GetStencilCoefficients
+ * (src/ew-cfromfort.C:1487): acof[384], ghcof[6], bope[48], sbop[5]. */
+int sw4g_stencil_coefficients(double* acof, double* ghcof, double* bope, double* sbop);
+
+/* ---------------------------------------------------------------------------
+ * Kernel-level entry points (one reference kernel each)
+ * ------------------------------------------------------------------------- */
+
+/* Lu = div(sigma(u)) with supergrid stretching; replaces rhs4sg / rhs4sg_rev
+ * (src/EW.C:141-149, src/rhs4sg.C:38, src/rhs4sg_rev.C:44).  The SBP tables
+ * acof/bope/ghcof of the reference signature are fixed constants of the scheme
+ * and are held on the device by the library.  onesided[6] is a host array;
+ * only onesided[4] (top) and onesided[5] (bottom) are used.  Only the interior
+ * i,j in [first+2, last-2] and k rows are written, as in the reference. */
+int sw4g_rhs4sg(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                int nk, const int* onesided, double* lu, const double* u, const double* mu,
+                const double* lambda, double h, const double* strx, const double* stry,
+                const double* strz, void* stream);
+
+/* up = 2u - um + dt2/rho (lu + fo) over all points; replaces EW::predfort
+ * (src/ew-cfromfort.C:70). */
+int sw4g_predfort(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
+                  const double* u, const double* um, const double* lu, const double* fo,
+                  const double* rho, double dt2, void* stream);
+
+/* up += dt4/(12 rho) (lu + fo); replaces EW::corrfort (src/ew-cfromfort.C:40). */
+int sw4g_corrfort(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
+                  const double* lu, const double* fo, const double* rho, double dt4, void* stream);
+
+/* u2 = dt2i (up - 2u + um); replaces EW::dpdmtfort (src/ew-cfromfort.C:116). */
+int sw4g_dpdmtfort(int ib, int ie, int jb, int je, int kb, int ke, const double* up,
+                   const double* u, const double* um, double* u2, double dt2i, void* stream);
+
+/* 4th-order supergrid damping on up; replaces EW::addsgd4fort / addsgd4fort_indrev
+ * (src/ew-cfromfort.C:748, :952). */
+int sw4g_addsgd4fort(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                     double* up, const double* u, const double* um, const double* rho,
+                     const double* dcx, const double* dcy, const double* dcz, const double* strx,
+                     const double* stry, const double* strz, const double* cox, const double* coy,
+                     const double* coz, double beta, void* stream);
+
+/* 6th-order supergrid damping; replaces EW::addsgd6fort / addsgd6fort_indrev
+ * (src/ew-cfromfort.C:852, :1059). */
+int sw4g_addsgd6fort(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                     double* up, const double* u, const double* um, const double* rho,
+                     const double* dcx, const double* dcy, const double* dcz, const double* strx,
+                     const double* stry, const double* strz, const double* cox, const double* coy,
+                     const double* coz, double beta, void* stream);
+
+/* Ghost-point closures; replaces EW::bcfortsg / bcfortsg_indrev
+ * (src/ew-cfromfort.C:205, :480).  wind[36], bccnd[6] and sbop[5] are host
+ * arrays; bforce[s] (6 device pointers, host array of pointers) may hold NULL
+ * entries, read as zero boundary data.  The unused (t, om, ph, cv) arguments
+ * of the reference signature are dropped. */
+int sw4g_bcfortsg(int soa, int ib, int ie, int jb, int je, int kb, int ke, const int* wind,
+                  int nx, int ny, int nz, double* u, double h, const int* bccnd, const double* sbop,
+                  const double* mu, const double* lambda, const double* const* bforce,
+                  const double* strx, const double* stry, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Host-side set-up helpers (no device work)
+ * ------------------------------------------------------------------------- */
+
+/* Grid description: one Cartesian grid, 2 ghost points per side. */
+typedef struct {
+   int nx, ny, nz;    /* interior points per axis */
+   double h;          /* grid spacing */
+   double zmin;       /* z of the first interior plane */
+   int bc[6];         /* per side: 0 free surface, 1 Dirichlet, 2 supergrid, 3 periodic */
+   int sg_gp;         /* supergrid layer width in grid points (reference default 20) */
+   double sg_damping; /* supergrid damping coefficient (reference default 0.02) */
+   int sg_order;      /* damping order, 4 or 6 */
+   int soa;           /* must be 1 for the time loop */
+} sw4g_grid;
+
+/* Supergrid profiles along one axis of g (0 x, 1 y, 2 z) over the array index
+ * range; replaces SuperGrid::dampingCoeff/stretching/cornerTaper sampled as in
+ * EW::assign_supergrid_damping_arrays (src/SuperGrid.C:108-198,
+ * src/EW.C:4671-4803).  Arrays have n+4 entries for an axis with n points. */
+int sw4g_supergrid_profile(const sw4g_grid* g, int axis, double* dc, double* str, double* corner);
+
+/* Boundary windows and point counts; replaces EW::setup_boundary_arrays
+ * (src/EW.C:3347). */
+int sw4g_boundary_windows(const sw4g_grid* g, int* wind, int* npts);
+
+/* A point source: force (moment == 0) or moment tensor.  kind selects the time
+ * function: 0 Gaussian, 1 C6SmoothBump, 2 Ricker, 3 VerySmoothBump. */
+typedef struct {
+   double x, y, z;
+   int moment;
+   double fx, fy, fz;
+   double mxx, mxy, mxz, myy, myz, mzz;
+   double freq, t0;
+   int kind;
+} sw4g_source;
+
+/* Grid-point sources of one source; replaces Source::set_grid_point_sources4
+ * (src/Source.C:1074) for a Cartesian grid.  Writes at most `cap` entries and
+ * returns the count through *n (the full count even when it exceeds cap). */
+int sw4g_discretize_source(const sw4g_grid* g, const sw4g_source* s, int cap, int* ijk,
+                           double* amp, int* n);
+
+/* ---------------------------------------------------------------------------
+ * Phase-level driver: the EW time loop on one grid (src/EW.C:2339-2930)
+ * ------------------------------------------------------------------------- */
+typedef struct sw4g_ew sw4g_ew;
+
+/* mode for sw4g_ew_step */
+#define SW4G_MODE_PHASES 0 /* reference phase order, dense Lu/F/Uacc arrays */
+#define SW4G_MODE_FUSED 1  /* fused predictor / corrector stage kernels */
+
+int sw4g_ew_create(const sw4g_grid* g, void* stream, sw4g_ew** out);
+int sw4g_ew_destroy(sw4g_ew* ew);
+/* number of array points (ghosts included) */
+long long sw4g_ew_npts(const sw4g_ew* ew);
+/* material over the full array: host (on_device=0) or device pointers */
+int sw4g_ew_set_material(sw4g_ew* ew, const double* rho, const double* mu, const double* lambda,
+                         int on_device);
+int sw4g_ew_add_source(sw4g_ew* ew, const sw4g_source* s);
+int sw4g_ew_add_grid_point_sources(sw4g_ew* ew, int n, const int* ijk, const double* amp,
+                                   const double* freq, const double* t0, const int* kind);
+int sw4g_ew_clear_sources(sw4g_ew* ew);
+int sw4g_ew_num_grid_point_sources(const sw4g_ew* ew);
+int sw4g_ew_set_time_step(sw4g_ew* ew, double dt, double t0);
+/* dt from the CFL number, adjusted to end at tmax (EW::computeDT, src/EW.C:5041) */
+int sw4g_ew_compute_time_step(sw4g_ew* ew, double cfl, double tmax, double* dt, int* nsteps);
+double sw4g_ew_time(const sw4g_ew* ew);
+/* current (u) and previous (um) levels, 3*npts each, host or device */
+int sw4g_ew_set_fields(sw4g_ew* ew, const double* u, const double* um, int on_device);
+int sw4g_ew_get_fields(const sw4g_ew* ew, double* u, double* um, int on_device);
+/* device pointer of the current (which=0) or previous (which=1) level */
+double* sw4g_ew_field(const sw4g_ew* ew, int which);
+/* advance nsteps time steps */
+int sw4g_ew_step(sw4g_ew* ew, int nsteps, int mode);
+/* boundary conditions of this grid on a caller's 3-component device array */
+int sw4g_ew_enforce_bc(sw4g_ew* ew, double* u);
+/* kernel launches one step enqueues */
+int sw4g_ew_launches_per_step(const sw4g_ew* ew, int mode);
+/* Per-kernel device time of a fused step (CUDA events on the EW stream), each
+ * piece launched nrep times on the current levels without advancing time; the
+ * counterpart of the reference's phase timers (src/EW.C:2863-2873, reporttiming):
+ * ms[0] predictor stage kernel, ms[1] corrector stage kernel, ms[2] one-sided
+ * rows, ms[3] boundary conditions and forcing.  Synchronises the stream. */
+int sw4g_ew_profile_kernels(sw4g_ew* ew, int nrep, double* ms);
+
+/* Arithmetic throughput probe (no reference counterpart): FMA chains on every SM
+ * in FP64 (precision=64) or FP32 (32); writes TFLOP/s.  Synchronises the stream. */
+int sw4g_fma_peak(int precision, double* tflops, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -140,6 +140,33 @@ static inline double d2var(const double a[5], const double f[5])
 /* 12h * centred 4th-order first difference. */
 static const double DW[5] = {1, -8, 0, 8, -1};
 
+/* Strided forms used by the centred rows: `mst` is the point stride of the
+ * material arrays along the axis, `fst` the stride of the field. */
+static inline double d2v_axis(const double* mu, const double* la, long mst, const double* sa,
+                              const double* f, long fst, int twomu)
+{
+   double a[5], ff[5];
+   for (int m = -2; m <= 2; m++) {
+      const double c = twomu ? 2 * mu[m * mst] + la[m * mst] : mu[m * mst];
+      a[m + 2] = c * sa[m];
+      ff[m + 2] = f[m * fst];
+   }
+   return d2var(a, ff);
+}
+
+/* sum_m DW[m] coef(m along outer) * (12h d/d inner of f at that point) */
+static inline double mixed_axis(const double* coef, long cst, const double* f, long fo, long fi)
+{
+   double s = 0;
+   for (int m = -2; m <= 2; m++) {
+      if (m == 0) continue;
+      const double* g = f + m * fo;
+      const double inner = (g[-2 * fi] - g[2 * fi]) + 8 * (g[fi] - g[-fi]);
+      s += DW[m + 2] * coef[m * cst] * inner;
+   }
+   return s;
+}
+
 /* ------------------------------------------------------------------------ */
 /* rhs4sg: src/rhs4sg_rev.C:44-864 (SoA) and src/rhs4sg.C:38-849 (AoS).      */
 /* ------------------------------------------------------------------------ */
@@ -285,25 +312,39 @@ void sw4o_rhs4sg(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfir
    int k2 = onesided[5] == 1 ? nk - 6 : klast - 2;
 
    /* Centred rows, src/rhs4sg_rev.C:111-348. */
+   const long fx = b.ps, fy = b.ps * b.ni, fz = b.ps * b.nij; /* field strides */
+   const long mx = 1, my = b.ni, mz = b.nij;                  /* material strides */
 #pragma omp parallel for collapse(2) schedule(static)
    for (int k = k1; k <= k2; k++)
       for (int j = jfirst + 2; j <= jlast - 2; j++)
          for (int i = ifirst + 2; i <= ilast - 2; i++) {
-            double sx = strx[i - ifirst], sy = stry[j - jfirst], sz = strz[k - kfirst];
+            const long p = PT(&b, i, j, k);
+            const double* sxp = strx + (i - ifirst);
+            const double* syp = stry + (j - jfirst);
+            const double* szp = strz + (k - kfirst);
+            const double sx = *sxp, sy = *syp, sz = *szp;
+            const double* m0 = mu + p;
+            const double* l0 = la + p;
+            const double* U0 = u + b.ps * p;            /* component 0 */
+            const double* U1 = U0 + b.cs;
+            const double* U2 = U0 + 2 * b.cs;
             double r[3];
-            r[0] = i6 * (sx * secder(&o, 0, 1, 0, i, j, k) + sy * secder(&o, 1, 0, 0, i, j, k) +
-                         sz * secder(&o, 2, 0, 0, i, j, k));
-            r[1] = i6 * (sx * secder(&o, 0, 0, 1, i, j, k) + sy * secder(&o, 1, 1, 1, i, j, k) +
-                         sz * secder(&o, 2, 0, 1, i, j, k));
-            r[2] = i6 * (sx * secder(&o, 0, 0, 2, i, j, k) + sy * secder(&o, 1, 0, 2, i, j, k) +
-                         sz * secder(&o, 2, 1, 2, i, j, k));
-            r[0] += i144 * (sx * sy * (mixed(&o, la, 0, 1, 1, i, j, k) + mixed(&o, mu, 1, 0, 1, i, j, k)) +
-                            sx * sz * (mixed(&o, la, 0, 2, 2, i, j, k) + mixed(&o, mu, 2, 0, 2, i, j, k)));
-            r[1] += i144 * (sx * sy * (mixed(&o, mu, 0, 1, 0, i, j, k) + mixed(&o, la, 1, 0, 0, i, j, k)) +
-                            sy * sz * (mixed(&o, la, 1, 2, 2, i, j, k) + mixed(&o, mu, 2, 1, 2, i, j, k)));
-            r[2] += i144 * (sx * sz * (mixed(&o, mu, 0, 2, 0, i, j, k) + mixed(&o, la, 2, 0, 0, i, j, k)) +
-                            sy * sz * (mixed(&o, mu, 1, 2, 1, i, j, k) + mixed(&o, la, 2, 1, 1, i, j, k)));
-            for (int c = 0; c < 3; c++) lu[CX(&b, c, i, j, k)] = cof * r[c];
+            r[0] = i6 * (sx * d2v_axis(m0, l0, mx, sxp, U0, fx, 1) +
+                         sy * d2v_axis(m0, l0, my, syp, U0, fy, 0) +
+                         sz * d2v_axis(m0, l0, mz, szp, U0, fz, 0));
+            r[1] = i6 * (sx * d2v_axis(m0, l0, mx, sxp, U1, fx, 0) +
+                         sy * d2v_axis(m0, l0, my, syp, U1, fy, 1) +
+                         sz * d2v_axis(m0, l0, mz, szp, U1, fz, 0));
+            r[2] = i6 * (sx * d2v_axis(m0, l0, mx, sxp, U2, fx, 0) +
+                         sy * d2v_axis(m0, l0, my, syp, U2, fy, 0) +
+                         sz * d2v_axis(m0, l0, mz, szp, U2, fz, 1));
+            r[0] += i144 * (sx * sy * (mixed_axis(l0, mx, U1, fx, fy) + mixed_axis(m0, my, U1, fy, fx)) +
+                            sx * sz * (mixed_axis(l0, mx, U2, fx, fz) + mixed_axis(m0, mz, U2, fz, fx)));
+            r[1] += i144 * (sx * sy * (mixed_axis(m0, mx, U0, fx, fy) + mixed_axis(l0, my, U0, fy, fx)) +
+                            sy * sz * (mixed_axis(l0, my, U2, fy, fz) + mixed_axis(m0, mz, U2, fz, fy)));
+            r[2] += i144 * (sx * sz * (mixed_axis(m0, mx, U0, fx, fz) + mixed_axis(l0, mz, U0, fz, fx)) +
+                            sy * sz * (mixed_axis(m0, my, U1, fy, fz) + mixed_axis(l0, mz, U1, fz, fy)));
+            for (int c = 0; c < 3; c++) lu[c * b.cs + b.ps * p] = cof * r[c];
          }
 
    /* One-sided SBP rows at the top (k=1..6, src/rhs4sg_rev.C:349-600) and the
@@ -396,34 +437,31 @@ void sw4o_addsgd4(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfi
 {
    if (beta == 0) return;
    box b = make_box(soa, ifirst, ilast, jfirst, jlast, kfirst, klast);
+   const long fst[3] = {b.ps, b.ps * b.ni, b.ps * b.nij}, mst[3] = {1, b.ni, b.nij};
 #pragma omp parallel for collapse(2) schedule(static)
    for (int k = kfirst + 2; k <= klast - 2; k++)
       for (int j = jfirst + 2; j <= jlast - 2; j++)
          for (int i = ifirst + 2; i <= ilast - 2; i++) {
-            double birho = beta / rho[PT(&b, i, j, k)];
-            double wx = strx[i - ifirst] * coy[j - jfirst] * coz[k - kfirst];
-            double wy = stry[j - jfirst] * cox[i - ifirst] * coz[k - kfirst];
-            double wz = strz[k - kfirst] * cox[i - ifirst] * coy[j - jfirst];
+            const long p = PT(&b, i, j, k);
+            const double birho = beta / rho[p];
+            const double w[3] = {strx[i - ifirst] * coy[j - jfirst] * coz[k - kfirst],
+                                 stry[j - jfirst] * cox[i - ifirst] * coz[k - kfirst],
+                                 strz[k - kfirst] * cox[i - ifirst] * coy[j - jfirst]};
+            const double* dcp[3] = {dcx + (i - ifirst), dcy + (j - jfirst), dcz + (k - kfirst)};
             for (int c = 0; c < 3; c++) {
+               const long q = c * b.cs + b.ps * p;
                double tot = 0;
                for (int ax = 0; ax < 3; ax++) {
-                  int di = ax == 0, dj = ax == 1, dk = ax == 2;
-                  const double* dc = ax == 0 ? dcx : ax == 1 ? dcy : dcz;
-                  int off = ax == 0 ? i - ifirst : ax == 1 ? j - jfirst : k - kfirst;
+                  const long f = fst[ax], ms = mst[ax];
                   double d[5];
-                  for (int m = -2; m <= 2; m++) {
-                     long q = CX(&b, c, i + di * m, j + dj * m, k + dk * m);
-                     d[m + 2] = u[q] - um[q];
-                  }
-                  double s = 0;
-                  const double w3[3] = {1, -2, 1};
-                  for (int m = -1; m <= 1; m++) {
-                     double e = rho[PT(&b, i + di * m, j + dj * m, k + dk * m)] * dc[off + m];
-                     s += w3[m + 1] * e * (d[m + 3] - 2 * d[m + 2] + d[m + 1]);
-                  }
-                  tot += (ax == 0 ? wx : ax == 1 ? wy : wz) * s;
+                  for (int m = -2; m <= 2; m++) d[m + 2] = u[q + m * f] - um[q + m * f];
+                  const double e0 = rho[p - ms] * dcp[ax][-1], e1 = rho[p] * dcp[ax][0],
+                               e2 = rho[p + ms] * dcp[ax][1];
+                  const double sgx = e2 * (d[4] - 2 * d[3] + d[2]) - 2 * e1 * (d[3] - 2 * d[2] + d[1]) +
+                                     e0 * (d[2] - 2 * d[1] + d[0]);
+                  tot += w[ax] * sgx;
                }
-               up[CX(&b, c, i, j, k)] -= birho * tot;
+               up[q] -= birho * tot;
             }
          }
 }

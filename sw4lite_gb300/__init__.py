@@ -1,0 +1,262 @@
+"""sw4lite_gb300: GB300-native (sm_103a) elastic-wave time step behind sw4lite's
+kernel/phase API.
+
+The compute path is libsw4g.so (CUDA kernels + C ABI, include/sw4g.h), built in-tree
+by ``python -m sw4lite_gb300.build``.  This module loads it with ctypes and offers a
+thin Python view of the C ABI for tests and benchmarks; PyTorch is used only for
+device memory and streams.  There is no CPU fallback: every call that computes
+runs on the GPU, and loading fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libsw4g.so"
+HEADER = _PKG.parent / "include" / "sw4g.h"
+
+_lib = None
+
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+_VP = C.c_void_p
+
+
+class Sw4gError(RuntimeError):
+    pass
+
+
+class GridDesc(C.Structure):
+    """sw4g_grid (include/sw4g.h)."""
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("h", C.c_double),
+                ("zmin", C.c_double), ("bc", C.c_int * 6), ("sg_gp", C.c_int),
+                ("sg_damping", C.c_double), ("sg_order", C.c_int), ("soa", C.c_int)]
+
+
+class SourceDesc(C.Structure):
+    """sw4g_source (include/sw4g.h)."""
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double), ("moment", C.c_int),
+                ("fx", C.c_double), ("fy", C.c_double), ("fz", C.c_double),
+                ("mxx", C.c_double), ("mxy", C.c_double), ("mxz", C.c_double),
+                ("myy", C.c_double), ("myz", C.c_double), ("mzz", C.c_double),
+                ("freq", C.c_double), ("t0", C.c_double), ("kind", C.c_int)]
+
+
+# time-function kinds
+GAUSSIAN, C6SMOOTHBUMP, RICKER, VERYSMOOTHBUMP = 0, 1, 2, 3
+# boundary kinds (the reference's boundaryConditionType numbering)
+FREE, DIRICHLET, SUPERGRID, PERIODIC = 0, 1, 2, 3
+MODE_PHASES, MODE_FUSED = 0, 1
+
+_SIGS = {
+    "sw4g_version": ([], C.c_char_p),
+    "sw4g_status_string": ([C.c_int], C.c_char_p),
+    "sw4g_stencil_coefficients": ([_D, _D, _D, _D], C.c_int),
+    "sw4g_rhs4sg": ([C.c_int] * 8 + [_I, _VP, _VP, _VP, _VP, C.c_double, _VP, _VP, _VP, _VP],
+                    C.c_int),
+    "sw4g_predfort": ([C.c_int] * 7 + [_VP] * 6 + [C.c_double, _VP], C.c_int),
+    "sw4g_corrfort": ([C.c_int] * 7 + [_VP] * 4 + [C.c_double, _VP], C.c_int),
+    "sw4g_dpdmtfort": ([C.c_int] * 6 + [_VP] * 4 + [C.c_double, _VP], C.c_int),
+    "sw4g_addsgd4fort": ([C.c_int] * 7 + [_VP] * 13 + [C.c_double, _VP], C.c_int),
+    "sw4g_addsgd6fort": ([C.c_int] * 7 + [_VP] * 13 + [C.c_double, _VP], C.c_int),
+    "sw4g_bcfortsg": ([C.c_int] * 7 + [_I, C.c_int, C.c_int, C.c_int, _VP, C.c_double, _I, _D,
+                                       _VP, _VP, C.POINTER(_VP), _VP, _VP, _VP], C.c_int),
+    "sw4g_supergrid_profile": ([C.POINTER(GridDesc), C.c_int, _D, _D, _D], C.c_int),
+    "sw4g_boundary_windows": ([C.POINTER(GridDesc), _I, _I], C.c_int),
+    "sw4g_discretize_source": ([C.POINTER(GridDesc), C.POINTER(SourceDesc), C.c_int, _I, _D, _I],
+                               C.c_int),
+    "sw4g_ew_create": ([C.POINTER(GridDesc), _VP, C.POINTER(_VP)], C.c_int),
+    "sw4g_ew_destroy": ([_VP], C.c_int),
+    "sw4g_ew_npts": ([_VP], C.c_longlong),
+    "sw4g_ew_set_material": ([_VP, _VP, _VP, _VP, C.c_int], C.c_int),
+    "sw4g_ew_add_source": ([_VP, C.POINTER(SourceDesc)], C.c_int),
+    "sw4g_ew_add_grid_point_sources": ([_VP, C.c_int, _I, _D, _D, _D, _I], C.c_int),
+    "sw4g_ew_clear_sources": ([_VP], C.c_int),
+    "sw4g_ew_num_grid_point_sources": ([_VP], C.c_int),
+    "sw4g_ew_set_time_step": ([_VP, C.c_double, C.c_double], C.c_int),
+    "sw4g_ew_compute_time_step": ([_VP, C.c_double, C.c_double, _D, _I], C.c_int),
+    "sw4g_ew_time": ([_VP], C.c_double),
+    "sw4g_ew_set_fields": ([_VP, _VP, _VP, C.c_int], C.c_int),
+    "sw4g_ew_get_fields": ([_VP, _VP, _VP, C.c_int], C.c_int),
+    "sw4g_ew_field": ([_VP, C.c_int], _VP),
+    "sw4g_ew_step": ([_VP, C.c_int, C.c_int], C.c_int),
+    "sw4g_ew_enforce_bc": ([_VP, _VP], C.c_int),
+    "sw4g_ew_launches_per_step": ([_VP, C.c_int], C.c_int),
+    "sw4g_ew_profile_kernels": ([_VP, C.c_int, _D], C.c_int),
+    "sw4g_fma_peak": ([C.c_int, _D, _VP], C.c_int),
+}
+
+
+def build(force: bool = False) -> Path:
+    import importlib
+    return importlib.import_module(__name__ + ".build").build(force=force)
+
+
+def lib():
+    """The loaded libsw4g.so.  Raises Sw4gError if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise Sw4gError(f"{LIB_PATH} is missing: build it with `python -m sw4lite_gb300.build`"
+                            " (there is no CPU fallback)")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def check(status: int, what: str = "") -> None:
+    if status != 0:
+        msg = lib().sw4g_status_string(status).decode()
+        raise Sw4gError(f"{what}: sw4g status {status} ({msg})")
+
+
+def header_functions() -> list[str]:
+    """Names of every function the C ABI header declares."""
+    import re
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    return sorted(set(re.findall(r"\b(sw4g_[a-z0-9_]+)\s*\(", text)))
+
+
+def stencil_coefficients():
+    import numpy as np
+    acof, ghcof, bope, sbop = np.zeros(384), np.zeros(6), np.zeros(48), np.zeros(5)
+    check(lib().sw4g_stencil_coefficients(*[a.ctypes.data_as(_D) for a in (acof, ghcof, bope, sbop)]))
+    return acof, ghcof, bope, sbop
+
+
+def grid_desc(nx, ny, nz, h, bc=(SUPERGRID,) * 4 + (FREE, SUPERGRID), zmin=0.0, sg_gp=20,
+              sg_damping=0.02, sg_order=4, soa=1) -> GridDesc:
+    g = GridDesc()
+    g.nx, g.ny, g.nz, g.h, g.zmin = nx, ny, nz, h, zmin
+    for s in range(6):
+        g.bc[s] = int(bc[s])
+    g.sg_gp, g.sg_damping, g.sg_order, g.soa = sg_gp, sg_damping, sg_order, soa
+    return g
+
+
+def source_desc(x, y, z, *, force=None, moment=None, freq=1.0, t0=0.0, kind=GAUSSIAN) -> SourceDesc:
+    s = SourceDesc()
+    s.x, s.y, s.z = x, y, z
+    if moment is not None:
+        s.moment = 1
+        s.mxx, s.mxy, s.mxz, s.myy, s.myz, s.mzz = moment
+    else:
+        s.moment = 0
+        s.fx, s.fy, s.fz = force if force is not None else (0.0, 0.0, 0.0)
+    s.freq, s.t0, s.kind = freq, t0, kind
+    return s
+
+
+def _ptr(t) -> int:
+    """Device (or host) address of a torch tensor / numpy array."""
+    if hasattr(t, "data_ptr"):
+        return t.data_ptr()
+    return t.ctypes.data
+
+
+def _stream_ptr(stream) -> int | None:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream or None
+    return getattr(stream, "cuda_stream", stream) or None
+
+
+class EW:
+    """One Cartesian grid's time loop on the GPU (sw4g_ew_* in include/sw4g.h)."""
+
+    def __init__(self, grid: GridDesc, stream=None):
+        self.grid = grid
+        self._stream = _stream_ptr(stream)
+        h = _VP()
+        check(lib().sw4g_ew_create(C.byref(grid), self._stream, C.byref(h)), "sw4g_ew_create")
+        self._h = h
+        self.npts = lib().sw4g_ew_npts(h)
+        self.shape = (grid.nz + 4, grid.ny + 4, grid.nx + 4)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sw4g_ew_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_material(self, rho, mu, la):
+        on_dev = int(hasattr(rho, "is_cuda") and rho.is_cuda)
+        check(lib().sw4g_ew_set_material(self._h, _ptr(rho), _ptr(mu), _ptr(la), on_dev),
+              "set_material")
+
+    def add_source(self, src: SourceDesc):
+        check(lib().sw4g_ew_add_source(self._h, C.byref(src)), "add_source")
+
+    def add_grid_point_sources(self, ijk, amp, freq, t0, kind):
+        import numpy as np
+        ijk = np.ascontiguousarray(ijk, dtype=np.int32)
+        amp = np.ascontiguousarray(amp, dtype=np.float64)
+        freq = np.ascontiguousarray(freq, dtype=np.float64)
+        t0 = np.ascontiguousarray(t0, dtype=np.float64)
+        kind = np.ascontiguousarray(kind, dtype=np.int32)
+        n = len(freq)
+        check(lib().sw4g_ew_add_grid_point_sources(self._h, n, ijk.ctypes.data_as(_I),
+                                                   amp.ctypes.data_as(_D), freq.ctypes.data_as(_D),
+                                                   t0.ctypes.data_as(_D), kind.ctypes.data_as(_I)),
+              "add_grid_point_sources")
+
+    def num_grid_point_sources(self) -> int:
+        return lib().sw4g_ew_num_grid_point_sources(self._h)
+
+    def set_time_step(self, dt, t0=0.0):
+        check(lib().sw4g_ew_set_time_step(self._h, dt, t0), "set_time_step")
+
+    def compute_time_step(self, cfl, tmax):
+        dt = C.c_double()
+        n = C.c_int()
+        check(lib().sw4g_ew_compute_time_step(self._h, cfl, tmax, C.byref(dt), C.byref(n)),
+              "compute_time_step")
+        return dt.value, n.value
+
+    @property
+    def time(self) -> float:
+        return lib().sw4g_ew_time(self._h)
+
+    def set_fields(self, u, um):
+        on_dev = int(hasattr(u, "is_cuda") and u.is_cuda)
+        check(lib().sw4g_ew_set_fields(self._h, _ptr(u), _ptr(um), on_dev), "set_fields")
+
+    def get_fields(self, u, um):
+        on_dev = int(hasattr(u, "is_cuda") and u.is_cuda)
+        check(lib().sw4g_ew_get_fields(self._h, _ptr(u), _ptr(um) if um is not None else None,
+                                       on_dev), "get_fields")
+
+    def field_ptr(self, which=0) -> int:
+        return lib().sw4g_ew_field(self._h, which)
+
+    def step(self, nsteps=1, mode=MODE_FUSED):
+        check(lib().sw4g_ew_step(self._h, nsteps, mode), "step")
+
+    def enforce_bc(self, u):
+        check(lib().sw4g_ew_enforce_bc(self._h, _ptr(u)), "enforce_bc")
+
+    def launches_per_step(self, mode=MODE_FUSED) -> int:
+        return lib().sw4g_ew_launches_per_step(self._h, mode)
+
+    def profile_kernels(self, nrep=5):
+        ms = (C.c_double * 4)()
+        check(lib().sw4g_ew_profile_kernels(self._h, nrep, ms), "profile_kernels")
+        return dict(pred_stage=ms[0], corr_stage=ms[1], rows=ms[2], bc_force=ms[3])
+
+
+def fma_peak(precision=64, stream=None) -> float:
+    """Measured FMA throughput of this GPU in TFLOP/s (FP64 or FP32)."""
+    t = C.c_double()
+    check(lib().sw4g_fma_peak(precision, C.byref(t), _stream_ptr(stream)), "fma_peak")
+    return t.value

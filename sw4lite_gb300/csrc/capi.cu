@@ -1,0 +1,326 @@
+// extern "C" entry points of libsw4g.so (declared in include/sw4g.h).
+#include <cstring>
+#include <exception>
+#include <new>
+
+#include "../../include/sw4g.h"
+#include "ew.h"
+#include "kernels.h"
+#include "sbp.h"
+#include "setup.h"
+
+using namespace sw4g;
+
+struct sw4g_ew {
+   EW* impl;
+};
+
+namespace {
+
+cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+bool bounds_ok(int ib, int ie, int jb, int je, int kb, int ke)
+{
+   return ie >= ib && je >= jb && ke >= kb;
+}
+
+GridSpec to_spec(const sw4g_grid* g)
+{
+   GridSpec s;
+   s.nx = g->nx;
+   s.ny = g->ny;
+   s.nz = g->nz;
+   s.h = g->h;
+   s.zmin = g->zmin;
+   for (int q = 0; q < 6; q++) s.bc[q] = g->bc[q];
+   s.sg_gp = g->sg_gp;
+   s.sg_damping = g->sg_damping;
+   s.sg_order = g->sg_order;
+   s.soa = g->soa;
+   return s;
+}
+
+SourceSpec to_source(const sw4g_source* s)
+{
+   SourceSpec o;
+   o.x = s->x;
+   o.y = s->y;
+   o.z = s->z;
+   o.moment = s->moment != 0;
+   o.f[0] = s->fx;
+   o.f[1] = s->fy;
+   o.f[2] = s->fz;
+   o.m[0] = s->mxx;
+   o.m[1] = s->mxy;
+   o.m[2] = s->mxz;
+   o.m[3] = s->myy;
+   o.m[4] = s->myz;
+   o.m[5] = s->mzz;
+   o.freq = s->freq;
+   o.t0 = s->t0;
+   o.kind = s->kind;
+   return o;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* sw4g_version(void) { return "sw4g 0.1 (sm_103a)"; }
+
+const char* sw4g_status_string(int status)
+{
+   switch (status) {
+      case SW4G_OK: return "ok";
+      case SW4G_BAD_ARGUMENT: return "bad argument";
+      case SW4G_CUDA_ERROR: return "CUDA error";
+      case SW4G_NAN_DETECTED: return "NaN detected";
+      case SW4G_NOT_SUPPORTED: return "not supported";
+      case SW4G_TIMEOUT: return "device wait timed out";
+      default: return "unknown status";
+   }
+}
+
+int sw4g_stencil_coefficients(double* acof, double* ghcof, double* bope, double* sbop)
+{
+   if (!acof || !ghcof || !bope || !sbop) return SW4G_BAD_ARGUMENT;
+   sbp_coefficients(acof, ghcof, bope, sbop);
+   return SW4G_OK;
+}
+
+int sw4g_rhs4sg(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                int nk, const int* onesided, double* lu, const double* u, const double* mu,
+                const double* lambda, double h, const double* strx, const double* stry,
+                const double* strz, void* stream)
+{
+   if (!onesided || !lu || !u || !mu || !lambda || !strx || !stry || !strz || !(h > 0))
+      return SW4G_BAD_ARGUMENT;
+   if (!bounds_ok(ifirst, ilast, jfirst, jlast, kfirst, klast)) return SW4G_BAD_ARGUMENT;
+   // one-sided rows read planes 0..8 (top) or nk-7..nk+1 (bottom)
+   if (onesided[4] == 1 && (kfirst > 0 || klast < 8)) return SW4G_BAD_ARGUMENT;
+   if (onesided[5] == 1 && (kfirst > nk - 7 || klast < nk + 1)) return SW4G_BAD_ARGUMENT;
+   return launch_rhs4sg_direct(soa, ifirst, ilast, jfirst, jlast, kfirst, klast, nk, onesided, lu,
+                               u, mu, lambda, h, strx, stry, strz, as_stream(stream));
+}
+
+int sw4g_predfort(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
+                  const double* u, const double* um, const double* lu, const double* fo,
+                  const double* rho, double dt2, void* stream)
+{
+   if (!up || !u || !um || !lu || !fo || !rho || !bounds_ok(ib, ie, jb, je, kb, ke))
+      return SW4G_BAD_ARGUMENT;
+   return launch_predfort(soa, ib, ie, jb, je, kb, ke, up, u, um, lu, fo, rho, dt2,
+                          as_stream(stream));
+}
+
+int sw4g_corrfort(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
+                  const double* lu, const double* fo, const double* rho, double dt4, void* stream)
+{
+   if (!up || !lu || !fo || !rho || !bounds_ok(ib, ie, jb, je, kb, ke)) return SW4G_BAD_ARGUMENT;
+   return launch_corrfort(soa, ib, ie, jb, je, kb, ke, up, lu, fo, rho, dt4, as_stream(stream));
+}
+
+int sw4g_dpdmtfort(int ib, int ie, int jb, int je, int kb, int ke, const double* up,
+                   const double* u, const double* um, double* u2, double dt2i, void* stream)
+{
+   if (!up || !u || !um || !u2 || !bounds_ok(ib, ie, jb, je, kb, ke)) return SW4G_BAD_ARGUMENT;
+   return launch_dpdmtfort(ib, ie, jb, je, kb, ke, up, u, um, u2, dt2i, as_stream(stream));
+}
+
+static int addsgd_common(int order, int soa, int ifirst, int ilast, int jfirst, int jlast,
+                         int kfirst, int klast, double* up, const double* u, const double* um,
+                         const double* rho, const double* dcx, const double* dcy,
+                         const double* dcz, const double* strx, const double* stry,
+                         const double* strz, const double* cox, const double* coy,
+                         const double* coz, double beta, void* stream)
+{
+   if (!up || !u || !um || !rho || !dcx || !dcy || !dcz || !strx || !stry || !strz || !cox ||
+       !coy || !coz || !bounds_ok(ifirst, ilast, jfirst, jlast, kfirst, klast))
+      return SW4G_BAD_ARGUMENT;
+   return launch_addsgd(order, soa, ifirst, ilast, jfirst, jlast, kfirst, klast, up, u, um, rho,
+                        dcx, dcy, dcz, strx, stry, strz, cox, coy, coz, beta, as_stream(stream));
+}
+
+int sw4g_addsgd4fort(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                     double* up, const double* u, const double* um, const double* rho,
+                     const double* dcx, const double* dcy, const double* dcz, const double* strx,
+                     const double* stry, const double* strz, const double* cox, const double* coy,
+                     const double* coz, double beta, void* stream)
+{
+   return addsgd_common(4, soa, ifirst, ilast, jfirst, jlast, kfirst, klast, up, u, um, rho, dcx,
+                        dcy, dcz, strx, stry, strz, cox, coy, coz, beta, stream);
+}
+
+int sw4g_addsgd6fort(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                     double* up, const double* u, const double* um, const double* rho,
+                     const double* dcx, const double* dcy, const double* dcz, const double* strx,
+                     const double* stry, const double* strz, const double* cox, const double* coy,
+                     const double* coz, double beta, void* stream)
+{
+   return addsgd_common(6, soa, ifirst, ilast, jfirst, jlast, kfirst, klast, up, u, um, rho, dcx,
+                        dcy, dcz, strx, stry, strz, cox, coy, coz, beta, stream);
+}
+
+int sw4g_bcfortsg(int soa, int ib, int ie, int jb, int je, int kb, int ke, const int* wind,
+                  int nx, int ny, int nz, double* u, double h, const int* bccnd, const double* sbop,
+                  const double* mu, const double* lambda, const double* const* bforce,
+                  const double* strx, const double* stry, void* stream)
+{
+   if (!wind || !u || !bccnd || !sbop || !mu || !lambda || !strx || !stry ||
+       !bounds_ok(ib, ie, jb, je, kb, ke))
+      return SW4G_BAD_ARGUMENT;
+   return launch_bcfortsg(soa, ib, ie, jb, je, kb, ke, wind, nx, ny, nz, u, h, bccnd, sbop, mu,
+                          lambda, bforce, strx, stry, as_stream(stream));
+}
+
+int sw4g_supergrid_profile(const sw4g_grid* g, int axis, double* dc, double* str, double* corner)
+{
+   if (!g || axis < 0 || axis > 2 || !dc || !str || !corner) return SW4G_BAD_ARGUMENT;
+   const SupergridProfiles p = supergrid_profiles(to_spec(g));
+   const size_t n = p.dc[axis].size();
+   std::memcpy(dc, p.dc[axis].data(), n * sizeof(double));
+   std::memcpy(str, p.str[axis].data(), n * sizeof(double));
+   std::memcpy(corner, p.co[axis].data(), n * sizeof(double));
+   return SW4G_OK;
+}
+
+int sw4g_boundary_windows(const sw4g_grid* g, int* wind, int* npts)
+{
+   if (!g || !wind || !npts) return SW4G_BAD_ARGUMENT;
+   boundary_windows(to_spec(g), wind, npts);
+   return SW4G_OK;
+}
+
+int sw4g_discretize_source(const sw4g_grid* g, const sw4g_source* s, int cap, int* ijk,
+                           double* amp, int* n)
+{
+   if (!g || !s || !n || cap < 0 || (cap > 0 && (!ijk || !amp))) return SW4G_BAD_ARGUMENT;
+   const GridSpec spec = to_spec(g);
+   int onesided[6];
+   onesided_flags(spec, onesided);
+   std::vector<GridPointSource> out;
+   discretize_source(spec, onesided, to_source(s), out);
+   *n = (int)out.size();
+   for (int q = 0; q < (int)out.size() && q < cap; q++) {
+      ijk[3 * q] = out[q].i;
+      ijk[3 * q + 1] = out[q].j;
+      ijk[3 * q + 2] = out[q].k;
+      for (int c = 0; c < 3; c++) amp[3 * q + c] = out[q].amp[c];
+   }
+   return SW4G_OK;
+}
+
+int sw4g_ew_create(const sw4g_grid* g, void* stream, sw4g_ew** out)
+{
+   if (!g || !out) return SW4G_BAD_ARGUMENT;
+   *out = nullptr;
+   EW* e = new (std::nothrow) EW(to_spec(g), as_stream(stream));
+   if (!e) return SW4G_BAD_ARGUMENT;
+   int st = e->init();
+   if (st != SW4G_OK) {
+      delete e;
+      return st;
+   }
+   sw4g_ew* h = new (std::nothrow) sw4g_ew{e};
+   if (!h) {
+      delete e;
+      return SW4G_BAD_ARGUMENT;
+   }
+   *out = h;
+   return SW4G_OK;
+}
+
+int sw4g_ew_destroy(sw4g_ew* ew)
+{
+   if (!ew) return SW4G_BAD_ARGUMENT;
+   delete ew->impl;
+   delete ew;
+   return SW4G_OK;
+}
+
+long long sw4g_ew_npts(const sw4g_ew* ew) { return ew ? ew->impl->npts() : -1; }
+
+int sw4g_ew_set_material(sw4g_ew* ew, const double* rho, const double* mu, const double* lambda,
+                         int on_device)
+{
+   if (!ew) return SW4G_BAD_ARGUMENT;
+   return ew->impl->set_material(rho, mu, lambda, on_device != 0);
+}
+
+int sw4g_ew_add_source(sw4g_ew* ew, const sw4g_source* s)
+{
+   if (!ew || !s) return SW4G_BAD_ARGUMENT;
+   return ew->impl->add_source(to_source(s));
+}
+
+int sw4g_ew_add_grid_point_sources(sw4g_ew* ew, int n, const int* ijk, const double* amp,
+                                   const double* freq, const double* t0, const int* kind)
+{
+   if (!ew) return SW4G_BAD_ARGUMENT;
+   return ew->impl->add_grid_point_sources(n, ijk, amp, freq, t0, kind);
+}
+
+int sw4g_ew_clear_sources(sw4g_ew* ew) { return ew ? ew->impl->clear_sources() : SW4G_BAD_ARGUMENT; }
+
+int sw4g_ew_num_grid_point_sources(const sw4g_ew* ew)
+{
+   return ew ? ew->impl->num_grid_point_sources() : -1;
+}
+
+int sw4g_ew_set_time_step(sw4g_ew* ew, double dt, double t0)
+{
+   return ew ? ew->impl->set_time_step(dt, t0) : SW4G_BAD_ARGUMENT;
+}
+
+int sw4g_ew_compute_time_step(sw4g_ew* ew, double cfl, double tmax, double* dt, int* nsteps)
+{
+   return ew ? ew->impl->compute_time_step(cfl, tmax, dt, nsteps) : SW4G_BAD_ARGUMENT;
+}
+
+double sw4g_ew_time(const sw4g_ew* ew) { return ew ? ew->impl->time() : 0.0; }
+
+int sw4g_ew_set_fields(sw4g_ew* ew, const double* u, const double* um, int on_device)
+{
+   return ew ? ew->impl->set_fields(u, um, on_device != 0) : SW4G_BAD_ARGUMENT;
+}
+
+int sw4g_ew_get_fields(const sw4g_ew* ew, double* u, double* um, int on_device)
+{
+   return ew ? ew->impl->get_fields(u, um, on_device != 0) : SW4G_BAD_ARGUMENT;
+}
+
+double* sw4g_ew_field(const sw4g_ew* ew, int which)
+{
+   if (!ew) return nullptr;
+   return which == 0 ? ew->impl->field_u() : which == 1 ? ew->impl->field_um() : nullptr;
+}
+
+int sw4g_ew_step(sw4g_ew* ew, int nsteps, int mode)
+{
+   return ew ? ew->impl->step(nsteps, mode) : SW4G_BAD_ARGUMENT;
+}
+
+int sw4g_ew_enforce_bc(sw4g_ew* ew, double* u)
+{
+   if (!ew || !u) return SW4G_BAD_ARGUMENT;
+   return ew->impl->enforce_bc(u);
+}
+
+int sw4g_ew_launches_per_step(const sw4g_ew* ew, int mode)
+{
+   return ew ? ew->impl->launches_per_step(mode) : -1;
+}
+
+int sw4g_ew_profile_kernels(sw4g_ew* ew, int nrep, double* ms)
+{
+   if (!ew || !ms) return SW4G_BAD_ARGUMENT;
+   return ew->impl->profile_kernels(nrep, ms);
+}
+
+int sw4g_fma_peak(int precision, double* tflops, void* stream)
+{
+   if (!tflops || (precision != 64 && precision != 32)) return SW4G_BAD_ARGUMENT;
+   return fma_peak(precision, tflops, as_stream(stream));
+}
+
+}  // extern "C"

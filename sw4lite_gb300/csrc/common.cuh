@@ -1,0 +1,67 @@
+// Shared definitions for the sm_103a kernels of the sw4lite elastic time step.
+//
+// Index conventions are the reference's (src/EW.C:1921-1949, src/rhs4sg_rev.C:58-78):
+// inclusive 1-based bounds [ib,ie]x[jb,je]x[kb,ke] that include 2 ghost points
+// per side, i fastest.  A 3-component field is stored either component-major
+// ("SoA", the reference's _rev/_indrev layout, u[c*npts + p]) or point-major
+// ("AoS", u[3*p + c]); Box carries the two strides so one kernel serves both.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace sw4g {
+
+struct Box {
+   int ib, ie, jb, je, kb, ke;
+   long long ni, nij, npts;
+   long long cs;  // component stride: npts (SoA) or 1 (AoS)
+   long long ps;  // point stride: 1 (SoA) or 3 (AoS)
+};
+
+inline Box make_box(int soa, int ib, int ie, int jb, int je, int kb, int ke)
+{
+   Box b;
+   b.ib = ib; b.ie = ie; b.jb = jb; b.je = je; b.kb = kb; b.ke = ke;
+   b.ni = ie - ib + 1;
+   b.nij = b.ni * (je - jb + 1);
+   b.npts = b.nij * (ke - kb + 1);
+   b.cs = soa ? b.npts : 1;
+   b.ps = soa ? 1 : 3;
+   return b;
+}
+
+__host__ __device__ __forceinline__ long long pidx(const Box& b, int i, int j, int k)
+{
+   return (long long)(i - b.ib) + b.ni * (j - b.jb) + b.nij * (long long)(k - b.kb);
+}
+
+__host__ __device__ __forceinline__ long long cidx(const Box& b, int c, int i, int j, int k)
+{
+   return c * b.cs + b.ps * pidx(b, i, j, k);
+}
+
+// Status codes returned through the C ABI (include/sw4g.h).
+enum Status : int {
+   kOk = 0,
+   kBadArgument = 1,
+   kCudaError = 2,
+   kNanDetected = 3,
+   kNotSupported = 4,
+   kTimeout = 5,
+};
+
+// Converts the sticky/launch error state into a status code.
+inline int launch_status()
+{
+   cudaError_t e = cudaGetLastError();
+   return e == cudaSuccess ? kOk : kCudaError;
+}
+
+inline int blocks_for(long long n, int threads)
+{
+   long long b = (n + threads - 1) / threads;
+   return (int)(b > 0 ? b : 1);
+}
+
+}  // namespace sw4g

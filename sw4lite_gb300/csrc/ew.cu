@@ -1,0 +1,461 @@
+// Host-side time loop for one Cartesian grid; see ew.h.
+#include "ew.h"
+
+#include <cstring>
+
+#include "sbp.h"
+
+namespace sw4g {
+
+namespace {
+#define SW4G_TRY(expr)                  \
+   do {                                 \
+      int _st = (expr);                 \
+      if (_st != kOk) return _st;       \
+   } while (0)
+
+int cuda_ok(cudaError_t e) { return e == cudaSuccess ? kOk : kCudaError; }
+}  // namespace
+
+EW::EW(const GridSpec& g, cudaStream_t stream) : g_(g), stream_(stream) {}
+
+EW::~EW()
+{
+   auto f = [](void* p) {
+      if (p) cudaFree(p);
+   };
+   f(rho_);
+   f(mu_);
+   f(la_);
+   f(irho_);
+   for (auto* p : dprof_) f(p);
+   f(wstore_);
+   for (auto* p : lev_) f(p);
+   f(lu_);
+   f(f_);
+   f(uacc_);
+   f(slab_);
+   f(dsrc_mem_);
+}
+
+int EW::init()
+{
+   if (g_.nx < 8 || g_.ny < 8 || g_.nz < 8 || !(g_.h > 0)) return kBadArgument;
+   if (g_.soa != 1) return kNotSupported;  // the time loop keeps fields component-major
+   for (int s = 0; s < 6; s++) {
+      const int t = g_.bc[s];
+      if (!(t == kStressFree || t == kDirichlet || t == kSuperGrid || t == kPeriodic)) return kBadArgument;
+      if (t == kStressFree && s < 4) return kNotSupported;
+   }
+   if (g_.sg_order != 4 && g_.sg_order != 6) return kBadArgument;
+   if ((g_.bc[4] == kStressFree && g_.nz < 14) || (g_.bc[5] == kStressFree && g_.nz < 14))
+      return kBadArgument;  // the one-sided rows need 8 interior planes on each such side
+   b_ = grid_bounds(g_);
+   npts_ = b_.npts();
+   boundary_windows(g_, wind_, bcpts_);
+   onesided_flags(g_, onesided_);
+   double acof[384], ghcof[6], bope[48];
+   sbp_coefficients(acof, ghcof, bope, sbop_);
+   prof_ = supergrid_profiles(g_);
+
+   const size_t n = (size_t)npts_;
+   SW4G_TRY(cuda_ok(cudaMalloc(&rho_, n * sizeof(double))));
+   SW4G_TRY(cuda_ok(cudaMalloc(&mu_, n * sizeof(double))));
+   SW4G_TRY(cuda_ok(cudaMalloc(&la_, n * sizeof(double))));
+   SW4G_TRY(cuda_ok(cudaMalloc(&irho_, n * sizeof(double))));
+   SW4G_TRY(cuda_ok(cudaMalloc(&wstore_, kWeightArrays * n * sizeof(double))));
+   for (int q = 0; q < kWeightArrays; q++) w_.p[q] = wstore_ + q * n;
+   for (int q = 0; q < 4; q++) {
+      SW4G_TRY(cuda_ok(cudaMalloc(&lev_[q], 3 * n * sizeof(double))));
+      SW4G_TRY(cuda_ok(cudaMemsetAsync(lev_[q], 0, 3 * n * sizeof(double), stream_)));
+   }
+   const int len[3] = {b_.ie - b_.ib + 1, b_.je - b_.jb + 1, b_.ke - b_.kb + 1};
+   for (int w = 0; w < 3; w++)
+      for (int ax = 0; ax < 3; ax++) {
+         double*& d = dprof_[3 * w + ax];
+         SW4G_TRY(cuda_ok(cudaMalloc(&d, len[ax] * sizeof(double))));
+         const std::vector<double>& src = w == 0 ? prof_.dc[ax] : w == 1 ? prof_.str[ax] : prof_.co[ax];
+         SW4G_TRY(cuda_ok(cudaMemcpy(d, src.data(), len[ax] * sizeof(double), cudaMemcpyHostToDevice)));
+      }
+   // slab for the corrector's stage field on the one-sided rows: planes kb..8
+   // (top) or nz-7..ke (bottom)
+   const long long nij = (long long)len[0] * len[1];
+   slab_len_ = 3 * nij * 10;
+   if (onesided_[4] || onesided_[5])
+      SW4G_TRY(cuda_ok(cudaMalloc(&slab_, 2 * slab_len_ * sizeof(double))));
+   SW4G_TRY(upload_sbp_tables_direct());
+   SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
+   ready_ = true;
+   return kOk;
+}
+
+const double* EW::profile(int which, int axis) const
+{
+   if (which < 0 || which > 2 || axis < 0 || axis > 2) return nullptr;
+   return dprof_[3 * which + axis];
+}
+
+int EW::set_material(const double* rho, const double* mu, const double* la, bool on_device)
+{
+   if (!ready_ || !rho || !mu || !la) return kBadArgument;
+   const size_t bytes = (size_t)npts_ * sizeof(double);
+   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+   SW4G_TRY(cuda_ok(cudaMemcpyAsync(rho_, rho, bytes, kind, stream_)));
+   SW4G_TRY(cuda_ok(cudaMemcpyAsync(mu_, mu, bytes, kind, stream_)));
+   SW4G_TRY(cuda_ok(cudaMemcpyAsync(la_, la, bytes, kind, stream_)));
+   SW4G_TRY(launch_inverse(npts_, rho_, irho_, stream_));
+   Box b = make_box(1, b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke);
+   SW4G_TRY(launch_weights(b, mu_, la_, dprof_[3], dprof_[4], dprof_[5], g_.h, w_, stream_));
+   SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
+   material_ = true;
+   return kOk;
+}
+
+int EW::add_source(const SourceSpec& s)
+{
+   if (!ready_) return kBadArgument;
+   if (s.kind < 0 || s.kind > 3 || !(s.freq > 0)) return kBadArgument;
+   discretize_source(g_, onesided_, s, hsrc_);
+   src_dirty_ = true;
+   return kOk;
+}
+
+int EW::add_grid_point_sources(int n, const int* ijk, const double* amp, const double* freq,
+                               const double* t0, const int* kind)
+{
+   if (!ready_ || n < 0 || (n > 0 && (!ijk || !amp || !freq || !t0 || !kind))) return kBadArgument;
+   for (int s = 0; s < n; s++) {
+      GridPointSource p;
+      p.i = ijk[3 * s];
+      p.j = ijk[3 * s + 1];
+      p.k = ijk[3 * s + 2];
+      if (p.i < 1 || p.i > g_.nx || p.j < 1 || p.j > g_.ny || p.k < 1 || p.k > g_.nz)
+         return kBadArgument;
+      if (kind[s] < 0 || kind[s] > 3) return kBadArgument;
+      for (int c = 0; c < 3; c++) p.amp[c] = amp[3 * s + c];
+      p.freq = freq[s];
+      p.t0 = t0[s];
+      p.kind = kind[s];
+      hsrc_.push_back(p);
+   }
+   src_dirty_ = true;
+   return kOk;
+}
+
+int EW::clear_sources()
+{
+   hsrc_.clear();
+   src_dirty_ = true;
+   return kOk;
+}
+
+int EW::upload_sources()
+{
+   if (!src_dirty_) return kOk;
+   std::vector<GridPointSource> src = hsrc_;
+   std::vector<int> start;
+   group_sources(src, start);
+   const int ns = (int)src.size(), np = (int)start.size() - 1;
+   // one block: start | ijk | kind | amp | freq | t0   (ints first, then doubles, 8-aligned)
+   const size_t ints = (size_t)(np + 1) + 3 * (size_t)ns + ns;
+   const size_t int_bytes = ((ints * sizeof(int) + 7) / 8) * 8;
+   const size_t bytes = int_bytes + (5 * (size_t)ns) * sizeof(double);
+   if (dsrc_mem_) {
+      SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
+      cudaFree(dsrc_mem_);
+      dsrc_mem_ = nullptr;
+   }
+   dsrc_ = SourceSet{};
+   src_dirty_ = false;
+   if (ns == 0) return kOk;
+   std::vector<unsigned char> host(bytes, 0);
+   int* hi = reinterpret_cast<int*>(host.data());
+   for (int r = 0; r <= np; r++) hi[r] = start[r];
+   int* hijk = hi + np + 1;
+   int* hkind = hijk + 3 * ns;
+   double* hd = reinterpret_cast<double*>(host.data() + int_bytes);
+   double* hamp = hd;
+   double* hfreq = hamp + 3 * ns;
+   double* ht0 = hfreq + ns;
+   for (int s = 0; s < ns; s++) {
+      hijk[3 * s] = src[s].i;
+      hijk[3 * s + 1] = src[s].j;
+      hijk[3 * s + 2] = src[s].k;
+      hkind[s] = src[s].kind;
+      for (int c = 0; c < 3; c++) hamp[3 * s + c] = src[s].amp[c];
+      hfreq[s] = src[s].freq;
+      ht0[s] = src[s].t0;
+   }
+   SW4G_TRY(cuda_ok(cudaMalloc(&dsrc_mem_, bytes)));
+   SW4G_TRY(cuda_ok(cudaMemcpy(dsrc_mem_, host.data(), bytes, cudaMemcpyHostToDevice)));
+   unsigned char* base = static_cast<unsigned char*>(dsrc_mem_);
+   const int* di = reinterpret_cast<const int*>(base);
+   const double* dd = reinterpret_cast<const double*>(base + int_bytes);
+   dsrc_.npoints = np;
+   dsrc_.nsources = ns;
+   dsrc_.start = di;
+   dsrc_.ijk = di + np + 1;
+   dsrc_.kind = di + np + 1 + 3 * ns;
+   dsrc_.amp = dd;
+   dsrc_.freq = dd + 3 * ns;
+   dsrc_.t0 = dd + 4 * ns;
+   return kOk;
+}
+
+int EW::set_time_step(double dt, double t0)
+{
+   if (!(dt > 0)) return kBadArgument;
+   dt_ = dt;
+   t_ = t0;
+   return kOk;
+}
+
+int EW::compute_time_step(double cfl, double tmax, double* dt, int* nsteps)
+{
+   if (!material_ || !(cfl > 0)) return kBadArgument;
+   const size_t n = (size_t)npts_;
+   std::vector<double> r(n), m(n), l(n);
+   SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
+   SW4G_TRY(cuda_ok(cudaMemcpy(r.data(), rho_, n * sizeof(double), cudaMemcpyDeviceToHost)));
+   SW4G_TRY(cuda_ok(cudaMemcpy(m.data(), mu_, n * sizeof(double), cudaMemcpyDeviceToHost)));
+   SW4G_TRY(cuda_ok(cudaMemcpy(l.data(), la_, n * sizeof(double), cudaMemcpyDeviceToHost)));
+   int ns = 0;
+   const double d = cfl_time_step(g_, r.data(), m.data(), l.data(), cfl, t_, tmax, &ns);
+   dt_ = d;
+   if (dt) *dt = d;
+   if (nsteps) *nsteps = ns;
+   return kOk;
+}
+
+int EW::set_fields(const double* u, const double* um, bool on_device)
+{
+   if (!ready_ || !u || !um) return kBadArgument;
+   const size_t bytes = 3 * (size_t)npts_ * sizeof(double);
+   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+   SW4G_TRY(cuda_ok(cudaMemcpyAsync(lev_[iu_], u, bytes, kind, stream_)));
+   SW4G_TRY(cuda_ok(cudaMemcpyAsync(lev_[ium_], um, bytes, kind, stream_)));
+   return kOk;
+}
+
+int EW::get_fields(double* u, double* um, bool on_device) const
+{
+   if (!ready_) return kBadArgument;
+   const size_t bytes = 3 * (size_t)npts_ * sizeof(double);
+   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+   if (u) SW4G_TRY(cuda_ok(cudaMemcpyAsync(u, lev_[iu_], bytes, kind, stream_)));
+   if (um) SW4G_TRY(cuda_ok(cudaMemcpyAsync(um, lev_[ium_], bytes, kind, stream_)));
+   if (!on_device) SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
+   return kOk;
+}
+
+int EW::enforce_bc(double* u)
+{
+   return launch_bcfortsg(1, b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke, wind_, g_.nx, g_.ny, g_.nz,
+                          u, g_.h, g_.bc, sbop_, mu_, la_, nullptr, dprof_[3], dprof_[4], stream_);
+}
+
+int EW::ensure_phase_arrays()
+{
+   if (lu_) return kOk;
+   const size_t bytes = 3 * (size_t)npts_ * sizeof(double);
+   SW4G_TRY(cuda_ok(cudaMalloc(&lu_, bytes)));
+   SW4G_TRY(cuda_ok(cudaMalloc(&f_, bytes)));
+   SW4G_TRY(cuda_ok(cudaMalloc(&uacc_, bytes)));
+   SW4G_TRY(cuda_ok(cudaMemsetAsync(lu_, 0, bytes, stream_)));
+   SW4G_TRY(cuda_ok(cudaMemsetAsync(uacc_, 0, bytes, stream_)));
+   return kOk;
+}
+
+int EW::step(int nsteps, int mode)
+{
+   if (!ready_ || !material_ || !(dt_ > 0) || nsteps < 0) return kBadArgument;
+   if (mode != kModePhases && mode != kModeFused) return kBadArgument;
+   SW4G_TRY(upload_sources());
+   if (mode == kModePhases) SW4G_TRY(ensure_phase_arrays());
+   for (int n = 0; n < nsteps; n++) SW4G_TRY(mode == kModePhases ? step_phases() : step_fused());
+   return kOk;
+}
+
+// The reference CPU phase order (src/EW.C:2537-2756) with the GPU kernels.
+int EW::step_phases()
+{
+   const Bounds& b = b_;
+   int ip = 0;
+   while (ip == iu_ || ip == ium_) ip++;
+   double *up = lev_[ip], *u = lev_[iu_], *um = lev_[ium_];
+   const double dt = dt_;
+   SW4G_TRY(launch_force_dense(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, f_, dsrc_, t_, 0, stream_));
+   SW4G_TRY(launch_rhs4sg_direct(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, g_.nz, onesided_, lu_, u,
+                                 mu_, la_, g_.h, dprof_[3], dprof_[4], dprof_[5], stream_));
+   SW4G_TRY(launch_predfort(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, up, u, um, lu_, f_, rho_,
+                            dt * dt, stream_));
+   SW4G_TRY(enforce_bc(up));
+   SW4G_TRY(launch_force_dense(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, f_, dsrc_, t_, 1, stream_));
+   SW4G_TRY(launch_dpdmtfort(b.ib, b.ie, b.jb, b.je, b.kb, b.ke, up, u, um, uacc_, 1 / (dt * dt),
+                             stream_));
+   SW4G_TRY(launch_rhs4sg_direct(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, g_.nz, onesided_, lu_,
+                                 uacc_, mu_, la_, g_.h, dprof_[3], dprof_[4], dprof_[5], stream_));
+   SW4G_TRY(launch_corrfort(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, up, lu_, f_, rho_,
+                            dt * dt * dt * dt, stream_));
+   if (prof_.used && g_.sg_damping != 0)
+      SW4G_TRY(launch_addsgd(g_.sg_order, 1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, up, u, um, rho_,
+                             dprof_[0], dprof_[1], dprof_[2], dprof_[3], dprof_[4], dprof_[5],
+                             dprof_[6], dprof_[7], dprof_[8], g_.sg_damping, stream_));
+   SW4G_TRY(enforce_bc(up));
+   ium_ = iu_;
+   iu_ = ip;
+   t_ += dt;
+   return kOk;
+}
+
+// Fused stages: predictor kernel (+ one-sided rows, sparse forcing, BC), then the
+// corrector kernel with supergrid damping (+ rows, forcing, BC).  A step is the
+// pieces 0..5 in order: 0 predictor stage kernel, 1 predictor rows, 2 predictor
+// forcing + BC, 3 corrector stage kernel, 4 corrector rows (+ 6th-order damping),
+// 5 corrector forcing + BC; ip receives the predicted level, iq the new level.
+int EW::fused_piece(int piece, int ip, int iq)
+{
+   const Bounds& bd = b_;
+   Box b = make_box(1, bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke);
+   double *up = lev_[ip], *out = lev_[iq], *u = lev_[iu_], *um = lev_[ium_];
+   const double dt = dt_, dt2 = dt * dt;
+   const int nz = g_.nz;
+   const double beta = (prof_.used && g_.sg_damping != 0) ? g_.sg_damping : 0.0;
+   const double beta4 = g_.sg_order == 4 ? beta : 0.0;
+   const double* dc[3] = {dprof_[0], dprof_[1], dprof_[2]};
+   const double* st[3] = {dprof_[3], dprof_[4], dprof_[5]};
+   const double* co[3] = {dprof_[6], dprof_[7], dprof_[8]};
+
+   if (piece == 0 || piece == 3) {
+      FusedStage fs;
+      fs.b = b;
+      fs.k1 = onesided_[4] ? 7 : 1;
+      fs.k2 = onesided_[5] ? nz - 6 : nz;
+      fs.mu = mu_;
+      fs.la = la_;
+      fs.rho = rho_;
+      fs.irho = irho_;
+      fs.w = w_;
+      for (int q = 0; q < 3; q++) {
+         fs.st[q] = st[q];
+         fs.dc[q] = dc[q];
+         fs.co[q] = co[q];
+      }
+      fs.h = g_.h;
+      fs.dt = dt;
+      fs.u = u;
+      fs.um = um;
+      if (piece == 0) {
+         fs.corrector = 0;
+         fs.up = nullptr;
+         fs.out = up;
+         fs.beta = 0;
+      } else {
+         fs.corrector = 1;
+         fs.up = up;
+         fs.out = out;
+         fs.beta = beta4;
+      }
+      return launch_fused_stage(fs, stream_);
+   }
+   if (piece == 1) {
+      for (int side = 0; side < 2; side++)
+         if (onesided_[4 + side])
+            SW4G_TRY(launch_stage_rows(0, side == 0, b, nz, u, b, mu_, la_, g_.h, st[0], st[1], st[2],
+                                       u, um, nullptr, up, rho_, irho_, dt2, 0.0, dc, st, co, stream_));
+      return kOk;
+   }
+   if (piece == 2) {
+      SW4G_TRY(launch_force_update(1, bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, up, rho_, dsrc_, t_, 0,
+                                   dt2, stream_));
+      return enforce_bc(up);
+   }
+   if (piece == 4) {
+      for (int side = 0; side < 2; side++) {
+         if (!onesided_[4 + side]) continue;
+         const int k0 = side == 0 ? bd.kb : nz - 7, k1 = side == 0 ? 8 : bd.ke;
+         double* slab = slab_ + side * slab_len_;
+         SW4G_TRY(launch_uacc_slab(b, k0, k1, up, u, um, slab, stream_));
+         Box sb = make_box(1, bd.ib, bd.ie, bd.jb, bd.je, k0, k1);
+         SW4G_TRY(launch_stage_rows(1, side == 0, b, nz, slab, sb, mu_, la_, g_.h, st[0], st[1],
+                                    st[2], u, um, up, out, rho_, irho_, dt2 / 12, beta4, dc, st, co,
+                                    stream_));
+      }
+      if (beta != 0 && g_.sg_order == 6)
+         SW4G_TRY(launch_addsgd(6, 1, bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, out, u, um, rho_,
+                                dc[0], dc[1], dc[2], st[0], st[1], st[2], co[0], co[1], co[2], beta,
+                                stream_));
+      return kOk;
+   }
+   if (piece == 5) {
+      SW4G_TRY(launch_force_update(1, bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, out, rho_, dsrc_, t_, 1,
+                                   dt2 * dt2 / 12, stream_));
+      return enforce_bc(out);
+   }
+   return kBadArgument;
+}
+
+int EW::step_fused()
+{
+   int ip = 0;
+   while (ip == iu_ || ip == ium_) ip++;
+   int iq = ip + 1;
+   while (iq == iu_ || iq == ium_) iq++;
+   for (int piece = 0; piece < 6; piece++) SW4G_TRY(fused_piece(piece, ip, iq));
+   ium_ = iu_;
+   iu_ = iq;
+   t_ += dt_;
+   return kOk;
+}
+
+int EW::profile_kernels(int nrep, double ms[4])
+{
+   if (!ready_ || !material_ || !(dt_ > 0) || nrep < 1 || !ms) return kBadArgument;
+   SW4G_TRY(upload_sources());
+   int ip = 0;
+   while (ip == iu_ || ip == ium_) ip++;
+   int iq = ip + 1;
+   while (iq == iu_ || iq == ium_) iq++;
+   // one full fused step's pieces first, so every input level holds valid data
+   for (int piece = 0; piece < 6; piece++) SW4G_TRY(fused_piece(piece, ip, iq));
+   const int groups[4][2] = {{0, -1}, {3, -1}, {1, 4}, {2, 5}};
+   cudaEvent_t e0, e1;
+   SW4G_TRY(cuda_ok(cudaEventCreate(&e0)));
+   SW4G_TRY(cuda_ok(cudaEventCreate(&e1)));
+   int status = kOk;
+   for (int g = 0; g < 4 && status == kOk; g++) {
+      cudaEventRecord(e0, stream_);
+      for (int r = 0; r < nrep && status == kOk; r++)
+         for (int q = 0; q < 2 && status == kOk; q++)
+            if (groups[g][q] >= 0) status = fused_piece(groups[g][q], ip, iq);
+      cudaEventRecord(e1, stream_);
+      if (cudaEventSynchronize(e1) != cudaSuccess) status = kCudaError;
+      float t = 0;
+      cudaEventElapsedTime(&t, e0, e1);
+      ms[g] = t / nrep;
+   }
+   cudaEventDestroy(e0);
+   cudaEventDestroy(e1);
+   return status;
+}
+
+int EW::launches_per_step(int mode) const
+{
+   int bc = 0;
+   for (int s = 0; s < 6; s++) {
+      const int t = g_.bc[s];
+      if ((t == kDirichlet || t == kSuperGrid || t == kPeriodic) && bcpts_[s] > 0) bc++;
+      if (t == kStressFree) bc++;
+   }
+   const int rows = onesided_[4] + onesided_[5];
+   const int src = hsrc_.empty() ? 0 : 1;
+   const bool damp = prof_.used && g_.sg_damping != 0;
+   if (mode == kModePhases) {
+      // force(memset+kernel), rhs (center + rows), pred, bc, force, dpdm, rhs, corr, addsgd, bc
+      const int rhs = 1 + rows;
+      return 2 * (1 + src) + 2 * rhs + 3 + (damp ? 1 : 0) + 2 * bc;
+   }
+   return 2 * (1 + rows + src + bc) + rows + (damp && g_.sg_order == 6 ? 1 : 0);
+}
+
+}  // namespace sw4g

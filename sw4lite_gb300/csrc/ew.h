@@ -1,0 +1,112 @@
+// Host-side driver of the elastic time step for one Cartesian grid on one GPU:
+// the GB300 counterpart of the reference's EW time loop (src/EW.C:2339-2930)
+// for the Forcing, Scheme, BC-phys and Supergrid phases.
+//
+// Ownership: the EW object owns its device arrays (material, 1-D profiles,
+// precomputed weights, four rotating time levels and source lists).  Stepping
+// enqueues kernels on the stream given at creation and never synchronises the
+// host; no allocation happens after set-up, so a step sequence can be captured
+// into a CUDA graph.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "kernels.h"
+#include "setup.h"
+
+namespace sw4g {
+
+enum StepMode : int {
+   kModePhases = 0,  // reference phase order with dense Lu / F / Uacc arrays
+   kModeFused = 1,   // fused predictor and corrector stage kernels
+};
+
+class EW {
+ public:
+   EW(const GridSpec& g, cudaStream_t stream);
+   ~EW();
+   EW(const EW&) = delete;
+   EW& operator=(const EW&) = delete;
+
+   int init();  // allocates device memory; returns a Status
+   const GridSpec& grid() const { return g_; }
+   const Bounds& bounds() const { return b_; }
+   long long npts() const { return npts_; }
+   cudaStream_t stream() const { return stream_; }
+
+   // Material (rho, mu, lambda) over the full array (ghosts included), host or device.
+   int set_material(const double* rho, const double* mu, const double* la, bool on_device);
+   // Sources: discretised on the host, uploaded before the next step.
+   int add_source(const SourceSpec& s);
+   int add_grid_point_sources(int n, const int* ijk, const double* amp, const double* freq,
+                              const double* t0, const int* kind);
+   int clear_sources();
+   int num_grid_point_sources() const { return (int)hsrc_.size(); }
+   // Time step: explicit dt, or computed from the CFL number and an end time.
+   int set_time_step(double dt, double t0);
+   int compute_time_step(double cfl, double tmax, double* dt, int* nsteps);
+   double time() const { return t_; }
+   double dt() const { return dt_; }
+
+   // Solution levels U (current) and Um (previous), 3*npts doubles each.
+   int set_fields(const double* u, const double* um, bool on_device);
+   int get_fields(double* u, double* um, bool on_device) const;
+   double* field_u() const { return lev_[iu_]; }
+   double* field_um() const { return lev_[ium_]; }
+
+   int step(int nsteps, int mode);
+   // Boundary conditions on an arbitrary 3-component device array of this grid.
+   int enforce_bc(double* u);
+
+   // Device pointers of set-up arrays (tests / bench)
+   const double* profile(int which, int axis) const;  // which: 0 dc, 1 str, 2 co
+   const double* weights(int slot) const { return w_.p[slot]; }
+   int launches_per_step(int mode) const;
+   // Average device time (ms, CUDA events on the EW stream) of each piece of a
+   // fused step, each launched nrep times on the current levels without advancing
+   // time: [0] predictor stage kernel, [1] corrector stage kernel, [2] one-sided
+   // rows of both stages, [3] boundary conditions + forcing of both stages.
+   int profile_kernels(int nrep, double ms[4]);
+
+ private:
+   int upload_sources();
+   int step_phases();
+   int step_fused();
+   int fused_piece(int piece, int ip, int iq);
+   int ensure_phase_arrays();
+
+   GridSpec g_;
+   Bounds b_{};
+   cudaStream_t stream_ = nullptr;
+   long long npts_ = 0;
+   bool ready_ = false, material_ = false;
+   int wind_[36] = {}, bcpts_[6] = {}, onesided_[6] = {};
+   double sbop_[5] = {};
+   SupergridProfiles prof_;
+
+   double* rho_ = nullptr;
+   double* mu_ = nullptr;
+   double* la_ = nullptr;
+   double* irho_ = nullptr;
+   double* dprof_[9] = {};  // dc x,y,z ; str x,y,z ; co x,y,z
+   WeightPtrs w_{};
+   double* wstore_ = nullptr;
+   double* lev_[4] = {};
+   int iu_ = 0, ium_ = 1;
+   double* lu_ = nullptr;   // phase mode work arrays
+   double* f_ = nullptr;
+   double* uacc_ = nullptr;
+   double* slab_ = nullptr; // corrector stage field on the one-sided rows
+   long long slab_len_ = 0;
+
+   std::vector<GridPointSource> hsrc_;
+   bool src_dirty_ = true;
+   SourceSet dsrc_{};
+   void* dsrc_mem_ = nullptr;
+
+   double t_ = 0, dt_ = 0;
+};
+
+}  // namespace sw4g

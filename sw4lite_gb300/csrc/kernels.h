@@ -1,0 +1,106 @@
+// Host-side launchers of the sm_103a kernels.  Every launcher enqueues on the
+// given stream, allocates nothing and returns a Status code (common.cuh).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace sw4g {
+
+// Precomputed second-difference weights: slot axis*4 + type*2 + n, with type 0
+// for mu*s and 1 for (2mu+lambda)*s, n 0 for W1 and 1 for W2 (stage_fused.cu).
+constexpr int kWeightArrays = 12;
+struct WeightPtrs {
+   double* p[kWeightArrays];
+};
+
+// One fused stage launch over the centred rows [k1,k2] of a SoA grid.
+struct FusedStage {
+   Box b;
+   int k1 = 0, k2 = -1;
+   int corrector = 0;
+   int kchunk = 0;  // planes per CTA; 0 picks one
+   const double* u = nullptr;
+   const double* um = nullptr;
+   const double* up = nullptr;
+   double* out = nullptr;
+   const double* mu = nullptr;
+   const double* la = nullptr;
+   const double* rho = nullptr;
+   const double* irho = nullptr;
+   WeightPtrs w{};
+   const double* st[3] = {nullptr, nullptr, nullptr};
+   const double* dc[3] = {nullptr, nullptr, nullptr};
+   const double* co[3] = {nullptr, nullptr, nullptr};
+   double h = 1, dt = 0, beta = 0;
+};
+
+// Device-resident grid-point sources grouped by grid point: the sources of point
+// r are [start[r], start[r+1]); all share ijk[3*start[r] .. +2].
+struct SourceSet {
+   int npoints = 0;
+   int nsources = 0;
+   const int* start = nullptr;   // npoints+1
+   const int* ijk = nullptr;     // 3*nsources
+   const double* amp = nullptr;  // 3*nsources
+   const double* freq = nullptr; // nsources
+   const double* t0 = nullptr;   // nsources
+   const int* kind = nullptr;    // nsources
+};
+
+__host__ __device__ double timefunc(int kind, double freq, double t, bool tt);
+
+int upload_sbp_tables_direct();
+
+int launch_rhs4sg_direct(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst,
+                         int klast, int nk, const int onesided[6], double* lu, const double* u,
+                         const double* mu, const double* la, double h, const double* strx,
+                         const double* stry, const double* strz, cudaStream_t stream);
+
+int launch_predfort(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
+                    const double* u, const double* um, const double* lu, const double* fo,
+                    const double* rho, double dt2, cudaStream_t s);
+int launch_corrfort(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
+                    const double* lu, const double* fo, const double* rho, double dt4,
+                    cudaStream_t s);
+int launch_dpdmtfort(int ib, int ie, int jb, int je, int kb, int ke, const double* up,
+                     const double* u, const double* um, double* u2, double dt2i, cudaStream_t s);
+int launch_addsgd(int order, int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst,
+                  int klast, double* up, const double* u, const double* um, const double* rho,
+                  const double* dcx, const double* dcy, const double* dcz, const double* strx,
+                  const double* stry, const double* strz, const double* cox, const double* coy,
+                  const double* coz, double beta, cudaStream_t s);
+
+int launch_bcfortsg(int soa, int ib, int ie, int jb, int je, int kb, int ke, const int wind[36],
+                    int nx, int ny, int nz, double* u, double h, const int bccnd[6],
+                    const double sbop[5], const double* mu, const double* la,
+                    const double* const bforce[6], const double* strx, const double* stry,
+                    cudaStream_t s);
+
+int launch_force_dense(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* f,
+                       const SourceSet& src, double t, int tt, cudaStream_t s);
+int launch_force_update(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
+                        const double* rho, const SourceSet& src, double t, int tt, double coef,
+                        cudaStream_t s);
+int launch_force_update_f32(int soa, int ib, int ie, int jb, int je, int kb, int ke, float* up,
+                            const double* rho, const SourceSet& src, double t, int tt,
+                            double coef, cudaStream_t s);
+
+int fma_peak(int precision, double* tflops, cudaStream_t s);
+
+int launch_weights(const Box& b, const double* mu, const double* la, const double* sx,
+                   const double* sy, const double* sz, double h, WeightPtrs w, cudaStream_t s);
+int launch_inverse(long long n, const double* x, double* y, cudaStream_t s);
+int launch_uacc_slab(const Box& b, int k0, int k1, const double* up, const double* u,
+                     const double* um, double* out, cudaStream_t s);
+int launch_fused_stage(const FusedStage& st, cudaStream_t stream);
+int launch_stage_rows(int corrector, bool top, const Box& b, int nk, const double* field,
+                      const Box& field_box, const double* mu, const double* la, double h,
+                      const double* strx, const double* stry, const double* strz,
+                      const double* u, const double* um, const double* up, double* out,
+                      const double* rho, const double* irho, double coef, double beta,
+                      const double* const dc[3], const double* const st[3],
+                      const double* const co[3], cudaStream_t stream);
+
+}  // namespace sw4g

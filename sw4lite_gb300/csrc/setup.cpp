@@ -1,0 +1,309 @@
+// Host-side set-up for one Cartesian grid; see setup.h.
+#include "setup.h"
+
+#include <algorithm>
+#include <cmath>
+#include <tuple>
+
+namespace sw4g {
+
+Bounds grid_bounds(const GridSpec& g)
+{
+   return Bounds{-1, g.nx + 2, -1, g.ny + 2, -1, g.nz + 2};
+}
+
+namespace {
+
+// C5 smooth step of the supergrid taper (src/SuperGrid.C:148-176): 0 for xi<=0,
+// 1 for xi>=1.  Evaluated as monomials in the same order as the reference: near
+// xi=1 the polynomial cancels to ~1 and the stretching 1-(1-epsL)psi cancels
+// again, so the evaluation order shows in dc = psi/phi at the 1e-9 level.
+double psi0(double xi)
+{
+   if (xi <= 0.) return 0;
+   if (xi >= 1.) return 1.0;
+   return xi * xi * xi * xi * xi * xi *
+          (462 - 1980 * xi + 3465 * xi * xi - 3080 * xi * xi * xi + 1386 * xi * xi * xi * xi -
+           252 * xi * xi * xi * xi * xi);
+}
+
+struct Taper {
+   bool left = false, right = false;
+   double x0 = 0, x1 = 1, width = 0.1, trans = 0.05;
+   static constexpr double epsL = 1e-4;
+
+   double psi_aux(double x) const
+   {
+      if (left && x < x0 + width) return psi0((x0 + width - x) / width);
+      if (right && x > x1 - width) return psi0((x - (x1 - width)) / width);
+      return 0;
+   }
+   double psi_damp(double x) const
+   {
+      if (left && x < x0 + width) return psi0((x0 + width - x) / trans);
+      if (right && x > x1 - width) return psi0((x - (x1 - width)) / trans);
+      return 0;
+   }
+   double lin(double x) const
+   {
+      if (left && x < x0 + width) return (x0 + width - x) / width;
+      if (right && x > x1 - width) return (x - (x1 - width)) / width;
+      return 0;
+   }
+   double stretching(double x) const { return 1 - (1 - epsL) * psi_aux(x); }
+   double damping(double x) const { return psi_damp(x) / stretching(x); }
+   double corner(double x) const { return 1.0 - (1.0 - 0.33) * lin(x); }
+};
+
+Taper make_taper(bool left, double x0, bool right, double x1, double width)
+{
+   Taper t;
+   t.left = left;
+   t.right = right;
+   t.x0 = x0;
+   t.x1 = x1;
+   t.width = width;
+   t.trans = 0.5 * width;
+   return t;
+}
+
+}  // namespace
+
+SupergridProfiles supergrid_profiles(const GridSpec& g)
+{
+   SupergridProfiles p;
+   const Bounds b = grid_bounds(g);
+   const int first[3] = {b.ib, b.jb, b.kb}, last[3] = {b.ie, b.je, b.ke};
+   for (int s = 0; s < 6; s++)
+      if (g.bc[s] == kSuperGrid) p.used = true;
+   const double width = g.sg_gp * g.h;
+   const double xmax = (g.nx - 1) * g.h, ymax = (g.ny - 1) * g.h, zmax = g.zmin + (g.nz - 1) * g.h;
+   Taper t[3];
+   t[0] = make_taper(g.bc[0] == kSuperGrid, 0.0, g.bc[1] == kSuperGrid, xmax, width);
+   t[1] = make_taper(g.bc[2] == kSuperGrid, 0.0, g.bc[3] == kSuperGrid, ymax, width);
+   // Single Cartesian grid: the z taper starts at 0 as the reference's
+   // define_taper(..., 0.0, ..., m_global_zmax, ...) (src/EW.C:4655-4658).
+   t[2] = make_taper(g.bc[4] == kSuperGrid, 0.0, g.bc[5] == kSuperGrid, zmax, width);
+   for (int ax = 0; ax < 3; ax++) {
+      const int n = last[ax] - first[ax] + 1;
+      p.dc[ax].resize(n);
+      p.str[ax].resize(n);
+      p.co[ax].resize(n);
+      for (int q = first[ax]; q <= last[ax]; q++) {
+         const double x = (ax == 2 ? g.zmin : 0.0) + (q - 1) * g.h;
+         if (p.used) {
+            p.dc[ax][q - first[ax]] = t[ax].damping(x);
+            p.str[ax][q - first[ax]] = t[ax].stretching(x);
+            p.co[ax][q - first[ax]] = t[ax].corner(x);
+         } else {
+            p.dc[ax][q - first[ax]] = 0;
+            p.str[ax][q - first[ax]] = 1;
+            p.co[ax][q - first[ax]] = 1;
+         }
+      }
+   }
+   return p;
+}
+
+void boundary_windows(const GridSpec& g, int wind[36], int npts[6])
+{
+   const Bounds b = grid_bounds(g);
+   const int ng = 2;
+   for (int s = 0; s < 6; s++) {
+      npts[s] = 0;
+      for (int q = 0; q < 6; q++) wind[6 * s + q] = (q % 2 == 0) ? 999 : -999;
+      const int t = g.bc[s];
+      if (!(t == kStressFree || t == kDirichlet || t == kSuperGrid || t == kPeriodic)) continue;
+      int w[6] = {b.ib, b.ie, b.jb, b.je, b.kb, b.ke};
+      const int layers = t == kStressFree ? 1 : ng;
+      const int lo = 2 * (s / 2), hi = lo + 1;  // index pair of the side's axis in w
+      if (s % 2 == 0) w[hi] = w[lo] + layers - 1;
+      else w[lo] = w[hi] - (layers - 1);
+      if (t == kStressFree) {
+         // the boundary plane itself, just inside the ghost points
+         if (s % 2 == 0) w[lo] += ng;
+         else w[lo] -= ng;
+         w[hi] = w[lo];
+      }
+      for (int q = 0; q < 6; q++) wind[6 * s + q] = w[q];
+      npts[s] = (w[5] - w[4] + 1) * (w[3] - w[2] + 1) * (w[1] - w[0] + 1);
+   }
+}
+
+void onesided_flags(const GridSpec& g, int onesided[6])
+{
+   for (int s = 0; s < 6; s++) onesided[s] = 0;
+   // one grid: only a free surface (stress-free) side uses the SBP closure
+   onesided[4] = g.bc[4] == kStressFree;
+   onesided[5] = g.bc[5] == kStressFree;
+}
+
+double cfl_time_step(const GridSpec& g, const double* rho, const double* mu, const double* la,
+                     double cfl, double tstart, double tmax, int* nsteps)
+{
+   const long long n = grid_bounds(g).npts();
+   double eigmax = -1;
+   for (long long p = 0; p < n; p++) {
+      const double e = (4 * mu[p] + la[p]) / rho[p];
+      eigmax = e > eigmax ? e : eigmax;
+   }
+   double dt = cfl * g.h * (1 / std::sqrt(eigmax));
+   int ns = static_cast<int>((tmax - tstart) / dt + 0.5);
+   ns = ns == 0 ? 1 : ns;
+   dt = (tmax - tstart) / ns;
+   if (nsteps) *nsteps = ns;
+   return dt;
+}
+
+namespace {
+
+// 6-point delta weights at offsets -2..3 for a source at fractional position a
+// (moments 0..4 exact), src/Source.C:553-584.
+void delta_weights(double a, double w[6])
+{
+   const double a2 = a * a, a3 = a2 * a, a4 = a3 * a, a5 = a4 * a;
+   const double p5 = a5 * (5.0 / 3 - 7.0 / 24 * a - 17 / 12.0 * a2 + 1.125 * a3 - 0.25 * a4);
+   w[0] = 1.0 / 24 * (2 * a - a2 - 2 * a3 - 19 * a4) + p5;
+   w[1] = 1.0 / 6 * (-4 * a + 4 * a2 + a3) + 4 * a4 - 5 * p5;
+   w[2] = 1 - 1.25 * a2 - 97.0 / 12 * a4 + 10 * p5;
+   w[3] = 1.0 / 6 * (4 * a + 4 * a2 - a3 + 49 * a4) - 10 * p5;
+   w[4] = 1.0 / 24 * (-2 * a - a2 + 2 * a3) - 4.125 * a4 + 5 * p5;
+   w[5] = 5.0 / 6 * a4 - p5;
+}
+
+// 6-point delta' weights, src/Source.C:587-619.
+void ddelta_weights(double a, double w[6])
+{
+   const double a2 = a * a, a3 = a2 * a, a4 = a3 * a;
+   const double p5 = a4 * (-25.0 / 12 - 0.75 * a + 59.0 / 12 * a2 - 4 * a3 + a4);
+   w[0] = 1.0 / 12 * (-1 + a + 3 * a2 + 8 * a3) + p5;
+   w[1] = 2.0 / 3 * (1 - 2 * a) - 0.5 * a2 - 3.5 * a3 - 5 * p5;
+   w[2] = 2.5 * a + 22.0 / 3 * a3 + 10 * p5;
+   w[3] = 2.0 / 3 * (-1 - 2 * a) + 0.5 * a2 - 23.0 / 3 * a3 - 10 * p5;
+   w[4] = (1 + a) / 12 - 0.25 * a2 + 4 * a3 + 5 * p5;
+   w[5] = -5.0 / 6 * a3 - p5;
+}
+
+// Five-point variants used next to the free surface when the source lies above
+// the third grid plane (src/Source.C:622-679).
+void delta_weights_low(double a, double w[6])
+{
+   const double a2 = a * a, a3 = a2 * a, a4 = a3 * a;
+   w[0] = (2 * a - a2 - 2 * a3 + a4) / 24;
+   w[1] = (-4 * a + 4 * a2 + a3 - a4) / 6;
+   w[2] = 1 - 1.25 * a2 + 0.25 * a4;
+   w[3] = (4 * a + 4 * a2 - a3 - a4) / 6;
+   w[4] = (-2 * a - a2 + 2 * a3 + a4) / 24;
+   w[5] = 0;
+}
+
+void ddelta_weights_low(double a, double w[6])
+{
+   const double a2 = a * a, a3 = a2 * a;
+   w[0] = (-1 + a + 3 * a2 - 2 * a3) / 12;
+   w[1] = (2 - 4 * a - 1.5 * a2 + 2 * a3) / 3;
+   w[2] = 2.5 * a - a3;
+   w[3] = (-2 - 4 * a + 1.5 * a2 + 2 * a3) / 3;
+   w[4] = (1 + a - 3 * a2 - 2 * a3) / 12;
+   w[5] = 0;
+}
+
+}  // namespace
+
+void discretize_source(const GridSpec& g, const int onesided[6], const SourceSpec& s,
+                       std::vector<GridPointSource>& out)
+{
+   const double h = g.h;
+   const int Ni = g.nx, Nj = g.ny, Nz = g.nz;
+   // mapped coordinates (src/EW.C:5722-5735, Cartesian)
+   const double q0 = s.x / h + 1, r0 = s.y / h + 1, s0 = (s.z - g.zmin) / h + 1;
+   int ic = static_cast<int>(std::floor(q0));
+   int jc = static_cast<int>(std::floor(r0));
+   int kc = static_cast<int>(std::floor(s0));
+   // keep the 6-point stencil away from the ghost points (src/Source.C:1145-1183)
+   if (ic <= 2) ic = 3;
+   if (ic >= Ni - 2) ic = Ni - 3;
+   if (jc <= 2) jc = 3;
+   if (jc >= Nj - 2) jc = Nj - 3;
+   if (kc >= Nz) kc = Nz - 1;
+   if (kc < 1) kc = 1;
+   if (kc <= 2) kc = 3;
+   if (kc >= Nz - 2) kc = Nz - 3;
+   const double ai = q0 - ic, bi = r0 - jc, ci = s0 - kc;
+
+   double wi[6], wj[6], wk[6], dwi[6], dwj[6], dwk[6];
+   delta_weights(ai, wi);
+   delta_weights(bi, wj);
+   delta_weights(ci, wk);
+   ddelta_weights(ai, dwi);
+   ddelta_weights(bi, dwj);
+   ddelta_weights(ci, dwk);
+   if (kc == 3 && ci <= 0) {
+      delta_weights_low(ci, wk);
+      ddelta_weights_low(ci, dwk);
+   }
+   // SBP quadrature normalisation of the weights on the first/last 4 planes
+   // (src/Source.C:1437-1468)
+   const double normwgh[4] = {17.0 / 48.0, 59.0 / 48.0, 43.0 / 48.0, 49.0 / 48.0};
+   if (onesided[4]) {
+      for (int k = 0; k <= 5; k++)
+         if (1 <= k + kc - 2 && k + kc - 2 <= 4) {
+            wk[k] /= normwgh[k + kc - 3];
+            dwk[k] /= normwgh[k + kc - 3];
+         }
+   }
+   if (onesided[5]) {
+      for (int k = 0; k <= 5; k++)
+         if (Nz - 3 <= k + kc - 2 && k + kc - 2 <= Nz) {
+            wk[k] /= normwgh[Nz - k - kc + 2];
+            dwk[k] /= normwgh[Nz - k - kc + 2];
+         }
+   }
+   const double ih3 = 1.0 / (h * h * h);
+   for (int k = kc - 2; k <= kc + 3; k++)
+      for (int j = jc - 2; j <= jc + 3; j++)
+         for (int i = ic - 2; i <= ic + 3; i++) {
+            if (!(1 <= i && i <= Ni && 1 <= j && j <= Nj)) continue;
+            if (!(1 <= k && k <= Nz)) continue;
+            GridPointSource p;
+            p.i = i;
+            p.j = j;
+            p.k = k;
+            p.freq = s.freq;
+            p.t0 = s.t0;
+            p.kind = s.kind;
+            if (!s.moment) {
+               // point force (src/Source.C:1479-1500)
+               double wF = wi[i - ic + 2] * wj[j - jc + 2] * wk[k - kc + 2];
+               if (wF == 0 || (s.f[0] == 0 && s.f[1] == 0 && s.f[2] == 0)) continue;
+               wF *= ih3;
+               for (int c = 0; c < 3; c++) p.amp[c] = wF * s.f[c];
+            } else {
+               // moment tensor: F = -M grad(delta) (src/Source.C:1710-1930, Cartesian metric)
+               const double hi = 1.0 / h;
+               const double wFx = hi * dwi[i - ic + 2] * wj[j - jc + 2] * wk[k - kc + 2];
+               const double wFy = wi[i - ic + 2] * hi * dwj[j - jc + 2] * wk[k - kc + 2];
+               const double wFz = wi[i - ic + 2] * wj[j - jc + 2] * hi * dwk[k - kc + 2];
+               const double* M = s.m;  // xx, xy, xz, yy, yz, zz
+               p.amp[0] = -(M[0] * wFx + M[1] * wFy + M[2] * wFz) * ih3;
+               p.amp[1] = -(M[1] * wFx + M[3] * wFy + M[4] * wFz) * ih3;
+               p.amp[2] = -(M[2] * wFx + M[4] * wFy + M[5] * wFz) * ih3;
+            }
+            out.push_back(p);
+         }
+}
+
+void group_sources(std::vector<GridPointSource>& src, std::vector<int>& start)
+{
+   auto key = [](const GridPointSource& a) {
+      return std::make_tuple(a.k, a.j, a.i);
+   };
+   std::stable_sort(src.begin(), src.end(),
+                    [&](const GridPointSource& a, const GridPointSource& b) { return key(a) < key(b); });
+   start.clear();
+   start.push_back(0);
+   for (size_t s = 1; s <= src.size(); s++)
+      if (s == src.size() || key(src[s]) != key(src[s - 1])) start.push_back((int)s);
+}
+
+}  // namespace sw4g

@@ -1,0 +1,78 @@
+// Host-side set-up of one Cartesian grid for the elastic time step: supergrid
+// profiles, boundary windows, one-sided flags, the CFL time step, and the
+// discretisation of point sources into grid-point sources.  Everything here runs
+// once before time stepping and is O(N^2) or less.
+#pragma once
+
+#include <vector>
+
+namespace sw4g {
+
+// Boundary condition kinds, numbered as the reference's boundaryConditionType
+// (src/double/sw4.h:38).
+enum Bc : int { kStressFree = 0, kDirichlet = 1, kSuperGrid = 2, kPeriodic = 3, kNone = 8 };
+
+struct GridSpec {
+   int nx = 0, ny = 0, nz = 0;  // interior points per axis
+   double h = 0;                // grid spacing
+   double zmin = 0;             // z of the first interior plane
+   int bc[6] = {kSuperGrid, kSuperGrid, kSuperGrid, kSuperGrid, kStressFree, kSuperGrid};
+   int sg_gp = 20;              // supergrid layer width in grid points (src/EW.C:176)
+   double sg_damping = 0.02;    // supergrid damping coefficient (src/EW.C:174)
+   int sg_order = 4;            // 4 or 6 (src/EW.C:1288-1305)
+   int soa = 1;                 // component layout: 1 SoA (corder=1), 0 AoS
+};
+
+// Array bounds of the grid: 2 ghost points per side.
+struct Bounds {
+   int ib, ie, jb, je, kb, ke;
+   long long npts() const { return (long long)(ie - ib + 1) * (je - jb + 1) * (ke - kb + 1); }
+};
+Bounds grid_bounds(const GridSpec& g);
+
+// 1-D supergrid coefficient profiles (damping dc, stretching str, corner taper co)
+// along each axis, sampled at every array index (src/EW.C:4636-4803, src/SuperGrid.C).
+struct SupergridProfiles {
+   std::vector<double> dc[3], str[3], co[3];
+   bool used = false;
+};
+SupergridProfiles supergrid_profiles(const GridSpec& g);
+
+// Boundary windows and point counts per side (src/EW.C:3347-3444) and the
+// one-sided flags of the top/bottom sides (src/EW.C:4863-4868).
+void boundary_windows(const GridSpec& g, int wind[36], int npts[6]);
+void onesided_flags(const GridSpec& g, int onesided[6]);
+
+// dt = cfl * h / sqrt(max((4 mu + lambda)/rho)) over all array points, then
+// adjusted to land on tmax (src/EW.C:5041-5146).  Returns dt; nsteps out.
+double cfl_time_step(const GridSpec& g, const double* rho, const double* mu, const double* la,
+                     double cfl, double tstart, double tmax, int* nsteps);
+
+// One source: either a point force (fx,fy,fz) or a moment tensor (mxx..mzz).
+struct SourceSpec {
+   double x = 0, y = 0, z = 0;
+   bool moment = false;
+   double f[3] = {0, 0, 0};                  // fx, fy, fz
+   double m[6] = {0, 0, 0, 0, 0, 0};         // mxx, mxy, mxz, myy, myz, mzz
+   double freq = 1, t0 = 0;
+   int kind = 0;                             // timefunc kind (forcing.cu)
+};
+
+struct GridPointSource {
+   int i, j, k;
+   double amp[3];
+   double freq, t0;
+   int kind;
+};
+
+// Cartesian single-grid source discretisation (src/Source.C:1074-1920):
+// 6-point moment-exact delta / delta' weights per axis with the SBP boundary
+// normalisation near one-sided boundaries.
+void discretize_source(const GridSpec& g, const int onesided[6], const SourceSpec& s,
+                       std::vector<GridPointSource>& out);
+
+// Sort grid-point sources by point and build the per-point groups
+// (src/EW.C:6370-6433).  start has npoints+1 entries.
+void group_sources(std::vector<GridPointSource>& src, std::vector<int>& start);
+
+}  // namespace sw4g

@@ -1,0 +1,555 @@
+// Fused stage kernels of the elastic time step on Cartesian grids, sm_103a, FP64.
+//
+// One launch computes, for every centred row k1..k2 of the interior,
+//   predictor stage  out = 2u - um + dt^2/rho * L(u)
+//   corrector stage  out = up + dt^2/12/rho * L(up - 2u + um) - beta/rho * SG(u - um)
+// where L is the divergence-of-stress operator of the reference's rhs4sg
+// (src/rhs4sg_rev.C:111-348) and SG its 4th-order supergrid damping
+// (src/ew-cfromfort.C:952-1057).  These replace the reference's GPU phase
+// sequence RHSPredCU_center / evalDpDmInTimeCU / RHSCorrCU_center /
+// addSuperGridDampingCU_center (src/EW_cuda.C:1228-1509): each input field
+// crosses HBM once per stage and no intermediate (Lu, Uacc, F) is written.
+//
+// Design for GB300's FP64 pipe, which bounds this kernel (~8 flop per byte):
+//  * CTA = 32 x 8 columns; the CTA marches up z through a 5-plane ring of the
+//    stage field (with a 2-point x/y halo) in shared memory.
+//  * The variable-coefficient second differences use per-point weights
+//    W1,W2 of mu*s and (2mu+lambda)*s that are precomputed once (material is
+//    time-invariant): no FP64 work is spent rebuilding them every stage.
+//  * Each mixed derivative (c f_b)_a is evaluated as an outer difference of a
+//    per-point product G = c * D_b f computed once per point: G for the x (y)
+//    outer difference is staged in shared memory over an x (y) halo, G for the
+//    z outer difference rides a per-thread register queue.  The reference
+//    recomputes the inner differences inside every outer term.
+//  * The corrector stage forms (up - 2u + um) and (u - um) while staging the
+//    plane; 1/dt^2 is folded into the update coefficient.
+#include <algorithm>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "stencil.cuh"
+
+namespace sw4g {
+namespace {
+
+constexpr int TX = 32, TY = 8, HALO = 2;
+constexpr int PX = TX + 2 * HALO;  // 36
+constexpr int PY = TY + 2 * HALO;  // 12
+constexpr int PLANE = PX * PY;     // 432
+constexpr int NTHREADS = TX * TY;
+
+struct FusedArgs {
+   int ib, ie, jb, je, kb, ke;
+   long long ni, nij, npts;
+   int k1, k2, kchunk;
+   const double* __restrict__ u;
+   const double* __restrict__ um;
+   const double* __restrict__ up;  // corrector input (predicted level)
+   double* __restrict__ out;
+   const double* __restrict__ mu;
+   const double* __restrict__ la;
+   const double* __restrict__ rho;
+   const double* __restrict__ irho;
+   const double* __restrict__ w[kWeightArrays];
+   const double* __restrict__ sx;
+   const double* __restrict__ sy;
+   const double* __restrict__ sz;
+   const double* __restrict__ dc[3];
+   const double* __restrict__ co[3];
+   double cof144;  // 1/(144 h^2)
+   double coef;    // dt^2 (predictor) or dt^2/12 (corrector)
+   double beta;    // supergrid damping coefficient (corrector)
+};
+
+__host__ __device__ constexpr int smem_doubles(int corr)
+{
+   // V ring (5 planes x 3) + [D ring (3 planes x 3) + RHO plane] + MU, LA planes + GX + GY
+   return 15 * PLANE + (corr ? 9 * PLANE + PLANE : 0) + 2 * PLANE + 3 * TY * PX + 3 * PY * TX;
+}
+
+__device__ __forceinline__ int mod5(int k) { return ((k % 5) + 5) % 5; }
+__device__ __forceinline__ int mod3(int k) { return ((k % 3) + 3) % 3; }
+
+template <int CORR>
+__global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
+{
+   extern __shared__ double sm[];
+   double* V = sm;                                   // [5 slots][3][PLANE]
+   double* Dd = V + 15 * PLANE;                      // [3 slots][3][PLANE]   (corrector)
+   double* RH = Dd + (CORR ? 9 * PLANE : 0);         // [PLANE]               (corrector)
+   double* MU = RH + (CORR ? PLANE : 0);             // [PLANE]
+   double* LA = MU + PLANE;                          // [PLANE]
+   double* GX = LA + PLANE;                          // [3][TY][PX]
+   double* GY = GX + 3 * TY * PX;                    // [3][PY][TX]
+
+   const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + TX * ty;
+   const int i0 = a.ib + 2 + blockIdx.x * TX;
+   const int j0 = a.jb + 2 + blockIdx.y * TY;
+   const int kbeg = a.k1 + blockIdx.z * a.kchunk;
+   if (kbeg > a.k2) return;
+   const int kend = min(kbeg + a.kchunk - 1, a.k2);
+   const int i = i0 + tx, j = j0 + ty;
+   const bool active = (i <= a.ie - 2) && (j <= a.je - 2);
+   const int own = (ty + HALO) * PX + (tx + HALO);
+   const long long npts = a.npts;
+
+   auto gidx = [&](int gi, int gj, int gk) -> long long {
+      return (long long)(gi - a.ib) + a.ni * (gj - a.jb) + a.nij * (long long)(gk - a.kb);
+   };
+
+   // Stage plane kk (with halo) of the stage field, and for the corrector the
+   // damping field u - um.  Points beyond the array edge are never read by an
+   // active column and are zero-filled.
+   auto load_plane = [&](int kk) {
+      double* vs = V + mod5(kk) * 3 * PLANE;
+      double* ds = Dd + mod3(kk) * 3 * PLANE;
+      for (int idx = tid; idx < PLANE; idx += NTHREADS) {
+         const int li = idx % PX, lj = idx / PX;
+         const int gi = i0 - HALO + li, gj = j0 - HALO + lj;
+         double v[3] = {0, 0, 0}, d[3] = {0, 0, 0};
+         if (gi <= a.ie && gj <= a.je) {
+            const long long p = gidx(gi, gj, kk);
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+               if (!CORR) {
+                  v[c] = __ldg(a.u + p + c * npts);
+               } else {
+                  const double uu = __ldg(a.u + p + c * npts), uum = __ldg(a.um + p + c * npts);
+                  v[c] = (__ldg(a.up + p + c * npts) - 2 * uu) + uum;
+                  d[c] = uu - uum;
+               }
+            }
+         }
+#pragma unroll
+         for (int c = 0; c < 3; c++) {
+            vs[c * PLANE + idx] = v[c];
+            if (CORR) ds[c * PLANE + idx] = d[c];
+         }
+      }
+   };
+
+   auto load_material = [&](int kk) {
+      for (int idx = tid; idx < PLANE; idx += NTHREADS) {
+         const int li = idx % PX, lj = idx / PX;
+         const int gi = i0 - HALO + li, gj = j0 - HALO + lj;
+         double m = 0, l = 0, r = 0;
+         if (gi <= a.ie && gj <= a.je) {
+            const long long p = gidx(gi, gj, kk);
+            m = __ldg(a.mu + p);
+            l = __ldg(a.la + p);
+            if (CORR) r = __ldg(a.rho + p);
+         }
+         MU[idx] = m;
+         LA[idx] = l;
+         if (CORR) RH[idx] = r;
+      }
+   };
+
+   // Own-column stretching factors
+   const double sxi = active ? __ldg(a.sx + (i - a.ib)) : 0.0;
+   const double syj = active ? __ldg(a.sy + (j - a.jb)) : 0.0;
+
+   // z-outer products G_z at plane kk for the own column: components for
+   // (mu w_x)_z, (mu w_y)_z and (lambda (u_x, v_y))_z.
+   auto compute_gz = [&](int kk, double g[3]) {
+      const double* vs = V + mod5(kk) * 3 * PLANE;
+      const double* vu = vs;
+      const double* vv = vs + PLANE;
+      const double* vw = vs + 2 * PLANE;
+      const double dxw = d1c(vw[own - 2], vw[own - 1], vw[own + 1], vw[own + 2]);
+      const double dyw = d1c(vw[own - 2 * PX], vw[own - PX], vw[own + PX], vw[own + 2 * PX]);
+      const double dxu = d1c(vu[own - 2], vu[own - 1], vu[own + 1], vu[own + 2]);
+      const double dyv = d1c(vv[own - 2 * PX], vv[own - PX], vv[own + PX], vv[own + 2 * PX]);
+      const long long p = gidx(i, j, kk);
+      const double m = __ldg(a.mu + p), l = __ldg(a.la + p);
+      g[0] = m * sxi * dxw;
+      g[1] = m * syj * dyw;
+      g[2] = l * (sxi * dxu + syj * dyv);
+   };
+
+   double gz[5][3];   // G_z at planes k-2..k+2
+   double dq[5][3];   // (u - um) own column at planes k-2..k+2 (corrector)
+
+   // ---- prologue: planes kbeg-2 .. kbeg+1 ----
+   for (int kk = kbeg - 2; kk <= kbeg; kk++) load_plane(kk);
+   __syncthreads();
+   for (int kk = kbeg - 2; kk <= kbeg; kk++) {
+      const int q = kk - kbeg + 3;  // 1..3
+      if (active) compute_gz(kk, gz[q]);
+      if (CORR) {
+         const double* ds = Dd + mod3(kk) * 3 * PLANE;
+#pragma unroll
+         for (int c = 0; c < 3; c++) dq[q][c] = ds[c * PLANE + own];
+      }
+   }
+   __syncthreads();
+   load_plane(kbeg + 1);
+   __syncthreads();
+   if (active) compute_gz(kbeg + 1, gz[4]);
+   if (CORR) {
+      const double* ds = Dd + mod3(kbeg + 1) * 3 * PLANE;
+#pragma unroll
+      for (int c = 0; c < 3; c++) dq[4][c] = ds[c * PLANE + own];
+   }
+
+   for (int k = kbeg; k <= kend; k++) {
+      load_plane(k + 2);
+      load_material(k);
+      __syncthreads();
+
+      // shift the register queues and append plane k+2
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+#pragma unroll
+         for (int c = 0; c < 3; c++) {
+            gz[q][c] = gz[q + 1][c];
+            if (CORR) dq[q][c] = dq[q + 1][c];
+         }
+      if (active) compute_gz(k + 2, gz[4]);
+      if (CORR) {
+         const double* ds = Dd + mod3(k + 2) * 3 * PLANE;
+#pragma unroll
+         for (int c = 0; c < 3; c++) dq[4][c] = ds[c * PLANE + own];
+      }
+
+      const double szk = __ldg(a.sz + (k - a.kb));
+      const double* vm2 = V + mod5(k - 2) * 3 * PLANE;
+      const double* vm1 = V + mod5(k - 1) * 3 * PLANE;
+      const double* v0 = V + mod5(k) * 3 * PLANE;
+      const double* vp1 = V + mod5(k + 1) * 3 * PLANE;
+      const double* vp2 = V + mod5(k + 2) * 3 * PLANE;
+      auto dz = [&](int c, int idx) {
+         return d1c(vm2[c * PLANE + idx], vm1[c * PLANE + idx], vp1[c * PLANE + idx],
+                    vp2[c * PLANE + idx]);
+      };
+
+      // x-outer products over the x-extended rows (all 36 columns, own 8 rows):
+      //   G_x = { la (s_y v_y + s_z w_z),  mu s_y u_y,  mu s_z u_z }
+      for (int idx = tid; idx < TY * PX; idx += NTHREADS) {
+         const int li = idx % PX, ljr = idx / PX;
+         const int s = (ljr + HALO) * PX + li;
+         const int gi = i0 - HALO + li, gj = j0 + ljr;
+         double g0 = 0, g1 = 0, g2 = 0;
+         if (gi <= a.ie && gj <= a.je) {
+            const double syy = __ldg(a.sy + (gj - a.jb));
+            const double* vu = v0;
+            const double* vv = v0 + PLANE;
+            const double dyv = d1c(vv[s - 2 * PX], vv[s - PX], vv[s + PX], vv[s + 2 * PX]);
+            const double dyu = d1c(vu[s - 2 * PX], vu[s - PX], vu[s + PX], vu[s + 2 * PX]);
+            const double dzw = dz(2, s), dzu = dz(0, s);
+            const double m = MU[s], l = LA[s];
+            g0 = l * (syy * dyv + szk * dzw);
+            g1 = m * syy * dyu;
+            g2 = m * szk * dzu;
+         }
+         GX[0 * TY * PX + idx] = g0;
+         GX[1 * TY * PX + idx] = g1;
+         GX[2 * TY * PX + idx] = g2;
+      }
+      // y-outer products over the y-extended columns (own 32 columns, all 12 rows):
+      //   G_y = { mu s_x v_x,  la (s_x u_x + s_z w_z),  mu s_z v_z }
+      for (int idx = tid; idx < PY * TX; idx += NTHREADS) {
+         const int lic = idx % TX, lj = idx / TX;
+         const int s = lj * PX + lic + HALO;
+         const int gi = i0 + lic, gj = j0 - HALO + lj;
+         double g0 = 0, g1 = 0, g2 = 0;
+         if (gi <= a.ie && gj <= a.je) {
+            const double sxx = __ldg(a.sx + (gi - a.ib));
+            const double* vu = v0;
+            const double* vv = v0 + PLANE;
+            const double dxv = d1c(vv[s - 2], vv[s - 1], vv[s + 1], vv[s + 2]);
+            const double dxu = d1c(vu[s - 2], vu[s - 1], vu[s + 1], vu[s + 2]);
+            const double dzw = dz(2, s), dzv = dz(1, s);
+            const double m = MU[s], l = LA[s];
+            g0 = m * sxx * dxv;
+            g1 = l * (sxx * dxu + szk * dzw);
+            g2 = m * szk * dzv;
+         }
+         GY[0 * PY * TX + idx] = g0;
+         GY[1 * PY * TX + idx] = g1;
+         GY[2 * PY * TX + idx] = g2;
+      }
+      __syncthreads();
+
+      if (active) {
+         const long long p = gidx(i, j, k);
+         double lu[3];
+         // variable-coefficient second differences with precomputed weights
+         {
+            const long long off[3] = {1, a.ni, a.nij};
+            const double sc[3] = {sxi, syj, szk};
+            double acc[3] = {0, 0, 0};
+#pragma unroll
+            for (int ax = 0; ax < 3; ax++) {
+               const long long o = off[ax];
+               double wt[2][4];
+#pragma unroll
+               for (int t = 0; t < 2; t++) {
+                  const double* w1 = a.w[ax * 4 + t * 2 + 0];
+                  const double* w2 = a.w[ax * 4 + t * 2 + 1];
+                  wt[t][0] = __ldg(w1 + p);
+                  wt[t][1] = __ldg(w2 + p);
+                  wt[t][2] = __ldg(w2 + p + o);
+                  wt[t][3] = __ldg(w1 + p + 2 * o);
+               }
+#pragma unroll
+               for (int c = 0; c < 3; c++) {
+                  double f[5];
+                  if (ax == 0) {
+#pragma unroll
+                     for (int m = -2; m <= 2; m++) f[m + 2] = v0[c * PLANE + own + m];
+                  } else if (ax == 1) {
+#pragma unroll
+                     for (int m = -2; m <= 2; m++) f[m + 2] = v0[c * PLANE + own + m * PX];
+                  } else {
+                     f[0] = vm2[c * PLANE + own];
+                     f[1] = vm1[c * PLANE + own];
+                     f[2] = v0[c * PLANE + own];
+                     f[3] = vp1[c * PLANE + own];
+                     f[4] = vp2[c * PLANE + own];
+                  }
+                  const double* wv = wt[ax == c ? 1 : 0];
+                  const double s = wv[0] * (f[0] - f[2]) + wv[1] * (f[1] - f[2]) +
+                                   wv[2] * (f[3] - f[2]) + wv[3] * (f[4] - f[2]);
+                  acc[c] += sc[ax] * s;
+               }
+            }
+            // mixed terms: outer differences of the staged products
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+               const double* gx = GX + c * TY * PX + ty * PX + tx;  // li = tx .. tx+4
+               const double* gy = GY + c * PY * TX + ty * TX + tx;  // lj = ty .. ty+4
+               const double cx = d1c(gx[0], gx[1], gx[3], gx[4]);
+               const double cy = d1c(gy[0], gy[TX], gy[3 * TX], gy[4 * TX]);
+               const double cz = d1c(gz[0][c], gz[1][c], gz[3][c], gz[4][c]);
+               lu[c] = acc[c] + a.cof144 * (sxi * cx + syj * cy + szk * cz);
+            }
+         }
+         const double ir = __ldg(a.irho + p);
+         const double cr = a.coef * ir;
+         if (!CORR) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+               const long long q = p + c * npts;
+               a.out[q] = 2 * v0[c * PLANE + own] - __ldg(a.um + q) + cr * lu[c];
+            }
+         } else {
+            double sg[3] = {0, 0, 0};
+            if (a.beta != 0) {
+               const double* ds = Dd + mod3(k) * 3 * PLANE;
+               const double cxi = __ldg(a.co[0] + (i - a.ib));
+               const double cyj = __ldg(a.co[1] + (j - a.jb));
+               const double czk = __ldg(a.co[2] + (k - a.kb));
+               // x: e = rho*dc at i-1..i+1 (skipped where dc vanishes: the term is exactly 0)
+               const double dx0 = __ldg(a.dc[0] + (i - 1 - a.ib)), dx1 = __ldg(a.dc[0] + (i - a.ib)),
+                            dx2 = __ldg(a.dc[0] + (i + 1 - a.ib));
+               if (dx0 != 0 || dx1 != 0 || dx2 != 0) {
+                  const double e0 = RH[own - 1] * dx0, e1 = RH[own] * dx1, e2 = RH[own + 1] * dx2;
+                  const double wx = sxi * cyj * czk;
+#pragma unroll
+                  for (int c = 0; c < 3; c++) {
+                     const double* d = ds + c * PLANE + own;
+                     const double s = e2 * (d[2] - 2 * d[1] + d[0]) - 2 * e1 * (d[1] - 2 * d[0] + d[-1]) +
+                                      e0 * (d[0] - 2 * d[-1] + d[-2]);
+                     sg[c] += wx * s;
+                  }
+               }
+               const double dy0 = __ldg(a.dc[1] + (j - 1 - a.jb)), dy1 = __ldg(a.dc[1] + (j - a.jb)),
+                            dy2 = __ldg(a.dc[1] + (j + 1 - a.jb));
+               if (dy0 != 0 || dy1 != 0 || dy2 != 0) {
+                  const double e0 = RH[own - PX] * dy0, e1 = RH[own] * dy1, e2 = RH[own + PX] * dy2;
+                  const double wy = syj * cxi * czk;
+#pragma unroll
+                  for (int c = 0; c < 3; c++) {
+                     const double* d = ds + c * PLANE + own;
+                     const double s = e2 * (d[2 * PX] - 2 * d[PX] + d[0]) -
+                                      2 * e1 * (d[PX] - 2 * d[0] + d[-PX]) +
+                                      e0 * (d[0] - 2 * d[-PX] + d[-2 * PX]);
+                     sg[c] += wy * s;
+                  }
+               }
+               const double dz0 = __ldg(a.dc[2] + (k - 1 - a.kb)), dz1 = __ldg(a.dc[2] + (k - a.kb)),
+                            dz2 = __ldg(a.dc[2] + (k + 1 - a.kb));
+               if (dz0 != 0 || dz1 != 0 || dz2 != 0) {
+                  const double e0 = __ldg(a.rho + p - a.nij) * dz0, e1 = RH[own] * dz1,
+                               e2 = __ldg(a.rho + p + a.nij) * dz2;
+                  const double wz = szk * cxi * cyj;
+#pragma unroll
+                  for (int c = 0; c < 3; c++) {
+                     const double s = e2 * (dq[4][c] - 2 * dq[3][c] + dq[2][c]) -
+                                      2 * e1 * (dq[3][c] - 2 * dq[2][c] + dq[1][c]) +
+                                      e0 * (dq[2][c] - 2 * dq[1][c] + dq[0][c]);
+                     sg[c] += wz * s;
+                  }
+               }
+            }
+            const double birho = a.beta * ir;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+               const long long q = p + c * npts;
+               a.out[q] = (__ldg(a.up + q) + cr * lu[c]) - birho * sg[c];
+            }
+         }
+      }
+      __syncthreads();
+   }
+}
+
+// Weights of the variable-coefficient second difference (src/rhs4sg_rev.C:114-136)
+// along each axis, for coefficient mu*s (type 0) and (2mu+lambda)*s (type 1):
+//   W1(q) = a(q-1) - 3/4 (a(q) + a(q-2))           (pair q-2, q)
+//   W2(q) = a(q-2) + a(q+1) + 3 (a(q) + a(q-1))     (pair q-1, q)
+// scaled by 1/(6 h^2); the operator at q uses W1(q), W2(q), W2(q+1), W1(q+2).
+__global__ void weights_kernel(Box b, const double* __restrict__ mu, const double* __restrict__ la,
+                               const double* __restrict__ sx, const double* __restrict__ sy,
+                               const double* __restrict__ sz, double scale, WeightPtrs w)
+{
+   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < b.npts;
+        p += (long long)gridDim.x * blockDim.x) {
+      const int i = b.ib + (int)(p % b.ni);
+      const int j = b.jb + (int)((p / b.ni) % (b.je - b.jb + 1));
+      const int k = b.kb + (int)(p / b.nij);
+      const int qv[3] = {i, j, k}, lo[3] = {b.ib, b.jb, b.kb}, hi[3] = {b.ie, b.je, b.ke};
+      const long long st[3] = {1, b.ni, b.nij};
+      const double* sv[3] = {sx, sy, sz};
+#pragma unroll
+      for (int ax = 0; ax < 3; ax++) {
+         double w1[2] = {0, 0}, w2[2] = {0, 0};
+         const int q = qv[ax];
+         if (q - 2 >= lo[ax]) {
+            double am[2][4];  // offsets -2..+1
+            for (int m = -2; m <= 1; m++) {
+               if (q + m > hi[ax]) {
+                  am[0][m + 2] = am[1][m + 2] = 0;
+                  continue;
+               }
+               const long long pm = p + m * st[ax];
+               const double s = sv[ax][q + m - lo[ax]];
+               am[0][m + 2] = mu[pm] * s;
+               am[1][m + 2] = (2 * mu[pm] + la[pm]) * s;
+            }
+            for (int t = 0; t < 2; t++) {
+               w1[t] = am[t][1] - 0.75 * (am[t][2] + am[t][0]);
+               if (q + 1 <= hi[ax]) w2[t] = am[t][0] + am[t][3] + 3 * (am[t][2] + am[t][1]);
+            }
+         }
+         for (int t = 0; t < 2; t++) {
+            w.p[ax * 4 + t * 2 + 0][p] = scale * w1[t];
+            w.p[ax * 4 + t * 2 + 1][p] = scale * w2[t];
+         }
+      }
+   }
+}
+
+__global__ void inverse_kernel(long long n, const double* __restrict__ x, double* __restrict__ y)
+{
+   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+        p += (long long)gridDim.x * blockDim.x)
+      y[p] = 1.0 / x[p];
+}
+
+// (up - 2u + um) on a slab of planes [k0, k1] into a compact scratch array.
+__global__ void uacc_slab_kernel(Box b, int k0, int k1, const double* __restrict__ up,
+                                 const double* __restrict__ u, const double* __restrict__ um,
+                                 double* __restrict__ out)
+{
+   const long long nslab = b.nij * (k1 - k0 + 1);
+   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < 3 * nslab;
+        q += (long long)gridDim.x * blockDim.x) {
+      const int c = (int)(q / nslab);
+      const long long r = q % nslab;
+      const long long p = r + b.nij * (long long)(k0 - b.kb) + c * b.npts;
+      out[q] = (up[p] - 2 * u[p]) + um[p];
+   }
+}
+
+int grid_stride_blocks(long long n)
+{
+   long long g = (n + 255) / 256;
+   return (int)std::min<long long>(std::max<long long>(g, 1), 152LL * 16);
+}
+
+}  // namespace
+
+int launch_weights(const Box& b, const double* mu, const double* la, const double* sx,
+                   const double* sy, const double* sz, double h, WeightPtrs w, cudaStream_t s)
+{
+   weights_kernel<<<grid_stride_blocks(b.npts), 256, 0, s>>>(b, mu, la, sx, sy, sz,
+                                                             1.0 / (6 * h * h), w);
+   return launch_status();
+}
+
+int launch_inverse(long long n, const double* x, double* y, cudaStream_t s)
+{
+   inverse_kernel<<<grid_stride_blocks(n), 256, 0, s>>>(n, x, y);
+   return launch_status();
+}
+
+int launch_uacc_slab(const Box& b, int k0, int k1, const double* up, const double* u,
+                     const double* um, double* out, cudaStream_t s)
+{
+   const long long n = 3 * b.nij * (k1 - k0 + 1);
+   uacc_slab_kernel<<<grid_stride_blocks(n), 256, 0, s>>>(b, k0, k1, up, u, um, out);
+   return launch_status();
+}
+
+int launch_fused_stage(const FusedStage& st, cudaStream_t stream)
+{
+   if (st.k2 < st.k1) return kOk;
+   const Box& b = st.b;
+   if (b.cs != b.npts) return kNotSupported;  // SoA only
+   FusedArgs a;
+   a.ib = b.ib; a.ie = b.ie; a.jb = b.jb; a.je = b.je; a.kb = b.kb; a.ke = b.ke;
+   a.ni = b.ni; a.nij = b.nij; a.npts = b.npts;
+   a.k1 = st.k1;
+   a.k2 = st.k2;
+   a.u = st.u;
+   a.um = st.um;
+   a.up = st.up;
+   a.out = st.out;
+   a.mu = st.mu;
+   a.la = st.la;
+   a.rho = st.rho;
+   a.irho = st.irho;
+   for (int q = 0; q < kWeightArrays; q++) a.w[q] = st.w.p[q];
+   a.sx = st.st[0];
+   a.sy = st.st[1];
+   a.sz = st.st[2];
+   for (int q = 0; q < 3; q++) {
+      a.dc[q] = st.dc[q];
+      a.co[q] = st.co[q];
+   }
+   a.cof144 = 1.0 / (144 * st.h * st.h);
+   a.coef = st.corrector ? st.dt * st.dt / 12 : st.dt * st.dt;
+   a.beta = st.beta;
+   const int ni = b.ie - b.ib - 3, nj = b.je - b.jb - 3, nk = st.k2 - st.k1 + 1;
+   const int gx = blocks_for(ni, TX), gy = blocks_for(nj, TY);
+   // enough CTAs to fill every SM several times over; a chunk of at least 16 planes
+   // keeps the 4-plane warm-up of the ring small
+   int chunks = 1;
+   const long long cols = (long long)gx * gy;
+   const long long want = 152LL * 8;
+   if (cols < want) chunks = (int)std::min<long long>((want + cols - 1) / cols, std::max(1, nk / 16));
+   if (st.kchunk > 0) chunks = (nk + st.kchunk - 1) / st.kchunk;
+   a.kchunk = (nk + chunks - 1) / chunks;
+   const dim3 grid(gx, gy, (nk + a.kchunk - 1) / a.kchunk), block(TX, TY, 1);
+   const size_t smem = smem_doubles(st.corrector) * sizeof(double);
+   // the opt-in shared-memory size is a per-device function attribute
+   int dev = 0;
+   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return kCudaError;
+   static bool attr_set[2][64] = {};
+   if (!attr_set[st.corrector][dev]) {
+      cudaError_t e = st.corrector
+          ? cudaFuncSetAttribute(fused_stage_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+          : cudaFuncSetAttribute(fused_stage_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return kCudaError;
+      attr_set[st.corrector][dev] = true;
+   }
+   if (st.corrector)
+      fused_stage_kernel<1><<<grid, block, smem, stream>>>(a);
+   else
+      fused_stage_kernel<0><<<grid, block, smem, stream>>>(a);
+   return launch_status();
+}
+
+}  // namespace sw4g
