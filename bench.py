@@ -176,8 +176,9 @@ def max_over_ranks(x, world):
 # --------------------------------------------------------------------------
 # CPU baseline: the oracle time step on a bounded sample of the workload
 # --------------------------------------------------------------------------
-def cpu_sample(n=96, steps=1, use_ref=False):
-    """Time `steps` CPU time steps of the C2 workload restricted to an n^3 grid."""
+def cpu_sample(n=96, steps=1, min_seconds=0.0, max_steps=40):
+    """Time CPU time steps of the C2 workload restricted to an n^3 grid: `steps`
+    steps, continued until at least `min_seconds` have elapsed (at most max_steps)."""
     from oracle import oracle as O
     import sw4lite_gb300 as sg
     from tests.gpu_util import OracleProblem
@@ -199,12 +200,14 @@ def cpu_sample(n=96, steps=1, use_ref=False):
     O.step(prob.P, 1, 0.0, up, u, um, lu, f, uacc)
     t0 = time.perf_counter()
     t = cfg["src"]["t0"]
-    for _ in range(steps):
+    done = 0
+    while done < steps or (time.perf_counter() - t0 < min_seconds and done < max_steps):
         O.step(prob.P, 1, t, up, u, um, lu, f, uacc)
         um, u, up = u, up, um
         t += dt
+        done += 1
     el = time.perf_counter() - t0
-    return n ** 3 * steps / el, el, n
+    return n ** 3 * done / el, el, n, done
 
 
 def run_reference(args, rank, world):
@@ -216,7 +219,7 @@ def run_reference(args, rank, world):
     n = args.cpu_n
     samples = []
     for s in range(args.warmup + args.steps):
-        rate, el, _ = cpu_sample(n=n, steps=1)
+        rate, el, _, _ = cpu_sample(n=n, steps=1)
         if s >= args.warmup:
             samples.append((rate, el))
     rate = len(samples) * n ** 3 / sum(e for _, e in samples)
@@ -314,10 +317,10 @@ def run_ours(args, rank, world):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         ncores = os.cpu_count() or 1
         os.environ.setdefault("OMP_NUM_THREADS", str(ncores))
-        rate, el, cn = cpu_sample(n=args.cpu_n, steps=1)
+        rate, el, cn, done = cpu_sample(n=args.cpu_n, steps=1, min_seconds=args.cpu_seconds)
         cpu = {"value": rate, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]),
                "kind": "port",
-               "sample": f"1 time step of a {cn}^3 grid of the workload ({el:.1f} s, oracle "
+               "sample": f"{done} time steps of a {cn}^3 grid of the workload ({el:.1f} s; oracle "
                          "restatement of the reference kernels, OpenMP)"}
 
     if rank == 0:
@@ -358,7 +361,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--mode", choices=["fused", "phases"], default="fused")
     ap.add_argument("--n", type=int, default=512, help="grid points per axis")
-    ap.add_argument("--cpu-n", type=int, default=96, help="CPU sample grid points per axis")
+    ap.add_argument("--cpu-n", type=int, default=256, help="CPU sample grid points per axis")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="minimum CPU work of the baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -184,9 +184,10 @@ class Problem(C.Structure):
                 ("src_t0", _D), ("src_kind", _I)]
 
 
-def step(problem: Problem, soa, t, up, u, um, lu, f, uacc):
-    lib().sw4o_step(C.byref(problem), C.c_int(soa), C.c_double(t), _dp(up), _dp(u), _dp(um),
-                    _dp(lu), _dp(f), _dp(uacc))
+def step(problem: Problem, soa, t, up, u, um, lu, f, uacc, which="oracle"):
+    fn = ref().sw4ref_step if which == "ref" else lib().sw4o_step
+    fn(C.byref(problem), C.c_int(soa), C.c_double(t), _dp(up), _dp(u), _dp(um), _dp(lu), _dp(f),
+       _dp(uacc))
 
 
 def set_threads(n: int) -> None:

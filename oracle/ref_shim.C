@@ -11,6 +11,8 @@
 // constructor (src/EW.C:162) would parse an input deck and start MPI.
 #include <cstring>
 #include <new>
+#include <vector>
+#include "../oracle/sw4_oracle.h"
 #include "sw4.h"
 #include "EW.h"
 #include "SuperGrid.h"
@@ -211,6 +213,71 @@ double sw4ref_timefunc(int kind, double freq, double t, int tt)
    int ipar[1] = {0};
    if (kind == 0) return tt ? Gaussian_tt(freq, t, par, 2, ipar, 1) : Gaussian(freq, t, par, 2, ipar, 1);
    return tt ? C6SmoothBump_tt(freq, t, par, 2, ipar, 1) : C6SmoothBump(freq, t, par, 2, ipar, 1);
+}
+
+// One time step with the reference's own kernels, in the CPU phase order of
+// EW::timesteploop (src/EW.C:2537-2756); forcing from the same grid-point source
+// list the oracle uses (sw4o_force), boundary data zero.  Same contract as
+// sw4o_step (oracle/sw4_oracle.h).
+void sw4ref_step(const sw4o_problem* p, int soa, double t, double* up, const double* u,
+                 const double* um, double* lu, double* f, double* uacc)
+{
+   double acof[384], ghcof[6], bope[48], sbop[5];
+   kernel_host(soa)->GetStencilCoefficients(acof, ghcof, bope, sbop);
+   const long npts = (long)(p->ie - p->ib + 1) * (p->je - p->jb + 1) * (p->ke - p->kb + 1);
+   const double dt = p->dt;
+   int onesided[6], wind[36];
+   for (int s = 0; s < 6; s++) onesided[s] = p->onesided[s];
+   for (int s = 0; s < 36; s++) wind[s] = p->wind[s];
+   int npw[6];
+   sw4o_boundary_windows(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, p->nx, p->ny, p->nz, p->bccnd,
+                         wind, npw);
+   std::vector<std::vector<double>> bf(6);
+   for (int s = 0; s < 6; s++) bf[s].assign(3 * (npw[s] > 0 ? npw[s] : 1), 0.0);
+   auto bc = [&](double* w) {
+      sw4ref_bcfortsg(soa, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, wind, p->nx, p->ny, p->nz, w,
+                      p->h, p->bccnd, sbop, const_cast<double*>(p->mu), const_cast<double*>(p->la), t + dt,
+                      bf[0].data(), bf[1].data(), bf[2].data(), bf[3].data(), bf[4].data(),
+                      bf[5].data(), const_cast<double*>(p->strx), const_cast<double*>(p->stry));
+   };
+   double* U = const_cast<double*>(u);
+   double* UM = const_cast<double*>(um);
+   EW* ew = kernel_host(soa);
+   sw4o_force(soa, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, f, p->nsrc, p->src_ijk, p->src_amp,
+              p->src_freq, p->src_t0, p->src_kind, t, 0);
+   std::memset(lu, 0, 3 * npts * sizeof(double));
+   sw4ref_rhs4sg(soa, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, p->nz, onesided, acof, bope, ghcof,
+                 lu, U, const_cast<double*>(p->mu), const_cast<double*>(p->la), p->h,
+                 const_cast<double*>(p->strx), const_cast<double*>(p->stry),
+                 const_cast<double*>(p->strz));
+   ew->predfort(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, U, UM, lu, f,
+                const_cast<double*>(p->rho), dt * dt);
+   bc(up);
+   sw4o_force(soa, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, f, p->nsrc, p->src_ijk, p->src_amp,
+              p->src_freq, p->src_t0, p->src_kind, t, 1);
+   ew->dpdmtfort(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, U, UM, uacc, 1.0 / (dt * dt));
+   sw4ref_rhs4sg(soa, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, p->nz, onesided, acof, bope, ghcof,
+                 lu, uacc, const_cast<double*>(p->mu), const_cast<double*>(p->la), p->h,
+                 const_cast<double*>(p->strx), const_cast<double*>(p->stry),
+                 const_cast<double*>(p->strz));
+   ew->corrfort(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, lu, f, const_cast<double*>(p->rho),
+                dt * dt * dt * dt);
+   if (p->sg_beta != 0) {
+      double* pr[9] = {const_cast<double*>(p->dcx), const_cast<double*>(p->dcy),
+                       const_cast<double*>(p->dcz), const_cast<double*>(p->strx),
+                       const_cast<double*>(p->stry), const_cast<double*>(p->strz),
+                       const_cast<double*>(p->cox), const_cast<double*>(p->coy),
+                       const_cast<double*>(p->coz)};
+      if (p->sg_order == 6)
+         sw4ref_addsgd6(soa, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, U, UM,
+                        const_cast<double*>(p->rho), pr[0], pr[1], pr[2], pr[3], pr[4], pr[5],
+                        pr[6], pr[7], pr[8], p->sg_beta);
+      else
+         sw4ref_addsgd4(soa, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, U, UM,
+                        const_cast<double*>(p->rho), pr[0], pr[1], pr[2], pr[3], pr[4], pr[5],
+                        pr[6], pr[7], pr[8], p->sg_beta);
+   }
+   bc(up);
 }
 
 }  // extern "C"

@@ -2,7 +2,7 @@
 kernel/phase API.
 
 The compute path is libsw4g.so (CUDA kernels + C ABI, include/sw4g.h), built in-tree
-by ``python -m sw4lite_gb300.build``.  This module loads it with ctypes and offers a
+by ``python -m sw4lite_gb300.builder``.  This module loads it with ctypes and offers a
 thin Python view of the C ABI for tests and benchmarks; PyTorch is used only for
 device memory and streams.  There is no CPU fallback: every call that computes
 runs on the GPU, and loading fails loudly when the library is missing.
@@ -91,7 +91,7 @@ _SIGS = {
 
 def build(force: bool = False) -> Path:
     import importlib
-    return importlib.import_module(__name__ + ".build").build(force=force)
+    return importlib.import_module(__name__ + ".builder").build(force=force)
 
 
 def lib():
@@ -99,7 +99,7 @@ def lib():
     global _lib
     if _lib is None:
         if not LIB_PATH.exists():
-            raise Sw4gError(f"{LIB_PATH} is missing: build it with `python -m sw4lite_gb300.build`"
+            raise Sw4gError(f"{LIB_PATH} is missing: build it with `python -m sw4lite_gb300.builder`"
                             " (there is no CPU fallback)")
         L = C.CDLL(str(LIB_PATH))
         for name, (args, res) in _SIGS.items():

@@ -359,6 +359,7 @@ int EW::fused_piece(int piece, int ip, int iq)
       return launch_fused_stage(fs, stream_);
    }
    if (piece == 1) {
+      SW4G_TRY(launch_ghost_shell(b, 0, up, u, um, nullptr, stream_));
       for (int side = 0; side < 2; side++)
          if (onesided_[4 + side])
             SW4G_TRY(launch_stage_rows(0, side == 0, b, nz, u, b, mu_, la_, g_.h, st[0], st[1], st[2],
@@ -371,6 +372,7 @@ int EW::fused_piece(int piece, int ip, int iq)
       return enforce_bc(up);
    }
    if (piece == 4) {
+      SW4G_TRY(launch_ghost_shell(b, 1, out, u, um, up, stream_));
       for (int side = 0; side < 2; side++) {
          if (!onesided_[4 + side]) continue;
          const int k0 = side == 0 ? bd.kb : nz - 7, k1 = side == 0 ? 8 : bd.ke;
@@ -455,7 +457,9 @@ int EW::launches_per_step(int mode) const
       const int rhs = 1 + rows;
       return 2 * (1 + src) + 2 * rhs + 3 + (damp ? 1 : 0) + 2 * bc;
    }
-   return 2 * (1 + rows + src + bc) + rows + (damp && g_.sg_order == 6 ? 1 : 0);
+   // per stage: stage kernel, ghost shell, one-sided rows, forcing, BC sides;
+   // the corrector adds the rows' slab kernels (and 6th-order damping)
+   return 2 * (2 + rows + src + bc) + rows + (damp && g_.sg_order == 6 ? 1 : 0);
 }
 
 }  // namespace sw4g

@@ -72,6 +72,9 @@ int launch_addsgd(int order, int soa, int ifirst, int ilast, int jfirst, int jla
                   const double* stry, const double* strz, const double* cox, const double* coy,
                   const double* coz, double beta, cudaStream_t s);
 
+int launch_ghost_shell(const Box& b, int corrector, double* out, const double* u,
+                       const double* um, const double* up, cudaStream_t s);
+
 int launch_bcfortsg(int soa, int ib, int ie, int jb, int je, int kb, int ke, const int wind[36],
                     int nx, int ny, int nz, double* u, double h, const int bccnd[6],
                     const double sbop[5], const double* mu, const double* la,

@@ -145,6 +145,50 @@ __global__ void __launch_bounds__(256) addsgd6_kernel(SgArgs a)
    }
 }
 
+// Ghost shell of a stage: every array point outside the interior box
+// [ib+2,ie-2]x[jb+2,je-2]x[kb+2,ke-2] gets the stage update with Lu = F = 0, as
+// the reference's pointwise predfort/corrfort do over the whole array
+// (src/ew-cfromfort.C:40-114): predictor out = 2u - um, corrector out = up.
+// Points are enumerated as the 4 outer k-planes, then the 4 outer j-rows of the
+// inner planes, then the 4 outer i-columns of the inner rows.
+__global__ void ghost_shell_kernel(Box b, int corrector, double* __restrict__ out,
+                                   const double* __restrict__ u, const double* __restrict__ um,
+                                   const double* __restrict__ up)
+{
+   const long long ni = b.ni, nj = b.je - b.jb + 1, nk = b.ke - b.kb + 1;
+   const long long nA = 4 * ni * nj, nB = 4 * ni * (nk - 4), nC = 4 * (nj - 4) * (nk - 4);
+   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nA + nB + nC;
+        q += (long long)gridDim.x * blockDim.x) {
+      int i, j, k;
+      if (q < nA) {
+         const int s = (int)(q / (ni * nj));
+         const long long r = q % (ni * nj);
+         k = s < 2 ? b.kb + s : b.ke - (3 - s);
+         j = b.jb + (int)(r / ni);
+         i = b.ib + (int)(r % ni);
+      } else if (q < nA + nB) {
+         const long long r0 = q - nA;
+         const int s = (int)(r0 / (ni * (nk - 4)));
+         const long long r = r0 % (ni * (nk - 4));
+         j = s < 2 ? b.jb + s : b.je - (3 - s);
+         k = b.kb + 2 + (int)(r / ni);
+         i = b.ib + (int)(r % ni);
+      } else {
+         const long long r0 = q - nA - nB;
+         const int s = (int)(r0 / ((nj - 4) * (nk - 4)));
+         const long long r = r0 % ((nj - 4) * (nk - 4));
+         i = s < 2 ? b.ib + s : b.ie - (3 - s);
+         k = b.kb + 2 + (int)(r / (nj - 4));
+         j = b.jb + 2 + (int)(r % (nj - 4));
+      }
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+         const long long x = cidx(b, c, i, j, k);
+         out[x] = corrector ? up[x] : 2 * u[x] - um[x];
+      }
+   }
+}
+
 int stream_grid(long long n)
 {
    long long b = (n + 255) / 256;
@@ -177,6 +221,16 @@ int launch_dpdmtfort(int ib, int ie, int jb, int je, int kb, int ke, const doubl
 {
    const long long n = 3LL * (ie - ib + 1) * (je - jb + 1) * (ke - kb + 1);
    dpdm_kernel<<<stream_grid(n), 256, 0, s>>>(n, up, u, um, u2, dt2i);
+   return launch_status();
+}
+
+int launch_ghost_shell(const Box& b, int corrector, double* out, const double* u,
+                       const double* um, const double* up, cudaStream_t s)
+{
+   const long long ni = b.ni, nj = b.je - b.jb + 1, nk = b.ke - b.kb + 1;
+   if (ni < 5 || nj < 5 || nk < 5) return kBadArgument;
+   const long long n = 4 * ni * nj + 4 * ni * (nk - 4) + 4 * (nj - 4) * (nk - 4);
+   ghost_shell_kernel<<<stream_grid(n), 256, 0, s>>>(b, corrector, out, u, um, up);
    return launch_status();
 }
 

@@ -138,25 +138,37 @@ class OracleProblem:
         self.P = P
         self.npts = (nx + 4) * (ny + 4) * (nz + 4)
 
-    def run(self, u, um, t0, nsteps):
+    def run(self, u, um, t0, nsteps, which="oracle"):
         n3 = 3 * self.npts
         u, um = u.copy(), um.copy()
         up, lu, f, uacc = (np.zeros(n3) for _ in range(4))
         t = t0
         for _ in range(nsteps):
-            O.step(self.P, 1, t, up, u, um, lu, f, uacc)
+            O.step(self.P, 1, t, up, u, um, lu, f, uacc, which=which)
             um, u, up = u, up, um
             t += self.P.dt
         return u, um
 
 
 def solution_mask(grid):
-    """Array points that determine the solution: everything except the free-surface
-    side's outer ghost plane (never set by a boundary condition, never read)."""
+    """Every array point: the GPU paths reproduce the reference's values on the
+    whole array, ghost shell included."""
     nx, ny, nz = grid.nx, grid.ny, grid.nz
-    m = np.ones((nz + 4, ny + 4, nx + 4), dtype=bool)
-    if grid.bc[4] == 0:
-        m[0] = False
-    if grid.bc[5] == 0:
-        m[-1] = False
-    return np.broadcast_to(m, (3,) + m.shape).ravel()
+    return np.ones(3 * (nz + 4) * (ny + 4) * (nx + 4), dtype=bool)
+
+
+def describe_error(a, b, grid, mask=None):
+    """Location and size of the largest |a-b| over a 3-component field on grid."""
+    shape = (3, grid.nz + 4, grid.ny + 4, grid.nx + 4)
+    d = np.abs(np.asarray(a) - np.asarray(b))
+    if mask is not None:
+        d = np.where(mask, d, 0.0)
+    q = int(np.argmax(d))
+    c, kk, jj, ii = np.unravel_index(q, shape)
+    scale = np.max(np.abs(b))
+    # per-plane maximum of the error, to tell boundary rows from the interior
+    planes = d.reshape(shape).max(axis=(0, 2, 3))
+    worst = np.argsort(planes)[::-1][:4]
+    return (f"max |diff| {d.flat[q]:.3e} (rel {d.flat[q] / scale:.3e}) at c={c} "
+            f"i={ii - 1} j={jj - 1} k={kk - 1}; worst planes k=" +
+            ", ".join(f"{w - 1}:{planes[w] / scale:.1e}" for w in worst))

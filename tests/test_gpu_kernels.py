@@ -80,7 +80,8 @@ def test_pointwise_updates(soa):
     ref2 = np.zeros_like(u)
     O.dpdmtfort(g.bounds, up0, u, um, ref2, 1 / dt ** 2)
     out = dev(np.zeros_like(u))
-    sg.check(L.sw4g_dpdmtfort(*g.bounds, dev(up0).data_ptr(), d["u"].data_ptr(),
+    dup0 = dev(up0)
+    sg.check(L.sw4g_dpdmtfort(*g.bounds, dup0.data_ptr(), d["u"].data_ptr(),
                               d["um"].data_ptr(), out.data_ptr(), 1 / dt ** 2, stream()))
     np.testing.assert_allclose(host(out), ref2, rtol=1e-14, atol=1e-12)
 
@@ -97,11 +98,12 @@ def test_addsgd(order, soa):
     co = (g.strip(rng, g.ni, 0.3, 1), g.strip(rng, g.nj, 0.3, 1), g.strip(rng, g.nk, 0.3, 1))
     ref = up0.copy()
     O.addsgd(order, soa, g.bounds, ref, u, um, rho, dc, st, co, 0.02)
-    dup = dev(up0)
+    # every device buffer stays referenced until the kernel has run
+    dup, du, dum, drho = dev(up0), dev(u), dev(um), dev(rho)
     prof = [dev(a) for a in (*dc, *st, *co)]
     fn = sg.lib().sw4g_addsgd6fort if order == 6 else sg.lib().sw4g_addsgd4fort
-    sg.check(fn(soa, *g.bounds, dup.data_ptr(), dev(u).data_ptr(), dev(um).data_ptr(),
-                dev(rho).data_ptr(), *[p.data_ptr() for p in prof], 0.02, stream()))
+    sg.check(fn(soa, *g.bounds, dup.data_ptr(), du.data_ptr(), dum.data_ptr(),
+                drho.data_ptr(), *[p.data_ptr() for p in prof], 0.02, stream()))
     got = host(dup)
     assert rel_err(got - up0, ref - up0) <= 1e-13
 
@@ -127,7 +129,8 @@ def test_bcfortsg(soa, bccnd):
     w = (C.c_int * 36)(*[int(x) for x in wind])
     bc = (C.c_int * 6)(*bccnd)
     sb = (C.c_double * 6)(*sbop)
+    dmu, dla, dsx, dsy = dev(mu), dev(la), dev(sx), dev(sy)
     sg.check(sg.lib().sw4g_bcfortsg(soa, *g.bounds, w, g.nx, g.ny, g.nz, du.data_ptr(), g.h, bc,
-                                    C.cast(sb, sg._D), dev(mu).data_ptr(), dev(la).data_ptr(), ptrs,
-                                    dev(sx).data_ptr(), dev(sy).data_ptr(), stream()))
+                                    C.cast(sb, sg._D), dmu.data_ptr(), dla.data_ptr(), ptrs,
+                                    dsx.data_ptr(), dsy.data_ptr(), stream()))
     assert rel_err(host(du), ref) <= 1e-14

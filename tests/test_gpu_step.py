@@ -11,7 +11,8 @@ import pytest
 import sw4lite_gb300 as sg
 from oracle import oracle as O
 from tests.fields import rel_err
-from tests.gpu_util import OracleProblem, dev, host, smooth_fields, smooth_material, solution_mask
+from tests.gpu_util import (OracleProblem, describe_error, dev, host, smooth_fields, smooth_material,
+                            solution_mask)
 
 pytestmark = pytest.mark.gpu
 
@@ -71,8 +72,8 @@ def test_steps_match_oracle(name, mode):
     ref_u, ref_um = OracleProblem(g, *mat, dt, srcs).run(*fields, 0.0, nsteps)
     u, um = _gpu_run(g, mat, fields, srcs, dt, nsteps, mode)
     m = solution_mask(g)
-    assert rel_err(u[m], ref_u[m]) <= 1e-12
-    assert rel_err(um[m], ref_um[m]) <= 1e-12
+    assert rel_err(u[m], ref_u[m]) <= 1e-12, describe_error(u, ref_u, g, m)
+    assert rel_err(um[m], ref_um[m]) <= 1e-12, describe_error(um, ref_um, g, m)
 
 
 def test_sixth_order_damping_step():
