@@ -97,6 +97,39 @@ int sw4g_bcfortsg(int soa, int ib, int ie, int jb, int je, int kb, int ke, const
                   const double* strx, const double* stry, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Phase-level entry points for the one-sided SBP rows (SoA fields only)
+ * ------------------------------------------------------------------------- */
+
+/* Size in doubles of the scratch sw4g_corr_rows needs: the corrector's stage
+ * field on 10 planes of the array, 3 components. */
+long long sw4g_corr_rows_scratch_len(int ifirst, int ilast, int jfirst, int jlast);
+
+/* Predictor on the 6 one-sided rows next to a free surface, fused with the
+ * operator: out = 2u - um + dt^2/rho L(u) at k=1..6 (side 0, top) or nz-5..nz
+ * (side 1, bottom), i,j in [first+2, last-2]; forcing is added separately.
+ * Replaces rhs4_lowk_pred_gpu / rhs4_highk_pred_gpu (src/device-routines.h:337,
+ * :344).  The array must hold planes 0..8 (top) or nz-7..nz+1 (bottom). */
+int sw4g_pred_rows(int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast, int nz,
+                   int side, double* out, const double* u, const double* um, const double* mu,
+                   const double* lambda, const double* rho, const double* strx, const double* stry,
+                   const double* strz, double h, double dt, void* stream);
+
+/* Corrector with 4th-order supergrid damping on the 6 one-sided rows:
+ *   out = up + dt^4/(12 rho) L((up - 2u + um)/dt^2) - beta/rho SG(u - um)
+ * Replaces rhs4_lowk_corr_gpu / rhs4_highk_corr_gpu (src/device-routines.h:351,
+ * :358) together with evalDpDmInTimeCU (src/EW_cuda.C:267) and the supergrid
+ * damping of those rows (addSuperGridDampingCU_upper_boundary,
+ * src/EW_cuda.C:1420-1466).  `scratch` is a caller-owned device buffer of at
+ * least sw4g_corr_rows_scratch_len(...) doubles, overwritten by the call. */
+int sw4g_corr_rows(int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast, int nz,
+                   int side, double* out, const double* up, const double* u, const double* um,
+                   const double* mu, const double* lambda, const double* rho, const double* strx,
+                   const double* stry, const double* strz, const double* dcx, const double* dcy,
+                   const double* dcz, const double* cox, const double* coy, const double* coz,
+                   double h, double dt, double beta, double* scratch, long long scratch_len,
+                   void* stream);
+
+/* ---------------------------------------------------------------------------
  * Host-side set-up helpers (no device work)
  * ------------------------------------------------------------------------- */
 

@@ -86,6 +86,10 @@ _SIGS = {
     "sw4g_ew_launches_per_step": ([_VP, C.c_int], C.c_int),
     "sw4g_ew_profile_kernels": ([_VP, C.c_int, _D], C.c_int),
     "sw4g_fma_peak": ([C.c_int, _D, _VP], C.c_int),
+    "sw4g_corr_rows_scratch_len": ([C.c_int] * 4, C.c_longlong),
+    "sw4g_pred_rows": ([C.c_int] * 8 + [_VP] * 9 + [C.c_double, C.c_double, _VP], C.c_int),
+    "sw4g_corr_rows": ([C.c_int] * 8 + [_VP] * 16 + [C.c_double] * 3 + [_VP, C.c_longlong, _VP],
+                       C.c_int),
 }
 
 

@@ -173,6 +173,66 @@ int sw4g_bcfortsg(int soa, int ib, int ie, int jb, int je, int kb, int ke, const
                           lambda, bforce, strx, stry, as_stream(stream));
 }
 
+long long sw4g_corr_rows_scratch_len(int ifirst, int ilast, int jfirst, int jlast)
+{
+   if (ilast < ifirst || jlast < jfirst) return 0;
+   return 3LL * 10 * (ilast - ifirst + 1) * (long long)(jlast - jfirst + 1);
+}
+
+namespace {
+bool rows_args_ok(int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast, int nz,
+                  int side)
+{
+   if (!bounds_ok(ifirst, ilast, jfirst, jlast, kfirst, klast)) return false;
+   if (ilast - ifirst < 4 || jlast - jfirst < 4 || nz < 8) return false;
+   if (side == 0) return kfirst <= -1 && klast >= 8;
+   if (side == 1) return kfirst <= nz - 7 && klast >= nz + 2;
+   return false;
+}
+}  // namespace
+
+int sw4g_pred_rows(int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast, int nz,
+                   int side, double* out, const double* u, const double* um, const double* mu,
+                   const double* lambda, const double* rho, const double* strx, const double* stry,
+                   const double* strz, double h, double dt, void* stream)
+{
+   if (!rows_args_ok(ifirst, ilast, jfirst, jlast, kfirst, klast, nz, side) || !out || !u ||
+       !um || !mu || !lambda || !rho || !strx || !stry || !strz || !(h > 0))
+      return SW4G_BAD_ARGUMENT;
+   const Box b = make_box(1, ifirst, ilast, jfirst, jlast, kfirst, klast);
+   const double* none[3] = {strx, stry, strz};
+   return launch_stage_rows(0, side == 0, b, nz, u, b, mu, lambda, h, strx, stry, strz, u, um,
+                            nullptr, out, rho, nullptr, dt * dt, 0.0, none, none, none,
+                            as_stream(stream));
+}
+
+int sw4g_corr_rows(int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast, int nz,
+                   int side, double* out, const double* up, const double* u, const double* um,
+                   const double* mu, const double* lambda, const double* rho, const double* strx,
+                   const double* stry, const double* strz, const double* dcx, const double* dcy,
+                   const double* dcz, const double* cox, const double* coy, const double* coz,
+                   double h, double dt, double beta, double* scratch, long long scratch_len,
+                   void* stream)
+{
+   if (!rows_args_ok(ifirst, ilast, jfirst, jlast, kfirst, klast, nz, side) || !out || !up ||
+       !u || !um || !mu || !lambda || !rho || !strx || !stry || !strz || !dcx || !dcy || !dcz ||
+       !cox || !coy || !coz || !scratch || !(h > 0))
+      return SW4G_BAD_ARGUMENT;
+   if (scratch_len < sw4g_corr_rows_scratch_len(ifirst, ilast, jfirst, jlast))
+      return SW4G_BAD_ARGUMENT;
+   const Box b = make_box(1, ifirst, ilast, jfirst, jlast, kfirst, klast);
+   const int k0 = side == 0 ? -1 : nz - 7, k1 = side == 0 ? 8 : nz + 2;
+   int st = launch_uacc_slab(b, k0, k1, up, u, um, scratch, as_stream(stream));
+   if (st != SW4G_OK) return st;
+   const Box sb = make_box(1, ifirst, ilast, jfirst, jlast, k0, k1);
+   const double* dc[3] = {dcx, dcy, dcz};
+   const double* sv[3] = {strx, stry, strz};
+   const double* co[3] = {cox, coy, coz};
+   return launch_stage_rows(1, side == 0, b, nz, scratch, sb, mu, lambda, h, strx, stry, strz, u,
+                            um, up, out, rho, nullptr, dt * dt / 12, beta, dc, sv, co,
+                            as_stream(stream));
+}
+
 int sw4g_supergrid_profile(const sw4g_grid* g, int axis, double* dc, double* str, double* corner)
 {
    if (!g || axis < 0 || axis > 2 || !dc || !str || !corner) return SW4G_BAD_ARGUMENT;

@@ -279,8 +279,9 @@ __global__ void __launch_bounds__(256) stage_rows_kernel(OpArgs a, RowUpdate w)
    double r[3];
    lu_bndry_point<TOP>(a, i, j, k, r);
    const long long p = pidx(a.b, i, j, k);
-   const double cr = w.coef * __ldg(w.irho + p);
-   const double birho = w.beta * __ldg(w.irho + p);
+   const double ir = w.irho ? __ldg(w.irho + p) : 1.0 / __ldg(w.rho + p);
+   const double cr = w.coef * ir;
+   const double birho = w.beta * ir;
    for (int c = 0; c < 3; c++) {
       const long long q = cidx(a.b, c, i, j, k);
       const double lu = a.cof * r[c];
