@@ -129,6 +129,27 @@ int sw4g_corr_rows(int ifirst, int ilast, int jfirst, int jlast, int kfirst, int
                    double h, double dt, double beta, double* scratch, long long scratch_len,
                    void* stream);
 
+/* sw4g_corr_rows for callers that cannot allocate device memory (no counterpart
+ * in the reference).  Some callers may not call cudaMalloc: code holding a host
+ * allocator lock, launch-interception tools, frameworks that forbid allocation
+ * after start-up.  They cannot hand sw4g_corr_rows its scratch slab, so this
+ * entry point keeps the slab in a 64 MiB array of device memory owned by the
+ * library (held by every GPU that loads it, until exit) and allocates nothing.
+ * Limit: (ilast-ifirst+1)*(jlast-jfirst+1) <= 279,620 points per plane; larger
+ * planes return SW4G_BAD_ARGUMENT without device work.  All calls on a device
+ * share the array, so calls that overlap on the GPU race; serialise them on
+ * one stream.  Every scratch element the call reads it writes first, so the
+ * array carries no state between calls.  The first call on each device looks up
+ * the array's address (cudaGetSymbolAddress) with that device current; make it
+ * before capturing a stream into a CUDA graph. */
+int sw4g_corr_rows_noalloc(int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                           int nz, int side, double* out, const double* up, const double* u,
+                           const double* um, const double* mu, const double* lambda,
+                           const double* rho, const double* strx, const double* stry,
+                           const double* strz, const double* dcx, const double* dcy,
+                           const double* dcz, const double* cox, const double* coy,
+                           const double* coz, double h, double dt, double beta, void* stream);
+
 /* ---------------------------------------------------------------------------
  * Host-side set-up helpers (no device work)
  * ------------------------------------------------------------------------- */

@@ -90,6 +90,7 @@ _SIGS = {
     "sw4g_pred_rows": ([C.c_int] * 8 + [_VP] * 9 + [C.c_double, C.c_double, _VP], C.c_int),
     "sw4g_corr_rows": ([C.c_int] * 8 + [_VP] * 16 + [C.c_double] * 3 + [_VP, C.c_longlong, _VP],
                        C.c_int),
+    "sw4g_corr_rows_noalloc": ([C.c_int] * 8 + [_VP] * 16 + [C.c_double] * 3 + [_VP], C.c_int),
 }
 
 
