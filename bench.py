@@ -91,6 +91,9 @@ CORR_STAGE_DRAM_BYTES_PER_PT = 243.49
 # reference flop counts per interior point (tests/testil/testil.C:271, :299):
 # rhs4sg 666, addsgd4 375, corrector+dpdm ~23 -> corrector stage; predictor ~683
 CORR_STAGE_REF_FLOPS = 666 + 375 + 11 + 12
+# mixed form, corrector stage: reads Up, U, Um as double-float pairs (9 x 8 B), mu,
+# lambda, rho in FP32 (3 x 4 B), writes the new level (3 x 8 B)
+MIXED_CORR_STAGE_BYTES = 9 * 8 + 3 * 4 + 3 * 8
 STEP_REF_FLOPS = 1747
 
 
@@ -247,29 +250,27 @@ def run_reference(args, rank, world):
 # --------------------------------------------------------------------------
 # GPU arm
 # --------------------------------------------------------------------------
-def run_ours(args, rank, world):
-    import torch
-    import sw4lite_gb300 as sg
-
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    sg.build()
-    cfg = c2_config(args.n)
-    n = args.n
-    g = sg.grid_desc(n, n, n, cfg["h"], bc=cfg["bc"], sg_gp=cfg["sg_gp"], sg_damping=cfg["sg_damping"])
-    stream = torch.cuda.Stream()
+def _make_ew(sg, cfg, n, precision, stream):
+    g = sg.grid_desc(n, n, n, cfg["h"], bc=cfg["bc"], sg_gp=cfg["sg_gp"],
+                     sg_damping=cfg["sg_damping"], precision=precision)
     ew = sg.EW(g, stream=stream)
     rho, mu, la = layered_material(cfg)
     ew.set_material(rho, mu, la)
-    del rho, mu, la
     ew.add_source(sg.source_desc(cfg["src"]["x"], cfg["src"]["y"], cfg["src"]["z"],
                                  moment=cfg["src"]["moment"], freq=cfg["src"]["freq"],
                                  t0=cfg["src"]["t0"], kind=sg.GAUSSIAN))
-    dt = cfl_dt(cfg)
-    ew.set_time_step(dt, 0.0)
+    ew.set_time_step(cfl_dt(cfg), 0.0)
+    return ew
+
+
+def _time_form(args, sg, torch, precision, stream, world, local):
+    """Warm up, then time args.steps steps of one form (CUDA events on its stream);
+    per-kernel times; end-to-end run through the C ABI with pinned host buffers."""
+    n = args.n
+    cfg = c2_config(n)
+    ew = _make_ew(sg, cfg, n, precision, stream)
     mode = sg.MODE_FUSED if args.mode == "fused" else sg.MODE_PHASES
     npts_int = n ** 3
-
     with torch.cuda.stream(stream):
         ew.step(args.warmup, mode)
         torch.cuda.synchronize()
@@ -286,25 +287,14 @@ def run_ours(args, rank, world):
     barrier(world)
     ms = max_over_ranks(ms, world)
     ms_step = ms / args.steps
-    value = world * npts_int / (ms_step * 1e-3)
-
-    # per-kernel device times of a fused step (CUDA events on the EW stream)
-    prof = ew.profile_kernels(nrep=3)
-    corr_ms = prof["corr_stage"]
-    peak_hbm, peak_kind = measured_peaks()
-    corr_bytes = CORR_STAGE_WORDS * 8 * npts_int
-    achieved = corr_bytes / (corr_ms * 1e-3) / 1e9
-    fp64_peak = sg.fma_peak(64, stream=stream)
-    fp64_equiv = CORR_STAGE_REF_FLOPS * npts_int / (corr_ms * 1e-3) / 1e12
-
-    # end to end through the C ABI with host buffers: H2D of (U, Um) from pinned
-    # host memory, the K steps, D2H of U
-    e2e = None
+    out = {"value": world * npts_int / (ms_step * 1e-3), "ms_per_step": ms_step,
+           "clocks": clocks.summary(), "gpu_launches": ew.launches_per_step(mode) * args.steps}
+    out["kernel_ms"] = ew.profile_kernels(nrep=3)
     if not args.no_e2e:
         n3 = 3 * ew.npts
         hu = torch.zeros(n3, dtype=torch.float64, pin_memory=True)
         hum = torch.zeros(n3, dtype=torch.float64, pin_memory=True)
-        ew.get_fields(hu, hum)  # current state as the "input" the user holds
+        ew.get_fields(hu, hum)
         torch.cuda.synchronize()
         barrier(world)
         t0 = time.perf_counter()
@@ -314,9 +304,68 @@ def run_ours(args, rank, world):
             ew.get_fields(hu, None)
         torch.cuda.synchronize()
         el = max_over_ranks(time.perf_counter() - t0, world)
-        e2e = {"value": world * npts_int * args.steps / el, "unit": UNIT,
-               "h2d_bytes_per_step": int(2 * n3 * 8 / args.steps),
-               "d2h_bytes_per_step": int(n3 * 8 / args.steps)}
+        out["e2e"] = {"value": world * npts_int * args.steps / el, "unit": UNIT,
+                      "h2d_bytes_per_step": int(2 * n3 * 8 / args.steps),
+                      "d2h_bytes_per_step": int(n3 * 8 / args.steps)}
+        del hu, hum
+    ew.close()
+    torch.cuda.empty_cache()
+    return out
+
+
+def _mixed_l2_error(args, sg, torch, stream):
+    """Relative L2 difference of the mixed form from the FP64 form after
+    args.err_steps steps of the workload at args.err_n^3."""
+    n = args.err_n
+    cfg = c2_config(n)
+    res = []
+    for prec in (sg.FP64, sg.MIXED):
+        ew = _make_ew(sg, cfg, n, prec, stream)
+        with torch.cuda.stream(stream):
+            ew.step(args.err_steps, sg.MODE_FUSED)
+            u = torch.zeros(3 * ew.npts, dtype=torch.float64, device="cuda")
+            ew.get_fields(u, None)
+        torch.cuda.synchronize()
+        res.append(u)
+        ew.close()
+    a, b = res
+    l2 = float(torch.linalg.norm(b - a) / torch.linalg.norm(a))
+    linf = float((b - a).abs().max() / a.abs().max())
+    return {"l2_rel": l2, "linf_rel": linf, "grid": [n, n, n], "steps": args.err_steps,
+            "t_end": args.err_steps * cfl_dt(cfg)}
+
+
+def run_ours(args, rank, world):
+    import torch
+    import sw4lite_gb300 as sg
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    sg.build()
+    n = args.n
+    npts_int = n ** 3
+    stream = torch.cuda.Stream()
+    fp64 = _time_form(args, sg, torch, sg.FP64, stream, world, local)
+    mixed = None
+    if not args.no_mixed:
+        mixed = _time_form(args, sg, torch, sg.MIXED, stream, world, local)
+        if not args.no_err:
+            mixed["error_vs_fp64"] = _mixed_l2_error(args, sg, torch, stream)
+        mixed["speedup_vs_fp64"] = mixed["value"] / fp64["value"]
+        cm = mixed["kernel_ms"]["corr_stage"]
+        mixed["roofline"] = {"bound": "hbm", "kernel": "mixed corrector stage",
+                             "achieved": MIXED_CORR_STAGE_BYTES * npts_int / (cm * 1e-3) / 1e9,
+                             "unit": "GB/s", "algorithmic_bytes_per_pt": MIXED_CORR_STAGE_BYTES}
+
+    corr_ms = fp64["kernel_ms"]["corr_stage"]
+    peak_hbm, peak_kind = measured_peaks()
+    corr_bytes = CORR_STAGE_WORDS * 8 * npts_int
+    achieved = corr_bytes / (corr_ms * 1e-3) / 1e9
+    fp64_peak = sg.fma_peak(64, stream=stream)
+    fp64_equiv = CORR_STAGE_REF_FLOPS * npts_int / (corr_ms * 1e-3) / 1e12
+    if mixed is not None:
+        mixed["roofline"]["peak"] = peak_hbm
+        mixed["roofline"]["frac"] = mixed["roofline"]["achieved"] / peak_hbm
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -330,11 +379,12 @@ def run_ours(args, rank, world):
 
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "metric": METRIC, "value": fp64["value"], "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": fp64["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
             "config": {"workload": f"C2 layer-over-halfspace {n}^3 h=50, FP64, fused time step",
-                       "grid": [n, n, n], "mode": args.mode, "dt": dt,
+                       "grid": [n, n, n], "mode": args.mode, "dt": cfl_dt(c2_config(n)),
                        "l2": "inputs larger than L2 (3.3 GB per field), no flush",
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": {"bound": "hbm", "kernel": "fused corrector stage", "achieved": achieved,
@@ -349,14 +399,14 @@ def run_ours(args, rank, world):
                           "frac": fp64_equiv / fp64_peak,
                           "basis": f"{CORR_STAGE_REF_FLOPS} reference flops per point "
                                    "(rhs4sg 666 + addsgd4 375 + update 23)"},
-            "kernel_ms": prof,
-            "clocks": clocks.summary(),
-            "e2e": e2e,
-            "gpu_launches": ew.launches_per_step(mode) * args.steps,
+            "kernel_ms": fp64["kernel_ms"],
+            "clocks": fp64["clocks"],
+            "e2e": fp64.get("e2e"),
+            "gpu_launches": fp64["gpu_launches"],
             "cpu_baseline": cpu,
+            "mixed": mixed,
         }
         print(json.dumps(line), flush=True)
-    ew.close()
     return 0
 
 
@@ -373,6 +423,10 @@ def main():
                     help="minimum CPU work of the baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the FP32-mixed form")
+    ap.add_argument("--no-err", action="store_true", help="skip the mixed-vs-FP64 error run")
+    ap.add_argument("--err-n", type=int, default=256, help="grid of the mixed-vs-FP64 error run")
+    ap.add_argument("--err-steps", type=int, default=1000, help="steps of the error run")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -164,6 +164,10 @@ typedef struct {
    double sg_damping; /* supergrid damping coefficient (reference default 0.02) */
    int sg_order;      /* damping order, 4 or 6 */
    int soa;           /* must be 1 for the time loop */
+   int precision;     /* 0: FP64 throughout.  1: FP32-mixed form -- FP32 fields-in-
+                         stencil and material, double-float (FP32 compensated)
+                         time-level accumulation, FP64 one-sided SBP rows,
+                         free-surface solve and forcing */
 } sw4g_grid;
 
 /* Supergrid profiles along one axis of g (0 x, 1 y, 2 z) over the array index

@@ -32,7 +32,8 @@ class GridDesc(C.Structure):
     """sw4g_grid (include/sw4g.h)."""
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("h", C.c_double),
                 ("zmin", C.c_double), ("bc", C.c_int * 6), ("sg_gp", C.c_int),
-                ("sg_damping", C.c_double), ("sg_order", C.c_int), ("soa", C.c_int)]
+                ("sg_damping", C.c_double), ("sg_order", C.c_int), ("soa", C.c_int),
+                ("precision", C.c_int)]
 
 
 class SourceDesc(C.Structure):
@@ -135,13 +136,17 @@ def stencil_coefficients():
     return acof, ghcof, bope, sbop
 
 
+FP64, MIXED = 0, 1
+
+
 def grid_desc(nx, ny, nz, h, bc=(SUPERGRID,) * 4 + (FREE, SUPERGRID), zmin=0.0, sg_gp=20,
-              sg_damping=0.02, sg_order=4, soa=1) -> GridDesc:
+              sg_damping=0.02, sg_order=4, soa=1, precision=FP64) -> GridDesc:
     g = GridDesc()
     g.nx, g.ny, g.nz, g.h, g.zmin = nx, ny, nz, h, zmin
     for s in range(6):
         g.bc[s] = int(bc[s])
     g.sg_gp, g.sg_damping, g.sg_order, g.soa = sg_gp, sg_damping, sg_order, soa
+    g.precision = precision
     return g
 
 

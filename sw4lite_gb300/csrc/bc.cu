@@ -19,8 +19,8 @@ struct Win {
    int i0, i1, j0, j1, k0, k1;
 };
 
-__global__ void fill_window_kernel(Box b, Win w, double* __restrict__ u,
-                                   const double* __restrict__ bforce)
+template <class Field>
+__global__ void fill_window_kernel(Box b, Win w, Field u, const double* __restrict__ bforce)
 {
    const long long idel = w.i1 - w.i0 + 1, ijdel = idel * (w.j1 - w.j0 + 1);
    const long long n = ijdel * (w.k1 - w.k0 + 1);
@@ -31,12 +31,12 @@ __global__ void fill_window_kernel(Box b, Win w, double* __restrict__ u,
       const int j = w.j0 + (int)(r / idel);
       const int i = w.i0 + (int)(r % idel);
 #pragma unroll
-      for (int c = 0; c < 3; c++) u[cidx(b, c, i, j, k)] = bforce ? bforce[3 * q + c] : 0.0;
+      for (int c = 0; c < 3; c++) u.set(cidx(b, c, i, j, k), bforce ? bforce[3 * q + c] : 0.0);
    }
 }
 
-__global__ void periodic_window_kernel(Box b, Win w, double* __restrict__ u, int di, int dj,
-                                       int dk)
+template <class Field>
+__global__ void periodic_window_kernel(Box b, Win w, Field u, int di, int dj, int dk)
 {
    const long long idel = w.i1 - w.i0 + 1, ijdel = idel * (w.j1 - w.j0 + 1);
    const long long n = ijdel * (w.k1 - w.k0 + 1);
@@ -47,7 +47,7 @@ __global__ void periodic_window_kernel(Box b, Win w, double* __restrict__ u, int
       const int j = w.j0 + (int)(r / idel);
       const int i = w.i0 + (int)(r % idel);
 #pragma unroll
-      for (int c = 0; c < 3; c++) u[cidx(b, c, i, j, k)] = u[cidx(b, c, i + di, j + dj, k + dk)];
+      for (int c = 0; c < 3; c++) u.set(cidx(b, c, i, j, k), u.get(cidx(b, c, i + di, j + dj, k + dk)));
    }
 }
 
@@ -56,7 +56,8 @@ struct FreeSurf {
 };
 
 // Ghost plane of a flat free surface (src/ew-cfromfort.C:415-476, :686-744).
-__global__ void free_surface_kernel(Box b, double* __restrict__ u, const double* __restrict__ mu,
+template <class Field>
+__global__ void free_surface_kernel(Box b, Field u, const double* __restrict__ mu,
                                     const double* __restrict__ la,
                                     const double* __restrict__ bforce,
                                     const double* __restrict__ strx,
@@ -69,7 +70,7 @@ __global__ void free_surface_kernel(Box b, double* __restrict__ u, const double*
    const double d4a = 2.0 / 3.0, d4b = -1.0 / 12.0;
    const long long qq = (i - b.ib) + b.ni * (j - b.jb);
    const long long p = pidx(b, i, j, k);
-   auto U = [&](int c, int ii, int jj, int kk) { return u[cidx(b, c, ii, jj, kk)]; };
+   auto U = [&](int c, int ii, int jj, int kk) { return u.get(cidx(b, c, ii, jj, kk)); };
    const double sx = strx[i - b.ib], sy = stry[j - b.jb];
    const double wx = sx * (d4a * (U(2, i + 1, j, k) - U(2, i - 1, j, k)) +
                            d4b * (U(2, i + 2, j, k) - U(2, i - 2, j, k)));
@@ -91,9 +92,9 @@ __global__ void free_surface_kernel(Box b, double* __restrict__ u, const double*
    const double f1 = bforce ? bforce[3 * qq + 1] : 0.0;
    const double f2 = bforce ? bforce[3 * qq + 2] : 0.0;
    const double m = mu[p], l = la[p];
-   u[cidx(b, 0, i, j, k - kl)] = (-uz - kl * wx + kl * h * f0 / m) / fs.sbop[0];
-   u[cidx(b, 1, i, j, k - kl)] = (-vz - kl * wy + kl * h * f1 / m) / fs.sbop[0];
-   u[cidx(b, 2, i, j, k - kl)] = (-wz + (-kl * l * (ux + vy) + kl * h * f2) / (2 * m + l)) / fs.sbop[0];
+   u.set(cidx(b, 0, i, j, k - kl), (-uz - kl * wx + kl * h * f0 / m) / fs.sbop[0]);
+   u.set(cidx(b, 1, i, j, k - kl), (-vz - kl * wy + kl * h * f1 / m) / fs.sbop[0]);
+   u.set(cidx(b, 2, i, j, k - kl), (-wz + (-kl * l * (ux + vy) + kl * h * f2) / (2 * m + l)) / fs.sbop[0]);
 }
 
 int small_grid(long long n)
@@ -105,8 +106,9 @@ int small_grid(long long n)
 
 }  // namespace
 
-int launch_bcfortsg(int soa, int ib, int ie, int jb, int je, int kb, int ke, const int wind[36],
-                    int nx, int ny, int nz, double* u, double h, const int bccnd[6],
+template <class Field>
+int bc_sides(int soa, int ib, int ie, int jb, int je, int kb, int ke, const int wind[36],
+             int nx, int ny, int nz, Field u, double h, const int bccnd[6],
                     const double sbop[5], const double* mu, const double* la,
                     const double* const bforce[6], const double* strx, const double* stry,
                     cudaStream_t s)
@@ -140,6 +142,26 @@ int launch_bcfortsg(int soa, int ib, int ie, int jb, int je, int kb, int ke, con
       }
    }
    return launch_status();
+}
+
+int launch_bcfortsg(int soa, int ib, int ie, int jb, int je, int kb, int ke, const int wind[36],
+                    int nx, int ny, int nz, double* u, double h, const int bccnd[6],
+                    const double sbop[5], const double* mu, const double* la,
+                    const double* const bforce[6], const double* strx, const double* stry,
+                    cudaStream_t s)
+{
+   return bc_sides(soa, ib, ie, jb, je, kb, ke, wind, nx, ny, nz, F64Field{u}, h, bccnd, sbop, mu,
+                   la, bforce, strx, stry, s);
+}
+
+int launch_bcfortsg_df(int ib, int ie, int jb, int je, int kb, int ke, const int wind[36], int nx,
+                       int ny, int nz, float* uh, double h, const int bccnd[6], const double sbop[5],
+                       const double* mu, const double* la, const double* strx, const double* stry,
+                       cudaStream_t s)
+{
+   const Box b = make_box(1, ib, ie, jb, je, kb, ke);
+   return bc_sides(1, ib, ie, jb, je, kb, ke, wind, nx, ny, nz, DFField{uh, 3 * b.npts}, h, bccnd,
+                   sbop, mu, la, nullptr, strx, stry, s);
 }
 
 }  // namespace sw4g

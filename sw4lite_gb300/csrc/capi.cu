@@ -37,6 +37,7 @@ GridSpec to_spec(const sw4g_grid* g)
    s.sg_damping = g->sg_damping;
    s.sg_order = g->sg_order;
    s.soa = g->soa;
+   s.precision = g->precision;
    return s;
 }
 
@@ -202,7 +203,7 @@ int sw4g_pred_rows(int ifirst, int ilast, int jfirst, int jlast, int kfirst, int
    const Box b = make_box(1, ifirst, ilast, jfirst, jlast, kfirst, klast);
    const double* none[3] = {strx, stry, strz};
    return launch_stage_rows(0, side == 0, b, nz, u, b, mu, lambda, h, strx, stry, strz, u, um,
-                            nullptr, out, rho, nullptr, dt * dt, 0.0, none, none, none,
+                            nullptr, out, rho, nullptr, dt * dt, 0.0, none, none, none, nullptr,
                             as_stream(stream));
 }
 
@@ -229,7 +230,7 @@ int sw4g_corr_rows(int ifirst, int ilast, int jfirst, int jlast, int kfirst, int
    const double* sv[3] = {strx, stry, strz};
    const double* co[3] = {cox, coy, coz};
    return launch_stage_rows(1, side == 0, b, nz, scratch, sb, mu, lambda, h, strx, stry, strz, u,
-                            um, up, out, rho, nullptr, dt * dt / 12, beta, dc, sv, co,
+                            um, up, out, rho, nullptr, dt * dt / 12, beta, dc, sv, co, nullptr,
                             as_stream(stream));
 }
 

@@ -41,6 +41,30 @@ __host__ __device__ __forceinline__ long long cidx(const Box& b, int c, int i, i
    return c * b.cs + b.ps * pidx(b, i, j, k);
 }
 
+// Field accessors for the kernels that run in FP64 arithmetic whatever the
+// storage: plain FP64 arrays, or the mixed form's double-float pairs (hi at q,
+// lo at q + lo_offset; see df.cuh).
+struct F64Field {
+   double* p;
+   __device__ __forceinline__ double get(long long q) const { return p[q]; }
+   __device__ __forceinline__ void set(long long q, double v) const { p[q] = v; }
+};
+
+struct DFField {
+   float* h;
+   long long lo;  // offset of the lo half
+   __device__ __forceinline__ double get(long long q) const
+   {
+      return (double)h[q] + (double)h[q + lo];
+   }
+   __device__ __forceinline__ void set(long long q, double v) const
+   {
+      const float a = __double2float_rn(v);
+      h[q] = a;
+      h[q + lo] = __double2float_rn(v - (double)a);
+   }
+};
+
 // Status codes returned through the C ABI (include/sw4g.h).
 enum Status : int {
    kOk = 0,

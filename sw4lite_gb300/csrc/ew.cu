@@ -35,7 +35,16 @@ EW::~EW()
    f(f_);
    f(uacc_);
    f(slab_);
+   f(zc_[0]);
+   f(zc_[1]);
    f(dsrc_mem_);
+   f(rho32_);
+   f(mu32_);
+   f(la32_);
+   f(irho32_);
+   f(wdf_);
+   for (auto* p : prof32_) f(p);
+   f(staging_);
 }
 
 int EW::init()
@@ -48,6 +57,9 @@ int EW::init()
       if (t == kStressFree && s < 4) return kNotSupported;
    }
    if (g_.sg_order != 4 && g_.sg_order != 6) return kBadArgument;
+   if (g_.precision != 0 && g_.precision != 1) return kBadArgument;
+   mixed_ = g_.precision == 1;
+   if (mixed_ && g_.sg_order != 4) return kNotSupported;
    if ((g_.bc[4] == kStressFree && g_.nz < 14) || (g_.bc[5] == kStressFree && g_.nz < 14))
       return kBadArgument;  // the one-sided rows need 8 interior planes on each such side
    b_ = grid_bounds(g_);
@@ -63,8 +75,22 @@ int EW::init()
    SW4G_TRY(cuda_ok(cudaMalloc(&mu_, n * sizeof(double))));
    SW4G_TRY(cuda_ok(cudaMalloc(&la_, n * sizeof(double))));
    SW4G_TRY(cuda_ok(cudaMalloc(&irho_, n * sizeof(double))));
-   SW4G_TRY(cuda_ok(cudaMalloc(&wstore_, kWeightArrays * n * sizeof(double))));
-   for (int q = 0; q < kWeightArrays; q++) w_.p[q] = wstore_ + q * n;
+   if (!mixed_) {
+      SW4G_TRY(cuda_ok(cudaMalloc(&wstore_, kWeightArrays * n * sizeof(double))));
+      for (int q = 0; q < kWeightArrays; q++) w_.p[q] = wstore_ + q * n;
+   } else {
+      SW4G_TRY(cuda_ok(cudaMalloc(&rho32_, n * sizeof(float))));
+      SW4G_TRY(cuda_ok(cudaMalloc(&mu32_, 2 * n * sizeof(float))));
+      SW4G_TRY(cuda_ok(cudaMalloc(&la32_, 2 * n * sizeof(float))));
+      SW4G_TRY(cuda_ok(cudaMalloc(&irho32_, 2 * n * sizeof(float))));
+      SW4G_TRY(cuda_ok(cudaMalloc(&wdf_, 2 * kWeightArrays * n * sizeof(float))));
+      for (int q = 0; q < kWeightArrays; q++) {
+         wd_.h[q] = wdf_ + (2 * q) * n;
+         wd_.l[q] = wdf_ + (2 * q + 1) * n;
+      }
+   }
+   // a level holds 3*npts doubles, or in the mixed form 3*npts hi + 3*npts lo floats
+   // (the same bytes)
    for (int q = 0; q < 4; q++) {
       SW4G_TRY(cuda_ok(cudaMalloc(&lev_[q], 3 * n * sizeof(double))));
       SW4G_TRY(cuda_ok(cudaMemsetAsync(lev_[q], 0, 3 * n * sizeof(double), stream_)));
@@ -76,6 +102,11 @@ int EW::init()
          SW4G_TRY(cuda_ok(cudaMalloc(&d, len[ax] * sizeof(double))));
          const std::vector<double>& src = w == 0 ? prof_.dc[ax] : w == 1 ? prof_.str[ax] : prof_.co[ax];
          SW4G_TRY(cuda_ok(cudaMemcpy(d, src.data(), len[ax] * sizeof(double), cudaMemcpyHostToDevice)));
+         if (mixed_) {
+            float*& d32 = prof32_[3 * w + ax];
+            SW4G_TRY(cuda_ok(cudaMalloc(&d32, len[ax] * sizeof(float))));
+            SW4G_TRY(launch_to_f32(len[ax], d, d32, stream_));
+         }
       }
    // slab for the corrector's stage field on the one-sided rows: planes kb..8
    // (top) or nz-7..ke (bottom)
@@ -83,6 +114,12 @@ int EW::init()
    slab_len_ = 3 * nij * 10;
    if (onesided_[4] || onesided_[5])
       SW4G_TRY(cuda_ok(cudaMalloc(&slab_, 2 * slab_len_ * sizeof(double))));
+   {
+      const Box bx = make_box(1, b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke);
+      for (int side = 0; side < 2; side++)
+         if (onesided_[4 + side])
+            SW4G_TRY(cuda_ok(cudaMalloc(&zc_[side], zcoef_len(bx) * sizeof(double))));
+   }
    SW4G_TRY(upload_sbp_tables_direct());
    SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
    ready_ = true;
@@ -105,7 +142,17 @@ int EW::set_material(const double* rho, const double* mu, const double* la, bool
    SW4G_TRY(cuda_ok(cudaMemcpyAsync(la_, la, bytes, kind, stream_)));
    SW4G_TRY(launch_inverse(npts_, rho_, irho_, stream_));
    Box b = make_box(1, b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke);
-   SW4G_TRY(launch_weights(b, mu_, la_, dprof_[3], dprof_[4], dprof_[5], g_.h, w_, stream_));
+   for (int side = 0; side < 2; side++)
+      if (zc_[side]) SW4G_TRY(launch_zcoef(b, g_.nz, side == 0, mu_, la_, zc_[side], stream_));
+   if (!mixed_) {
+      SW4G_TRY(launch_weights(b, mu_, la_, dprof_[3], dprof_[4], dprof_[5], g_.h, w_, stream_));
+   } else {
+      SW4G_TRY(launch_to_f32(npts_, rho_, rho32_, stream_));
+      SW4G_TRY(launch_df_from_f64(npts_, mu_, mu32_, mu32_ + npts_, stream_));
+      SW4G_TRY(launch_df_from_f64(npts_, la_, la32_, la32_ + npts_, stream_));
+      SW4G_TRY(launch_df_from_f64(npts_, irho_, irho32_, irho32_ + npts_, stream_));
+      SW4G_TRY(launch_weights_df(b, mu_, la_, dprof_[3], dprof_[4], dprof_[5], wd_, stream_));
+   }
    SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
    material_ = true;
    return kOk;
@@ -227,13 +274,35 @@ int EW::compute_time_step(double cfl, double tmax, double* dt, int* nsteps)
    return kOk;
 }
 
+int EW::ensure_staging()
+{
+   if (staging_) return kOk;
+   return cuda_ok(cudaMalloc(&staging_, 3 * (size_t)npts_ * sizeof(double)));
+}
+
 int EW::set_fields(const double* u, const double* um, bool on_device)
 {
    if (!ready_ || !u || !um) return kBadArgument;
    const size_t bytes = 3 * (size_t)npts_ * sizeof(double);
    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-   SW4G_TRY(cuda_ok(cudaMemcpyAsync(lev_[iu_], u, bytes, kind, stream_)));
-   SW4G_TRY(cuda_ok(cudaMemcpyAsync(lev_[ium_], um, bytes, kind, stream_)));
+   if (!mixed_) {
+      SW4G_TRY(cuda_ok(cudaMemcpyAsync(lev_[iu_], u, bytes, kind, stream_)));
+      SW4G_TRY(cuda_ok(cudaMemcpyAsync(lev_[ium_], um, bytes, kind, stream_)));
+      return kOk;
+   }
+   const long long n3 = 3 * npts_;
+   const double* src[2] = {u, um};
+   const int dst[2] = {iu_, ium_};
+   for (int q = 0; q < 2; q++) {
+      const double* from = src[q];
+      if (!on_device) {
+         SW4G_TRY(ensure_staging());
+         SW4G_TRY(cuda_ok(cudaMemcpyAsync(staging_, src[q], bytes, kind, stream_)));
+         from = staging_;
+      }
+      float* h = reinterpret_cast<float*>(lev_[dst[q]]);
+      SW4G_TRY(launch_df_from_f64(n3, from, h, h + n3, stream_));
+   }
    return kOk;
 }
 
@@ -242,14 +311,32 @@ int EW::get_fields(double* u, double* um, bool on_device) const
    if (!ready_) return kBadArgument;
    const size_t bytes = 3 * (size_t)npts_ * sizeof(double);
    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-   if (u) SW4G_TRY(cuda_ok(cudaMemcpyAsync(u, lev_[iu_], bytes, kind, stream_)));
-   if (um) SW4G_TRY(cuda_ok(cudaMemcpyAsync(um, lev_[ium_], bytes, kind, stream_)));
+   if (!mixed_) {
+      if (u) SW4G_TRY(cuda_ok(cudaMemcpyAsync(u, lev_[iu_], bytes, kind, stream_)));
+      if (um) SW4G_TRY(cuda_ok(cudaMemcpyAsync(um, lev_[ium_], bytes, kind, stream_)));
+   } else {
+      const long long n3 = 3 * npts_;
+      double* dst[2] = {u, um};
+      const int srcl[2] = {iu_, ium_};
+      for (int q = 0; q < 2; q++) {
+         if (!dst[q]) continue;
+         const float* h = reinterpret_cast<const float*>(lev_[srcl[q]]);
+         if (on_device) {
+            SW4G_TRY(launch_df_to_f64(n3, h, h + n3, dst[q], stream_));
+         } else {
+            SW4G_TRY(const_cast<EW*>(this)->ensure_staging());
+            SW4G_TRY(launch_df_to_f64(n3, h, h + n3, staging_, stream_));
+            SW4G_TRY(cuda_ok(cudaMemcpyAsync(dst[q], staging_, bytes, kind, stream_)));
+         }
+      }
+   }
    if (!on_device) SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
    return kOk;
 }
 
 int EW::enforce_bc(double* u)
 {
+   if (mixed_) return kNotSupported;  // levels are double-float pairs in the mixed form
    return launch_bcfortsg(1, b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke, wind_, g_.nx, g_.ny, g_.nz,
                           u, g_.h, g_.bc, sbop_, mu_, la_, nullptr, dprof_[3], dprof_[4], stream_);
 }
@@ -272,6 +359,7 @@ int EW::step(int nsteps, int mode)
    if (mode != kModePhases && mode != kModeFused) return kBadArgument;
    SW4G_TRY(upload_sources());
    if (mode == kModePhases) SW4G_TRY(ensure_phase_arrays());
+   if (mixed_ && mode == kModePhases) return kNotSupported;
    for (int n = 0; n < nsteps; n++) SW4G_TRY(mode == kModePhases ? step_phases() : step_fused());
    return kOk;
 }
@@ -363,7 +451,8 @@ int EW::fused_piece(int piece, int ip, int iq)
       for (int side = 0; side < 2; side++)
          if (onesided_[4 + side])
             SW4G_TRY(launch_stage_rows(0, side == 0, b, nz, u, b, mu_, la_, g_.h, st[0], st[1], st[2],
-                                       u, um, nullptr, up, rho_, irho_, dt2, 0.0, dc, st, co, stream_));
+                                       u, um, nullptr, up, rho_, irho_, dt2, 0.0, dc, st, co,
+                                       zc_[side], stream_));
       return kOk;
    }
    if (piece == 2) {
@@ -381,7 +470,7 @@ int EW::fused_piece(int piece, int ip, int iq)
          Box sb = make_box(1, bd.ib, bd.ie, bd.jb, bd.je, k0, k1);
          SW4G_TRY(launch_stage_rows(1, side == 0, b, nz, slab, sb, mu_, la_, g_.h, st[0], st[1],
                                     st[2], u, um, up, out, rho_, irho_, dt2 / 12, beta4, dc, st, co,
-                                    stream_));
+                                    zc_[side], stream_));
       }
       if (beta != 0 && g_.sg_order == 6)
          SW4G_TRY(launch_addsgd(6, 1, bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, out, u, um, rho_,
@@ -397,13 +486,104 @@ int EW::fused_piece(int piece, int ip, int iq)
    return kBadArgument;
 }
 
+// The same six pieces for the FP32-mixed form: double-float levels, FP32 interior
+// stage kernels, FP64 one-sided rows / free surface / forcing.
+int EW::mixed_piece(int piece, int ip, int iq)
+{
+   const Bounds& bd = b_;
+   Box b = make_box(1, bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke);
+   float* up = reinterpret_cast<float*>(lev_[ip]);
+   float* out = reinterpret_cast<float*>(lev_[iq]);
+   const float* u = reinterpret_cast<const float*>(lev_[iu_]);
+   const float* um = reinterpret_cast<const float*>(lev_[ium_]);
+   const double dt = dt_, dt2 = dt * dt;
+   const int nz = g_.nz;
+   const double beta = (prof_.used && g_.sg_damping != 0) ? g_.sg_damping : 0.0;
+   const double* dc[3] = {dprof_[0], dprof_[1], dprof_[2]};
+   const double* st[3] = {dprof_[3], dprof_[4], dprof_[5]};
+   const double* co[3] = {dprof_[6], dprof_[7], dprof_[8]};
+   if (piece == 0 || piece == 3) {
+      MixedStage ms;
+      ms.b = b;
+      ms.k1 = onesided_[4] ? 7 : 1;
+      ms.k2 = onesided_[5] ? nz - 6 : nz;
+      ms.muh = mu32_;
+      ms.mul = mu32_ + npts_;
+      ms.lah = la32_;
+      ms.lal = la32_ + npts_;
+      ms.irh = irho32_;
+      ms.irl = irho32_ + npts_;
+      ms.rho = rho32_;
+      for (int q = 0; q < kWeightArrays; q++) {
+         ms.wh[q] = wd_.h[q];
+         ms.wl[q] = wd_.l[q];
+      }
+      for (int q = 0; q < 3; q++) {
+         ms.dc[q] = prof32_[q];
+         ms.st[q] = prof32_[3 + q];
+         ms.co[q] = prof32_[6 + q];
+      }
+      ms.h = g_.h;
+      ms.dt = dt;
+      ms.u = u;
+      ms.um = um;
+      if (piece == 0) {
+         ms.corrector = 0;
+         ms.out = up;
+         ms.beta = 0;
+      } else {
+         ms.corrector = 1;
+         ms.up = up;
+         ms.out = out;
+         ms.beta = beta;
+      }
+      return launch_mixed_stage(ms, stream_);
+   }
+   if (piece == 1) {
+      SW4G_TRY(launch_ghost_shell_df(b, 0, up, u, um, nullptr, stream_));
+      for (int side = 0; side < 2; side++)
+         if (onesided_[4 + side])
+            SW4G_TRY(launch_stage_rows_df(0, side == 0, b, nz, nullptr, u, b, mu_, la_, g_.h, st[0],
+                                          st[1], st[2], u, um, nullptr, up, rho_, irho_, dt2, 0.0,
+                                          dc, st, co, zc_[side], stream_));
+      return kOk;
+   }
+   if (piece == 2) {
+      SW4G_TRY(launch_force_update_df(bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, up, rho_, dsrc_, t_,
+                                      0, dt2, stream_));
+      return launch_bcfortsg_df(bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, wind_, g_.nx, g_.ny, g_.nz,
+                                up, g_.h, g_.bc, sbop_, mu_, la_, dprof_[3], dprof_[4], stream_);
+   }
+   if (piece == 4) {
+      SW4G_TRY(launch_ghost_shell_df(b, 1, out, u, um, up, stream_));
+      for (int side = 0; side < 2; side++) {
+         if (!onesided_[4 + side]) continue;
+         const int k0 = side == 0 ? bd.kb : nz - 7, k1 = side == 0 ? 8 : bd.ke;
+         double* slab = slab_ + side * slab_len_;
+         SW4G_TRY(launch_uacc_slab_df(b, k0, k1, up, u, um, slab, stream_));
+         Box sb = make_box(1, bd.ib, bd.ie, bd.jb, bd.je, k0, k1);
+         SW4G_TRY(launch_stage_rows_df(1, side == 0, b, nz, slab, nullptr, sb, mu_, la_, g_.h, st[0],
+                                       st[1], st[2], u, um, up, out, rho_, irho_, dt2 / 12, beta,
+                                       dc, st, co, zc_[side], stream_));
+      }
+      return kOk;
+   }
+   if (piece == 5) {
+      SW4G_TRY(launch_force_update_df(bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, out, rho_, dsrc_, t_,
+                                      1, dt2 * dt2 / 12, stream_));
+      return launch_bcfortsg_df(bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, wind_, g_.nx, g_.ny, g_.nz,
+                                out, g_.h, g_.bc, sbop_, mu_, la_, dprof_[3], dprof_[4], stream_);
+   }
+   return kBadArgument;
+}
+
 int EW::step_fused()
 {
    int ip = 0;
    while (ip == iu_ || ip == ium_) ip++;
    int iq = ip + 1;
    while (iq == iu_ || iq == ium_) iq++;
-   for (int piece = 0; piece < 6; piece++) SW4G_TRY(fused_piece(piece, ip, iq));
+   for (int which = 0; which < 6; which++) SW4G_TRY(piece(which, ip, iq));
    ium_ = iu_;
    iu_ = iq;
    t_ += dt_;
@@ -419,7 +599,7 @@ int EW::profile_kernels(int nrep, double ms[4])
    int iq = ip + 1;
    while (iq == iu_ || iq == ium_) iq++;
    // one full fused step's pieces first, so every input level holds valid data
-   for (int piece = 0; piece < 6; piece++) SW4G_TRY(fused_piece(piece, ip, iq));
+   for (int which = 0; which < 6; which++) SW4G_TRY(piece(which, ip, iq));
    const int groups[4][2] = {{0, -1}, {3, -1}, {1, 4}, {2, 5}};
    cudaEvent_t e0, e1;
    SW4G_TRY(cuda_ok(cudaEventCreate(&e0)));
@@ -429,7 +609,7 @@ int EW::profile_kernels(int nrep, double ms[4])
       cudaEventRecord(e0, stream_);
       for (int r = 0; r < nrep && status == kOk; r++)
          for (int q = 0; q < 2 && status == kOk; q++)
-            if (groups[g][q] >= 0) status = fused_piece(groups[g][q], ip, iq);
+            if (groups[g][q] >= 0) status = piece(groups[g][q], ip, iq);
       cudaEventRecord(e1, stream_);
       if (cudaEventSynchronize(e1) != cudaSuccess) status = kCudaError;
       float t = 0;

@@ -75,6 +75,9 @@ class EW {
    int step_phases();
    int step_fused();
    int fused_piece(int piece, int ip, int iq);
+   int mixed_piece(int piece, int ip, int iq);
+   int piece(int which, int ip, int iq) { return mixed_ ? mixed_piece(which, ip, iq) : fused_piece(which, ip, iq); }
+   int ensure_staging();
    int ensure_phase_arrays();
 
    GridSpec g_;
@@ -86,6 +89,15 @@ class EW {
    double sbop_[5] = {};
    SupergridProfiles prof_;
 
+   bool mixed_ = false;
+   float* rho32_ = nullptr;  // mixed form: FP32 rho and profiles, (hi, lo) pairs of
+   float* mu32_ = nullptr;   // mu, lambda, 1/rho (2*npts floats each) and of the
+   float* la32_ = nullptr;   // second-difference weights
+   float* irho32_ = nullptr;
+   float* wdf_ = nullptr;
+   WeightPtrsDF wd_{};
+   float* prof32_[9] = {};
+   double* staging_ = nullptr;  // FP64 buffer for converting the mixed form's levels
    double* rho_ = nullptr;
    double* mu_ = nullptr;
    double* la_ = nullptr;
@@ -98,6 +110,7 @@ class EW {
    double* lu_ = nullptr;   // phase mode work arrays
    double* f_ = nullptr;
    double* uacc_ = nullptr;
+   double* zc_[2] = {nullptr, nullptr};  // SBP z coefficients of the top / bottom rows
    double* slab_ = nullptr; // corrector stage field on the one-sided rows
    long long slab_len_ = 0;
 

@@ -94,7 +94,40 @@ __global__ void force_update_kernel(Box b, S* __restrict__ up, const double* __r
    }
 }
 
+// Same as force_update_kernel for a double-float level: the add runs in FP64.
+__global__ void force_update_df_kernel(Box b, DFField up, const double* __restrict__ rho,
+                                       SourceSet src, double t, int tt, double coef)
+{
+   const int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= src.npoints) return;
+   double acc[3] = {0, 0, 0};
+   for (int s = src.start[r]; s < src.start[r + 1]; s++) {
+      const double g = timefunc(src.kind[s], src.freq[s], t - src.t0[s], tt != 0);
+      acc[0] += src.amp[3 * s] * g;
+      acc[1] += src.amp[3 * s + 1] * g;
+      acc[2] += src.amp[3 * s + 2] * g;
+   }
+   const int s0 = src.start[r];
+   const int i = src.ijk[3 * s0], j = src.ijk[3 * s0 + 1], k = src.ijk[3 * s0 + 2];
+   const double c0 = coef / rho[pidx(b, i, j, k)];
+   for (int c = 0; c < 3; c++) {
+      const long long q = cidx(b, c, i, j, k);
+      up.set(q, up.get(q) + c0 * acc[c]);
+   }
+}
+
 }  // namespace
+
+int launch_force_update_df(int ib, int ie, int jb, int je, int kb, int ke, float* uph,
+                           const double* rho, const SourceSet& src, double t, int tt, double coef,
+                           cudaStream_t s)
+{
+   if (src.npoints == 0) return kOk;
+   Box b = make_box(1, ib, ie, jb, je, kb, ke);
+   force_update_df_kernel<<<blocks_for(src.npoints, 128), 128, 0, s>>>(b, DFField{uph, 3 * b.npts},
+                                                                      rho, src, t, tt, coef);
+   return launch_status();
+}
 
 int launch_force_dense(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* f,
                        const SourceSet& src, double t, int tt, cudaStream_t s)

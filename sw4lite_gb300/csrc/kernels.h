@@ -36,6 +36,36 @@ struct FusedStage {
    double h = 1, dt = 0, beta = 0;
 };
 
+struct WeightPtrsDF {
+   float* h[kWeightArrays];
+   float* l[kWeightArrays];
+};
+
+// One mixed-form stage launch (stage_mixed.cu): double-float levels (hi at
+// [c*npts+p], lo 3*npts further), FP32 material and profiles.
+struct MixedStage {
+   Box b;
+   int k1 = 0, k2 = -1;
+   int corrector = 0;
+   const float* u = nullptr;
+   const float* um = nullptr;
+   const float* up = nullptr;
+   float* out = nullptr;
+   const float* muh = nullptr;  // (hi, lo) pairs of mu, lambda and 1/rho
+   const float* mul = nullptr;
+   const float* lah = nullptr;
+   const float* lal = nullptr;
+   const float* irh = nullptr;
+   const float* irl = nullptr;
+   const float* rho = nullptr;
+   const float* wh[kWeightArrays] = {};
+   const float* wl[kWeightArrays] = {};
+   const float* st[3] = {nullptr, nullptr, nullptr};
+   const float* dc[3] = {nullptr, nullptr, nullptr};
+   const float* co[3] = {nullptr, nullptr, nullptr};
+   double h = 1, dt = 0, beta = 0;
+};
+
 // Device-resident grid-point sources grouped by grid point: the sources of point
 // r are [start[r], start[r+1]); all share ijk[3*start[r] .. +2].
 struct SourceSet {
@@ -92,6 +122,31 @@ int launch_force_update_f32(int soa, int ib, int ie, int jb, int je, int kb, int
 
 int fma_peak(int precision, double* tflops, cudaStream_t s);
 
+int launch_mixed_stage(const MixedStage& st, cudaStream_t stream);
+int launch_df_from_f64(long long n, const double* x, float* h, float* l, cudaStream_t s);
+int launch_df_to_f64(long long n, const float* h, const float* l, double* x, cudaStream_t s);
+int launch_to_f32(long long n, const double* x, float* y, cudaStream_t s);
+int launch_weights_df(const Box& b, const double* mu, const double* la, const double* sx,
+                      const double* sy, const double* sz, WeightPtrsDF w, cudaStream_t s);
+int launch_force_update_df(int ib, int ie, int jb, int je, int kb, int ke, float* uph,
+                           const double* rho, const SourceSet& src, double t, int tt, double coef,
+                           cudaStream_t s);
+int launch_ghost_shell_df(const Box& b, int corrector, float* out, const float* u, const float* um,
+                          const float* up, cudaStream_t s);
+int launch_uacc_slab_df(const Box& b, int k0, int k1, const float* up, const float* u,
+                        const float* um, double* out, cudaStream_t s);
+int launch_bcfortsg_df(int ib, int ie, int jb, int je, int kb, int ke, const int wind[36], int nx,
+                       int ny, int nz, float* uh, double h, const int bccnd[6], const double sbop[5],
+                       const double* mu, const double* la, const double* strx, const double* stry,
+                       cudaStream_t s);
+int launch_stage_rows_df(int corrector, bool top, const Box& b, int nz, const double* field_f64,
+                         const float* field_df, const Box& field_box, const double* mu,
+                         const double* la, double h, const double* strx, const double* stry,
+                         const double* strz, const float* u, const float* um, const float* up,
+                         float* out, const double* rho, const double* irho, double coef,
+                         double beta, const double* const dc[3], const double* const st[3],
+                         const double* const co[3], const double* zc, cudaStream_t stream);
+
 int launch_weights(const Box& b, const double* mu, const double* la, const double* sx,
                    const double* sy, const double* sz, double h, WeightPtrs w, cudaStream_t s);
 int launch_inverse(long long n, const double* x, double* y, cudaStream_t s);
@@ -104,6 +159,9 @@ int launch_stage_rows(int corrector, bool top, const Box& b, int nk, const doubl
                       const double* u, const double* um, const double* up, double* out,
                       const double* rho, const double* irho, double coef, double beta,
                       const double* const dc[3], const double* const st[3],
-                      const double* const co[3], cudaStream_t stream);
+                      const double* const co[3], const double* zc, cudaStream_t stream);
+long long zcoef_len(const Box& b);
+int launch_zcoef(const Box& b, int nk, bool top, const double* mu, const double* la, double* zc,
+                 cudaStream_t s);
 
 }  // namespace sw4g

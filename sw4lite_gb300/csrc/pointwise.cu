@@ -151,9 +151,8 @@ __global__ void __launch_bounds__(256) addsgd6_kernel(SgArgs a)
 // (src/ew-cfromfort.C:40-114): predictor out = 2u - um, corrector out = up.
 // Points are enumerated as the 4 outer k-planes, then the 4 outer j-rows of the
 // inner planes, then the 4 outer i-columns of the inner rows.
-__global__ void ghost_shell_kernel(Box b, int corrector, double* __restrict__ out,
-                                   const double* __restrict__ u, const double* __restrict__ um,
-                                   const double* __restrict__ up)
+template <class Field>
+__global__ void ghost_shell_kernel(Box b, int corrector, Field out, Field u, Field um, Field up)
 {
    const long long ni = b.ni, nj = b.je - b.jb + 1, nk = b.ke - b.kb + 1;
    const long long nA = 4 * ni * nj, nB = 4 * ni * (nk - 4), nC = 4 * (nj - 4) * (nk - 4);
@@ -184,7 +183,7 @@ __global__ void ghost_shell_kernel(Box b, int corrector, double* __restrict__ ou
 #pragma unroll
       for (int c = 0; c < 3; c++) {
          const long long x = cidx(b, c, i, j, k);
-         out[x] = corrector ? up[x] : 2 * u[x] - um[x];
+         out.set(x, corrector ? up.get(x) : 2 * u.get(x) - um.get(x));
       }
    }
 }
@@ -230,7 +229,23 @@ int launch_ghost_shell(const Box& b, int corrector, double* out, const double* u
    const long long ni = b.ni, nj = b.je - b.jb + 1, nk = b.ke - b.kb + 1;
    if (ni < 5 || nj < 5 || nk < 5) return kBadArgument;
    const long long n = 4 * ni * nj + 4 * ni * (nk - 4) + 4 * (nj - 4) * (nk - 4);
-   ghost_shell_kernel<<<stream_grid(n), 256, 0, s>>>(b, corrector, out, u, um, up);
+   ghost_shell_kernel<<<stream_grid(n), 256, 0, s>>>(b, corrector, F64Field{out},
+                                                     F64Field{const_cast<double*>(u)},
+                                                     F64Field{const_cast<double*>(um)},
+                                                     F64Field{const_cast<double*>(up)});
+   return launch_status();
+}
+
+int launch_ghost_shell_df(const Box& b, int corrector, float* out, const float* u, const float* um,
+                          const float* up, cudaStream_t s)
+{
+   const long long ni = b.ni, nj = b.je - b.jb + 1, nk = b.ke - b.kb + 1;
+   if (ni < 5 || nj < 5 || nk < 5) return kBadArgument;
+   const long long n = 4 * ni * nj + 4 * ni * (nk - 4) + 4 * (nj - 4) * (nk - 4);
+   const long long lo = 3 * b.npts;
+   ghost_shell_kernel<<<stream_grid(n), 256, 0, s>>>(
+       b, corrector, DFField{out, lo}, DFField{const_cast<float*>(u), lo},
+       DFField{const_cast<float*>(um), lo}, DFField{const_cast<float*>(up), lo});
    return launch_status();
 }
 

@@ -21,6 +21,7 @@ struct OpArgs {
    Box b;   // material / output box
    Box bu;  // box of the field u (equal to b except for a scratch field slab)
    const double* __restrict__ u;
+   const float* __restrict__ udf;  // double-float field instead of u when set (lo at 3*npts)
    const double* __restrict__ mu;
    const double* __restrict__ la;
    const double* __restrict__ sx;
@@ -29,14 +30,20 @@ struct OpArgs {
    double* __restrict__ lu;
    double cof;
    int nk;
+   // optional SBP z coefficients of the one-sided rows, per column (zcoef_kernel):
+   // zc[((r*8 + q)*2 + t)*nij + column], row r=0..5, point q=0..7, t 0 mu, 1 2mu+lambda
+   const double* __restrict__ zc;
 };
 
-struct Pt {
+template <bool DF>
+struct PtT {
    const OpArgs& a;
-   __device__ Pt(const OpArgs& a_) : a(a_) {}
+   __device__ PtT(const OpArgs& a_) : a(a_) {}
    __device__ __forceinline__ double u(int c, int i, int j, int k) const
    {
-      return __ldg(a.u + cidx(a.bu, c, i, j, k));
+      const long long q = cidx(a.bu, c, i, j, k);
+      if (DF) return (double)__ldg(a.udf + q) + (double)__ldg(a.udf + q + 3 * a.bu.npts);
+      return __ldg(a.u + q);
    }
    __device__ __forceinline__ double mu(int i, int j, int k) const
    {
@@ -53,8 +60,11 @@ struct Pt {
    }
 };
 
+using Pt = PtT<false>;
+
 // (coef * f_ai)_ao times 144 h^2 with f = component c (src/rhs4sg_rev.C:221-347).
-__device__ __forceinline__ double mixed(const Pt& P, bool la_coef, int ao, int ai, int c, int i,
+template <class P_>
+__device__ __forceinline__ double mixed(const P_& P, bool la_coef, int ao, int ai, int c, int i,
                                         int j, int k)
 {
    double s = 0;
@@ -74,7 +84,8 @@ __device__ __forceinline__ double mixed(const Pt& P, bool la_coef, int ao, int a
 }
 
 // s_ax-stretched coefficient stencils along axis ax at (i,j,k): a = mu*s, b = (2mu+la)*s.
-__device__ __forceinline__ void coef_stencil(const Pt& P, int ax, int i, int j, int k, double am[5],
+template <class P_>
+__device__ __forceinline__ void coef_stencil(const P_& P, int ax, int i, int j, int k, double am[5],
                                              double bm[5])
 {
 #pragma unroll
@@ -87,7 +98,8 @@ __device__ __forceinline__ void coef_stencil(const Pt& P, int ax, int i, int j, 
    }
 }
 
-__device__ __forceinline__ void field_stencil(const Pt& P, int ax, int c, int i, int j, int k,
+template <class P_>
+__device__ __forceinline__ void field_stencil(const P_& P, int ax, int c, int i, int j, int k,
                                               double f[5])
 {
 #pragma unroll
@@ -129,12 +141,12 @@ __global__ void __launch_bounds__(256) rhs4_center_kernel(OpArgs a, int k1)
 // row is kk = k (top) or nk-k+1 (bottom) and the z-stencil point q (1..8) sits at
 // k=q (top) or nk-q+1 (bottom), with the first-derivative weights negated at the
 // bottom (src/rhs4sg_rev.C:602-856).  strz is not applied on these rows.
-template <bool TOP>
+template <bool TOP, bool DF = false>
 __device__ __forceinline__ void lu_bndry_point(const OpArgs& a, int i, int j, int k, double r[3])
 {
    const int nk = a.nk;
    const int kk = TOP ? k : nk - k + 1;
-   Pt P(a);
+   PtT<DF> P(a);
    const double i6 = 1.0 / 6, i12 = 1.0 / 12, i144 = 1.0 / 144;
    const double sx = P.s(0, i), sy = P.s(1, j);
    auto kq = [&](int q) { return TOP ? q : nk - q + 1; };  // q = 1..8
@@ -152,18 +164,27 @@ __device__ __forceinline__ void lu_bndry_point(const OpArgs& a, int i, int j, in
          acc += (ax == 0 ? sx : sy) * d2var(ax == c ? bm[ax] : am[ax], f);
       }
       // z: sum_q (sum_m acof(kk,q,m) coef(m)) u(q) + ghcof(kk) coef(bnd) u(ghost)
-      double cz[8];
-      for (int m = 1; m <= 8; m++) {
-         const double mu = P.mu(i, j, kq(m));
-         cz[m - 1] = c == 2 ? 2 * mu + P.la(i, j, kq(m)) : mu;
-      }
+      const int t = c == 2 ? 1 : 0;
       double zz = 0;
-      for (int q = 1; q <= 8; q++) {
-         double cq = 0;
-         for (int m = 1; m <= 8; m++) cq += k_acof[(kk - 1) + 6 * (q - 1) + 48 * (m - 1)] * cz[m - 1];
-         zz += cq * P.u(c, i, j, kq(q));
+      if (a.zc) {
+         const long long col = (long long)(i - a.b.ib) + a.b.ni * (j - a.b.jb);
+         const double* zr = a.zc + ((long long)(kk - 1) * 16 + t) * a.b.nij + col;
+         for (int q = 1; q <= 8; q++) zz += __ldg(zr + (long long)(q - 1) * 2 * a.b.nij) * P.u(c, i, j, kq(q));
+      } else {
+         double cz[8];
+         for (int m = 1; m <= 8; m++) {
+            const double mu = P.mu(i, j, kq(m));
+            cz[m - 1] = t ? 2 * mu + P.la(i, j, kq(m)) : mu;
+         }
+         for (int q = 1; q <= 8; q++) {
+            double cq = 0;
+            for (int m = 1; m <= 8; m++) cq += k_acof[(kk - 1) + 6 * (q - 1) + 48 * (m - 1)] * cz[m - 1];
+            zz += cq * P.u(c, i, j, kq(q));
+         }
       }
-      zz += k_ghcof[kk - 1] * cz[0] * P.u(c, i, j, TOP ? 0 : nk + 1);
+      const double mub = P.mu(i, j, TOP ? 1 : nk);
+      const double cb = t ? 2 * mub + P.la(i, j, TOP ? 1 : nk) : mub;
+      zz += k_ghcof[kk - 1] * cb * P.u(c, i, j, TOP ? 0 : nk + 1);
       r[c] = i6 * acc + zz;
    }
    // centred mixed x-y terms
@@ -230,6 +251,12 @@ struct RowUpdate {
    const double* __restrict__ um;
    const double* __restrict__ up;
    double* __restrict__ out;
+   // double-float levels (mixed form) used instead of the four above when set
+   const float* __restrict__ udf;
+   const float* __restrict__ umdf;
+   const float* __restrict__ updf;
+   float* __restrict__ outdf;
+   long long lo;
    const double* __restrict__ irho;
    const double* __restrict__ rho;
    double coef;  // dt^2 (predictor) or dt^2/12 (corrector)
@@ -239,6 +266,14 @@ struct RowUpdate {
    const double* __restrict__ co[3];
 };
 
+template <bool DF>
+__device__ __forceinline__ double lvl(const double* d, const float* f, long long q, long long lo)
+{
+   if (DF) return (double)__ldg(f + q) + (double)__ldg(f + q + lo);
+   return __ldg(d + q);
+}
+
+template <bool DF>
 __device__ __forceinline__ double sg4_point(const Box& b, const RowUpdate& w, int c, int i, int j,
                                             int k)
 {
@@ -250,7 +285,7 @@ __device__ __forceinline__ double sg4_point(const Box& b, const RowUpdate& w, in
 #pragma unroll
       for (int m = -2; m <= 2; m++) {
          const long long q = cidx(b, c, i + di * m, j + dj * m, k + dk * m);
-         d[m + 2] = __ldg(w.u + q) - __ldg(w.um + q);
+         d[m + 2] = lvl<DF>(w.u, w.udf, q, w.lo) - lvl<DF>(w.um, w.umdf, q, w.lo);
       }
       double e[3];
 #pragma unroll
@@ -269,7 +304,9 @@ __device__ __forceinline__ double sg4_point(const Box& b, const RowUpdate& w, in
    return tot;
 }
 
-template <bool TOP>
+// DF: the levels (and, when the stage field is not an FP64 slab, the field) are
+// double-float pairs; FDF: the stage field is double-float.
+template <bool TOP, bool DF, bool FDF>
 __global__ void __launch_bounds__(256) stage_rows_kernel(OpArgs a, RowUpdate w)
 {
    const int i = a.b.ib + 2 + blockIdx.x * blockDim.x + threadIdx.x;
@@ -277,7 +314,7 @@ __global__ void __launch_bounds__(256) stage_rows_kernel(OpArgs a, RowUpdate w)
    if (i > a.b.ie - 2 || j > a.b.je - 2) return;
    const int k = TOP ? 1 + (int)blockIdx.z : a.nk - 5 + (int)blockIdx.z;
    double r[3];
-   lu_bndry_point<TOP>(a, i, j, k, r);
+   lu_bndry_point<TOP, FDF>(a, i, j, k, r);
    const long long p = pidx(a.b, i, j, k);
    const double ir = w.irho ? __ldg(w.irho + p) : 1.0 / __ldg(w.rho + p);
    const double cr = w.coef * ir;
@@ -285,11 +322,18 @@ __global__ void __launch_bounds__(256) stage_rows_kernel(OpArgs a, RowUpdate w)
    for (int c = 0; c < 3; c++) {
       const long long q = cidx(a.b, c, i, j, k);
       const double lu = a.cof * r[c];
+      double v;
       if (!w.corrector) {
-         w.out[q] = 2 * __ldg(w.u + q) - __ldg(w.um + q) + cr * lu;
+         v = 2 * lvl<DF>(w.u, w.udf, q, w.lo) - lvl<DF>(w.um, w.umdf, q, w.lo) + cr * lu;
       } else {
-         double v = __ldg(w.up + q) + cr * lu;
-         if (w.beta != 0) v -= birho * sg4_point(a.b, w, c, i, j, k);
+         v = lvl<DF>(w.up, w.updf, q, w.lo) + cr * lu;
+         if (w.beta != 0) v -= birho * sg4_point<DF>(a.b, w, c, i, j, k);
+      }
+      if (DF) {
+         const float hh = __double2float_rn(v);
+         w.outdf[q] = hh;
+         w.outdf[q + w.lo] = __double2float_rn(v - (double)hh);
+      } else {
          w.out[q] = v;
       }
    }
@@ -325,6 +369,8 @@ int launch_rhs4sg_direct(int soa, int ifirst, int ilast, int jfirst, int jlast, 
    a.b = make_box(soa, ifirst, ilast, jfirst, jlast, kfirst, klast);
    a.bu = a.b;
    a.u = u;
+   a.udf = nullptr;
+   a.zc = nullptr;
    a.mu = mu;
    a.la = la;
    a.sx = strx;
@@ -359,11 +405,12 @@ int launch_stage_rows(int corrector, bool top, const Box& b, int nk, const doubl
                       const double* u, const double* um, const double* up, double* out,
                       const double* rho, const double* irho, double coef, double beta,
                       const double* const dc[3], const double* const st[3],
-                      const double* const co[3], cudaStream_t stream)
+                      const double* const co[3], const double* zc, cudaStream_t stream)
 {
    int status = upload_sbp_tables_direct();
    if (status != kOk) return status;
    OpArgs a;
+   a.zc = zc;
    a.b = b;
    a.bu = field_box;
    a.u = field;
@@ -376,6 +423,10 @@ int launch_stage_rows(int corrector, bool top, const Box& b, int nk, const doubl
    a.cof = 1.0 / (h * h);
    a.nk = nk;
    RowUpdate w;
+   w.udf = w.umdf = w.updf = nullptr;
+   w.outdf = nullptr;
+   w.lo = 0;
+   a.udf = nullptr;
    w.corrector = corrector;
    w.u = u;
    w.um = um;
@@ -394,9 +445,106 @@ int launch_stage_rows(int corrector, bool top, const Box& b, int nk, const doubl
    if (ni <= 0 || nj <= 0) return kOk;
    const dim3 block(32, 8, 1), grid(blocks_for(ni, 32), blocks_for(nj, 8), 6);
    if (top)
-      stage_rows_kernel<true><<<grid, block, 0, stream>>>(a, w);
+      stage_rows_kernel<true, false, false><<<grid, block, 0, stream>>>(a, w);
    else
-      stage_rows_kernel<false><<<grid, block, 0, stream>>>(a, w);
+      stage_rows_kernel<false, false, false><<<grid, block, 0, stream>>>(a, w);
+   return launch_status();
+}
+
+int launch_stage_rows_df(int corrector, bool top, const Box& b, int nz, const double* field_f64,
+                         const float* field_df, const Box& field_box, const double* mu,
+                         const double* la, double h, const double* strx, const double* stry,
+                         const double* strz, const float* u, const float* um, const float* up,
+                         float* out, const double* rho, const double* irho, double coef,
+                         double beta, const double* const dc[3], const double* const st[3],
+                         const double* const co[3], const double* zc, cudaStream_t stream)
+{
+   int status = upload_sbp_tables_direct();
+   if (status != kOk) return status;
+   OpArgs a;
+   a.zc = zc;
+   a.b = b;
+   a.bu = field_box;
+   a.u = field_f64;
+   a.udf = field_df;
+   a.mu = mu;
+   a.la = la;
+   a.sx = strx;
+   a.sy = stry;
+   a.sz = strz;
+   a.lu = nullptr;
+   a.cof = 1.0 / (h * h);
+   a.nk = nz;
+   RowUpdate w;
+   w.corrector = corrector;
+   w.u = w.um = w.up = nullptr;
+   w.out = nullptr;
+   w.udf = u;
+   w.umdf = um;
+   w.updf = up;
+   w.outdf = out;
+   w.lo = 3 * b.npts;
+   w.irho = irho;
+   w.rho = rho;
+   w.coef = coef;
+   w.beta = beta;
+   for (int q = 0; q < 3; q++) {
+      w.dc[q] = dc[q];
+      w.st[q] = st[q];
+      w.co[q] = co[q];
+   }
+   const int ni = b.ie - b.ib - 3, nj = b.je - b.jb - 3;
+   if (ni <= 0 || nj <= 0) return kOk;
+   const dim3 block(32, 8, 1), grid(blocks_for(ni, 32), blocks_for(nj, 8), 6);
+   const bool fdf = field_df != nullptr;
+   if (top) {
+      if (fdf) stage_rows_kernel<true, true, true><<<grid, block, 0, stream>>>(a, w);
+      else stage_rows_kernel<true, true, false><<<grid, block, 0, stream>>>(a, w);
+   } else {
+      if (fdf) stage_rows_kernel<false, true, true><<<grid, block, 0, stream>>>(a, w);
+      else stage_rows_kernel<false, true, false><<<grid, block, 0, stream>>>(a, w);
+   }
+   return launch_status();
+}
+
+namespace {
+// SBP z coefficients of the 6 one-sided rows for every column (time-invariant):
+// zc[((r*8 + q)*2 + t)*nij + col] = sum_m acof(r+1, q+1, m) * c_t(kq(m)), with
+// c_0 = mu, c_1 = 2 mu + lambda and kq the row's stencil planes (top or bottom).
+template <bool TOP>
+__global__ void zcoef_kernel(Box b, int nk, const double* __restrict__ mu,
+                             const double* __restrict__ la, double* __restrict__ zc)
+{
+   const long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+   if (col >= b.nij) return;
+   double cm[2][8];
+   for (int m = 1; m <= 8; m++) {
+      const int km = TOP ? m : nk - m + 1;
+      const long long p = col + b.nij * (long long)(km - b.kb);
+      cm[0][m - 1] = mu[p];
+      cm[1][m - 1] = 2 * mu[p] + la[p];
+   }
+   for (int r = 0; r < 6; r++)
+      for (int q = 0; q < 8; q++)
+         for (int t = 0; t < 2; t++) {
+            double v = 0;
+            for (int m = 0; m < 8; m++) v += k_acof[r + 6 * q + 48 * m] * cm[t][m];
+            zc[((long long)(r * 8 + q) * 2 + t) * b.nij + col] = v;
+         }
+}
+}  // namespace
+
+long long zcoef_len(const Box& b) { return 96LL * b.nij; }
+
+int launch_zcoef(const Box& b, int nk, bool top, const double* mu, const double* la, double* zc,
+                 cudaStream_t s)
+{
+   int status = upload_sbp_tables_direct();
+   if (status != kOk) return status;
+   if (top)
+      zcoef_kernel<true><<<blocks_for(b.nij, 128), 128, 0, s>>>(b, nk, mu, la, zc);
+   else
+      zcoef_kernel<false><<<blocks_for(b.nij, 128), 128, 0, s>>>(b, nk, mu, la, zc);
    return launch_status();
 }
 

@@ -21,6 +21,7 @@ struct GridSpec {
    double sg_damping = 0.02;    // supergrid damping coefficient (src/EW.C:174)
    int sg_order = 4;            // 4 or 6 (src/EW.C:1288-1305)
    int soa = 1;                 // component layout: 1 SoA (corder=1), 0 AoS
+   int precision = 0;           // 0: FP64 throughout; 1: FP32-mixed (stage_mixed.cu)
 };
 
 // Array bounds of the grid: 2 ghost points per side.

@@ -463,6 +463,20 @@ __global__ void uacc_slab_kernel(Box b, int k0, int k1, const double* __restrict
    }
 }
 
+// Same for double-float levels (the slab itself is FP64).
+__global__ void uacc_slab_df_kernel(Box b, int k0, int k1, DFField up, DFField u, DFField um,
+                                    double* __restrict__ out)
+{
+   const long long nslab = b.nij * (k1 - k0 + 1);
+   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < 3 * nslab;
+        q += (long long)gridDim.x * blockDim.x) {
+      const int c = (int)(q / nslab);
+      const long long r = q % nslab;
+      const long long p = r + b.nij * (long long)(k0 - b.kb) + c * b.npts;
+      out[q] = (up.get(p) - 2 * u.get(p)) + um.get(p);
+   }
+}
+
 int grid_stride_blocks(long long n)
 {
    long long g = (n + 255) / 256;
@@ -490,6 +504,16 @@ int launch_uacc_slab(const Box& b, int k0, int k1, const double* up, const doubl
 {
    const long long n = 3 * b.nij * (k1 - k0 + 1);
    uacc_slab_kernel<<<grid_stride_blocks(n), 256, 0, s>>>(b, k0, k1, up, u, um, out);
+   return launch_status();
+}
+
+int launch_uacc_slab_df(const Box& b, int k0, int k1, const float* up, const float* u,
+                        const float* um, double* out, cudaStream_t s)
+{
+   const long long n = 3 * b.nij * (k1 - k0 + 1), lo = 3 * b.npts;
+   uacc_slab_df_kernel<<<grid_stride_blocks(n), 256, 0, s>>>(
+       b, k0, k1, DFField{const_cast<float*>(up), lo}, DFField{const_cast<float*>(u), lo},
+       DFField{const_cast<float*>(um), lo}, out);
    return launch_status();
 }
 
