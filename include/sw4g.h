@@ -229,6 +229,32 @@ int sw4g_ew_get_fields(const sw4g_ew* ew, double* u, double* um, int on_device);
 double* sw4g_ew_field(const sw4g_ew* ew, int which);
 /* advance nsteps time steps */
 int sw4g_ew_step(sw4g_ew* ew, int nsteps, int mode);
+
+/* Receivers (replace TimeSeries + EW::extractRecordData, src/EW.C:5854-6072, and the
+ * per-step recording in the time loop, src/EW.C:2485-2500 and 2797-2835).
+ * Record modes are numbered as TimeSeries::receiverMode (src/TimeSeries.h:52);
+ * values per receiver and step: */
+#define SW4G_REC_DISPLACEMENT 0 /* 3: ux, uy, uz */
+#define SW4G_REC_DIV 1          /* 1 */
+#define SW4G_REC_CURL 2         /* 3 */
+#define SW4G_REC_STRAINS 3      /* 6: xx, yy, zz, xy, xz, yz */
+#define SW4G_REC_VELOCITY 4     /* 3: (u^{n+1} - u^{n-1}) / (2 dt) */
+#define SW4G_REC_GRADIENT 5     /* 9: du_c/dx_a, c-major */
+/* Nearest grid point of (x, y, z) on one Cartesian grid, as
+ * EW::computeNearestGridPoint (src/EW.C:5149).  ijk receives 1-based indices;
+ * SW4G_BAD_ARGUMENT if the point is outside the interior. */
+int sw4g_nearest_grid_point(const sw4g_grid* g, double x, double y, double z, int* ijk);
+/* Sets n receivers at grid points ijk[3n] with modes mode[n] and allocates a device
+ * record array of `capacity` rows.  The first step after this call first writes the
+ * initial data (velocity entries of that row are 0: the reference records no
+ * velocity for it), then every step appends one row of all receivers' values in
+ * receiver order.  A step that would overflow the array returns SW4G_BAD_ARGUMENT
+ * before doing anything.  n = 0 removes the receivers. */
+int sw4g_ew_set_receivers(sw4g_ew* ew, int n, const int* ijk, const int* mode, int capacity);
+/* rows written so far and values per row */
+int sw4g_ew_record_shape(const sw4g_ew* ew, int* rows, int* nvals);
+/* copies rows x nvals doubles (row-major) to host (on_device=0) or device memory */
+int sw4g_ew_get_records(const sw4g_ew* ew, double* out, int on_device);
 /* boundary conditions of this grid on a caller's 3-component device array */
 int sw4g_ew_enforce_bc(sw4g_ew* ew, double* u);
 /* kernel launches one step enqueues */

@@ -190,5 +190,57 @@ def step(problem: Problem, soa, t, up, u, um, lu, f, uacc, which="oracle"):
        _dp(uacc))
 
 
+def nearest_grid_point(h, zmin, x, y, z):
+    """EW::computeNearestGridPoint (src/EW.C:5149-5177) for one Cartesian grid:
+    1-based (i, j, k) of the nearest point, a half-way point going to the lower index."""
+    i = int(np.floor(x / h)) + 1
+    if x - ((i - 0.5) * h) > 0.0:
+        i += 1
+    j = int(np.floor(y / h)) + 1
+    if y - ((j - 0.5) * h) > 0.0:
+        j += 1
+    k = int(np.floor((z - zmin) / h)) + 1
+    if z - (zmin + (k - 0.5) * h) > 0.0:
+        k += 1
+    return i, j, k
+
+
+REC_VALUES = {0: 3, 1: 1, 2: 3, 3: 6, 4: 3, 5: 9}
+
+
+def record(mode, ijk, u, um, dt, h, dims, initial=False):
+    """Values one receiver records (EW::extractRecordData, src/EW.C:5854-6072,
+    Cartesian formulas).  u, um: SoA 3-component fields over the array of an
+    nx x ny x nz grid (index -1 .. n+2 per axis); dims = (nx, ny, nz).  Velocity
+    is not recorded for the initial data (src/EW.C:2489-2491): zeros there."""
+    nx, ny, nz = dims
+    U = np.asarray(u).reshape(3, nz + 4, ny + 4, nx + 4)
+    Um = np.asarray(um).reshape(3, nz + 4, ny + 4, nx + 4)
+    i, j, k = ijk
+
+    def at(A, c, ii, jj, kk):
+        return A[c, kk + 1, jj + 1, ii + 1]
+
+    if mode == 0:
+        return [at(U, c, i, j, k) for c in range(3)]
+    if mode == 4:
+        if initial:
+            return [0.0, 0.0, 0.0]
+        return [(at(U, c, i, j, k) - at(Um, c, i, j, k)) / (2 * dt) for c in range(3)]
+    f = 1.0 / (2 * h)
+    if mode == 1:
+        return [(at(U, 0, i + 1, j, k) - at(U, 0, i - 1, j, k) + at(U, 1, i, j + 1, k) -
+                 at(U, 1, i, j - 1, k) + at(U, 2, i, j, k + 1) - at(U, 2, i, j, k - 1)) * f]
+    g = [[(at(U, c, i + 1, j, k) - at(U, c, i - 1, j, k)) * f,
+          (at(U, c, i, j + 1, k) - at(U, c, i, j - 1, k)) * f,
+          (at(U, c, i, j, k + 1) - at(U, c, i, j, k - 1)) * f] for c in range(3)]
+    if mode == 2:
+        return [g[2][1] - g[1][2], g[0][2] - g[2][0], g[1][0] - g[0][1]]
+    if mode == 3:
+        return [g[0][0], g[1][1], g[2][2], 0.5 * (g[1][0] + g[0][1]), 0.5 * (g[2][0] + g[0][2]),
+                0.5 * (g[1][2] + g[2][1])]
+    return [g[c][a] for c in range(3) for a in range(3)]
+
+
 def set_threads(n: int) -> None:
     os.environ["OMP_NUM_THREADS"] = str(n)

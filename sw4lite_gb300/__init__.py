@@ -50,6 +50,8 @@ GAUSSIAN, C6SMOOTHBUMP, RICKER, VERYSMOOTHBUMP = 0, 1, 2, 3
 # boundary kinds (the reference's boundaryConditionType numbering)
 FREE, DIRICHLET, SUPERGRID, PERIODIC = 0, 1, 2, 3
 MODE_PHASES, MODE_FUSED = 0, 1
+# receiver record modes (the reference's TimeSeries::receiverMode numbering)
+REC_DISPLACEMENT, REC_DIV, REC_CURL, REC_STRAINS, REC_VELOCITY, REC_GRADIENT = 0, 1, 2, 3, 4, 5
 
 _SIGS = {
     "sw4g_version": ([], C.c_char_p),
@@ -84,6 +86,11 @@ _SIGS = {
     "sw4g_ew_field": ([_VP, C.c_int], _VP),
     "sw4g_ew_step": ([_VP, C.c_int, C.c_int], C.c_int),
     "sw4g_ew_enforce_bc": ([_VP, _VP], C.c_int),
+    "sw4g_nearest_grid_point": ([C.POINTER(GridDesc), C.c_double, C.c_double, C.c_double, _I],
+                                C.c_int),
+    "sw4g_ew_set_receivers": ([_VP, C.c_int, _I, _I, C.c_int], C.c_int),
+    "sw4g_ew_record_shape": ([_VP, _I, _I], C.c_int),
+    "sw4g_ew_get_records": ([_VP, _VP, C.c_int], C.c_int),
     "sw4g_ew_launches_per_step": ([_VP, C.c_int], C.c_int),
     "sw4g_ew_profile_kernels": ([_VP, C.c_int, _D], C.c_int),
     "sw4g_fma_peak": ([C.c_int, _D, _VP], C.c_int),
@@ -256,6 +263,34 @@ class EW:
     def enforce_bc(self, u):
         check(lib().sw4g_ew_enforce_bc(self._h, _ptr(u)), "enforce_bc")
 
+    def set_receivers(self, ijk, modes, capacity):
+        """Receivers at 1-based grid points ijk (n x 3) with record modes (REC_*);
+        room for `capacity` record rows (initial data + one per step)."""
+        import numpy as np
+        ijk = np.ascontiguousarray(np.asarray(ijk, dtype=np.int32).reshape(-1, 3))
+        modes = np.ascontiguousarray(np.asarray(modes, dtype=np.int32).reshape(-1))
+        n = len(modes)
+        if ijk.shape[0] != n:
+            raise Sw4gError("set_receivers: one mode per receiver")
+        check(lib().sw4g_ew_set_receivers(self._h, n, ijk.ctypes.data_as(_I),
+                                          modes.ctypes.data_as(_I), capacity), "set_receivers")
+
+    def record_shape(self):
+        rows, nvals = C.c_int(), C.c_int()
+        check(lib().sw4g_ew_record_shape(self._h, C.byref(rows), C.byref(nvals)), "record_shape")
+        return rows.value, nvals.value
+
+    def records(self, out=None):
+        """The record array, rows x values: into `out` (host array or device tensor)
+        or a new host array."""
+        rows, nvals = self.record_shape()
+        if out is None:
+            import numpy as np
+            out = np.zeros((rows, nvals))
+        on_dev = int(hasattr(out, "is_cuda") and out.is_cuda)
+        check(lib().sw4g_ew_get_records(self._h, _ptr(out), on_dev), "get_records")
+        return out
+
     def launches_per_step(self, mode=MODE_FUSED) -> int:
         return lib().sw4g_ew_launches_per_step(self._h, mode)
 
@@ -263,6 +298,13 @@ class EW:
         ms = (C.c_double * 4)()
         check(lib().sw4g_ew_profile_kernels(self._h, nrep, ms), "profile_kernels")
         return dict(pred_stage=ms[0], corr_stage=ms[1], rows=ms[2], bc_force=ms[3])
+
+
+def nearest_grid_point(g, x, y, z):
+    """1-based (i, j, k) of the grid point nearest to (x, y, z) on grid g."""
+    ijk = (C.c_int * 3)()
+    check(lib().sw4g_nearest_grid_point(C.byref(g), x, y, z, ijk), "nearest_grid_point")
+    return tuple(ijk)
 
 
 def fma_peak(precision=64, stream=None) -> float:

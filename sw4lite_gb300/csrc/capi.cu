@@ -1,4 +1,5 @@
 // extern "C" entry points of libsw4g.so (declared in include/sw4g.h).
+#include <cmath>
 #include <cstring>
 #include <exception>
 #include <new>
@@ -322,6 +323,40 @@ int sw4g_ew_add_grid_point_sources(sw4g_ew* ew, int n, const int* ijk, const dou
 }
 
 int sw4g_ew_clear_sources(sw4g_ew* ew) { return ew ? ew->impl->clear_sources() : SW4G_BAD_ARGUMENT; }
+
+int sw4g_nearest_grid_point(const sw4g_grid* g, double x, double y, double z, int* ijk)
+{
+   if (!g || !ijk || !(g->h > 0)) return SW4G_BAD_ARGUMENT;
+   // src/EW.C:5149-5177 for one Cartesian grid: round to the nearest point, a
+   // point exactly half-way going to the lower index
+   const double h = g->h;
+   int i = (int)std::floor(x / h) + 1;
+   if (x - ((i - 0.5) * h) > 0.) i++;
+   int j = (int)std::floor(y / h) + 1;
+   if (y - ((j - 0.5) * h) > 0.) j++;
+   int k = (int)std::floor((z - g->zmin) / h) + 1;
+   if (z - (g->zmin + (k - 0.5) * h) > 0.) k++;
+   ijk[0] = i;
+   ijk[1] = j;
+   ijk[2] = k;
+   return (i >= 1 && i <= g->nx && j >= 1 && j <= g->ny && k >= 1 && k <= g->nz) ? SW4G_OK
+                                                                                : SW4G_BAD_ARGUMENT;
+}
+
+int sw4g_ew_set_receivers(sw4g_ew* ew, int n, const int* ijk, const int* mode, int capacity)
+{
+   return ew ? ew->impl->set_receivers(n, ijk, mode, capacity) : SW4G_BAD_ARGUMENT;
+}
+
+int sw4g_ew_record_shape(const sw4g_ew* ew, int* rows, int* nvals)
+{
+   return ew ? ew->impl->record_shape(rows, nvals) : SW4G_BAD_ARGUMENT;
+}
+
+int sw4g_ew_get_records(const sw4g_ew* ew, double* out, int on_device)
+{
+   return ew ? ew->impl->get_records(out, on_device != 0) : SW4G_BAD_ARGUMENT;
+}
 
 int sw4g_ew_num_grid_point_sources(const sw4g_ew* ew)
 {

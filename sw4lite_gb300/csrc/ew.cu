@@ -38,6 +38,8 @@ EW::~EW()
    f(zc_[0]);
    f(zc_[1]);
    f(dsrc_mem_);
+   f(drec_mem_);
+   f(records_);
    f(rho32_);
    f(mu32_);
    f(la32_);
@@ -357,10 +359,96 @@ int EW::step(int nsteps, int mode)
 {
    if (!ready_ || !material_ || !(dt_ > 0) || nsteps < 0) return kBadArgument;
    if (mode != kModePhases && mode != kModeFused) return kBadArgument;
+   if (mixed_ && mode == kModePhases) return kNotSupported;
+   if (drec_.n > 0 && rec_rows_ + (rec_initial_ ? 1 : 0) + nsteps > rec_cap_) return kBadArgument;
    SW4G_TRY(upload_sources());
    if (mode == kModePhases) SW4G_TRY(ensure_phase_arrays());
-   if (mixed_ && mode == kModePhases) return kNotSupported;
+   if (drec_.n > 0 && rec_initial_) {
+      SW4G_TRY(record(lev_[iu_], lev_[ium_], 1));
+      rec_initial_ = false;
+   }
    for (int n = 0; n < nsteps; n++) SW4G_TRY(mode == kModePhases ? step_phases() : step_fused());
+   return kOk;
+}
+
+int EW::record(double* up, double* um, int initial)
+{
+   double* row = records_ + (size_t)rec_rows_ * rec_nvals_;
+   if (mixed_)
+      SW4G_TRY(launch_record_df(make_box(1, b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke),
+                                reinterpret_cast<const float*>(up),
+                                reinterpret_cast<const float*>(um), drec_, row, dt_, g_.h, initial,
+                                stream_));
+   else
+      SW4G_TRY(launch_record(make_box(1, b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke), up, um, drec_,
+                             row, dt_, g_.h, initial, stream_));
+   rec_rows_++;
+   return kOk;
+}
+
+int EW::set_receivers(int n, const int* ijk, const int* mode, int capacity)
+{
+   if (!ready_ || n < 0 || (n > 0 && (!ijk || !mode || capacity < 1))) return kBadArgument;
+   std::vector<int> host(5 * (size_t)n);
+   int nvals = 0;
+   for (int r = 0; r < n; r++) {
+      const int i = ijk[3 * r], j = ijk[3 * r + 1], k = ijk[3 * r + 2];
+      const int nv = receiver_values(mode[r]);
+      if (nv == 0) return kBadArgument;
+      // the value itself needs (i,j,k) in the array; the differences need its neighbours
+      const int m = (mode[r] == kRecDisplacement || mode[r] == kRecVelocity) ? 0 : 1;
+      if (i - m < b_.ib || i + m > b_.ie || j - m < b_.jb || j + m > b_.je || k - m < b_.kb ||
+          k + m > b_.ke)
+         return kBadArgument;
+      host[3 * r] = i;
+      host[3 * r + 1] = j;
+      host[3 * r + 2] = k;
+      host[3 * n + r] = mode[r];
+      host[4 * n + r] = nvals;
+      nvals += nv;
+   }
+   if (drec_mem_ || records_) SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
+   if (drec_mem_) cudaFree(drec_mem_);
+   if (records_) cudaFree(records_);
+   drec_mem_ = nullptr;
+   records_ = nullptr;
+   drec_ = ReceiverSet{};
+   rec_cap_ = rec_rows_ = rec_nvals_ = 0;
+   rec_initial_ = false;
+   if (n == 0) return kOk;
+   SW4G_TRY(cuda_ok(cudaMalloc(&drec_mem_, host.size() * sizeof(int))));
+   SW4G_TRY(cuda_ok(cudaMemcpy(drec_mem_, host.data(), host.size() * sizeof(int),
+                               cudaMemcpyHostToDevice)));
+   SW4G_TRY(cuda_ok(cudaMalloc(&records_, (size_t)capacity * nvals * sizeof(double))));
+   SW4G_TRY(cuda_ok(cudaMemsetAsync(records_, 0, (size_t)capacity * nvals * sizeof(double), stream_)));
+   const int* d = static_cast<const int*>(drec_mem_);
+   drec_.n = n;
+   drec_.ijk = d;
+   drec_.mode = d + 3 * n;
+   drec_.off = d + 4 * n;
+   rec_cap_ = capacity;
+   rec_nvals_ = nvals;
+   rec_initial_ = true;
+   return kOk;
+}
+
+int EW::record_shape(int* rows, int* nvals) const
+{
+   if (!rows || !nvals) return kBadArgument;
+   *rows = rec_rows_;
+   *nvals = rec_nvals_;
+   return kOk;
+}
+
+int EW::get_records(double* out, bool on_device) const
+{
+   if (!out) return kBadArgument;
+   if (rec_rows_ == 0) return kOk;
+   const size_t bytes = (size_t)rec_rows_ * rec_nvals_ * sizeof(double);
+   SW4G_TRY(cuda_ok(cudaMemcpyAsync(out, records_, bytes,
+                                    on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                    stream_)));
+   if (!on_device) SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
    return kOk;
 }
 
@@ -390,6 +478,7 @@ int EW::step_phases()
                              dprof_[0], dprof_[1], dprof_[2], dprof_[3], dprof_[4], dprof_[5],
                              dprof_[6], dprof_[7], dprof_[8], g_.sg_damping, stream_));
    SW4G_TRY(enforce_bc(up));
+   if (drec_.n > 0) SW4G_TRY(record(up, um, 0));
    ium_ = iu_;
    iu_ = ip;
    t_ += dt;
@@ -584,6 +673,7 @@ int EW::step_fused()
    int iq = ip + 1;
    while (iq == iu_ || iq == ium_) iq++;
    for (int which = 0; which < 6; which++) SW4G_TRY(piece(which, ip, iq));
+   if (drec_.n > 0) SW4G_TRY(record(lev_[iq], lev_[ium_], 0));
    ium_ = iu_;
    iu_ = iq;
    t_ += dt_;
@@ -632,14 +722,15 @@ int EW::launches_per_step(int mode) const
    const int rows = onesided_[4] + onesided_[5];
    const int src = hsrc_.empty() ? 0 : 1;
    const bool damp = prof_.used && g_.sg_damping != 0;
+   const int rec = drec_.n > 0 ? 1 : 0;
    if (mode == kModePhases) {
       // force(memset+kernel), rhs (center + rows), pred, bc, force, dpdm, rhs, corr, addsgd, bc
       const int rhs = 1 + rows;
-      return 2 * (1 + src) + 2 * rhs + 3 + (damp ? 1 : 0) + 2 * bc;
+      return 2 * (1 + src) + 2 * rhs + 3 + (damp ? 1 : 0) + 2 * bc + rec;
    }
    // per stage: stage kernel, ghost shell, one-sided rows, forcing, BC sides;
    // the corrector adds the rows' slab kernels (and 6th-order damping)
-   return 2 * (2 + rows + src + bc) + rows + (damp && g_.sg_order == 6 ? 1 : 0);
+   return 2 * (2 + rows + src + bc) + rows + (damp && g_.sg_order == 6 ? 1 : 0) + rec;
 }
 
 }  // namespace sw4g

@@ -57,6 +57,15 @@ class EW {
    double* field_um() const { return lev_[ium_]; }
 
    int step(int nsteps, int mode);
+
+   // Receivers at grid points (i,j,k) with record modes (kernels.h RecMode).  Each
+   // step appends one row of values (all receivers, in order) to a device record
+   // array of `capacity` rows; the first row holds the initial data and is written
+   // by the first step after this call.  A step that would overflow the array is
+   // refused before it starts.
+   int set_receivers(int n, const int* ijk, const int* mode, int capacity);
+   int record_shape(int* rows, int* nvals) const;
+   int get_records(double* out, bool on_device) const;
    // Boundary conditions on an arbitrary 3-component device array of this grid.
    int enforce_bc(double* u);
 
@@ -72,6 +81,7 @@ class EW {
 
  private:
    int upload_sources();
+   int record(double* up, double* um, int initial);
    int step_phases();
    int step_fused();
    int fused_piece(int piece, int ip, int iq);
@@ -118,6 +128,12 @@ class EW {
    bool src_dirty_ = true;
    SourceSet dsrc_{};
    void* dsrc_mem_ = nullptr;
+
+   ReceiverSet drec_{};
+   void* drec_mem_ = nullptr;
+   double* records_ = nullptr;
+   int rec_cap_ = 0, rec_rows_ = 0, rec_nvals_ = 0;
+   bool rec_initial_ = false;  // the initial-data row is still to be written
 
    double t_ = 0, dt_ = 0;
 };

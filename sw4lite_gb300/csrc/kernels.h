@@ -81,6 +81,32 @@ struct SourceSet {
 
 __host__ __device__ double timefunc(int kind, double freq, double t, bool tt);
 
+// Receiver record modes, numbered as the reference's TimeSeries::receiverMode
+// (src/TimeSeries.h:52).
+enum RecMode : int {
+   kRecDisplacement = 0,
+   kRecDiv = 1,
+   kRecCurl = 2,
+   kRecStrains = 3,
+   kRecVelocity = 4,
+   kRecGradient = 5,
+};
+
+// Device-resident receivers: grid point and mode of each, and the offset of its
+// values within one record row.
+struct ReceiverSet {
+   int n = 0;
+   const int* ijk = nullptr;   // 3*n
+   const int* mode = nullptr;  // n
+   const int* off = nullptr;   // n
+};
+
+int receiver_values(int mode);  // values one receiver records per step (0: bad mode)
+int launch_record(const Box& b, const double* up, const double* um, const ReceiverSet& r,
+                  double* row, double dt, double h, int initial, cudaStream_t s);
+int launch_record_df(const Box& b, const float* up, const float* um, const ReceiverSet& r,
+                     double* row, double dt, double h, int initial, cudaStream_t s);
+
 int upload_sbp_tables_direct();
 
 int launch_rhs4sg_direct(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst,

@@ -138,15 +138,29 @@ class OracleProblem:
         self.P = P
         self.npts = (nx + 4) * (ny + 4) * (nz + 4)
 
-    def run(self, u, um, t0, nsteps, which="oracle"):
+    def run(self, u, um, t0, nsteps, which="oracle", receivers=None):
+        """nsteps oracle steps from (u, um); with receivers [(ijk, mode), ...] also
+        returns the record rows (initial data, then one row per step)."""
         n3 = 3 * self.npts
         u, um = u.copy(), um.copy()
         up, lu, f, uacc = (np.zeros(n3) for _ in range(4))
         t = t0
+        g = self.g
+        dims = (g.nx, g.ny, g.nz)
+
+        def row(a, b, initial):
+            return np.concatenate([O.record(m, ijk, a, b, self.P.dt, g.h, dims, initial)
+                                   for ijk, m in receivers])
+
+        rows = [row(u, um, True)] if receivers else []
         for _ in range(nsteps):
             O.step(self.P, 1, t, up, u, um, lu, f, uacc, which=which)
+            if receivers:
+                rows.append(row(up, um, False))
             um, u, up = u, up, um
             t += self.P.dt
+        if receivers:
+            return u, um, np.array(rows)
         return u, um
 
 

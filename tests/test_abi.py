@@ -119,3 +119,18 @@ def test_bad_arguments_are_rejected_without_device_work(lib):
     assert lib.sw4g_ew_create(C.byref(g), None, C.byref(h)) == 4
     assert lib.sw4g_rhs4sg(1, 1, 0, 1, 0, 1, 0, 1, (C.c_int * 6)(), None, None, None, None, 1.0,
                            None, None, None, None) == 1
+
+
+def test_nearest_grid_point_matches_reference_rule(lib):
+    """sw4g_nearest_grid_point against the oracle's restatement of
+    EW::computeNearestGridPoint, including points exactly half-way between two."""
+    g = sg.grid_desc(40, 30, 20, 0.25, zmin=1.5)
+    rng = np.random.default_rng(5)
+    pts = list(rng.uniform([0, 0, 1.5], [9.75, 7.25, 6.25], size=(200, 3)))
+    pts += [(0.125, 0.375, 1.625), (2.5, 2.5, 1.5), (9.75, 7.25, 6.25)]
+    for x, y, z in pts:
+        assert sg.nearest_grid_point(g, x, y, z) == O.nearest_grid_point(0.25, 1.5, x, y, z)
+    with pytest.raises(sg.Sw4gError):
+        sg.nearest_grid_point(g, 20.0, 1.0, 2.0)
+    with pytest.raises(sg.Sw4gError):
+        sg.nearest_grid_point(g, 1.0, 1.0, 0.0)
