@@ -242,5 +242,35 @@ def record(mode, ijk, u, um, dt, h, dims, initial=False):
     return [g[c][a] for c in range(3) for a in range(3)]
 
 
+def exact_point_source(bounds, h, zmin, rho, cp, cs, x0, y0, z0, t, *, force=None, moment=None,
+                       kind=1, freq=1.0, t0=0.0):
+    """Analytic whole-space displacement (SoA, over the array `bounds`) of one force
+    or moment-tensor point source; the field of the reference's point-source test
+    (EW::get_exact_point_source, src/EW.C:3899-4524)."""
+    ib, ie, jb, je, kb, ke = bounds
+    npts = (ie - ib + 1) * (je - jb + 1) * (ke - kb + 1)
+    u = np.zeros(3 * npts)
+    f = np.ascontiguousarray(force if force is not None else np.zeros(3), dtype=np.float64)
+    m = np.ascontiguousarray(moment if moment is not None else np.zeros(6), dtype=np.float64)
+    lib().sw4o_exact_point_source(ib, ie, jb, je, kb, ke, C.c_double(h), C.c_double(zmin),
+                                  C.c_double(rho), C.c_double(cp), C.c_double(cs), C.c_double(x0),
+                                  C.c_double(y0), C.c_double(z0), int(moment is not None), _dp(f),
+                                  _dp(m), kind, C.c_double(freq), C.c_double(t0), C.c_double(t),
+                                  _dp(u))
+    return u
+
+
+def solerr3(bounds, h, zmin, uex, u, x0, y0, z0, radius, region):
+    """(Linf, L2, max uex) of u - uex over region = (imin, imax, jmin, jmax, kmin, kmax)
+    outside the ball of `radius` around (x0, y0, z0) (EW::solerr3fort,
+    src/ew-cfromfort.C:144; EW::normOfDifference, src/EW.C:4537)."""
+    ib, ie, jb, je, kb, ke = bounds
+    li, l2, xli = C.c_double(), C.c_double(), C.c_double()
+    lib().sw4o_solerr3(ib, ie, jb, je, kb, ke, C.c_double(h), C.c_double(zmin), _dp(uex), _dp(u),
+                       C.c_double(x0), C.c_double(y0), C.c_double(z0), C.c_double(radius),
+                       *[int(r) for r in region], C.byref(li), C.byref(l2), C.byref(xli))
+    return li.value, l2.value, xli.value
+
+
 def set_threads(n: int) -> None:
     os.environ["OMP_NUM_THREADS"] = str(n)

@@ -747,3 +747,164 @@ void sw4o_step(const sw4o_problem* p, int soa, double t, double* up, const doubl
    }
    enforce_bc(p, soa, up);
 }
+
+
+/* ------------------------------------------------------------------------ */
+/* Analytic point-source solution.                                           */
+/*                                                                          */
+/* Time history g(s) of the source (force X0(t) or moment M_pq(t) = M_pq g(t)),   */
+/* its derivative, and I(s) = int_{R/a}^{R/b} tau g(s - tau) dtau, the         */
+/* near-field integral.  The whole-space Green's functions are the published  */
+/* ones (Aki & Richards, Quantitative Seismology, eq. 4.23 for a force and     */
+/* eq. 4.29 for a moment tensor).                                              */
+/* ------------------------------------------------------------------------ */
+
+/* bump B(x) on (0,1) and B'(x): C6SmoothBump 51480 x^7 (1-x)^7 and
+ * VerySmoothBump 1024 x^5 (1-x)^5 */
+static double bump(int kind, double x, int deriv)
+{
+   if (!(x > 0 && x < 1)) return 0.0;
+   const double y = x * (1 - x);
+   if (kind == 1) return deriv ? 51480.0 * 7 * pow(y, 6) * (1 - 2 * x) : 51480.0 * pow(y, 7);
+   return deriv ? 1024.0 * 5 * pow(y, 4) * (1 - 2 * x) : 1024.0 * pow(y, 5);
+}
+
+static double hist(int kind, double freq, double s)
+{
+   if (kind == 0) return freq / sqrt(2 * M_PI) * exp(-(s * freq) * (s * freq) / 2);
+   return bump(kind, freq * s, 0);
+}
+
+static double hist_dt(int kind, double freq, double s)
+{
+   if (kind == 0) return -s * freq * freq * hist(0, freq, s);
+   return freq * bump(kind, freq * s, 1);
+}
+
+/* Gauss-Legendre nodes and weights on [-1, 1] by Newton iteration on P_n */
+#define GL_N 10
+static double gl_x[GL_N], gl_w[GL_N];
+static int gl_ready = 0;
+
+static void gl_init(void)
+{
+   if (gl_ready) return;
+   for (int i = 0; i < GL_N; i++) {
+      double x = cos(M_PI * (i + 0.75) / (GL_N + 0.5)), dp = 1;
+      for (int it = 0; it < 100; it++) {
+         double p0 = 1, p1 = x;
+         for (int k = 2; k <= GL_N; k++) {
+            const double p2 = ((2 * k - 1) * x * p1 - (k - 1) * p0) / k;
+            p0 = p1;
+            p1 = p2;
+         }
+         dp = GL_N * (x * p1 - p0) / (x * x - 1);
+         const double dx = p1 / dp;
+         x -= dx;
+         if (fabs(dx) < 1e-16) break;
+      }
+      gl_x[i] = x;
+      gl_w[i] = 2 / ((1 - x * x) * dp * dp);
+   }
+   gl_ready = 1;
+}
+
+static double near_integral(int kind, double freq, double s, double lo, double hi)
+{
+   if (kind == 0) {
+      /* tau = s - v:  int (s - v) phi(v) dv over v in [s-hi, s-lo], phi the
+       * Gaussian density with sigma = 1/freq: s (Phi(U) - Phi(L)) + sigma^2 (phi(U) - phi(L)) */
+      const double sig = 1 / freq, U = s - lo, L = s - hi;
+      const double Phi = 0.5 * (erf(U / (sig * sqrt(2.0))) - erf(L / (sig * sqrt(2.0))));
+      return s * Phi + sig * sig * (hist(0, freq, U) - hist(0, freq, L));
+   }
+   /* the bump is a polynomial of degree 14 on s - tau in (0, 1/freq): integrate
+    * tau * g(s - tau) exactly over the part of [lo, hi] where it is nonzero */
+   const double a = fmax(lo, s - 1 / freq), b = fmin(hi, s);
+   if (!(b > a)) return 0.0;
+   gl_init();
+   const double c = 0.5 * (a + b), d = 0.5 * (b - a);
+   double acc = 0;
+   for (int q = 0; q < GL_N; q++) {
+      const double tau = c + d * gl_x[q];
+      acc += gl_w[q] * tau * hist(kind, freq, s - tau);
+   }
+   return d * acc;
+}
+
+void sw4o_exact_point_source(int ib, int ie, int jb, int je, int kb, int ke, double h, double zmin,
+                             double rho, double cp, double cs, double x0, double y0, double z0,
+                             int moment, const double* f, const double* m, int kind, double freq,
+                             double t0, double t, double* u)
+{
+   const long ni = ie - ib + 1, nij = ni * (je - jb + 1), npts = nij * (ke - kb + 1);
+   const double a = cp, b = cs, s = t - t0, eps = 1e-3 * h, c4 = 1 / (4 * M_PI * rho);
+   double M[3][3] = {{0}};
+   if (moment) {
+      M[0][0] = m[0]; M[0][1] = M[1][0] = m[1]; M[0][2] = M[2][0] = m[2];
+      M[1][1] = m[3]; M[1][2] = M[2][1] = m[4]; M[2][2] = m[5];
+   }
+   gl_init();
+#pragma omp parallel for collapse(2)
+   for (int k = kb; k <= ke; k++)
+      for (int j = jb; j <= je; j++)
+         for (int i = ib; i <= ie; i++) {
+            const long p = (i - ib) + ni * (j - jb) + nij * (k - kb);
+            const double d[3] = {(i - 1) * h - x0, (j - 1) * h - y0, zmin + (k - 1) * h - z0};
+            const double R = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            double out[3] = {0, 0, 0};
+            if (R >= eps) {
+               const double g[3] = {d[0] / R, d[1] / R, d[2] / R};
+               const double ga = hist(kind, freq, s - R / a), gb = hist(kind, freq, s - R / b);
+               const double I = near_integral(kind, freq, s, R / a, R / b);
+               if (!moment) {
+                  /* A&R 4.23 */
+                  const double gf = g[0] * f[0] + g[1] * f[1] + g[2] * f[2];
+                  for (int n = 0; n < 3; n++)
+                     out[n] = c4 * (g[n] * gf * (3 * I / (R * R * R) + ga / (a * a * R) - gb / (b * b * R)) +
+                                    f[n] * (gb / (b * b * R) - I / (R * R * R)));
+               } else {
+                  /* A&R 4.29 contracted with the symmetric M */
+                  const double da = hist_dt(kind, freq, s - R / a), db = hist_dt(kind, freq, s - R / b);
+                  double Mg[3], gMg = 0, tr = M[0][0] + M[1][1] + M[2][2];
+                  for (int n = 0; n < 3; n++) {
+                     Mg[n] = M[n][0] * g[0] + M[n][1] * g[1] + M[n][2] * g[2];
+                     gMg += g[n] * Mg[n];
+                  }
+                  const double R2 = R * R, R4 = R2 * R2;
+                  for (int n = 0; n < 3; n++)
+                     out[n] = c4 * ((15 * g[n] * gMg - 3 * g[n] * tr - 6 * Mg[n]) * I / R4 +
+                                    (6 * g[n] * gMg - g[n] * tr - 2 * Mg[n]) * ga / (a * a * R2) -
+                                    (6 * g[n] * gMg - g[n] * tr - 3 * Mg[n]) * gb / (b * b * R2) +
+                                    g[n] * gMg * da / (a * a * a * R) -
+                                    (g[n] * gMg - Mg[n]) * db / (b * b * b * R));
+               }
+            }
+            for (int c = 0; c < 3; c++) u[c * npts + p] = out[c];
+         }
+}
+
+void sw4o_solerr3(int ib, int ie, int jb, int je, int kb, int ke, double h, double zmin,
+                  const double* uex, const double* u, double x0, double y0, double z0,
+                  double radius, int imin, int imax, int jmin, int jmax, int kmin, int kmax,
+                  double* li, double* l2, double* xli)
+{
+   const long ni = ie - ib + 1, nij = ni * (je - jb + 1), npts = nij * (ke - kb + 1);
+   const double r2 = radius < 0 ? -radius * radius : radius * radius, h3 = h * h * h;
+   double mx = 0, sq = 0, xm = 0;
+   for (int c = 0; c < 3; c++)
+      for (int k = kmin; k <= kmax; k++)
+         for (int j = jmin; j <= jmax; j++)
+            for (int i = imin; i <= imax; i++) {
+               const double dx = (i - 1) * h - x0, dy = (j - 1) * h - y0, dz = (k - 1) * h + zmin - z0;
+               if (!(dx * dx + dy * dy + dz * dz > r2)) continue;
+               const long q = c * npts + (i - ib) + ni * (j - jb) + nij * (k - kb);
+               const double e = u[q] - uex[q];
+               if (fabs(e) > mx) mx = fabs(e);
+               if (uex[q] > xm) xm = uex[q];
+               sq += h3 * e * e;
+            }
+   *li = mx;
+   *l2 = sqrt(sq);
+   *xli = xm;
+}

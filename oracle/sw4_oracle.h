@@ -112,6 +112,28 @@ typedef struct {
 void sw4o_step(const sw4o_problem* p, int soa, double t, double* up, const double* u,
                const double* um, double* lu, double* f, double* uacc);
 
+/* Analytic whole-space displacement of one point source in a homogeneous medium
+ * (rho, cp, cs) at time t, written SoA over the array [ib,ie]x[jb,je]x[kb,ke]
+ * with x=(i-1)h, y=(j-1)h, z=zmin+(k-1)h: the field the reference compares
+ * its point-source test against (EW::get_exact_point_source, src/EW.C:3899).
+ * moment=0: force (f[0..2]); moment=1: moment tensor m[] = mxx,mxy,mxz,myy,myz,mzz.
+ * kind: 0 Gaussian, 1 C6SmoothBump, 3 VerySmoothBump (as sw4o_timefunc).
+ * Points closer than 1e-3 h to the source get 0, as in the reference. */
+void sw4o_exact_point_source(int ib, int ie, int jb, int je, int kb, int ke, double h, double zmin,
+                             double rho, double cp, double cs, double x0, double y0, double z0,
+                             int moment, const double* f, const double* m, int kind, double freq,
+                             double t0, double t, double* u);
+
+/* Error norms of u against uex (SoA) over [imin,imax]x[jmin,jmax]x[kmin,kmax],
+ * skipping points within `radius` of (x0,y0,z0) (radius < 0: skip none):
+ * li = max |u - uex|, l2 = sqrt(sum h^3 (u - uex)^2), xli = max(0, max uex)
+ * (EW::solerr3fort, src/ew-cfromfort.C:144, and the square root taken in
+ * EW::normOfDifference, src/EW.C:4537-4600). */
+void sw4o_solerr3(int ib, int ie, int jb, int je, int kb, int ke, double h, double zmin,
+                  const double* uex, const double* u, double x0, double y0, double z0,
+                  double radius, int imin, int imax, int jmin, int jmax, int kmin, int kmax,
+                  double* li, double* l2, double* xli);
+
 #ifdef __cplusplus
 }
 #endif
