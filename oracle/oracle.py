@@ -122,6 +122,78 @@ def addsgd(order, soa, bounds, up, u, um, rho, dc, st, co, beta, which="oracle")
        _dp(co[1]), _dp(co[2]), C.c_double(beta))
 
 
+def rhs4sgcurv(soa, bounds, onesided, lu, u, mu, la, met, jac, strx, stry, which="oracle"):
+    """Curvilinear operator (rhs4sgcurv_rev.C / rhs4sgcurv.C)."""
+    os_arr, os_p = _ip(onesided)
+    if which == "ref":
+        acof, ghcof, bope, _ = stencil_coefficients("ref")
+        ref().sw4ref_rhs4sgcurv(C.c_int(soa), *[C.c_int(b) for b in bounds], _dp(u), _dp(mu),
+                                _dp(la), _dp(met), _dp(jac), _dp(lu), os_p, _dp(acof), _dp(bope),
+                                _dp(ghcof), _dp(strx), _dp(stry))
+    else:
+        lib().sw4o_rhs4sgcurv(C.c_int(soa), *[C.c_int(b) for b in bounds], _dp(u), _dp(mu),
+                              _dp(la), _dp(met), _dp(jac), _dp(lu), os_p, _dp(strx), _dp(stry))
+
+
+def metric(soa, bounds, h, z, met, jac, which="oracle"):
+    """Numerical metric from z (EW::metric_rev); returns the status (0 ok)."""
+    if which == "ref":
+        ib, ie, jb, je, kb, ke = bounds
+        shape = (ke - kb + 1, je - jb + 1, ie - ib + 1)
+        k, j, i = np.meshgrid(np.arange(kb, ke + 1), np.arange(jb, je + 1), np.arange(ib, ie + 1),
+                              indexing="ij")
+        x = np.ascontiguousarray(((i - 1) * h).reshape(-1), dtype=np.float64)
+        y = np.ascontiguousarray(((j - 1) * h).reshape(-1), dtype=np.float64)
+        assert x.size == int(np.prod(shape))
+        ref().sw4ref_metric.restype = C.c_int
+        return ref().sw4ref_metric(C.c_int(soa), *[C.c_int(b) for b in bounds], _dp(x), _dp(y),
+                                   _dp(z), _dp(met), _dp(jac))
+    lib().sw4o_metric.restype = C.c_int
+    return lib().sw4o_metric(C.c_int(soa), *[C.c_int(b) for b in bounds], C.c_double(h), _dp(z),
+                             _dp(met), _dp(jac))
+
+
+def gaussian_hill_z(bounds, nz, h, zmax, amp, xc, yc, lx, ly, zeta_break=0.95, order=4):
+    """z of the curvilinear grid over a Gaussian hill (EW::grid_mapping)."""
+    ib, ie, jb, je, kb, ke = bounds
+    z = np.zeros((ie - ib + 1) * (je - jb + 1) * (ke - kb + 1))
+    lib().sw4o_gaussian_hill_z(*[C.c_int(b) for b in bounds], C.c_int(nz), C.c_double(h),
+                               C.c_double(zmax), C.c_double(zeta_break), C.c_int(order),
+                               C.c_double(amp), C.c_double(xc), C.c_double(yc), C.c_double(lx),
+                               C.c_double(ly), _dp(z))
+    return z
+
+
+def freesurfcurvisg(soa, bounds, nz, side, u, mu, la, met, sbop, forcing, strx, stry,
+                    which="oracle"):
+    ib, ie, jb, je, kb, ke = bounds
+    if forcing is None and which == "ref":
+        forcing = np.zeros(3 * (ie - ib + 1) * (je - jb + 1))
+    fn = ref().sw4ref_freesurfcurvisg if which == "ref" else lib().sw4o_freesurfcurvisg
+    fn(C.c_int(soa), *[C.c_int(b) for b in bounds], C.c_int(nz), C.c_int(side), _dp(u), _dp(mu),
+       _dp(la), _dp(met), _dp(sbop), _dp(forcing) if forcing is not None else _D(), _dp(strx),
+       _dp(stry))
+
+
+def addsgd4c(soa, bounds, up, u, um, rho, dcx, dcy, strx, stry, jac, cox, coy, beta,
+             which="oracle"):
+    fn = ref().sw4ref_addsgd4c if which == "ref" else lib().sw4o_addsgd4c
+    fn(C.c_int(soa), *[C.c_int(b) for b in bounds], _dp(up), _dp(u), _dp(um), _dp(rho), _dp(dcx),
+       _dp(dcy), _dp(strx), _dp(stry), _dp(jac), _dp(cox), _dp(coy), C.c_double(beta))
+
+
+def sym3_min_eig(a6):
+    a = np.ascontiguousarray(a6, dtype=np.float64)
+    lib().sw4o_sym3_min_eig.restype = C.c_double
+    return lib().sw4o_sym3_min_eig(_dp(a))
+
+
+def curv_dt(soa, bounds, rho, mu, la, met, jac, cfl):
+    lib().sw4o_curv_dt.restype = C.c_double
+    return lib().sw4o_curv_dt(C.c_int(soa), *[C.c_int(b) for b in bounds], _dp(rho), _dp(mu),
+                              _dp(la), _dp(met), _dp(jac), C.c_double(cfl))
+
+
 def boundary_windows(bounds, nxyz, bccnd):
     wind = np.zeros(36, dtype=np.int32)
     npts = np.zeros(6, dtype=np.int32)

@@ -112,6 +112,36 @@ typedef struct {
 void sw4o_step(const sw4o_problem* p, int soa, double t, double* up, const double* u,
                const double* um, double* lu, double* f, double* uacc);
 
+/* ---- curvilinear grid (sw4_oracle_curv.c) ---- */
+/* Curvilinear operator, rhs4sgcurv_rev.C:34 (soa=1) / rhs4sgcurv.C:34 (soa=0);
+ * met is 4 components (SoA or AoS as u).  Only onesided[4] (top) is used. */
+void sw4o_rhs4sgcurv(int soa, int ib, int ie, int jb, int je, int kb, int ke, const double* u,
+                     const double* mu, const double* la, const double* met, const double* jac,
+                     double* lu, const int* onesided, const double* strx, const double* stry);
+/* Numerical metric from z (EW::metric_rev, curvilinear-c.C:175); -1 if z_r <= 0. */
+int sw4o_metric(int soa, int ib, int ie, int jb, int je, int kb, int ke, double h, const double* z,
+                double* met, double* jac);
+/* z of a curvilinear grid over a Gaussian hill (EW::grid_mapping, EW.C:5694). */
+void sw4o_gaussian_hill_z(int ib, int ie, int jb, int je, int kb, int ke, int nz, double h,
+                          double zmax, double zeta_break, int order, double amp, double xc,
+                          double yc, double lx, double ly, double* z);
+/* Curvilinear free-surface ghost plane (EW::freesurfcurvisg_rev, curvilinear-c.C:621). */
+void sw4o_freesurfcurvisg(int soa, int ib, int ie, int jb, int je, int kb, int ke, int nz, int side,
+                          double* u, const double* mu, const double* la, const double* met,
+                          const double* sbop, const double* forcing, const double* strx,
+                          const double* stry);
+/* Curvilinear supergrid damping (EW::addsgd4cfort_indrev, ew-cfromfort.C:1323). */
+void sw4o_addsgd4c(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
+                   const double* u, const double* um, const double* rho, const double* dcx,
+                   const double* dcy, const double* strx, const double* stry, const double* jac,
+                   const double* cox, const double* coy, double beta);
+/* Smallest eigenvalue of a symmetric 3x3 matrix [a00 a01 a02 a11 a12 a22]. */
+double sw4o_sym3_min_eig(const double a[6]);
+/* Curvilinear time-step limit cfl / sqrt(max eig) (EW::computeDT, EW.C:5066-5125). */
+double sw4o_curv_dt(int soa, int ib, int ie, int jb, int je, int kb, int ke, const double* rho,
+                    const double* mu, const double* la, const double* met, const double* jac,
+                    double cfl);
+
 /* Analytic whole-space displacement of one point source in a homogeneous medium
  * (rho, cp, cs) at time t, written SoA over the array [ib,ie]x[jb,je]x[kb,ke]
  * with x=(i-1)h, y=(j-1)h, z=zmin+(k-1)h: the field the reference compares
