@@ -97,6 +97,62 @@ int sw4g_bcfortsg(int soa, int ib, int ie, int jb, int je, int kb, int ke, const
                   const double* strx, const double* stry, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Curvilinear-grid kernels (topography).  met is the 4-component metric in the
+ * same layout as u (soa=1: component-major, met[c*npts + p]; soa=0: met[4p + c]).
+ * ------------------------------------------------------------------------- */
+
+/* lu = curvilinear divergence of stress over i,j in [first+2, last-2] and
+ * k in [kfirst+2, klast-2], with the SBP top rows k=1..6 when onesided[4] == 1
+ * (then kfirst <= 0 and klast >= 8 are required); replaces rhs4sgcurv /
+ * rhs4sgcurv_rev (src/EW.C:150-160, src/rhs4sgcurv.C:34, src/rhs4sgcurv_rev.C:34).
+ * The SBP tables are the library's own (the reference passes acof/bope/ghcof). */
+int sw4g_rhs4sgcurv(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                    const int* onesided, double* lu, const double* u, const double* mu,
+                    const double* lambda, const double* met, const double* jac, const double* strx,
+                    const double* stry, void* stream);
+
+/* Metric and Jacobian from the grid's z over the whole array (x, y are (i-1)h,
+ * (j-1)h); replaces EW::metric / metric_rev (src/curvilinear-c.C:53, :175).
+ * Synchronises the stream; SW4G_BAD_ARGUMENT if z_r <= 0 somewhere (the
+ * reference returns -1). */
+int sw4g_metric(int soa, int ib, int ie, int jb, int je, int kb, int ke, double h, const double* z,
+                double* met, double* jac, void* stream);
+
+/* z of a curvilinear grid of nz points over a Gaussian hill
+ * -amp*exp(-((x-xc)/lx)^2-((y-yc)/ly)^2) down to z = zmax (SoA scalar array);
+ * replaces EW::generate_grid with the analytic topography (src/EW.C:6164,
+ * grid_mapping :5694, interpolate_topography :5619-5627). */
+int sw4g_gaussian_hill_grid(int ib, int ie, int jb, int je, int kb, int ke, int nz, double h,
+                            double zmax, double zeta_break, int order, double amp, double xc,
+                            double yc, double lx, double ly, double* z, void* stream);
+
+/* Ghost plane k=0 (side 5) or k=nz+1 (side 6) from the traction condition on a
+ * curvilinear grid, i,j in [first+2, last-2]; forcing: 3 x ni x nj point-major
+ * device array or NULL; sbop: 5 host doubles; replaces EW::freesurfcurvisg /
+ * freesurfcurvisg_rev (src/curvilinear-c.C:465, :621). */
+int sw4g_freesurfcurvisg(int soa, int ib, int ie, int jb, int je, int kb, int ke, int nz, int side,
+                         double* u, const double* mu, const double* lambda, const double* met,
+                         const double* sbop, const double* forcing, const double* strx,
+                         const double* stry, void* stream);
+
+/* 4th-order supergrid damping in x and y on a curvilinear grid; replaces
+ * EW::addsgd4cfort / addsgd4cfort_indrev (src/ew-cfromfort.C:1160, :1323). */
+int sw4g_addsgd4cfort(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                      double* up, const double* u, const double* um, const double* rho,
+                      const double* dcx, const double* dcy, const double* strx, const double* stry,
+                      const double* jac, const double* cox, const double* coy, double beta,
+                      void* stream);
+
+/* dt = cfl / sqrt(max over the grid of -lambda_min(A)/(4 rho)), the curvilinear
+ * limit of EW::computeDT (src/EW.C:5066-5125).  The reference gets lambda_min from
+ * LAPACK dspev; here it is the closed form for a symmetric 3x3 matrix.
+ * Synchronises the stream. */
+int sw4g_curvilinear_time_step(int soa, int ib, int ie, int jb, int je, int kb, int ke,
+                               const double* rho, const double* mu, const double* lambda,
+                               const double* met, const double* jac, double cfl, double* dt,
+                               void* stream);
+
+/* ---------------------------------------------------------------------------
  * Phase-level entry points for the one-sided SBP rows (SoA fields only)
  * ------------------------------------------------------------------------- */
 

@@ -86,6 +86,13 @@ _SIGS = {
     "sw4g_ew_field": ([_VP, C.c_int], _VP),
     "sw4g_ew_step": ([_VP, C.c_int, C.c_int], C.c_int),
     "sw4g_ew_enforce_bc": ([_VP, _VP], C.c_int),
+    "sw4g_rhs4sgcurv": ([C.c_int] * 7 + [_I] + [_VP] * 8 + [_VP], C.c_int),
+    "sw4g_metric": ([C.c_int] * 7 + [C.c_double, _VP, _VP, _VP, _VP], C.c_int),
+    "sw4g_gaussian_hill_grid": ([C.c_int] * 7 + [C.c_double] * 3 + [C.c_int] + [C.c_double] * 5
+                                + [_VP, _VP], C.c_int),
+    "sw4g_freesurfcurvisg": ([C.c_int] * 9 + [_VP] * 4 + [_D] + [_VP] * 3 + [_VP], C.c_int),
+    "sw4g_addsgd4cfort": ([C.c_int] * 7 + [_VP] * 11 + [C.c_double, _VP], C.c_int),
+    "sw4g_curvilinear_time_step": ([C.c_int] * 7 + [_VP] * 5 + [C.c_double, _D, _VP], C.c_int),
     "sw4g_nearest_grid_point": ([C.POINTER(GridDesc), C.c_double, C.c_double, C.c_double, _I],
                                 C.c_int),
     "sw4g_ew_set_receivers": ([_VP, C.c_int, _I, _I, C.c_int], C.c_int),

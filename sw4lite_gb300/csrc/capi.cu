@@ -1,5 +1,6 @@
 // extern "C" entry points of libsw4g.so (declared in include/sw4g.h).
 #include <cmath>
+#include <vector>
 #include <cstring>
 #include <exception>
 #include <new>
@@ -103,6 +104,110 @@ int sw4g_rhs4sg(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirs
    if (onesided[5] == 1 && (kfirst > nk - 7 || klast < nk + 1)) return SW4G_BAD_ARGUMENT;
    return launch_rhs4sg_direct(soa, ifirst, ilast, jfirst, jlast, kfirst, klast, nk, onesided, lu,
                                u, mu, lambda, h, strx, stry, strz, as_stream(stream));
+}
+
+int sw4g_rhs4sgcurv(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                    const int* onesided, double* lu, const double* u, const double* mu,
+                    const double* lambda, const double* met, const double* jac, const double* strx,
+                    const double* stry, void* stream)
+{
+   if (!onesided || !lu || !u || !mu || !lambda || !met || !jac || !strx || !stry)
+      return SW4G_BAD_ARGUMENT;
+   if (!bounds_ok(ifirst, ilast, jfirst, jlast, kfirst, klast)) return SW4G_BAD_ARGUMENT;
+   if (onesided[4] == 1 && (kfirst > 0 || klast < 8)) return SW4G_BAD_ARGUMENT;
+   CurvSpec c;
+   c.soa = soa;
+   c.ib = ifirst; c.ie = ilast; c.jb = jfirst; c.je = jlast; c.kb = kfirst; c.ke = klast;
+   c.u = u; c.mu = mu; c.la = lambda; c.met = met; c.jac = jac; c.strx = strx; c.stry = stry;
+   return launch_rhs4sgcurv(c, onesided, lu, as_stream(stream));
+}
+
+int sw4g_metric(int soa, int ib, int ie, int jb, int je, int kb, int ke, double h, const double* z,
+                double* met, double* jac, void* stream)
+{
+   if (!z || !met || !jac || !(h > 0) || !bounds_ok(ib, ie, jb, je, kb, ke)) return SW4G_BAD_ARGUMENT;
+   int* flag = nullptr;
+   if (cudaMalloc(&flag, sizeof(int)) != cudaSuccess) return SW4G_CUDA_ERROR;
+   cudaStream_t s = as_stream(stream);
+   int st = cudaMemsetAsync(flag, 0, sizeof(int), s) == cudaSuccess ? SW4G_OK : SW4G_CUDA_ERROR;
+   if (st == SW4G_OK) st = launch_metric(soa, ib, ie, jb, je, kb, ke, h, z, met, jac, flag, s);
+   int bad = 0;
+   if (st == SW4G_OK &&
+       (cudaMemcpyAsync(&bad, flag, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess))
+      st = SW4G_CUDA_ERROR;
+   cudaFree(flag);
+   if (st == SW4G_OK && bad) st = SW4G_BAD_ARGUMENT;
+   return st;
+}
+
+int sw4g_gaussian_hill_grid(int ib, int ie, int jb, int je, int kb, int ke, int nz, double h,
+                            double zmax, double zeta_break, int order, double amp, double xc,
+                            double yc, double lx, double ly, double* z, void* stream)
+{
+   if (!z || !(h > 0) || nz < 2 || order < 1 || !(zeta_break > 0) || !(lx > 0) || !(ly > 0) ||
+       !bounds_ok(ib, ie, jb, je, kb, ke))
+      return SW4G_BAD_ARGUMENT;
+   return launch_gaussian_hill_z(ib, ie, jb, je, kb, ke, nz, h, zmax, zeta_break, order, amp, xc,
+                                 yc, lx, ly, z, as_stream(stream));
+}
+
+int sw4g_freesurfcurvisg(int soa, int ib, int ie, int jb, int je, int kb, int ke, int nz, int side,
+                         double* u, const double* mu, const double* lambda, const double* met,
+                         const double* sbop, const double* forcing, const double* strx,
+                         const double* stry, void* stream)
+{
+   if (!u || !mu || !lambda || !met || !sbop || !strx || !stry || !bounds_ok(ib, ie, jb, je, kb, ke))
+      return SW4G_BAD_ARGUMENT;
+   if (side != 5 && side != 6) return SW4G_BAD_ARGUMENT;
+   const int k = side == 5 ? 1 : nz;
+   if (k - 1 < kb || k + 1 > ke || (side == 5 && 4 > ke) || (side == 6 && nz - 3 < kb))
+      return SW4G_BAD_ARGUMENT;
+   CurvSpec c;
+   c.soa = soa;
+   c.ib = ib; c.ie = ie; c.jb = jb; c.je = je; c.kb = kb; c.ke = ke;
+   c.u = u; c.mu = mu; c.la = lambda; c.met = met; c.strx = strx; c.stry = stry;
+   return launch_freesurfcurvisg(c, nz, side, sbop, forcing, u, as_stream(stream));
+}
+
+int sw4g_addsgd4cfort(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                      double* up, const double* u, const double* um, const double* rho,
+                      const double* dcx, const double* dcy, const double* strx, const double* stry,
+                      const double* jac, const double* cox, const double* coy, double beta,
+                      void* stream)
+{
+   if (!up || !u || !um || !rho || !dcx || !dcy || !strx || !stry || !jac || !cox || !coy ||
+       !bounds_ok(ifirst, ilast, jfirst, jlast, kfirst, klast))
+      return SW4G_BAD_ARGUMENT;
+   return launch_addsgd4c(soa, ifirst, ilast, jfirst, jlast, kfirst, klast, up, u, um, rho, dcx,
+                          dcy, strx, stry, jac, cox, coy, beta, as_stream(stream));
+}
+
+int sw4g_curvilinear_time_step(int soa, int ib, int ie, int jb, int je, int kb, int ke,
+                               const double* rho, const double* mu, const double* lambda,
+                               const double* met, const double* jac, double cfl, double* dt,
+                               void* stream)
+{
+   if (!rho || !mu || !lambda || !met || !jac || !dt || !(cfl > 0) || !bounds_ok(ib, ie, jb, je, kb, ke))
+      return SW4G_BAD_ARGUMENT;
+   const long long n = (long long)(ie - ib + 1) * (je - jb + 1) * (ke - kb + 1);
+   const int nb = 152 * 4;
+   double* bm = nullptr;
+   if (cudaMalloc(&bm, nb * sizeof(double)) != cudaSuccess) return SW4G_CUDA_ERROR;
+   cudaStream_t s = as_stream(stream);
+   std::vector<double> h(nb);
+   int st = launch_curv_eig(soa, n, rho, mu, lambda, met, jac, bm, nb, s);
+   if (st == SW4G_OK &&
+       (cudaMemcpyAsync(h.data(), bm, nb * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess))
+      st = SW4G_CUDA_ERROR;
+   cudaFree(bm);
+   if (st != SW4G_OK) return st;
+   double e = -1;
+   for (double v : h) e = v > e ? v : e;
+   if (!(e > 0)) return SW4G_BAD_ARGUMENT;
+   *dt = cfl / std::sqrt(e);
+   return SW4G_OK;
 }
 
 int sw4g_predfort(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,

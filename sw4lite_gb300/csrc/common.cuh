@@ -75,6 +75,15 @@ enum Status : int {
    kTimeout = 5,
 };
 
+// Returns from the calling function with the status of expr unless it is kOk.
+#define SW4G_TRY(expr)            \
+   do {                           \
+      int _st = (expr);           \
+      if (_st != kOk) return _st; \
+   } while (0)
+
+inline int cuda_ok(cudaError_t e) { return e == cudaSuccess ? kOk : kCudaError; }
+
 // Converts the sticky/launch error state into a status code.
 inline int launch_status()
 {

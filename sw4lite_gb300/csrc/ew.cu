@@ -7,16 +7,6 @@
 
 namespace sw4g {
 
-namespace {
-#define SW4G_TRY(expr)                  \
-   do {                                 \
-      int _st = (expr);                 \
-      if (_st != kOk) return _st;       \
-   } while (0)
-
-int cuda_ok(cudaError_t e) { return e == cudaSuccess ? kOk : kCudaError; }
-}  // namespace
-
 EW::EW(const GridSpec& g, cudaStream_t stream) : g_(g), stream_(stream) {}
 
 EW::~EW()

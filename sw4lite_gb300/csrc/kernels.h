@@ -101,6 +101,36 @@ struct ReceiverSet {
    const int* off = nullptr;   // n
 };
 
+// A curvilinear grid's arrays for the curvilinear kernels (curv.cu): 3-component
+// field u and 4-component metric met in the same layout (soa: component-major).
+struct CurvSpec {
+   int soa = 1;
+   int ib = 0, ie = 0, jb = 0, je = 0, kb = 0, ke = 0;
+   const double* u = nullptr;
+   const double* mu = nullptr;
+   const double* la = nullptr;
+   const double* met = nullptr;
+   const double* jac = nullptr;
+   const double* strx = nullptr;
+   const double* stry = nullptr;
+};
+
+int launch_rhs4sgcurv(const CurvSpec& s, const int onesided[6], double* lu, cudaStream_t st);
+int launch_metric(int soa, int ib, int ie, int jb, int je, int kb, int ke, double h, const double* z,
+                  double* met, double* jac, int* bad_flag, cudaStream_t st);
+int launch_gaussian_hill_z(int ib, int ie, int jb, int je, int kb, int ke, int nz, double h,
+                           double zmax, double zeta_break, int order, double amp, double xc,
+                           double yc, double lx, double ly, double* z, cudaStream_t st);
+int launch_freesurfcurvisg(const CurvSpec& s, int nz, int side, const double* sbop,
+                           const double* forcing, double* u, cudaStream_t st);
+int launch_addsgd4c(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
+                    const double* u, const double* um, const double* rho, const double* dcx,
+                    const double* dcy, const double* strx, const double* stry, const double* jac,
+                    const double* cox, const double* coy, double beta, cudaStream_t st);
+int launch_curv_eig(int soa, long long n, const double* rho, const double* mu, const double* la,
+                    const double* met, const double* jac, double* blockmax, int nblocks,
+                    cudaStream_t st);
+
 int receiver_values(int mode);  // values one receiver records per step (0: bad mode)
 int launch_record(const Box& b, const double* up, const double* um, const ReceiverSet& r,
                   double* row, double dt, double h, int initial, cudaStream_t s);
