@@ -262,6 +262,23 @@ def step(problem: Problem, soa, t, up, u, um, lu, f, uacc, which="oracle"):
        _dp(uacc))
 
 
+class Curv(C.Structure):
+    """Mirror of sw4o_curv (oracle/sw4_oracle.h)."""
+    _fields_ = [("ib", C.c_int), ("ie", C.c_int), ("jb", C.c_int), ("je", C.c_int),
+                ("kb", C.c_int), ("ke", C.c_int), ("nx", C.c_int), ("ny", C.c_int),
+                ("nz", C.c_int), ("h", C.c_double), ("bccnd", C.c_int * 6),
+                ("wind", C.c_int * 36), ("rho", _D), ("mu", _D), ("la", _D), ("met", _D),
+                ("jac", _D), ("strx", _D), ("stry", _D), ("dcx", _D), ("dcy", _D), ("cox", _D),
+                ("coy", _D)]
+
+
+def step_topo(problem: Problem, curv: Curv, t, cart_arrays, curv_arrays, which="oracle"):
+    """One two-grid step; *_arrays = (up, u, um, lu, f, uacc) of each grid."""
+    fn = ref().sw4ref_step_topo if which == "ref" else lib().sw4o_step_topo
+    fn(C.byref(problem), C.byref(curv), C.c_double(t), *[_dp(a) for a in cart_arrays],
+       *[_dp(a) for a in curv_arrays])
+
+
 def nearest_grid_point(h, zmin, x, y, z):
     """EW::computeNearestGridPoint (src/EW.C:5149-5177) for one Cartesian grid:
     1-based (i, j, k) of the nearest point, a half-way point going to the lower index."""

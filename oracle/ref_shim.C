@@ -280,4 +280,98 @@ void sw4ref_step(const sw4o_problem* p, int soa, double t, double* up, const dou
    bc(up);
 }
 
+
+// The two-grid step of sw4o_step_topo with the reference's own kernels
+// (rhs4sg_rev, rhs4sgcurv_rev, predfort, dpdmtfort, corrfort, addsgd4fort_indrev,
+// addsgd4cfort_indrev, bcfortsg_indrev, freesurfcurvisg_rev) in the order of
+// src/EW.C:2537-2756 and the interface copy of src/EW.C:3504.
+void sw4ref_step_topo(const sw4o_problem* p, const sw4o_curv* cv, double t, double* up,
+                      const double* u, const double* um, double* lu, double* f, double* uacc,
+                      double* cup, const double* cu, const double* cum, double* clu, double* cf,
+                      double* cuacc)
+{
+   double acof[384], ghcof[6], bope[48], sbop[5];
+   EW* ew = kernel_host(1);
+   ew->GetStencilCoefficients(acof, ghcof, bope, sbop);
+   const long npts = (long)(p->ie - p->ib + 1) * (p->je - p->jb + 1) * (p->ke - p->kb + 1);
+   const long cnpts = (long)(cv->ie - cv->ib + 1) * (cv->je - cv->jb + 1) * (cv->ke - cv->kb + 1);
+   const double dt = p->dt;
+   int onesided[6], onesided_c[6] = {0, 0, 0, 0, cv->bccnd[4] == 0, 0};
+   for (int s = 0; s < 6; s++) onesided[s] = p->onesided[s];
+   int wind[36], cwind[36], npw[6], cnpw[6];
+   sw4o_boundary_windows(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, p->nx, p->ny, p->nz, p->bccnd,
+                         wind, npw);
+   sw4o_boundary_windows(cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cv->nx, cv->ny, cv->nz,
+                         cv->bccnd, cwind, cnpw);
+   std::vector<std::vector<double>> bf(6), cbf(6);
+   for (int s = 0; s < 6; s++) {
+      bf[s].assign(3 * (npw[s] > 0 ? npw[s] : 1), 0.0);
+      cbf[s].assign(3 * (cnpw[s] > 0 ? cnpw[s] : 1), 0.0);
+   }
+   std::vector<double> fsforce(3 * (size_t)(cv->ie - cv->ib + 1) * (cv->je - cv->jb + 1), 0.0);
+   auto D = [](const double* x) { return const_cast<double*>(x); };
+   auto bc = [&](double* w, double* cw) {
+      sw4ref_bcfortsg(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, wind, p->nx, p->ny, p->nz, w,
+                      p->h, p->bccnd, sbop, D(p->mu), D(p->la), t + dt, bf[0].data(), bf[1].data(),
+                      bf[2].data(), bf[3].data(), bf[4].data(), bf[5].data(), D(p->strx), D(p->stry));
+      sw4ref_bcfortsg(1, cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cwind, cv->nx, cv->ny,
+                      cv->nz, cw, cv->h, cv->bccnd, sbop, D(cv->mu), D(cv->la), t + dt,
+                      cbf[0].data(), cbf[1].data(), cbf[2].data(), cbf[3].data(), cbf[4].data(),
+                      cbf[5].data(), D(cv->strx), D(cv->stry));
+      if (cv->bccnd[4] == 0)
+         ew->freesurfcurvisg_rev(cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cv->nz, 5, cw,
+                                 D(cv->mu), D(cv->la), D(cv->met), sbop, fsforce.data(),
+                                 D(cv->strx), D(cv->stry));
+      // enforceCartTopo, src/EW.C:3504-3530, with 2 ghost points
+      const long ni = p->ie - p->ib + 1, nij = ni * (p->je - p->jb + 1);
+      const long cni = cv->ie - cv->ib + 1, cnij = cni * (cv->je - cv->jb + 1);
+      for (int j = p->jb; j <= p->je; j++)
+         for (int i = p->ib; i <= p->ie; i++)
+            for (int c = 0; c < 3; c++) {
+               for (int q = 0; q < 2; q++)
+                  w[c * npts + (i - p->ib) + ni * (j - p->jb) + nij * (p->kb + q - p->kb)] =
+                      cw[c * cnpts + (i - cv->ib) + cni * (j - cv->jb) +
+                         cnij * (cv->ke - 4 + q - cv->kb)];
+               for (int q = 0; q <= 2; q++)
+                  cw[c * cnpts + (i - cv->ib) + cni * (j - cv->jb) + cnij * (cv->ke - q - cv->kb)] =
+                      w[c * npts + (i - p->ib) + ni * (j - p->jb) + nij * (p->kb + 4 - q - p->kb)];
+            }
+   };
+   sw4o_force(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, f, p->nsrc, p->src_ijk, p->src_amp,
+              p->src_freq, p->src_t0, p->src_kind, t, 0);
+   std::memset(cf, 0, 3 * cnpts * sizeof(double));
+   std::memset(lu, 0, 3 * npts * sizeof(double));
+   std::memset(clu, 0, 3 * cnpts * sizeof(double));
+   rhs4sg_rev(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, p->nz, onesided, acof, bope, ghcof, lu,
+              D(u), D(p->mu), D(p->la), p->h, D(p->strx), D(p->stry), D(p->strz));
+   rhs4sgcurv_rev(cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, D(cu), D(cv->mu), D(cv->la),
+                  D(cv->met), D(cv->jac), clu, onesided_c, acof, bope, ghcof, D(cv->strx),
+                  D(cv->stry));
+   ew->predfort(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, D(u), D(um), lu, f, D(p->rho), dt * dt);
+   ew->predfort(cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cup, D(cu), D(cum), clu, cf,
+                D(cv->rho), dt * dt);
+   bc(up, cup);
+   sw4o_force(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, f, p->nsrc, p->src_ijk, p->src_amp,
+              p->src_freq, p->src_t0, p->src_kind, t, 1);
+   ew->dpdmtfort(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, D(u), D(um), uacc, 1.0 / (dt * dt));
+   ew->dpdmtfort(cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cup, D(cu), D(cum), cuacc,
+                 1.0 / (dt * dt));
+   rhs4sg_rev(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, p->nz, onesided, acof, bope, ghcof, lu,
+              uacc, D(p->mu), D(p->la), p->h, D(p->strx), D(p->stry), D(p->strz));
+   rhs4sgcurv_rev(cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cuacc, D(cv->mu), D(cv->la),
+                  D(cv->met), D(cv->jac), clu, onesided_c, acof, bope, ghcof, D(cv->strx),
+                  D(cv->stry));
+   ew->corrfort(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, lu, f, D(p->rho), dt * dt * dt * dt);
+   ew->corrfort(cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cup, clu, cf, D(cv->rho),
+                dt * dt * dt * dt);
+   if (p->sg_beta != 0) {
+      ew->addsgd4fort_indrev(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, D(u), D(um), D(p->rho),
+                             D(p->dcx), D(p->dcy), D(p->dcz), D(p->strx), D(p->stry), D(p->strz),
+                             D(p->cox), D(p->coy), D(p->coz), p->sg_beta);
+      ew->addsgd4cfort_indrev(cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cup, D(cu), D(cum),
+                              D(cv->rho), D(cv->dcx), D(cv->dcy), D(cv->strx), D(cv->stry),
+                              D(cv->jac), D(cv->cox), D(cv->coy), p->sg_beta);
+   }
+   bc(up, cup);
+}
 }  // extern "C"

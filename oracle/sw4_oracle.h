@@ -142,6 +142,30 @@ double sw4o_curv_dt(int soa, int ib, int ie, int jb, int je, int kb, int ke, con
                     const double* mu, const double* la, const double* met, const double* jac,
                     double cfl);
 
+/* Two-grid step over topography: a curvilinear grid on top of the Cartesian grid
+ * of `cart` (whose top side, bccnd[4] = 4, is the interface).  The reference's
+ * time loop order for both grids (EW.C:2537-2756) with the curvilinear operator,
+ * free surface, damping and the interface copy enforceCartTopo (EW.C:3504). */
+typedef struct {
+   int ib, ie, jb, je, kb, ke;
+   int nx, ny, nz;
+   double h;
+   int bccnd[6]; /* sides 0-3 as the Cartesian grid, 4 free surface (0), 5 interface (4) */
+   int wind[36];
+   const double *rho, *mu, *la, *met, *jac;
+   const double *strx, *stry, *dcx, *dcy, *cox, *coy;
+} sw4o_curv;
+
+/* cart: arrays up, u, um, lu, f, uacc of the Cartesian grid; c*: the curvilinear
+ * grid's (its forcing is zero: sources lie in the Cartesian grid). */
+void sw4o_step_topo(const sw4o_problem* cart, const sw4o_curv* cv, double t, double* up,
+                    const double* u, const double* um, double* lu, double* f, double* uacc,
+                    double* cup, const double* cu, const double* cum, double* clu, double* cf,
+                    double* cuacc);
+/* enforceCartTopo (EW.C:3504): Cartesian k=-1,0 from curvilinear k=nz-2,nz-1;
+ * curvilinear k=nz..nz+2 from Cartesian k=1..3 (SoA, same i,j bounds). */
+void sw4o_cart_topo(const sw4o_problem* cart, const sw4o_curv* cv, double* ucart, double* ucurv);
+
 /* Analytic whole-space displacement of one point source in a homogeneous medium
  * (rho, cp, cs) at time t, written SoA over the array [ib,ie]x[jb,je]x[kb,ke]
  * with x=(i-1)h, y=(j-1)h, z=zmin+(k-1)h: the field the reference compares

@@ -9,7 +9,9 @@
  * points, i fastest; 3-component fields and the 4-component metric stored
  * component-major (soa=1, the _rev kernels) or point-major (soa=0).
  */
+#ifndef _GNU_SOURCE
 #define _GNU_SOURCE
+#endif
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -538,4 +540,83 @@ double sw4o_curv_dt(int soa, int ib, int ie, int jb, int je, int kb, int ke, con
       if (e > eigmax) eigmax = e;
    }
    return cfl / sqrt(eigmax);
+}
+
+
+/* ------------------------------------------------------------------------ */
+/* Two-grid time step over topography.                                       */
+/* ------------------------------------------------------------------------ */
+void sw4o_cart_topo(const sw4o_problem* cart, const sw4o_curv* cv, double* ucart, double* ucurv)
+{
+   const cbox bc = make_cbox(1, cart->ib, cart->ie, cart->jb, cart->je, cart->kb, cart->ke);
+   const cbox bv = make_cbox(1, cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke);
+   const int nzc = cv->nz;
+   for (int c = 0; c < 3; c++)
+      for (int j = cart->jb; j <= cart->je; j++)
+         for (int i = cart->ib; i <= cart->ie; i++) {
+            for (int q = 0; q < 2; q++)
+               ucart[c * bc.cs + P(&bc, i, j, cart->kb + q)] = ucurv[c * bv.cs + P(&bv, i, j, nzc - 2 + q)];
+            for (int q = 0; q <= 2; q++)
+               ucurv[c * bv.cs + P(&bv, i, j, cv->ke - q)] = ucart[c * bc.cs + P(&bc, i, j, cart->kb + 4 - q)];
+         }
+}
+
+static void topo_bc(const sw4o_problem* p, const sw4o_curv* cv, const double* sbop, double* up,
+                    double* cup)
+{
+   double* nob[6] = {NULL, NULL, NULL, NULL, NULL, NULL};
+   sw4o_bcfortsg(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, p->wind, p->nx, p->ny, p->nz, up,
+                 p->h, p->bccnd, sbop, p->mu, p->la, nob, p->strx, p->stry);
+   sw4o_bcfortsg(1, cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cv->wind, cv->nx, cv->ny, cv->nz,
+                 cup, cv->h, cv->bccnd, sbop, cv->mu, cv->la, nob, cv->strx, cv->stry);
+   if (cv->bccnd[4] == 0)
+      sw4o_freesurfcurvisg(1, cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cv->nz, 5, cup, cv->mu,
+                           cv->la, cv->met, sbop, NULL, cv->strx, cv->stry);
+   sw4o_cart_topo(p, cv, up, cup);
+}
+
+void sw4o_step_topo(const sw4o_problem* p, const sw4o_curv* cv, double t, double* up,
+                    const double* u, const double* um, double* lu, double* f, double* uacc,
+                    double* cup, const double* cu, const double* cum, double* clu, double* cf,
+                    double* cuacc)
+{
+   double acof[384], ghcof[6], bope[48], sbop[5];
+   sw4o_stencil_coefficients(acof, ghcof, bope, sbop);
+   const long npts = (long)(p->ie - p->ib + 1) * (p->je - p->jb + 1) * (p->ke - p->kb + 1);
+   const long cnpts = (long)(cv->ie - cv->ib + 1) * (cv->je - cv->jb + 1) * (cv->ke - cv->kb + 1);
+   const double dt = p->dt;
+   const int onesided_c[6] = {0, 0, 0, 0, cv->bccnd[4] == 0, 0};
+   memset(cf, 0, 3 * cnpts * sizeof(double));
+
+   sw4o_force(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, f, p->nsrc, p->src_ijk, p->src_amp,
+              p->src_freq, p->src_t0, p->src_kind, t, 0);
+   memset(lu, 0, 3 * npts * sizeof(double));
+   memset(clu, 0, 3 * cnpts * sizeof(double));
+   sw4o_rhs4sg(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, p->nz, p->onesided, acof, bope, ghcof,
+               lu, u, p->mu, p->la, p->h, p->strx, p->stry, p->strz);
+   sw4o_rhs4sgcurv(1, cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cu, cv->mu, cv->la, cv->met,
+                   cv->jac, clu, onesided_c, cv->strx, cv->stry);
+   sw4o_predfort(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, u, um, lu, f, p->rho, dt * dt);
+   sw4o_predfort(1, cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cup, cu, cum, clu, cf, cv->rho,
+                 dt * dt);
+   topo_bc(p, cv, sbop, up, cup);
+
+   sw4o_force(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, f, p->nsrc, p->src_ijk, p->src_amp,
+              p->src_freq, p->src_t0, p->src_kind, t, 1);
+   sw4o_dpdmtfort(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, u, um, uacc, 1.0 / (dt * dt));
+   sw4o_dpdmtfort(cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cup, cu, cum, cuacc, 1.0 / (dt * dt));
+   sw4o_rhs4sg(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, p->nz, p->onesided, acof, bope, ghcof,
+               lu, uacc, p->mu, p->la, p->h, p->strx, p->stry, p->strz);
+   sw4o_rhs4sgcurv(1, cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cuacc, cv->mu, cv->la, cv->met,
+                   cv->jac, clu, onesided_c, cv->strx, cv->stry);
+   sw4o_corrfort(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, lu, f, p->rho, dt * dt * dt * dt);
+   sw4o_corrfort(1, cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cup, clu, cf, cv->rho,
+                 dt * dt * dt * dt);
+   if (p->sg_beta != 0) {
+      sw4o_addsgd4(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, u, um, p->rho, p->dcx, p->dcy,
+                   p->dcz, p->strx, p->stry, p->strz, p->cox, p->coy, p->coz, p->sg_beta);
+      sw4o_addsgd4c(1, cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cup, cu, cum, cv->rho, cv->dcx,
+                    cv->dcy, cv->strx, cv->stry, cv->jac, cv->cox, cv->coy, p->sg_beta);
+   }
+   topo_bc(p, cv, sbop, up, cup);
 }
