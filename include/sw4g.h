@@ -286,6 +286,38 @@ double* sw4g_ew_field(const sw4g_ew* ew, int which);
 /* advance nsteps time steps */
 int sw4g_ew_step(sw4g_ew* ew, int nsteps, int mode);
 
+/* Topography (replaces the reference's topography + curvilinear grid set-up,
+ * src/EW.C:540-720 (deck), 2018-2046 (dimensions), 6164 (generate_grid), 6229
+ * (setup_metric), and the curvilinear grid's share of every phase of the time
+ * loop).  A Gaussian hill z_s = -amp exp(-((x-xc)/lx)^2 - ((y-yc)/ly)^2) is
+ * meshed by a curvilinear grid from z_s down to the Cartesian grid's zmin (the
+ * reference's topography zmax); zeta_break and order as the reference's
+ * topography options (defaults 0.95 and 4). */
+typedef struct sw4g_topography {
+   double amp, xc, yc, lx, ly;
+   double zeta_break;
+   int order;
+} sw4g_topography;
+/* An EW object with a curvilinear grid (grid 1) over topography t on top of the
+ * Cartesian grid g (grid 0), whose bc[4] must be SW4G_BC_INTERFACE.  The
+ * curvilinear grid has g's nx, ny and nz = 1 + round((zmin - z_avg)/h) points,
+ * z_avg the midpoint of the topography's z range (src/EW.C:2039-2044).  FP64,
+ * 4th-order damping; sources must lie in the Cartesian grid.  SW4G_BAD_ARGUMENT
+ * if the grid folds (topography too steep for h). */
+#define SW4G_BC_INTERFACE 4
+int sw4g_ew_create_topo(const sw4g_grid* g, const sw4g_topography* t, void* stream, sw4g_ew** out);
+/* 1, or 2 with topography */
+int sw4g_ew_num_grids(const sw4g_ew* ew);
+int sw4g_ew_grid_dims(const sw4g_ew* ew, int grid, int* nx, int* ny, int* nz, long long* npts);
+int sw4g_ew_set_material_grid(sw4g_ew* ew, int grid, const double* rho, const double* mu,
+                              const double* lambda, int on_device);
+int sw4g_ew_set_fields_grid(sw4g_ew* ew, int grid, const double* u, const double* um,
+                            int on_device);
+int sw4g_ew_get_fields_grid(const sw4g_ew* ew, int grid, double* u, double* um, int on_device);
+/* z (npts), metric (4 x npts, component-major) and Jacobian (npts) of grid 1 */
+int sw4g_ew_curvilinear_arrays(const sw4g_ew* ew, double* z, double* met, double* jac,
+                               int on_device);
+
 /* Receivers (replace TimeSeries + EW::extractRecordData, src/EW.C:5854-6072, and the
  * per-step recording in the time loop, src/EW.C:2485-2500 and 2797-2835).
  * Record modes are numbered as TimeSeries::receiverMode (src/TimeSeries.h:52);

@@ -45,10 +45,22 @@ class SourceDesc(C.Structure):
                 ("freq", C.c_double), ("t0", C.c_double), ("kind", C.c_int)]
 
 
+class TopoDesc(C.Structure):
+    """sw4g_topography (include/sw4g.h)."""
+    _fields_ = [("amp", C.c_double), ("xc", C.c_double), ("yc", C.c_double), ("lx", C.c_double),
+                ("ly", C.c_double), ("zeta_break", C.c_double), ("order", C.c_int)]
+
+
+def topo_desc(amp, xc, yc, lx, ly, zeta_break=0.95, order=4) -> TopoDesc:
+    t = TopoDesc()
+    t.amp, t.xc, t.yc, t.lx, t.ly, t.zeta_break, t.order = amp, xc, yc, lx, ly, zeta_break, order
+    return t
+
+
 # time-function kinds
 GAUSSIAN, C6SMOOTHBUMP, RICKER, VERYSMOOTHBUMP = 0, 1, 2, 3
 # boundary kinds (the reference's boundaryConditionType numbering)
-FREE, DIRICHLET, SUPERGRID, PERIODIC = 0, 1, 2, 3
+FREE, DIRICHLET, SUPERGRID, PERIODIC, INTERFACE = 0, 1, 2, 3, 4
 MODE_PHASES, MODE_FUSED = 0, 1
 # receiver record modes (the reference's TimeSeries::receiverMode numbering)
 REC_DISPLACEMENT, REC_DIV, REC_CURL, REC_STRAINS, REC_VELOCITY, REC_GRADIENT = 0, 1, 2, 3, 4, 5
@@ -71,6 +83,14 @@ _SIGS = {
     "sw4g_discretize_source": ([C.POINTER(GridDesc), C.POINTER(SourceDesc), C.c_int, _I, _D, _I],
                                C.c_int),
     "sw4g_ew_create": ([C.POINTER(GridDesc), _VP, C.POINTER(_VP)], C.c_int),
+    "sw4g_ew_create_topo": ([C.POINTER(GridDesc), C.POINTER(TopoDesc), _VP, C.POINTER(_VP)],
+                            C.c_int),
+    "sw4g_ew_num_grids": ([_VP], C.c_int),
+    "sw4g_ew_grid_dims": ([_VP, C.c_int, _I, _I, _I, C.POINTER(C.c_longlong)], C.c_int),
+    "sw4g_ew_set_material_grid": ([_VP, C.c_int, _VP, _VP, _VP, C.c_int], C.c_int),
+    "sw4g_ew_set_fields_grid": ([_VP, C.c_int, _VP, _VP, C.c_int], C.c_int),
+    "sw4g_ew_get_fields_grid": ([_VP, C.c_int, _VP, _VP, C.c_int], C.c_int),
+    "sw4g_ew_curvilinear_arrays": ([_VP, _VP, _VP, _VP, C.c_int], C.c_int),
     "sw4g_ew_destroy": ([_VP], C.c_int),
     "sw4g_ew_npts": ([_VP], C.c_longlong),
     "sw4g_ew_set_material": ([_VP, _VP, _VP, _VP, C.c_int], C.c_int),
@@ -194,11 +214,15 @@ def _stream_ptr(stream) -> int | None:
 class EW:
     """One Cartesian grid's time loop on the GPU (sw4g_ew_* in include/sw4g.h)."""
 
-    def __init__(self, grid: GridDesc, stream=None):
+    def __init__(self, grid: GridDesc, stream=None, topo: TopoDesc = None):
         self.grid = grid
         self._stream = _stream_ptr(stream)
         h = _VP()
-        check(lib().sw4g_ew_create(C.byref(grid), self._stream, C.byref(h)), "sw4g_ew_create")
+        if topo is None:
+            check(lib().sw4g_ew_create(C.byref(grid), self._stream, C.byref(h)), "sw4g_ew_create")
+        else:
+            check(lib().sw4g_ew_create_topo(C.byref(grid), C.byref(topo), self._stream,
+                                            C.byref(h)), "sw4g_ew_create_topo")
         self._h = h
         self.npts = lib().sw4g_ew_npts(h)
         self.shape = (grid.nz + 4, grid.ny + 4, grid.nx + 4)
@@ -269,6 +293,40 @@ class EW:
 
     def enforce_bc(self, u):
         check(lib().sw4g_ew_enforce_bc(self._h, _ptr(u)), "enforce_bc")
+
+    @property
+    def num_grids(self) -> int:
+        return lib().sw4g_ew_num_grids(self._h)
+
+    def grid_dims(self, grid=0):
+        """(nx, ny, nz, npts) of grid 0 (Cartesian) or 1 (curvilinear)."""
+        nx, ny, nz, n = C.c_int(), C.c_int(), C.c_int(), C.c_longlong()
+        check(lib().sw4g_ew_grid_dims(self._h, grid, C.byref(nx), C.byref(ny), C.byref(nz),
+                                      C.byref(n)), "grid_dims")
+        return nx.value, ny.value, nz.value, n.value
+
+    def set_material_grid(self, grid, rho, mu, la):
+        on_dev = int(hasattr(rho, "is_cuda") and rho.is_cuda)
+        check(lib().sw4g_ew_set_material_grid(self._h, grid, _ptr(rho), _ptr(mu), _ptr(la), on_dev),
+              "set_material_grid")
+
+    def set_fields_grid(self, grid, u, um):
+        on_dev = int(hasattr(u, "is_cuda") and u.is_cuda)
+        check(lib().sw4g_ew_set_fields_grid(self._h, grid, _ptr(u), _ptr(um), on_dev),
+              "set_fields_grid")
+
+    def get_fields_grid(self, grid, u, um=None):
+        on_dev = int(hasattr(u, "is_cuda") and u.is_cuda)
+        check(lib().sw4g_ew_get_fields_grid(self._h, grid, _ptr(u),
+                                            _ptr(um) if um is not None else None, on_dev),
+              "get_fields_grid")
+
+    def curvilinear_arrays(self, z=None, met=None, jac=None):
+        ref = next(a for a in (z, met, jac) if a is not None)
+        on_dev = int(hasattr(ref, "is_cuda") and ref.is_cuda)
+        p = lambda a: _ptr(a) if a is not None else None
+        check(lib().sw4g_ew_curvilinear_arrays(self._h, p(z), p(met), p(jac), on_dev),
+              "curvilinear_arrays")
 
     def set_receivers(self, ijk, modes, capacity):
         """Receivers at 1-based grid points ijk (n x 3) with record modes (REC_*);

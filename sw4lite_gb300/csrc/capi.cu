@@ -397,6 +397,62 @@ int sw4g_ew_create(const sw4g_grid* g, void* stream, sw4g_ew** out)
    return SW4G_OK;
 }
 
+int sw4g_ew_create_topo(const sw4g_grid* g, const sw4g_topography* t, void* stream, sw4g_ew** out)
+{
+   if (!g || !t || !out) return SW4G_BAD_ARGUMENT;
+   *out = nullptr;
+   TopoSpec ts;
+   ts.amp = t->amp;
+   ts.xc = t->xc;
+   ts.yc = t->yc;
+   ts.lx = t->lx;
+   ts.ly = t->ly;
+   ts.zeta_break = t->zeta_break;
+   ts.order = t->order;
+   EW* e = new (std::nothrow) EW(to_spec(g), as_stream(stream), &ts);
+   if (!e) return SW4G_BAD_ARGUMENT;
+   int st = e->init();
+   if (st != SW4G_OK) {
+      delete e;
+      return st;
+   }
+   sw4g_ew* h = new (std::nothrow) sw4g_ew{e};
+   if (!h) {
+      delete e;
+      return SW4G_BAD_ARGUMENT;
+   }
+   *out = h;
+   return SW4G_OK;
+}
+
+int sw4g_ew_num_grids(const sw4g_ew* ew) { return ew ? ew->impl->num_grids() : -1; }
+
+int sw4g_ew_grid_dims(const sw4g_ew* ew, int grid, int* nx, int* ny, int* nz, long long* npts)
+{
+   return ew ? ew->impl->grid_dims(grid, nx, ny, nz, npts) : SW4G_BAD_ARGUMENT;
+}
+
+int sw4g_ew_set_material_grid(sw4g_ew* ew, int grid, const double* rho, const double* mu,
+                              const double* lambda, int on_device)
+{
+   return ew ? ew->impl->set_material_grid(grid, rho, mu, lambda, on_device != 0) : SW4G_BAD_ARGUMENT;
+}
+
+int sw4g_ew_set_fields_grid(sw4g_ew* ew, int grid, const double* u, const double* um, int on_device)
+{
+   return ew ? ew->impl->set_fields_grid(grid, u, um, on_device != 0) : SW4G_BAD_ARGUMENT;
+}
+
+int sw4g_ew_get_fields_grid(const sw4g_ew* ew, int grid, double* u, double* um, int on_device)
+{
+   return ew ? ew->impl->get_fields_grid(grid, u, um, on_device != 0) : SW4G_BAD_ARGUMENT;
+}
+
+int sw4g_ew_curvilinear_arrays(const sw4g_ew* ew, double* z, double* met, double* jac, int on_device)
+{
+   return ew ? ew->impl->curvilinear_arrays(z, met, jac, on_device != 0) : SW4G_BAD_ARGUMENT;
+}
+
 int sw4g_ew_destroy(sw4g_ew* ew)
 {
    if (!ew) return SW4G_BAD_ARGUMENT;

@@ -494,6 +494,26 @@ __global__ void curv_eig_kernel(long long n, long long mcs, long long mps,
    if (threadIdx.x == 0) blockmax[blockIdx.x] = red[0];
 }
 
+// enforceCartTopo (src/EW.C:3504-3530) with 2 ghost points: Cartesian k = -1, 0
+// from curvilinear k = nzc-2, nzc-1, and curvilinear k = nzc..nzc+2 from Cartesian
+// k = 1..3, over the shared i, j range; one thread per (i, j).
+__global__ void cart_topo_kernel(Box bc, Box bv, int nzc, double* __restrict__ uc,
+                                 double* __restrict__ uv)
+{
+   const int i = bc.ib + blockIdx.x * blockDim.x + threadIdx.x;
+   const int j = bc.jb + blockIdx.y * blockDim.y + threadIdx.y;
+   if (i > bc.ie || j > bc.je) return;
+#pragma unroll
+   for (int c = 0; c < 3; c++) {
+#pragma unroll
+      for (int q = 0; q < 2; q++)
+         uc[c * bc.cs + pidx(bc, i, j, bc.kb + q)] = uv[c * bv.cs + pidx(bv, i, j, nzc - 2 + q)];
+#pragma unroll
+      for (int q = 0; q <= 2; q++)
+         uv[c * bv.cs + pidx(bv, i, j, bv.ke - q)] = uc[c * bc.cs + pidx(bc, i, j, bc.kb + 4 - q)];
+   }
+}
+
 int grid_stride(long long n)
 {
    long long b = (n + 255) / 256;
@@ -590,6 +610,14 @@ int launch_addsgd4c(int soa, int ib, int ie, int jb, int je, int kb, int ke, dou
    if (ni <= 0 || nj <= 0 || nk <= 0) return kOk;
    const dim3 blk(32, 4), g((ni + 31) / 32, (nj + 3) / 4, nk);
    addsgd4c_kernel<<<g, blk, 0, st>>>(b, up, u, um, rho, dcx, dcy, strx, stry, jac, cox, coy, beta);
+   return launch_status();
+}
+
+int launch_cart_topo(const Box& cart, const Box& curv, int nzc, double* ucart, double* ucurv,
+                     cudaStream_t st)
+{
+   const dim3 blk(32, 4), g((cart.ie - cart.ib + 32) / 32, (cart.je - cart.jb + 4) / 4);
+   cart_topo_kernel<<<g, blk, 0, st>>>(cart, curv, nzc, ucart, ucurv);
    return launch_status();
 }
 

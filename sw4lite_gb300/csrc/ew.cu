@@ -1,13 +1,21 @@
 // Host-side time loop for one Cartesian grid; see ew.h.
 #include "ew.h"
 
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "sbp.h"
 
 namespace sw4g {
 
-EW::EW(const GridSpec& g, cudaStream_t stream) : g_(g), stream_(stream) {}
+EW::EW(const GridSpec& g, cudaStream_t stream, const TopoSpec* topo) : g_(g), stream_(stream)
+{
+   if (topo) {
+      cv_.reset(new CurvGrid());
+      cv_->topo = *topo;
+   }
+}
 
 EW::~EW()
 {
@@ -45,9 +53,14 @@ int EW::init()
    if (g_.soa != 1) return kNotSupported;  // the time loop keeps fields component-major
    for (int s = 0; s < 6; s++) {
       const int t = g_.bc[s];
+      if (s == 4 && cv_) {
+         if (t != kInterface) return kBadArgument;  // the top is the curvilinear grid
+         continue;
+      }
       if (!(t == kStressFree || t == kDirichlet || t == kSuperGrid || t == kPeriodic)) return kBadArgument;
       if (t == kStressFree && s < 4) return kNotSupported;
    }
+   if (cv_ && (g_.precision != 0 || g_.sg_order != 4)) return kNotSupported;
    if (g_.sg_order != 4 && g_.sg_order != 6) return kBadArgument;
    if (g_.precision != 0 && g_.precision != 1) return kBadArgument;
    mixed_ = g_.precision == 1;
@@ -113,6 +126,7 @@ int EW::init()
             SW4G_TRY(cuda_ok(cudaMalloc(&zc_[side], zcoef_len(bx) * sizeof(double))));
    }
    SW4G_TRY(upload_sbp_tables_direct());
+   if (cv_) SW4G_TRY(init_topo());
    SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
    ready_ = true;
    return kOk;
@@ -154,6 +168,7 @@ int EW::add_source(const SourceSpec& s)
 {
    if (!ready_) return kBadArgument;
    if (s.kind < 0 || s.kind > 3 || !(s.freq > 0)) return kBadArgument;
+   if (cv_ && s.z < g_.zmin) return kNotSupported;  // sources in the curvilinear grid: not built
    discretize_source(g_, onesided_, s, hsrc_);
    src_dirty_ = true;
    return kOk;
@@ -259,7 +274,18 @@ int EW::compute_time_step(double cfl, double tmax, double* dt, int* nsteps)
    SW4G_TRY(cuda_ok(cudaMemcpy(m.data(), mu_, n * sizeof(double), cudaMemcpyDeviceToHost)));
    SW4G_TRY(cuda_ok(cudaMemcpy(l.data(), la_, n * sizeof(double), cudaMemcpyDeviceToHost)));
    int ns = 0;
-   const double d = cfl_time_step(g_, r.data(), m.data(), l.data(), cfl, t_, tmax, &ns);
+   double d = cfl_time_step(g_, r.data(), m.data(), l.data(), cfl, t_, tmax, &ns);
+   if (cv_) {
+      // min over both grids of the raw limits, then land on tmax (src/EW.C:5041-5146)
+      double eigmax = -1;
+      for (size_t p = 0; p < n; p++) eigmax = std::max(eigmax, (4 * m[p] + l[p]) / r[p]);
+      double dc = cfl * g_.h * (1 / std::sqrt(eigmax)), dv = 0;
+      SW4G_TRY(curv_time_step(cfl, &dv));
+      dc = std::min(dc, dv);
+      ns = static_cast<int>((tmax - t_) / dc + 0.5);
+      ns = ns == 0 ? 1 : ns;
+      d = (tmax - t_) / ns;
+   }
    dt_ = d;
    if (dt) *dt = d;
    if (nsteps) *nsteps = ns;
@@ -348,6 +374,7 @@ int EW::ensure_phase_arrays()
 int EW::step(int nsteps, int mode)
 {
    if (!ready_ || !material_ || !(dt_ > 0) || nsteps < 0) return kBadArgument;
+   if (cv_ && !cv_->material) return kBadArgument;
    if (mode != kModePhases && mode != kModeFused) return kBadArgument;
    if (mixed_ && mode == kModePhases) return kNotSupported;
    if (drec_.n > 0 && rec_rows_ + (rec_initial_ ? 1 : 0) + nsteps > rec_cap_) return kBadArgument;
@@ -455,7 +482,9 @@ int EW::step_phases()
                                  mu_, la_, g_.h, dprof_[3], dprof_[4], dprof_[5], stream_));
    SW4G_TRY(launch_predfort(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, up, u, um, lu_, f_, rho_,
                             dt * dt, stream_));
+   if (cv_) SW4G_TRY(curv_pred(ip));
    SW4G_TRY(enforce_bc(up));
+   if (cv_) SW4G_TRY(curv_bc(up, cv_->lev[ip]));
    SW4G_TRY(launch_force_dense(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, f_, dsrc_, t_, 1, stream_));
    SW4G_TRY(launch_dpdmtfort(b.ib, b.ie, b.jb, b.je, b.kb, b.ke, up, u, um, uacc_, 1 / (dt * dt),
                              stream_));
@@ -467,7 +496,9 @@ int EW::step_phases()
       SW4G_TRY(launch_addsgd(g_.sg_order, 1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, up, u, um, rho_,
                              dprof_[0], dprof_[1], dprof_[2], dprof_[3], dprof_[4], dprof_[5],
                              dprof_[6], dprof_[7], dprof_[8], g_.sg_damping, stream_));
+   if (cv_) SW4G_TRY(curv_corr(ip, ip));
    SW4G_TRY(enforce_bc(up));
+   if (cv_) SW4G_TRY(curv_bc(up, cv_->lev[ip]));
    if (drec_.n > 0) SW4G_TRY(record(up, um, 0));
    ium_ = iu_;
    iu_ = ip;
@@ -662,7 +693,14 @@ int EW::step_fused()
    while (ip == iu_ || ip == ium_) ip++;
    int iq = ip + 1;
    while (iq == iu_ || iq == ium_) iq++;
-   for (int which = 0; which < 6; which++) SW4G_TRY(piece(which, ip, iq));
+   for (int which = 0; which < 6; which++) {
+      SW4G_TRY(piece(which, ip, iq));
+      if (!cv_) continue;
+      if (which == 0) SW4G_TRY(curv_pred(ip));
+      if (which == 2) SW4G_TRY(curv_bc(lev_[ip], cv_->lev[ip]));
+      if (which == 3) SW4G_TRY(curv_corr(ip, iq));
+      if (which == 5) SW4G_TRY(curv_bc(lev_[iq], cv_->lev[iq]));
+   }
    if (drec_.n > 0) SW4G_TRY(record(lev_[iq], lev_[ium_], 0));
    ium_ = iu_;
    iu_ = iq;
@@ -716,11 +754,12 @@ int EW::launches_per_step(int mode) const
    if (mode == kModePhases) {
       // force(memset+kernel), rhs (center + rows), pred, bc, force, dpdm, rhs, corr, addsgd, bc
       const int rhs = 1 + rows;
-      return 2 * (1 + src) + 2 * rhs + 3 + (damp ? 1 : 0) + 2 * bc + rec;
+      return 2 * (1 + src) + 2 * rhs + 3 + (damp ? 1 : 0) + 2 * bc + rec + curv_launches(mode);
    }
    // per stage: stage kernel, ghost shell, one-sided rows, forcing, BC sides;
    // the corrector adds the rows' slab kernels (and 6th-order damping)
-   return 2 * (2 + rows + src + bc) + rows + (damp && g_.sg_order == 6 ? 1 : 0) + rec;
+   return 2 * (2 + rows + src + bc) + rows + (damp && g_.sg_order == 6 ? 1 : 0) + rec +
+          curv_launches(mode);
 }
 
 }  // namespace sw4g

@@ -11,12 +11,39 @@
 
 #include <cuda_runtime.h>
 
+#include <memory>
 #include <vector>
 
 #include "kernels.h"
 #include "setup.h"
 
 namespace sw4g {
+
+// Topography over this Cartesian grid: a Gaussian hill
+// z_s = -amp exp(-((x-xc)/lx)^2 - ((y-yc)/ly)^2), mapped onto a curvilinear grid
+// from z_s down to the Cartesian grid's zmin as the reference's grid_mapping does
+// (src/EW.C:5694, zeta_break and order are its m_zetaBreak and
+// m_grid_interpolation_order, defaults src/EW.C:180-181).
+struct TopoSpec {
+   double amp = 0, xc = 0, yc = 0, lx = 1, ly = 1;
+   double zeta_break = 0.95;
+   int order = 4;
+};
+
+// The curvilinear grid on top of the Cartesian grid (ew_topo.cu).
+struct CurvGrid {
+   TopoSpec topo;
+   int nz = 0;
+   Bounds b{};
+   long long npts = 0;
+   int bc[6] = {}, wind[36] = {}, bcpts[6] = {};
+   double *z = nullptr, *met = nullptr, *jac = nullptr;
+   double *rho = nullptr, *mu = nullptr, *la = nullptr;
+   double* lev[4] = {};
+   double *lu = nullptr, *uacc = nullptr, *fzero = nullptr;
+   bool material = false;
+   ~CurvGrid();
+};
 
 enum StepMode : int {
    kModePhases = 0,  // reference phase order with dense Lu / F / Uacc arrays
@@ -25,7 +52,9 @@ enum StepMode : int {
 
 class EW {
  public:
-   EW(const GridSpec& g, cudaStream_t stream);
+   // topo != nullptr: a curvilinear grid over that topography on top of this grid,
+   // whose top side must then be the interface (bc[4] == kInterface).
+   EW(const GridSpec& g, cudaStream_t stream, const TopoSpec* topo = nullptr);
    ~EW();
    EW(const EW&) = delete;
    EW& operator=(const EW&) = delete;
@@ -58,6 +87,16 @@ class EW {
 
    int step(int nsteps, int mode);
 
+   // Grids: 0 the Cartesian grid, 1 the curvilinear grid (with topography).
+   int num_grids() const { return cv_ ? 2 : 1; }
+   int grid_dims(int grid, int* nx, int* ny, int* nz, long long* npts) const;
+   int set_material_grid(int grid, const double* rho, const double* mu, const double* la,
+                         bool on_device);
+   int set_fields_grid(int grid, const double* u, const double* um, bool on_device);
+   int get_fields_grid(int grid, double* u, double* um, bool on_device) const;
+   // z, metric (4 x npts, SoA) and Jacobian of the curvilinear grid; any may be null
+   int curvilinear_arrays(double* z, double* met, double* jac, bool on_device) const;
+
    // Receivers at grid points (i,j,k) with record modes (kernels.h RecMode).  Each
    // step appends one row of values (all receivers, in order) to a device record
    // array of `capacity` rows; the first row holds the initial data and is written
@@ -88,6 +127,12 @@ class EW {
    int mixed_piece(int piece, int ip, int iq);
    int piece(int which, int ip, int iq) { return mixed_ ? mixed_piece(which, ip, iq) : fused_piece(which, ip, iq); }
    int ensure_staging();
+   int init_topo();
+   int curv_pred(int ip);
+   int curv_corr(int ip, int iq);
+   int curv_bc(double* ucart, double* ucurv);
+   int curv_time_step(double cfl, double* dt);
+   int curv_launches(int mode) const;
    int ensure_phase_arrays();
 
    GridSpec g_;
@@ -134,6 +179,8 @@ class EW {
    double* records_ = nullptr;
    int rec_cap_ = 0, rec_rows_ = 0, rec_nvals_ = 0;
    bool rec_initial_ = false;  // the initial-data row is still to be written
+
+   std::unique_ptr<CurvGrid> cv_;
 
    double t_ = 0, dt_ = 0;
 };

@@ -1,0 +1,251 @@
+// The curvilinear grid of an EW object with topography: set-up and its part of
+// each time step (see ew.h).
+//
+// The reference keeps a list of grids, Cartesian below and one curvilinear grid
+// on top (src/EW.C:2018-2046), and runs every phase of the time loop over all of
+// them (src/EW.C:2537-2756).  The curvilinear grid's phases here:
+//   predictor   rhs4sgcurv(U) with the SBP top rows, then predfort (no forcing:
+//               sources lie in the Cartesian grid);
+//   BC          bcfortsg on its x/y sides and flat free surface, the curvilinear
+//               free-surface ghost plane (freesurfcurvisg) over it, then the
+//               interface copy enforceCartTopo (src/EW.C:3446-3530);
+//   corrector   dpdmtfort, rhs4sgcurv(Uacc), corrfort, addsgd4cfort.
+// Its time levels rotate with the Cartesian grid's: the fused Cartesian
+// corrector writes a fourth level, so the curvilinear corrector works in place
+// and then swaps its buffer into that slot.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "ew.h"
+
+namespace sw4g {
+
+CurvGrid::~CurvGrid()
+{
+   auto f = [](void* p) {
+      if (p) cudaFree(p);
+   };
+   f(z);
+   f(met);
+   f(jac);
+   f(rho);
+   f(mu);
+   f(la);
+   for (auto* p : lev) f(p);
+   f(lu);
+   f(uacc);
+   f(fzero);
+}
+
+namespace {
+CurvSpec curv_spec(const CurvGrid& c, const double* u, const double* strx, const double* stry)
+{
+   CurvSpec s;
+   s.soa = 1;
+   s.ib = c.b.ib; s.ie = c.b.ie; s.jb = c.b.jb; s.je = c.b.je; s.kb = c.b.kb; s.ke = c.b.ke;
+   s.u = u;
+   s.mu = c.mu;
+   s.la = c.la;
+   s.met = c.met;
+   s.jac = c.jac;
+   s.strx = strx;
+   s.stry = stry;
+   return s;
+}
+}  // namespace
+
+int EW::init_topo()
+{
+   CurvGrid& c = *cv_;
+   const TopoSpec& t = c.topo;
+   if (!(t.lx > 0) || !(t.ly > 0) || !(t.zeta_break > 0) || t.order < 1) return kBadArgument;
+   // topography z range over the array's (x, y) points; the curvilinear grid has
+   // nz = 1 + round((zmax - avg)/h) points, avg the midpoint of that range
+   // (src/EW.C:2018-2046)
+   double zlo = 1e300, zhi = -1e300;
+   for (int j = b_.jb; j <= b_.je; j++)
+      for (int i = b_.ib; i <= b_.ie; i++) {
+         const double x = (i - 1.0) * g_.h, y = (j - 1.0) * g_.h;
+         const double zs = -t.amp * std::exp(-(x - t.xc) * (x - t.xc) / (t.lx * t.lx) -
+                                             (y - t.yc) * (y - t.yc) / (t.ly * t.ly));
+         zlo = std::min(zlo, zs);
+         zhi = std::max(zhi, zs);
+      }
+   const double avg = 0.5 * (zlo + zhi);
+   c.nz = 1 + static_cast<int>(std::lround((g_.zmin - avg) / g_.h));
+   if (c.nz < 8) return kBadArgument;  // the SBP top rows need 8 planes
+   c.b = Bounds{b_.ib, b_.ie, b_.jb, b_.je, -1, c.nz + 2};
+   c.npts = c.b.npts();
+   const int cbc[6] = {g_.bc[0], g_.bc[1], g_.bc[2], g_.bc[3], kStressFree, kInterface};
+   GridSpec cg = g_;
+   cg.nz = c.nz;
+   for (int s = 0; s < 6; s++) c.bc[s] = cg.bc[s] = cbc[s];
+   boundary_windows(cg, c.wind, c.bcpts);
+
+   const size_t n = (size_t)c.npts;
+   for (double** p : {&c.z, &c.jac, &c.rho, &c.mu, &c.la})
+      SW4G_TRY(cuda_ok(cudaMalloc(p, n * sizeof(double))));
+   SW4G_TRY(cuda_ok(cudaMalloc(&c.met, 4 * n * sizeof(double))));
+   for (double** p : {&c.lev[0], &c.lev[1], &c.lev[2], &c.lev[3], &c.lu, &c.uacc, &c.fzero}) {
+      SW4G_TRY(cuda_ok(cudaMalloc(p, 3 * n * sizeof(double))));
+      SW4G_TRY(cuda_ok(cudaMemsetAsync(*p, 0, 3 * n * sizeof(double), stream_)));
+   }
+   const Bounds& b = c.b;
+   SW4G_TRY(launch_gaussian_hill_z(b.ib, b.ie, b.jb, b.je, b.kb, b.ke, c.nz, g_.h, g_.zmin,
+                                   t.zeta_break, t.order, t.amp, t.xc, t.yc, t.lx, t.ly, c.z,
+                                   stream_));
+   int* flag = nullptr;
+   SW4G_TRY(cuda_ok(cudaMalloc(&flag, sizeof(int))));
+   int bad = 0;
+   int st = cuda_ok(cudaMemsetAsync(flag, 0, sizeof(int), stream_));
+   if (st == kOk)
+      st = launch_metric(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, g_.h, c.z, c.met, c.jac, flag, stream_);
+   if (st == kOk) st = cuda_ok(cudaMemcpyAsync(&bad, flag, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+   if (st == kOk) st = cuda_ok(cudaStreamSynchronize(stream_));
+   cudaFree(flag);
+   if (st != kOk) return st;
+   return bad ? kBadArgument : kOk;  // the grid folds (z_r <= 0): topography too steep for h
+}
+
+int EW::grid_dims(int grid, int* nx, int* ny, int* nz, long long* npts) const
+{
+   if (grid < 0 || grid >= num_grids()) return kBadArgument;
+   if (nx) *nx = g_.nx;
+   if (ny) *ny = g_.ny;
+   if (nz) *nz = grid == 0 ? g_.nz : cv_->nz;
+   if (npts) *npts = grid == 0 ? npts_ : cv_->npts;
+   return kOk;
+}
+
+int EW::set_material_grid(int grid, const double* rho, const double* mu, const double* la,
+                          bool on_device)
+{
+   if (grid == 0) return set_material(rho, mu, la, on_device);
+   if (grid != 1 || !cv_ || !ready_ || !rho || !mu || !la) return kBadArgument;
+   const size_t bytes = (size_t)cv_->npts * sizeof(double);
+   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+   SW4G_TRY(cuda_ok(cudaMemcpyAsync(cv_->rho, rho, bytes, kind, stream_)));
+   SW4G_TRY(cuda_ok(cudaMemcpyAsync(cv_->mu, mu, bytes, kind, stream_)));
+   SW4G_TRY(cuda_ok(cudaMemcpyAsync(cv_->la, la, bytes, kind, stream_)));
+   SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
+   cv_->material = true;
+   return kOk;
+}
+
+int EW::set_fields_grid(int grid, const double* u, const double* um, bool on_device)
+{
+   if (grid == 0) return set_fields(u, um, on_device);
+   if (grid != 1 || !cv_ || !ready_ || !u || !um) return kBadArgument;
+   const size_t bytes = 3 * (size_t)cv_->npts * sizeof(double);
+   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+   SW4G_TRY(cuda_ok(cudaMemcpyAsync(cv_->lev[iu_], u, bytes, kind, stream_)));
+   SW4G_TRY(cuda_ok(cudaMemcpyAsync(cv_->lev[ium_], um, bytes, kind, stream_)));
+   if (!on_device) SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
+   return kOk;
+}
+
+int EW::get_fields_grid(int grid, double* u, double* um, bool on_device) const
+{
+   if (grid == 0) return get_fields(u, um, on_device);
+   if (grid != 1 || !cv_ || !ready_) return kBadArgument;
+   const size_t bytes = 3 * (size_t)cv_->npts * sizeof(double);
+   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+   if (u) SW4G_TRY(cuda_ok(cudaMemcpyAsync(u, cv_->lev[iu_], bytes, kind, stream_)));
+   if (um) SW4G_TRY(cuda_ok(cudaMemcpyAsync(um, cv_->lev[ium_], bytes, kind, stream_)));
+   if (!on_device) SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
+   return kOk;
+}
+
+int EW::curvilinear_arrays(double* z, double* met, double* jac, bool on_device) const
+{
+   if (!cv_ || !ready_) return kBadArgument;
+   const size_t bytes = (size_t)cv_->npts * sizeof(double);
+   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+   if (z) SW4G_TRY(cuda_ok(cudaMemcpyAsync(z, cv_->z, bytes, kind, stream_)));
+   if (met) SW4G_TRY(cuda_ok(cudaMemcpyAsync(met, cv_->met, 4 * bytes, kind, stream_)));
+   if (jac) SW4G_TRY(cuda_ok(cudaMemcpyAsync(jac, cv_->jac, bytes, kind, stream_)));
+   if (!on_device) SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
+   return kOk;
+}
+
+int EW::curv_pred(int ip)
+{
+   CurvGrid& c = *cv_;
+   const Bounds& b = c.b;
+   const int onesided[6] = {0, 0, 0, 0, 1, 0};
+   SW4G_TRY(launch_rhs4sgcurv(curv_spec(c, c.lev[iu_], dprof_[3], dprof_[4]), onesided, c.lu, stream_));
+   return launch_predfort(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, c.lev[ip], c.lev[iu_], c.lev[ium_],
+                          c.lu, c.fzero, c.rho, dt_ * dt_, stream_);
+}
+
+int EW::curv_corr(int ip, int iq)
+{
+   CurvGrid& c = *cv_;
+   const Bounds& b = c.b;
+   const double dt = dt_;
+   const int onesided[6] = {0, 0, 0, 0, 1, 0};
+   double *up = c.lev[ip], *u = c.lev[iu_], *um = c.lev[ium_];
+   SW4G_TRY(launch_dpdmtfort(b.ib, b.ie, b.jb, b.je, b.kb, b.ke, up, u, um, c.uacc, 1 / (dt * dt),
+                             stream_));
+   SW4G_TRY(launch_rhs4sgcurv(curv_spec(c, c.uacc, dprof_[3], dprof_[4]), onesided, c.lu, stream_));
+   SW4G_TRY(launch_corrfort(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, up, c.lu, c.fzero, c.rho,
+                            dt * dt * dt * dt, stream_));
+   if (prof_.used && g_.sg_damping != 0)
+      SW4G_TRY(launch_addsgd4c(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, up, u, um, c.rho, dprof_[0],
+                               dprof_[1], dprof_[3], dprof_[4], c.jac, dprof_[6], dprof_[7],
+                               g_.sg_damping, stream_));
+   if (ip != iq) std::swap(c.lev[ip], c.lev[iq]);
+   return kOk;
+}
+
+int EW::curv_bc(double* ucart, double* ucurv)
+{
+   CurvGrid& c = *cv_;
+   const Bounds& b = c.b;
+   SW4G_TRY(launch_bcfortsg(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, c.wind, g_.nx, g_.ny, c.nz, ucurv,
+                            g_.h, c.bc, sbop_, c.mu, c.la, nullptr, dprof_[3], dprof_[4], stream_));
+   SW4G_TRY(launch_freesurfcurvisg(curv_spec(c, ucurv, dprof_[3], dprof_[4]), c.nz, 5, sbop_,
+                                   nullptr, ucurv, stream_));
+   return launch_cart_topo(make_box(1, b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke),
+                           make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke), c.nz, ucart, ucurv,
+                           stream_);
+}
+
+int EW::curv_time_step(double cfl, double* dt)
+{
+   CurvGrid& c = *cv_;
+   if (!c.material) return kBadArgument;
+   const int nb = 152 * 4;
+   double* bm = nullptr;
+   SW4G_TRY(cuda_ok(cudaMalloc(&bm, nb * sizeof(double))));
+   std::vector<double> h(nb);
+   int st = launch_curv_eig(1, c.npts, c.rho, c.mu, c.la, c.met, c.jac, bm, nb, stream_);
+   if (st == kOk)
+      st = cuda_ok(cudaMemcpyAsync(h.data(), bm, nb * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+   if (st == kOk) st = cuda_ok(cudaStreamSynchronize(stream_));
+   cudaFree(bm);
+   if (st != kOk) return st;
+   double e = -1;
+   for (double v : h) e = std::max(e, v);
+   if (!(e > 0)) return kBadArgument;
+   *dt = cfl / std::sqrt(e);
+   return kOk;
+}
+
+int EW::curv_launches(int mode) const
+{
+   (void)mode;
+   if (!cv_) return 0;
+   int bc = 1 /* free surface */ + 1 /* interface copy */;
+   for (int s = 0; s < 4; s++) {
+      const int t = cv_->bc[s];
+      if ((t == kDirichlet || t == kSuperGrid || t == kPeriodic) && cv_->bcpts[s] > 0) bc++;
+   }
+   bc++;  // flat free surface of bcfortsg on the top side
+   const int rhs = 2;  // SBP top rows + interior
+   const bool damp = prof_.used && g_.sg_damping != 0;
+   return (rhs + 1) + (1 + rhs + 1 + (damp ? 1 : 0)) + 2 * bc;
+}
+
+}  // namespace sw4g

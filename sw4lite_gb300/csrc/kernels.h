@@ -127,6 +127,8 @@ int launch_addsgd4c(int soa, int ib, int ie, int jb, int je, int kb, int ke, dou
                     const double* u, const double* um, const double* rho, const double* dcx,
                     const double* dcy, const double* strx, const double* stry, const double* jac,
                     const double* cox, const double* coy, double beta, cudaStream_t st);
+int launch_cart_topo(const Box& cart, const Box& curv, int nzc, double* ucart, double* ucurv,
+                     cudaStream_t st);
 int launch_curv_eig(int soa, long long n, const double* rho, const double* mu, const double* la,
                     const double* met, const double* jac, double* blockmax, int nblocks,
                     cudaStream_t st);

@@ -10,7 +10,14 @@ namespace sw4g {
 
 // Boundary condition kinds, numbered as the reference's boundaryConditionType
 // (src/double/sw4.h:38).
-enum Bc : int { kStressFree = 0, kDirichlet = 1, kSuperGrid = 2, kPeriodic = 3, kNone = 8 };
+enum Bc : int {
+   kStressFree = 0,
+   kDirichlet = 1,
+   kSuperGrid = 2,
+   kPeriodic = 3,
+   kInterface = 4,  // bCCInterface: the top of a Cartesian grid below a curvilinear grid
+   kNone = 8
+};
 
 struct GridSpec {
    int nx = 0, ny = 0, nz = 0;  // interior points per axis

@@ -1,0 +1,100 @@
+"""The two-grid (topography) time loop on the GPU against the oracle's two-grid
+step (pinned to the reference's kernels in tests/test_oracle_topo_pin.py).
+
+Tolerance: after 6 steps both grids' fields agree with the oracle to 1e-12
+relative to each field's largest magnitude.
+"""
+import numpy as np
+import pytest
+
+import sw4lite_gb300 as sg
+from oracle import oracle as O
+from tests.gpu_util import dev, host
+from tests.topo_util import TopoCase, smooth_topo_fields
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    sg.build()
+    O.lib()
+
+
+def _case(bc_bottom=2):
+    nx, ny, ncart, h = 30, 28, 22, 0.1
+    src = [sg.source_desc(0.5 * nx * h, 0.45 * ny * h, 1.0 + 0.5 * ncart * h * 0.5,
+                          force=(1.0, -0.5, 0.3), freq=8.0, t0=0.1, kind=sg.GAUSSIAN),
+           sg.source_desc(0.4 * nx * h, 0.55 * ny * h, 1.0 + 0.3 * ncart * h,
+                          moment=(1.0, 0.2, -0.3, 0.7, 0.1, -0.5), freq=6.0, kind=sg.C6SMOOTHBUMP)]
+    return TopoCase(nx, ny, ncart, h, zmax_topo=1.0, amp=0.2, xc=1.4, yc=1.3, lx=0.6, ly=0.5,
+                    gp=5, sources=src, bc_bottom=bc_bottom)
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+def _gpu(case, fields, dt, nsteps, mode):
+    t = sg.topo_desc(**case.hill)
+    ew = sg.EW(case.grid, topo=t)
+    assert ew.num_grids == 2
+    nx, ny, nz, n = ew.grid_dims(1)
+    assert (nx, ny, nz) == (case.nx, case.ny, case.nc) and n == case.z.size
+    ew.set_material(*[dev(a) for a in case.cart_mat])
+    ew.set_material_grid(1, *[dev(a) for a in case.curv_mat])
+    for s in case.sources:
+        ew.add_source(s)
+    ew.set_time_step(dt, 0.0)
+    ew.set_fields(dev(fields[0]), dev(fields[1]))
+    ew.set_fields_grid(1, dev(fields[2]), dev(fields[3]))
+    z, met, jac = (dev(np.zeros(m * n)) for m in (1, 4, 1))
+    ew.curvilinear_arrays(z, met, jac)
+    ew.step(nsteps, mode)
+    out = [dev(np.zeros_like(f)) for f in fields]
+    ew.get_fields(out[0], out[1])
+    ew.get_fields_grid(1, out[2], out[3])
+    ew.close()
+    return [host(o) for o in out], (host(z), host(met), host(jac))
+
+
+def test_grid_set_up_matches_oracle():
+    c = _case()
+    _, (z, met, jac) = _gpu(c, smooth_topo_fields(c, 1), 1e-3, 0, sg.MODE_FUSED)
+    assert _rel(z, c.z) <= 1e-14
+    assert _rel(met, c.met) <= 1e-14
+    assert _rel(jac, c.jac) <= 1e-14
+
+
+@pytest.mark.parametrize("mode", [sg.MODE_FUSED, sg.MODE_PHASES])
+@pytest.mark.parametrize("bc_bottom", [2, 0])
+def test_topo_steps_match_oracle(mode, bc_bottom):
+    c = _case(bc_bottom)
+    dt = c.time_step(1.3)
+    fields = smooth_topo_fields(c, seed=6)
+    ref = c.oracle(dt).run(*fields, 0.0, 6)
+    got, _ = _gpu(c, fields, dt, 6, mode)
+    for a, b in zip(got, ref):
+        assert _rel(a, b) <= 1e-12
+
+
+def test_topo_time_step_and_bad_inputs():
+    c = _case()
+    ew = sg.EW(c.grid, topo=sg.topo_desc(**c.hill))
+    ew.set_material(*[dev(a) for a in c.cart_mat])
+    with pytest.raises(sg.Sw4gError):
+        ew.compute_time_step(1.3, 0.5)  # curvilinear material not set
+    ew.set_material_grid(1, *[dev(a) for a in c.curv_mat])
+    dt, n = ew.compute_time_step(1.3, 0.5)
+    assert n * dt == pytest.approx(0.5, rel=1e-14)
+    raw = c.time_step(1.3)
+    assert dt <= raw * (1 + 1e-12) and n == int(0.5 / raw + 0.5)
+    with pytest.raises(sg.Sw4gError):  # a source above the Cartesian grid
+        ew.add_source(sg.source_desc(1.0, 1.0, 0.5, force=(1.0, 0, 0)))
+    ew.close()
+    g = sg.grid_desc(c.nx, c.ny, c.ncart, c.h, bc=(2, 2, 2, 2, 0, 2), zmin=1.0)
+    with pytest.raises(sg.Sw4gError):  # top side must be the interface
+        sg.EW(g, topo=sg.topo_desc(**c.hill))
+    steep = dict(c.hill, amp=2.0)
+    with pytest.raises(sg.Sw4gError):  # the grid would fold
+        sg.EW(c.grid, topo=sg.topo_desc(**steep))
