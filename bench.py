@@ -313,6 +313,109 @@ def _time_form(args, sg, torch, precision, stream, world, local):
     return out
 
 
+def c3_config(nx=384, ny=384, nz_total=128):
+    """Topography workload: a curvilinear grid over a 1 km Gaussian hill (width
+    3 km) at the domain centre on top of a Cartesian grid, 384 x 384 x 128 points
+    in all at h = 50 m; the interface between the grids at z = 2000 m.  Material
+    vs = 2000 + 0.5 depth, vp = sqrt(3) vs, rho = 2500 below the surface.  A
+    vertical point force 3 km below the datum z = 0 under the hill top (in the
+    Cartesian grid), Gaussian (sigma 0.05 s)."""
+    h = 50.0
+    return dict(nx=nx, ny=ny, nz_total=nz_total, h=h, zmax_topo=2000.0, amp=1000.0,
+                xc=(nx - 1) * h / 2, yc=(ny - 1) * h / 2, lx=3000.0, ly=3000.0, vs0=2000.0,
+                grad=0.5, rho=2500.0, gp=30, damping=0.02,
+                src=dict(x=(nx - 1) * h / 2, y=(ny - 1) * h / 2, z=3000.0, force=(0.0, 0.0, 1e15),
+                         freq=20.0, t0=0.3),
+                cfl=1.3)
+
+
+def _make_topo_ew(sg, cfg, stream):
+    """The C3 EW object: the curvilinear grid's point count comes from the
+    topography (1 + round((zmax - z_avg)/h)); the Cartesian grid takes the rest of
+    the nz_total planes (the grids share the interface plane)."""
+    import torch
+    h, nx, ny = cfg["h"], cfg["nx"], cfg["ny"]
+    topo = sg.topo_desc(cfg["amp"], cfg["xc"], cfg["yc"], cfg["lx"], cfg["ly"])
+    i = np.arange(-1, nx + 3)
+    j = np.arange(-1, ny + 3)
+    X, Y = np.meshgrid((i - 1) * h, (j - 1) * h, indexing="xy")
+    zs = -cfg["amp"] * np.exp(-((X - cfg["xc"]) / cfg["lx"]) ** 2 - ((Y - cfg["yc"]) / cfg["ly"]) ** 2)
+    nc = 1 + int(round((cfg["zmax_topo"] - 0.5 * (zs.min() + zs.max())) / h))
+    ncart = cfg["nz_total"] - (nc - 1)
+    g = sg.grid_desc(nx, ny, ncart, h, bc=(2, 2, 2, 2, sg.INTERFACE, 2), zmin=cfg["zmax_topo"],
+                     sg_gp=cfg["gp"], sg_damping=cfg["damping"])
+    ew = sg.EW(g, stream=stream, topo=topo)
+    assert ew.grid_dims(1)[2] == nc
+
+    def material(z_planes, grid_shape):
+        depth = torch.clamp(z_planes - torch.from_numpy(zs).to("cuda"), min=0.0)
+        vs = cfg["vs0"] + cfg["grad"] * depth
+        rho = torch.full_like(vs, cfg["rho"])
+        mu = rho * vs * vs
+        la = rho * 3.0 * vs * vs - 2 * mu
+        return [a.reshape(-1).contiguous() for a in (rho, mu, la)]
+
+    kk = torch.arange(-1, ncart + 3, dtype=torch.float64, device="cuda")
+    zc = (cfg["zmax_topo"] + (kk - 1) * h)[:, None, None].expand(ncart + 4, ny + 4, nx + 4)
+    ew.set_material(*material(zc, None))
+    n1 = ew.grid_dims(1)[3]
+    z1 = torch.zeros(n1, dtype=torch.float64, device="cuda")
+    ew.curvilinear_arrays(z=z1)
+    ew.set_material_grid(1, *material(z1.reshape(nc + 4, ny + 4, nx + 4), None))
+    sc = cfg["src"]
+    ew.add_source(sg.source_desc(sc["x"], sc["y"], sc["z"], force=sc["force"], freq=sc["freq"],
+                                 t0=sc["t0"], kind=sg.GAUSSIAN))
+    # dt from the CFL number of both grids, landing on t = 1 s
+    dt, _ = ew.compute_time_step(cfg["cfl"], 1.0)
+    ew.set_time_step(dt, 0.0)
+    return ew, nc, ncart, dt
+
+
+def _time_topo(args, sg, torch, stream, world):
+    """C3: timed fused steps of both grids; end-to-end through the C ABI with
+    both grids' levels in pinned host memory."""
+    cfg = c3_config()
+    ew, nc, ncart, dt = _make_topo_ew(sg, cfg, stream)
+    nx, ny = cfg["nx"], cfg["ny"]
+    pts = nx * ny * (ncart + nc)  # interior points of both grids
+    with torch.cuda.stream(stream):
+        ew.step(args.warmup, sg.MODE_FUSED)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ew.step(args.steps, sg.MODE_FUSED)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = max_over_ranks(e0.elapsed_time(e1), world) / args.steps
+    out = {"value": world * pts / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+           "grids": {"cartesian": [nx, ny, ncart], "curvilinear": [nx, ny, nc]},
+           "dt": dt, "gpu_launches": ew.launches_per_step(sg.MODE_FUSED) * args.steps,
+           "workload": "C3 Gaussian-hill topography 384x384x128 h=50, FP64, fused Cartesian "
+                       "stages + curvilinear kernels"}
+    if not args.no_e2e:
+        n0, n1 = 3 * ew.grid_dims(0)[3], 3 * ew.grid_dims(1)[3]
+        hb = [torch.zeros(n, dtype=torch.float64, pin_memory=True) for n in (n0, n0, n1, n1)]
+        ew.get_fields(hb[0], hb[1])
+        ew.get_fields_grid(1, hb[2], hb[3])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            ew.set_fields(hb[0], hb[1])
+            ew.set_fields_grid(1, hb[2], hb[3])
+            ew.step(args.steps, sg.MODE_FUSED)
+            ew.get_fields(hb[0], None)
+            ew.get_fields_grid(1, hb[2], None)
+        torch.cuda.synchronize()
+        el = max_over_ranks(time.perf_counter() - t0, world)
+        out["e2e"] = {"value": world * pts * args.steps / el, "unit": UNIT,
+                      "h2d_bytes_per_step": int(2 * (n0 + n1) * 8 / args.steps),
+                      "d2h_bytes_per_step": int((n0 + n1) * 8 / args.steps)}
+    ew.close()
+    torch.cuda.empty_cache()
+    return out
+
+
 RECEIVER_SEED = 20240611
 
 
@@ -400,6 +503,8 @@ def run_ours(args, rank, world):
         mixed["roofline"]["peak"] = peak_hbm
         mixed["roofline"]["frac"] = mixed["roofline"]["achieved"] / peak_hbm
 
+    topo = None if args.no_topo else _time_topo(args, sg, torch, stream, world)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         ncores = os.cpu_count() or 1
@@ -438,6 +543,7 @@ def run_ours(args, rank, world):
             "gpu_launches": fp64["gpu_launches"],
             "cpu_baseline": cpu,
             "mixed": mixed,
+            "topography": topo,
         }
         print(json.dumps(line), flush=True)
     return 0
@@ -457,6 +563,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the FP32-mixed form")
+    ap.add_argument("--no-topo", action="store_true", help="skip the topography workload")
     ap.add_argument("--no-err", action="store_true", help="skip the mixed-vs-FP64 error run")
     ap.add_argument("--err-n", type=int, default=256, help="grid of the mixed-vs-FP64 error run")
     ap.add_argument("--err-steps", type=int, default=1000, help="steps of the error run")

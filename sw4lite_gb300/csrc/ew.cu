@@ -275,6 +275,7 @@ int EW::compute_time_step(double cfl, double tmax, double* dt, int* nsteps)
    SW4G_TRY(cuda_ok(cudaMemcpy(l.data(), la_, n * sizeof(double), cudaMemcpyDeviceToHost)));
    int ns = 0;
    double d = cfl_time_step(g_, r.data(), m.data(), l.data(), cfl, t_, tmax, &ns);
+   if (!(d > 0) || !(tmax > t_)) return kBadArgument;
    if (cv_) {
       // min over both grids of the raw limits, then land on tmax (src/EW.C:5041-5146)
       double eigmax = -1;
@@ -282,6 +283,7 @@ int EW::compute_time_step(double cfl, double tmax, double* dt, int* nsteps)
       double dc = cfl * g_.h * (1 / std::sqrt(eigmax)), dv = 0;
       SW4G_TRY(curv_time_step(cfl, &dv));
       dc = std::min(dc, dv);
+      if (!((tmax - t_) / dc < 2.0e9)) return kBadArgument;
       ns = static_cast<int>((tmax - t_) / dc + 0.5);
       ns = ns == 0 ? 1 : ns;
       d = (tmax - t_) / ns;

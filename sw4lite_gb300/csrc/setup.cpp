@@ -148,6 +148,7 @@ double cfl_time_step(const GridSpec& g, const double* rho, const double* mu, con
       eigmax = e > eigmax ? e : eigmax;
    }
    double dt = cfl * g.h * (1 / std::sqrt(eigmax));
+   if (!((tmax - tstart) / dt < 2.0e9)) return -1;  // the step count would not fit an int
    int ns = static_cast<int>((tmax - tstart) / dt + 0.5);
    ns = ns == 0 ? 1 : ns;
    dt = (tmax - tstart) / ns;
