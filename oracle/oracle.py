@@ -279,6 +279,41 @@ def step_topo(problem: Problem, curv: Curv, t, cart_arrays, curv_arrays, which="
        *[_dp(a) for a in curv_arrays])
 
 
+def step_pred(problem: Problem, t, up, u, um, lu, f, uacc, pred):
+    """sw4o_step that also returns the predicted level in pred."""
+    lib().sw4o_step_pred(C.byref(problem), C.c_int(1), C.c_double(t), _dp(up), _dp(u), _dp(um),
+                         _dp(lu), _dp(f), _dp(uacc), _dp(pred))
+
+
+def apply_lt(bounds, nz, y, mu, la, h, strx, stry, strz):
+    """L^T y = W L (W^-1 y) on the interior (zero ghosts), W = 1/(sx sy sz)."""
+    lt = np.zeros_like(y)
+    lib().sw4o_apply_lt(*[C.c_int(b) for b in bounds], C.c_int(nz), _dp(y), _dp(mu), _dp(la),
+                        C.c_double(h), _dp(strx), _dp(stry), _dp(strz), _dp(lt))
+    return lt
+
+
+def sg_adjoint(bounds, y, rho, dc, st, co):
+    """SG^T (y / rho) on the interior."""
+    z = np.zeros_like(y)
+    lib().sw4o_sg_adjoint(*[C.c_int(b) for b in bounds], _dp(y), _dp(rho), *[_dp(a) for a in dc],
+                          *[_dp(a) for a in st], *[_dp(a) for a in co], _dp(z))
+    return z
+
+
+def coef_gradient(bounds, v, w, h, st, gmu, gla):
+    """gmu, gla += gradient of v . L(w) with respect to mu, lambda."""
+    lib().sw4o_coef_gradient(*[C.c_int(b) for b in bounds], _dp(v), _dp(w), C.c_double(h),
+                             *[_dp(a) for a in st], _dp(gmu), _dp(gla))
+
+
+def sg_rho_gradient(bounds, a1, d, rho, dc, st, co, beta, grho):
+    """grho += -beta * d/drho [(R a1) . SG(d)] at fixed R."""
+    lib().sw4o_sg_rho_gradient(*[C.c_int(b) for b in bounds], _dp(a1), _dp(d), _dp(rho),
+                               *[_dp(a) for a in dc], *[_dp(a) for a in st], *[_dp(a) for a in co],
+                               C.c_double(beta), _dp(grho))
+
+
 def nearest_grid_point(h, zmin, x, y, z):
     """EW::computeNearestGridPoint (src/EW.C:5149-5177) for one Cartesian grid:
     1-based (i, j, k) of the nearest point, a half-way point going to the lower index."""

@@ -715,6 +715,12 @@ static void enforce_bc(const sw4o_problem* p, int soa, double* u)
 void sw4o_step(const sw4o_problem* p, int soa, double t, double* up, const double* u,
                const double* um, double* lu, double* f, double* uacc)
 {
+   sw4o_step_pred(p, soa, t, up, u, um, lu, f, uacc, NULL);
+}
+
+void sw4o_step_pred(const sw4o_problem* p, int soa, double t, double* up, const double* u,
+                    const double* um, double* lu, double* f, double* uacc, double* pred)
+{
    double acof[384], ghcof[6], bope[48], sbop[5];
    sw4o_stencil_coefficients(acof, ghcof, bope, sbop);
    const long npts = (long)(p->ie - p->ib + 1) * (p->je - p->jb + 1) * (p->ke - p->kb + 1);
@@ -727,6 +733,7 @@ void sw4o_step(const sw4o_problem* p, int soa, double t, double* up, const doubl
                ghcof, lu, u, p->mu, p->la, p->h, p->strx, p->stry, p->strz);
    sw4o_predfort(soa, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, u, um, lu, f, p->rho, dt * dt);
    enforce_bc(p, soa, up);
+   if (pred) memcpy(pred, up, 3 * npts * sizeof(double));
 
    sw4o_force(soa, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, f, p->nsrc, p->src_ijk, p->src_amp,
               p->src_freq, p->src_t0, p->src_kind, t, 1);

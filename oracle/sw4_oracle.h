@@ -166,6 +166,26 @@ void sw4o_step_topo(const sw4o_problem* cart, const sw4o_curv* cv, double t, dou
  * curvilinear k=nz..nz+2 from Cartesian k=1..3 (SoA, same i,j bounds). */
 void sw4o_cart_topo(const sw4o_problem* cart, const sw4o_curv* cv, double* ucart, double* ucurv);
 
+/* ---- discrete adjoint (sw4_oracle_adj.c): grids with zero ghost points ---- */
+void sw4o_apply_lt(int ib, int ie, int jb, int je, int kb, int ke, int nz, const double* y,
+                   const double* mu, const double* la, double h, const double* strx,
+                   const double* stry, const double* strz, double* lt);
+void sw4o_sg_adjoint(int ib, int ie, int jb, int je, int kb, int ke, const double* y,
+                     const double* rho, const double* dcx, const double* dcy, const double* dcz,
+                     const double* strx, const double* stry, const double* strz, const double* cox,
+                     const double* coy, const double* coz, double* z);
+void sw4o_coef_gradient(int ib, int ie, int jb, int je, int kb, int ke, const double* v,
+                        const double* w, double h, const double* strx, const double* stry,
+                        const double* strz, double* gmu, double* gla);
+void sw4o_sg_rho_gradient(int ib, int ie, int jb, int je, int kb, int ke, const double* a1,
+                          const double* d, const double* rho, const double* dcx, const double* dcy,
+                          const double* dcz, const double* strx, const double* stry,
+                          const double* strz, const double* cox, const double* coy,
+                          const double* coz, double beta, double* grho);
+/* sw4o_step that also returns the predicted level (after its boundary pass) in pred */
+void sw4o_step_pred(const sw4o_problem* p, int soa, double t, double* up, const double* u,
+                    const double* um, double* lu, double* f, double* uacc, double* pred);
+
 /* Analytic whole-space displacement of one point source in a homogeneous medium
  * (rho, cp, cs) at time t, written SoA over the array [ib,ie]x[jb,je]x[kb,ke]
  * with x=(i-1)h, y=(j-1)h, z=zmin+(k-1)h: the field the reference compares

@@ -1,0 +1,259 @@
+/* CPU oracle for the discrete adjoint of the Cartesian time step --
+ * TEST INFRASTRUCTURE ONLY (tests/ and the bench's CPU leg use it as a checker).
+ *
+ * The reference has no material-gradient adjoint (sw4lite computes source
+ * gradients only, src/GridPointSource.C:659); these functions restate the exact
+ * transpose of the oracle's own step (sw4o_step) for grids whose ghost points
+ * are zero after every boundary pass (Dirichlet / supergrid sides with zero
+ * boundary data, no free surface), so the state is the interior points I.
+ *
+ * Step (on I, R = diag(1/rho)):
+ *   up = 2u - um + dt^2 R L(u) + dt^2 R F
+ *   u+ = up + dt^2/12 R L(up - 2u + um) - beta R SG(u - um) + dt^4/12 R F_tt
+ * Transposes:
+ *   L^T = W L W^-1 with W = 1/(sx sy sz) (W L is symmetric: the stretched
+ *   elastic operator is self-adjoint in the stretched volume);
+ *   SG = sum_ax diag(w_ax) D2 E_ax D2 with E_ax = rho dc_ax, so
+ *   SG^T y = sum_ax D2 E_ax D2 (w_ax y).
+ * Adjoint recursion a^n = g^n + A^T a^{n+1} + B^T a^{n+2}:
+ *   s = L^T R a1, m = a1 + dt^2/12 s, t = L^T R m,
+ *   a^n = g^n + 2m + dt^2 t - dt^2/6 s - a2 - beta SG^T R (a1 - a2).
+ * Gradient of a1 . u+ with respect to (rho, mu, lambda) at fixed (u, um):
+ *   mu, lambda: G(R a1 dt^2/12, up - 2u + um) + G(R m dt^2, u), G(v, w) the
+ *   coefficient gradient of v . L(w);
+ *   rho: -(1/rho)[m.(up - 2u + um) + a1.(u+ - up)] - beta dSG/drho terms.
+ */
+#ifndef _GNU_SOURCE
+#define _GNU_SOURCE
+#endif
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "sw4_oracle.h"
+
+typedef struct {
+   int ib, ie, jb, je, kb, ke;
+   long ni, nij, npts;
+} abox;
+
+static abox mk(int ib, int ie, int jb, int je, int kb, int ke)
+{
+   abox b = {ib, ie, jb, je, kb, ke, ie - ib + 1, 0, 0};
+   b.nij = b.ni * (je - jb + 1);
+   b.npts = b.nij * (ke - kb + 1);
+   return b;
+}
+
+static inline long IX(const abox* b, int i, int j, int k)
+{
+   return (i - b->ib) + b->ni * (j - b->jb) + b->nij * (long)(k - b->kb);
+}
+
+static inline int interior(const abox* b, int i, int j, int k)
+{
+   return i >= b->ib + 2 && i <= b->ie - 2 && j >= b->jb + 2 && j <= b->je - 2 && k >= b->kb + 2 &&
+          k <= b->ke - 2;
+}
+
+/* lt = L^T y = W L (W^-1 y) on I (SoA, zero outside I).  onesided must be all 0. */
+void sw4o_apply_lt(int ib, int ie, int jb, int je, int kb, int ke, int nz, const double* y,
+                   const double* mu, const double* la, double h, const double* strx,
+                   const double* stry, const double* strz, double* lt)
+{
+   double acof[384], ghcof[6], bope[48], sbop[5];
+   sw4o_stencil_coefficients(acof, ghcof, bope, sbop);
+   const abox b = mk(ib, ie, jb, je, kb, ke);
+   double* wy = (double*)calloc(3 * b.npts, sizeof(double));
+   for (int k = kb; k <= ke; k++)
+      for (int j = jb; j <= je; j++)
+         for (int i = ib; i <= ie; i++) {
+            if (!interior(&b, i, j, k)) continue;
+            const long p = IX(&b, i, j, k);
+            const double iw = strx[i - ib] * stry[j - jb] * strz[k - kb];
+            for (int c = 0; c < 3; c++) wy[c * b.npts + p] = iw * y[c * b.npts + p];
+         }
+   memset(lt, 0, 3 * b.npts * sizeof(double));
+   const int os[6] = {0, 0, 0, 0, 0, 0};
+   sw4o_rhs4sg(1, ib, ie, jb, je, kb, ke, nz, os, acof, bope, ghcof, lt, wy, mu, la, h, strx, stry,
+               strz);
+   for (int k = kb; k <= ke; k++)
+      for (int j = jb; j <= je; j++)
+         for (int i = ib; i <= ie; i++) {
+            const long p = IX(&b, i, j, k);
+            const double w = interior(&b, i, j, k) ? 1 / (strx[i - ib] * stry[j - jb] * strz[k - kb]) : 0;
+            for (int c = 0; c < 3; c++) lt[c * b.npts + p] *= w;
+         }
+   free(wy);
+}
+
+/* weights w_ax of the damping terms at a point (sw4o_addsgd4) */
+static void sg_w(const abox* b, int i, int j, int k, const double* strx, const double* stry,
+                 const double* strz, const double* cox, const double* coy, const double* coz,
+                 double w[3])
+{
+   w[0] = strx[i - b->ib] * coy[j - b->jb] * coz[k - b->kb];
+   w[1] = stry[j - b->jb] * cox[i - b->ib] * coz[k - b->kb];
+   w[2] = strz[k - b->kb] * cox[i - b->ib] * coy[j - b->jb];
+}
+
+/* z = SG^T (y / rho) on I: sum_ax D2 E D2 (w_ax y / rho), with the vector zero
+ * outside I. */
+void sw4o_sg_adjoint(int ib, int ie, int jb, int je, int kb, int ke, const double* y,
+                     const double* rho, const double* dcx, const double* dcy, const double* dcz,
+                     const double* strx, const double* stry, const double* strz, const double* cox,
+                     const double* coy, const double* coz, double* z)
+{
+   const abox b = mk(ib, ie, jb, je, kb, ke);
+   const double* dcs[3] = {dcx, dcy, dcz};
+   const long st[3] = {1, b.ni, b.nij};
+   memset(z, 0, 3 * b.npts * sizeof(double));
+#pragma omp parallel for collapse(2)
+   for (int k = kb + 2; k <= ke - 2; k++)
+      for (int j = jb + 2; j <= je - 2; j++)
+         for (int i = ib + 2; i <= ie - 2; i++) {
+            const long p = IX(&b, i, j, k);
+            const int qa[3] = {i - ib, j - jb, k - kb};
+            for (int c = 0; c < 3; c++) {
+               double tot = 0;
+               for (int ax = 0; ax < 3; ax++) {
+                  double v[5];
+                  for (int m = -2; m <= 2; m++) {
+                     int ii = i + (ax == 0) * m, jj = j + (ax == 1) * m, kk = k + (ax == 2) * m;
+                     if (!interior(&b, ii, jj, kk)) {
+                        v[m + 2] = 0;
+                        continue;
+                     }
+                     double w[3];
+                     sg_w(&b, ii, jj, kk, strx, stry, strz, cox, coy, coz, w);
+                     const long q = IX(&b, ii, jj, kk);
+                     v[m + 2] = w[ax] * y[c * b.npts + q] / rho[q];
+                  }
+                  const double* dc = dcs[ax] + qa[ax];
+                  const double e0 = rho[p - st[ax]] * dc[-1], e1 = rho[p] * dc[0], e2 = rho[p + st[ax]] * dc[1];
+                  tot += e2 * (v[4] - 2 * v[3] + v[2]) - 2 * e1 * (v[3] - 2 * v[2] + v[1]) +
+                         e0 * (v[2] - 2 * v[1] + v[0]);
+               }
+               z[c * b.npts + p] = tot;
+            }
+         }
+}
+
+/* G(v, w): gradient of v . L(w) with respect to mu and lambda at every array
+ * point, added into gmu, gla.  v zero outside I; w zero at ghost points. */
+static const double DW[5] = {1, -8, 0, 8, -1};
+
+void sw4o_coef_gradient(int ib, int ie, int jb, int je, int kb, int ke, const double* v,
+                        const double* w, double h, const double* strx, const double* stry,
+                        const double* strz, double* gmu, double* gla)
+{
+   const abox b = mk(ib, ie, jb, je, kb, ke);
+   const double* sp[3] = {strx, stry, strz};
+   const int lo[3] = {ib, jb, kb}, hi[3] = {ie, je, ke};
+   const double c6 = 1.0 / (6 * h * h), c144 = 1.0 / (144 * h * h);
+   /* mixed terms: (equation c, component d, outer, inner, 0 mu / 1 lambda) */
+   static const int mix[12][5] = {{0, 1, 0, 1, 1}, {0, 1, 1, 0, 0}, {0, 2, 0, 2, 1}, {0, 2, 2, 0, 0},
+                                  {1, 0, 0, 1, 0}, {1, 0, 1, 0, 1}, {1, 2, 1, 2, 1}, {1, 2, 2, 1, 0},
+                                  {2, 0, 0, 2, 0}, {2, 0, 2, 0, 1}, {2, 1, 1, 2, 0}, {2, 1, 2, 1, 1}};
+#pragma omp parallel for collapse(2)
+   for (int k = kb; k <= ke; k++)
+      for (int j = jb; j <= je; j++)
+         for (int i = ib; i <= ie; i++) {
+            const int pc[3] = {i, j, k};
+            const long p = IX(&b, i, j, k);
+            double gm = 0, gl = 0;
+            /* same-axis second differences: rows q = p - n e_ax */
+            for (int ax = 0; ax < 3; ax++)
+               for (int n = -2; n <= 2; n++) {
+                  int qc[3] = {i, j, k};
+                  qc[ax] -= n;
+                  if (!interior(&b, qc[0], qc[1], qc[2])) continue;
+                  const long q = IX(&b, qc[0], qc[1], qc[2]);
+                  const long st = ax == 0 ? 1 : ax == 1 ? b.ni : b.nij;
+                  for (int c = 0; c < 3; c++) {
+                     const double vq = v[c * b.npts + q];
+                     if (vq == 0) continue;
+                     const double* wq = w + c * b.npts + q;
+                     double d[5];
+                     for (int m = -2; m <= 2; m++) d[m + 2] = wq[m * st] - wq[0];
+                     double K;
+                     switch (n) {
+                        case -2: K = -0.75 * d[0] + d[1]; break;
+                        case -1: K = d[0] + 3 * d[1] + d[3]; break;
+                        case 0: K = -0.75 * (d[0] + d[4]) + 3 * (d[1] + d[3]); break;
+                        case 1: K = d[1] + 3 * d[3] + d[4]; break;
+                        default: K = d[3] - 0.75 * d[4]; break;
+                     }
+                     const double f = c6 * vq * sp[ax][qc[ax] - lo[ax]] * K * sp[ax][pc[ax] - lo[ax]];
+                     if (c == ax) {
+                        gm += 2 * f;
+                        gl += f;
+                     } else {
+                        gm += f;
+                     }
+                  }
+               }
+            /* mixed terms: -(1/144h^2) s_ai(p) (DW.w_d along ai)(p) (DW.(s_ao v_c) along ao)(p) */
+            for (int t = 0; t < 12; t++) {
+               const int c = mix[t][0], d = mix[t][1], ao = mix[t][2], ai = mix[t][3];
+               if (pc[ai] < lo[ai] + 2 || pc[ai] > hi[ai] - 2) continue;
+               double inner = 0, outer = 0;
+               for (int m = -2; m <= 2; m++) {
+                  if (m == 0) continue;
+                  int a[3] = {i, j, k};
+                  a[ai] += m;
+                  inner += DW[m + 2] * w[d * b.npts + IX(&b, a[0], a[1], a[2])];
+                  int o[3] = {i, j, k};
+                  o[ao] += m;
+                  if (o[ao] < lo[ao] || o[ao] > hi[ao] || !interior(&b, o[0], o[1], o[2])) continue;
+                  outer += DW[m + 2] * sp[ao][o[ao] - lo[ao]] * v[c * b.npts + IX(&b, o[0], o[1], o[2])];
+               }
+               const double g = -c144 * sp[ai][pc[ai] - lo[ai]] * inner * outer;
+               if (mix[t][4]) gl += g;
+               else gm += g;
+            }
+            gmu[p] += gm;
+            gla[p] += gl;
+         }
+}
+
+/* rho gradient of the damping term: -beta * (R a1) . dSG(d)/drho at every point,
+ * added into grho; d = u - um (zero ghosts), a1 zero outside I. */
+void sw4o_sg_rho_gradient(int ib, int ie, int jb, int je, int kb, int ke, const double* a1,
+                          const double* d, const double* rho, const double* dcx, const double* dcy,
+                          const double* dcz, const double* strx, const double* stry,
+                          const double* strz, const double* cox, const double* coy,
+                          const double* coz, double beta, double* grho)
+{
+   const abox b = mk(ib, ie, jb, je, kb, ke);
+   const double* dcs[3] = {dcx, dcy, dcz};
+   const int lo[3] = {ib, jb, kb}, hi[3] = {ie, je, ke};
+#pragma omp parallel for collapse(2)
+   for (int k = kb; k <= ke; k++)
+      for (int j = jb; j <= je; j++)
+         for (int i = ib; i <= ie; i++) {
+            const int pc[3] = {i, j, k};
+            double g = 0;
+            for (int ax = 0; ax < 3; ax++) {
+               if (pc[ax] - 1 < lo[ax] || pc[ax] + 1 > hi[ax]) continue;
+               for (int c = 0; c < 3; c++) {
+                  double vv[3], dd[3];
+                  for (int m = -1; m <= 1; m++) {
+                     int q[3] = {i, j, k};
+                     q[ax] += m;
+                     const long qi = IX(&b, q[0], q[1], q[2]);
+                     dd[m + 1] = d[c * b.npts + qi];
+                     if (interior(&b, q[0], q[1], q[2])) {
+                        double w[3];
+                        sg_w(&b, q[0], q[1], q[2], strx, stry, strz, cox, coy, coz, w);
+                        vv[m + 1] = w[ax] * a1[c * b.npts + qi] / rho[qi];
+                     } else {
+                        vv[m + 1] = 0;
+                     }
+                  }
+                  g += dcs[ax][pc[ax] - lo[ax]] * (dd[2] - 2 * dd[1] + dd[0]) * (vv[2] - 2 * vv[1] + vv[0]);
+               }
+            }
+            grho[IX(&b, i, j, k)] -= beta * g;
+         }
+}

@@ -1,0 +1,129 @@
+"""The oracle's discrete adjoint (oracle/sw4_oracle_adj.c) on CPU.
+
+No reference output exists for a material gradient (sw4lite has source gradients
+only), so the adjoint is checked by its defining identities:
+  * dot products: <L x, y> = <x, L^T y> and <SG x, R y> = <x, SG^T R y> on the
+    interior, to 1e-13 relative;
+  * the coefficient gradient of v . L(w): L is linear in (mu, lambda), so
+    sum_p mu_p G_mu[p] + la_p G_la[p] = v . L(w) (Euler), and each entry equals
+    v . L(w; indicator) at sampled points, to 1e-12;
+  * the whole gradient against central finite differences of the misfit along a
+    smooth random direction in (rho, mu, lambda), to 1e-6 relative (the bar the
+    adjoint is held to on the GPU).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.adjoint_util import AdjointCase, misfit, oracle_forward, oracle_gradient, smooth_random
+from tests.gpu_util import OracleProblem
+
+pytest.importorskip("scipy")
+
+
+def _bounds(c):
+    return (-1, c.nx + 2, -1, c.ny + 2, -1, c.nz + 2)
+
+
+def _interior_mask(c):
+    m = np.zeros((c.nz + 4, c.ny + 4, c.nx + 4), dtype=bool)
+    m[2:-2, 2:-2, 2:-2] = True
+    return np.tile(m.reshape(-1), 3)
+
+
+def _rand_interior(c, seed):
+    x = np.random.default_rng(seed).standard_normal(3 * c.npts)
+    x[~_interior_mask(c)] = 0
+    return x
+
+
+def _profiles(c):
+    P = OracleProblem(c.grid, *c.mat, c.dt)
+    return [p[0] for p in P.prof], [p[1] for p in P.prof], [p[2] for p in P.prof]
+
+
+def test_lt_dot_product():
+    c = AdjointCase()
+    dc, st, co = _profiles(c)
+    x, y = _rand_interior(c, 1), _rand_interior(c, 2)
+    Lx = np.zeros_like(x)
+    acof = O.stencil_coefficients()
+    O.rhs4sg(1, _bounds(c), c.nz, (0,) * 6, Lx, x, c.mat[1], c.mat[2], c.h, *st)
+    Lx[~_interior_mask(c)] = 0
+    lhs = float(Lx @ y)
+    rhs = float(x @ O.apply_lt(_bounds(c), c.nz, y, c.mat[1], c.mat[2], c.h, *st))
+    assert abs(lhs - rhs) <= 1e-13 * abs(lhs)
+    assert np.max(np.abs(np.array(st[0]) - 1)) > 0.1  # stretched layers are present
+
+
+def test_sg_adjoint_dot_product():
+    c = AdjointCase()
+    dc, st, co = _profiles(c)
+    rho = c.mat[0]
+    x, y = _rand_interior(c, 3), _rand_interior(c, 4)
+    up = np.zeros_like(x)
+    # sw4o_addsgd4: up -= beta/rho SG(u - um)
+    O.addsgd(4, 1, _bounds(c), up, x, np.zeros_like(x), rho, dc, st, co, 1.0)
+    lhs = -float(up @ y)                 # <R SG x, y>
+    rhs = float(x @ O.sg_adjoint(_bounds(c), y, rho, dc, st, co))  # <x, SG^T R y>
+    assert abs(lhs - rhs) <= 1e-13 * abs(lhs)
+
+
+def test_coef_gradient_identities():
+    c = AdjointCase(shape=(14, 13, 15))
+    _, st, _ = _profiles(c)
+    v = _rand_interior(c, 5)
+    w = _rand_interior(c, 6)
+    mu, la = c.mat[1], c.mat[2]
+    n = c.npts
+    gm, gl = np.zeros(n), np.zeros(n)
+    O.coef_gradient(_bounds(c), v, w, c.h, st, gm, gl)
+
+    def vLw(m, l):
+        out = np.zeros_like(w)
+        O.rhs4sg(1, _bounds(c), c.nz, (0,) * 6, out, w, m, l, c.h, *st)
+        out[~_interior_mask(c)] = 0
+        return float(v @ out)
+
+    full = vLw(mu, la)
+    assert abs(float(mu @ gm + la @ gl) - full) <= 1e-12 * abs(full)
+    rng = np.random.default_rng(7)
+    for p in rng.integers(0, n, size=12):
+        e = np.zeros(n)
+        e[p] = 1.0
+        assert gm[p] == pytest.approx(vLw(e, np.zeros(n)), rel=1e-11, abs=1e-12 * abs(full))
+        assert gl[p] == pytest.approx(vLw(np.zeros(n), e), rel=1e-11, abs=1e-12 * abs(full))
+
+
+def test_sg_rho_gradient_identity():
+    c = AdjointCase(shape=(14, 13, 15))
+    dc, st, co = _profiles(c)
+    rho = c.mat[0]
+    a1, d = _rand_interior(c, 8), _rand_interior(c, 9)
+    g = np.zeros(c.npts)
+    O.sg_rho_gradient(_bounds(c), a1, d, rho, dc, st, co, 0.02, g)
+    up = np.zeros_like(d)
+    O.addsgd(4, 1, _bounds(c), up, d, np.zeros_like(d), rho, dc, st, co, 0.02)
+    # -beta (R a1).SG(d) is linear in rho through E = rho dc at fixed R
+    assert float(rho @ g) == pytest.approx(float(a1 @ up), rel=1e-12)
+
+
+@pytest.mark.parametrize("which", ["rho", "mu", "la", "all"])
+def test_oracle_gradient_matches_finite_differences(which):
+    c = AdjointCase()
+    # observed data: the same shot in a slightly different medium
+    obs_case = AdjointCase(seed=11)
+    obs = obs_case.records(oracle_forward(obs_case)[0][1:])
+    J, gr, gm, gl = oracle_gradient(c, obs)
+    shape = (c.nz + 4, c.ny + 4, c.nx + 4)
+    # a smooth direction of order the material itself (values in about [-0.6, 1.5])
+    dirs = [smooth_random(shape, 40 + q, corr=3.0, amp=0.3).reshape(-1) - 1.0 for q in range(3)]
+    keep = {"rho": (0,), "mu": (1,), "la": (2,), "all": (0, 1, 2)}[which]
+    dm = [dirs[q] * c.mat[q] if q in keep else np.zeros(c.npts) for q in range(3)]
+    pred = float(gr @ dm[0] + gm @ dm[1] + gl @ dm[2])
+    eps = 1e-5  # central difference: truncation ~eps^2, rounding ~1e-16/eps
+    Jp = misfit(c, oracle_forward(c, [c.mat[q] + eps * dm[q] for q in range(3)])[0], obs)
+    Jm = misfit(c, oracle_forward(c, [c.mat[q] - eps * dm[q] for q in range(3)])[0], obs)
+    fd = (Jp - Jm) / (2 * eps)
+    assert abs(pred) > 0
+    assert abs(fd - pred) <= 1e-6 * abs(pred), (fd, pred)
