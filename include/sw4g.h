@@ -286,6 +286,20 @@ double* sw4g_ew_field(const sw4g_ew* ew, int which);
 /* advance nsteps time steps */
 int sw4g_ew_step(sw4g_ew* ew, int nsteps, int mode);
 
+/* Discrete adjoint (no reference counterpart: sw4lite computes source-parameter
+ * gradients only, src/GridPointSource.C:659-760).  Runs nsteps fused FP64 steps
+ * from the current levels, recording the receivers (all SW4G_REC_DISPLACEMENT,
+ * capacity >= nsteps+1; rows are rewritten from row 0), and returns the misfit
+ * J = 1/2 sum_{n=0..nsteps} sum_r |rec^n_r - obs^n_r|^2 (obs: (nsteps+1) x nvals,
+ * the record layout) and dJ/drho, dJ/dmu, dJ/dlambda at every array point (npts
+ * each), by the exact transpose of the step with checkpoints every
+ * checkpoint_every steps.  Device memory: (2*ceil(nsteps/C) + 2*C + 11) levels of
+ * 3*npts doubles.  Requires Dirichlet or supergrid sides (zero ghost data), 4th-order
+ * damping, no topography.  The object ends at the end of the forward run. */
+int sw4g_ew_gradient(sw4g_ew* ew, int nsteps, int checkpoint_every, const double* observed,
+                     int obs_on_device, double* misfit, double* grad_rho, double* grad_mu,
+                     double* grad_lambda, int grad_on_device);
+
 /* Topography (replaces the reference's topography + curvilinear grid set-up,
  * src/EW.C:540-720 (deck), 2018-2046 (dimensions), 6164 (generate_grid), 6229
  * (setup_metric), and the curvilinear grid's share of every phase of the time

@@ -86,6 +86,8 @@ _SIGS = {
     "sw4g_ew_create_topo": ([C.POINTER(GridDesc), C.POINTER(TopoDesc), _VP, C.POINTER(_VP)],
                             C.c_int),
     "sw4g_ew_num_grids": ([_VP], C.c_int),
+    "sw4g_ew_gradient": ([_VP, C.c_int, C.c_int, _VP, C.c_int, _D, _VP, _VP, _VP, C.c_int],
+                         C.c_int),
     "sw4g_ew_grid_dims": ([_VP, C.c_int, _I, _I, _I, C.POINTER(C.c_longlong)], C.c_int),
     "sw4g_ew_set_material_grid": ([_VP, C.c_int, _VP, _VP, _VP, C.c_int], C.c_int),
     "sw4g_ew_set_fields_grid": ([_VP, C.c_int, _VP, _VP, C.c_int], C.c_int),
@@ -293,6 +295,19 @@ class EW:
 
     def enforce_bc(self, u):
         check(lib().sw4g_ew_enforce_bc(self._h, _ptr(u)), "enforce_bc")
+
+    def gradient(self, nsteps, checkpoint_every, observed, g_rho, g_mu, g_la):
+        """Misfit of the receiver records against `observed` ((nsteps+1) x nvals) over
+        nsteps steps from the current levels, and its gradient with respect to
+        (rho, mu, lambda) written into g_rho, g_mu, g_la (npts each; host arrays or
+        device tensors).  Returns the misfit."""
+        J = C.c_double()
+        od = int(hasattr(observed, "is_cuda") and observed.is_cuda)
+        gd = int(hasattr(g_rho, "is_cuda") and g_rho.is_cuda)
+        check(lib().sw4g_ew_gradient(self._h, nsteps, checkpoint_every, _ptr(observed), od,
+                                     C.byref(J), _ptr(g_rho), _ptr(g_mu), _ptr(g_la), gd),
+              "gradient")
+        return J.value
 
     @property
     def num_grids(self) -> int:

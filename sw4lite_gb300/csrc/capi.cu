@@ -425,6 +425,15 @@ int sw4g_ew_create_topo(const sw4g_grid* g, const sw4g_topography* t, void* stre
    return SW4G_OK;
 }
 
+int sw4g_ew_gradient(sw4g_ew* ew, int nsteps, int checkpoint_every, const double* observed,
+                     int obs_on_device, double* misfit, double* grad_rho, double* grad_mu,
+                     double* grad_lambda, int grad_on_device)
+{
+   if (!ew) return SW4G_BAD_ARGUMENT;
+   return ew->impl->gradient(nsteps, checkpoint_every, observed, obs_on_device != 0, misfit,
+                             grad_rho, grad_mu, grad_lambda, grad_on_device != 0);
+}
+
 int sw4g_ew_num_grids(const sw4g_ew* ew) { return ew ? ew->impl->num_grids() : -1; }
 
 int sw4g_ew_grid_dims(const sw4g_ew* ew, int grid, int* nx, int* ny, int* nz, long long* npts)

@@ -697,6 +697,9 @@ int EW::step_fused()
    while (iq == iu_ || iq == ium_) iq++;
    for (int which = 0; which < 6; which++) {
       SW4G_TRY(piece(which, ip, iq));
+      if (which == 2 && capture_pred_)
+         SW4G_TRY(cuda_ok(cudaMemcpyAsync(capture_pred_, lev_[ip], 3 * (size_t)npts_ * sizeof(double),
+                                          cudaMemcpyDeviceToDevice, stream_)));
       if (!cv_) continue;
       if (which == 0) SW4G_TRY(curv_pred(ip));
       if (which == 2) SW4G_TRY(curv_bc(lev_[ip], cv_->lev[ip]));

@@ -87,6 +87,14 @@ class EW {
 
    int step(int nsteps, int mode);
 
+   // Misfit J = 1/2 sum_{n=0..nsteps} |rec^n - obs^n|^2 of the receivers (all in
+   // displacement mode) over nsteps fused steps from the current levels, and its
+   // gradient with respect to rho, mu, lambda at every array point, by the
+   // discrete adjoint (adjoint.cu) with checkpoints every ckpt steps.  FP64,
+   // Dirichlet / supergrid sides only.  The object ends after the forward run.
+   int gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, double* misfit,
+                double* g_rho, double* g_mu, double* g_la, bool grad_on_device);
+
    // Grids: 0 the Cartesian grid, 1 the curvilinear grid (with topography).
    int num_grids() const { return cv_ ? 2 : 1; }
    int grid_dims(int grid, int* nx, int* ny, int* nz, long long* npts) const;
@@ -181,6 +189,7 @@ class EW {
    bool rec_initial_ = false;  // the initial-data row is still to be written
 
    std::unique_ptr<CurvGrid> cv_;
+   double* capture_pred_ = nullptr;  // if set, a fused step copies its predicted level here
 
    double t_ = 0, dt_ = 0;
 };

@@ -1,0 +1,125 @@
+"""The discrete adjoint on the GPU (sw4g_ew_gradient).
+
+* Against the oracle's adjoint (tests/test_oracle_adjoint.py checks it by dot
+  products and finite differences): misfit to 1e-12, gradients to 1e-9 relative
+  to each gradient's largest magnitude, for several checkpoint spacings.
+* Against central finite differences of GPU forward runs on a 48^3 copy of the
+  adjoint workload (smooth 5% log-normal heterogeneity, one point force, 16
+  receivers): the directional derivative along a smooth random direction in
+  (rho, mu, lambda) to 1e-6 relative.
+"""
+import numpy as np
+import pytest
+
+import sw4lite_gb300 as sg
+from oracle import oracle as O
+from tests.adjoint_util import AdjointCase, oracle_forward, oracle_gradient, smooth_random
+from tests.gpu_util import dev, host
+
+pytestmark = pytest.mark.gpu
+pytest.importorskip("scipy")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    sg.build()
+    O.lib()
+
+
+def _ew(case, mat=None):
+    mat = case.mat if mat is None else mat
+    ew = sg.EW(case.grid)
+    ew.set_material(*[dev(a) for a in mat])
+    for s in case.sources:
+        ew.add_source(s)
+    ew.set_time_step(case.dt, 0.0)
+    ew.set_receivers(case.rec, [sg.REC_DISPLACEMENT] * len(case.rec), case.nsteps + 1)
+    return ew
+
+
+def _gpu_gradient(case, obs, ckpt):
+    ew = _ew(case)
+    g = [dev(np.zeros(case.npts)) for _ in range(3)]
+    J = ew.gradient(case.nsteps, ckpt, dev(obs), *g)
+    # the object ends after the forward run
+    assert ew.time == pytest.approx(case.nsteps * case.dt, rel=1e-14)
+    u = dev(np.zeros(3 * case.npts))
+    ew.get_fields(u, None)
+    ew.close()
+    return J, [host(x) for x in g], host(u)
+
+
+def _gpu_misfit(case, obs, mat):
+    ew = _ew(case, mat)
+    ew.step(case.nsteps, sg.MODE_FUSED)
+    rec = ew.records()
+    ew.close()
+    return 0.5 * float(np.sum((rec - obs) ** 2))
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+@pytest.mark.parametrize("ckpt", [30, 7, 1])
+def test_gradient_matches_oracle_adjoint(ckpt):
+    c = AdjointCase()
+    obs_case = AdjointCase(seed=11)
+    obs = obs_case.records(oracle_forward(obs_case)[0][1:])
+    J0, gr, gm, gl = oracle_gradient(c, obs)
+    J, (r, m, l), ufin = _gpu_gradient(c, obs, ckpt)
+    assert J == pytest.approx(J0, rel=1e-12)
+    assert _rel(r, gr) <= 1e-9
+    assert _rel(m, gm) <= 1e-9
+    assert _rel(l, gl) <= 1e-9
+    levels = oracle_forward(c)[0]
+    assert _rel(ufin, levels[-1]) <= 1e-12
+
+
+def test_gradient_matches_finite_differences_48():
+    # the finite-difference copy of the adjoint workload: 48^3, 5% log-normal
+    # heterogeneity with correlation length 10h (here 10 points), 16 receivers
+    c = AdjointCase(shape=(48, 48, 48), h=0.05, gp=10, seed=21, nsteps=160, nrec=16,
+                    vp=1.732, vs=1.0, rho=1.0)
+    from scipy.ndimage import gaussian_filter  # noqa: F401  (smooth_random needs scipy)
+    obs_case = AdjointCase(shape=(48, 48, 48), h=0.05, gp=10, seed=22, nsteps=160, nrec=16,
+                           vp=1.732, vs=1.0, rho=1.0)
+    obs_case.rec = c.rec
+    ew = _ew(obs_case)
+    ew.step(obs_case.nsteps, sg.MODE_FUSED)
+    obs = ew.records()
+    ew.close()
+    J, (gr, gm, gl), _ = _gpu_gradient(c, obs, 40)
+    shape = (c.nz + 4, c.ny + 4, c.nx + 4)
+    dirs = [smooth_random(shape, 60 + q, corr=5.0, amp=0.3).reshape(-1) - 1.0 for q in range(3)]
+    dm = [dirs[q] * c.mat[q] for q in range(3)]
+    pred = float(gr @ dm[0] + gm @ dm[1] + gl @ dm[2])
+    eps = 1e-5
+    Jp = _gpu_misfit(c, obs, [c.mat[q] + eps * dm[q] for q in range(3)])
+    Jm = _gpu_misfit(c, obs, [c.mat[q] - eps * dm[q] for q in range(3)])
+    fd = (Jp - Jm) / (2 * eps)
+    assert J > 0 and abs(pred) > 0
+    assert abs(fd - pred) <= 1e-6 * abs(pred), (fd, pred)
+
+
+def test_gradient_rejects_unsupported_set_ups():
+    c = AdjointCase(shape=(16, 16, 16), nsteps=4)
+    obs = np.zeros((5, 3 * len(c.rec)))
+    g = [np.zeros(c.npts) for _ in range(3)]
+    free = sg.grid_desc(16, 16, 16, c.h, bc=(2, 2, 2, 2, 0, 2), sg_gp=5)
+    for grid, code in ((free, "not supported"),):
+        ew = sg.EW(grid)
+        ew.set_material(*[dev(a) for a in c.mat])
+        ew.set_time_step(c.dt)
+        ew.set_receivers(c.rec, [sg.REC_DISPLACEMENT] * len(c.rec), 5)
+        with pytest.raises(sg.Sw4gError):
+            ew.gradient(4, 2, obs, *g)
+        ew.close()
+    ew = _ew(c)
+    ew.set_receivers(c.rec, [sg.REC_VELOCITY] * len(c.rec), 5)
+    with pytest.raises(sg.Sw4gError):
+        ew.gradient(4, 2, obs, *g)
+    ew.set_receivers(c.rec, [sg.REC_DISPLACEMENT] * len(c.rec), 3)
+    with pytest.raises(sg.Sw4gError):  # record capacity below nsteps + 1
+        ew.gradient(4, 2, obs, *g)
+    ew.close()
