@@ -416,6 +416,101 @@ def _time_topo(args, sg, torch, stream, world):
     return out
 
 
+def c4_config(n=256):
+    """Adjoint workload: a 5% log-normal medium (Gaussian correlation length 10h,
+    seeded) around vp 6000, vs 3464, rho 2700 on an n^3 grid at h = 50 m with
+    supergrid on all sides; one vertical point force at the centre (Gaussian,
+    sigma 0.05 s); 16 receivers at seeded interior points; the observed data are
+    the records of the same shot in the homogeneous background."""
+    return dict(n=n, h=50.0, vp=6000.0, vs=3464.0, rho=2700.0, std=0.05, corr=10.0, seed=4242,
+                gp=30, src=dict(force=(0.0, 0.0, 1e15), freq=20.0, t0=0.3), nrec=16, cfl=1.3)
+
+
+def _lognormal(torch, shape, std, corr, seed):
+    """exp(std * g), g a unit-variance Gaussian random field with Gaussian
+    correlation length `corr` points (white noise filtered in Fourier space)."""
+    gen = torch.Generator(device="cuda").manual_seed(seed)
+    w = torch.randn(shape, generator=gen, dtype=torch.float64, device="cuda")
+    f = torch.fft.rfftn(w)
+    ks = [torch.fft.fftfreq(s, device="cuda", dtype=torch.float64) for s in shape[:-1]]
+    ks.append(torch.fft.rfftfreq(shape[-1], device="cuda", dtype=torch.float64))
+    K = sum(k.reshape([-1 if d == a else 1 for d in range(3)]) ** 2 for a, k in enumerate(ks))
+    g = torch.fft.irfftn(f * torch.exp(-0.5 * (2 * np.pi * corr) ** 2 * K), s=shape)
+    g = (g - g.mean()) / g.std()
+    return torch.exp(std * g)
+
+
+def _make_c4(sg, torch, cfg, stream, nsteps, homogeneous=False, dt=None):
+    n, h = cfg["n"], cfg["h"]
+    g = sg.grid_desc(n, n, n, h, bc=(2,) * 6, sg_gp=cfg["gp"])
+    shape = (n + 4, n + 4, n + 4)
+    if homogeneous:
+        pr = ps = pv = torch.ones(shape, dtype=torch.float64, device="cuda")
+    else:
+        pr, ps, pv = (_lognormal(torch, shape, cfg["std"], cfg["corr"], cfg["seed"] + q)
+                      for q in range(3))
+    rho = cfg["rho"] * pr
+    vs = cfg["vs"] * ps
+    vp = cfg["vp"] * pv
+    mu = rho * vs * vs
+    la = rho * vp * vp - 2 * mu
+    ew = sg.EW(g, stream=stream)
+    mat = [a.reshape(-1).contiguous() for a in (rho, mu, la)]
+    ew.set_material(*mat)
+    c = (n - 1) * h / 2
+    sc = cfg["src"]
+    ew.add_source(sg.source_desc(c, c, c, force=sc["force"], freq=sc["freq"], t0=sc["t0"],
+                                 kind=sg.GAUSSIAN))
+    if dt is None:
+        dt = cfg["cfl"] * h / float(torch.sqrt(((4 * mu + la) / rho).max()))
+    ew.set_time_step(dt, 0.0)
+    rng = np.random.default_rng(cfg["seed"])
+    rec = [tuple(int(x) for x in rng.integers(cfg["gp"] + 2, n - cfg["gp"], size=3))
+           for _ in range(cfg["nrec"])]
+    ew.set_receivers(rec, [sg.REC_DISPLACEMENT] * len(rec), nsteps + 1)
+    return ew, dt
+
+
+def _time_adjoint(args, sg, torch, stream):
+    """Forward solve and misfit gradient of the adjoint workload, each timed with
+    CUDA events on the EW stream; the ratio is the gradient's cost in forward
+    solves."""
+    cfg = c4_config(args.adj_n)
+    N, C = args.adj_steps, args.adj_ckpt
+    with torch.cuda.stream(stream):
+        ew, dt = _make_c4(sg, torch, cfg, stream, N)
+        ew.close()
+        ew0, _ = _make_c4(sg, torch, cfg, stream, N, homogeneous=True, dt=dt)
+        ew0.step(N, sg.MODE_FUSED)
+        obs = torch.zeros(ew0.record_shape(), dtype=torch.float64, device="cuda")
+        ew0.records(obs)
+        torch.cuda.synchronize()
+        ew0.close()
+        ew, _ = _make_c4(sg, torch, cfg, stream, N, dt=dt)
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        torch.cuda.synchronize()
+        e[0].record(stream)
+        ew.step(N, sg.MODE_FUSED)
+        e[1].record(stream)
+        torch.cuda.synchronize()
+        ew.close()
+        ew, _ = _make_c4(sg, torch, cfg, stream, N, dt=dt)
+        g = [torch.zeros(ew.npts, dtype=torch.float64, device="cuda") for _ in range(3)]
+        torch.cuda.synchronize()
+        e[2].record(stream)
+        J = ew.gradient(N, C, obs, *g)
+        e[3].record(stream)
+        torch.cuda.synchronize()
+        ew.close()
+    fwd_ms, grad_ms = e[0].elapsed_time(e[1]), e[2].elapsed_time(e[3])
+    n = cfg["n"]
+    return {"workload": f"C4 adjoint {n}^3, 5% log-normal medium, 1 point force, 16 receivers, "
+                        f"{N} steps, checkpoints every {C}",
+            "forward_ms": fwd_ms, "gradient_ms": grad_ms, "gradient_over_forward": grad_ms / fwd_ms,
+            "misfit": J, "grad_norms": [float(x.norm()) for x in g],
+            "forward_value": n ** 3 * N / (fwd_ms * 1e-3), "unit": UNIT}
+
+
 RECEIVER_SEED = 20240611
 
 
@@ -504,6 +599,7 @@ def run_ours(args, rank, world):
         mixed["roofline"]["frac"] = mixed["roofline"]["achieved"] / peak_hbm
 
     topo = None if args.no_topo else _time_topo(args, sg, torch, stream, world)
+    adj = None if args.no_adjoint else _time_adjoint(args, sg, torch, stream)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -544,6 +640,7 @@ def run_ours(args, rank, world):
             "cpu_baseline": cpu,
             "mixed": mixed,
             "topography": topo,
+            "adjoint": adj,
         }
         print(json.dumps(line), flush=True)
     return 0
@@ -564,6 +661,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the FP32-mixed form")
     ap.add_argument("--no-topo", action="store_true", help="skip the topography workload")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint workload")
+    ap.add_argument("--adj-n", type=int, default=256, help="grid of the adjoint workload")
+    ap.add_argument("--adj-steps", type=int, default=200, help="steps of the adjoint workload")
+    ap.add_argument("--adj-ckpt", type=int, default=100, help="checkpoint spacing")
     ap.add_argument("--no-err", action="store_true", help="skip the mixed-vs-FP64 error run")
     ap.add_argument("--err-n", type=int, default=256, help="grid of the mixed-vs-FP64 error run")
     ap.add_argument("--err-steps", type=int, default=1000, help="steps of the error run")

@@ -15,15 +15,22 @@
 // B^T a^{n+2} becomes, with a1 = a^{n+1}, a2 = a^{n+2}:
 //   s = L^T R a1,  m = a1 + dt^2/12 s,  t = L^T R m,
 //   a^n = g^n + 2m + dt^2 t - dt^2/6 s - a2 - beta SG^T R (a1 - a2),
-// two operator applications per step like the forward.  The gradient of
-// a1 . u+ at fixed (u, um):
-//   mu, lambda : G(dt^2/12 R a1, up - 2u + um) + G(dt^2 R m, u), G(v, w) the
-//                coefficient gradient of v . L(w) (a local gather: the derivative
-//                of each second-difference row with respect to its five
-//                coefficients, and minus products of first differences for the
-//                mixed terms);
-//   rho        : -(1/rho)[m.(up - 2u + um) + a1.(u+ - up)] (the 1/rho factors and
-//                the forcing) - beta dc D2(u - um) . D2(w R a1) (the damping's
+// two operator applications per step like the forward.  In the scaled variable
+// b = W^-1 R a the recursion takes the forward's own form (the W factors commute
+// with each axis' damping term, so W^-1 R SG^T R W = R SG):
+//   mt = b1 + dt^2/12 R L(b1),
+//   b^n = 2 b1 - b2 + dt^2 R L(mt) - beta R SG(b1 - b2) + W^-1 R g^n,
+// which runs on the forward's fused stage kernels (predictor form with
+// coefficient dt^2/12, and the adjoint form of stage_fused.cu).  The gradient of
+// a1 . u+ at fixed (u, um) (a1 = rho W b1, m = rho W mt):
+//   mu, lambda : G(dt^2/12 W b1, up - 2u + um) + G(dt^2 W mt, u), G(v, w) the
+//                coefficient gradient of v . L(w).  The second differences have
+//                symmetric edge weights, v . D2(a) w = -sum_q sum_{m=1,2}
+//                W_m(q) (v(q+m)-v(q)) (w(q+m)-w(q)), so dG/da is 7 products of
+//                forward differences; the mixed terms give minus products of
+//                centred first differences;
+//   rho        : -W [mt.(up - 2u + um) + b1.(u+ - up)] (the 1/rho factors and
+//                the forcing) - beta dc D2(u - um) . D2(w W b1) (the damping's
 //                rho dc factors).
 // Forward levels come from checkpoints every C steps, recomputed one segment
 // at a time with every level and predicted level kept in HBM.
@@ -58,108 +65,45 @@ __device__ __forceinline__ void grid_point(const Box& b, long long p, int& i, in
    k = b.kb + (int)(p / b.nij);
 }
 
-// y = a * (sx sy sz) / rho on I, 0 elsewhere  (W^-1 R a)
-__global__ void adj_scale_kernel(Box b, Prof f, const double* __restrict__ a,
-                                 const double* __restrict__ rho, double* __restrict__ y)
+// w1 = up - 2u + um
+__global__ void adj_w1_kernel(long long n3, const double* __restrict__ up, const double* __restrict__ u,
+                              const double* __restrict__ um, double* __restrict__ w1)
 {
-   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < b.npts;
-        p += (long long)gridDim.x * blockDim.x) {
-      int i, j, k;
-      grid_point(b, p, i, j, k);
-      const double s = inside(b, i, j, k) ? sxyz(b, f, i, j, k) / rho[p] : 0.0;
-#pragma unroll
-      for (int c = 0; c < 3; c++) y[c * b.npts + p] = s * a[c * b.npts + p];
-   }
+   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n3;
+        q += (long long)gridDim.x * blockDim.x)
+      w1[q] = (up[q] - 2 * u[q]) + um[q];
 }
 
-// s = W lu, m = a1 + dt^2/12 s, y = W^-1 R m  (on I; 0 elsewhere)
-__global__ void adj_mid_kernel(Box b, Prof f, const double* __restrict__ lu,
-                               const double* __restrict__ a1, const double* __restrict__ rho,
-                               double c12, double* __restrict__ s, double* __restrict__ m,
-                               double* __restrict__ y)
+// v1 = c1 W b1, v2 = c2 W mt (W = 1/(sx sy sz); both zero outside I)
+__global__ void adj_v_kernel(Box b, Prof f, const double* __restrict__ b1,
+                             const double* __restrict__ mt, double c1, double c2,
+                             double* __restrict__ v1, double* __restrict__ v2)
 {
    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < b.npts;
         p += (long long)gridDim.x * blockDim.x) {
       int i, j, k;
       grid_point(b, p, i, j, k);
-      const bool in = inside(b, i, j, k);
-      const double iw = in ? sxyz(b, f, i, j, k) : 0.0;
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-         const long long q = c * b.npts + p;
-         const double sv = in ? lu[q] / iw : 0.0;
-         const double mv = in ? a1[q] + c12 * sv : 0.0;
-         s[q] = sv;
-         m[q] = mv;
-         y[q] = in ? mv * iw / rho[p] : 0.0;
-      }
-   }
-}
-
-// a^n = 2m + dt^2 W lu - dt^2/6 s - a2 - beta SG^T R (a1 - a2) on I; 0 elsewhere
-__global__ void adj_final_kernel(Box b, Prof f, const double* __restrict__ lu,
-                                 const double* __restrict__ s, const double* __restrict__ m,
-                                 const double* __restrict__ a1, const double* __restrict__ a2,
-                                 const double* __restrict__ rho, double dt2, double beta,
-                                 double* __restrict__ an)
-{
-   const long long st[3] = {1, b.ni, b.nij};
-   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < b.npts;
-        p += (long long)gridDim.x * blockDim.x) {
-      int i, j, k;
-      grid_point(b, p, i, j, k);
-      if (!inside(b, i, j, k)) {
-#pragma unroll
-         for (int c = 0; c < 3; c++) an[c * b.npts + p] = 0.0;
-         continue;
-      }
       const double w = 1.0 / sxyz(b, f, i, j, k);
-      const int pc[3] = {i, j, k};
-      const int lo[3] = {b.ib, b.jb, b.kb};
 #pragma unroll
       for (int c = 0; c < 3; c++) {
-         const long long q = c * b.npts + p;
-         double sg = 0;
-         if (beta != 0) {
-#pragma unroll
-            for (int ax = 0; ax < 3; ax++) {
-               double v[5];
-#pragma unroll
-               for (int mm = -2; mm <= 2; mm++) {
-                  int qc[3] = {i, j, k};
-                  qc[ax] += mm;
-                  if (!inside(b, qc[0], qc[1], qc[2])) {
-                     v[mm + 2] = 0;
-                     continue;
-                  }
-                  const long long pq = p + mm * st[ax];
-                  const int oi = qc[0] - b.ib, oj = qc[1] - b.jb, ok = qc[2] - b.kb;
-                  const double wax = ax == 0   ? f.st[0][oi] * f.co[1][oj] * f.co[2][ok]
-                                     : ax == 1 ? f.st[1][oj] * f.co[0][oi] * f.co[2][ok]
-                                               : f.st[2][ok] * f.co[0][oi] * f.co[1][oj];
-                  v[mm + 2] = wax * (a1[c * b.npts + pq] - a2[c * b.npts + pq]) / rho[pq];
-               }
-               const double* dc = f.dc[ax] + (pc[ax] - lo[ax]);
-               const double e0 = rho[p - st[ax]] * dc[-1], e1 = rho[p] * dc[0],
-                            e2 = rho[p + st[ax]] * dc[1];
-               sg += e2 * (v[4] - 2 * v[3] + v[2]) - 2 * e1 * (v[3] - 2 * v[2] + v[1]) +
-                     e0 * (v[2] - 2 * v[1] + v[0]);
-            }
-         }
-         an[q] = 2 * m[q] + dt2 * w * lu[q] - dt2 / 6 * s[q] - a2[q] - beta * sg;
+         v1[c * b.npts + p] = c1 * w * b1[c * b.npts + p];
+         v2[c * b.npts + p] = c2 * w * mt[c * b.npts + p];
       }
    }
 }
 
-// an[receiver point] += residual row (receivers in order, 3 values each)
-__global__ void adj_source_kernel(Box b, int nrec, const int* __restrict__ ijk,
-                                  const double* __restrict__ res, double* __restrict__ an)
+// b[receiver point] += W^-1 R res (receivers in order, 3 values each)
+__global__ void adj_source_kernel(Box b, Prof f, int nrec, const int* __restrict__ ijk,
+                                  const double* __restrict__ res, const double* __restrict__ rho,
+                                  double* __restrict__ an)
 {
    const int r = blockIdx.x * blockDim.x + threadIdx.x;
    if (r >= nrec) return;
-   const long long p = pidx(b, ijk[3 * r], ijk[3 * r + 1], ijk[3 * r + 2]);
+   const int i = ijk[3 * r], j = ijk[3 * r + 1], k = ijk[3 * r + 2];
+   const long long p = pidx(b, i, j, k);
+   const double s = sxyz(b, f, i, j, k) / rho[p];
 #pragma unroll
-   for (int c = 0; c < 3; c++) an[c * b.npts + p] += res[3 * r + c];
+   for (int c = 0; c < 3; c++) an[c * b.npts + p] += s * res[3 * r + c];
 }
 
 __device__ constexpr double kDW[5] = {1, -8, 0, 8, -1};
@@ -172,11 +116,11 @@ __device__ constexpr int kMix[12][5] = {{0, 1, 0, 1, 1}, {0, 1, 1, 0, 0}, {0, 2,
 struct GradArgs {
    Box b;
    Prof f;
-   const double *a1, *m, *rho, *u, *um, *up, *un;
+   const double *v1, *v2, *rho, *u, *um, *up, *un, *w1;
    double* gr;
    double* gm;
    double* gl;
-   double c1, c2;  // dt^2/12 and dt^2: v1 = c1 R a1, v2 = c2 R m
+   double c1, c2;  // v1 = c1 W b1 (pair with w1), v2 = c2 W mt (pair with u)
    double ih2, beta;
 };
 
@@ -192,47 +136,48 @@ __global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs g)
       int pc[3];
       grid_point(b, p, pc[0], pc[1], pc[2]);
       double gm = 0, gl = 0, gr = 0;
-      // v of pair t at point q (component c); zero outside I
-      auto vat = [&](int t, int c, long long q) {
-         return (t == 0 ? g.c1 * g.a1[c * n + q] : g.c2 * g.m[c * n + q]) / g.rho[q];
-      };
-      // w of pair t at point q
-      auto wat = [&](int t, int c, long long q) {
-         return t == 0 ? g.up[c * n + q] - 2 * g.u[c * n + q] + g.um[c * n + q] : g.u[c * n + q];
-      };
 #pragma unroll
       for (int t = 0; t < 2; t++) {
-         // same-axis second differences: rows q = p - nn e_ax
+         const double* vb = t == 0 ? g.v1 : g.v2;
+         const double* wf = t == 0 ? g.w1 : g.u;
+         // same-axis second differences in edge form
 #pragma unroll
-         for (int ax = 0; ax < 3; ax++)
+         for (int ax = 0; ax < 3; ax++) {
+            double sv[5];  // s_ax along the axis (0 beyond the array)
+            bool ok[5];
 #pragma unroll
-            for (int nn = -2; nn <= 2; nn++) {
-               int qc[3] = {pc[0], pc[1], pc[2]};
-               qc[ax] -= nn;
-               if (!inside(b, qc[0], qc[1], qc[2])) continue;
-               const long long q = p - nn * st[ax];
-               const double sq = g.f.st[ax][qc[ax] - lo[ax]], sp = g.f.st[ax][pc[ax] - lo[ax]];
+            for (int m = -2; m <= 2; m++) {
+               const int x = pc[ax] + m;
+               ok[m + 2] = x >= lo[ax] && x <= hi[ax];
+               sv[m + 2] = ok[m + 2] ? g.f.st[ax][x - lo[ax]] : 0.0;
+            }
 #pragma unroll
-               for (int c = 0; c < 3; c++) {
-                  const double vq = vat(t, c, q);
-                  double d[5];
+            for (int c = 0; c < 3; c++) {
+               double v[5], w[5];
 #pragma unroll
-                  for (int mm = -2; mm <= 2; mm++) d[mm + 2] = wat(t, c, q + mm * st[ax]) - wat(t, c, q);
-                  double K;
-                  if (nn == -2) K = -0.75 * d[0] + d[1];
-                  else if (nn == -1) K = d[0] + 3 * d[1] + d[3];
-                  else if (nn == 0) K = -0.75 * (d[0] + d[4]) + 3 * (d[1] + d[3]);
-                  else if (nn == 1) K = d[1] + 3 * d[3] + d[4];
-                  else K = d[3] - 0.75 * d[4];
-                  const double fv = g.ih2 / 6 * vq * sq * K * sp;
-                  if (c == ax) {
-                     gm += 2 * fv;
-                     gl += fv;
-                  } else {
-                     gm += fv;
+               for (int m = -2; m <= 2; m++) {
+                  if (!ok[m + 2]) {
+                     v[m + 2] = w[m + 2] = 0;
+                     continue;
                   }
+                  const long long q = c * n + p + m * st[ax];
+                  v[m + 2] = sv[m + 2] * vb[q];
+                  w[m + 2] = wf[q];
+               }
+               const double e1m2 = (v[1] - v[0]) * (w[1] - w[0]), e1m1 = (v[2] - v[1]) * (w[2] - w[1]);
+               const double e10 = (v[3] - v[2]) * (w[3] - w[2]), e1p1 = (v[4] - v[3]) * (w[4] - w[3]);
+               const double e2m2 = (v[2] - v[0]) * (w[2] - w[0]), e2m1 = (v[3] - v[1]) * (w[3] - w[1]);
+               const double e20 = (v[4] - v[2]) * (w[4] - w[2]);
+               const double val = -g.ih2 / 6 * sv[2] *
+                                  (e1p1 + e1m2 + 3 * (e1m1 + e10) + e2m1 - 0.75 * (e20 + e2m2));
+               if (c == ax) {
+                  gm += 2 * val;
+                  gl += val;
+               } else {
+                  gm += val;
                }
             }
+         }
          // mixed terms: -(1/144h^2) s_ai(p) (DW . w_d along ai)(p) (DW . (s_ao v_c) along ao)(p)
 #pragma unroll
          for (int e = 0; e < 12; e++) {
@@ -240,13 +185,13 @@ __global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs g)
             if (pc[ai] < lo[ai] + 2 || pc[ai] > hi[ai] - 2) continue;
             double inner = 0, outer = 0;
 #pragma unroll
-            for (int mm = -2; mm <= 2; mm++) {
-               if (mm == 0) continue;
-               inner += kDW[mm + 2] * wat(t, d, p + mm * st[ai]);
+            for (int m = -2; m <= 2; m++) {
+               if (m == 0) continue;
+               inner += kDW[m + 2] * wf[d * n + p + m * st[ai]];
                int oc[3] = {pc[0], pc[1], pc[2]};
-               oc[ao] += mm;
-               if (oc[ao] < lo[ao] || oc[ao] > hi[ao] || !inside(b, oc[0], oc[1], oc[2])) continue;
-               outer += kDW[mm + 2] * g.f.st[ao][oc[ao] - lo[ao]] * vat(t, c, p + mm * st[ao]);
+               oc[ao] += m;
+               if (oc[ao] < lo[ao] || oc[ao] > hi[ao]) continue;
+               outer += kDW[m + 2] * g.f.st[ao][oc[ao] - lo[ao]] * vb[c * n + p + m * st[ao]];
             }
             const double gg = -g.ih2 / 144 * g.f.st[ai][pc[ai] - lo[ai]] * inner * outer;
             if (kMix[e][4]) gl += gg;
@@ -255,43 +200,42 @@ __global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs g)
       }
       // rho: the 1/rho factors and forcing (interior points), and the damping's rho dc
       if (inside(b, pc[0], pc[1], pc[2])) {
-         double s = 0;
+         // W mt = v2/c2, W b1 = v1/c1
+         double s1 = 0, s2 = 0;
 #pragma unroll
          for (int c = 0; c < 3; c++) {
             const long long q = c * n + p;
-            s += g.m[q] * (g.up[q] - 2 * g.u[q] + g.um[q]) + g.a1[q] * (g.un[q] - g.up[q]);
+            s2 += g.v2[q] * g.w1[q];
+            s1 += g.v1[q] * (g.un[q] - g.up[q]);
          }
-         gr -= s / g.rho[p];
+         gr -= s2 / g.c2 + s1 / g.c1;
       }
       if (g.beta != 0) {
          double sgr = 0;
 #pragma unroll
          for (int ax = 0; ax < 3; ax++) {
             if (pc[ax] - 1 < lo[ax] || pc[ax] + 1 > hi[ax]) continue;
+            const double dcp = g.f.dc[ax][pc[ax] - lo[ax]];
+            if (dcp == 0) continue;  // the term is exactly zero there
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                double vv[3], dd[3];
 #pragma unroll
-               for (int mm = -1; mm <= 1; mm++) {
+               for (int m = -1; m <= 1; m++) {
                   int qc[3] = {pc[0], pc[1], pc[2]};
-                  qc[ax] += mm;
-                  const long long q = p + mm * st[ax];
-                  dd[mm + 1] = g.u[c * n + q] - g.um[c * n + q];
-                  if (inside(b, qc[0], qc[1], qc[2])) {
-                     const int oi = qc[0] - b.ib, oj = qc[1] - b.jb, ok = qc[2] - b.kb;
-                     const double wax = ax == 0   ? g.f.st[0][oi] * g.f.co[1][oj] * g.f.co[2][ok]
-                                        : ax == 1 ? g.f.st[1][oj] * g.f.co[0][oi] * g.f.co[2][ok]
-                                                  : g.f.st[2][ok] * g.f.co[0][oi] * g.f.co[1][oj];
-                     vv[mm + 1] = wax * g.a1[c * n + q] / g.rho[q];
-                  } else {
-                     vv[mm + 1] = 0;
-                  }
+                  qc[ax] += m;
+                  const long long q = p + m * st[ax];
+                  dd[m + 1] = g.u[c * n + q] - g.um[c * n + q];
+                  const int oi = qc[0] - b.ib, oj = qc[1] - b.jb, ok = qc[2] - b.kb;
+                  const double wax = ax == 0   ? g.f.st[0][oi] * g.f.co[1][oj] * g.f.co[2][ok]
+                                     : ax == 1 ? g.f.st[1][oj] * g.f.co[0][oi] * g.f.co[2][ok]
+                                               : g.f.st[2][ok] * g.f.co[0][oi] * g.f.co[1][oj];
+                  vv[m + 1] = wax * g.v1[c * n + q];
                }
-               sgr += g.f.dc[ax][pc[ax] - lo[ax]] * (dd[2] - 2 * dd[1] + dd[0]) *
-                      (vv[2] - 2 * vv[1] + vv[0]);
+               sgr += dcp * (dd[2] - 2 * dd[1] + dd[0]) * (vv[2] - 2 * vv[1] + vv[0]);
             }
          }
-         gr -= g.beta * sgr;
+         gr -= g.beta / g.c1 * sgr;  // vv holds c1 W b1
       }
       g.gm[p] += gm;
       g.gl[p] += gl;
@@ -375,7 +319,6 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       pf.co[a] = dprof_[6 + a];
    }
    const double beta = (prof_.used && g_.sg_damping != 0) ? g_.sg_damping : 0.0;
-   const int onesided[6] = {0, 0, 0, 0, 0, 0};
 
    auto run = [&]() -> int {
       SW4G_TRY(cuda_ok(cudaMemsetAsync(gr_d, 0, npts_ * sizeof(double), stream_)));
@@ -413,18 +356,34 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       *misfit = J;
       SW4G_TRY(cuda_ok(cudaMemcpy(resd, rec.data(), rec.size() * sizeof(double), cudaMemcpyHostToDevice)));
 
-      double* a1 = work;
-      double* a2 = work + n3;
-      double* an = work + 2 * n3;
-      double* s = work + 3 * n3;
-      double* m = work + 4 * n3;
-      double* y = work + 5 * n3;
-      double* lu = work + 6 * n3;
+      double* b1 = work;           // scaled adjoint b = W^-1 R a at n+1
+      double* b2 = work + n3;      // at n+2
+      double* bn = work + 2 * n3;  // at n
+      double* mt = work + 3 * n3;  // b1 + dt^2/12 R L(b1)
+      double* w1 = work + 4 * n3;  // up - 2u + um
+      double* v1 = work + 5 * n3;  // dt^2/12 W b1
+      double* v2 = work + 6 * n3;  // dt^2 W mt
       SW4G_TRY(cuda_ok(cudaMemsetAsync(work, 0, 7 * lv, stream_)));  // not fin
-      // a^N = g^N
-      adj_source_kernel<<<blocks_for(drec_.n, 64), 64, 0, stream_>>>(b, drec_.n, drec_.ijk,
-                                                                     resd + (size_t)nsteps * nval, a1);
+      // b^N = W^-1 R g^N
+      adj_source_kernel<<<blocks_for(drec_.n, 64), 64, 0, stream_>>>(
+          b, pf, drec_.n, drec_.ijk, resd + (size_t)nsteps * nval, rho_, b1);
       SW4G_TRY(launch_status());
+      FusedStage fs;
+      fs.b = b;
+      fs.k1 = 1;
+      fs.k2 = g_.nz;
+      fs.mu = mu_;
+      fs.la = la_;
+      fs.rho = rho_;
+      fs.irho = irho_;
+      fs.w = w_;
+      for (int q = 0; q < 3; q++) {
+         fs.st[q] = dprof_[3 + q];
+         fs.dc[q] = dprof_[q];
+         fs.co[q] = dprof_[6 + q];
+      }
+      fs.h = g_.h;
+      fs.dt = dt;
       const bool keep_rec = drec_.n > 0;
       const int saved_n = drec_.n;
       drec_.n = 0;  // no recording while segments are recomputed
@@ -453,31 +412,34 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
             const double* um = seg + (size_t)(nn - s0) * n3;
             const double* up = pred + (size_t)(nn - s0) * n3;
             const double* un = seg + (size_t)(nn - s0 + 2) * n3;
-            adj_scale_kernel<<<blocks, 256, 0, stream_>>>(b, pf, a1, rho_, y);
+            adj_w1_kernel<<<gs_blocks(n3, 256), 256, 0, stream_>>>(n3, up, u, um, w1);
             status = launch_status();
-            if (status == kOk)
-               status = launch_rhs4sg_direct(1, bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, g_.nz,
-                                             onesided, lu, y, mu_, la_, g_.h, dprof_[3], dprof_[4],
-                                             dprof_[5], stream_);
+            if (status == kOk) {  // mt = b1 + dt^2/12 R L(b1): predictor form, um = u
+               fs.corrector = 0;
+               fs.u = b1;
+               fs.um = b1;
+               fs.up = nullptr;
+               fs.out = mt;
+               fs.beta = 0;
+               fs.coef = dt * dt / 12;
+               status = launch_fused_stage(fs, stream_);
+            }
             if (status == kOk) {
-               adj_mid_kernel<<<blocks, 256, 0, stream_>>>(b, pf, lu, a1, rho_, dt * dt / 12, s, m, y);
+               adj_v_kernel<<<blocks, 256, 0, stream_>>>(b, pf, b1, mt, dt * dt / 12, dt * dt, v1, v2);
                status = launch_status();
             }
-            if (status == kOk)
-               status = launch_rhs4sg_direct(1, bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, g_.nz,
-                                             onesided, lu, y, mu_, la_, g_.h, dprof_[3], dprof_[4],
-                                             dprof_[5], stream_);
             if (status == kOk) {
                GradArgs ga;
                ga.b = b;
                ga.f = pf;
-               ga.a1 = a1;
-               ga.m = m;
+               ga.v1 = v1;
+               ga.v2 = v2;
                ga.rho = rho_;
                ga.u = u;
                ga.um = um;
                ga.up = up;
                ga.un = un;
+               ga.w1 = w1;
                ga.gr = gr_d;
                ga.gm = gm_d;
                ga.gl = gl_d;
@@ -488,21 +450,25 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
                adj_gradient_kernel<<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
                status = launch_status();
             }
-            if (status == kOk) {
-               adj_final_kernel<<<blocks, 256, 0, stream_>>>(b, pf, lu, s, m, a1, a2, rho_, dt * dt,
-                                                             beta, an);
-               status = launch_status();
+            if (status == kOk) {  // b^n = 2 b1 - b2 + dt^2 R L(mt) - beta R SG(b1 - b2)
+               fs.corrector = 2;
+               fs.u = b1;
+               fs.um = b2;
+               fs.up = mt;
+               fs.out = bn;
+               fs.beta = beta;
+               fs.coef = dt * dt;
+               status = launch_fused_stage(fs, stream_);
             }
             if (status == kOk) {
                adj_source_kernel<<<blocks_for(saved_n, 64), 64, 0, stream_>>>(
-                   b, saved_n, drec_.ijk, resd + (size_t)nn * nval, an);
+                   b, pf, saved_n, drec_.ijk, resd + (size_t)nn * nval, rho_, bn);
                status = launch_status();
             }
-            // rotate: a2 <- a1, a1 <- a^nn
-            double* tmp = a2;
-            a2 = a1;
-            a1 = an;
-            an = tmp;
+            double* tmp = b2;
+            b2 = b1;
+            b1 = bn;
+            bn = tmp;
          }
       }
       drec_.n = keep_rec ? saved_n : 0;

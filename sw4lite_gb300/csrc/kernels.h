@@ -19,7 +19,7 @@ struct WeightPtrs {
 struct FusedStage {
    Box b;
    int k1 = 0, k2 = -1;
-   int corrector = 0;
+   int corrector = 0;  // 0 predictor, 1 corrector, 2 adjoint stage (stage_fused.cu)
    int kchunk = 0;  // planes per CTA; 0 picks one
    const double* u = nullptr;
    const double* um = nullptr;
@@ -34,6 +34,7 @@ struct FusedStage {
    const double* dc[3] = {nullptr, nullptr, nullptr};
    const double* co[3] = {nullptr, nullptr, nullptr};
    double h = 1, dt = 0, beta = 0;
+   double coef = 0;  // > 0: the L(.) coefficient instead of dt^2 (dt^2/12 corrector)
 };
 
 struct WeightPtrsDF {

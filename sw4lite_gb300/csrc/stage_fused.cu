@@ -23,6 +23,9 @@
 //    recomputes the inner differences inside every outer term.
 //  * The corrector stage forms (up - 2u + um) and (u - um) while staging the
 //    plane; 1/dt^2 is folded into the update coefficient.
+//  * A third form serves the discrete adjoint (adjoint.cu):
+//      out = 2u - um + coef/rho * L(up) - beta/rho * SG(u - um)
+//    (the stage field read from `up` directly).
 #include <algorithm>
 
 #include "common.cuh"
@@ -66,6 +69,8 @@ __host__ __device__ constexpr int smem_doubles(int corr)
    // V ring (5 planes x 3) + [D ring (3 planes x 3) + RHO plane] + MU, LA planes + GX + GY
    return 15 * PLANE + (corr ? 9 * PLANE + PLANE : 0) + 2 * PLANE + 3 * TY * PX + 3 * PY * TX;
 }
+
+// CORR: 0 predictor, 1 corrector, 2 adjoint stage (see the header)
 
 __device__ __forceinline__ int mod5(int k) { return ((k % 5) + 5) % 5; }
 __device__ __forceinline__ int mod3(int k) { return ((k % 3) + 3) % 3; }
@@ -111,12 +116,15 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
             const long long p = gidx(gi, gj, kk);
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-               if (!CORR) {
+               if (CORR == 0) {
                   v[c] = __ldg(a.u + p + c * npts);
-               } else {
+               } else if (CORR == 1) {
                   const double uu = __ldg(a.u + p + c * npts), uum = __ldg(a.um + p + c * npts);
                   v[c] = (__ldg(a.up + p + c * npts) - 2 * uu) + uum;
                   d[c] = uu - uum;
+               } else {
+                  v[c] = __ldg(a.up + p + c * npts);
+                  d[c] = __ldg(a.u + p + c * npts) - __ldg(a.um + p + c * npts);
                }
             }
          }
@@ -387,7 +395,10 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                const long long q = p + c * npts;
-               a.out[q] = (__ldg(a.up + q) + cr * lu[c]) - birho * sg[c];
+               if (CORR == 1)
+                  a.out[q] = (__ldg(a.up + q) + cr * lu[c]) - birho * sg[c];
+               else
+                  a.out[q] = (2 * __ldg(a.u + q) - __ldg(a.um + q) + cr * lu[c]) - birho * sg[c];
             }
          }
       }
@@ -544,7 +555,7 @@ int launch_fused_stage(const FusedStage& st, cudaStream_t stream)
       a.co[q] = st.co[q];
    }
    a.cof144 = 1.0 / (144 * st.h * st.h);
-   a.coef = st.corrector ? st.dt * st.dt / 12 : st.dt * st.dt;
+   a.coef = st.coef > 0 ? st.coef : (st.corrector ? st.dt * st.dt / 12 : st.dt * st.dt);
    a.beta = st.beta;
    const int ni = b.ie - b.ib - 3, nj = b.je - b.jb - 3, nk = st.k2 - st.k1 + 1;
    const int gx = blocks_for(ni, TX), gy = blocks_for(nj, TY);
@@ -557,22 +568,28 @@ int launch_fused_stage(const FusedStage& st, cudaStream_t stream)
    if (st.kchunk > 0) chunks = (nk + st.kchunk - 1) / st.kchunk;
    a.kchunk = (nk + chunks - 1) / chunks;
    const dim3 grid(gx, gy, (nk + a.kchunk - 1) / a.kchunk), block(TX, TY, 1);
-   const size_t smem = smem_doubles(st.corrector) * sizeof(double);
+   const int form = st.corrector;  // 0, 1 or 2
+   if (form < 0 || form > 2) return kBadArgument;
+   const size_t smem = smem_doubles(form) * sizeof(double);
    // the opt-in shared-memory size is a per-device function attribute
    int dev = 0;
    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return kCudaError;
-   static bool attr_set[2][64] = {};
-   if (!attr_set[st.corrector][dev]) {
-      cudaError_t e = st.corrector
+   static bool attr_set[3][64] = {};
+   if (!attr_set[form][dev]) {
+      cudaError_t e = form == 0
+          ? cudaFuncSetAttribute(fused_stage_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+          : form == 1
           ? cudaFuncSetAttribute(fused_stage_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-          : cudaFuncSetAttribute(fused_stage_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+          : cudaFuncSetAttribute(fused_stage_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return kCudaError;
-      attr_set[st.corrector][dev] = true;
+      attr_set[form][dev] = true;
    }
-   if (st.corrector)
+   if (form == 0)
+      fused_stage_kernel<0><<<grid, block, smem, stream>>>(a);
+   else if (form == 1)
       fused_stage_kernel<1><<<grid, block, smem, stream>>>(a);
    else
-      fused_stage_kernel<0><<<grid, block, smem, stream>>>(a);
+      fused_stage_kernel<2><<<grid, block, smem, stream>>>(a);
    return launch_status();
 }
 

@@ -123,3 +123,30 @@ def test_gradient_rejects_unsupported_set_ups():
     with pytest.raises(sg.Sw4gError):  # record capacity below nsteps + 1
         ew.gradient(4, 2, obs, *g)
     ew.close()
+
+
+def test_torch_autograd_wrapper_matches_finite_differences():
+    import torch
+    from sw4lite_gb300 import autograd as sa
+    c = AdjointCase(shape=(24, 22, 26), nsteps=40)
+    obs_case = AdjointCase(shape=(24, 22, 26), nsteps=40, seed=11)
+    obs = torch.tensor(obs_case.records(oracle_forward(obs_case)[0][1:]), device="cuda")
+    shot = sa.Shot(grid=c.grid, dt=c.dt, nsteps=c.nsteps, checkpoint_every=10, receivers=c.rec,
+                   observed=obs, sources=c.sources)
+    rho, mu, la = [torch.tensor(a, device="cuda", requires_grad=True) for a in c.mat]
+    J = sa.misfit(rho, mu, la, shot)
+    J.backward()
+    shape = (c.nz + 4, c.ny + 4, c.nx + 4)
+    d = [torch.tensor(smooth_random(shape, 80 + q, corr=3.0, amp=0.3).reshape(-1) - 1.0,
+                      device="cuda") * x.detach() for q, x in enumerate((rho, mu, la))]
+    pred = float(sum((x.grad * dx).sum() for x, dx in zip((rho, mu, la), d)))
+    eps = 1e-5
+    base = [x.detach() for x in (rho, mu, la)]
+    Jp = sa.forward_misfit(*[b + eps * dx for b, dx in zip(base, d)], shot)
+    Jm = sa.forward_misfit(*[b - eps * dx for b, dx in zip(base, d)], shot)
+    fd = (Jp - Jm) / (2 * eps)
+    assert abs(fd - pred) <= 1e-6 * abs(pred), (fd, pred)
+    # and the FP64 reference gradient of the oracle
+    _, gr, gm, gl = oracle_gradient(c, obs.cpu().numpy())
+    for x, ref in zip((rho, mu, la), (gr, gm, gl)):
+        assert _rel(x.grad.cpu().numpy(), ref) <= 1e-9
