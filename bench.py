@@ -374,7 +374,7 @@ def _make_topo_ew(sg, cfg, stream):
 def _time_topo(args, sg, torch, stream, world):
     """C3: timed fused steps of both grids; end-to-end through the C ABI with
     both grids' levels in pinned host memory."""
-    cfg = c3_config()
+    cfg = c3_config(args.topo_nx, args.topo_nx, args.topo_nz)
     ew, nc, ncart, dt = _make_topo_ew(sg, cfg, stream)
     nx, ny = cfg["nx"], cfg["ny"]
     pts = nx * ny * (ncart + nc)  # interior points of both grids
@@ -391,8 +391,8 @@ def _time_topo(args, sg, torch, stream, world):
     out = {"value": world * pts / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
            "grids": {"cartesian": [nx, ny, ncart], "curvilinear": [nx, ny, nc]},
            "dt": dt, "gpu_launches": ew.launches_per_step(sg.MODE_FUSED) * args.steps,
-           "workload": "C3 Gaussian-hill topography 384x384x128 h=50, FP64, fused Cartesian "
-                       "stages + curvilinear kernels"}
+           "workload": f"C3 Gaussian-hill topography {nx}x{ny}x{cfg['nz_total']} h=50, FP64, "
+                       "fused Cartesian stages + curvilinear kernels"}
     if not args.no_e2e:
         n0, n1 = 3 * ew.grid_dims(0)[3], 3 * ew.grid_dims(1)[3]
         hb = [torch.zeros(n, dtype=torch.float64, pin_memory=True) for n in (n0, n0, n1, n1)]
@@ -662,6 +662,8 @@ def main():
     ap.add_argument("--no-mixed", action="store_true", help="skip the FP32-mixed form")
     ap.add_argument("--no-topo", action="store_true", help="skip the topography workload")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint workload")
+    ap.add_argument("--topo-nx", type=int, default=384, help="x and y points of the topography workload")
+    ap.add_argument("--topo-nz", type=int, default=128, help="z points of both grids together")
     ap.add_argument("--adj-n", type=int, default=256, help="grid of the adjoint workload")
     ap.add_argument("--adj-steps", type=int, default=200, help="steps of the adjoint workload")
     ap.add_argument("--adj-ckpt", type=int, default=100, help="checkpoint spacing")
