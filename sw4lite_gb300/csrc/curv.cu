@@ -563,6 +563,18 @@ int launch_rhs4sgcurv(const CurvSpec& s, const int onesided[6], double* lu, cuda
    return launch_status();
 }
 
+int launch_rhs4sgcurv_top(const CurvSpec& s, double* lu, cudaStream_t st)
+{
+   SW4G_TRY(upload_curv_tables());
+   if (s.kb > 0 || s.ke < 8) return kBadArgument;
+   const CurvView v = make_view(s);
+   const int ni = s.ie - s.ib - 3, nj = s.je - s.jb - 3;
+   if (ni <= 0 || nj <= 0) return kOk;
+   const dim3 blk(32, 4), g((ni + 31) / 32, (nj + 3) / 4, 6);
+   rhs4sgcurv_kernel<true><<<g, blk, 0, st>>>(v, lu, 1, 6);
+   return launch_status();
+}
+
 int launch_metric(int soa, int ib, int ie, int jb, int je, int kb, int ke, double h, const double* z,
                   double* met, double* jac, int* bad_flag, cudaStream_t st)
 {

@@ -41,6 +41,8 @@ struct CurvGrid {
    double *rho = nullptr, *mu = nullptr, *la = nullptr;
    double* lev[4] = {};
    double *lu = nullptr, *uacc = nullptr, *fzero = nullptr;
+   double* coef = nullptr;  // fused-stage coefficients (curv_stage.cu)
+   CurvCoef cc{};
    bool material = false;
    ~CurvGrid();
 };

@@ -36,6 +36,7 @@ CurvGrid::~CurvGrid()
    f(lu);
    f(uacc);
    f(fzero);
+   f(coef);
 }
 
 namespace {
@@ -128,6 +129,14 @@ int EW::set_material_grid(int grid, const double* rho, const double* mu, const d
    SW4G_TRY(cuda_ok(cudaMemcpyAsync(cv_->rho, rho, bytes, kind, stream_)));
    SW4G_TRY(cuda_ok(cudaMemcpyAsync(cv_->mu, mu, bytes, kind, stream_)));
    SW4G_TRY(cuda_ok(cudaMemcpyAsync(cv_->la, la, bytes, kind, stream_)));
+   if (!cv_->coef)
+      SW4G_TRY(cuda_ok(cudaMalloc(&cv_->coef, curv_coef_doubles(cv_->npts, (long long)(cv_->b.ie - cv_->b.ib + 1) *
+                                                                           (cv_->b.je - cv_->b.jb + 1)) *
+                                                 sizeof(double))));
+   const Bounds& cb = cv_->b;
+   SW4G_TRY(curv_coef_setup(make_box(1, cb.ib, cb.ie, cb.jb, cb.je, cb.kb, cb.ke), cv_->mu, cv_->la,
+                            cv_->rho, cv_->met, cv_->jac, dprof_[3], dprof_[4], cv_->coef, &cv_->cc,
+                            stream_));
    SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
    cv_->material = true;
    return kOk;
@@ -169,14 +178,38 @@ int EW::curvilinear_arrays(double* z, double* met, double* jac, bool on_device) 
    return kOk;
 }
 
+namespace {
+CurvStage curv_stage_args(const CurvGrid& c, double* const dprof[9], double dt, double beta)
+{
+   CurvStage st;
+   st.b = make_box(1, c.b.ib, c.b.ie, c.b.jb, c.b.je, c.b.kb, c.b.ke);
+   st.nz = c.nz;
+   st.cc = c.cc;
+   st.sx = dprof[3];
+   st.sy = dprof[4];
+   st.dcx = dprof[0];
+   st.dcy = dprof[1];
+   st.cox = dprof[6];
+   st.coy = dprof[7];
+   st.dt = dt;
+   st.beta = beta;
+   return st;
+}
+}  // namespace
+
 int EW::curv_pred(int ip)
 {
+   // fused: the stage kernel (rows 7..nz), the top-row kernel (rows 1..6) and the
+   // ghost shell
    CurvGrid& c = *cv_;
-   const Bounds& b = c.b;
-   const int onesided[6] = {0, 0, 0, 0, 1, 0};
-   SW4G_TRY(launch_rhs4sgcurv(curv_spec(c, c.lev[iu_], dprof_[3], dprof_[4]), onesided, c.lu, stream_));
-   return launch_predfort(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, c.lev[ip], c.lev[iu_], c.lev[ium_],
-                          c.lu, c.fzero, c.rho, dt_ * dt_, stream_);
+   CurvStage st = curv_stage_args(c, dprof_, dt_, 0.0);
+   st.corrector = 0;
+   st.u = c.lev[iu_];
+   st.um = c.lev[ium_];
+   st.out = c.lev[ip];
+   st.f = c.lev[iu_];
+   st.fbox = st.b;
+   return launch_curv_stage(st, stream_);
 }
 
 int EW::curv_corr(int ip, int iq)
@@ -184,6 +217,23 @@ int EW::curv_corr(int ip, int iq)
    CurvGrid& c = *cv_;
    const Bounds& b = c.b;
    const double dt = dt_;
+   if (ip != iq) {
+      // fused: the corrector reads level ip and writes level iq; the top rows read
+      // up - 2u + um from a slab of planes kb..8
+      const Box full = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke);
+      SW4G_TRY(launch_uacc_slab(full, b.kb, 8, c.lev[ip], c.lev[iu_], c.lev[ium_], c.uacc, stream_));
+      const double beta = (prof_.used && g_.sg_damping != 0) ? g_.sg_damping : 0.0;
+      CurvStage st = curv_stage_args(c, dprof_, dt, beta);
+      st.corrector = 1;
+      st.up = c.lev[ip];
+      st.u = c.lev[iu_];
+      st.um = c.lev[ium_];
+      st.out = c.lev[iq];
+      st.f = c.uacc;
+      st.fbox = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, 8);
+      return launch_curv_stage(st, stream_);
+   }
+   // phase order (in place): the reference's kernel sequence
    const int onesided[6] = {0, 0, 0, 0, 1, 0};
    double *up = c.lev[ip], *u = c.lev[iu_], *um = c.lev[ium_];
    SW4G_TRY(launch_dpdmtfort(b.ib, b.ie, b.jb, b.je, b.kb, b.ke, up, u, um, c.uacc, 1 / (dt * dt),
@@ -195,7 +245,6 @@ int EW::curv_corr(int ip, int iq)
       SW4G_TRY(launch_addsgd4c(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, up, u, um, c.rho, dprof_[0],
                                dprof_[1], dprof_[3], dprof_[4], c.jac, dprof_[6], dprof_[7],
                                g_.sg_damping, stream_));
-   if (ip != iq) std::swap(c.lev[ip], c.lev[iq]);
    return kOk;
 }
 
@@ -235,7 +284,6 @@ int EW::curv_time_step(double cfl, double* dt)
 
 int EW::curv_launches(int mode) const
 {
-   (void)mode;
    if (!cv_) return 0;
    int bc = 1 /* free surface */ + 1 /* interface copy */;
    for (int s = 0; s < 4; s++) {
@@ -243,9 +291,13 @@ int EW::curv_launches(int mode) const
       if ((t == kDirichlet || t == kSuperGrid || t == kPeriodic) && cv_->bcpts[s] > 0) bc++;
    }
    bc++;  // flat free surface of bcfortsg on the top side
-   const int rhs = 2;  // SBP top rows + interior
    const bool damp = prof_.used && g_.sg_damping != 0;
-   return (rhs + 1) + (1 + rhs + 1 + (damp ? 1 : 0)) + 2 * bc;
+   // predictor (both modes): shell, top rows, stage kernel
+   const int pred = 3;
+   // corrector: fused slab, shell, top rows, stage; phase order dpdm, two operator
+   // kernels, corrfort, damping
+   const int corr = mode == kModeFused ? 4 : 4 + (damp ? 1 : 0);
+   return pred + corr + 2 * bc;
 }
 
 }  // namespace sw4g

@@ -117,6 +117,44 @@ struct CurvSpec {
 };
 
 int launch_rhs4sgcurv(const CurvSpec& s, const int onesided[6], double* lu, cudaStream_t st);
+// only the SBP top rows k = 1..6 of the curvilinear operator
+int launch_rhs4sgcurv_top(const CurvSpec& s, double* lu, cudaStream_t st);
+
+// Time-invariant coefficients of the fused curvilinear stage (curv_stage.cu):
+// 20 second-difference weight arrays, 8 cross-term products, K = sx sy/(J rho),
+// rho J and 1/(rho J).
+struct CurvCoef {
+   double* w[20];
+   double* prod[8];
+   double* K;
+   double* rj;
+   double* irj;
+   double* topw;  // acof-contracted r-r coefficients of the top rows, per column
+};
+long long curv_coef_doubles(long long npts, long long ncol);
+int curv_coef_setup(const Box& b, const double* mu, const double* la, const double* rho,
+                    const double* met, const double* jac, const double* sx, const double* sy,
+                    double* store, CurvCoef* c, cudaStream_t s);
+// One fused curvilinear stage: rows 7..nz, the SBP top rows k = 1..6 and the
+// ghost shell.
+struct CurvStage {
+   Box b;
+   int nz = 0;
+   int corrector = 0;
+   const double* u = nullptr;
+   const double* um = nullptr;
+   const double* up = nullptr;
+   double* out = nullptr;
+   CurvCoef cc{};
+   const double *sx = nullptr, *sy = nullptr, *dcx = nullptr, *dcy = nullptr, *cox = nullptr,
+                *coy = nullptr;
+   // the stage field of the top rows: the grid's u (predictor) or a slab of
+   // up - 2u + um over planes kb..8 (corrector), and its array box
+   const double* f = nullptr;
+   Box fbox;
+   double dt = 0, beta = 0;
+};
+int launch_curv_stage(const CurvStage& st, cudaStream_t s);
 int launch_metric(int soa, int ib, int ie, int jb, int je, int kb, int ke, double h, const double* z,
                   double* met, double* jac, int* bad_flag, cudaStream_t st);
 int launch_gaussian_hill_z(int ib, int ie, int jb, int je, int kb, int ke, int nz, double h,
