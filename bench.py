@@ -329,7 +329,7 @@ def c3_config(nx=384, ny=384, nz_total=128):
                 cfl=1.3)
 
 
-def _make_topo_ew(sg, cfg, stream):
+def _make_topo_ew(sg, cfg, stream, precision=0):
     """The C3 EW object: the curvilinear grid's point count comes from the
     topography (1 + round((zmax - z_avg)/h)); the Cartesian grid takes the rest of
     the nz_total planes (the grids share the interface plane)."""
@@ -343,7 +343,7 @@ def _make_topo_ew(sg, cfg, stream):
     nc = 1 + int(round((cfg["zmax_topo"] - 0.5 * (zs.min() + zs.max())) / h))
     ncart = cfg["nz_total"] - (nc - 1)
     g = sg.grid_desc(nx, ny, ncart, h, bc=(2, 2, 2, 2, sg.INTERFACE, 2), zmin=cfg["zmax_topo"],
-                     sg_gp=cfg["gp"], sg_damping=cfg["damping"])
+                     sg_gp=cfg["gp"], sg_damping=cfg["damping"], precision=precision)
     ew = sg.EW(g, stream=stream, topo=topo)
     assert ew.grid_dims(1)[2] == nc
 
@@ -371,11 +371,13 @@ def _make_topo_ew(sg, cfg, stream):
     return ew, nc, ncart, dt
 
 
-def _time_topo(args, sg, torch, stream, world):
-    """C3: timed fused steps of both grids; end-to-end through the C ABI with
-    both grids' levels in pinned host memory."""
+def _time_topo(args, sg, torch, stream, world, precision=0):
+    """C3: timed fused steps of both grids (FP64, or FP32-mixed: FP32 interior
+    stencils, FP64 SBP top rows, curvilinear free surface and metric
+    coefficients, double-float levels); end-to-end through the C ABI with both
+    grids' levels in pinned host memory."""
     cfg = c3_config(args.topo_nx, args.topo_nx, args.topo_nz)
-    ew, nc, ncart, dt = _make_topo_ew(sg, cfg, stream)
+    ew, nc, ncart, dt = _make_topo_ew(sg, cfg, stream, precision)
     nx, ny = cfg["nx"], cfg["ny"]
     pts = nx * ny * (ncart + nc)  # interior points of both grids
     with torch.cuda.stream(stream):
@@ -391,8 +393,9 @@ def _time_topo(args, sg, torch, stream, world):
     out = {"value": world * pts / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
            "grids": {"cartesian": [nx, ny, ncart], "curvilinear": [nx, ny, nc]},
            "dt": dt, "gpu_launches": ew.launches_per_step(sg.MODE_FUSED) * args.steps,
-           "workload": f"C3 Gaussian-hill topography {nx}x{ny}x{cfg['nz_total']} h=50, FP64, "
-                       "fused Cartesian stages + curvilinear kernels"}
+           "workload": f"C3 Gaussian-hill topography {nx}x{ny}x{cfg['nz_total']} h=50, "
+                       + ("FP64" if precision == 0 else "FP32-mixed") +
+                       ", fused Cartesian and curvilinear stage kernels"}
     if not args.no_e2e:
         n0, n1 = 3 * ew.grid_dims(0)[3], 3 * ew.grid_dims(1)[3]
         hb = [torch.zeros(n, dtype=torch.float64, pin_memory=True) for n in (n0, n0, n1, n1)]
@@ -414,6 +417,35 @@ def _time_topo(args, sg, torch, stream, world):
     ew.close()
     torch.cuda.empty_cache()
     return out
+
+
+def _topo_mixed_error(args, sg, torch, stream, nsteps):
+    """Relative L2 error of the FP32-mixed two-grid run against the FP64 run after
+    nsteps steps from rest (the C3 shot), over both grids' fields."""
+    cfg = c3_config(args.topo_nx, args.topo_nx, args.topo_nz)
+    res = []
+    for prec in (0, 1):
+        ew, nc, ncart, dt = _make_topo_ew(sg, cfg, stream, prec)
+        with torch.cuda.stream(stream):
+            ew.step(nsteps, sg.MODE_FUSED)
+        n0, n1 = 3 * ew.grid_dims(0)[3], 3 * ew.grid_dims(1)[3]
+        u0 = torch.zeros(n0, dtype=torch.float64, device="cuda")
+        u1 = torch.zeros(n1, dtype=torch.float64, device="cuda")
+        ew.get_fields(u0, None)
+        ew.get_fields_grid(1, u1, None)
+        torch.cuda.synchronize()
+        res.append((u0, u1))
+        ew.close()
+    (a0, a1), (b0, b1) = res
+    num = float(torch.sum((b0 - a0) ** 2) + torch.sum((b1 - a1) ** 2))
+    den = float(torch.sum(a0 ** 2) + torch.sum(a1 ** 2))
+    lin = max(float(torch.max(torch.abs(b0 - a0))), float(torch.max(torch.abs(b1 - a1))))
+    amax = max(float(torch.max(torch.abs(a0))), float(torch.max(torch.abs(a1))))
+    del res, a0, a1, b0, b1
+    torch.cuda.empty_cache()
+    return {"steps": nsteps, "l2_rel": (num / den) ** 0.5 if den > 0 else None,
+            "linf_rel": lin / amax if amax > 0 else None,
+            "against": "FP64 two-grid run, both grids' final displacement"}
 
 
 def c4_config(n=256):
@@ -599,6 +631,13 @@ def run_ours(args, rank, world):
         mixed["roofline"]["frac"] = mixed["roofline"]["achieved"] / peak_hbm
 
     topo = None if args.no_topo else _time_topo(args, sg, torch, stream, world)
+    topo_mixed = None
+    if not args.no_topo and not args.no_mixed:
+        topo_mixed = _time_topo(args, sg, torch, stream, world, precision=1)
+        if topo:
+            topo_mixed["speedup_vs_fp64"] = topo["ms_per_step"] / topo_mixed["ms_per_step"]
+        if not args.no_err and args.topo_err_steps > 0:
+            topo_mixed["error"] = _topo_mixed_error(args, sg, torch, stream, args.topo_err_steps)
     adj = None if args.no_adjoint else _time_adjoint(args, sg, torch, stream)
 
     cpu = None
@@ -640,6 +679,7 @@ def run_ours(args, rank, world):
             "cpu_baseline": cpu,
             "mixed": mixed,
             "topography": topo,
+            "topography_mixed": topo_mixed,
             "adjoint": adj,
         }
         print(json.dumps(line), flush=True)
@@ -663,6 +703,8 @@ def main():
     ap.add_argument("--no-topo", action="store_true", help="skip the topography workload")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint workload")
     ap.add_argument("--topo-nx", type=int, default=384, help="x and y points of the topography workload")
+    ap.add_argument("--topo-err-steps", type=int, default=800,
+                    help="steps of the mixed-vs-FP64 error run of the topography workload (0: skip)")
     ap.add_argument("--topo-nz", type=int, default=128, help="z points of both grids together")
     ap.add_argument("--adj-n", type=int, default=256, help="grid of the adjoint workload")
     ap.add_argument("--adj-steps", type=int, default=200, help="steps of the adjoint workload")

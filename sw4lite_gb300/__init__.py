@@ -9,6 +9,7 @@ runs on the GPU, and loading fails loudly when the library is missing.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 import os
 from pathlib import Path
@@ -229,6 +230,25 @@ class EW:
         self.npts = lib().sw4g_ew_npts(h)
         self.shape = (grid.nz + 4, grid.ny + 4, grid.nx + 4)
 
+    @contextlib.contextmanager
+    def _ordered(self, *arrays):
+        """Stream order around a call that takes or fills device tensors: the
+        library's stream waits for torch's current stream before the call, and
+        torch's current stream waits for the library's stream after it (the rule
+        torch applies between its own streams)."""
+        if not any(getattr(a, "is_cuda", False) for a in arrays if a is not None):
+            yield
+            return
+        import torch
+        cur = torch.cuda.current_stream()
+        own = torch.cuda.ExternalStream(self._stream) if self._stream else torch.cuda.default_stream()
+        if own.cuda_stream == cur.cuda_stream:
+            yield
+            return
+        own.wait_stream(cur)
+        yield
+        cur.wait_stream(own)
+
     def close(self):
         if getattr(self, "_h", None):
             lib().sw4g_ew_destroy(self._h)
@@ -242,8 +262,9 @@ class EW:
 
     def set_material(self, rho, mu, la):
         on_dev = int(hasattr(rho, "is_cuda") and rho.is_cuda)
-        check(lib().sw4g_ew_set_material(self._h, _ptr(rho), _ptr(mu), _ptr(la), on_dev),
-              "set_material")
+        with self._ordered(rho, mu, la):
+            check(lib().sw4g_ew_set_material(self._h, _ptr(rho), _ptr(mu), _ptr(la), on_dev),
+                  "set_material")
 
     def add_source(self, src: SourceDesc):
         check(lib().sw4g_ew_add_source(self._h, C.byref(src)), "add_source")
@@ -280,12 +301,14 @@ class EW:
 
     def set_fields(self, u, um):
         on_dev = int(hasattr(u, "is_cuda") and u.is_cuda)
-        check(lib().sw4g_ew_set_fields(self._h, _ptr(u), _ptr(um), on_dev), "set_fields")
+        with self._ordered(u, um):
+            check(lib().sw4g_ew_set_fields(self._h, _ptr(u), _ptr(um), on_dev), "set_fields")
 
     def get_fields(self, u, um):
         on_dev = int(hasattr(u, "is_cuda") and u.is_cuda)
-        check(lib().sw4g_ew_get_fields(self._h, _ptr(u), _ptr(um) if um is not None else None,
-                                       on_dev), "get_fields")
+        with self._ordered(u, um):
+            check(lib().sw4g_ew_get_fields(self._h, _ptr(u), _ptr(um) if um is not None else None,
+                                           on_dev), "get_fields")
 
     def field_ptr(self, which=0) -> int:
         return lib().sw4g_ew_field(self._h, which)
@@ -294,7 +317,8 @@ class EW:
         check(lib().sw4g_ew_step(self._h, nsteps, mode), "step")
 
     def enforce_bc(self, u):
-        check(lib().sw4g_ew_enforce_bc(self._h, _ptr(u)), "enforce_bc")
+        with self._ordered(u):
+            check(lib().sw4g_ew_enforce_bc(self._h, _ptr(u)), "enforce_bc")
 
     def gradient(self, nsteps, checkpoint_every, observed, g_rho, g_mu, g_la):
         """Misfit of the receiver records against `observed` ((nsteps+1) x nvals) over
@@ -304,9 +328,10 @@ class EW:
         J = C.c_double()
         od = int(hasattr(observed, "is_cuda") and observed.is_cuda)
         gd = int(hasattr(g_rho, "is_cuda") and g_rho.is_cuda)
-        check(lib().sw4g_ew_gradient(self._h, nsteps, checkpoint_every, _ptr(observed), od,
-                                     C.byref(J), _ptr(g_rho), _ptr(g_mu), _ptr(g_la), gd),
-              "gradient")
+        with self._ordered(observed, g_rho, g_mu, g_la):
+            check(lib().sw4g_ew_gradient(self._h, nsteps, checkpoint_every, _ptr(observed), od,
+                                         C.byref(J), _ptr(g_rho), _ptr(g_mu), _ptr(g_la), gd),
+                  "gradient")
         return J.value
 
     @property
@@ -322,26 +347,30 @@ class EW:
 
     def set_material_grid(self, grid, rho, mu, la):
         on_dev = int(hasattr(rho, "is_cuda") and rho.is_cuda)
-        check(lib().sw4g_ew_set_material_grid(self._h, grid, _ptr(rho), _ptr(mu), _ptr(la), on_dev),
-              "set_material_grid")
+        with self._ordered(rho, mu, la):
+            check(lib().sw4g_ew_set_material_grid(self._h, grid, _ptr(rho), _ptr(mu), _ptr(la),
+                                                  on_dev), "set_material_grid")
 
     def set_fields_grid(self, grid, u, um):
         on_dev = int(hasattr(u, "is_cuda") and u.is_cuda)
-        check(lib().sw4g_ew_set_fields_grid(self._h, grid, _ptr(u), _ptr(um), on_dev),
-              "set_fields_grid")
+        with self._ordered(u, um):
+            check(lib().sw4g_ew_set_fields_grid(self._h, grid, _ptr(u), _ptr(um), on_dev),
+                  "set_fields_grid")
 
     def get_fields_grid(self, grid, u, um=None):
         on_dev = int(hasattr(u, "is_cuda") and u.is_cuda)
-        check(lib().sw4g_ew_get_fields_grid(self._h, grid, _ptr(u),
-                                            _ptr(um) if um is not None else None, on_dev),
-              "get_fields_grid")
+        with self._ordered(u, um):
+            check(lib().sw4g_ew_get_fields_grid(self._h, grid, _ptr(u),
+                                                _ptr(um) if um is not None else None, on_dev),
+                  "get_fields_grid")
 
     def curvilinear_arrays(self, z=None, met=None, jac=None):
         ref = next(a for a in (z, met, jac) if a is not None)
         on_dev = int(hasattr(ref, "is_cuda") and ref.is_cuda)
         p = lambda a: _ptr(a) if a is not None else None
-        check(lib().sw4g_ew_curvilinear_arrays(self._h, p(z), p(met), p(jac), on_dev),
-              "curvilinear_arrays")
+        with self._ordered(z, met, jac):
+            check(lib().sw4g_ew_curvilinear_arrays(self._h, p(z), p(met), p(jac), on_dev),
+                  "curvilinear_arrays")
 
     def set_receivers(self, ijk, modes, capacity):
         """Receivers at 1-based grid points ijk (n x 3) with record modes (REC_*);
@@ -368,7 +397,8 @@ class EW:
             import numpy as np
             out = np.zeros((rows, nvals))
         on_dev = int(hasattr(out, "is_cuda") and out.is_cuda)
-        check(lib().sw4g_ew_get_records(self._h, _ptr(out), on_dev), "get_records")
+        with self._ordered(out):
+            check(lib().sw4g_ew_get_records(self._h, _ptr(out), on_dev), "get_records")
         return out
 
     def launches_per_step(self, mode=MODE_FUSED) -> int:

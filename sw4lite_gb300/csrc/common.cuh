@@ -48,6 +48,11 @@ struct F64Field {
    double* p;
    __device__ __forceinline__ double get(long long q) const { return p[q]; }
    __device__ __forceinline__ void set(long long q, double v) const { p[q] = v; }
+   __device__ __forceinline__ static void copy(const F64Field& d, long long qd, const F64Field& s,
+                                               long long qs)
+   {
+      d.p[qd] = s.p[qs];
+   }
 };
 
 struct DFField {
@@ -62,6 +67,12 @@ struct DFField {
       const float a = __double2float_rn(v);
       h[q] = a;
       h[q + lo] = __double2float_rn(v - (double)a);
+   }
+   __device__ __forceinline__ static void copy(const DFField& d, long long qd, const DFField& s,
+                                               long long qs)
+   {
+      d.h[qd] = s.h[qs];
+      d.h[qd + d.lo] = s.h[qs + s.lo];
    }
 };
 

@@ -353,10 +353,12 @@ __global__ void hill_kernel(Box b, int nz, double h, double zmax, double izb, in
 }
 
 // Free-surface ghost plane; one thread per (i,j)
+template <class Field>
 __global__ void freesurf_curv_kernel(CurvView a, int k, int kl, double s0, double s1, double s2,
                                      double s3, double s4, const double* __restrict__ forcing,
-                                     double* __restrict__ u)
+                                     Field u)
 {
+   auto U = [&](int c, int ii, int jj, int kk) { return u.get(c * a.b.cs + a.b.ps * a.p(ii, jj, kk)); };
    const int i = a.b.ib + 2 + blockIdx.x * blockDim.x + threadIdx.x;
    const int j = a.b.jb + 2 + blockIdx.y * blockDim.y + threadIdx.y;
    if (i > a.b.ie - 2 || j > a.b.je - 2) return;
@@ -380,7 +382,7 @@ __global__ void freesurf_curv_kernel(CurvView a, int k, int kl, double s0, doubl
             for (int m = -2; m <= 2; m++) {
                int i2 = i, j2 = j, k2 = k;
                step_axis(ai, m, i2, j2, k2);
-               f[m + 2] = a.U(x.comp, i2, j2, k2);
+               f[m + 2] = U(x.comp, i2, j2, k2);
             }
             g += a.coef(x.kind, i, j, k) * scl[x.scale] * (kC2 * (f[4] - f[0]) + kC1 * (f[3] - f[1]));
          }
@@ -402,8 +404,8 @@ __global__ void freesurf_curv_kernel(CurvView a, int k, int kl, double s0, doubl
    for (int c = 0; c < 3; c++) {
       double s = 0;
 #pragma unroll
-      for (int w = 0; w < 4; w++) s += sb[w] * a.U(c, i, j, k + w * kl);
-      u[c * a.b.cs + a.b.ps * a.p(i, j, k - kl)] = -(1 / s0) * (s + bc * rhs[c] - dc * nrm[c]);
+      for (int w = 0; w < 4; w++) s += sb[w] * U(c, i, j, k + w * kl);
+      u.set(c * a.b.cs + a.b.ps * a.p(i, j, k - kl), -(1 / s0) * (s + bc * rhs[c] - dc * nrm[c]));
    }
 }
 
@@ -497,8 +499,9 @@ __global__ void curv_eig_kernel(long long n, long long mcs, long long mps,
 // enforceCartTopo (src/EW.C:3504-3530) with 2 ghost points: Cartesian k = -1, 0
 // from curvilinear k = nzc-2, nzc-1, and curvilinear k = nzc..nzc+2 from Cartesian
 // k = 1..3, over the shared i, j range; one thread per (i, j).
-__global__ void cart_topo_kernel(Box bc, Box bv, int nzc, double* __restrict__ uc,
-                                 double* __restrict__ uv)
+// The double-float form copies hi and lo (Field::copy).
+template <class Field>
+__global__ void cart_topo_kernel(Box bc, Box bv, int nzc, Field uc, Field uv)
 {
    const int i = bc.ib + blockIdx.x * blockDim.x + threadIdx.x;
    const int j = bc.jb + blockIdx.y * blockDim.y + threadIdx.y;
@@ -507,10 +510,10 @@ __global__ void cart_topo_kernel(Box bc, Box bv, int nzc, double* __restrict__ u
    for (int c = 0; c < 3; c++) {
 #pragma unroll
       for (int q = 0; q < 2; q++)
-         uc[c * bc.cs + pidx(bc, i, j, bc.kb + q)] = uv[c * bv.cs + pidx(bv, i, j, nzc - 2 + q)];
+         Field::copy(uc, c * bc.cs + pidx(bc, i, j, bc.kb + q), uv, c * bv.cs + pidx(bv, i, j, nzc - 2 + q));
 #pragma unroll
       for (int q = 0; q <= 2; q++)
-         uv[c * bv.cs + pidx(bv, i, j, bv.ke - q)] = uc[c * bc.cs + pidx(bc, i, j, bc.kb + 4 - q)];
+         Field::copy(uv, c * bv.cs + pidx(bv, i, j, bv.ke - q), uc, c * bc.cs + pidx(bc, i, j, bc.kb + 4 - q));
    }
 }
 
@@ -607,7 +610,22 @@ int launch_freesurfcurvisg(const CurvSpec& s, int nz, int side, const double* sb
    if (ni <= 0 || nj <= 0) return kOk;
    const dim3 blk(32, 4), g((ni + 31) / 32, (nj + 3) / 4);
    freesurf_curv_kernel<<<g, blk, 0, st>>>(v, k, kl, sbop[0], sbop[1], sbop[2], sbop[3], sbop[4],
-                                           forcing, u);
+                                           forcing, F64Field{u});
+   return launch_status();
+}
+
+int launch_freesurfcurvisg_df(const CurvSpec& s, int nz, int side, const double* sbop, float* uh,
+                              cudaStream_t st)
+{
+   if (side != 5 && side != 6) return kBadArgument;
+   if (!s.soa) return kNotSupported;
+   CurvView v = make_view(s);
+   const int k = side == 5 ? 1 : nz, kl = side == 5 ? 1 : -1;
+   const int ni = s.ie - s.ib - 3, nj = s.je - s.jb - 3;
+   if (ni <= 0 || nj <= 0) return kOk;
+   const dim3 blk(32, 4), g((ni + 31) / 32, (nj + 3) / 4);
+   freesurf_curv_kernel<<<g, blk, 0, st>>>(v, k, kl, sbop[0], sbop[1], sbop[2], sbop[3], sbop[4],
+                                           nullptr, DFField{uh, 3 * v.b.npts});
    return launch_status();
 }
 
@@ -629,7 +647,16 @@ int launch_cart_topo(const Box& cart, const Box& curv, int nzc, double* ucart, d
                      cudaStream_t st)
 {
    const dim3 blk(32, 4), g((cart.ie - cart.ib + 32) / 32, (cart.je - cart.jb + 4) / 4);
-   cart_topo_kernel<<<g, blk, 0, st>>>(cart, curv, nzc, ucart, ucurv);
+   cart_topo_kernel<<<g, blk, 0, st>>>(cart, curv, nzc, F64Field{ucart}, F64Field{ucurv});
+   return launch_status();
+}
+
+int launch_cart_topo_df(const Box& cart, const Box& curv, int nzc, float* ucart, float* ucurv,
+                        cudaStream_t st)
+{
+   const dim3 blk(32, 4), g((cart.ie - cart.ib + 32) / 32, (cart.je - cart.jb + 4) / 4);
+   cart_topo_kernel<<<g, blk, 0, st>>>(cart, curv, nzc, DFField{ucart, 3 * cart.npts},
+                                       DFField{ucurv, 3 * curv.npts});
    return launch_status();
 }
 

@@ -475,14 +475,28 @@ __global__ void curv_topw_kernel(Box b, const double* __restrict__ mu, const dou
    }
 }
 
+// Read-only views of a 3-component field: FP64, or a double-float level (hi at
+// q, lo at q + lo) read as hi + lo in FP64.
+struct RdF64 {
+   const double* __restrict__ p;
+   __device__ __forceinline__ double get(long long q) const { return __ldg(p + q); }
+};
+struct RdDF {
+   const float* __restrict__ h;
+   long long lo;
+   __device__ __forceinline__ double get(long long q) const
+   {
+      return (double)__ldg(h + q) + (double)__ldg(h + q + lo);
+   }
+};
+
+template <class RD, class WR, class SF>
 struct TopArgs {
    Box b;   // the grid
    Box fb;  // the stage field's array (the grid, or a slab of planes kb..8)
-   const double* __restrict__ f;
-   const double* __restrict__ u;
-   const double* __restrict__ um;
-   const double* __restrict__ up;
-   double* __restrict__ out;
+   SF f;
+   RD u, um, up;
+   WR out;
    CurvCoef cc;
    const double* __restrict__ topw;
    const double *sx, *sy, *dcx, *dcy, *cox, *coy;
@@ -491,8 +505,9 @@ struct TopArgs {
 
 // Rows k = 1..6 under the SBP top: the one-sided operator from precomputed
 // coefficients, with the stage update (and the corrector's x/y damping) fused.
-template <int CORR>
-__global__ void __launch_bounds__(128) curv_top_kernel(TopArgs a)
+// FP64 throughout; the levels are FP64 or double-float (RD, WR).
+template <int CORR, class RD, class WR, class SF>
+__global__ void __launch_bounds__(128) curv_top_kernel(TopArgs<RD, WR, SF> a)
 {
    const Box& b = a.b;
    const Box& fb = a.fb;
@@ -502,9 +517,7 @@ __global__ void __launch_bounds__(128) curv_top_kernel(TopArgs a)
    if (i > b.ie - 2 || j > b.je - 2) return;
    const long long n = b.npts, ncol = b.nij;
    const long long p = pidx(b, i, j, k), col = pidx(b, i, j, b.kb);
-   auto F = [&](int c, int ii, int jj, int kk) {
-      return __ldg(a.f + c * fb.npts + pidx(fb, ii, jj, kk));
-   };
+   auto F = [&](int c, int ii, int jj, int kk) { return a.f.get(c * fb.npts + pidx(fb, ii, jj, kk)); };
    auto Pr = [&](int t, long long q) { return __ldg(a.cc.prod[t] + q); };
    const double sxc = __ldg(a.sx + (i - b.ib)), syc = __ldg(a.sy + (j - b.jb));
    const double istrx = 1 / sxc, istry = 1 / syc;
@@ -636,7 +649,7 @@ __global__ void __launch_bounds__(128) curv_top_kernel(TopArgs a)
 #pragma unroll
       for (int c = 0; c < 3; c++) {
          const long long q = p + c * n;
-         a.out[q] = 2 * a.u[q] - a.um[q] + kk * s3[c];
+         a.out.set(q, 2 * a.u.get(q) - a.um.get(q) + kk * s3[c]);
       }
    } else {
       double sg[3] = {0, 0, 0};
@@ -655,7 +668,7 @@ __global__ void __launch_bounds__(128) curv_top_kernel(TopArgs a)
                const long long q = p + c * n;
                double d[5];
 #pragma unroll
-               for (int m = -2; m <= 2; m++) d[m + 2] = a.u[q + m * s] - a.um[q + m * s];
+               for (int m = -2; m <= 2; m++) d[m + 2] = a.u.get(q + m * s) - a.um.get(q + m * s);
                sg[c] += w[ax] * (e2 * (d[4] - 2 * d[3] + d[2]) - 2 * e1 * (d[3] - 2 * d[2] + d[1]) +
                                  e0 * (d[2] - 2 * d[1] + d[0]));
             }
@@ -665,9 +678,37 @@ __global__ void __launch_bounds__(128) curv_top_kernel(TopArgs a)
 #pragma unroll
       for (int c = 0; c < 3; c++) {
          const long long q = p + c * n;
-         a.out[q] = (a.up[q] + kk * s3[c]) - birj * sg[c];
+         a.out.set(q, (a.up.get(q) + kk * s3[c]) - birj * sg[c]);
       }
    }
+}
+
+template <int CORR, class RD, class WR, class SF, class ST>
+int launch_top(const ST& st, RD u, RD um, RD up, WR out, SF f, cudaStream_t s)
+{
+   const Box& b = st.b;
+   TopArgs<RD, WR, SF> t;
+   t.b = b;
+   t.fb = st.fbox;
+   t.f = f;
+   t.u = u;
+   t.um = um;
+   t.up = up;
+   t.out = out;
+   t.cc = st.cc;
+   t.topw = st.cc.topw;
+   t.sx = st.sx;
+   t.sy = st.sy;
+   t.dcx = st.dcx;
+   t.dcy = st.dcy;
+   t.cox = st.cox;
+   t.coy = st.coy;
+   t.coef = CORR ? st.dt * st.dt / 12 : st.dt * st.dt;
+   t.beta = st.beta;
+   const int ni = b.ie - b.ib - 3, nj = b.je - b.jb - 3;
+   const dim3 blk(32, 4), g((ni + 31) / 32, (nj + 3) / 4, 6);
+   curv_top_kernel<CORR><<<g, blk, 0, s>>>(t);
+   return launch_status();
 }
 
 int gsb(long long n)
@@ -702,6 +743,18 @@ int curv_coef_setup(const Box& b, const double* mu, const double* la, const doub
    return launch_status();
 }
 
+int launch_curv_top_df(const CurvStageDF& st, cudaStream_t s)
+{
+   const long long lo = 3 * st.b.npts;
+   if (st.corrector)
+      return launch_top<1>(st, RdDF{st.u, lo}, RdDF{st.um, lo}, RdDF{st.up, lo}, DFField{st.out, lo},
+                           RdF64{st.f}, s);
+   CurvStageDF p = st;
+   p.fbox = st.b;
+   return launch_top<0>(p, RdDF{st.u, lo}, RdDF{st.um, lo}, RdDF{nullptr, lo}, DFField{st.out, lo},
+                        RdDF{st.u, lo}, s);
+}
+
 int launch_curv_stage(const CurvStage& st, cudaStream_t s)
 {
    const Box& b = st.b;
@@ -726,31 +779,10 @@ int launch_curv_stage(const CurvStage& st, cudaStream_t s)
    else curv_shell_kernel<0><<<gsb(b.npts), 256, 0, s>>>(b, st.nz, st.u, st.um, st.up, st.out);
    SW4G_TRY(launch_status());
    // the SBP top rows k = 1..6
-   {
-      TopArgs t;
-      t.b = b;
-      t.fb = st.fbox;
-      t.f = st.f;
-      t.u = st.u;
-      t.um = st.um;
-      t.up = st.up;
-      t.out = st.out;
-      t.cc = st.cc;
-      t.topw = st.cc.topw;
-      t.sx = st.sx;
-      t.sy = st.sy;
-      t.dcx = st.dcx;
-      t.dcy = st.dcy;
-      t.cox = st.cox;
-      t.coy = st.coy;
-      t.coef = a.coef;
-      t.beta = st.beta;
-      const int ni = b.ie - b.ib - 3, nj = b.je - b.jb - 3;
-      const dim3 blk(32, 4), g((ni + 31) / 32, (nj + 3) / 4, 6);
-      if (corr) curv_top_kernel<1><<<g, blk, 0, s>>>(t);
-      else curv_top_kernel<0><<<g, blk, 0, s>>>(t);
-      SW4G_TRY(launch_status());
-   }
+   if (corr)
+      SW4G_TRY(launch_top<1>(st, RdF64{st.u}, RdF64{st.um}, RdF64{st.up}, F64Field{st.out}, RdF64{st.f}, s));
+   else
+      SW4G_TRY(launch_top<0>(st, RdF64{st.u}, RdF64{st.um}, RdF64{nullptr}, F64Field{st.out}, RdF64{st.f}, s));
    a.coef = corr ? st.dt * st.dt / 12 : st.dt * st.dt;
    a.k1 = 7;
    a.k2 = st.nz;

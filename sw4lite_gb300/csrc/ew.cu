@@ -60,7 +60,7 @@ int EW::init()
       if (!(t == kStressFree || t == kDirichlet || t == kSuperGrid || t == kPeriodic)) return kBadArgument;
       if (t == kStressFree && s < 4) return kNotSupported;
    }
-   if (cv_ && (g_.precision != 0 || g_.sg_order != 4)) return kNotSupported;
+   if (cv_ && g_.sg_order != 4) return kNotSupported;
    if (g_.sg_order != 4 && g_.sg_order != 6) return kBadArgument;
    if (g_.precision != 0 && g_.precision != 1) return kBadArgument;
    mixed_ = g_.precision == 1;

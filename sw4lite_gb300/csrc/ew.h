@@ -43,6 +43,8 @@ struct CurvGrid {
    double *lu = nullptr, *uacc = nullptr, *fzero = nullptr;
    double* coef = nullptr;  // fused-stage coefficients (curv_stage.cu)
    CurvCoef cc{};
+   float* coefdf = nullptr;  // the mixed form's (hi, lo) coefficients (curv_mixed.cu)
+   CurvCoefDF cd{};
    bool material = false;
    ~CurvGrid();
 };

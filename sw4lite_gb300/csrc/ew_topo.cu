@@ -37,6 +37,7 @@ CurvGrid::~CurvGrid()
    f(uacc);
    f(fzero);
    f(coef);
+   f(coefdf);
 }
 
 namespace {
@@ -137,6 +138,11 @@ int EW::set_material_grid(int grid, const double* rho, const double* mu, const d
    SW4G_TRY(curv_coef_setup(make_box(1, cb.ib, cb.ie, cb.jb, cb.je, cb.kb, cb.ke), cv_->mu, cv_->la,
                             cv_->rho, cv_->met, cv_->jac, dprof_[3], dprof_[4], cv_->coef, &cv_->cc,
                             stream_));
+   if (mixed_) {
+      if (!cv_->coefdf)
+         SW4G_TRY(cuda_ok(cudaMalloc(&cv_->coefdf, curv_coef_df_floats(cv_->npts) * sizeof(float))));
+      SW4G_TRY(curv_coef_df_setup(cv_->npts, cv_->cc, cv_->coefdf, &cv_->cd, stream_));
+   }
    SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
    cv_->material = true;
    return kOk;
@@ -148,8 +154,20 @@ int EW::set_fields_grid(int grid, const double* u, const double* um, bool on_dev
    if (grid != 1 || !cv_ || !ready_ || !u || !um) return kBadArgument;
    const size_t bytes = 3 * (size_t)cv_->npts * sizeof(double);
    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-   SW4G_TRY(cuda_ok(cudaMemcpyAsync(cv_->lev[iu_], u, bytes, kind, stream_)));
-   SW4G_TRY(cuda_ok(cudaMemcpyAsync(cv_->lev[ium_], um, bytes, kind, stream_)));
+   if (!mixed_) {
+      SW4G_TRY(cuda_ok(cudaMemcpyAsync(cv_->lev[iu_], u, bytes, kind, stream_)));
+      SW4G_TRY(cuda_ok(cudaMemcpyAsync(cv_->lev[ium_], um, bytes, kind, stream_)));
+   } else {
+      // through the FP64 work array uacc, then split into (hi, lo)
+      const long long n3 = 3 * cv_->npts;
+      const double* src[2] = {u, um};
+      const int dst[2] = {iu_, ium_};
+      for (int q = 0; q < 2; q++) {
+         SW4G_TRY(cuda_ok(cudaMemcpyAsync(cv_->uacc, src[q], bytes, kind, stream_)));
+         float* h = reinterpret_cast<float*>(cv_->lev[dst[q]]);
+         SW4G_TRY(launch_df_from_f64(n3, cv_->uacc, h, h + n3, stream_));
+      }
+   }
    if (!on_device) SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
    return kOk;
 }
@@ -160,8 +178,21 @@ int EW::get_fields_grid(int grid, double* u, double* um, bool on_device) const
    if (grid != 1 || !cv_ || !ready_) return kBadArgument;
    const size_t bytes = 3 * (size_t)cv_->npts * sizeof(double);
    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-   if (u) SW4G_TRY(cuda_ok(cudaMemcpyAsync(u, cv_->lev[iu_], bytes, kind, stream_)));
-   if (um) SW4G_TRY(cuda_ok(cudaMemcpyAsync(um, cv_->lev[ium_], bytes, kind, stream_)));
+   if (!mixed_) {
+      if (u) SW4G_TRY(cuda_ok(cudaMemcpyAsync(u, cv_->lev[iu_], bytes, kind, stream_)));
+      if (um) SW4G_TRY(cuda_ok(cudaMemcpyAsync(um, cv_->lev[ium_], bytes, kind, stream_)));
+   } else {
+      // (hi, lo) -> FP64 in the work array uacc, then out
+      const long long n3 = 3 * cv_->npts;
+      double* dst[2] = {u, um};
+      const int src[2] = {iu_, ium_};
+      for (int q = 0; q < 2; q++) {
+         if (!dst[q]) continue;
+         const float* h = reinterpret_cast<const float*>(cv_->lev[src[q]]);
+         SW4G_TRY(launch_df_to_f64(n3, h, h + n3, cv_->uacc, stream_));
+         SW4G_TRY(cuda_ok(cudaMemcpyAsync(dst[q], cv_->uacc, bytes, kind, stream_)));
+      }
+   }
    if (!on_device) SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
    return kOk;
 }
@@ -195,10 +226,45 @@ CurvStage curv_stage_args(const CurvGrid& c, double* const dprof[9], double dt, 
    st.beta = beta;
    return st;
 }
+CurvStageDF curv_stage_args_df(const CurvGrid& c, double* const dprof[9], float* const prof32[9],
+                               double dt, double beta)
+{
+   CurvStageDF st;
+   st.b = make_box(1, c.b.ib, c.b.ie, c.b.jb, c.b.je, c.b.kb, c.b.ke);
+   st.nz = c.nz;
+   st.cc = c.cc;
+   st.cd = c.cd;
+   st.sx = dprof[3];
+   st.sy = dprof[4];
+   st.dcx = dprof[0];
+   st.dcy = dprof[1];
+   st.cox = dprof[6];
+   st.coy = dprof[7];
+   st.sx32 = prof32[3];
+   st.sy32 = prof32[4];
+   st.dcx32 = prof32[0];
+   st.dcy32 = prof32[1];
+   st.cox32 = prof32[6];
+   st.coy32 = prof32[7];
+   st.dt = dt;
+   st.beta = beta;
+   return st;
+}
+
+float* df(double* p) { return reinterpret_cast<float*>(p); }
 }  // namespace
 
 int EW::curv_pred(int ip)
 {
+   if (mixed_) {
+      CurvGrid& c = *cv_;
+      CurvStageDF st = curv_stage_args_df(c, dprof_, prof32_, dt_, 0.0);
+      st.corrector = 0;
+      st.u = df(c.lev[iu_]);
+      st.um = df(c.lev[ium_]);
+      st.out = df(c.lev[ip]);
+      return launch_curv_stage_df(st, stream_);
+   }
    // fused: the stage kernel (rows 7..nz), the top-row kernel (rows 1..6) and the
    // ghost shell
    CurvGrid& c = *cv_;
@@ -217,6 +283,22 @@ int EW::curv_corr(int ip, int iq)
    CurvGrid& c = *cv_;
    const Bounds& b = c.b;
    const double dt = dt_;
+   if (mixed_) {
+      if (ip == iq) return kNotSupported;
+      const Box full = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke);
+      SW4G_TRY(launch_uacc_slab_df(full, b.kb, 8, df(c.lev[ip]), df(c.lev[iu_]), df(c.lev[ium_]), c.uacc,
+                                   stream_));
+      const double beta = (prof_.used && g_.sg_damping != 0) ? g_.sg_damping : 0.0;
+      CurvStageDF st = curv_stage_args_df(c, dprof_, prof32_, dt, beta);
+      st.corrector = 1;
+      st.up = df(c.lev[ip]);
+      st.u = df(c.lev[iu_]);
+      st.um = df(c.lev[ium_]);
+      st.out = df(c.lev[iq]);
+      st.f = c.uacc;
+      st.fbox = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, 8);
+      return launch_curv_stage_df(st, stream_);
+   }
    if (ip != iq) {
       // fused: the corrector reads level ip and writes level iq; the top rows read
       // up - 2u + um from a slab of planes kb..8
@@ -252,6 +334,15 @@ int EW::curv_bc(double* ucart, double* ucurv)
 {
    CurvGrid& c = *cv_;
    const Bounds& b = c.b;
+   if (mixed_) {
+      SW4G_TRY(launch_bcfortsg_df(b.ib, b.ie, b.jb, b.je, b.kb, b.ke, c.wind, g_.nx, g_.ny, c.nz, df(ucurv),
+                                  g_.h, c.bc, sbop_, c.mu, c.la, dprof_[3], dprof_[4], stream_));
+      SW4G_TRY(launch_freesurfcurvisg_df(curv_spec(c, nullptr, dprof_[3], dprof_[4]), c.nz, 5, sbop_,
+                                         df(ucurv), stream_));
+      return launch_cart_topo_df(make_box(1, b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke),
+                                 make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke), c.nz, df(ucart),
+                                 df(ucurv), stream_);
+   }
    SW4G_TRY(launch_bcfortsg(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, c.wind, g_.nx, g_.ny, c.nz, ucurv,
                             g_.h, c.bc, sbop_, c.mu, c.la, nullptr, dprof_[3], dprof_[4], stream_));
    SW4G_TRY(launch_freesurfcurvisg(curv_spec(c, ucurv, dprof_[3], dprof_[4]), c.nz, 5, sbop_,

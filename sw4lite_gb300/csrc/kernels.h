@@ -155,6 +155,47 @@ struct CurvStage {
    double dt = 0, beta = 0;
 };
 int launch_curv_stage(const CurvStage& st, cudaStream_t s);
+
+// The curvilinear coefficients of the FP32-mixed stage as (hi, lo) FP32 pairs:
+// products 0..7 as CurvCoef::prod, 8 = (2mu+la) m2 m1, 9 = (2mu+la) m3 m1; the
+// twenty second-difference weights x144; K/144; 1/(rho J); rho J in FP32.
+struct CurvCoefDF {
+   float* ph[10];
+   float* pl[10];
+   float* wh[20];
+   float* wl[20];
+   float *Kh, *Kl, *irh, *irl, *rj;
+};
+long long curv_coef_df_floats(long long npts);
+int curv_coef_df_setup(long long npts, const CurvCoef& c, float* store, CurvCoefDF* d, cudaStream_t s);
+
+// One fused curvilinear stage of the FP32-mixed form over double-float levels:
+// FP32 interior rows 7..nz, FP64 SBP top rows and the ghost shell.
+struct CurvStageDF {
+   Box b;
+   int nz = 0;
+   int corrector = 0;
+   const float* u = nullptr;  // double-float levels: hi at [c*npts + p], lo at 3*npts further
+   const float* um = nullptr;
+   const float* up = nullptr;
+   float* out = nullptr;
+   CurvCoef cc{};    // FP64 coefficients (top rows)
+   CurvCoefDF cd{};  // (hi, lo) coefficients (interior)
+   const double *sx = nullptr, *sy = nullptr, *dcx = nullptr, *dcy = nullptr, *cox = nullptr,
+                *coy = nullptr;
+   const float *sx32 = nullptr, *sy32 = nullptr, *dcx32 = nullptr, *dcy32 = nullptr,
+               *cox32 = nullptr, *coy32 = nullptr;
+   // corrector: up - 2u + um over planes kb..8 in FP64 (the top rows' stage field)
+   const double* f = nullptr;
+   Box fbox;
+   double dt = 0, beta = 0;
+};
+int launch_curv_stage_df(const CurvStageDF& st, cudaStream_t s);
+int launch_curv_top_df(const CurvStageDF& st, cudaStream_t s);
+int launch_freesurfcurvisg_df(const CurvSpec& s, int nz, int side, const double* sbop, float* uh,
+                              cudaStream_t st);
+int launch_cart_topo_df(const Box& cart, const Box& curv, int nzc, float* ucart, float* ucurv,
+                        cudaStream_t st);
 int launch_metric(int soa, int ib, int ie, int jb, int je, int kb, int ke, double h, const double* z,
                   double* met, double* jac, int* bad_flag, cudaStream_t st);
 int launch_gaussian_hill_z(int ib, int ie, int jb, int je, int kb, int ke, int nz, double h,

@@ -1,0 +1,58 @@
+"""Stream order between torch and the library for device tensors.
+
+An EW object runs on its own CUDA stream.  Device tensors that torch produced on
+its current stream must be complete before the library reads them, and tensors
+the library fills must be complete before torch reads them.  Each test keeps one
+stream busy with a timed spin (torch.cuda._sleep) so that a missing dependency
+would read stale values deterministically.
+"""
+import numpy as np
+import pytest
+
+import sw4lite_gb300 as sg
+from tests.gpu_util import smooth_fields
+
+pytestmark = pytest.mark.gpu
+
+SPIN = 200_000_000  # GPU cycles, about 0.1 s at 2 GHz
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    sg.build()
+
+
+def test_inputs_wait_for_torch_stream():
+    import torch
+    g = sg.grid_desc(16, 16, 16, 0.1)
+    s = torch.cuda.Stream()
+    ew = sg.EW(g, stream=s)
+    n = ew.npts
+    rho, mu, la = (torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3))
+    torch.cuda._sleep(SPIN)  # on torch's current stream, before the values exist
+    rho.fill_(2.0)
+    mu.fill_(3.0)
+    la.fill_(1.0)
+    ew.set_material(rho, mu, la)
+    dt, nsteps = ew.compute_time_step(1.0, 1.0)
+    ew.close()
+    ref = sg.EW(g)
+    ref.set_material(*(np.full(n, v) for v in (2.0, 3.0, 1.0)))
+    assert (dt, nsteps) == ref.compute_time_step(1.0, 1.0)
+    ref.close()
+
+
+def test_outputs_complete_before_torch_reads():
+    import torch
+    g = sg.grid_desc(16, 16, 16, 0.1)
+    s = torch.cuda.Stream()
+    ew = sg.EW(g, stream=s)
+    u, um = smooth_fields(16, 16, 16, seed=5)
+    ew.set_fields(u, um)  # host arrays: synchronous
+    out = torch.zeros(3 * ew.npts, dtype=torch.float64, device="cuda")
+    with torch.cuda.stream(s):
+        torch.cuda._sleep(SPIN)  # the library's stream is busy when the copy is queued
+    ew.get_fields(out, None)
+    got = out.cpu().numpy()  # on torch's current stream
+    ew.close()
+    assert np.array_equal(got, u)

@@ -3,6 +3,11 @@ step (pinned to the reference's kernels in tests/test_oracle_topo_pin.py).
 
 Tolerance: after 6 steps both grids' fields agree with the oracle to 1e-12
 relative to each field's largest magnitude.
+
+The FP32-mixed form of the two-grid loop (FP32 interior stencils on both grids,
+FP64 SBP top rows, curvilinear free surface and interface copy, double-float
+levels) against the FP64 form: level storage round trip 1e-14, one step 1e-6
+relative to the field maximum, 120 steps relative L2 error <= 1e-5 on each grid.
 """
 import numpy as np
 import pytest
@@ -31,13 +36,29 @@ def _case(bc_bottom=2):
                     gp=5, sources=src, bc_bottom=bc_bottom)
 
 
+def _long_case():
+    # runs of more than a few steps need supergrid layers of at least ~15 points:
+    # the damping coefficient PsiDamp/phi reaches 1/epsL = 1e4 at the boundary, and
+    # thinner layers (5-10 points) grow without bound in the reference formulation
+    # at any CFL number
+    nx, ny, ncart, h = 44, 42, 30, 0.1
+    src = [sg.source_desc(0.5 * nx * h, 0.45 * ny * h, 1.0 + 0.3 * ncart * h, force=(1.0, -0.5, 0.3),
+                          freq=8.0, t0=0.1, kind=sg.GAUSSIAN)]
+    return TopoCase(nx, ny, ncart, h, zmax_topo=1.0, amp=0.2, xc=2.2, yc=2.1, lx=0.6, ly=0.5,
+                    gp=15, sources=src)
+
+
 def _rel(a, b):
     return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
 
-def _gpu(case, fields, dt, nsteps, mode):
+def _gpu(case, fields, dt, nsteps, mode, precision=sg.FP64):
     t = sg.topo_desc(**case.hill)
-    ew = sg.EW(case.grid, topo=t)
+    g = case.grid
+    if precision != sg.FP64:
+        g = sg.grid_desc(case.nx, case.ny, case.ncart, case.h, bc=case.bc, zmin=case.zmax_topo,
+                         sg_gp=g.sg_gp, sg_damping=g.sg_damping, precision=precision)
+    ew = sg.EW(g, topo=t)
     assert ew.num_grids == 2
     nx, ny, nz, n = ew.grid_dims(1)
     assert (nx, ny, nz) == (case.nx, case.ny, case.nc) and n == case.z.size
@@ -98,3 +119,34 @@ def test_topo_time_step_and_bad_inputs():
     steep = dict(c.hill, amp=2.0)
     with pytest.raises(sg.Sw4gError):  # the grid would fold
         sg.EW(c.grid, topo=sg.topo_desc(**steep))
+
+
+def test_mixed_topo_level_round_trip():
+    c = _case()
+    fields = smooth_topo_fields(c, seed=3)
+    got, _ = _gpu(c, fields, 1e-3, 0, sg.MODE_FUSED, sg.MIXED)
+    for a, b in zip(got, fields):
+        assert _rel(a, b) <= 1e-14
+
+
+@pytest.mark.parametrize("nsteps,tol", [(1, 1e-6), (120, 1e-5)])
+def test_mixed_topo_close_to_fp64(nsteps, tol):
+    c = _case() if nsteps == 1 else _long_case()
+    dt = c.time_step(1.3)
+    fields = smooth_topo_fields(c, seed=6)
+    a, _ = _gpu(c, fields, dt, nsteps, sg.MODE_FUSED)
+    b, _ = _gpu(c, fields, dt, nsteps, sg.MODE_FUSED, sg.MIXED)
+    for x, y in zip(b, a):
+        if nsteps == 1:
+            assert _rel(x, y) <= tol
+        else:
+            l2 = float(np.linalg.norm(x - y) / np.linalg.norm(y))
+            assert l2 <= tol, l2
+    ew = sg.EW(sg.grid_desc(c.nx, c.ny, c.ncart, c.h, bc=c.bc, zmin=c.zmax_topo, sg_gp=c.grid.sg_gp,
+                            precision=sg.MIXED), topo=sg.topo_desc(**c.hill))
+    ew.set_material(*[dev(q) for q in c.cart_mat])
+    ew.set_material_grid(1, *[dev(q) for q in c.curv_mat])
+    ew.set_time_step(dt)
+    with pytest.raises(sg.Sw4gError):
+        ew.step(1, sg.MODE_PHASES)
+    ew.close()
