@@ -499,9 +499,84 @@ struct TopArgs {
    WR out;
    CurvCoef cc;
    const double* __restrict__ topw;
+   // per column: one-sided r derivatives DR[(k-1)*3 + c] and r-outer sums
+   // RO[(k-1)*3 + c] of rows k = 1..6 (curv_top_pre_kernel), 18 x ncol each
+   const double* __restrict__ dr;
+   const double* __restrict__ ro;
    const double *sx, *sy, *dcx, *dcy, *cox, *coy;
    double coef, beta;
 };
+
+// Per column, the parts of the top rows that do not depend on the row's own
+// position: the one-sided r derivatives sum_q bope(k,q) f(q) of the stage field
+// (all columns; the p- and q-outer cross terms read them at the four neighbouring
+// columns) and the r-outer cross terms sum_q bope(k,q) G(q) with G the PR + QR
+// products at planes q = 1..8 (interior columns), for k = 1..6
+// (src/rhs4sgcurv_rev.C:224-275).
+template <class SF>
+__global__ void __launch_bounds__(128) curv_top_pre_kernel(Box b, Box fb, SF f, CurvCoef cc,
+                                                           const double* __restrict__ sx,
+                                                           const double* __restrict__ sy,
+                                                           double* __restrict__ dr,
+                                                           double* __restrict__ ro)
+{
+   const long long ncol = b.nij;
+   auto F = [&](int c, int ii, int jj, int kk) { return f.get(c * fb.npts + pidx(fb, ii, jj, kk)); };
+   auto Pr = [&](int t, long long q) { return __ldg(cc.prod[t] + q); };
+   const double i12 = 1.0 / 12;
+   auto cd = [&](double fm2, double fm1, double fp1, double fp2) { return i12 * d1c(fm2, fm1, fp1, fp2); };
+   for (long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x; col < ncol;
+        col += (long long)gridDim.x * blockDim.x) {
+      const int i = b.ib + (int)(col % b.ni), j = b.jb + (int)(col / b.ni);
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+         double fq[8];
+#pragma unroll
+         for (int q = 1; q <= 8; q++) fq[q - 1] = F(c, i, j, q);
+#pragma unroll
+         for (int k = 1; k <= 6; k++) {
+            double s = 0;
+#pragma unroll
+            for (int q = 1; q <= 8; q++) s += t_bope[(k - 1) + 6 * (q - 1)] * fq[q - 1];
+            dr[((k - 1) * 3 + c) * ncol + col] = s;
+         }
+      }
+      if (i < b.ib + 2 || i > b.ie - 2 || j < b.jb + 2 || j > b.je - 2) continue;
+      const double sxc = __ldg(sx + (i - b.ib)), syc = __ldg(sy + (j - b.jb));
+      const double istrx = 1 / sxc, istry = 1 / syc;
+      double acc[6][3];
+#pragma unroll
+      for (int k = 0; k < 6; k++) acc[k][0] = acc[k][1] = acc[k][2] = 0;
+#pragma unroll 1
+      for (int qq = 1; qq <= 8; qq++) {
+         const long long q = pidx(b, i, j, qq);
+         double dp[3], dq[3];
+#pragma unroll
+         for (int c = 0; c < 3; c++) {
+            dp[c] = cd(F(c, i - 2, j, qq), F(c, i - 1, j, qq), F(c, i + 1, j, qq), F(c, i + 2, j, qq));
+            dq[c] = cd(F(c, i, j - 2, qq), F(c, i, j - 1, qq), F(c, i, j + 1, qq), F(c, i, j + 2, qq));
+         }
+         const double p21m = Pr(2, q), p21l = Pr(3, q), p31m = Pr(4, q), p31l = Pr(5, q),
+                      p41m = Pr(6, q), p41l = Pr(7, q);
+         const double g0 = (2 * p21m + p21l) * sxc * istry * dp[0] + p31m * dp[1] + p41m * istry * dp[2] +
+                           p31m * syc * istrx * dq[0] + p21l * dq[1];
+         const double g1 = p31l * dp[0] + p21m * sxc * istry * dp[1] + p21m * dq[0] +
+                           (2 * p31m + p31l) * syc * istrx * dq[1] + p41m * istrx * dq[2];
+         const double g2 = istry * (p41l * dp[0] + p21m * sxc * dp[2]) + istrx * (p31m * syc * dq[2] + p41l * dq[1]);
+#pragma unroll
+         for (int k = 0; k < 6; k++) {
+            const double bw = t_bope[k + 6 * (qq - 1)];
+            acc[k][0] += bw * g0;
+            acc[k][1] += bw * g1;
+            acc[k][2] += bw * g2;
+         }
+      }
+#pragma unroll
+      for (int k = 0; k < 6; k++)
+#pragma unroll
+         for (int c = 0; c < 3; c++) ro[(k * 3 + c) * ncol + col] = acc[k][c];
+   }
+}
 
 // Rows k = 1..6 under the SBP top: the one-sided operator from precomputed
 // coefficients, with the stage update (and the corrector's x/y damping) fused.
@@ -570,10 +645,7 @@ __global__ void __launch_bounds__(128) curv_top_kernel(TopArgs<RD, WR, SF> a)
    }
    // one-sided r derivative of component c at column (ii, jj), row k
    auto drb = [&](int c, int ii, int jj) {
-      double s = 0;
-#pragma unroll
-      for (int q = 1; q <= 8; q++) s += t_bope[(k - 1) + 6 * (q - 1)] * F(c, ii, jj, q);
-      return s;
+      return __ldg(a.dr + ((k - 1) * 3 + c) * ncol + pidx(b, ii, jj, b.kb));
    };
    // p-outer: QP (central) + RP (one-sided r)
    {
@@ -620,30 +692,8 @@ __global__ void __launch_bounds__(128) curv_top_kernel(TopArgs<RD, WR, SF> a)
       for (int c = 0; c < 3; c++) s3[c] += cd(G[c][0], G[c][1], G[c][2], G[c][3]);
    }
    // r-outer (one-sided): PR + QR products at planes 1..8 of this column
-   {
-      double acc[3] = {0, 0, 0};
 #pragma unroll
-      for (int qq = 1; qq <= 8; qq++) {
-         const double bw = t_bope[(k - 1) + 6 * (qq - 1)];
-         const long long q = pidx(b, i, j, qq);
-         double dp[3], dq[3];
-#pragma unroll
-         for (int c = 0; c < 3; c++) {
-            dp[c] = cd(F(c, i - 2, j, qq), F(c, i - 1, j, qq), F(c, i + 1, j, qq), F(c, i + 2, j, qq));
-            dq[c] = cd(F(c, i, j - 2, qq), F(c, i, j - 1, qq), F(c, i, j + 1, qq), F(c, i, j + 2, qq));
-         }
-         const double p21m = Pr(2, q), p21l = Pr(3, q), p31m = Pr(4, q), p31l = Pr(5, q),
-                      p41m = Pr(6, q), p41l = Pr(7, q);
-         acc[0] += bw * ((2 * p21m + p21l) * sxc * istry * dp[0] + p31m * dp[1] + p41m * istry * dp[2] +
-                         p31m * syc * istrx * dq[0] + p21l * dq[1]);
-         acc[1] += bw * (p31l * dp[0] + p21m * sxc * istry * dp[1] + p21m * dq[0] +
-                         (2 * p31m + p31l) * syc * istrx * dq[1] + p41m * istrx * dq[2]);
-         acc[2] += bw * (istry * (p41l * dp[0] + p21m * sxc * dp[2]) +
-                         istrx * (p31m * syc * dq[2] + p41l * dq[1]));
-      }
-#pragma unroll
-      for (int c = 0; c < 3; c++) s3[c] += acc[c];
-   }
+   for (int c = 0; c < 3; c++) s3[c] += __ldg(a.ro + ((k - 1) * 3 + c) * ncol + col);
    const double kk = a.coef * __ldg(a.cc.K + p);
    if (!CORR) {
 #pragma unroll
@@ -683,6 +733,13 @@ __global__ void __launch_bounds__(128) curv_top_kernel(TopArgs<RD, WR, SF> a)
    }
 }
 
+int gsb(long long n, int threads = 256)
+{
+   long long b = (n + threads - 1) / threads;
+   if (b > 152 * 16) b = 152 * 16;
+   return (int)(b > 0 ? b : 1);
+}
+
 template <int CORR, class RD, class WR, class SF, class ST>
 int launch_top(const ST& st, RD u, RD um, RD up, WR out, SF f, cudaStream_t s)
 {
@@ -697,6 +754,8 @@ int launch_top(const ST& st, RD u, RD um, RD up, WR out, SF f, cudaStream_t s)
    t.out = out;
    t.cc = st.cc;
    t.topw = st.cc.topw;
+   t.dr = st.scratch;
+   t.ro = st.scratch + 18 * b.nij;
    t.sx = st.sx;
    t.sy = st.sy;
    t.dcx = st.dcx;
@@ -705,18 +764,16 @@ int launch_top(const ST& st, RD u, RD um, RD up, WR out, SF f, cudaStream_t s)
    t.coy = st.coy;
    t.coef = CORR ? st.dt * st.dt / 12 : st.dt * st.dt;
    t.beta = st.beta;
+   if (!st.scratch) return kBadArgument;
+   curv_top_pre_kernel<<<gsb(b.nij, 128), 128, 0, s>>>(b, st.fbox, f, st.cc, st.sx, st.sy, st.scratch,
+                                                       st.scratch + 18 * b.nij);
+   SW4G_TRY(launch_status());
    const int ni = b.ie - b.ib - 3, nj = b.je - b.jb - 3;
    const dim3 blk(32, 4), g((ni + 31) / 32, (nj + 3) / 4, 6);
    curv_top_kernel<CORR><<<g, blk, 0, s>>>(t);
    return launch_status();
 }
 
-int gsb(long long n)
-{
-   long long b = (n + 255) / 256;
-   if (b > 152 * 16) b = 152 * 16;
-   return (int)(b > 0 ? b : 1);
-}
 
 }  // namespace
 

@@ -44,6 +44,7 @@ struct CurvGrid {
    double* coef = nullptr;  // fused-stage coefficients (curv_stage.cu)
    CurvCoef cc{};
    float* coefdf = nullptr;  // the mixed form's (hi, lo) coefficients (curv_mixed.cu)
+   double* topscr = nullptr;  // work array of the SBP top rows, 36 doubles per column
    CurvCoefDF cd{};
    bool material = false;
    ~CurvGrid();

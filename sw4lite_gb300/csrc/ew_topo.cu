@@ -38,6 +38,7 @@ CurvGrid::~CurvGrid()
    f(fzero);
    f(coef);
    f(coefdf);
+   f(topscr);
 }
 
 namespace {
@@ -89,6 +90,8 @@ int EW::init_topo()
    for (double** p : {&c.z, &c.jac, &c.rho, &c.mu, &c.la})
       SW4G_TRY(cuda_ok(cudaMalloc(p, n * sizeof(double))));
    SW4G_TRY(cuda_ok(cudaMalloc(&c.met, 4 * n * sizeof(double))));
+   SW4G_TRY(cuda_ok(cudaMalloc(&c.topscr, 36 * (size_t)(b_.ie - b_.ib + 1) * (b_.je - b_.jb + 1) *
+                                              sizeof(double))));
    for (double** p : {&c.lev[0], &c.lev[1], &c.lev[2], &c.lev[3], &c.lu, &c.uacc, &c.fzero}) {
       SW4G_TRY(cuda_ok(cudaMalloc(p, 3 * n * sizeof(double))));
       SW4G_TRY(cuda_ok(cudaMemsetAsync(*p, 0, 3 * n * sizeof(double), stream_)));
@@ -222,6 +225,7 @@ CurvStage curv_stage_args(const CurvGrid& c, double* const dprof[9], double dt, 
    st.dcy = dprof[1];
    st.cox = dprof[6];
    st.coy = dprof[7];
+   st.scratch = c.topscr;
    st.dt = dt;
    st.beta = beta;
    return st;
@@ -246,6 +250,7 @@ CurvStageDF curv_stage_args_df(const CurvGrid& c, double* const dprof[9], float*
    st.dcy32 = prof32[1];
    st.cox32 = prof32[6];
    st.coy32 = prof32[7];
+   st.scratch = c.topscr;
    st.dt = dt;
    st.beta = beta;
    return st;
@@ -383,11 +388,11 @@ int EW::curv_launches(int mode) const
    }
    bc++;  // flat free surface of bcfortsg on the top side
    const bool damp = prof_.used && g_.sg_damping != 0;
-   // predictor (both modes): shell, top rows, stage kernel
-   const int pred = 3;
-   // corrector: fused slab, shell, top rows, stage; phase order dpdm, two operator
-   // kernels, corrfort, damping
-   const int corr = mode == kModeFused ? 4 : 4 + (damp ? 1 : 0);
+   // predictor (both modes): shell, top-row column pass, top rows, stage kernel
+   const int pred = 4;
+   // corrector: fused slab, shell, top-row column pass, top rows, stage; phase
+   // order dpdm, two operator kernels, corrfort, damping
+   const int corr = mode == kModeFused ? 5 : 4 + (damp ? 1 : 0);
    return pred + corr + 2 * bc;
 }
 

@@ -152,6 +152,8 @@ struct CurvStage {
    // up - 2u + um over planes kb..8 (corrector), and its array box
    const double* f = nullptr;
    Box fbox;
+   // work array of the top rows: 36 x (columns of the grid) doubles
+   double* scratch = nullptr;
    double dt = 0, beta = 0;
 };
 int launch_curv_stage(const CurvStage& st, cudaStream_t s);
@@ -188,6 +190,8 @@ struct CurvStageDF {
    // corrector: up - 2u + um over planes kb..8 in FP64 (the top rows' stage field)
    const double* f = nullptr;
    Box fbox;
+   // work array of the top rows: 36 x (columns of the grid) doubles
+   double* scratch = nullptr;
    double dt = 0, beta = 0;
 };
 int launch_curv_stage_df(const CurvStageDF& st, cudaStream_t s);
