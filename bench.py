@@ -608,6 +608,13 @@ def run_ours(args, rank, world):
     n = args.n
     npts_int = n ** 3
     stream = torch.cuda.Stream()
+    if args.only_topo:
+        # the topography workload alone (launch lists and kernel captures)
+        prec = 0 if args.only_topo == "fp64" else 1
+        t = _time_topo(args, sg, torch, stream, world, precision=prec)
+        if rank == 0:
+            print(json.dumps({"only": "topography " + args.only_topo, "topography": t}), flush=True)
+        return 0
     fp64 = _time_form(args, sg, torch, sg.FP64, stream, world, local)
     mixed = None
     if not args.no_mixed:
@@ -709,6 +716,8 @@ def main():
     ap.add_argument("--adj-n", type=int, default=256, help="grid of the adjoint workload")
     ap.add_argument("--adj-steps", type=int, default=200, help="steps of the adjoint workload")
     ap.add_argument("--adj-ckpt", type=int, default=100, help="checkpoint spacing")
+    ap.add_argument("--only-topo", choices=["fp64", "mixed"], default=None,
+                    help="time only the topography workload in that form (for profiling)")
     ap.add_argument("--no-err", action="store_true", help="skip the mixed-vs-FP64 error run")
     ap.add_argument("--err-n", type=int, default=256, help="grid of the mixed-vs-FP64 error run")
     ap.add_argument("--err-steps", type=int, default=1000, help="steps of the error run")

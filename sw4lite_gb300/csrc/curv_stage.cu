@@ -503,6 +503,8 @@ struct TopArgs {
    // RO[(k-1)*3 + c] of rows k = 1..6 (curv_top_pre_kernel), 18 x ncol each
    const double* __restrict__ dr;
    const double* __restrict__ ro;
+   // corrector, optional: u - um in FP64 over the stage field's planes (box fb)
+   const double* __restrict__ dd;
    const double *sx, *sy, *dcx, *dcy, *cox, *coy;
    double coef, beta;
 };
@@ -716,9 +718,11 @@ __global__ void __launch_bounds__(128) curv_top_kernel(TopArgs<RD, WR, SF> a)
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                const long long q = p + c * n;
+               const long long qs = c * fb.npts + pidx(fb, i, j, k);
                double d[5];
 #pragma unroll
-               for (int m = -2; m <= 2; m++) d[m + 2] = a.u.get(q + m * s) - a.um.get(q + m * s);
+               for (int m = -2; m <= 2; m++)
+                  d[m + 2] = a.dd ? __ldg(a.dd + qs + m * s) : a.u.get(q + m * s) - a.um.get(q + m * s);
                sg[c] += w[ax] * (e2 * (d[4] - 2 * d[3] + d[2]) - 2 * e1 * (d[3] - 2 * d[2] + d[1]) +
                                  e0 * (d[2] - 2 * d[1] + d[0]));
             }
@@ -741,7 +745,7 @@ int gsb(long long n, int threads = 256)
 }
 
 template <int CORR, class RD, class WR, class SF, class ST>
-int launch_top(const ST& st, RD u, RD um, RD up, WR out, SF f, cudaStream_t s)
+int launch_top(const ST& st, RD u, RD um, RD up, WR out, SF f, cudaStream_t s, const double* dd = nullptr)
 {
    const Box& b = st.b;
    TopArgs<RD, WR, SF> t;
@@ -756,6 +760,7 @@ int launch_top(const ST& st, RD u, RD um, RD up, WR out, SF f, cudaStream_t s)
    t.topw = st.cc.topw;
    t.dr = st.scratch;
    t.ro = st.scratch + 18 * b.nij;
+   t.dd = dd;
    t.sx = st.sx;
    t.sy = st.sy;
    t.dcx = st.dcx;
@@ -802,14 +807,16 @@ int curv_coef_setup(const Box& b, const double* mu, const double* la, const doub
 
 int launch_curv_top_df(const CurvStageDF& st, cudaStream_t s)
 {
+   // the stage field (and the corrector's u - um) come as FP64 slabs over planes
+   // kb..8: converting each double-float value once there keeps the float-to-double
+   // conversions off the stencil loads
    const long long lo = 3 * st.b.npts;
+   if (!st.f) return kBadArgument;
    if (st.corrector)
       return launch_top<1>(st, RdDF{st.u, lo}, RdDF{st.um, lo}, RdDF{st.up, lo}, DFField{st.out, lo},
-                           RdF64{st.f}, s);
-   CurvStageDF p = st;
-   p.fbox = st.b;
-   return launch_top<0>(p, RdDF{st.u, lo}, RdDF{st.um, lo}, RdDF{nullptr, lo}, DFField{st.out, lo},
-                        RdDF{st.u, lo}, s);
+                           RdF64{st.f}, s, st.dd);
+   return launch_top<0>(st, RdDF{st.u, lo}, RdDF{st.um, lo}, RdDF{nullptr, lo}, DFField{st.out, lo},
+                        RdF64{st.f}, s);
 }
 
 int launch_curv_stage(const CurvStage& st, cudaStream_t s)

@@ -268,6 +268,7 @@ int EW::curv_pred(int ip)
       st.u = df(c.lev[iu_]);
       st.um = df(c.lev[ium_]);
       st.out = df(c.lev[ip]);
+      st.work1 = c.uacc;
       return launch_curv_stage_df(st, stream_);
    }
    // fused: the stage kernel (rows 7..nz), the top-row kernel (rows 1..6) and the
@@ -290,9 +291,6 @@ int EW::curv_corr(int ip, int iq)
    const double dt = dt_;
    if (mixed_) {
       if (ip == iq) return kNotSupported;
-      const Box full = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke);
-      SW4G_TRY(launch_uacc_slab_df(full, b.kb, 8, df(c.lev[ip]), df(c.lev[iu_]), df(c.lev[ium_]), c.uacc,
-                                   stream_));
       const double beta = (prof_.used && g_.sg_damping != 0) ? g_.sg_damping : 0.0;
       CurvStageDF st = curv_stage_args_df(c, dprof_, prof32_, dt, beta);
       st.corrector = 1;
@@ -300,8 +298,8 @@ int EW::curv_corr(int ip, int iq)
       st.u = df(c.lev[iu_]);
       st.um = df(c.lev[ium_]);
       st.out = df(c.lev[iq]);
-      st.f = c.uacc;
-      st.fbox = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, 8);
+      st.work1 = c.uacc;
+      st.work2 = c.lu;
       return launch_curv_stage_df(st, stream_);
    }
    if (ip != iq) {
@@ -388,11 +386,13 @@ int EW::curv_launches(int mode) const
    }
    bc++;  // flat free surface of bcfortsg on the top side
    const bool damp = prof_.used && g_.sg_damping != 0;
-   // predictor (both modes): shell, top-row column pass, top rows, stage kernel
-   const int pred = 4;
-   // corrector: fused slab, shell, top-row column pass, top rows, stage; phase
-   // order dpdm, two operator kernels, corrfort, damping
-   const int corr = mode == kModeFused ? 5 : 4 + (damp ? 1 : 0);
+   // predictor (both modes): shell, top-row column pass, top rows, stage kernel;
+   // the mixed form adds the FP64 slab of u
+   const int pred = mixed_ ? 5 : 4;
+   // corrector: slab, shell, top-row column pass, top rows, stage (the mixed form
+   // adds the slab of u - um); phase order dpdm, two operator kernels, corrfort,
+   // damping
+   const int corr = mode == kModeFused ? (mixed_ ? 6 : 5) : 4 + (damp ? 1 : 0);
    return pred + corr + 2 * bc;
 }
 

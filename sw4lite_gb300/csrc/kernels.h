@@ -187,8 +187,13 @@ struct CurvStageDF {
                 *coy = nullptr;
    const float *sx32 = nullptr, *sy32 = nullptr, *dcx32 = nullptr, *dcy32 = nullptr,
                *cox32 = nullptr, *coy32 = nullptr;
-   // corrector: up - 2u + um over planes kb..8 in FP64 (the top rows' stage field)
+   // FP64 work slabs over planes kb..8 (3 x columns x (9 - kb) doubles each): the top
+   // rows' stage field (u, or up - 2u + um) and the corrector's u - um; f, fbox and dd
+   // are set by launch_curv_stage_df
+   double* work1 = nullptr;
+   double* work2 = nullptr;
    const double* f = nullptr;
+   const double* dd = nullptr;
    Box fbox;
    // work array of the top rows: 36 x (columns of the grid) doubles
    double* scratch = nullptr;
