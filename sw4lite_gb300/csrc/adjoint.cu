@@ -1,5 +1,6 @@
-// Discrete adjoint of the FP64 Cartesian time step and the material gradient of
-// a receiver misfit, sm_103a.
+// Discrete adjoint of the Cartesian time step and the material gradient of a
+// receiver misfit, sm_103a: FP64, or the FP32-mixed form (double-float levels and
+// adjoint variables, FP32 stages and gradient terms, FP64 gradient accumulation).
 //
 // The reference computes no material gradient (sw4lite has source-parameter
 // gradients only, src/GridPointSource.C:659-760); this is the exact transpose of
@@ -38,6 +39,7 @@
 #include <cmath>
 #include <vector>
 
+#include "df.cuh"
 #include "ew.h"
 
 namespace sw4g {
@@ -49,13 +51,29 @@ __device__ __forceinline__ bool inside(const Box& b, int i, int j, int k)
           k <= b.ke - 2;
 }
 
-struct Prof {
-   const double *dc[3], *st[3], *co[3];
+template <class T>
+struct ProfT {
+   const T *dc[3], *st[3], *co[3];
 };
+using Prof = ProfT<double>;
 
-__device__ __forceinline__ double sxyz(const Box& b, const Prof& f, int i, int j, int k)
+template <class T>
+__device__ __forceinline__ T sxyz(const Box& b, const ProfT<T>& f, int i, int j, int k)
 {
    return f.st[0][i - b.ib] * f.st[1][j - b.jb] * f.st[2][k - b.kb];
+}
+
+// a[q] - b[q] of two levels: FP64, or double-float (hi at q, lo at q + lo) formed
+// exactly and rounded once to FP32
+__device__ __forceinline__ double lev_diff(const double* a, const double* b, long long q, long long)
+{
+   return a[q] - b[q];
+}
+__device__ __forceinline__ float lev_diff(const float* a, const float* b, long long q, long long lo)
+{
+   float d, e;
+   two_sum(__ldg(a + q), -__ldg(b + q), d, e);
+   return d + (e + (__ldg(a + q + lo) - __ldg(b + q + lo)));
 }
 
 __device__ __forceinline__ void grid_point(const Box& b, long long p, int& i, int& j, int& k)
@@ -106,6 +124,54 @@ __global__ void adj_source_kernel(Box b, Prof f, int nrec, const int* __restrict
    for (int c = 0; c < 3; c++) an[c * b.npts + p] += s * res[3 * r + c];
 }
 
+// The mixed form's helpers over double-float levels (hi at q, lo at q + 3 npts):
+// w1 = up - 2u + um formed exactly and rounded to FP32; v1 = c1 W b1, v2 = c2 W mt in
+// FP32; the adjoint source added to a double-float level in FP64.
+__global__ void adj_w1_df_kernel(long long n3, const float* __restrict__ up, const float* __restrict__ u,
+                                 const float* __restrict__ um, float* __restrict__ w1)
+{
+   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n3;
+        q += (long long)gridDim.x * blockDim.x) {
+      float s1, e1, s2, e2;
+      two_sum(up[q], -2.f * u[q], s1, e1);
+      two_sum(s1, um[q], s2, e2);
+      w1[q] = s2 + ((e1 + e2) + ((up[q + n3] - 2.f * u[q + n3]) + um[q + n3]));
+   }
+}
+
+__global__ void adj_v_df_kernel(Box b, ProfT<float> f, const float* __restrict__ b1,
+                                const float* __restrict__ mt, float c1, float c2,
+                                float* __restrict__ v1, float* __restrict__ v2)
+{
+   const long long lo = 3 * b.npts;
+   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < b.npts;
+        p += (long long)gridDim.x * blockDim.x) {
+      int i, j, k;
+      grid_point(b, p, i, j, k);
+      const float w = 1.f / sxyz(b, f, i, j, k);
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+         const long long q = c * b.npts + p;
+         v1[q] = (c1 * w) * (b1[q] + b1[q + lo]);
+         v2[q] = (c2 * w) * (mt[q] + mt[q + lo]);
+      }
+   }
+}
+
+__global__ void adj_source_df_kernel(Box b, Prof f, int nrec, const int* __restrict__ ijk,
+                                     const double* __restrict__ res, const double* __restrict__ rho,
+                                     float* __restrict__ an)
+{
+   const int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if (r >= nrec) return;
+   const int i = ijk[3 * r], j = ijk[3 * r + 1], k = ijk[3 * r + 2];
+   const long long p = pidx(b, i, j, k);
+   const double s = sxyz(b, f, i, j, k) / rho[p];
+   const DFField a{an, 3 * b.npts};
+#pragma unroll
+   for (int c = 0; c < 3; c++) a.set(c * b.npts + p, a.get(c * b.npts + p) + s * res[3 * r + c]);
+}
+
 __device__ constexpr double kDW[5] = {1, -8, 0, 8, -1};
 // mixed terms of the operator: (equation, component, outer axis, inner axis, lambda?)
 __device__ constexpr int kMix[12][5] = {{0, 1, 0, 1, 1}, {0, 1, 1, 0, 0}, {0, 2, 0, 2, 1},
@@ -113,19 +179,26 @@ __device__ constexpr int kMix[12][5] = {{0, 1, 0, 1, 1}, {0, 1, 1, 0, 0}, {0, 2,
                                         {1, 2, 1, 2, 1}, {1, 2, 2, 1, 0}, {2, 0, 0, 2, 0},
                                         {2, 0, 2, 0, 1}, {2, 1, 1, 2, 0}, {2, 1, 2, 1, 1}};
 
+// T = double: FP64 throughout.  T = float (the mixed form): the levels u, um, up, un
+// are double-float (lo = 3 npts further; the stencil terms read the hi halves, the
+// level differences un - up and u - um are formed exactly), the products and sums are
+// FP32 and each point's contribution is accumulated into the FP64 gradients.
+template <class T>
 struct GradArgs {
    Box b;
-   Prof f;
-   const double *v1, *v2, *rho, *u, *um, *up, *un, *w1;
+   ProfT<T> f;
+   const T *v1, *v2, *rho, *u, *um, *up, *un, *w1;
    double* gr;
    double* gm;
    double* gl;
-   double c1, c2;  // v1 = c1 W b1 (pair with w1), v2 = c2 W mt (pair with u)
-   double ih2, beta;
+   T c1, c2;  // v1 = c1 W b1 (pair with w1), v2 = c2 W mt (pair with u)
+   T ih2, beta;
+   long long lo;  // offset of the levels' lo halves (float only)
 };
 
 // gradient of a1 . u+ at every array point (one thread per point)
-__global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs g)
+template <class T>
+__global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs<T> g)
 {
    const Box& b = g.b;
    const long long n = b.npts;
@@ -135,25 +208,25 @@ __global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs g)
         p += (long long)gridDim.x * blockDim.x) {
       int pc[3];
       grid_point(b, p, pc[0], pc[1], pc[2]);
-      double gm = 0, gl = 0, gr = 0;
+      T gm = 0, gl = 0, gr = 0;
 #pragma unroll
       for (int t = 0; t < 2; t++) {
-         const double* vb = t == 0 ? g.v1 : g.v2;
-         const double* wf = t == 0 ? g.w1 : g.u;
+         const T* vb = t == 0 ? g.v1 : g.v2;
+         const T* wf = t == 0 ? g.w1 : g.u;
          // same-axis second differences in edge form
 #pragma unroll
          for (int ax = 0; ax < 3; ax++) {
-            double sv[5];  // s_ax along the axis (0 beyond the array)
+            T sv[5];  // s_ax along the axis (0 beyond the array)
             bool ok[5];
 #pragma unroll
             for (int m = -2; m <= 2; m++) {
                const int x = pc[ax] + m;
                ok[m + 2] = x >= lo[ax] && x <= hi[ax];
-               sv[m + 2] = ok[m + 2] ? g.f.st[ax][x - lo[ax]] : 0.0;
+               sv[m + 2] = ok[m + 2] ? g.f.st[ax][x - lo[ax]] : T(0);
             }
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-               double v[5], w[5];
+               T v[5], w[5];
 #pragma unroll
                for (int m = -2; m <= 2; m++) {
                   if (!ok[m + 2]) {
@@ -164,12 +237,12 @@ __global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs g)
                   v[m + 2] = sv[m + 2] * vb[q];
                   w[m + 2] = wf[q];
                }
-               const double e1m2 = (v[1] - v[0]) * (w[1] - w[0]), e1m1 = (v[2] - v[1]) * (w[2] - w[1]);
-               const double e10 = (v[3] - v[2]) * (w[3] - w[2]), e1p1 = (v[4] - v[3]) * (w[4] - w[3]);
-               const double e2m2 = (v[2] - v[0]) * (w[2] - w[0]), e2m1 = (v[3] - v[1]) * (w[3] - w[1]);
-               const double e20 = (v[4] - v[2]) * (w[4] - w[2]);
-               const double val = -g.ih2 / 6 * sv[2] *
-                                  (e1p1 + e1m2 + 3 * (e1m1 + e10) + e2m1 - 0.75 * (e20 + e2m2));
+               const T e1m2 = (v[1] - v[0]) * (w[1] - w[0]), e1m1 = (v[2] - v[1]) * (w[2] - w[1]);
+               const T e10 = (v[3] - v[2]) * (w[3] - w[2]), e1p1 = (v[4] - v[3]) * (w[4] - w[3]);
+               const T e2m2 = (v[2] - v[0]) * (w[2] - w[0]), e2m1 = (v[3] - v[1]) * (w[3] - w[1]);
+               const T e20 = (v[4] - v[2]) * (w[4] - w[2]);
+               const T val = -g.ih2 / T(6) * sv[2] *
+                             (e1p1 + e1m2 + T(3) * (e1m1 + e10) + e2m1 - T(0.75) * (e20 + e2m2));
                if (c == ax) {
                   gm += 2 * val;
                   gl += val;
@@ -183,17 +256,17 @@ __global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs g)
          for (int e = 0; e < 12; e++) {
             const int c = kMix[e][0], d = kMix[e][1], ao = kMix[e][2], ai = kMix[e][3];
             if (pc[ai] < lo[ai] + 2 || pc[ai] > hi[ai] - 2) continue;
-            double inner = 0, outer = 0;
+            T inner = 0, outer = 0;
 #pragma unroll
             for (int m = -2; m <= 2; m++) {
                if (m == 0) continue;
-               inner += kDW[m + 2] * wf[d * n + p + m * st[ai]];
+               inner += T(kDW[m + 2]) * wf[d * n + p + m * st[ai]];
                int oc[3] = {pc[0], pc[1], pc[2]};
                oc[ao] += m;
                if (oc[ao] < lo[ao] || oc[ao] > hi[ao]) continue;
-               outer += kDW[m + 2] * g.f.st[ao][oc[ao] - lo[ao]] * vb[c * n + p + m * st[ao]];
+               outer += T(kDW[m + 2]) * g.f.st[ao][oc[ao] - lo[ao]] * vb[c * n + p + m * st[ao]];
             }
-            const double gg = -g.ih2 / 144 * g.f.st[ai][pc[ai] - lo[ai]] * inner * outer;
+            const T gg = -g.ih2 / T(144) * g.f.st[ai][pc[ai] - lo[ai]] * inner * outer;
             if (kMix[e][4]) gl += gg;
             else gm += gg;
          }
@@ -201,33 +274,33 @@ __global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs g)
       // rho: the 1/rho factors and forcing (interior points), and the damping's rho dc
       if (inside(b, pc[0], pc[1], pc[2])) {
          // W mt = v2/c2, W b1 = v1/c1
-         double s1 = 0, s2 = 0;
+         T s1 = 0, s2 = 0;
 #pragma unroll
          for (int c = 0; c < 3; c++) {
             const long long q = c * n + p;
             s2 += g.v2[q] * g.w1[q];
-            s1 += g.v1[q] * (g.un[q] - g.up[q]);
+            s1 += g.v1[q] * lev_diff(g.un, g.up, q, g.lo);
          }
          gr -= s2 / g.c2 + s1 / g.c1;
       }
       if (g.beta != 0) {
-         double sgr = 0;
+         T sgr = 0;
 #pragma unroll
          for (int ax = 0; ax < 3; ax++) {
             if (pc[ax] - 1 < lo[ax] || pc[ax] + 1 > hi[ax]) continue;
-            const double dcp = g.f.dc[ax][pc[ax] - lo[ax]];
+            const T dcp = g.f.dc[ax][pc[ax] - lo[ax]];
             if (dcp == 0) continue;  // the term is exactly zero there
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-               double vv[3], dd[3];
+               T vv[3], dd[3];
 #pragma unroll
                for (int m = -1; m <= 1; m++) {
                   int qc[3] = {pc[0], pc[1], pc[2]};
                   qc[ax] += m;
                   const long long q = p + m * st[ax];
-                  dd[m + 1] = g.u[c * n + q] - g.um[c * n + q];
+                  dd[m + 1] = lev_diff(g.u, g.um, c * n + q, g.lo);
                   const int oi = qc[0] - b.ib, oj = qc[1] - b.jb, ok = qc[2] - b.kb;
-                  const double wax = ax == 0   ? g.f.st[0][oi] * g.f.co[1][oj] * g.f.co[2][ok]
+                  const T wax = ax == 0   ? g.f.st[0][oi] * g.f.co[1][oj] * g.f.co[2][ok]
                                      : ax == 1 ? g.f.st[1][oj] * g.f.co[0][oi] * g.f.co[2][ok]
                                                : g.f.st[2][ok] * g.f.co[0][oi] * g.f.co[1][oj];
                   vv[m + 1] = wax * g.v1[c * n + q];
@@ -237,9 +310,9 @@ __global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs g)
          }
          gr -= g.beta / g.c1 * sgr;  // vv holds c1 W b1
       }
-      g.gm[p] += gm;
-      g.gl[p] += gl;
-      g.gr[p] += gr;
+      g.gm[p] += (double)gm;
+      g.gl[p] += (double)gl;
+      g.gr[p] += (double)gr;
    }
 }
 
@@ -252,13 +325,73 @@ int gs_blocks(long long n, int threads)
 
 }  // namespace
 
+// One adjoint step of the mixed form (double-float b, mt and levels; FP32 w1, v1,
+// v2 in the first half of their buffers): the same sequence as the FP64 step.
+int EW::adjoint_step_mixed(const MixedStage& base, const void* pfv, const void* pf32v, const Box& b,
+                           size_t n3, const double* u, const double* um, const double* up,
+                           const double* un, double* b1, double* b2, double* bn, double* mt,
+                           double* w1, double* v1, double* v2, double* gr, double* gm, double* gl,
+                           double dt, double beta, int nrec, const double* res)
+{
+   const Prof& pf = *static_cast<const Prof*>(pfv);
+   const ProfT<float>& pf32 = *static_cast<const ProfT<float>*>(pf32v);
+   auto F = [](double* x) { return reinterpret_cast<float*>(x); };
+   auto CF = [](const double* x) { return reinterpret_cast<const float*>(x); };
+   adj_w1_df_kernel<<<gs_blocks((long long)n3, 256), 256, 0, stream_>>>((long long)n3, CF(up), CF(u),
+                                                                          CF(um), F(w1));
+   SW4G_TRY(launch_status());
+   MixedStage ms = base;  // mt = b1 + dt^2/12 R L(b1): predictor form, um = u
+   ms.corrector = 0;
+   ms.u = CF(b1);
+   ms.um = CF(b1);
+   ms.up = nullptr;
+   ms.out = F(mt);
+   ms.beta = 0;
+   ms.coef = dt * dt / 12;
+   SW4G_TRY(launch_mixed_stage(ms, stream_));
+   adj_v_df_kernel<<<gs_blocks(npts_, 256), 256, 0, stream_>>>(b, pf32, CF(b1), CF(mt), (float)(dt * dt / 12),
+                                                               (float)(dt * dt), F(v1), F(v2));
+   SW4G_TRY(launch_status());
+   GradArgs<float> ga;
+   ga.b = b;
+   ga.f = pf32;
+   ga.v1 = CF(v1);
+   ga.v2 = CF(v2);
+   ga.rho = rho32_;
+   ga.u = CF(u);
+   ga.um = CF(um);
+   ga.up = CF(up);
+   ga.un = CF(un);
+   ga.w1 = CF(w1);
+   ga.gr = gr;
+   ga.gm = gm;
+   ga.gl = gl;
+   ga.c1 = (float)(dt * dt / 12);
+   ga.c2 = (float)(dt * dt);
+   ga.ih2 = (float)(1 / (g_.h * g_.h));
+   ga.beta = (float)beta;
+   ga.lo = 3 * npts_;
+   adj_gradient_kernel<float><<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
+   SW4G_TRY(launch_status());
+   ms = base;  // b^n = 2 b1 - b2 + dt^2 R L(mt) - beta R SG(b1 - b2): adjoint form
+   ms.corrector = 2;
+   ms.u = CF(b1);
+   ms.um = CF(b2);
+   ms.up = CF(mt);
+   ms.out = F(bn);
+   ms.beta = beta;
+   SW4G_TRY(launch_mixed_stage(ms, stream_));
+   adj_source_df_kernel<<<blocks_for(nrec, 64), 64, 0, stream_>>>(b, pf, nrec, drec_.ijk, res, rho_, F(bn));
+   return launch_status();
+}
+
 int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, double* misfit,
                  double* g_rho, double* g_mu, double* g_la, bool grad_on_device)
 {
    if (!ready_ || !material_ || !(dt_ > 0) || nsteps < 1 || ckpt < 1 || !obs || !misfit || !g_rho ||
        !g_mu || !g_la)
       return kBadArgument;
-   if (mixed_ || cv_ || g_.sg_order != 4) return kNotSupported;
+   if (cv_ || g_.sg_order != 4) return kNotSupported;
    for (int s = 0; s < 6; s++)
       if (g_.bc[s] != kDirichlet && g_.bc[s] != kSuperGrid) return kNotSupported;
    if (drec_.n == 0) return kBadArgument;
@@ -319,6 +452,38 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       pf.co[a] = dprof_[6 + a];
    }
    const double beta = (prof_.used && g_.sg_damping != 0) ? g_.sg_damping : 0.0;
+   // the mixed form: double-float levels, FP32 stages and gradient terms
+   ProfT<float> pf32{};
+   MixedStage ms;
+   if (mixed_) {
+      for (int a = 0; a < 3; a++) {
+         pf32.dc[a] = prof32_[a];
+         pf32.st[a] = prof32_[3 + a];
+         pf32.co[a] = prof32_[6 + a];
+      }
+      ms.b = b;
+      ms.k1 = 1;
+      ms.k2 = g_.nz;
+      ms.muh = mu32_;
+      ms.mul = mu32_ + npts_;
+      ms.lah = la32_;
+      ms.lal = la32_ + npts_;
+      ms.irh = irho32_;
+      ms.irl = irho32_ + npts_;
+      ms.rho = rho32_;
+      for (int q = 0; q < kWeightArrays; q++) {
+         ms.wh[q] = wd_.h[q];
+         ms.wl[q] = wd_.l[q];
+      }
+      for (int q = 0; q < 3; q++) {
+         ms.dc[q] = prof32_[q];
+         ms.st[q] = prof32_[3 + q];
+         ms.co[q] = prof32_[6 + q];
+      }
+      ms.h = g_.h;
+      ms.dt = dt;
+   }
+   auto F = [](double* x) { return reinterpret_cast<float*>(x); };
 
    auto run = [&]() -> int {
       SW4G_TRY(cuda_ok(cudaMemsetAsync(gr_d, 0, npts_ * sizeof(double), stream_)));
@@ -365,8 +530,12 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       double* v2 = work + 6 * n3;  // dt^2 W mt
       SW4G_TRY(cuda_ok(cudaMemsetAsync(work, 0, 7 * lv, stream_)));  // not fin
       // b^N = W^-1 R g^N
-      adj_source_kernel<<<blocks_for(drec_.n, 64), 64, 0, stream_>>>(
-          b, pf, drec_.n, drec_.ijk, resd + (size_t)nsteps * nval, rho_, b1);
+      if (mixed_)
+         adj_source_df_kernel<<<blocks_for(drec_.n, 64), 64, 0, stream_>>>(
+             b, pf, drec_.n, drec_.ijk, resd + (size_t)nsteps * nval, rho_, F(b1));
+      else
+         adj_source_kernel<<<blocks_for(drec_.n, 64), 64, 0, stream_>>>(
+             b, pf, drec_.n, drec_.ijk, resd + (size_t)nsteps * nval, rho_, b1);
       SW4G_TRY(launch_status());
       FusedStage fs;
       fs.b = b;
@@ -412,58 +581,64 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
             const double* um = seg + (size_t)(nn - s0) * n3;
             const double* up = pred + (size_t)(nn - s0) * n3;
             const double* un = seg + (size_t)(nn - s0 + 2) * n3;
-            adj_w1_kernel<<<gs_blocks(n3, 256), 256, 0, stream_>>>(n3, up, u, um, w1);
-            status = launch_status();
-            if (status == kOk) {  // mt = b1 + dt^2/12 R L(b1): predictor form, um = u
-               fs.corrector = 0;
-               fs.u = b1;
-               fs.um = b1;
-               fs.up = nullptr;
-               fs.out = mt;
-               fs.beta = 0;
-               fs.coef = dt * dt / 12;
-               status = launch_fused_stage(fs, stream_);
-            }
-            if (status == kOk) {
-               adj_v_kernel<<<blocks, 256, 0, stream_>>>(b, pf, b1, mt, dt * dt / 12, dt * dt, v1, v2);
+            if (mixed_) {
+               status = adjoint_step_mixed(ms, &pf, &pf32, b, n3, u, um, up, un, b1, b2, bn, mt, w1, v1, v2,
+                                           gr_d, gm_d, gl_d, dt, beta, saved_n, resd + (size_t)nn * nval);
+            } else {
+               adj_w1_kernel<<<gs_blocks(n3, 256), 256, 0, stream_>>>(n3, up, u, um, w1);
                status = launch_status();
-            }
-            if (status == kOk) {
-               GradArgs ga;
-               ga.b = b;
-               ga.f = pf;
-               ga.v1 = v1;
-               ga.v2 = v2;
-               ga.rho = rho_;
-               ga.u = u;
-               ga.um = um;
-               ga.up = up;
-               ga.un = un;
-               ga.w1 = w1;
-               ga.gr = gr_d;
-               ga.gm = gm_d;
-               ga.gl = gl_d;
-               ga.c1 = dt * dt / 12;
-               ga.c2 = dt * dt;
-               ga.ih2 = 1 / (g_.h * g_.h);
-               ga.beta = beta;
-               adj_gradient_kernel<<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
-               status = launch_status();
-            }
-            if (status == kOk) {  // b^n = 2 b1 - b2 + dt^2 R L(mt) - beta R SG(b1 - b2)
-               fs.corrector = 2;
-               fs.u = b1;
-               fs.um = b2;
-               fs.up = mt;
-               fs.out = bn;
-               fs.beta = beta;
-               fs.coef = dt * dt;
-               status = launch_fused_stage(fs, stream_);
-            }
-            if (status == kOk) {
-               adj_source_kernel<<<blocks_for(saved_n, 64), 64, 0, stream_>>>(
-                   b, pf, saved_n, drec_.ijk, resd + (size_t)nn * nval, rho_, bn);
-               status = launch_status();
+               if (status == kOk) {  // mt = b1 + dt^2/12 R L(b1): predictor form, um = u
+                  fs.corrector = 0;
+                  fs.u = b1;
+                  fs.um = b1;
+                  fs.up = nullptr;
+                  fs.out = mt;
+                  fs.beta = 0;
+                  fs.coef = dt * dt / 12;
+                  status = launch_fused_stage(fs, stream_);
+               }
+               if (status == kOk) {
+                  adj_v_kernel<<<blocks, 256, 0, stream_>>>(b, pf, b1, mt, dt * dt / 12, dt * dt, v1, v2);
+                  status = launch_status();
+               }
+               if (status == kOk) {
+                  GradArgs<double> ga;
+                  ga.lo = 0;
+                  ga.b = b;
+                  ga.f = pf;
+                  ga.v1 = v1;
+                  ga.v2 = v2;
+                  ga.rho = rho_;
+                  ga.u = u;
+                  ga.um = um;
+                  ga.up = up;
+                  ga.un = un;
+                  ga.w1 = w1;
+                  ga.gr = gr_d;
+                  ga.gm = gm_d;
+                  ga.gl = gl_d;
+                  ga.c1 = dt * dt / 12;
+                  ga.c2 = dt * dt;
+                  ga.ih2 = 1 / (g_.h * g_.h);
+                  ga.beta = beta;
+                  adj_gradient_kernel<double><<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
+                  status = launch_status();
+               }
+               if (status == kOk) {  // b^n = 2 b1 - b2 + dt^2 R L(mt) - beta R SG(b1 - b2)
+                  fs.corrector = 2;
+                  fs.u = b1;
+                  fs.um = b2;
+                  fs.up = mt;
+                  fs.out = bn;
+                  fs.beta = beta;
+                  fs.coef = dt * dt;
+                  status = launch_fused_stage(fs, stream_);
+               }
+               if (status == kOk) {
+                  adj_source_kernel<<<blocks_for(saved_n, 64), 64, 0, stream_>>>(
+                      b, pf, saved_n, drec_.ijk, resd + (size_t)nn * nval, rho_, bn);
+                  status = launch_status();
+               }
             }
             double* tmp = b2;
             b2 = b1;

@@ -356,7 +356,10 @@ int EW::get_fields(double* u, double* um, bool on_device) const
 
 int EW::enforce_bc(double* u)
 {
-   if (mixed_) return kNotSupported;  // levels are double-float pairs in the mixed form
+   if (mixed_)  // levels are double-float pairs in the mixed form
+      return launch_bcfortsg_df(b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke, wind_, g_.nx, g_.ny, g_.nz,
+                                reinterpret_cast<float*>(u), g_.h, g_.bc, sbop_, mu_, la_, dprof_[3],
+                                dprof_[4], stream_);
    return launch_bcfortsg(1, b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke, wind_, g_.nx, g_.ny, g_.nz,
                           u, g_.h, g_.bc, sbop_, mu_, la_, nullptr, dprof_[3], dprof_[4], stream_);
 }

@@ -65,6 +65,9 @@ struct MixedStage {
    const float* dc[3] = {nullptr, nullptr, nullptr};
    const float* co[3] = {nullptr, nullptr, nullptr};
    double h = 1, dt = 0, beta = 0;
+   // corrector 0 predictor, 1 corrector, 2 adjoint form (stage_mixed.cu); coef != 0
+   // replaces the stage's dt^2 (predictor, adjoint) or dt^2/12 (corrector)
+   double coef = 0;
 };
 
 // Device-resident grid-point sources grouped by grid point: the sources of point

@@ -3,6 +3,9 @@
 // Same stages as the FP64 form (stage_fused.cu):
 //   predictor  out = 2u - um + dt^2/rho * L(u)
 //   corrector  out = up + dt^2/12/rho * L(up - 2u + um) - beta/rho * SG(u - um)
+//   adjoint    out = 2u - um + dt^2/rho * L(up) - beta/rho * SG(u - um)
+// (the adjoint form is the scaled adjoint recursion of adjoint.cu; the predictor
+// form with a replaced coefficient gives its first stage)
 // with these precisions:
 //   * solution levels are double-float pairs (df.cuh): 48-bit storage, so the
 //     time-level accumulation keeps FP64-class precision, done with FP32
@@ -63,12 +66,13 @@ struct MixedArgs {
    float beta;
 };
 
-__host__ __device__ constexpr int smem_floats(int corr)
+__host__ __device__ constexpr int smem_floats(int form)
 {
    // predictor: hi and lo rings (5 x 3 planes each); corrector: field ring (5 x 3),
-   // damping ring (3 x 3) and rho plane; both: mu, lambda (hi, lo) planes, GX, GY
-   return (corr ? 15 * PLANE + 9 * PLANE + PLANE : 30 * PLANE) + 4 * PLANE + 3 * TY * PX +
-          3 * PY * TX;
+   // damping ring (3 x 3) and rho plane; adjoint: hi and lo rings, damping ring and rho
+   // plane; all: mu, lambda (hi, lo) planes, GX, GY
+   return (form == 1 ? 25 * PLANE : form == 2 ? 40 * PLANE : 30 * PLANE) + 4 * PLANE +
+          3 * TY * PX + 3 * PY * TX;
 }
 
 __device__ __forceinline__ int mod5(int k) { return ((k % 5) + 5) % 5; }
@@ -79,11 +83,13 @@ __global__ void __launch_bounds__(NTHREADS, 2) mixed_stage_kernel(MixedArgs a)
 {
    extern __shared__ float smf[];
    // predictor: VH | VL ; corrector: VH (the field) | DD | RH
+   // CORR: 0 predictor, 1 corrector, 2 adjoint (stencil field up as (hi, lo), damping
+   // of u - um, out = 2u - um + K L(up) - beta/rho SG(u - um))
    float* VH = smf;
-   float* VL = smf + 15 * PLANE;           // predictor only
-   float* DD = smf + 15 * PLANE;           // corrector only
-   float* RH = DD + 9 * PLANE;             // corrector only
-   float* MUH = smf + (CORR ? 25 * PLANE : 30 * PLANE);
+   float* VL = smf + 15 * PLANE;                       // predictor and adjoint forms
+   float* DD = smf + (CORR == 2 ? 30 : 15) * PLANE;    // corrector and adjoint forms
+   float* RH = DD + 9 * PLANE;                         // corrector and adjoint forms
+   float* MUH = smf + (CORR == 0 ? 30 : CORR == 1 ? 25 : 40) * PLANE;
    float* MUL = MUH + PLANE;
    float* LAH = MUL + PLANE;
    float* LAL = LAH + PLANE;
@@ -117,9 +123,19 @@ __global__ void __launch_bounds__(NTHREADS, 2) mixed_stage_kernel(MixedArgs a)
 #pragma unroll
          for (int c = 0; c < 3; c++) {
             const long long q = p + c * npts;
-            if (!CORR) {
-               vh[c * PLANE + idx] = in ? __ldg(a.u + q) : 0.f;
-               vl[c * PLANE + idx] = in ? __ldg(a.u + q + lo) : 0.f;
+            if (CORR != 1) {
+               const float* src = CORR == 2 ? a.up : a.u;
+               vh[c * PLANE + idx] = in ? __ldg(src + q) : 0.f;
+               vl[c * PLANE + idx] = in ? __ldg(src + q + lo) : 0.f;
+               if (CORR == 2) {
+                  float d = 0.f;
+                  if (in) {
+                     float d1, f1;
+                     two_sum(__ldg(a.u + q), -__ldg(a.um + q), d1, f1);
+                     d = d1 + (f1 + (__ldg(a.u + q + lo) - __ldg(a.um + q + lo)));
+                  }
+                  dd[c * PLANE + idx] = d;
+               }
             } else {
                float v = 0.f, d = 0.f;
                if (in) {
@@ -165,14 +181,14 @@ __global__ void __launch_bounds__(NTHREADS, 2) mixed_stage_kernel(MixedArgs a)
 
    // difference f(a) - f(b) of component c within one staged plane
    auto diff = [&](const float* vh, const float* vl, int ia, int ib_) -> float {
-      if (CORR) return vh[ia] - vh[ib_];
+      if (CORR == 1) return vh[ia] - vh[ib_];
       return (vh[ia] - vh[ib_]) + (vl[ia] - vl[ib_]);
    };
    // 12h * centred first difference from 4 samples given as (plane, index) pairs
    auto d1 = [&](const float* hm2, const float* lm2, int im2, const float* hm1, const float* lm1,
                  int im1, const float* hp1, const float* lp1, int ip1, const float* hp2,
                  const float* lp2, int ip2) -> float {
-      if (CORR) return (hm2[im2] - hp2[ip2]) + 8.f * (hp1[ip1] - hm1[im1]);
+      if (CORR == 1) return (hm2[im2] - hp2[ip2]) + 8.f * (hp1[ip1] - hm1[im1]);
       return ((hm2[im2] - hp2[ip2]) + (lm2[im2] - lp2[ip2])) +
              8.f * ((hp1[ip1] - hm1[im1]) + (lp1[ip1] - lm1[im1]));
    };
@@ -342,7 +358,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) mixed_stage_kernel(MixedArgs a)
                                    diff(ch, cl, own - PX, own), diff(ch, cl, own + PX, own),
                                    diff(ch, cl, own + 2 * PX, own));
             float dzm2, dzm1, dzp1, dzp2;
-            if (CORR) {
+            if (CORR == 1) {
                dzm2 = hm2[o + own] - ch[own];
                dzm1 = hm1[o + own] - ch[own];
                dzp1 = hp1[o + own] - ch[own];
@@ -429,10 +445,19 @@ __global__ void __launch_bounds__(NTHREADS, 2) mixed_stage_kernel(MixedArgs a)
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                const long long q = p + c * npts;
-               const float uph = __ldg(a.up + q), upl = __ldg(a.up + q + lo);
                float t, e, oh, ol;
-               two_sum(uph, scaled(xs[c]) - birho * sg[c], t, e);
-               fast_two_sum(t, e + upl, oh, ol);
+               if (CORR == 1) {
+                  const float uph = __ldg(a.up + q), upl = __ldg(a.up + q + lo);
+                  two_sum(uph, scaled(xs[c]) - birho * sg[c], t, e);
+                  fast_two_sum(t, e + upl, oh, ol);
+               } else {  // adjoint form: 2u - um + K L(up) - beta/rho SG(u - um)
+                  const float uh = __ldg(a.u + q), ul = __ldg(a.u + q + lo);
+                  const float mh = __ldg(a.um + q), ml = __ldg(a.um + q + lo);
+                  float s2, e1, e2;
+                  two_sum(2.f * uh, -mh, s2, e1);
+                  two_sum(s2, scaled(xs[c]) - birho * sg[c], t, e2);
+                  fast_two_sum(t, (e1 + e2) + (2.f * ul - ml), oh, ol);
+               }
                a.out[q] = oh;
                a.out[q + lo] = ol;
             }
@@ -571,7 +596,9 @@ int launch_mixed_stage(const MixedStage& st, cudaStream_t stream)
       a.dc[q] = st.dc[q];
       a.co[q] = st.co[q];
    }
-   const double K = (st.corrector ? st.dt * st.dt / 12 : st.dt * st.dt) / (144 * st.h * st.h);
+   if (st.corrector < 0 || st.corrector > 2) return kBadArgument;
+   const double coef = st.coef != 0 ? st.coef : (st.corrector == 1 ? st.dt * st.dt / 12 : st.dt * st.dt);
+   const double K = coef / (144 * st.h * st.h);
    a.Kh = (float)K;
    a.Kl = (float)(K - (double)a.Kh);
    a.beta = (float)st.beta;
@@ -586,17 +613,19 @@ int launch_mixed_stage(const MixedStage& st, cudaStream_t stream)
    const size_t smem = smem_floats(st.corrector) * sizeof(float);
    int dev = 0;
    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return kCudaError;
-   static bool attr_set[2][64] = {};
+   static bool attr_set[3][64] = {};
    if (!attr_set[st.corrector][dev]) {
       const cudaError_t e =
-          st.corrector
-              ? cudaFuncSetAttribute(mixed_stage_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-              : cudaFuncSetAttribute(mixed_stage_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+          st.corrector == 1   ? cudaFuncSetAttribute(mixed_stage_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+          : st.corrector == 2 ? cudaFuncSetAttribute(mixed_stage_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                              : cudaFuncSetAttribute(mixed_stage_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return kCudaError;
       attr_set[st.corrector][dev] = true;
    }
-   if (st.corrector)
+   if (st.corrector == 1)
       mixed_stage_kernel<1><<<grid, block, smem, stream>>>(a);
+   else if (st.corrector == 2)
+      mixed_stage_kernel<2><<<grid, block, smem, stream>>>(a);
    else
       mixed_stage_kernel<0><<<grid, block, smem, stream>>>(a);
    return launch_status();
