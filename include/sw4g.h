@@ -278,6 +278,12 @@ int sw4g_ew_set_time_step(sw4g_ew* ew, double dt, double t0);
 /* dt from the CFL number, adjusted to end at tmax (EW::computeDT, src/EW.C:5041) */
 int sw4g_ew_compute_time_step(sw4g_ew* ew, double cfl, double tmax, double* dt, int* nsteps);
 double sw4g_ew_time(const sw4g_ew* ew);
+/* CUDA graphs for the fused time loop and the gradient (on != 0): sw4g_ew_step and
+   sw4g_ew_gradient then replay captured chunks of steps, bit-identical to direct
+   launches; the forcing time and record row are kept in device memory.  Needs an
+   explicit (non-default) stream.  No reference counterpart: the reference launches
+   each kernel of timesteploop directly (src/EW.C:2537-2756). */
+int sw4g_ew_set_graphs(sw4g_ew* ew, int on);
 /* current (u) and previous (um) levels, 3*npts each, host or device */
 int sw4g_ew_set_fields(sw4g_ew* ew, const double* u, const double* um, int on_device);
 int sw4g_ew_get_fields(const sw4g_ew* ew, double* u, double* um, int on_device);

@@ -104,6 +104,7 @@ _SIGS = {
     "sw4g_ew_set_time_step": ([_VP, C.c_double, C.c_double], C.c_int),
     "sw4g_ew_compute_time_step": ([_VP, C.c_double, C.c_double, _D, _I], C.c_int),
     "sw4g_ew_time": ([_VP], C.c_double),
+    "sw4g_ew_set_graphs": ([_VP, C.c_int], C.c_int),
     "sw4g_ew_set_fields": ([_VP, _VP, _VP, C.c_int], C.c_int),
     "sw4g_ew_get_fields": ([_VP, _VP, _VP, C.c_int], C.c_int),
     "sw4g_ew_field": ([_VP, C.c_int], _VP),
@@ -287,6 +288,10 @@ class EW:
 
     def set_time_step(self, dt, t0=0.0):
         check(lib().sw4g_ew_set_time_step(self._h, dt, t0), "set_time_step")
+
+    def set_graphs(self, on=True):
+        """Replay the fused time loop (and the gradient's loops) as CUDA graphs."""
+        check(lib().sw4g_ew_set_graphs(self._h, int(bool(on))), "set_graphs")
 
     def compute_time_step(self, cfl, tmax):
         dt = C.c_double()

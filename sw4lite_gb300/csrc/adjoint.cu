@@ -113,10 +113,11 @@ __global__ void adj_v_kernel(Box b, Prof f, const double* __restrict__ b1,
 // b[receiver point] += W^-1 R res (receivers in order, 3 values each)
 __global__ void adj_source_kernel(Box b, Prof f, int nrec, const int* __restrict__ ijk,
                                   const double* __restrict__ res, const double* __restrict__ rho,
-                                  double* __restrict__ an)
+                                  double* __restrict__ an, const double* __restrict__ clk, int nval)
 {
    const int r = blockIdx.x * blockDim.x + threadIdx.x;
    if (r >= nrec) return;
+   if (clk) res += (long long)clk[2] * nval;  // the residual row from the device clock
    const int i = ijk[3 * r], j = ijk[3 * r + 1], k = ijk[3 * r + 2];
    const long long p = pidx(b, i, j, k);
    const double s = sxyz(b, f, i, j, k) / rho[p];
@@ -160,10 +161,11 @@ __global__ void adj_v_df_kernel(Box b, ProfT<float> f, const float* __restrict__
 
 __global__ void adj_source_df_kernel(Box b, Prof f, int nrec, const int* __restrict__ ijk,
                                      const double* __restrict__ res, const double* __restrict__ rho,
-                                     float* __restrict__ an)
+                                     float* __restrict__ an, const double* __restrict__ clk, int nval)
 {
    const int r = blockIdx.x * blockDim.x + threadIdx.x;
    if (r >= nrec) return;
+   if (clk) res += (long long)clk[2] * nval;
    const int i = ijk[3 * r], j = ijk[3 * r + 1], k = ijk[3 * r + 2];
    const long long p = pidx(b, i, j, k);
    const double s = sxyz(b, f, i, j, k) / rho[p];
@@ -331,7 +333,8 @@ int EW::adjoint_step_mixed(const MixedStage& base, const void* pfv, const void* 
                            size_t n3, const double* u, const double* um, const double* up,
                            const double* un, double* b1, double* b2, double* bn, double* mt,
                            double* w1, double* v1, double* v2, double* gr, double* gm, double* gl,
-                           double dt, double beta, int nrec, const double* res)
+                           double dt, double beta, int nrec, const double* res,
+                           const double* clk, int nval)
 {
    const Prof& pf = *static_cast<const Prof*>(pfv);
    const ProfT<float>& pf32 = *static_cast<const ProfT<float>*>(pf32v);
@@ -381,7 +384,8 @@ int EW::adjoint_step_mixed(const MixedStage& base, const void* pfv, const void* 
    ms.out = F(bn);
    ms.beta = beta;
    SW4G_TRY(launch_mixed_stage(ms, stream_));
-   adj_source_df_kernel<<<blocks_for(nrec, 64), 64, 0, stream_>>>(b, pf, nrec, drec_.ijk, res, rho_, F(bn));
+   adj_source_df_kernel<<<blocks_for(nrec, 64), 64, 0, stream_>>>(b, pf, nrec, drec_.ijk, res, rho_, F(bn),
+                                                                   clk, nval);
    return launch_status();
 }
 
@@ -495,13 +499,11 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       // forward with checkpoints; receivers record from row 0
       rec_rows_ = 0;
       rec_initial_ = true;
-      for (int nn = 0; nn < nsteps; nn++) {
-         if (nn % ckpt == 0) {
-            double* c0 = ck + 2 * (size_t)(nn / ckpt) * n3;
-            SW4G_TRY(cuda_ok(cudaMemcpyAsync(c0, lev_[iu_], lv, cudaMemcpyDeviceToDevice, stream_)));
-            SW4G_TRY(cuda_ok(cudaMemcpyAsync(c0 + n3, lev_[ium_], lv, cudaMemcpyDeviceToDevice, stream_)));
-         }
-         SW4G_TRY(step(1, kModeFused));
+      for (int nn = 0; nn < nsteps; nn += ckpt) {
+         double* c0 = ck + 2 * (size_t)(nn / ckpt) * n3;
+         SW4G_TRY(cuda_ok(cudaMemcpyAsync(c0, lev_[iu_], lv, cudaMemcpyDeviceToDevice, stream_)));
+         SW4G_TRY(cuda_ok(cudaMemcpyAsync(c0 + n3, lev_[ium_], lv, cudaMemcpyDeviceToDevice, stream_)));
+         SW4G_TRY(step(std::min(ckpt, nsteps - nn), kModeFused));  // graphed when graphs are on
       }
       const double t_end = t_;
       double* fin = work + 7 * n3;  // u^N, u^{N-1}: the recompute overwrites the levels
@@ -532,10 +534,10 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       // b^N = W^-1 R g^N
       if (mixed_)
          adj_source_df_kernel<<<blocks_for(drec_.n, 64), 64, 0, stream_>>>(
-             b, pf, drec_.n, drec_.ijk, resd + (size_t)nsteps * nval, rho_, F(b1));
+             b, pf, drec_.n, drec_.ijk, resd + (size_t)nsteps * nval, rho_, F(b1), nullptr, nval);
       else
          adj_source_kernel<<<blocks_for(drec_.n, 64), 64, 0, stream_>>>(
-             b, pf, drec_.n, drec_.ijk, resd + (size_t)nsteps * nval, rho_, b1);
+             b, pf, drec_.n, drec_.ijk, resd + (size_t)nsteps * nval, rho_, b1, nullptr, nval);
       SW4G_TRY(launch_status());
       FusedStage fs;
       fs.b = b;
@@ -556,10 +558,111 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       const bool keep_rec = drec_.n > 0;
       const int saved_n = drec_.n;
       drec_.n = 0;  // no recording while segments are recomputed
+      // one adjoint step nn of the segment starting at s0 (step nn maps u^nn, u^{nn-1}
+      // to u^{nn+1}); with the device clock its residual row is clock[2]
+      auto adj_step = [&](int nn, int s0, double* b1, double* b2, double* bn, bool clocked) -> int {
+         const double* u = seg + (size_t)(nn - s0 + 1) * n3;
+         const double* um = seg + (size_t)(nn - s0) * n3;
+         const double* up = pred + (size_t)(nn - s0) * n3;
+         const double* un = seg + (size_t)(nn - s0 + 2) * n3;
+         const double* clk = clocked ? dclock_ : nullptr;
+         const double* res = clocked ? resd : resd + (size_t)nn * nval;
+         int status = kOk;
+         if (mixed_) {
+            status = adjoint_step_mixed(ms, &pf, &pf32, b, n3, u, um, up, un, b1, b2, bn, mt, w1, v1, v2,
+                                        gr_d, gm_d, gl_d, dt, beta, saved_n, res, clk, nval);
+         } else {
+            adj_w1_kernel<<<gs_blocks(n3, 256), 256, 0, stream_>>>(n3, up, u, um, w1);
+            status = launch_status();
+            if (status == kOk) {  // mt = b1 + dt^2/12 R L(b1): predictor form, um = u
+               fs.corrector = 0;
+               fs.u = b1;
+               fs.um = b1;
+               fs.up = nullptr;
+               fs.out = mt;
+               fs.beta = 0;
+               fs.coef = dt * dt / 12;
+               status = launch_fused_stage(fs, stream_);
+            }
+            if (status == kOk) {
+               adj_v_kernel<<<blocks, 256, 0, stream_>>>(b, pf, b1, mt, dt * dt / 12, dt * dt, v1, v2);
+               status = launch_status();
+            }
+            if (status == kOk) {
+               GradArgs<double> ga;
+               ga.lo = 0;
+               ga.b = b;
+               ga.f = pf;
+               ga.v1 = v1;
+               ga.v2 = v2;
+               ga.rho = rho_;
+               ga.u = u;
+               ga.um = um;
+               ga.up = up;
+               ga.un = un;
+               ga.w1 = w1;
+               ga.gr = gr_d;
+               ga.gm = gm_d;
+               ga.gl = gl_d;
+               ga.c1 = dt * dt / 12;
+               ga.c2 = dt * dt;
+               ga.ih2 = 1 / (g_.h * g_.h);
+               ga.beta = beta;
+               adj_gradient_kernel<double><<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
+               status = launch_status();
+            }
+            if (status == kOk) {  // b^n = 2 b1 - b2 + dt^2 R L(mt) - beta R SG(b1 - b2)
+               fs.corrector = 2;
+               fs.u = b1;
+               fs.um = b2;
+               fs.up = mt;
+               fs.out = bn;
+               fs.beta = beta;
+               fs.coef = dt * dt;
+               status = launch_fused_stage(fs, stream_);
+            }
+            if (status == kOk) {
+               adj_source_kernel<<<blocks_for(saved_n, 64), 64, 0, stream_>>>(
+                   b, pf, saved_n, drec_.ijk, res, rho_, bn, clk, nval);
+               status = launch_status();
+            }
+         }
+         if (status == kOk && clocked) status = launch_clock_advance(dclock_, 0.0, 0.0, -1.0, stream_);
+         return status;
+      };
+      // recompute the segment from its checkpoint: seg[q] = u^{s0-1+q}, pred[q] = up^{s0+q}
+      auto recompute = [&](int s0, int s1) -> int {
+         for (int nn = s0; nn < s1; nn++) {
+            capture_pred_ = pred + (size_t)(nn - s0) * n3;
+            const int status = step_fused();
+            capture_pred_ = nullptr;
+            SW4G_TRY(status);
+            SW4G_TRY(cuda_ok(cudaMemcpyAsync(seg + (size_t)(nn - s0 + 2) * n3, lev_[iu_], lv,
+                                             cudaMemcpyDeviceToDevice, stream_)));
+         }
+         return kOk;
+      };
+      auto rotate = [&]() {
+         double* tmp = b2;
+         b2 = b1;
+         b1 = bn;
+         bn = tmp;
+      };
+      // CUDA graphs of full segments: one recompute graph (every full segment starts
+      // in the same level rotation state) and one adjoint graph per rotation phase
+      // of (b1, b2, bn); the first adjoint segment runs directly
+      cudaGraphExec_t rgraph = nullptr;
+      int r_iu = 0, r_ium = 0;
+      std::vector<std::pair<double*, cudaGraphExec_t>> agraphs;
+      bool adj_warm = false;
       int status = kOk;
       for (int sg = nseg - 1; sg >= 0 && status == kOk; sg--) {
          const int s0 = sg * ckpt, s1 = std::min(nsteps, s0 + ckpt);
-         // recompute the segment: seg[q] = u^{s0-1+q}, pred[q] = up^{s0+q}
+         const bool full = graphs_ && s1 - s0 == ckpt;
+         if (full) {
+            iu_ = 2;
+            ium_ = 3;
+         }
          double* c0 = ck + 2 * (size_t)sg * n3;
          status = cuda_ok(cudaMemcpyAsync(lev_[iu_], c0, lv, cudaMemcpyDeviceToDevice, stream_));
          if (status == kOk)
@@ -567,85 +670,57 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
          if (status == kOk) status = cuda_ok(cudaMemcpyAsync(seg, c0 + n3, lv, cudaMemcpyDeviceToDevice, stream_));
          if (status == kOk) status = cuda_ok(cudaMemcpyAsync(seg + n3, c0, lv, cudaMemcpyDeviceToDevice, stream_));
          t_ = t0 + s0 * dt;
-         for (int nn = s0; nn < s1 && status == kOk; nn++) {
-            capture_pred_ = pred + (size_t)(nn - s0) * n3;
-            status = step(1, kModeFused);
-            capture_pred_ = nullptr;
-            if (status == kOk)
-               status = cuda_ok(cudaMemcpyAsync(seg + (size_t)(nn - s0 + 2) * n3, lev_[iu_], lv,
-                                                cudaMemcpyDeviceToDevice, stream_));
-         }
-         // adjoint steps nn = s1-1 .. s0 (step nn maps u^nn, u^{nn-1} to u^{nn+1})
-         for (int nn = s1 - 1; nn >= s0 && status == kOk; nn--) {
-            const double* u = seg + (size_t)(nn - s0 + 1) * n3;
-            const double* um = seg + (size_t)(nn - s0) * n3;
-            const double* up = pred + (size_t)(nn - s0) * n3;
-            const double* un = seg + (size_t)(nn - s0 + 2) * n3;
-            if (mixed_) {
-               status = adjoint_step_mixed(ms, &pf, &pf32, b, n3, u, um, up, un, b1, b2, bn, mt, w1, v1, v2,
-                                           gr_d, gm_d, gl_d, dt, beta, saved_n, resd + (size_t)nn * nval);
-            } else {
-               adj_w1_kernel<<<gs_blocks(n3, 256), 256, 0, stream_>>>(n3, up, u, um, w1);
-               status = launch_status();
-               if (status == kOk) {  // mt = b1 + dt^2/12 R L(b1): predictor form, um = u
-                  fs.corrector = 0;
-                  fs.u = b1;
-                  fs.um = b1;
-                  fs.up = nullptr;
-                  fs.out = mt;
-                  fs.beta = 0;
-                  fs.coef = dt * dt / 12;
-                  status = launch_fused_stage(fs, stream_);
-               }
-               if (status == kOk) {
-                  adj_v_kernel<<<blocks, 256, 0, stream_>>>(b, pf, b1, mt, dt * dt / 12, dt * dt, v1, v2);
-                  status = launch_status();
-               }
-               if (status == kOk) {
-                  GradArgs<double> ga;
-                  ga.lo = 0;
-                  ga.b = b;
-                  ga.f = pf;
-                  ga.v1 = v1;
-                  ga.v2 = v2;
-                  ga.rho = rho_;
-                  ga.u = u;
-                  ga.um = um;
-                  ga.up = up;
-                  ga.un = un;
-                  ga.w1 = w1;
-                  ga.gr = gr_d;
-                  ga.gm = gm_d;
-                  ga.gl = gl_d;
-                  ga.c1 = dt * dt / 12;
-                  ga.c2 = dt * dt;
-                  ga.ih2 = 1 / (g_.h * g_.h);
-                  ga.beta = beta;
-                  adj_gradient_kernel<double><<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
-                  status = launch_status();
-               }
-               if (status == kOk) {  // b^n = 2 b1 - b2 + dt^2 R L(mt) - beta R SG(b1 - b2)
-                  fs.corrector = 2;
-                  fs.u = b1;
-                  fs.um = b2;
-                  fs.up = mt;
-                  fs.out = bn;
-                  fs.beta = beta;
-                  fs.coef = dt * dt;
-                  status = launch_fused_stage(fs, stream_);
-               }
-               if (status == kOk) {
-                  adj_source_kernel<<<blocks_for(saved_n, 64), 64, 0, stream_>>>(
-                      b, pf, saved_n, drec_.ijk, resd + (size_t)nn * nval, rho_, bn);
-                  status = launch_status();
-               }
+         if (status == kOk && full) {
+            status = sync_clock();
+            clocked_ = true;
+            if (status == kOk && !rgraph) {
+               status = capture([&]() { return recompute(s0, s1); }, &rgraph);
+               r_iu = iu_;
+               r_ium = ium_;
+               if (status == kOk) status = cuda_ok(cudaGraphLaunch(rgraph, stream_));
+            } else if (status == kOk) {
+               status = cuda_ok(cudaGraphLaunch(rgraph, stream_));
+               iu_ = r_iu;
+               ium_ = r_ium;
             }
-            double* tmp = b2;
-            b2 = b1;
-            b1 = bn;
-            bn = tmp;
+            clocked_ = false;
+         } else if (status == kOk) {
+            status = recompute(s0, s1);
+         }
+         if (status != kOk) break;
+         if (full && adj_warm) {
+            status = sync_clock((double)(s1 - 1));
+            cudaGraphExec_t ex = nullptr;
+            for (auto& g : agraphs)
+               if (g.first == b1) ex = g.second;
+            if (status == kOk && !ex) {
+               double* key = b1;
+               status = capture([&]() -> int {
+                  for (int nn = s1 - 1; nn >= s0; nn--) {
+                     SW4G_TRY(adj_step(nn, s0, b1, b2, bn, true));
+                     rotate();
+                  }
+                  return kOk;
+               }, &ex);
+               if (status == kOk) {
+                  agraphs.emplace_back(key, ex);
+                  status = cuda_ok(cudaGraphLaunch(ex, stream_));
+               }
+            } else if (status == kOk) {
+               status = cuda_ok(cudaGraphLaunch(ex, stream_));
+               for (int nn = s1 - 1; nn >= s0; nn--) rotate();
+            }
+         } else {
+            for (int nn = s1 - 1; nn >= s0 && status == kOk; nn--) {
+               status = adj_step(nn, s0, b1, b2, bn, false);
+               rotate();
+            }
+            adj_warm = true;
          }
       }
+      if (rgraph || !agraphs.empty()) cudaStreamSynchronize(stream_);
+      if (rgraph) cudaGraphExecDestroy(rgraph);
+      for (auto& g : agraphs) cudaGraphExecDestroy(g.second);
       drec_.n = keep_rec ? saved_n : 0;
       if (status != kOk) return status;
       // the object ends where the forward run ended

@@ -545,6 +545,11 @@ int sw4g_ew_compute_time_step(sw4g_ew* ew, double cfl, double tmax, double* dt, 
 
 double sw4g_ew_time(const sw4g_ew* ew) { return ew ? ew->impl->time() : 0.0; }
 
+int sw4g_ew_set_graphs(sw4g_ew* ew, int on)
+{
+   return ew ? ew->impl->set_graphs(on != 0) : SW4G_BAD_ARGUMENT;
+}
+
 int sw4g_ew_set_fields(sw4g_ew* ew, const double* u, const double* um, int on_device)
 {
    return ew ? ew->impl->set_fields(u, um, on_device != 0) : SW4G_BAD_ARGUMENT;

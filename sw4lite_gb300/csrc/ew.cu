@@ -19,9 +19,11 @@ EW::EW(const GridSpec& g, cudaStream_t stream, const TopoSpec* topo) : g_(g), st
 
 EW::~EW()
 {
+   drop_graphs();
    auto f = [](void* p) {
       if (p) cudaFree(p);
    };
+   f(dclock_);
    f(rho_);
    f(mu_);
    f(la_);
@@ -206,6 +208,7 @@ int EW::clear_sources()
 int EW::upload_sources()
 {
    if (!src_dirty_) return kOk;
+   drop_graphs();  // the graphs hold the old source list
    std::vector<GridPointSource> src = hsrc_;
    std::vector<int> start;
    group_sources(src, start);
@@ -259,6 +262,7 @@ int EW::upload_sources()
 int EW::set_time_step(double dt, double t0)
 {
    if (!(dt > 0)) return kBadArgument;
+   if (dt != dt_) drop_graphs();
    dt_ = dt;
    t_ = t0;
    return kOk;
@@ -288,6 +292,7 @@ int EW::compute_time_step(double cfl, double tmax, double* dt, int* nsteps)
       ns = ns == 0 ? 1 : ns;
       d = (tmax - t_) / ns;
    }
+   if (d != dt_) drop_graphs();
    dt_ = d;
    if (dt) *dt = d;
    if (nsteps) *nsteps = ns;
@@ -389,28 +394,124 @@ int EW::step(int nsteps, int mode)
       SW4G_TRY(record(lev_[iu_], lev_[ium_], 1));
       rec_initial_ = false;
    }
+   if (mode == kModeFused && graphs_) return run_graphed(nsteps);
    for (int n = 0; n < nsteps; n++) SW4G_TRY(mode == kModePhases ? step_phases() : step_fused());
    return kOk;
 }
 
 int EW::record(double* up, double* um, int initial)
 {
-   double* row = records_ + (size_t)rec_rows_ * rec_nvals_;
+   // with the device clock the kernel takes its row from clock[1]
+   const double* clk = clocked_ ? dclock_ : nullptr;
+   double* row = clk ? records_ : records_ + (size_t)rec_rows_ * rec_nvals_;
    if (mixed_)
       SW4G_TRY(launch_record_df(make_box(1, b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke),
                                 reinterpret_cast<const float*>(up),
                                 reinterpret_cast<const float*>(um), drec_, row, dt_, g_.h, initial,
-                                stream_));
+                                stream_, clk, rec_nvals_));
    else
       SW4G_TRY(launch_record(make_box(1, b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke), up, um, drec_,
-                             row, dt_, g_.h, initial, stream_));
+                             row, dt_, g_.h, initial, stream_, clk, rec_nvals_));
    rec_rows_++;
    return kOk;
+}
+
+int EW::set_graphs(bool on)
+{
+   if (!ready_) return kBadArgument;
+   if (on && !stream_) return kNotSupported;  // no stream capture on the legacy default stream
+   if (on && !dclock_) SW4G_TRY(cuda_ok(cudaMalloc(&dclock_, 4 * sizeof(double))));
+   if (!on) drop_graphs();
+   graphs_ = on;
+   return kOk;
+}
+
+void EW::drop_graphs()
+{
+   if (!graph_cache_.empty()) cudaStreamSynchronize(stream_);
+   for (GraphKey& g : graph_cache_) cudaGraphExecDestroy(g.exec);
+   graph_cache_.clear();
+}
+
+// The device clock from the host's time, record row and (adjoint) residual row.
+int EW::sync_clock(double res_row)
+{
+   const double h[3] = {t_, (double)rec_rows_, res_row};
+   SW4G_TRY(cuda_ok(cudaMemcpyAsync(dclock_, h, sizeof(h), cudaMemcpyHostToDevice, stream_)));
+   return cuda_ok(cudaStreamSynchronize(stream_));  // h lives on this stack frame
+}
+
+int EW::capture(const std::function<int()>& body, cudaGraphExec_t* exec)
+{
+   *exec = nullptr;
+   SW4G_TRY(cuda_ok(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal)));
+   const int st = body();
+   cudaGraph_t g = nullptr;
+   const cudaError_t e = cudaStreamEndCapture(stream_, &g);
+   if (st != kOk || e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      return st != kOk ? st : kCudaError;
+   }
+   const cudaError_t ei = cudaGraphInstantiate(exec, g, 0);
+   cudaGraphDestroy(g);
+   return ei == cudaSuccess ? kOk : kCudaError;
+}
+
+// Fused steps with the device clock; chunks of kGraphSteps steps that start in the
+// level rotation's 3-cycle replay a graph cached by (rotation state, recording), the
+// rest run directly.
+int EW::run_graphed(int nsteps)
+{
+   if (!dclock_) return kBadArgument;
+   if (!warm_ && nsteps > 0) {  // first launches (and their attribute set-up) outside capture
+      SW4G_TRY(step_fused());
+      warm_ = true;
+      nsteps--;
+   }
+   SW4G_TRY(sync_clock());
+   clocked_ = true;
+   auto in_cycle = [&]() {
+      return (iu_ == 2 && ium_ == 3) || (iu_ == 1 && ium_ == 2) || (iu_ == 3 && ium_ == 1);
+   };
+   int st = kOk;
+   while (nsteps > 0 && st == kOk) {
+      if (nsteps >= kGraphSteps && in_cycle() && !capture_pred_) {
+         const int rec = drec_.n > 0 ? 1 : 0;
+         cudaGraphExec_t ex = nullptr;
+         for (const GraphKey& g : graph_cache_)
+            if (g.iu == iu_ && g.ium == ium_ && g.rec == rec) ex = g.exec;
+         if (ex) {
+            st = cuda_ok(cudaGraphLaunch(ex, stream_));
+            for (int q = 0; q < kGraphSteps; q++) {  // the host side of the replayed steps
+               t_ += dt_;
+               rec_rows_ += rec;
+            }
+         } else {
+            const int iu0 = iu_, ium0 = ium_;
+            st = capture([&]() -> int {
+               for (int q = 0; q < kGraphSteps; q++) SW4G_TRY(step_fused());
+               return kOk;
+            }, &ex);
+            if (st == kOk) {
+               graph_cache_.push_back(GraphKey{iu0, ium0, rec, ex});
+               st = cuda_ok(cudaGraphLaunch(ex, stream_));
+            }
+         }
+         nsteps -= kGraphSteps;
+      } else {
+         st = step_fused();
+         nsteps--;
+      }
+   }
+   clocked_ = false;
+   return st;
 }
 
 int EW::set_receivers(int n, const int* ijk, const int* mode, int capacity)
 {
    if (!ready_ || n < 0 || (n > 0 && (!ijk || !mode || capacity < 1))) return kBadArgument;
+   drop_graphs();  // the graphs hold the old receiver set
    std::vector<int> host(5 * (size_t)n);
    int nvals = 0;
    for (int r = 0; r < n; r++) {
@@ -572,7 +673,7 @@ int EW::fused_piece(int piece, int ip, int iq)
    }
    if (piece == 2) {
       SW4G_TRY(launch_force_update(1, bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, up, rho_, dsrc_, t_, 0,
-                                   dt2, stream_));
+                                   dt2, stream_, clocked_ ? dclock_ : nullptr));
       return enforce_bc(up);
    }
    if (piece == 4) {
@@ -595,7 +696,7 @@ int EW::fused_piece(int piece, int ip, int iq)
    }
    if (piece == 5) {
       SW4G_TRY(launch_force_update(1, bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, out, rho_, dsrc_, t_, 1,
-                                   dt2 * dt2 / 12, stream_));
+                                   dt2 * dt2 / 12, stream_, clocked_ ? dclock_ : nullptr));
       return enforce_bc(out);
    }
    return kBadArgument;
@@ -665,7 +766,7 @@ int EW::mixed_piece(int piece, int ip, int iq)
    }
    if (piece == 2) {
       SW4G_TRY(launch_force_update_df(bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, up, rho_, dsrc_, t_,
-                                      0, dt2, stream_));
+                                      0, dt2, stream_, clocked_ ? dclock_ : nullptr));
       return launch_bcfortsg_df(bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, wind_, g_.nx, g_.ny, g_.nz,
                                 up, g_.h, g_.bc, sbop_, mu_, la_, dprof_[3], dprof_[4], stream_);
    }
@@ -685,7 +786,7 @@ int EW::mixed_piece(int piece, int ip, int iq)
    }
    if (piece == 5) {
       SW4G_TRY(launch_force_update_df(bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, out, rho_, dsrc_, t_,
-                                      1, dt2 * dt2 / 12, stream_));
+                                      1, dt2 * dt2 / 12, stream_, clocked_ ? dclock_ : nullptr));
       return launch_bcfortsg_df(bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, wind_, g_.nx, g_.ny, g_.nz,
                                 out, g_.h, g_.bc, sbop_, mu_, la_, dprof_[3], dprof_[4], stream_);
    }
@@ -710,6 +811,7 @@ int EW::step_fused()
       if (which == 5) SW4G_TRY(curv_bc(lev_[iq], cv_->lev[iq]));
    }
    if (drec_.n > 0) SW4G_TRY(record(lev_[iq], lev_[ium_], 0));
+   if (clocked_) SW4G_TRY(launch_clock_advance(dclock_, dt_, drec_.n > 0 ? 1.0 : 0.0, 0.0, stream_));
    ium_ = iu_;
    iu_ = iq;
    t_ += dt_;

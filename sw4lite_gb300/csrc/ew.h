@@ -11,6 +11,7 @@
 
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <memory>
 #include <vector>
 
@@ -91,6 +92,13 @@ class EW {
    double* field_um() const { return lev_[ium_]; }
 
    int step(int nsteps, int mode);
+   // CUDA graphs for the fused time loop: when on, step() replays captured chunks of
+   // kGraphSteps steps (a multiple of the level rotation's period 3) and gradient()
+   // replays its forward chunks, recompute segments and adjoint segments; the forcing
+   // time and the record row then live in a device clock.  Results are bit-identical
+   // to direct launches.
+   int set_graphs(bool on);
+   static constexpr int kGraphSteps = 30;
 
    // Misfit J = 1/2 sum_{n=0..nsteps} |rec^n - obs^n|^2 of the receivers (all in
    // displacement mode) over nsteps fused steps from the current levels, and its
@@ -145,13 +153,21 @@ class EW {
                           size_t n3, const double* u, const double* um, const double* up,
                           const double* un, double* b1, double* b2, double* bn, double* mt,
                           double* w1, double* v1, double* v2, double* gr, double* gm, double* gl,
-                          double dt, double beta, int nrec, const double* res);
+                          double dt, double beta, int nrec, const double* res, const double* clk,
+                          int nval);
    int curv_pred(int ip);
    int curv_corr(int ip, int iq);
    int curv_bc(double* ucart, double* ucurv);
    int curv_time_step(double cfl, double* dt);
    int curv_launches(int mode) const;
    int ensure_phase_arrays();
+   // graphs
+   int sync_clock(double res_row = 0);
+   int run_graphed(int nsteps);
+   void drop_graphs();
+   // records what body() enqueues on the stream as a graph and instantiates it (the
+   // host-side effects of body happen once, at capture)
+   int capture(const std::function<int()>& body, cudaGraphExec_t* exec);
 
    GridSpec g_;
    Bounds b_{};
@@ -202,6 +218,14 @@ class EW {
    double* capture_pred_ = nullptr;  // if set, a fused step copies its predicted level here
 
    double t_ = 0, dt_ = 0;
+
+   bool graphs_ = false, clocked_ = false, warm_ = false;
+   double* dclock_ = nullptr;  // [0] forcing time, [1] record row, [2] adjoint residual row
+   struct GraphKey {
+      int iu, ium, rec;
+      cudaGraphExec_t exec;
+   };
+   std::vector<GraphKey> graph_cache_;
 };
 
 }  // namespace sw4g

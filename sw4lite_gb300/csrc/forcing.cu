@@ -74,10 +74,12 @@ __global__ void force_dense_kernel(Box b, double* __restrict__ f, SourceSet src,
 
 template <typename S>
 __global__ void force_update_kernel(Box b, S* __restrict__ up, const double* __restrict__ rho,
-                                    SourceSet src, double t, int tt, double coef)
+                                    SourceSet src, double t, int tt, double coef,
+                                    const double* __restrict__ clk)
 {
    const int r = blockIdx.x * blockDim.x + threadIdx.x;
    if (r >= src.npoints) return;
+   if (clk) t = clk[0];  // the device clock of a captured time loop
    double acc[3] = {0, 0, 0};
    for (int s = src.start[r]; s < src.start[r + 1]; s++) {
       const double g = timefunc(src.kind[s], src.freq[s], t - src.t0[s], tt != 0);
@@ -96,10 +98,12 @@ __global__ void force_update_kernel(Box b, S* __restrict__ up, const double* __r
 
 // Same as force_update_kernel for a double-float level: the add runs in FP64.
 __global__ void force_update_df_kernel(Box b, DFField up, const double* __restrict__ rho,
-                                       SourceSet src, double t, int tt, double coef)
+                                       SourceSet src, double t, int tt, double coef,
+                                       const double* __restrict__ clk)
 {
    const int r = blockIdx.x * blockDim.x + threadIdx.x;
    if (r >= src.npoints) return;
+   if (clk) t = clk[0];
    double acc[3] = {0, 0, 0};
    for (int s = src.start[r]; s < src.start[r + 1]; s++) {
       const double g = timefunc(src.kind[s], src.freq[s], t - src.t0[s], tt != 0);
@@ -116,16 +120,33 @@ __global__ void force_update_df_kernel(Box b, DFField up, const double* __restri
    }
 }
 
+// The device clock of a captured time loop: [0] time of the next stage's forcing,
+// [1] next record row, [2] residual row of the next adjoint step.
+__global__ void clock_advance_kernel(double* clk, double dt, double drow, double dres)
+{
+   if (threadIdx.x == 0 && blockIdx.x == 0) {
+      clk[0] += dt;
+      clk[1] += drow;
+      clk[2] += dres;
+   }
+}
+
 }  // namespace
+
+int launch_clock_advance(double* clk, double dt, double drow, double dres, cudaStream_t s)
+{
+   clock_advance_kernel<<<1, 32, 0, s>>>(clk, dt, drow, dres);
+   return launch_status();
+}
 
 int launch_force_update_df(int ib, int ie, int jb, int je, int kb, int ke, float* uph,
                            const double* rho, const SourceSet& src, double t, int tt, double coef,
-                           cudaStream_t s)
+                           cudaStream_t s, const double* clk)
 {
    if (src.npoints == 0) return kOk;
    Box b = make_box(1, ib, ie, jb, je, kb, ke);
    force_update_df_kernel<<<blocks_for(src.npoints, 128), 128, 0, s>>>(b, DFField{uph, 3 * b.npts},
-                                                                      rho, src, t, tt, coef);
+                                                                      rho, src, t, tt, coef, clk);
    return launch_status();
 }
 
@@ -141,12 +162,12 @@ int launch_force_dense(int soa, int ib, int ie, int jb, int je, int kb, int ke, 
 
 int launch_force_update(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
                         const double* rho, const SourceSet& src, double t, int tt, double coef,
-                        cudaStream_t s)
+                        cudaStream_t s, const double* clk)
 {
    if (src.npoints == 0) return kOk;
    Box b = make_box(soa, ib, ie, jb, je, kb, ke);
    force_update_kernel<double><<<blocks_for(src.npoints, 128), 128, 0, s>>>(b, up, rho, src, t, tt,
-                                                                            coef);
+                                                                            coef, clk);
    return launch_status();
 }
 
@@ -157,7 +178,7 @@ int launch_force_update_f32(int soa, int ib, int ie, int jb, int je, int kb, int
    if (src.npoints == 0) return kOk;
    Box b = make_box(soa, ib, ie, jb, je, kb, ke);
    force_update_kernel<float><<<blocks_for(src.npoints, 128), 128, 0, s>>>(b, up, rho, src, t, tt,
-                                                                           coef);
+                                                                           coef, nullptr);
    return launch_status();
 }
 

@@ -227,9 +227,11 @@ int launch_curv_eig(int soa, long long n, const double* rho, const double* mu, c
 
 int receiver_values(int mode);  // values one receiver records per step (0: bad mode)
 int launch_record(const Box& b, const double* up, const double* um, const ReceiverSet& r,
-                  double* row, double dt, double h, int initial, cudaStream_t s);
+                  double* row, double dt, double h, int initial, cudaStream_t s,
+                  const double* clk = nullptr, int nvals = 0);
 int launch_record_df(const Box& b, const float* up, const float* um, const ReceiverSet& r,
-                     double* row, double dt, double h, int initial, cudaStream_t s);
+                     double* row, double dt, double h, int initial, cudaStream_t s,
+                  const double* clk = nullptr, int nvals = 0);
 
 int upload_sbp_tables_direct();
 
@@ -263,9 +265,13 @@ int launch_bcfortsg(int soa, int ib, int ie, int jb, int je, int kb, int ke, con
 
 int launch_force_dense(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* f,
                        const SourceSet& src, double t, int tt, cudaStream_t s);
+// clk (optional): the device clock of a captured time loop, [0] the forcing time,
+// [1] the record row, [2] the adjoint residual row (launch_clock_advance adds to each)
+int launch_clock_advance(double* clk, double dt, double drow, double dres, cudaStream_t s);
 int launch_force_update(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
                         const double* rho, const SourceSet& src, double t, int tt, double coef,
-                        cudaStream_t s);
+                        cudaStream_t s,
+                  const double* clk = nullptr);
 int launch_force_update_f32(int soa, int ib, int ie, int jb, int je, int kb, int ke, float* up,
                             const double* rho, const SourceSet& src, double t, int tt,
                             double coef, cudaStream_t s);
@@ -280,7 +286,8 @@ int launch_weights_df(const Box& b, const double* mu, const double* la, const do
                       const double* sy, const double* sz, WeightPtrsDF w, cudaStream_t s);
 int launch_force_update_df(int ib, int ie, int jb, int je, int kb, int ke, float* uph,
                            const double* rho, const SourceSet& src, double t, int tt, double coef,
-                           cudaStream_t s);
+                           cudaStream_t s,
+                  const double* clk = nullptr);
 int launch_ghost_shell_df(const Box& b, int corrector, float* out, const float* u, const float* um,
                           const float* up, cudaStream_t s);
 int launch_uacc_slab_df(const Box& b, int k0, int k1, const float* up, const float* u,

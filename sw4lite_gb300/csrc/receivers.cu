@@ -16,10 +16,12 @@ namespace {
 
 template <class Field>
 __global__ void record_kernel(Box b, Field up, Field um, ReceiverSet r, double* __restrict__ row,
-                              double dt, double inv2h, int initial)
+                              double dt, double inv2h, int initial, const double* __restrict__ clk,
+                              int nvals)
 {
    const int n = blockIdx.x * blockDim.x + threadIdx.x;
    if (n >= r.n) return;
+   if (clk) row += (long long)clk[1] * nvals;  // the row from the device clock
    const int i = r.ijk[3 * n], j = r.ijk[3 * n + 1], k = r.ijk[3 * n + 2];
    double* out = row + r.off[n];
    auto U = [&](int c, int ii, int jj, int kk) { return up.get(cidx(b, c, ii, jj, kk)); };
@@ -80,23 +82,25 @@ int receiver_values(int mode)
 }
 
 int launch_record(const Box& b, const double* up, const double* um, const ReceiverSet& r,
-                  double* row, double dt, double h, int initial, cudaStream_t s)
+                  double* row, double dt, double h, int initial, cudaStream_t s, const double* clk,
+                  int nvals)
 {
    if (r.n == 0) return kOk;
    record_kernel<<<blocks_for(r.n, 64), 64, 0, s>>>(b, F64Field{const_cast<double*>(up)},
                                                     F64Field{const_cast<double*>(um)}, r, row,
-                                                    dt, 1 / (2 * h), initial);
+                                                    dt, 1 / (2 * h), initial, clk, nvals);
    return launch_status();
 }
 
 int launch_record_df(const Box& b, const float* up, const float* um, const ReceiverSet& r,
-                     double* row, double dt, double h, int initial, cudaStream_t s)
+                     double* row, double dt, double h, int initial, cudaStream_t s,
+                     const double* clk, int nvals)
 {
    if (r.n == 0) return kOk;
    const long long lo = 3 * b.npts;
    record_kernel<<<blocks_for(r.n, 64), 64, 0, s>>>(b, DFField{const_cast<float*>(up), lo},
                                                     DFField{const_cast<float*>(um), lo}, r, row,
-                                                    dt, 1 / (2 * h), initial);
+                                                    dt, 1 / (2 * h), initial, clk, nvals);
    return launch_status();
 }
 
