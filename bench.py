@@ -543,6 +543,133 @@ def _time_adjoint(args, sg, torch, stream):
             "forward_value": n ** 3 * N / (fwd_ms * 1e-3), "unit": UNIT}
 
 
+def c5_config(n=256):
+    """Multi-shot workload: the adjoint workload's medium, receivers and source time
+    function, 16 vertical point forces at seeded interior points outside the
+    supergrid layers; observed data are each shot's records in the homogeneous
+    background (FP32-mixed forward)."""
+    cfg = c4_config(n)
+    rng = np.random.default_rng(cfg["seed"] + 100)
+    lo, hi = (cfg["gp"] + 4) * cfg["h"], (n - 5 - cfg["gp"]) * cfg["h"]
+    cfg["shots"] = [tuple(float(x) for x in rng.uniform(lo, hi, size=3)) for _ in range(16)]
+    return cfg
+
+
+def _c5_ew(sg, torch, cfg, stream, nsteps, precision, mat, dt):
+    n, h = cfg["n"], cfg["h"]
+    g = sg.grid_desc(n, n, n, h, bc=(2,) * 6, sg_gp=cfg["gp"], precision=precision)
+    ew = sg.EW(g, stream=stream)
+    ew.set_material(*mat)
+    ew.set_time_step(dt, 0.0)
+    rng = np.random.default_rng(cfg["seed"])
+    rec = [tuple(int(x) for x in rng.integers(cfg["gp"] + 2, n - cfg["gp"], size=3))
+           for _ in range(cfg["nrec"])]
+    ew.set_receivers(rec, [sg.REC_DISPLACEMENT] * len(rec), nsteps + 1)
+    ew.set_graphs(True)
+    return ew
+
+
+def _c5_medium(torch, cfg, homogeneous):
+    n = cfg["n"]
+    shape = (n + 4, n + 4, n + 4)
+    if homogeneous:
+        pr = ps = pv = torch.ones(shape, dtype=torch.float64, device="cuda")
+    else:
+        pr, ps, pv = (_lognormal(torch, shape, cfg["std"], cfg["corr"], cfg["seed"] + q) for q in range(3))
+    rho = cfg["rho"] * pr
+    mu = rho * (cfg["vs"] * ps) ** 2
+    la = rho * (cfg["vp"] * pv) ** 2 - 2 * mu
+    return [a.reshape(-1).contiguous() for a in (rho, mu, la)]
+
+
+def _c5_shot(sg, ew, cfg, s):
+    sc = cfg["src"]
+    x, y, z = cfg["shots"][s]
+    ew.clear_sources()
+    ew.add_source(sg.source_desc(x, y, z, force=sc["force"], freq=sc["freq"], t0=sc["t0"],
+                                 kind=sg.GAUSSIAN))
+
+
+def _time_multishot(args, sg, torch, stream):
+    """C5: the summed misfit gradient of args.ms_shots shots, FP32-mixed (double-float
+    levels, FP32 stencils and gradient terms) with FP64 accumulation, every time loop
+    replayed as CUDA graphs; per-shot time from CUDA events; error of the sum of the
+    first args.ms_err_shots shots against the FP64 gradient of the same shots."""
+    cfg = c5_config(args.adj_n)
+    N, C, S = args.ms_steps, args.adj_ckpt, args.ms_shots
+    n = cfg["n"]
+    with torch.cuda.stream(stream):
+        mat = _c5_medium(torch, cfg, False)
+        dt = cfg["cfl"] * cfg["h"] / float(torch.sqrt(((4 * mat[1] + mat[2]) / mat[0]).max()))
+        # observed data: each shot in the homogeneous background
+        ew0 = _c5_ew(sg, torch, cfg, stream, N, sg.MIXED, _c5_medium(torch, cfg, True), dt)
+        zero = torch.zeros(3 * ew0.npts, dtype=torch.float64, device="cuda")
+        obs = []
+        for s in range(S):
+            _c5_shot(sg, ew0, cfg, s)
+            ew0.set_time_step(dt, 0.0)
+            ew0.set_receivers(*_c5_receivers(cfg), N + 1)
+            ew0.set_fields(zero, zero)
+            ew0.step(N, sg.MODE_FUSED)
+            o = torch.zeros(ew0.record_shape(), dtype=torch.float64, device="cuda")
+            ew0.records(o)
+            obs.append(o)
+        ew0.close()
+        out = {}
+        for prec, nshots in ((sg.MIXED, S), (sg.FP64, min(args.ms_err_shots, S))):
+            if nshots == 0:
+                continue
+            ew = _c5_ew(sg, torch, cfg, stream, N, prec, mat, dt)
+            tot = [torch.zeros(ew.npts, dtype=torch.float64, device="cuda") for _ in range(3)]
+            part = None
+            g = [torch.zeros(ew.npts, dtype=torch.float64, device="cuda") for _ in range(3)]
+            ms = []
+            J = 0.0
+            for s in range(nshots):
+                _c5_shot(sg, ew, cfg, s)
+                ew.set_time_step(dt, 0.0)
+                ew.set_fields(zero, zero)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                J += ew.gradient(N, C, obs[s], *g)
+                for q in range(3):
+                    tot[q] += g[q]  # FP64 accumulation over shots, on the device
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+                if s + 1 == min(args.ms_err_shots, S):
+                    part = [t.clone() for t in tot]
+            ew.close()
+            out[prec] = dict(ms=ms, J=J, tot=tot, part=part)
+        mx = out[sg.MIXED]
+        res = {"workload": f"C5 multi-shot gradient {n}^3, C4 medium, {S} point-force shots, 16 receivers, "
+                           f"{N} steps, checkpoints every {C}, FP32-mixed with FP64 accumulation, "
+                           "time loops as CUDA graphs",
+               "shots": S, "steps": N, "per_shot_ms": sum(mx["ms"]) / len(mx["ms"]),
+               "total_ms": sum(mx["ms"]), "misfit": mx["J"],
+               "grad_norms": [float(x.norm()) for x in mx["tot"]]}
+        if sg.FP64 in out:
+            f64 = out[sg.FP64]
+            res["fp64_per_shot_ms"] = sum(f64["ms"]) / len(f64["ms"])
+            res["error_vs_fp64"] = {
+                "shots": len(f64["ms"]),
+                "l2_rel": [float((a - b).norm() / b.norm()) for a, b in zip(mx["part"], f64["tot"])],
+                "linf_rel": [float((a - b).abs().max() / b.abs().max()) for a, b in zip(mx["part"], f64["tot"])],
+                "against": "sum of the FP64 gradients of the same shots (rho, mu, lambda)"}
+        del out
+        torch.cuda.empty_cache()
+    return res
+
+
+def _c5_receivers(cfg):
+    n = cfg["n"]
+    rng = np.random.default_rng(cfg["seed"])
+    rec = [tuple(int(x) for x in rng.integers(cfg["gp"] + 2, n - cfg["gp"], size=3))
+           for _ in range(cfg["nrec"])]
+    import sw4lite_gb300 as sg
+    return rec, [sg.REC_DISPLACEMENT] * len(rec)
+
+
 RECEIVER_SEED = 20240611
 
 
@@ -646,6 +773,7 @@ def run_ours(args, rank, world):
         if not args.no_err and args.topo_err_steps > 0:
             topo_mixed["error"] = _topo_mixed_error(args, sg, torch, stream, args.topo_err_steps)
     adj = None if args.no_adjoint else _time_adjoint(args, sg, torch, stream)
+    multishot = None if args.no_multishot else _time_multishot(args, sg, torch, stream)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -688,6 +816,7 @@ def run_ours(args, rank, world):
             "topography": topo,
             "topography_mixed": topo_mixed,
             "adjoint": adj,
+            "multishot": multishot,
         }
         print(json.dumps(line), flush=True)
     return 0
@@ -716,6 +845,11 @@ def main():
     ap.add_argument("--adj-n", type=int, default=256, help="grid of the adjoint workload")
     ap.add_argument("--adj-steps", type=int, default=200, help="steps of the adjoint workload")
     ap.add_argument("--adj-ckpt", type=int, default=100, help="checkpoint spacing")
+    ap.add_argument("--no-multishot", action="store_true", help="skip the multi-shot gradient workload")
+    ap.add_argument("--ms-shots", type=int, default=16, help="shots of the multi-shot workload")
+    ap.add_argument("--ms-steps", type=int, default=150, help="steps of the multi-shot workload")
+    ap.add_argument("--ms-err-shots", type=int, default=2,
+                    help="shots whose summed gradient is compared with FP64 (0: skip)")
     ap.add_argument("--only-topo", choices=["fp64", "mixed"], default=None,
                     help="time only the topography workload in that form (for profiling)")
     ap.add_argument("--no-err", action="store_true", help="skip the mixed-vs-FP64 error run")

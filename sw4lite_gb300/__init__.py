@@ -283,6 +283,9 @@ class EW:
                                                    t0.ctypes.data_as(_D), kind.ctypes.data_as(_I)),
               "add_grid_point_sources")
 
+    def clear_sources(self):
+        check(lib().sw4g_ew_clear_sources(self._h), "clear_sources")
+
     def num_grid_point_sources(self) -> int:
         return lib().sw4g_ew_num_grid_point_sources(self._h)
 
