@@ -196,7 +196,79 @@ struct GradArgs {
    T c1, c2;  // v1 = c1 W b1 (pair with w1), v2 = c2 W mt (pair with u)
    T ih2, beta;
    long long lo;  // offset of the levels' lo halves (float only)
+   T* ed;         // edge products, 12 x npts (adj_edge_kernel)
 };
+
+// The forward edges (p, p+1) and (p, p+2) along ax of the second differences'
+// edge form, summed over the two pairs (v1, w1), (v2, u) and the three components
+// with the mu weights (2 for c == ax, else 1) and the lambda weights (c == ax only):
+// e = {EM1, EL1, EM2, EL2}.  Values beyond the array are zero; p may lie one or two
+// points below the array along ax (then only its in-array neighbours are read).
+template <class T>
+__device__ __forceinline__ void edges_at(const GradArgs<T>& g, int ax, const int pc[3], long long p,
+                                         T e[4])
+{
+   const Box& b = g.b;
+   const long long n = b.npts;
+   const long long st = ax == 0 ? 1 : ax == 1 ? b.ni : b.nij;
+   const int lo = ax == 0 ? b.ib : ax == 1 ? b.jb : b.kb, hi = ax == 0 ? b.ie : ax == 1 ? b.je : b.ke;
+   bool ok[3];
+   T sv[3];
+#pragma unroll
+   for (int m = 0; m < 3; m++) {
+      const int x = pc[ax] + m;
+      ok[m] = x >= lo && x <= hi;
+      sv[m] = ok[m] ? g.f.st[ax][x - lo] : T(0);
+   }
+   e[0] = e[1] = e[2] = e[3] = 0;
+#pragma unroll
+   for (int t = 0; t < 2; t++) {
+      const T* vb = t == 0 ? g.v1 : g.v2;
+      const T* wf = t == 0 ? g.w1 : g.u;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+         T v[3], w[3];
+#pragma unroll
+         for (int m = 0; m < 3; m++) {
+            if (!ok[m]) {
+               v[m] = w[m] = 0;
+               continue;
+            }
+            const long long q = c * n + p + m * st;
+            v[m] = sv[m] * vb[q];
+            w[m] = wf[q];
+         }
+         const T e1 = (v[1] - v[0]) * (w[1] - w[0]), e2 = (v[2] - v[0]) * (w[2] - w[0]);
+         if (c == ax) {
+            e[0] += 2 * e1;
+            e[1] += e1;
+            e[2] += 2 * e2;
+            e[3] += e2;
+         } else {
+            e[0] += e1;
+            e[2] += e2;
+         }
+      }
+   }
+}
+
+template <class T>
+__global__ void __launch_bounds__(128) adj_edge_kernel(GradArgs<T> g)
+{
+   const long long n = g.b.npts;
+   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+        p += (long long)gridDim.x * blockDim.x) {
+      int pc[3];
+      grid_point(g.b, p, pc[0], pc[1], pc[2]);
+#pragma unroll
+      for (int ax = 0; ax < 3; ax++) {
+         T e[4];
+         edges_at(g, ax, pc, p, e);
+#pragma unroll
+         for (int r = 0; r < 4; r++) g.ed[(ax * 4 + r) * n + p] = e[r];
+      }
+   }
+}
 
 // gradient of a1 . u+ at every array point (one thread per point)
 template <class T>
@@ -211,64 +283,64 @@ __global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs<T> g)
       int pc[3];
       grid_point(b, p, pc[0], pc[1], pc[2]);
       T gm = 0, gl = 0, gr = 0;
+      // same-axis second differences: the seven edges of each axis around p
+#pragma unroll
+      for (int ax = 0; ax < 3; ax++) {
+         T E[4][4];  // edges starting at p-2 .. p+1: {EM1, EL1, EM2, EL2}
+#pragma unroll
+         for (int m = -2; m <= 1; m++) {
+            const int x = pc[ax] + m;
+            if (x > hi[ax]) {
+               E[m + 2][0] = E[m + 2][1] = E[m + 2][2] = E[m + 2][3] = 0;
+            } else if (x >= lo[ax]) {
+#pragma unroll
+               for (int r = 0; r < 4; r++) E[m + 2][r] = g.ed[(ax * 4 + r) * n + p + m * st[ax]];
+            } else {  // an edge from below the array (ghost-point gradients)
+               int qc[3] = {pc[0], pc[1], pc[2]};
+               qc[ax] = x;
+               edges_at(g, ax, qc, p + m * st[ax], E[m + 2]);
+            }
+         }
+         const T s = -g.ih2 / T(6) * g.f.st[ax][pc[ax] - lo[ax]];
+#pragma unroll
+         for (int r = 0; r < 2; r++)  // r = 0: mu, 1: lambda
+         {
+            const T val = E[3][r] + E[0][r] + T(3) * (E[1][r] + E[2][r]) + E[1][2 + r] -
+                          T(0.75) * (E[2][2 + r] + E[0][2 + r]);
+            if (r == 0) gm += s * val;
+            else gl += s * val;
+         }
+      }
+      // mixed terms: -(1/144h^2) s_ai(p) (DW . w_d along ai)(p) (DW . (s_ao v_c) along ao)(p),
+      // each first difference computed once per pair
 #pragma unroll
       for (int t = 0; t < 2; t++) {
          const T* vb = t == 0 ? g.v1 : g.v2;
          const T* wf = t == 0 ? g.w1 : g.u;
-         // same-axis second differences in edge form
+         T din[3][3], dout[3][3];
 #pragma unroll
-         for (int ax = 0; ax < 3; ax++) {
-            T sv[5];  // s_ax along the axis (0 beyond the array)
-            bool ok[5];
-#pragma unroll
-            for (int m = -2; m <= 2; m++) {
-               const int x = pc[ax] + m;
-               ok[m + 2] = x >= lo[ax] && x <= hi[ax];
-               sv[m + 2] = ok[m + 2] ? g.f.st[ax][x - lo[ax]] : T(0);
-            }
+         for (int a = 0; a < 3; a++) {
+            const bool inner_ok = pc[a] >= lo[a] + 2 && pc[a] <= hi[a] - 2;
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-               T v[5], w[5];
+               T si = 0, so = 0;
 #pragma unroll
                for (int m = -2; m <= 2; m++) {
-                  if (!ok[m + 2]) {
-                     v[m + 2] = w[m + 2] = 0;
-                     continue;
-                  }
-                  const long long q = c * n + p + m * st[ax];
-                  v[m + 2] = sv[m + 2] * vb[q];
-                  w[m + 2] = wf[q];
+                  if (m == 0) continue;
+                  if (inner_ok) si += T(kDW[m + 2]) * wf[c * n + p + m * st[a]];
+                  const int x = pc[a] + m;
+                  if (x < lo[a] || x > hi[a]) continue;
+                  so += T(kDW[m + 2]) * g.f.st[a][x - lo[a]] * vb[c * n + p + m * st[a]];
                }
-               const T e1m2 = (v[1] - v[0]) * (w[1] - w[0]), e1m1 = (v[2] - v[1]) * (w[2] - w[1]);
-               const T e10 = (v[3] - v[2]) * (w[3] - w[2]), e1p1 = (v[4] - v[3]) * (w[4] - w[3]);
-               const T e2m2 = (v[2] - v[0]) * (w[2] - w[0]), e2m1 = (v[3] - v[1]) * (w[3] - w[1]);
-               const T e20 = (v[4] - v[2]) * (w[4] - w[2]);
-               const T val = -g.ih2 / T(6) * sv[2] *
-                             (e1p1 + e1m2 + T(3) * (e1m1 + e10) + e2m1 - T(0.75) * (e20 + e2m2));
-               if (c == ax) {
-                  gm += 2 * val;
-                  gl += val;
-               } else {
-                  gm += val;
-               }
+               din[c][a] = si;
+               dout[c][a] = so;
             }
          }
-         // mixed terms: -(1/144h^2) s_ai(p) (DW . w_d along ai)(p) (DW . (s_ao v_c) along ao)(p)
 #pragma unroll
          for (int e = 0; e < 12; e++) {
             const int c = kMix[e][0], d = kMix[e][1], ao = kMix[e][2], ai = kMix[e][3];
             if (pc[ai] < lo[ai] + 2 || pc[ai] > hi[ai] - 2) continue;
-            T inner = 0, outer = 0;
-#pragma unroll
-            for (int m = -2; m <= 2; m++) {
-               if (m == 0) continue;
-               inner += T(kDW[m + 2]) * wf[d * n + p + m * st[ai]];
-               int oc[3] = {pc[0], pc[1], pc[2]};
-               oc[ao] += m;
-               if (oc[ao] < lo[ao] || oc[ao] > hi[ao]) continue;
-               outer += T(kDW[m + 2]) * g.f.st[ao][oc[ao] - lo[ao]] * vb[c * n + p + m * st[ao]];
-            }
-            const T gg = -g.ih2 / T(144) * g.f.st[ai][pc[ai] - lo[ai]] * inner * outer;
+            const T gg = -g.ih2 / T(144) * g.f.st[ai][pc[ai] - lo[ai]] * din[d][ai] * dout[c][ao];
             if (kMix[e][4]) gl += gg;
             else gm += gg;
          }
@@ -374,6 +446,9 @@ int EW::adjoint_step_mixed(const MixedStage& base, const void* pfv, const void* 
    ga.ih2 = (float)(1 / (g_.h * g_.h));
    ga.beta = (float)beta;
    ga.lo = 3 * npts_;
+   ga.ed = reinterpret_cast<float*>(adj_edges_);
+   adj_edge_kernel<float><<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
+   SW4G_TRY(launch_status());
    adj_gradient_kernel<float><<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
    SW4G_TRY(launch_status());
    ms = base;  // b^n = 2 b1 - b2 + dt^2 R L(mt) - beta R SG(b1 - b2): adjoint form
@@ -430,6 +505,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
    if (st == kOk) st = alloc(&pred, (size_t)seglen * lv);
    if (st == kOk) st = alloc(&work, 9 * lv);  // adjoint work (7) + the forward's final levels (2)
    if (st == kOk) st = alloc(&resd, (size_t)(nsteps + 1) * nval * sizeof(double));
+   if (st == kOk) st = alloc(&adj_edges_, 12 * (size_t)npts_ * sizeof(double));
    double* gr_d = g_rho;
    double* gm_d = g_mu;
    double* gl_d = g_la;
@@ -443,6 +519,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
    auto cleanup = [&]() {
       cudaStreamSynchronize(stream_);
       for (double* p : bufs) cudaFree(p);
+      adj_edges_ = nullptr;
    };
    if (st != kOk) {
       cleanup();
@@ -608,8 +685,13 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
                ga.c2 = dt * dt;
                ga.ih2 = 1 / (g_.h * g_.h);
                ga.beta = beta;
-               adj_gradient_kernel<double><<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
+               ga.ed = adj_edges_;
+               adj_edge_kernel<double><<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
                status = launch_status();
+               if (status == kOk) {
+                  adj_gradient_kernel<double><<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
+                  status = launch_status();
+               }
             }
             if (status == kOk) {  // b^n = 2 b1 - b2 + dt^2 R L(mt) - beta R SG(b1 - b2)
                fs.corrector = 2;

@@ -216,6 +216,7 @@ class EW {
 
    std::unique_ptr<CurvGrid> cv_;
    double* capture_pred_ = nullptr;  // if set, a fused step copies its predicted level here
+   double* adj_edges_ = nullptr;     // gradient(): edge products of the adjoint step
 
    double t_ = 0, dt_ = 0;
 
