@@ -195,6 +195,7 @@ struct GradArgs {
    double* gl;
    T c1, c2;  // v1 = c1 W b1 (pair with w1), v2 = c2 W mt (pair with u)
    T ih2, beta;
+   T k6, k144, ic1, ic2, bc1;  // -ih2/6, -ih2/144, 1/c1, 1/c2, beta/c1 (set by grad_constants)
    long long lo;  // offset of the levels' lo halves (float only)
    T* ed;         // edge products, 12 x npts (adj_edge_kernel)
 };
@@ -253,6 +254,16 @@ __device__ __forceinline__ void edges_at(const GradArgs<T>& g, int ax, const int
 }
 
 template <class T>
+void grad_constants(GradArgs<T>& g)
+{
+   g.k6 = -g.ih2 / T(6);
+   g.k144 = -g.ih2 / T(144);
+   g.ic1 = T(1) / g.c1;
+   g.ic2 = T(1) / g.c2;
+   g.bc1 = g.beta / g.c1;
+}
+
+template <class T>
 __global__ void __launch_bounds__(128) adj_edge_kernel(GradArgs<T> g)
 {
    const long long n = g.b.npts;
@@ -301,7 +312,7 @@ __global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs<T> g)
                edges_at(g, ax, qc, p + m * st[ax], E[m + 2]);
             }
          }
-         const T s = -g.ih2 / T(6) * g.f.st[ax][pc[ax] - lo[ax]];
+         const T s = g.k6 * g.f.st[ax][pc[ax] - lo[ax]];
 #pragma unroll
          for (int r = 0; r < 2; r++)  // r = 0: mu, 1: lambda
          {
@@ -312,7 +323,15 @@ __global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs<T> g)
          }
       }
       // mixed terms: -(1/144h^2) s_ai(p) (DW . w_d along ai)(p) (DW . (s_ao v_c) along ao)(p),
-      // each first difference computed once per pair
+      // each first difference computed once per pair; ws = DW x s along each axis
+      T ws[3][5];
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+         for (int m = -2; m <= 2; m++) {
+            const int x = pc[a] + m;
+            ws[a][m + 2] = (m == 0 || x < lo[a] || x > hi[a]) ? T(0) : T(kDW[m + 2]) * g.f.st[a][x - lo[a]];
+         }
 #pragma unroll
       for (int t = 0; t < 2; t++) {
          const T* vb = t == 0 ? g.v1 : g.v2;
@@ -330,7 +349,7 @@ __global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs<T> g)
                   if (inner_ok) si += T(kDW[m + 2]) * wf[c * n + p + m * st[a]];
                   const int x = pc[a] + m;
                   if (x < lo[a] || x > hi[a]) continue;
-                  so += T(kDW[m + 2]) * g.f.st[a][x - lo[a]] * vb[c * n + p + m * st[a]];
+                  so += ws[a][m + 2] * vb[c * n + p + m * st[a]];
                }
                din[c][a] = si;
                dout[c][a] = so;
@@ -340,7 +359,7 @@ __global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs<T> g)
          for (int e = 0; e < 12; e++) {
             const int c = kMix[e][0], d = kMix[e][1], ao = kMix[e][2], ai = kMix[e][3];
             if (pc[ai] < lo[ai] + 2 || pc[ai] > hi[ai] - 2) continue;
-            const T gg = -g.ih2 / T(144) * g.f.st[ai][pc[ai] - lo[ai]] * din[d][ai] * dout[c][ao];
+            const T gg = g.k144 * g.f.st[ai][pc[ai] - lo[ai]] * din[d][ai] * dout[c][ao];
             if (kMix[e][4]) gl += gg;
             else gm += gg;
          }
@@ -355,7 +374,7 @@ __global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs<T> g)
             s2 += g.v2[q] * g.w1[q];
             s1 += g.v1[q] * lev_diff(g.un, g.up, q, g.lo);
          }
-         gr -= s2 / g.c2 + s1 / g.c1;
+         gr -= s2 * g.ic2 + s1 * g.ic1;
       }
       if (g.beta != 0) {
          T sgr = 0;
@@ -382,7 +401,7 @@ __global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs<T> g)
                sgr += dcp * (dd[2] - 2 * dd[1] + dd[0]) * (vv[2] - 2 * vv[1] + vv[0]);
             }
          }
-         gr -= g.beta / g.c1 * sgr;  // vv holds c1 W b1
+         gr -= g.bc1 * sgr;  // vv holds c1 W b1
       }
       g.gm[p] += (double)gm;
       g.gl[p] += (double)gl;
@@ -447,6 +466,7 @@ int EW::adjoint_step_mixed(const MixedStage& base, const void* pfv, const void* 
    ga.beta = (float)beta;
    ga.lo = 3 * npts_;
    ga.ed = reinterpret_cast<float*>(adj_edges_);
+   grad_constants(ga);
    adj_edge_kernel<float><<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
    SW4G_TRY(launch_status());
    adj_gradient_kernel<float><<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
@@ -686,6 +706,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
                ga.ih2 = 1 / (g_.h * g_.h);
                ga.beta = beta;
                ga.ed = adj_edges_;
+               grad_constants(ga);
                adj_edge_kernel<double><<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
                status = launch_status();
                if (status == kOk) {
