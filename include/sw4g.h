@@ -322,10 +322,23 @@ typedef struct sw4g_topography {
  * Cartesian grid g (grid 0), whose bc[4] must be SW4G_BC_INTERFACE.  The
  * curvilinear grid has g's nx, ny and nz = 1 + round((zmin - z_avg)/h) points,
  * z_avg the midpoint of the topography's z range (src/EW.C:2039-2044).  FP64,
- * 4th-order damping; sources must lie in the Cartesian grid.  SW4G_BAD_ARGUMENT
+ * 4th-order damping; sources anywhere below the topography.  SW4G_BAD_ARGUMENT
  * if the grid folds (topography too steep for h). */
 #define SW4G_BC_INTERFACE 4
 int sw4g_ew_create_topo(const sw4g_grid* g, const sw4g_topography* t, void* stream, sw4g_ew** out);
+/* Grid-point sources of one source on the two grids of g and t (the curvilinear grid:
+ * nzc planes, Jacobian jac over its array with 2 ghost points per side, host), as
+ * Source::set_grid_point_sources4 with the curvilinear branches (src/Source.C:1074-1990):
+ * at or above the interface the source goes to the curvilinear grid, below it to the
+ * Cartesian grid, and a stencil that reaches across the interface is split.  Up to
+ * cap entries per grid; the counts come back in *ncart, *ncurv.  SW4G_BAD_ARGUMENT
+ * for a source above the topography. */
+int sw4g_discretize_source_topo(const sw4g_grid* g, const sw4g_topography* t, int nzc,
+                                const double* jac, const sw4g_source* s, int cap, int* cart_ijk,
+                                double* cart_amp, int* ncart, int* curv_ijk, double* curv_amp,
+                                int* ncurv);
+/* The grid-point sources an EW object holds for grid 0 or 1 (host copy, up to cap). */
+int sw4g_ew_grid_point_sources(const sw4g_ew* ew, int grid, int cap, int* ijk, double* amp, int* n);
 /* 1, or 2 with topography */
 int sw4g_ew_num_grids(const sw4g_ew* ew);
 int sw4g_ew_grid_dims(const sw4g_ew* ew, int grid, int* nx, int* ny, int* nz, long long* npts);

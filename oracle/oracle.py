@@ -269,7 +269,8 @@ class Curv(C.Structure):
                 ("nz", C.c_int), ("h", C.c_double), ("bccnd", C.c_int * 6),
                 ("wind", C.c_int * 36), ("rho", _D), ("mu", _D), ("la", _D), ("met", _D),
                 ("jac", _D), ("strx", _D), ("stry", _D), ("dcx", _D), ("dcy", _D), ("cox", _D),
-                ("coy", _D)]
+                ("coy", _D), ("nsrc", C.c_int), ("src_ijk", _I), ("src_amp", _D),
+                ("src_freq", _D), ("src_t0", _D), ("src_kind", _I)]
 
 
 def step_topo(problem: Problem, curv: Curv, t, cart_arrays, curv_arrays, which="oracle"):

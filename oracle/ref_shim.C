@@ -339,7 +339,8 @@ void sw4ref_step_topo(const sw4o_problem* p, const sw4o_curv* cv, double t, doub
    };
    sw4o_force(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, f, p->nsrc, p->src_ijk, p->src_amp,
               p->src_freq, p->src_t0, p->src_kind, t, 0);
-   std::memset(cf, 0, 3 * cnpts * sizeof(double));
+   sw4o_force(1, cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cf, cv->nsrc, cv->src_ijk,
+              cv->src_amp, cv->src_freq, cv->src_t0, cv->src_kind, t, 0);
    std::memset(lu, 0, 3 * npts * sizeof(double));
    std::memset(clu, 0, 3 * cnpts * sizeof(double));
    rhs4sg_rev(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, p->nz, onesided, acof, bope, ghcof, lu,
@@ -353,6 +354,8 @@ void sw4ref_step_topo(const sw4o_problem* p, const sw4o_curv* cv, double t, doub
    bc(up, cup);
    sw4o_force(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, f, p->nsrc, p->src_ijk, p->src_amp,
               p->src_freq, p->src_t0, p->src_kind, t, 1);
+   sw4o_force(1, cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cf, cv->nsrc, cv->src_ijk,
+              cv->src_amp, cv->src_freq, cv->src_t0, cv->src_kind, t, 1);
    ew->dpdmtfort(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, D(u), D(um), uacc, 1.0 / (dt * dt));
    ew->dpdmtfort(cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cup, D(cu), D(cum), cuacc,
                  1.0 / (dt * dt));

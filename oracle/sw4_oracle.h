@@ -154,6 +154,11 @@ typedef struct {
    int wind[36];
    const double *rho, *mu, *la, *met, *jac;
    const double *strx, *stry, *dcx, *dcy, *cox, *coy;
+   /* grid-point sources of the curvilinear grid (as sw4o_problem's) */
+   int nsrc;
+   const int* src_ijk;
+   const double *src_amp, *src_freq, *src_t0;
+   const int* src_kind;
 } sw4o_curv;
 
 /* cart: arrays up, u, um, lu, f, uacc of the Cartesian grid; c*: the curvilinear

@@ -586,7 +586,8 @@ void sw4o_step_topo(const sw4o_problem* p, const sw4o_curv* cv, double t, double
    const long cnpts = (long)(cv->ie - cv->ib + 1) * (cv->je - cv->jb + 1) * (cv->ke - cv->kb + 1);
    const double dt = p->dt;
    const int onesided_c[6] = {0, 0, 0, 0, cv->bccnd[4] == 0, 0};
-   memset(cf, 0, 3 * cnpts * sizeof(double));
+   sw4o_force(1, cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cf, cv->nsrc, cv->src_ijk,
+              cv->src_amp, cv->src_freq, cv->src_t0, cv->src_kind, t, 0);
 
    sw4o_force(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, f, p->nsrc, p->src_ijk, p->src_amp,
               p->src_freq, p->src_t0, p->src_kind, t, 0);
@@ -603,6 +604,8 @@ void sw4o_step_topo(const sw4o_problem* p, const sw4o_curv* cv, double t, double
 
    sw4o_force(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, f, p->nsrc, p->src_ijk, p->src_amp,
               p->src_freq, p->src_t0, p->src_kind, t, 1);
+   sw4o_force(1, cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cf, cv->nsrc, cv->src_ijk,
+              cv->src_amp, cv->src_freq, cv->src_t0, cv->src_kind, t, 1);
    sw4o_dpdmtfort(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, u, um, uacc, 1.0 / (dt * dt));
    sw4o_dpdmtfort(cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cup, cu, cum, cuacc, 1.0 / (dt * dt));
    sw4o_rhs4sg(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, p->nz, p->onesided, acof, bope, ghcof,

@@ -105,6 +105,8 @@ _SIGS = {
     "sw4g_ew_compute_time_step": ([_VP, C.c_double, C.c_double, _D, _I], C.c_int),
     "sw4g_ew_time": ([_VP], C.c_double),
     "sw4g_ew_set_graphs": ([_VP, C.c_int], C.c_int),
+    "sw4g_discretize_source_topo": ([_VP, _VP, C.c_int, _D, _VP, C.c_int, _I, _D, _I, _I, _D, _I], C.c_int),
+    "sw4g_ew_grid_point_sources": ([_VP, C.c_int, C.c_int, _I, _D, _I], C.c_int),
     "sw4g_ew_set_fields": ([_VP, _VP, _VP, C.c_int], C.c_int),
     "sw4g_ew_get_fields": ([_VP, _VP, _VP, C.c_int], C.c_int),
     "sw4g_ew_field": ([_VP, C.c_int], _VP),
@@ -283,6 +285,19 @@ class EW:
                                                    t0.ctypes.data_as(_D), kind.ctypes.data_as(_I)),
               "add_grid_point_sources")
 
+    def grid_point_sources(self, grid=0):
+        """(ijk, amp) of the discretised grid-point sources of grid 0 or 1."""
+        import numpy as np
+        n = C.c_int()
+        check(lib().sw4g_ew_grid_point_sources(self._h, grid, 0, None, None, C.byref(n)),
+              "grid_point_sources")
+        ijk = np.zeros(3 * max(n.value, 1), dtype=np.int32)
+        amp = np.zeros(3 * max(n.value, 1))
+        check(lib().sw4g_ew_grid_point_sources(self._h, grid, n.value, ijk.ctypes.data_as(_I),
+                                               amp.ctypes.data_as(_D), C.byref(n)),
+              "grid_point_sources")
+        return ijk[:3 * n.value].reshape(-1, 3), amp[:3 * n.value].reshape(-1, 3)
+
     def clear_sources(self):
         check(lib().sw4g_ew_clear_sources(self._h), "clear_sources")
 
@@ -416,6 +431,25 @@ class EW:
         ms = (C.c_double * 4)()
         check(lib().sw4g_ew_profile_kernels(self._h, nrep, ms), "profile_kernels")
         return dict(pred_stage=ms[0], corr_stage=ms[1], rows=ms[2], bc_force=ms[3])
+
+
+def discretize_source_topo(g, topo, nzc, jac, src):
+    """Grid-point sources of `src` on the two grids of g (bc[4] = INTERFACE) and the
+    topography `topo` with nzc curvilinear planes and curvilinear Jacobian `jac`
+    (host, full array).  Returns ((ijk, amp) of grid 0, (ijk, amp) of grid 1)."""
+    import numpy as np
+    cap = 4096
+    jac = np.ascontiguousarray(jac, dtype=np.float64)
+    a_ijk, b_ijk = np.zeros(3 * cap, dtype=np.int32), np.zeros(3 * cap, dtype=np.int32)
+    a_amp, b_amp = np.zeros(3 * cap), np.zeros(3 * cap)
+    na, nb = C.c_int(), C.c_int()
+    check(lib().sw4g_discretize_source_topo(C.byref(g), C.byref(topo), nzc, jac.ctypes.data_as(_D),
+                                            C.byref(src), cap, a_ijk.ctypes.data_as(_I),
+                                            a_amp.ctypes.data_as(_D), C.byref(na),
+                                            b_ijk.ctypes.data_as(_I), b_amp.ctypes.data_as(_D),
+                                            C.byref(nb)), "discretize_source_topo")
+    return ((a_ijk[:3 * na.value].reshape(-1, 3), a_amp[:3 * na.value].reshape(-1, 3)),
+            (b_ijk[:3 * nb.value].reshape(-1, 3), b_amp[:3 * nb.value].reshape(-1, 3)))
 
 
 def nearest_grid_point(g, x, y, z):

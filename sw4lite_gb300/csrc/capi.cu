@@ -377,6 +377,63 @@ int sw4g_discretize_source(const sw4g_grid* g, const sw4g_source* s, int cap, in
    return SW4G_OK;
 }
 
+namespace {
+void copy_sources(const std::vector<GridPointSource>& v, int cap, int* ijk, double* amp, int* n)
+{
+   *n = (int)v.size();
+   for (int q = 0; q < (int)v.size() && q < cap; q++) {
+      ijk[3 * q] = v[q].i;
+      ijk[3 * q + 1] = v[q].j;
+      ijk[3 * q + 2] = v[q].k;
+      for (int c = 0; c < 3; c++) amp[3 * q + c] = v[q].amp[c];
+   }
+}
+}  // namespace
+
+int sw4g_discretize_source_topo(const sw4g_grid* g, const sw4g_topography* t, int nzc,
+                                const double* jac, const sw4g_source* s, int cap, int* cart_ijk,
+                                double* cart_amp, int* ncart, int* curv_ijk, double* curv_amp,
+                                int* ncurv)
+{
+   if (!g || !t || !jac || !s || !ncart || !ncurv || cap < 0 || nzc < 8 ||
+       (cap > 0 && (!cart_ijk || !cart_amp || !curv_ijk || !curv_amp)))
+      return SW4G_BAD_ARGUMENT;
+   const GridSpec spec = to_spec(g);
+   int onesided[6];
+   onesided_flags(spec, onesided);
+   CurvSourceGrid cs;
+   cs.nz = nzc;
+   cs.zmax = spec.zmin;
+   cs.amp = t->amp;
+   cs.xc = t->xc;
+   cs.yc = t->yc;
+   cs.lx = t->lx;
+   cs.ly = t->ly;
+   cs.zeta_break = t->zeta_break;
+   cs.order = t->order;
+   cs.jac = jac;
+   cs.ib = -1;
+   cs.jb = -1;
+   cs.kb = -1;
+   cs.ni = spec.nx + 4;
+   cs.nij = cs.ni * (spec.ny + 4);
+   std::vector<GridPointSource> cart, curv;
+   if (discretize_source_topo(spec, onesided, &cs, to_source(s), cart, curv) != 0) return SW4G_BAD_ARGUMENT;
+   copy_sources(cart, cap, cart_ijk, cart_amp, ncart);
+   copy_sources(curv, cap, curv_ijk, curv_amp, ncurv);
+   return SW4G_OK;
+}
+
+int sw4g_ew_grid_point_sources(const sw4g_ew* ew, int grid, int cap, int* ijk, double* amp, int* n)
+{
+   if (!ew || !n || cap < 0 || (cap > 0 && (!ijk || !amp))) return SW4G_BAD_ARGUMENT;
+   std::vector<GridPointSource> v;
+   const int st = ew->impl->grid_point_sources(grid, &v);
+   if (st != SW4G_OK) return st;
+   copy_sources(v, cap, ijk, amp, n);
+   return SW4G_OK;
+}
+
 int sw4g_ew_create(const sw4g_grid* g, void* stream, sw4g_ew** out)
 {
    if (!g || !out) return SW4G_BAD_ARGUMENT;

@@ -38,6 +38,7 @@ EW::~EW()
    f(zc_[0]);
    f(zc_[1]);
    f(dsrc_mem_);
+   f(dsrc_curv_mem_);
    f(drec_mem_);
    f(records_);
    f(rho32_);
@@ -170,8 +171,13 @@ int EW::add_source(const SourceSpec& s)
 {
    if (!ready_) return kBadArgument;
    if (s.kind < 0 || s.kind > 3 || !(s.freq > 0)) return kBadArgument;
-   if (cv_ && s.z < g_.zmin) return kNotSupported;  // sources in the curvilinear grid: not built
-   discretize_source(g_, onesided_, s, hsrc_);
+   if (cv_) {
+      // two grids: the source may go to either, or straddle the interface
+      const CurvSourceGrid cs = curv_source_grid();
+      if (discretize_source_topo(g_, onesided_, &cs, s, hsrc_, hsrc_curv_) != 0) return kBadArgument;
+   } else {
+      discretize_source(g_, onesided_, s, hsrc_);
+   }
    src_dirty_ = true;
    return kOk;
 }
@@ -201,29 +207,27 @@ int EW::add_grid_point_sources(int n, const int* ijk, const double* amp, const d
 int EW::clear_sources()
 {
    hsrc_.clear();
+   hsrc_curv_.clear();
    src_dirty_ = true;
    return kOk;
 }
 
-int EW::upload_sources()
+namespace {
+// One device block per source set: start | ijk | kind | amp | freq | t0 (ints first,
+// then doubles, 8-aligned).
+int pack_sources(std::vector<GridPointSource> src, SourceSet& ds, void*& mem)
 {
-   if (!src_dirty_) return kOk;
-   drop_graphs();  // the graphs hold the old source list
-   std::vector<GridPointSource> src = hsrc_;
    std::vector<int> start;
    group_sources(src, start);
    const int ns = (int)src.size(), np = (int)start.size() - 1;
-   // one block: start | ijk | kind | amp | freq | t0   (ints first, then doubles, 8-aligned)
    const size_t ints = (size_t)(np + 1) + 3 * (size_t)ns + ns;
    const size_t int_bytes = ((ints * sizeof(int) + 7) / 8) * 8;
    const size_t bytes = int_bytes + (5 * (size_t)ns) * sizeof(double);
-   if (dsrc_mem_) {
-      SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
-      cudaFree(dsrc_mem_);
-      dsrc_mem_ = nullptr;
+   if (mem) {
+      cudaFree(mem);
+      mem = nullptr;
    }
-   dsrc_ = SourceSet{};
-   src_dirty_ = false;
+   ds = SourceSet{};
    if (ns == 0) return kOk;
    std::vector<unsigned char> host(bytes, 0);
    int* hi = reinterpret_cast<int*>(host.data());
@@ -243,19 +247,37 @@ int EW::upload_sources()
       hfreq[s] = src[s].freq;
       ht0[s] = src[s].t0;
    }
-   SW4G_TRY(cuda_ok(cudaMalloc(&dsrc_mem_, bytes)));
-   SW4G_TRY(cuda_ok(cudaMemcpy(dsrc_mem_, host.data(), bytes, cudaMemcpyHostToDevice)));
-   unsigned char* base = static_cast<unsigned char*>(dsrc_mem_);
+   SW4G_TRY(cuda_ok(cudaMalloc(&mem, bytes)));
+   SW4G_TRY(cuda_ok(cudaMemcpy(mem, host.data(), bytes, cudaMemcpyHostToDevice)));
+   unsigned char* base = static_cast<unsigned char*>(mem);
    const int* di = reinterpret_cast<const int*>(base);
    const double* dd = reinterpret_cast<const double*>(base + int_bytes);
-   dsrc_.npoints = np;
-   dsrc_.nsources = ns;
-   dsrc_.start = di;
-   dsrc_.ijk = di + np + 1;
-   dsrc_.kind = di + np + 1 + 3 * ns;
-   dsrc_.amp = dd;
-   dsrc_.freq = dd + 3 * ns;
-   dsrc_.t0 = dd + 4 * ns;
+   ds.npoints = np;
+   ds.nsources = ns;
+   ds.start = di;
+   ds.ijk = di + np + 1;
+   ds.kind = di + np + 1 + 3 * ns;
+   ds.amp = dd;
+   ds.freq = dd + 3 * ns;
+   ds.t0 = dd + 4 * ns;
+   return kOk;
+}
+}  // namespace
+
+int EW::upload_sources()
+{
+   if (!src_dirty_) return kOk;
+   drop_graphs();  // the graphs hold the old source list
+   if (dsrc_mem_ || dsrc_curv_mem_) SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
+   src_dirty_ = false;
+   SW4G_TRY(pack_sources(hsrc_, dsrc_, dsrc_mem_));
+   return pack_sources(hsrc_curv_, dsrc_curv_, dsrc_curv_mem_);
+}
+
+int EW::grid_point_sources(int grid, std::vector<GridPointSource>* out) const
+{
+   if (grid < 0 || grid >= num_grids() || !out) return kBadArgument;
+   *out = grid == 0 ? hsrc_ : hsrc_curv_;
    return kOk;
 }
 

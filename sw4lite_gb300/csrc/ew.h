@@ -46,6 +46,7 @@ struct CurvGrid {
    CurvCoef cc{};
    float* coefdf = nullptr;  // the mixed form's (hi, lo) coefficients (curv_mixed.cu)
    double* topscr = nullptr;  // work array of the SBP top rows, 36 doubles per column
+   std::vector<double> hjac;  // host copy of the Jacobian (source discretisation)
    CurvCoefDF cd{};
    bool material = false;
    ~CurvGrid();
@@ -79,6 +80,8 @@ class EW {
                               const double* t0, const int* kind);
    int clear_sources();
    int num_grid_point_sources() const { return (int)hsrc_.size(); }
+   // the discretised grid-point sources of grid 0 (Cartesian) or 1 (curvilinear)
+   int grid_point_sources(int grid, std::vector<GridPointSource>* out) const;
    // Time step: explicit dt, or computed from the CFL number and an end time.
    int set_time_step(double dt, double t0);
    int compute_time_step(double cfl, double tmax, double* dt, int* nsteps);
@@ -160,6 +163,8 @@ class EW {
    int curv_bc(double* ucart, double* ucurv);
    int curv_time_step(double cfl, double* dt);
    int curv_launches(int mode) const;
+   int curv_force(double* lev, int tt, double coef);
+   CurvSourceGrid curv_source_grid() const;
    int ensure_phase_arrays();
    // graphs
    int sync_clock(double res_row = 0);
@@ -204,6 +209,9 @@ class EW {
    long long slab_len_ = 0;
 
    std::vector<GridPointSource> hsrc_;
+   std::vector<GridPointSource> hsrc_curv_;  // sources of the curvilinear grid
+   SourceSet dsrc_curv_{};
+   void* dsrc_curv_mem_ = nullptr;
    bool src_dirty_ = true;
    SourceSet dsrc_{};
    void* dsrc_mem_ = nullptr;

@@ -110,7 +110,45 @@ int EW::init_topo()
    if (st == kOk) st = cuda_ok(cudaStreamSynchronize(stream_));
    cudaFree(flag);
    if (st != kOk) return st;
-   return bad ? kBadArgument : kOk;  // the grid folds (z_r <= 0): topography too steep for h
+   if (bad) return kBadArgument;  // the grid folds (z_r <= 0): topography too steep for h
+   c.hjac.resize(n);
+   return cuda_ok(cudaMemcpy(c.hjac.data(), c.jac, n * sizeof(double), cudaMemcpyDeviceToHost));
+}
+
+CurvSourceGrid EW::curv_source_grid() const
+{
+   const CurvGrid& c = *cv_;
+   CurvSourceGrid cs;
+   cs.nz = c.nz;
+   cs.zmax = g_.zmin;
+   cs.amp = c.topo.amp;
+   cs.xc = c.topo.xc;
+   cs.yc = c.topo.yc;
+   cs.lx = c.topo.lx;
+   cs.ly = c.topo.ly;
+   cs.zeta_break = c.topo.zeta_break;
+   cs.order = c.topo.order;
+   cs.jac = c.hjac.data();
+   cs.ib = c.b.ib;
+   cs.jb = c.b.jb;
+   cs.kb = c.b.kb;
+   cs.ni = c.b.ie - c.b.ib + 1;
+   cs.nij = cs.ni * (c.b.je - c.b.jb + 1);
+   return cs;
+}
+
+// Grid-point sources of the curvilinear grid into one of its levels (the reference
+// adds F to every grid's predictor and corrector, src/EW.C:2537-2756).
+int EW::curv_force(double* lev, int tt, double coef)
+{
+   if (dsrc_curv_.npoints == 0) return kOk;
+   const Bounds& b = cv_->b;
+   const double* clk = clocked_ ? dclock_ : nullptr;
+   if (mixed_)
+      return launch_force_update_df(b.ib, b.ie, b.jb, b.je, b.kb, b.ke, reinterpret_cast<float*>(lev),
+                                    cv_->rho, dsrc_curv_, t_, tt, coef, stream_, clk);
+   return launch_force_update(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, lev, cv_->rho, dsrc_curv_, t_, tt,
+                              coef, stream_, clk);
 }
 
 int EW::grid_dims(int grid, int* nx, int* ny, int* nz, long long* npts) const
@@ -269,7 +307,8 @@ int EW::curv_pred(int ip)
       st.um = df(c.lev[ium_]);
       st.out = df(c.lev[ip]);
       st.work1 = c.uacc;
-      return launch_curv_stage_df(st, stream_);
+      SW4G_TRY(launch_curv_stage_df(st, stream_));
+      return curv_force(c.lev[ip], 0, dt_ * dt_);
    }
    // fused: the stage kernel (rows 7..nz), the top-row kernel (rows 1..6) and the
    // ghost shell
@@ -281,7 +320,8 @@ int EW::curv_pred(int ip)
    st.out = c.lev[ip];
    st.f = c.lev[iu_];
    st.fbox = st.b;
-   return launch_curv_stage(st, stream_);
+   SW4G_TRY(launch_curv_stage(st, stream_));
+   return curv_force(c.lev[ip], 0, dt_ * dt_);
 }
 
 int EW::curv_corr(int ip, int iq)
@@ -300,7 +340,8 @@ int EW::curv_corr(int ip, int iq)
       st.out = df(c.lev[iq]);
       st.work1 = c.uacc;
       st.work2 = c.lu;
-      return launch_curv_stage_df(st, stream_);
+      SW4G_TRY(launch_curv_stage_df(st, stream_));
+      return curv_force(c.lev[iq], 1, dt * dt * dt * dt / 12);
    }
    if (ip != iq) {
       // fused: the corrector reads level ip and writes level iq; the top rows read
@@ -316,7 +357,8 @@ int EW::curv_corr(int ip, int iq)
       st.out = c.lev[iq];
       st.f = c.uacc;
       st.fbox = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, 8);
-      return launch_curv_stage(st, stream_);
+      SW4G_TRY(launch_curv_stage(st, stream_));
+      return curv_force(c.lev[iq], 1, dt * dt * dt * dt / 12);
    }
    // phase order (in place): the reference's kernel sequence
    const int onesided[6] = {0, 0, 0, 0, 1, 0};
@@ -326,6 +368,7 @@ int EW::curv_corr(int ip, int iq)
    SW4G_TRY(launch_rhs4sgcurv(curv_spec(c, c.uacc, dprof_[3], dprof_[4]), onesided, c.lu, stream_));
    SW4G_TRY(launch_corrfort(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, up, c.lu, c.fzero, c.rho,
                             dt * dt * dt * dt, stream_));
+   SW4G_TRY(curv_force(up, 1, dt * dt * dt * dt / 12));
    if (prof_.used && g_.sg_damping != 0)
       SW4G_TRY(launch_addsgd4c(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, up, u, um, c.rho, dprof_[0],
                                dprof_[1], dprof_[3], dprof_[4], c.jac, dprof_[6], dprof_[7],
@@ -393,7 +436,8 @@ int EW::curv_launches(int mode) const
    // adds the slab of u - um); phase order dpdm, two operator kernels, corrfort,
    // damping
    const int corr = mode == kModeFused ? (mixed_ ? 6 : 5) : 4 + (damp ? 1 : 0);
-   return pred + corr + 2 * bc;
+   const int force = hsrc_curv_.empty() ? 0 : 2;
+   return pred + corr + 2 * bc + force;
 }
 
 }  // namespace sw4g

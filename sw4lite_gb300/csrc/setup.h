@@ -4,6 +4,7 @@
 // once before time stepping and is O(N^2) or less.
 #pragma once
 
+#include <cmath>
 #include <vector>
 
 namespace sw4g {
@@ -78,6 +79,36 @@ struct GridPointSource {
 // normalisation near one-sided boundaries.
 void discretize_source(const GridSpec& g, const int onesided[6], const SourceSpec& s,
                        std::vector<GridPointSource>& out);
+
+// The curvilinear grid of a two-grid set-up as the source discretisation sees it:
+// nz planes from the surface (k = 1) to the interface (k = nz, z = zmax), a Gaussian
+// hill elevation, the grid mapping's grading (zeta_break, order) and a host copy of
+// its Jacobian over the array (bounds ib.., jb.., kb..).
+struct CurvSourceGrid {
+   int nz = 0;
+   double zmax = 0;
+   double amp = 0, xc = 0, yc = 0, lx = 1, ly = 1, zeta_break = 0.95;
+   int order = 4;
+   const double* jac = nullptr;
+   int ib = 0, jb = 0, kb = 0;
+   long long ni = 0, nij = 0;
+   double elevation(double x, double y) const
+   {
+      return amp * std::exp(-((x - xc) / lx) * ((x - xc) / lx) - ((y - yc) / ly) * ((y - yc) / ly));
+   }
+   double J(int i, int j, int k) const { return jac[(i - ib) + ni * (j - jb) + nij * (long long)(k - kb)]; }
+};
+
+// Two-grid source discretisation (src/Source.C:1074-1990 with the curvilinear
+// branches): the source goes to the curvilinear grid at or above the interface
+// (s from the inverted grid mapping, weights divided by the Jacobian, the moment
+// source's z-derivative through the mapping's metric at the source) or to the
+// Cartesian grid below it; a stencil that reaches across the interface is split
+// between the grids.  cv == nullptr: one Cartesian grid.  Returns 0, 1 if the
+// source lies above the topography, 2 if the mapping cannot be inverted there.
+int discretize_source_topo(const GridSpec& g, const int onesided[6], const CurvSourceGrid* cv,
+                           const SourceSpec& s, std::vector<GridPointSource>& cart,
+                           std::vector<GridPointSource>& curv);
 
 // Sort grid-point sources by point and build the per-point groups
 // (src/EW.C:6370-6433).  start has npoints+1 entries.

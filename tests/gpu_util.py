@@ -115,6 +115,7 @@ class OracleProblem:
         P.dcx, P.strx, P.cox = [dp(a) for a in prof[0]]
         P.dcy, P.stry, P.coy = [dp(a) for a in prof[1]]
         P.dcz, P.strz, P.coz = [dp(a) for a in prof[2]]
+        self.P = P
         ijk, amp, freq, t0, kind = [], [], [], [], []
         for src in sources:
             a, b = discretize(grid, src)
@@ -124,19 +125,24 @@ class OracleProblem:
             freq += [src.freq] * n
             t0 += [src.t0] * n
             kind += [src.kind] * n
-        self.src = (np.ascontiguousarray(np.concatenate(ijk) if ijk else np.zeros(0), dtype=np.int32),
-                    np.ascontiguousarray(np.concatenate(amp) if amp else np.zeros(0)),
+        self.set_grid_point_sources(np.concatenate(ijk) if ijk else np.zeros(0),
+                                    np.concatenate(amp) if amp else np.zeros(0), freq, t0, kind)
+        self.npts = (nx + 4) * (ny + 4) * (nz + 4)
+
+    def set_grid_point_sources(self, ijk, amp, freq, t0, kind):
+        """Grid-point sources (flat ijk and amp, 3 per source) of this problem."""
+        self.src = (np.ascontiguousarray(ijk, dtype=np.int32).reshape(-1),
+                    np.ascontiguousarray(amp, dtype=np.float64).reshape(-1),
                     np.asarray(freq, dtype=np.float64), np.asarray(t0, dtype=np.float64),
                     np.asarray(kind, dtype=np.int32))
         self.keep += list(self.src)
-        P.nsrc = len(freq)
+        P = self.P
+        P.nsrc = len(self.src[2])
         P.src_ijk = self.src[0].ctypes.data_as(O._I)
         P.src_amp = self.src[1].ctypes.data_as(O._D)
         P.src_freq = self.src[2].ctypes.data_as(O._D)
         P.src_t0 = self.src[3].ctypes.data_as(O._D)
         P.src_kind = self.src[4].ctypes.data_as(O._I)
-        self.P = P
-        self.npts = (nx + 4) * (ny + 4) * (nz + 4)
 
     def run(self, u, um, t0, nsteps, which="oracle", receivers=None):
         """nsteps oracle steps from (u, um); with receivers [(ijk, mode), ...] also

@@ -110,8 +110,10 @@ def test_topo_time_step_and_bad_inputs():
     assert n * dt == pytest.approx(0.5, rel=1e-14)
     raw = c.time_step(1.3)
     assert dt <= raw * (1 + 1e-12) and n == int(0.5 / raw + 0.5)
-    with pytest.raises(sg.Sw4gError):  # a source above the Cartesian grid
-        ew.add_source(sg.source_desc(1.0, 1.0, 0.5, force=(1.0, 0, 0)))
+    ew.add_source(sg.source_desc(1.0, 1.0, 0.5, force=(1.0, 0, 0)))  # in the curvilinear grid
+    assert len(ew.grid_point_sources(1)[0]) > 0
+    with pytest.raises(sg.Sw4gError):  # above the topography (the hill top is at z = -0.2)
+        ew.add_source(sg.source_desc(1.4, 1.3, -0.5, force=(1.0, 0, 0)))
     ew.close()
     g = sg.grid_desc(c.nx, c.ny, c.ncart, c.h, bc=(2, 2, 2, 2, 0, 2), zmin=1.0)
     with pytest.raises(sg.Sw4gError):  # top side must be the interface
@@ -150,3 +152,28 @@ def test_mixed_topo_close_to_fp64(nsteps, tol):
     with pytest.raises(sg.Sw4gError):
         ew.step(1, sg.MODE_PHASES)
     ew.close()
+
+
+@pytest.mark.parametrize("mode", [sg.MODE_FUSED, sg.MODE_PHASES])
+def test_topo_steps_with_curvilinear_sources(mode):
+    # a point force and a moment tensor under the hill in the curvilinear grid, a
+    # force just below the interface (its stencil reaches into the curvilinear grid)
+    # and one just above it (split into the Cartesian grid)
+    nx, ny, ncart, h = 30, 28, 22, 0.1
+    src = [sg.source_desc(1.37, 1.21, -0.05, force=(1.0, -0.5, 0.3), freq=8.0, t0=0.1),
+           sg.source_desc(1.52, 1.33, 0.35, moment=(1.0, 0.2, -0.3, 0.7, 0.1, -0.5), freq=6.0,
+                          kind=sg.C6SMOOTHBUMP),
+           sg.source_desc(1.20, 1.50, 1.04, force=(0.2, 0.4, -1.0), freq=7.0, t0=0.12),
+           sg.source_desc(1.60, 1.10, 0.96, force=(-0.6, 0.3, 0.8), freq=7.0, t0=0.08)]
+    c = TopoCase(nx, ny, ncart, h, zmax_topo=1.0, amp=0.2, xc=1.4, yc=1.3, lx=0.6, ly=0.5,
+                 gp=5, sources=src)
+    dt = c.time_step(1.3)
+    fields = smooth_topo_fields(c, seed=8)
+    ref = c.oracle(dt).run(*fields, 0.0, 8)
+    got, _ = _gpu(c, fields, dt, 8, mode)
+    for a, b in zip(got, ref):
+        assert _rel(a, b) <= 1e-12
+    # the sources change the curvilinear field (not a vacuous check)
+    quiet = TopoCase(nx, ny, ncart, h, zmax_topo=1.0, amp=0.2, xc=1.4, yc=1.3, lx=0.6, ly=0.5, gp=5)
+    base = quiet.oracle(dt).run(*fields, 0.0, 8)
+    assert _rel(ref[2], base[2]) > 1e-3
