@@ -386,22 +386,6 @@ __global__ void __launch_bounds__(NTHREADS, 2) curv_mixed_kernel(MArgs a)
    }
 }
 
-// out = a (- b) in FP64 over planes k0..k1 of double-float levels (component-major
-// slab of 3 x nij x (k1 - k0 + 1) values)
-__global__ void df_slab_kernel(Box bx, int k0, int k1, const float* __restrict__ a,
-                               const float* __restrict__ bsub, double* __restrict__ out)
-{
-   const long long nslab = bx.nij * (k1 - k0 + 1), lo = 3 * bx.npts;
-   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < 3 * nslab;
-        q += (long long)gridDim.x * blockDim.x) {
-      const int c = (int)(q / nslab);
-      const long long p = q % nslab + bx.nij * (long long)(k0 - bx.kb) + c * bx.npts;
-      double v = (double)a[p] + (double)a[p + lo];
-      if (bsub) v -= (double)bsub[p] + (double)bsub[p + lo];
-      out[q] = v;
-   }
-}
-
 int gsb(long long n)
 {
    long long g = (n + 255) / 256;
@@ -445,15 +429,12 @@ int launch_curv_stage_df(const CurvStageDF& st, cudaStream_t s)
    CurvStageDF t = st;
    t.fbox = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, 8);
    t.f = st.work1;
-   const long long nslab = 3 * b.nij * (8 - b.kb + 1);
    if (corr) {
       SW4G_TRY(launch_uacc_slab_df(b, b.kb, 8, st.up, st.u, st.um, st.work1, s));
-      df_slab_kernel<<<gsb(nslab), 256, 0, s>>>(b, b.kb, 8, st.u, st.um, st.work2);
-      SW4G_TRY(launch_status());
+      SW4G_TRY(launch_df_slab(b, b.kb, 8, st.u, st.um, st.work2, s));
       t.dd = st.work2;
    } else {
-      df_slab_kernel<<<gsb(nslab), 256, 0, s>>>(b, b.kb, 8, st.u, nullptr, st.work1);
-      SW4G_TRY(launch_status());
+      SW4G_TRY(launch_df_slab(b, b.kb, 8, st.u, nullptr, st.work1, s));
    }
    // the ghost shell, then the SBP top rows k = 1..6 in FP64
    SW4G_TRY(launch_ghost_shell_df(b, corr, st.out, st.u, st.um, st.up, s));

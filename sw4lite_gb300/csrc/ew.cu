@@ -120,8 +120,8 @@ int EW::init()
    // (top) or nz-7..ke (bottom)
    const long long nij = (long long)len[0] * len[1];
    slab_len_ = 3 * nij * 10;
-   if (onesided_[4] || onesided_[5])
-      SW4G_TRY(cuda_ok(cudaMalloc(&slab_, 2 * slab_len_ * sizeof(double))));
+   if (onesided_[4] || onesided_[5])  // the mixed form also keeps u - um slabs
+      SW4G_TRY(cuda_ok(cudaMalloc(&slab_, (mixed_ ? 4 : 2) * slab_len_ * sizeof(double))));
    {
       const Box bx = make_box(1, b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke);
       for (int side = 0; side < 2; side++)
@@ -779,11 +779,17 @@ int EW::mixed_piece(int piece, int ip, int iq)
    }
    if (piece == 1) {
       SW4G_TRY(launch_ghost_shell_df(b, 0, up, u, um, nullptr, stream_));
-      for (int side = 0; side < 2; side++)
-         if (onesided_[4 + side])
-            SW4G_TRY(launch_stage_rows_df(0, side == 0, b, nz, nullptr, u, b, mu_, la_, g_.h, st[0],
-                                          st[1], st[2], u, um, nullptr, up, rho_, irho_, dt2, 0.0,
-                                          dc, st, co, zc_[side], stream_));
+      for (int side = 0; side < 2; side++) {
+         if (!onesided_[4 + side]) continue;
+         // the stage field as an FP64 slab: one conversion per value
+         const int k0 = side == 0 ? bd.kb : nz - 7, k1 = side == 0 ? 8 : bd.ke;
+         double* slab = slab_ + side * slab_len_;
+         SW4G_TRY(launch_df_slab(b, k0, k1, u, nullptr, slab, stream_));
+         Box sb = make_box(1, bd.ib, bd.ie, bd.jb, bd.je, k0, k1);
+         SW4G_TRY(launch_stage_rows_df(0, side == 0, b, nz, slab, nullptr, sb, mu_, la_, g_.h, st[0],
+                                       st[1], st[2], u, um, nullptr, up, rho_, irho_, dt2, 0.0, dc,
+                                       st, co, zc_[side], stream_));
+      }
       return kOk;
    }
    if (piece == 2) {
@@ -798,11 +804,13 @@ int EW::mixed_piece(int piece, int ip, int iq)
          if (!onesided_[4 + side]) continue;
          const int k0 = side == 0 ? bd.kb : nz - 7, k1 = side == 0 ? 8 : bd.ke;
          double* slab = slab_ + side * slab_len_;
+         double* dslab = slab_ + (2 + side) * slab_len_;  // u - um for the damping
          SW4G_TRY(launch_uacc_slab_df(b, k0, k1, up, u, um, slab, stream_));
+         if (beta != 0) SW4G_TRY(launch_df_slab(b, k0, k1, u, um, dslab, stream_));
          Box sb = make_box(1, bd.ib, bd.ie, bd.jb, bd.je, k0, k1);
          SW4G_TRY(launch_stage_rows_df(1, side == 0, b, nz, slab, nullptr, sb, mu_, la_, g_.h, st[0],
                                        st[1], st[2], u, um, up, out, rho_, irho_, dt2 / 12, beta,
-                                       dc, st, co, zc_[side], stream_));
+                                       dc, st, co, zc_[side], stream_, beta != 0 ? dslab : nullptr));
       }
       return kOk;
    }
@@ -889,8 +897,10 @@ int EW::launches_per_step(int mode) const
       return 2 * (1 + src) + 2 * rhs + 3 + (damp ? 1 : 0) + 2 * bc + rec + curv_launches(mode);
    }
    // per stage: stage kernel, ghost shell, one-sided rows, forcing, BC sides;
-   // the corrector adds the rows' slab kernels (and 6th-order damping)
-   return 2 * (2 + rows + src + bc) + rows + (damp && g_.sg_order == 6 ? 1 : 0) + rec +
+   // the corrector adds the rows' slab kernels (and 6th-order damping); the mixed
+   // form adds an FP64 slab of the predictor's field and of the corrector's u - um
+   const int mslabs = mixed_ ? rows * (1 + (damp ? 1 : 0)) : 0;
+   return 2 * (2 + rows + src + bc) + rows + (damp && g_.sg_order == 6 ? 1 : 0) + rec + mslabs +
           curv_launches(mode);
 }
 

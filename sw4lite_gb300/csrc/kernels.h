@@ -290,6 +290,9 @@ int launch_force_update_df(int ib, int ie, int jb, int je, int kb, int ke, float
                   const double* clk = nullptr);
 int launch_ghost_shell_df(const Box& b, int corrector, float* out, const float* u, const float* um,
                           const float* up, cudaStream_t s);
+// out = a (- bsub) in FP64 over planes k0..k1 of double-float levels of box b
+int launch_df_slab(const Box& b, int k0, int k1, const float* a, const float* bsub, double* out,
+                   cudaStream_t s);
 int launch_uacc_slab_df(const Box& b, int k0, int k1, const float* up, const float* u,
                         const float* um, double* out, cudaStream_t s);
 int launch_bcfortsg_df(int ib, int ie, int jb, int je, int kb, int ke, const int wind[36], int nx,
@@ -302,7 +305,8 @@ int launch_stage_rows_df(int corrector, bool top, const Box& b, int nz, const do
                          const double* strz, const float* u, const float* um, const float* up,
                          float* out, const double* rho, const double* irho, double coef,
                          double beta, const double* const dc[3], const double* const st[3],
-                         const double* const co[3], const double* zc, cudaStream_t stream);
+                         const double* const co[3], const double* zc, cudaStream_t stream,
+                         const double* dd = nullptr);
 
 int launch_weights(const Box& b, const double* mu, const double* la, const double* sx,
                    const double* sy, const double* sz, double h, WeightPtrs w, cudaStream_t s);

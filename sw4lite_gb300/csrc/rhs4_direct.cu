@@ -257,6 +257,9 @@ struct RowUpdate {
    const float* __restrict__ updf;
    float* __restrict__ outdf;
    long long lo;
+   // optional FP64 slab of u - um (box ddb) read by the damping instead of u, um
+   const double* __restrict__ dd;
+   Box ddb;
    const double* __restrict__ irho;
    const double* __restrict__ rho;
    double coef;  // dt^2 (predictor) or dt^2/12 (corrector)
@@ -284,6 +287,10 @@ __device__ __forceinline__ double sg4_point(const Box& b, const RowUpdate& w, in
       double d[5];
 #pragma unroll
       for (int m = -2; m <= 2; m++) {
+         if (w.dd) {
+            d[m + 2] = __ldg(w.dd + cidx(w.ddb, c, i + di * m, j + dj * m, k + dk * m));
+            continue;
+         }
          const long long q = cidx(b, c, i + di * m, j + dj * m, k + dk * m);
          d[m + 2] = lvl<DF>(w.u, w.udf, q, w.lo) - lvl<DF>(w.um, w.umdf, q, w.lo);
       }
@@ -426,6 +433,7 @@ int launch_stage_rows(int corrector, bool top, const Box& b, int nk, const doubl
    w.udf = w.umdf = w.updf = nullptr;
    w.outdf = nullptr;
    w.lo = 0;
+   w.dd = nullptr;
    a.udf = nullptr;
    w.corrector = corrector;
    w.u = u;
@@ -457,7 +465,8 @@ int launch_stage_rows_df(int corrector, bool top, const Box& b, int nz, const do
                          const double* strz, const float* u, const float* um, const float* up,
                          float* out, const double* rho, const double* irho, double coef,
                          double beta, const double* const dc[3], const double* const st[3],
-                         const double* const co[3], const double* zc, cudaStream_t stream)
+                         const double* const co[3], const double* zc, cudaStream_t stream,
+                         const double* dd)
 {
    int status = upload_sbp_tables_direct();
    if (status != kOk) return status;
@@ -484,6 +493,8 @@ int launch_stage_rows_df(int corrector, bool top, const Box& b, int nz, const do
    w.updf = up;
    w.outdf = out;
    w.lo = 3 * b.npts;
+   w.dd = dd;
+   w.ddb = field_box;
    w.irho = irho;
    w.rho = rho;
    w.coef = coef;

@@ -488,6 +488,22 @@ __global__ void uacc_slab_df_kernel(Box b, int k0, int k1, DFField up, DFField u
    }
 }
 
+// out = a (- b) in FP64 over planes k0..k1 of double-float levels (a
+// component-major slab of 3 x nij x (k1 - k0 + 1) values)
+__global__ void df_slab_kernel(Box bx, int k0, int k1, const float* __restrict__ a,
+                               const float* __restrict__ bsub, double* __restrict__ out)
+{
+   const long long nslab = bx.nij * (k1 - k0 + 1), lo = 3 * bx.npts;
+   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < 3 * nslab;
+        q += (long long)gridDim.x * blockDim.x) {
+      const int c = (int)(q / nslab);
+      const long long p = q % nslab + bx.nij * (long long)(k0 - bx.kb) + c * bx.npts;
+      double v = (double)a[p] + (double)a[p + lo];
+      if (bsub) v -= (double)bsub[p] + (double)bsub[p + lo];
+      out[q] = v;
+   }
+}
+
 int grid_stride_blocks(long long n)
 {
    long long g = (n + 255) / 256;
@@ -515,6 +531,14 @@ int launch_uacc_slab(const Box& b, int k0, int k1, const double* up, const doubl
 {
    const long long n = 3 * b.nij * (k1 - k0 + 1);
    uacc_slab_kernel<<<grid_stride_blocks(n), 256, 0, s>>>(b, k0, k1, up, u, um, out);
+   return launch_status();
+}
+
+int launch_df_slab(const Box& b, int k0, int k1, const float* a, const float* bsub, double* out,
+                   cudaStream_t s)
+{
+   const long long n = 3 * b.nij * (k1 - k0 + 1);
+   df_slab_kernel<<<grid_stride_blocks(n), 256, 0, s>>>(b, k0, k1, a, bsub, out);
    return launch_status();
 }
 
