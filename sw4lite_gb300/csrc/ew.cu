@@ -39,6 +39,7 @@ EW::~EW()
    f(zc_[1]);
    f(dsrc_mem_);
    f(dsrc_curv_mem_);
+   f(rscr_);
    f(drec_mem_);
    f(records_);
    f(rho32_);
@@ -120,8 +121,10 @@ int EW::init()
    // (top) or nz-7..ke (bottom)
    const long long nij = (long long)len[0] * len[1];
    slab_len_ = 3 * nij * 10;
-   if (onesided_[4] || onesided_[5])  // the mixed form also keeps u - um slabs
+   if (onesided_[4] || onesided_[5]) {  // the mixed form also keeps u - um slabs
       SW4G_TRY(cuda_ok(cudaMalloc(&slab_, (mixed_ ? 4 : 2) * slab_len_ * sizeof(double))));
+      SW4G_TRY(cuda_ok(cudaMalloc(&rscr_, 42 * nij * sizeof(double))));
+   }
    {
       const Box bx = make_box(1, b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke);
       for (int side = 0; side < 2; side++)
@@ -690,7 +693,7 @@ int EW::fused_piece(int piece, int ip, int iq)
          if (onesided_[4 + side])
             SW4G_TRY(launch_stage_rows(0, side == 0, b, nz, u, b, mu_, la_, g_.h, st[0], st[1], st[2],
                                        u, um, nullptr, up, rho_, irho_, dt2, 0.0, dc, st, co,
-                                       zc_[side], stream_));
+                                       zc_[side], stream_, rscr_));
       return kOk;
    }
    if (piece == 2) {
@@ -708,7 +711,7 @@ int EW::fused_piece(int piece, int ip, int iq)
          Box sb = make_box(1, bd.ib, bd.ie, bd.jb, bd.je, k0, k1);
          SW4G_TRY(launch_stage_rows(1, side == 0, b, nz, slab, sb, mu_, la_, g_.h, st[0], st[1],
                                     st[2], u, um, up, out, rho_, irho_, dt2 / 12, beta4, dc, st, co,
-                                    zc_[side], stream_));
+                                    zc_[side], stream_, rscr_));
       }
       if (beta != 0 && g_.sg_order == 6)
          SW4G_TRY(launch_addsgd(6, 1, bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, out, u, um, rho_,
@@ -788,7 +791,7 @@ int EW::mixed_piece(int piece, int ip, int iq)
          Box sb = make_box(1, bd.ib, bd.ie, bd.jb, bd.je, k0, k1);
          SW4G_TRY(launch_stage_rows_df(0, side == 0, b, nz, slab, nullptr, sb, mu_, la_, g_.h, st[0],
                                        st[1], st[2], u, um, nullptr, up, rho_, irho_, dt2, 0.0, dc,
-                                       st, co, zc_[side], stream_));
+                                       st, co, zc_[side], stream_, nullptr, rscr_));
       }
       return kOk;
    }
@@ -810,7 +813,8 @@ int EW::mixed_piece(int piece, int ip, int iq)
          Box sb = make_box(1, bd.ib, bd.ie, bd.jb, bd.je, k0, k1);
          SW4G_TRY(launch_stage_rows_df(1, side == 0, b, nz, slab, nullptr, sb, mu_, la_, g_.h, st[0],
                                        st[1], st[2], u, um, up, out, rho_, irho_, dt2 / 12, beta,
-                                       dc, st, co, zc_[side], stream_, beta != 0 ? dslab : nullptr));
+                                       dc, st, co, zc_[side], stream_, beta != 0 ? dslab : nullptr,
+                                       rscr_));
       }
       return kOk;
    }
@@ -900,7 +904,8 @@ int EW::launches_per_step(int mode) const
    // the corrector adds the rows' slab kernels (and 6th-order damping); the mixed
    // form adds an FP64 slab of the predictor's field and of the corrector's u - um
    const int mslabs = mixed_ ? rows * (1 + (damp ? 1 : 0)) : 0;
-   return 2 * (2 + rows + src + bc) + rows + (damp && g_.sg_order == 6 ? 1 : 0) + rec + mslabs +
+   // and each rows launch its per-column pass
+   return 2 * (2 + 2 * rows + src + bc) + rows + (damp && g_.sg_order == 6 ? 1 : 0) + rec + mslabs +
           curv_launches(mode);
 }
 

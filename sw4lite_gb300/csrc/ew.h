@@ -206,6 +206,7 @@ class EW {
    double* uacc_ = nullptr;
    double* zc_[2] = {nullptr, nullptr};  // SBP z coefficients of the top / bottom rows
    double* slab_ = nullptr; // corrector stage field on the one-sided rows
+   double* rscr_ = nullptr; // per-column terms of the one-sided rows (42 x columns)
    long long slab_len_ = 0;
 
    std::vector<GridPointSource> hsrc_;

@@ -5,6 +5,8 @@
 // for the reference's rhs4sg / rhs4sg_rev, src/EW.C:141-149) for any bounds and
 // onesided flags, and are the baseline the fused z-marching stage kernels
 // (stage_fused.cu) are checked against.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "sbp.h"
@@ -33,6 +35,11 @@ struct OpArgs {
    // optional SBP z coefficients of the one-sided rows, per column (zcoef_kernel):
    // zc[((r*8 + q)*2 + t)*nij + column], row r=0..5, point q=0..7, t 0 mu, 1 2mu+lambda
    const double* __restrict__ zc;
+   // optional per-column terms of the one-sided rows (rows_pre_kernel): the one-sided z
+   // derivatives dzc[((kk-1)*3 + c)*nij + column] of every column and the z-differences
+   // of the centred x/y products roc[((kk-1)*4 + t)*nij + column] of interior columns
+   const double* __restrict__ dzc;
+   const double* __restrict__ roc;
 };
 
 template <bool DF>
@@ -141,7 +148,8 @@ __global__ void __launch_bounds__(256) rhs4_center_kernel(OpArgs a, int k1)
 // row is kk = k (top) or nk-k+1 (bottom) and the z-stencil point q (1..8) sits at
 // k=q (top) or nk-q+1 (bottom), with the first-derivative weights negated at the
 // bottom (src/rhs4sg_rev.C:602-856).  strz is not applied on these rows.
-template <bool TOP, bool DF = false>
+// PRE: the per-column terms come from rows_pre_kernel (a.dzc, a.roc).
+template <bool TOP, bool DF = false, bool PRE = false>
 __device__ __forceinline__ void lu_bndry_point(const OpArgs& a, int i, int j, int k, double r[3])
 {
    const int nk = a.nk;
@@ -198,7 +206,12 @@ __device__ __forceinline__ void lu_bndry_point(const OpArgs& a, int i, int j, in
          if (m == 0) continue;
          const int ii = i + (ax == 0) * m, jj = j + (ax == 1) * m;
          double dz = 0;
-         for (int q = 1; q <= 8; q++) dz += wz(q) * P.u(c, ii, jj, kq(q));
+         if (PRE)
+            dz = __ldg(a.dzc + ((long long)(kk - 1) * 3 + c) * a.b.nij + (ii - a.b.ib) +
+                       a.b.ni * (long long)(jj - a.b.jb));
+         else
+#pragma unroll 1
+            for (int q = 1; q <= 8; q++) dz += wz(q) * P.u(c, ii, jj, kq(q));
          const double cf = la_coef ? P.la(ii, jj, k) : P.mu(ii, jj, k);
          const double w = (m == -2) ? 1.0 : (m == -1) ? -8.0 : (m == 1) ? 8.0 : -1.0;
          s += w * cf * dz;
@@ -209,6 +222,12 @@ __device__ __forceinline__ void lu_bndry_point(const OpArgs& a, int i, int j, in
    auto dz_of_inner = [&](bool la_coef, int ax, int c) {
       double s = 0;
       const int di = ax == 0, dj = ax == 1;
+      if (PRE) {
+         const int t = la_coef ? 2 + ax : ax;
+         return __ldg(a.roc + ((long long)(kk - 1) * 4 + t) * a.b.nij + (i - a.b.ib) +
+                      a.b.ni * (long long)(j - a.b.jb));
+      }
+#pragma unroll 1
       for (int q = 1; q <= 8; q++) {
          const int kz = kq(q);
          const double inner = d1c(P.u(c, i - 2 * di, j - 2 * dj, kz), P.u(c, i - di, j - dj, kz),
@@ -226,6 +245,71 @@ __device__ __forceinline__ void lu_bndry_point(const OpArgs& a, int i, int j, in
    r[2] += sy * outer_of_dz(false, 1, 1);
    r[2] += sx * dz_of_inner(true, 0, 0);
    r[2] += sy * dz_of_inner(true, 1, 1);
+}
+
+// Per column, the parts of the one-sided rows that do not depend on the row's own
+// x/y position: the one-sided z derivatives sum_q wz(kk,q) u_c(q) of every column
+// (the outer x/y differences of the rows read them at four neighbours), and for
+// interior columns the z-differences sum_q wz(kk,q) coef(q) D_a u_c(q)/12 of the four
+// centred products (mu D_x w, mu D_y w, la D_x u, la D_y v) of all six rows
+// (src/rhs4sg_rev.C:349-600).
+template <bool TOP>
+__global__ void __launch_bounds__(128) rows_pre_kernel(OpArgs a, double* __restrict__ dzc,
+                                                       double* __restrict__ roc)
+{
+   const long long nij = a.b.nij;
+   const int nk = a.nk;
+   Pt P(a);
+   auto kq = [&](int q) { return TOP ? q : nk - q + 1; };
+   auto wz = [&](int kk, int q) {
+      const double w = k_bope[(kk - 1) + 6 * (q - 1)];
+      return TOP ? w : -w;
+   };
+   const double i12 = 1.0 / 12;
+   for (long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x; col < nij;
+        col += (long long)gridDim.x * blockDim.x) {
+      const int i = a.b.ib + (int)(col % a.b.ni), j = a.b.jb + (int)(col / a.b.ni);
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+         double f[8];
+#pragma unroll
+         for (int q = 1; q <= 8; q++) f[q - 1] = P.u(c, i, j, kq(q));
+#pragma unroll
+         for (int kk = 1; kk <= 6; kk++) {
+            double dz = 0;
+#pragma unroll
+            for (int q = 1; q <= 8; q++) dz += wz(kk, q) * f[q - 1];
+            dzc[((long long)(kk - 1) * 3 + c) * nij + col] = dz;
+         }
+      }
+      if (i < a.b.ib + 2 || i > a.b.ie - 2 || j < a.b.jb + 2 || j > a.b.je - 2) continue;
+      // t: 0 mu D_x w, 1 mu D_y w, 2 la D_x u, 3 la D_y v
+      double acc[6][4];
+#pragma unroll
+      for (int kk = 0; kk < 6; kk++) acc[kk][0] = acc[kk][1] = acc[kk][2] = acc[kk][3] = 0;
+#pragma unroll 1
+      for (int q = 1; q <= 8; q++) {
+         const int kz = kq(q);
+         const double mu = P.mu(i, j, kz), la = P.la(i, j, kz);
+         double g[4];
+#pragma unroll
+         for (int t = 0; t < 4; t++) {
+            const int ax = t & 1, c = t < 2 ? 2 : ax;
+            const int di = ax == 0, dj = ax == 1;
+            const double inner = d1c(P.u(c, i - 2 * di, j - 2 * dj, kz), P.u(c, i - di, j - dj, kz),
+                                     P.u(c, i + di, j + dj, kz), P.u(c, i + 2 * di, j + 2 * dj, kz));
+            g[t] = (t < 2 ? mu : la) * inner * i12;
+         }
+#pragma unroll
+         for (int kk = 1; kk <= 6; kk++)
+#pragma unroll
+            for (int t = 0; t < 4; t++) acc[kk - 1][t] += wz(kk, q) * g[t];
+      }
+#pragma unroll
+      for (int kk = 0; kk < 6; kk++)
+#pragma unroll
+         for (int t = 0; t < 4; t++) roc[((long long)kk * 4 + t) * nij + col] = acc[kk][t];
+   }
 }
 
 template <bool TOP>
@@ -313,7 +397,7 @@ __device__ __forceinline__ double sg4_point(const Box& b, const RowUpdate& w, in
 
 // DF: the levels (and, when the stage field is not an FP64 slab, the field) are
 // double-float pairs; FDF: the stage field is double-float.
-template <bool TOP, bool DF, bool FDF>
+template <bool TOP, bool DF, bool FDF, bool PRE>
 __global__ void __launch_bounds__(256) stage_rows_kernel(OpArgs a, RowUpdate w)
 {
    const int i = a.b.ib + 2 + blockIdx.x * blockDim.x + threadIdx.x;
@@ -321,7 +405,7 @@ __global__ void __launch_bounds__(256) stage_rows_kernel(OpArgs a, RowUpdate w)
    if (i > a.b.ie - 2 || j > a.b.je - 2) return;
    const int k = TOP ? 1 + (int)blockIdx.z : a.nk - 5 + (int)blockIdx.z;
    double r[3];
-   lu_bndry_point<TOP, FDF>(a, i, j, k, r);
+   lu_bndry_point<TOP, FDF, PRE>(a, i, j, k, r);
    const long long p = pidx(a.b, i, j, k);
    const double ir = w.irho ? __ldg(w.irho + p) : 1.0 / __ldg(w.rho + p);
    const double cr = w.coef * ir;
@@ -378,6 +462,7 @@ int launch_rhs4sg_direct(int soa, int ifirst, int ilast, int jfirst, int jlast, 
    a.u = u;
    a.udf = nullptr;
    a.zc = nullptr;
+   a.dzc = a.roc = nullptr;
    a.mu = mu;
    a.la = la;
    a.sx = strx;
@@ -412,12 +497,14 @@ int launch_stage_rows(int corrector, bool top, const Box& b, int nk, const doubl
                       const double* u, const double* um, const double* up, double* out,
                       const double* rho, const double* irho, double coef, double beta,
                       const double* const dc[3], const double* const st[3],
-                      const double* const co[3], const double* zc, cudaStream_t stream)
+                      const double* const co[3], const double* zc, cudaStream_t stream,
+                      double* rscr)
 {
    int status = upload_sbp_tables_direct();
    if (status != kOk) return status;
    OpArgs a;
    a.zc = zc;
+   a.dzc = a.roc = nullptr;
    a.b = b;
    a.bu = field_box;
    a.u = field;
@@ -452,10 +539,23 @@ int launch_stage_rows(int corrector, bool top, const Box& b, int nk, const doubl
    const int ni = b.ie - b.ib - 3, nj = b.je - b.jb - 3;
    if (ni <= 0 || nj <= 0) return kOk;
    const dim3 block(32, 8, 1), grid(blocks_for(ni, 32), blocks_for(nj, 8), 6);
-   if (top)
-      stage_rows_kernel<true, false, false><<<grid, block, 0, stream>>>(a, w);
-   else
-      stage_rows_kernel<false, false, false><<<grid, block, 0, stream>>>(a, w);
+   if (rscr) {  // the per-column terms once, then the rows read them
+      a.dzc = rscr;
+      a.roc = rscr + 18 * b.nij;
+      const int nb = (int)std::min<long long>((b.nij + 127) / 128, 152LL * 16);
+      if (top) rows_pre_kernel<true><<<nb, 128, 0, stream>>>(a, rscr, rscr + 18 * b.nij);
+      else rows_pre_kernel<false><<<nb, 128, 0, stream>>>(a, rscr, rscr + 18 * b.nij);
+      const int st = launch_status();
+      if (st != kOk) return st;
+   }
+   const bool pre = rscr != nullptr;
+   if (top) {
+      if (pre) stage_rows_kernel<true, false, false, true><<<grid, block, 0, stream>>>(a, w);
+      else stage_rows_kernel<true, false, false, false><<<grid, block, 0, stream>>>(a, w);
+   } else {
+      if (pre) stage_rows_kernel<false, false, false, true><<<grid, block, 0, stream>>>(a, w);
+      else stage_rows_kernel<false, false, false, false><<<grid, block, 0, stream>>>(a, w);
+   }
    return launch_status();
 }
 
@@ -466,12 +566,13 @@ int launch_stage_rows_df(int corrector, bool top, const Box& b, int nz, const do
                          float* out, const double* rho, const double* irho, double coef,
                          double beta, const double* const dc[3], const double* const st[3],
                          const double* const co[3], const double* zc, cudaStream_t stream,
-                         const double* dd)
+                         const double* dd, double* rscr)
 {
    int status = upload_sbp_tables_direct();
    if (status != kOk) return status;
    OpArgs a;
    a.zc = zc;
+   a.dzc = a.roc = nullptr;
    a.b = b;
    a.bu = field_box;
    a.u = field_f64;
@@ -507,13 +608,24 @@ int launch_stage_rows_df(int corrector, bool top, const Box& b, int nz, const do
    const int ni = b.ie - b.ib - 3, nj = b.je - b.jb - 3;
    if (ni <= 0 || nj <= 0) return kOk;
    const dim3 block(32, 8, 1), grid(blocks_for(ni, 32), blocks_for(nj, 8), 6);
+   if (rscr) {  // the per-column terms once, then the rows read them
+      a.dzc = rscr;
+      a.roc = rscr + 18 * b.nij;
+      const int nb = (int)std::min<long long>((b.nij + 127) / 128, 152LL * 16);
+      if (top) rows_pre_kernel<true><<<nb, 128, 0, stream>>>(a, rscr, rscr + 18 * b.nij);
+      else rows_pre_kernel<false><<<nb, 128, 0, stream>>>(a, rscr, rscr + 18 * b.nij);
+      const int st = launch_status();
+      if (st != kOk) return st;
+   }
    const bool fdf = field_df != nullptr;
    if (top) {
-      if (fdf) stage_rows_kernel<true, true, true><<<grid, block, 0, stream>>>(a, w);
-      else stage_rows_kernel<true, true, false><<<grid, block, 0, stream>>>(a, w);
+      if (fdf) stage_rows_kernel<true, true, true, false><<<grid, block, 0, stream>>>(a, w);
+      else if (rscr) stage_rows_kernel<true, true, false, true><<<grid, block, 0, stream>>>(a, w);
+      else stage_rows_kernel<true, true, false, false><<<grid, block, 0, stream>>>(a, w);
    } else {
-      if (fdf) stage_rows_kernel<false, true, true><<<grid, block, 0, stream>>>(a, w);
-      else stage_rows_kernel<false, true, false><<<grid, block, 0, stream>>>(a, w);
+      if (fdf) stage_rows_kernel<false, true, true, false><<<grid, block, 0, stream>>>(a, w);
+      else if (rscr) stage_rows_kernel<false, true, false, true><<<grid, block, 0, stream>>>(a, w);
+      else stage_rows_kernel<false, true, false, false><<<grid, block, 0, stream>>>(a, w);
    }
    return launch_status();
 }
