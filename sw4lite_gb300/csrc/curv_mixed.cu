@@ -82,7 +82,7 @@ __host__ __device__ constexpr int mixed_smem_floats(int corr)
 __device__ __forceinline__ int m5(int k) { return ((k % 5) + 5) % 5; }
 
 template <int CORR>
-__global__ void __launch_bounds__(NTHREADS, 2) curv_mixed_kernel(MArgs a)
+__global__ void __launch_bounds__(NTHREADS, 3) curv_mixed_kernel(MArgs a)
 {
    extern __shared__ float smf[];
    float* VH = smf;                       // [5][3][PLANE] stencil field (hi)

@@ -79,7 +79,7 @@ __device__ __forceinline__ int mod5(int k) { return ((k % 5) + 5) % 5; }
 __device__ __forceinline__ int mod3(int k) { return ((k % 3) + 3) % 3; }
 
 template <int CORR>
-__global__ void __launch_bounds__(NTHREADS, 2) mixed_stage_kernel(MixedArgs a)
+__global__ void __launch_bounds__(NTHREADS, 3) mixed_stage_kernel(MixedArgs a)
 {
    extern __shared__ float smf[];
    // predictor: VH | VL ; corrector: VH (the field) | DD | RH
