@@ -565,17 +565,11 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       ms.b = b;
       ms.k1 = 1;
       ms.k2 = g_.nz;
-      ms.muh = mu32_;
-      ms.mul = mu32_ + npts_;
-      ms.lah = la32_;
-      ms.lal = la32_ + npts_;
-      ms.irh = irho32_;
-      ms.irl = irho32_ + npts_;
+      ms.mu2 = reinterpret_cast<const float2*>(mu32_);
+      ms.la2 = reinterpret_cast<const float2*>(la32_);
+      ms.ir2 = reinterpret_cast<const float2*>(irho32_);
       ms.rho = rho32_;
-      for (int q = 0; q < kWeightArrays; q++) {
-         ms.wh[q] = wd_.h[q];
-         ms.wl[q] = wd_.l[q];
-      }
+      for (int q = 0; q < kWeightArrays; q++) ms.w2[q] = wd_.p[q];
       for (int q = 0; q < 3; q++) {
          ms.dc[q] = prof32_[q];
          ms.st[q] = prof32_[3 + q];

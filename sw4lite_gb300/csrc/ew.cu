@@ -93,10 +93,7 @@ int EW::init()
       SW4G_TRY(cuda_ok(cudaMalloc(&la32_, 2 * n * sizeof(float))));
       SW4G_TRY(cuda_ok(cudaMalloc(&irho32_, 2 * n * sizeof(float))));
       SW4G_TRY(cuda_ok(cudaMalloc(&wdf_, 2 * kWeightArrays * n * sizeof(float))));
-      for (int q = 0; q < kWeightArrays; q++) {
-         wd_.h[q] = wdf_ + (2 * q) * n;
-         wd_.l[q] = wdf_ + (2 * q + 1) * n;
-      }
+      for (int q = 0; q < kWeightArrays; q++) wd_.p[q] = reinterpret_cast<float2*>(wdf_) + q * n;
    }
    // a level holds 3*npts doubles, or in the mixed form 3*npts hi + 3*npts lo floats
    // (the same bytes)
@@ -160,9 +157,9 @@ int EW::set_material(const double* rho, const double* mu, const double* la, bool
       SW4G_TRY(launch_weights(b, mu_, la_, dprof_[3], dprof_[4], dprof_[5], g_.h, w_, stream_));
    } else {
       SW4G_TRY(launch_to_f32(npts_, rho_, rho32_, stream_));
-      SW4G_TRY(launch_df_from_f64(npts_, mu_, mu32_, mu32_ + npts_, stream_));
-      SW4G_TRY(launch_df_from_f64(npts_, la_, la32_, la32_ + npts_, stream_));
-      SW4G_TRY(launch_df_from_f64(npts_, irho_, irho32_, irho32_ + npts_, stream_));
+      SW4G_TRY(launch_df2_from_f64(npts_, mu_, reinterpret_cast<float2*>(mu32_), stream_));
+      SW4G_TRY(launch_df2_from_f64(npts_, la_, reinterpret_cast<float2*>(la32_), stream_));
+      SW4G_TRY(launch_df2_from_f64(npts_, irho_, reinterpret_cast<float2*>(irho32_), stream_));
       SW4G_TRY(launch_weights_df(b, mu_, la_, dprof_[3], dprof_[4], dprof_[5], wd_, stream_));
    }
    SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
@@ -748,17 +745,11 @@ int EW::mixed_piece(int piece, int ip, int iq)
       ms.b = b;
       ms.k1 = onesided_[4] ? 7 : 1;
       ms.k2 = onesided_[5] ? nz - 6 : nz;
-      ms.muh = mu32_;
-      ms.mul = mu32_ + npts_;
-      ms.lah = la32_;
-      ms.lal = la32_ + npts_;
-      ms.irh = irho32_;
-      ms.irl = irho32_ + npts_;
+      ms.mu2 = reinterpret_cast<const float2*>(mu32_);
+      ms.la2 = reinterpret_cast<const float2*>(la32_);
+      ms.ir2 = reinterpret_cast<const float2*>(irho32_);
       ms.rho = rho32_;
-      for (int q = 0; q < kWeightArrays; q++) {
-         ms.wh[q] = wd_.h[q];
-         ms.wl[q] = wd_.l[q];
-      }
+      for (int q = 0; q < kWeightArrays; q++) ms.w2[q] = wd_.p[q];
       for (int q = 0; q < 3; q++) {
          ms.dc[q] = prof32_[q];
          ms.st[q] = prof32_[3 + q];

@@ -37,9 +37,9 @@ struct FusedStage {
    double coef = 0;  // > 0: the L(.) coefficient instead of dt^2 (dt^2/12 corrector)
 };
 
+// (hi, lo) pairs interleaved: one 8-byte load per coefficient
 struct WeightPtrsDF {
-   float* h[kWeightArrays];
-   float* l[kWeightArrays];
+   float2* p[kWeightArrays];
 };
 
 // One mixed-form stage launch (stage_mixed.cu): double-float levels (hi at
@@ -52,15 +52,11 @@ struct MixedStage {
    const float* um = nullptr;
    const float* up = nullptr;
    float* out = nullptr;
-   const float* muh = nullptr;  // (hi, lo) pairs of mu, lambda and 1/rho
-   const float* mul = nullptr;
-   const float* lah = nullptr;
-   const float* lal = nullptr;
-   const float* irh = nullptr;
-   const float* irl = nullptr;
+   const float2* mu2 = nullptr;  // interleaved (hi, lo) pairs of mu, lambda and 1/rho
+   const float2* la2 = nullptr;
+   const float2* ir2 = nullptr;
    const float* rho = nullptr;
-   const float* wh[kWeightArrays] = {};
-   const float* wl[kWeightArrays] = {};
+   const float2* w2[kWeightArrays] = {};
    const float* st[3] = {nullptr, nullptr, nullptr};
    const float* dc[3] = {nullptr, nullptr, nullptr};
    const float* co[3] = {nullptr, nullptr, nullptr};
@@ -280,6 +276,8 @@ int fma_peak(int precision, double* tflops, cudaStream_t s);
 
 int launch_mixed_stage(const MixedStage& st, cudaStream_t stream);
 int launch_df_from_f64(long long n, const double* x, float* h, float* l, cudaStream_t s);
+// FP64 -> interleaved (hi, lo) FP32 pairs
+int launch_df2_from_f64(long long n, const double* x, float2* hl, cudaStream_t s);
 int launch_df_to_f64(long long n, const float* h, const float* l, double* x, cudaStream_t s);
 int launch_to_f32(long long n, const double* x, float* y, cudaStream_t s);
 int launch_weights_df(const Box& b, const double* mu, const double* la, const double* sx,

@@ -48,15 +48,11 @@ struct MixedArgs {
    const float* __restrict__ um;
    const float* __restrict__ up;
    float* __restrict__ out;
-   const float* __restrict__ muh;   // mu = muh + mul
-   const float* __restrict__ mul;
-   const float* __restrict__ lah;   // lambda = lah + lal
-   const float* __restrict__ lal;
+   const float2* __restrict__ mu2;  // mu, lambda, 1/rho as interleaved (hi, lo) pairs
+   const float2* __restrict__ la2;
+   const float2* __restrict__ ir2;
    const float* __restrict__ rho;   // FP32, supergrid damping only
-   const float* __restrict__ irh;   // 1/rho = irh + irl
-   const float* __restrict__ irl;
-   const float* __restrict__ wh[kWeightArrays];  // second-difference weights (unscaled)
-   const float* __restrict__ wl[kWeightArrays];
+   const float2* __restrict__ w2[kWeightArrays];  // second-difference weights (unscaled), pairs
    const float* __restrict__ sx;
    const float* __restrict__ sy;
    const float* __restrict__ sz;
@@ -165,10 +161,11 @@ __global__ void __launch_bounds__(NTHREADS, 3) mixed_stage_kernel(MixedArgs a)
          float mh = 0.f, ml = 0.f, lh = 0.f, ll = 0.f, r = 0.f;
          if (gi <= a.ie && gj <= a.je) {
             const long long p = gidx(gi, gj, kk);
-            mh = __ldg(a.muh + p);
-            ml = __ldg(a.mul + p);
-            lh = __ldg(a.lah + p);
-            ll = __ldg(a.lal + p);
+            const float2 m2 = __ldg(a.mu2 + p), l2 = __ldg(a.la2 + p);
+            mh = m2.x;
+            ml = m2.y;
+            lh = l2.x;
+            ll = l2.y;
             if (CORR) r = __ldg(a.rho + p);
          }
          MUH[idx] = mh;
@@ -206,8 +203,8 @@ __global__ void __launch_bounds__(NTHREADS, 3) mixed_stage_kernel(MixedArgs a)
       const float dxu = d1(hu, lu_, own - 2, hu, lu_, own - 1, hu, lu_, own + 1, hu, lu_, own + 2);
       const float dyv = d1(hv, lv, own - 2 * PX, hv, lv, own - PX, hv, lv, own + PX, hv, lv, own + 2 * PX);
       const long long p = gidx(i, j, kk);
-      const float mh = __ldg(a.muh + p), ml = __ldg(a.mul + p);
-      const float lh = __ldg(a.lah + p), ll = __ldg(a.lal + p);
+      const float2 m2 = __ldg(a.mu2 + p), l2 = __ldg(a.la2 + p);
+      const float mh = m2.x, ml = m2.y, lh = l2.x, ll = l2.y;
       const float x0 = sxi * dxw, x1 = syj * dyw, x2 = sxi * dxu + syj * dyv;
       g[0] = fmaf(mh, x0, ml * x0);
       g[1] = fmaf(mh, x1, ml * x1);
@@ -330,14 +327,16 @@ __global__ void __launch_bounds__(NTHREADS, 3) mixed_stage_kernel(MixedArgs a)
             for (int t = 0; t < 2; t++) {
                const int s1 = ax * 4 + t * 2, s2 = s1 + 1;
                const long long o = off[ax];
-               wth[ax][t][0] = __ldg(a.wh[s1] + p);
-               wth[ax][t][1] = __ldg(a.wh[s2] + p);
-               wth[ax][t][2] = __ldg(a.wh[s2] + p + o);
-               wth[ax][t][3] = __ldg(a.wh[s1] + p + 2 * o);
-               wtl[ax][t][0] = __ldg(a.wl[s1] + p);
-               wtl[ax][t][1] = __ldg(a.wl[s2] + p);
-               wtl[ax][t][2] = __ldg(a.wl[s2] + p + o);
-               wtl[ax][t][3] = __ldg(a.wl[s1] + p + 2 * o);
+               const float2 q0 = __ldg(a.w2[s1] + p), q1 = __ldg(a.w2[s2] + p),
+                            q2 = __ldg(a.w2[s2] + p + o), q3 = __ldg(a.w2[s1] + p + 2 * o);
+               wth[ax][t][0] = q0.x;
+               wth[ax][t][1] = q1.x;
+               wth[ax][t][2] = q2.x;
+               wth[ax][t][3] = q3.x;
+               wtl[ax][t][0] = q0.y;
+               wtl[ax][t][1] = q1.y;
+               wtl[ax][t][2] = q2.y;
+               wtl[ax][t][3] = q3.y;
             }
          auto wsum = [&](int ax, int t, float dm2, float dm1, float dp1, float dp2) {
             const float* h = wth[ax][t];
@@ -380,7 +379,8 @@ __global__ void __launch_bounds__(NTHREADS, 3) mixed_stage_kernel(MixedArgs a)
             xs[c] = (16.f * sd + 8.f * sd) + (sxi * cx + syj * cy + szk * cz);
          }
          // per-point scale K/rho as a (hi, lo) pair: ph + pl = (Kh + Kl) * (irh + irl)
-         const float irh = __ldg(a.irh + p), irl = __ldg(a.irl + p);
+         const float2 ir = __ldg(a.ir2 + p);
+         const float irh = ir.x, irl = ir.y;
          const float ph = a.Kh * irh;
          const float pl = fmaf(a.Kh, irh, -ph) + fmaf(a.Kh, irl, a.Kl * irh);
          auto scaled = [&](float x) { return fmaf(x, ph, x * pl); };
@@ -502,8 +502,11 @@ __global__ void weights_df_kernel(Box b, const double* __restrict__ mu, const do
             }
          }
          for (int t = 0; t < 2; t++) {
-            df_split(w1[t], w.h[ax * 4 + t * 2][p], w.l[ax * 4 + t * 2][p]);
-            df_split(w2[t], w.h[ax * 4 + t * 2 + 1][p], w.l[ax * 4 + t * 2 + 1][p]);
+            float h1, l1, h2, l2;
+            df_split(w1[t], h1, l1);
+            df_split(w2[t], h2, l2);
+            w.p[ax * 4 + t * 2][p] = make_float2(h1, l1);
+            w.p[ax * 4 + t * 2 + 1][p] = make_float2(h2, l2);
          }
       }
    }
@@ -515,6 +518,16 @@ __global__ void df_from_f64_kernel(long long n, const double* __restrict__ x, fl
    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
         q += (long long)gridDim.x * blockDim.x)
       df_split(x[q], h[q], l[q]);
+}
+
+__global__ void df2_from_f64_kernel(long long n, const double* __restrict__ x, float2* __restrict__ hl)
+{
+   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+        q += (long long)gridDim.x * blockDim.x) {
+      float h, l;
+      df_split(x[q], h, l);
+      hl[q] = make_float2(h, l);
+   }
 }
 
 __global__ void df_to_f64_kernel(long long n, const float* __restrict__ h, const float* __restrict__ l,
@@ -539,6 +552,12 @@ int gs_blocks(long long n)
 }
 
 }  // namespace
+
+int launch_df2_from_f64(long long n, const double* x, float2* hl, cudaStream_t s)
+{
+   df2_from_f64_kernel<<<gs_blocks(n), 256, 0, s>>>(n, x, hl);
+   return launch_status();
+}
 
 int launch_df_from_f64(long long n, const double* x, float* h, float* l, cudaStream_t s)
 {
@@ -578,16 +597,12 @@ int launch_mixed_stage(const MixedStage& st, cudaStream_t stream)
    a.um = st.um;
    a.up = st.up;
    a.out = st.out;
-   a.muh = st.muh;
-   a.mul = st.mul;
-   a.lah = st.lah;
-   a.lal = st.lal;
+   a.mu2 = st.mu2;
+   a.la2 = st.la2;
    a.rho = st.rho;
-   a.irh = st.irh;
-   a.irl = st.irl;
+   a.ir2 = st.ir2;
    for (int q = 0; q < kWeightArrays; q++) {
-      a.wh[q] = st.wh[q];
-      a.wl[q] = st.wl[q];
+      a.w2[q] = st.w2[q];
    }
    a.sx = st.st[0];
    a.sy = st.st[1];
