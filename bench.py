@@ -735,6 +735,14 @@ def run_ours(args, rank, world):
     n = args.n
     npts_int = n ** 3
     stream = torch.cuda.Stream()
+    if args.only_c2:
+        # one form of the C2 workload alone (launch lists and kernel captures)
+        f = _time_form(args, sg, torch, sg.FP64 if args.only_c2 == "fp64" else sg.MIXED, stream,
+                       world, local)
+        if rank == 0:
+            print(json.dumps({"only": "C2 " + args.only_c2, "ms_per_step": f["ms_per_step"],
+                              "value": f["value"], "kernel_ms": f["kernel_ms"]}), flush=True)
+        return 0
     if args.only_topo:
         # the topography workload alone (launch lists and kernel captures)
         prec = 0 if args.only_topo == "fp64" else 1
@@ -850,6 +858,8 @@ def main():
     ap.add_argument("--ms-steps", type=int, default=150, help="steps of the multi-shot workload")
     ap.add_argument("--ms-err-shots", type=int, default=2,
                     help="shots whose summed gradient is compared with FP64 (0: skip)")
+    ap.add_argument("--only-c2", choices=["fp64", "mixed"], default=None,
+                    help="time only the C2 workload in that form (for profiling)")
     ap.add_argument("--only-topo", choices=["fp64", "mixed"], default=None,
                     help="time only the topography workload in that form (for profiling)")
     ap.add_argument("--no-err", action="store_true", help="skip the mixed-vs-FP64 error run")

@@ -8,6 +8,7 @@
 // The pointwise kernels cover every array point, ghosts included, as the
 // reference does; they are HBM-streaming kernels (grid-stride, coalesced).
 #include "common.cuh"
+#include "df.cuh"
 #include "kernels.h"
 
 namespace sw4g {
@@ -151,6 +152,29 @@ __global__ void __launch_bounds__(256) addsgd6_kernel(SgArgs a)
 // (src/ew-cfromfort.C:40-114): predictor out = 2u - um, corrector out = up.
 // Points are enumerated as the 4 outer k-planes, then the 4 outer j-rows of the
 // inner planes, then the 4 outer i-columns of the inner rows.
+// The shell point's update: corrector up, predictor 2u - um (FP64, or in double-float
+// arithmetic on the FP32 pipe: TwoSum, then FastTwoSum of the error terms).
+__device__ __forceinline__ void shell_update(const F64Field& out, const F64Field& u, const F64Field& um,
+                                             const F64Field& up, long long x, int corrector)
+{
+   out.set(x, corrector ? up.get(x) : 2 * u.get(x) - um.get(x));
+}
+
+__device__ __forceinline__ void shell_update(const DFField& out, const DFField& u, const DFField& um,
+                                             const DFField& up, long long x, int corrector)
+{
+   if (corrector) {
+      out.h[x] = up.h[x];
+      out.h[x + out.lo] = up.h[x + up.lo];
+      return;
+   }
+   float s, e, oh, ol;
+   two_sum(2.f * u.h[x], -um.h[x], s, e);
+   fast_two_sum(s, e + (2.f * u.h[x + u.lo] - um.h[x + um.lo]), oh, ol);
+   out.h[x] = oh;
+   out.h[x + out.lo] = ol;
+}
+
 template <class Field>
 __global__ void ghost_shell_kernel(Box b, int corrector, Field out, Field u, Field um, Field up)
 {
@@ -181,10 +205,7 @@ __global__ void ghost_shell_kernel(Box b, int corrector, Field out, Field u, Fie
          j = b.jb + 2 + (int)(r % (nj - 4));
       }
 #pragma unroll
-      for (int c = 0; c < 3; c++) {
-         const long long x = cidx(b, c, i, j, k);
-         out.set(x, corrector ? up.get(x) : 2 * u.get(x) - um.get(x));
-      }
+      for (int c = 0; c < 3; c++) shell_update(out, u, um, up, cidx(b, c, i, j, k), corrector);
    }
 }
 

@@ -398,7 +398,7 @@ __device__ __forceinline__ double sg4_point(const Box& b, const RowUpdate& w, in
 // DF: the levels (and, when the stage field is not an FP64 slab, the field) are
 // double-float pairs; FDF: the stage field is double-float.
 template <bool TOP, bool DF, bool FDF, bool PRE>
-__global__ void __launch_bounds__(256) stage_rows_kernel(OpArgs a, RowUpdate w)
+__global__ void __launch_bounds__(256, 2) stage_rows_kernel(OpArgs a, RowUpdate w)
 {
    const int i = a.b.ib + 2 + blockIdx.x * blockDim.x + threadIdx.x;
    const int j = a.b.jb + 2 + blockIdx.y * blockDim.y + threadIdx.y;
