@@ -85,8 +85,9 @@ int EW::init()
    SW4G_TRY(cuda_ok(cudaMalloc(&la_, n * sizeof(double))));
    SW4G_TRY(cuda_ok(cudaMalloc(&irho_, n * sizeof(double))));
    if (!mixed_) {
-      SW4G_TRY(cuda_ok(cudaMalloc(&wstore_, kWeightArrays * n * sizeof(double))));
+      SW4G_TRY(cuda_ok(cudaMalloc(&wstore_, (kWeightArrays + kWeightSums) * n * sizeof(double))));
       for (int q = 0; q < kWeightArrays; q++) w_.p[q] = wstore_ + q * n;
+      for (int q = 0; q < kWeightSums; q++) w_.s[q] = wstore_ + (kWeightArrays + q) * n;
    } else {
       SW4G_TRY(cuda_ok(cudaMalloc(&rho32_, n * sizeof(float))));
       SW4G_TRY(cuda_ok(cudaMalloc(&mu32_, 2 * n * sizeof(float))));

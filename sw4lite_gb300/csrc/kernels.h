@@ -11,8 +11,12 @@ namespace sw4g {
 // Precomputed second-difference weights: slot axis*4 + type*2 + n, with type 0
 // for mu*s and 1 for (2mu+lambda)*s, n 0 for W1 and 1 for W2 (stage_fused.cu).
 constexpr int kWeightArrays = 12;
+// s[ax*2 + t] = W1(p) + W2(p) + W2(p+o) + W1(p+2o), the sum of the four weights a
+// point's second difference along ax applies (t: 0 mu s, 1 (2mu+la) s)
+constexpr int kWeightSums = 6;
 struct WeightPtrs {
    double* p[kWeightArrays];
+   double* s[kWeightSums];
 };
 
 // One fused stage launch over the centred rows [k1,k2] of a SoA grid.
