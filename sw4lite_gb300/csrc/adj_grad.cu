@@ -1,0 +1,386 @@
+// Material gradient of one FP64 adjoint step, in double-float arithmetic.
+//
+// The gradient of a1 . u+ with respect to (rho, mu, lambda) at fixed (u, um) is a
+// sum of products of differences of an adjoint level (b1, or mt = b1 + dt^2/12 R
+// L(b1)) and a forward level (w1 = up - 2u + um, or u).  The stretching factors
+// cancel along every difference: with v = c W b (W = 1/(sx sy sz)),
+//   (s_a v)(q + m e_a) - (s_a v)(q) = c / (s_b s_c) (b(q + m e_a) - b(q)),
+// the factor constant along axis a.  So each step needs only plain differences and
+// their products, and the profile factors enter once per point:
+//   mu, lambda : K [ sum_a 24 s_a/(s_b s_c) S_a + sum_t M_t / s_t ],
+//                K = -(dt^2/12) / (144 h^2),
+//     S_a  the seven-edge combination of the same-axis second differences
+//          (v . D2(a) w = -sum_q sum_{m=1,2} W_m(q) (v(q+m)-v(q)) (w(q+m)-w(q))),
+//          summed over the pairs (b1, w1) and 12 x (mt, u);
+//     M_t  the mixed terms whose two axes are not t: products of centred first
+//          differences (lambda: the diagonal ones, mu: the off-diagonal ones);
+//   rho        : -W [mt . w1 + b1 . (un - up)]  (interior points)
+//                - beta sum_a dc_a co_b co_c/(s_b s_c) sum_c D2_a(u - um) D2_a(b1).
+// The products run on the FP32 pipe in double-float arithmetic: a value is the
+// unevaluated sum of two FP32 numbers (47 significant bits), sums use Knuth's
+// TwoSum and Dekker's FastTwoSum, products FMA.  GB300 issues FP32 at 64 times its
+// FP64 rate, so this costs a fraction of the FP64 form of the same sums.  Before the
+// split every value is scaled by a power of two (adjoint levels by a bound from the
+// injected residuals, forward levels by the maximum over the recomputed segment) that
+// maps the level's largest value near 2^28: values down to about 2^-131 of it keep
+// all 47 bits, values below 2^-154 of it count as zero.  Each point's sums go into
+// double-float accumulators, added to the FP64 gradients once per segment.
+//
+// The cancellations that matter stay in FP64: w1 = (up - 2u) + um and un - up are
+// formed from the FP64 levels before the split.
+#include "common.cuh"
+#include "df.cuh"
+#include "kernels.h"
+
+namespace sw4g {
+namespace {
+
+struct DF {
+   float h, l;
+};
+
+__device__ __forceinline__ DF df_zero() { return {0.f, 0.f}; }
+__device__ __forceinline__ DF df_of(float2 a) { return {a.x, a.y}; }
+__device__ __forceinline__ DF df_neg(DF a) { return {-a.h, -a.l}; }
+
+// a - b: the leading difference exact (TwoSum), the trailing parts added once
+__device__ __forceinline__ DF df_diff(DF a, DF b)
+{
+   float s, e;
+   two_sum(a.h, -b.h, s, e);
+   return {s, __fadd_rn(e, __fsub_rn(a.l, b.l))};
+}
+
+// a + b, renormalised
+__device__ __forceinline__ DF df_add(DF a, DF b)
+{
+   float s, e;
+   two_sum(a.h, b.h, s, e);
+   e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+   DF r;
+   fast_two_sum(s, e, r.h, r.l);
+   return r;
+}
+
+// a * b to about 2^-46 relative (the lo * lo term dropped)
+__device__ __forceinline__ DF df_mul(DF a, DF b)
+{
+   const float p = __fmul_rn(a.h, b.h);
+   float e = __fmaf_rn(a.h, b.h, -p);
+   e = __fmaf_rn(a.h, b.l, e);
+   e = __fmaf_rn(a.l, b.h, e);
+   return {p, e};
+}
+
+// k a for a small integer k (the rounding of k a.h kept)
+__device__ __forceinline__ DF df_scale(DF a, float k)
+{
+   const float p = __fmul_rn(k, a.h);
+   return {p, __fmaf_rn(k, a.l, __fmaf_rn(k, a.h, -p))};
+}
+
+// the shift of a level class: 2^(emax - 1023 + margin) bounds its values
+__device__ __forceinline__ int shift_of(int emax, int margin)
+{
+   return min(900, max(-800, emax - 1023 + margin));
+}
+
+// x 2^-sh as a pair (hi: the leading 24 bits, lo: the next 23, rounded) by integer
+// operations on the FP64 bit pattern; kb = (896 + sh) << 20.  Values below
+// 2^(sh - 126) give (0, 0); below 2^(sh - 103) the lo part is dropped.
+__device__ __forceinline__ float2 to_df(double x, int kb)
+{
+   const int H = __double2hiint(x);
+   const unsigned L = (unsigned)__double2loint(x);
+   const int M = (H & 0x7fffffff) - kb;  // FP32 exponent field << 20 | top 20 mantissa bits
+   if (M < (1 << 20)) return make_float2(0.f, 0.f);
+   const unsigned sgn = (unsigned)H & 0x80000000u;
+   const float hi = __uint_as_float(__funnelshift_l(L, (unsigned)M, 3) | sgn);
+   const int eb = (M >> 20) - 23;  // exponent field of 2^(E - 23)
+   float lo = 0.f;
+   if (eb > 0) {
+      // (r >> 6, rounded) 2^(E - 46) as 2^(E-23) (1 + r'/2^23) - 2^(E-23), exact
+      const int base = eb << 23;
+      const int r = (int)(((L & 0x1fffffffu) + 32u) >> 6);
+      const float m = __int_as_float(base + r) - __int_as_float(base);
+      lo = __uint_as_float(__float_as_uint(m) | sgn);
+   }
+   return make_float2(hi, lo);
+}
+
+__device__ __forceinline__ void acc_add(float2* a, long long p, DF v)
+{
+   const DF s = df_add(df_of(a[p]), v);
+   a[p] = make_float2(s.h, s.l);
+}
+
+// the largest FP64 exponent field over n values, into *out (atomicMax)
+__global__ void __launch_bounds__(256) exp_max_kernel(const double* __restrict__ x, long long n,
+                                                      int* __restrict__ out)
+{
+   int m = 0;
+   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+        q += (long long)gridDim.x * blockDim.x)
+      m = max(m, (__double2hiint(__ldg(x + q)) >> 20) & 0x7ff);
+   m = __reduce_max_sync(0xffffffffu, m);
+   if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(out, m);
+}
+
+// the largest exponent field of the injected adjoint sources sxyz/rho res over
+// every residual row and receiver
+__global__ void inj_exp_kernel(Box b, const double* __restrict__ s0, const double* __restrict__ s1,
+                               const double* __restrict__ s2, int nrec, const int* __restrict__ ijk,
+                               const double* __restrict__ res, long long rows, int nval,
+                               const double* __restrict__ rho, int* __restrict__ out)
+{
+   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+   int m = 0;
+   if (t < rows * nrec) {
+      const int r = (int)(t % nrec);
+      const long long row = t / nrec;
+      const int i = ijk[3 * r], j = ijk[3 * r + 1], k = ijk[3 * r + 2];
+      const double s = s0[i - b.ib] * s1[j - b.jb] * s2[k - b.kb] / rho[pidx(b, i, j, k)];
+      for (int c = 0; c < 3; c++)
+         m = max(m, (__double2hiint(fabs(s * res[row * nval + 3 * r + c])) >> 20) & 0x7ff);
+   }
+   m = __reduce_max_sync(0xffffffffu, m);
+   if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(out, m);
+}
+
+// per axis: 24 st, 1/st, co/st, beta dc as pairs
+__global__ void grad_profiles_kernel(int n, const double* __restrict__ st, const double* __restrict__ co,
+                                     const double* __restrict__ dc, double beta, float2* __restrict__ st24,
+                                     float2* __restrict__ ist, float2* __restrict__ cist,
+                                     float2* __restrict__ bdc)
+{
+   const int x = blockIdx.x * blockDim.x + threadIdx.x;
+   if (x >= n) return;
+   float h, l;
+   df_split(24 * st[x], h, l);
+   st24[x] = make_float2(h, l);
+   df_split(1 / st[x], h, l);
+   ist[x] = make_float2(h, l);
+   df_split(co[x] / st[x], h, l);
+   cist[x] = make_float2(h, l);
+   df_split(beta * dc[x], h, l);
+   bdc[x] = make_float2(h, l);
+}
+
+// w1 = up - 2u + um; the pairs of b1, mt (adjoint shift) and w1, u, um (forward
+// shift); the rho terms -W [mt . w1 + b1 . (un - up)] of the interior points
+__global__ void __launch_bounds__(128) grad_prep_kernel(GradDF g)
+{
+   const Box& b = g.b;
+   const int i = b.ib + blockIdx.x * blockDim.x + threadIdx.x, j = b.jb + blockIdx.y,
+             k = b.kb + blockIdx.z;
+   if (i > b.ie) return;
+   const long long n = b.npts;
+   const long long p = (i - b.ib) + (j - b.jb) * b.ni + (k - b.kb) * b.nij;
+   const int ka = (896 + shift_of(g.emax[0], g.marg_a)) << 20;
+   const int kf = (896 + shift_of(g.emax[1], g.marg_f)) << 20;
+   const bool in = i >= b.ib + 2 && i <= b.ie - 2 && j >= b.jb + 2 && j <= b.je - 2 && k >= b.kb + 2 &&
+                   k <= b.ke - 2;
+   DF acc = df_zero();
+#pragma unroll
+   for (int c = 0; c < 3; c++) {
+      const long long q = c * n + p;
+      const double uq = __ldg(g.u + q), umq = __ldg(g.um + q), upq = __ldg(g.up + q);
+      const double w1 = (upq - 2 * uq) + umq;
+      const float2 vb = to_df(__ldg(g.b1 + q), ka), vm = to_df(__ldg(g.mt + q), ka), fw = to_df(w1, kf);
+      g.db1[q] = vb;
+      g.dmt[q] = vm;
+      g.dw1[q] = fw;
+      g.du[q] = to_df(uq, kf);
+      g.dum[q] = to_df(umq, kf);
+      if (in) {
+         const float2 d = to_df(__ldg(g.un + q) - upq, kf);
+         acc = df_add(acc, df_add(df_mul(df_of(vm), df_of(fw)), df_mul(df_of(vb), df_of(d))));
+      }
+   }
+   if (in) {
+      const DF w = df_mul(df_mul(df_of(g.ist[0][i - b.ib]), df_of(g.ist[1][j - b.jb])),
+                          df_of(g.ist[2][k - b.kb]));
+      acc_add(g.ar, p, df_neg(df_mul(w, acc)));
+   }
+}
+
+// the mu, lambda and damping rho sums of one point (32 x 4 points per CTA)
+constexpr int kGradThreads = 128;
+
+__global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
+{
+   // centred first differences of the current pair, [slot][thread]: slot c*3 + a for
+   // the adjoint level, 9 + c*3 + a for the forward level
+   __shared__ float2 fd[18][kGradThreads];
+   const int tid = threadIdx.y * 32 + threadIdx.x;
+   const Box& b = g.b;
+   const int pc[3] = {b.ib + (int)(blockIdx.x * 32 + threadIdx.x), b.jb + (int)(blockIdx.y * 4 + threadIdx.y),
+                      b.kb + (int)blockIdx.z};
+   if (pc[0] > b.ie || pc[1] > b.je) return;
+   const long long n = b.npts;
+   const long long p = (pc[0] - b.ib) + (pc[1] - b.jb) * b.ni + (pc[2] - b.kb) * b.nij;
+   const int off[3] = {pc[0] - b.ib, pc[1] - b.jb, pc[2] - b.kb};
+   DF gm = df_zero(), gl = df_zero(), gr = df_zero();
+   // pair 0: (mt, u) with weight 12 (c2 = 12 c1) and the damping term; pair 1: (b1, w1)
+#pragma unroll 1
+   for (int t = 0; t < 2; t++) {
+      const float2* __restrict__ A = t == 0 ? g.dmt : g.db1;
+      const float2* __restrict__ F = t == 0 ? g.du : g.dw1;
+      const float wt = t == 0 ? 12.f : 1.f;
+#pragma unroll 1
+      for (int a = 0; a < 3; a++) {
+         const int a1 = a == 2 ? 0 : a + 1, a2 = a == 0 ? 2 : a - 1;
+         const int x0 = a == 0 ? pc[0] : a == 1 ? pc[1] : pc[2];
+         const int xl = a == 0 ? b.ib : a == 1 ? b.jb : b.kb, xh = a == 0 ? b.ie : a == 1 ? b.je : b.ke;
+         const long long sd = a == 0 ? 1 : a == 1 ? b.ni : b.nij;
+         const int oa = x0 - xl, o1 = a1 == 0 ? off[0] : a1 == 1 ? off[1] : off[2],
+                   o2 = a2 == 0 ? off[0] : a2 == 1 ? off[1] : off[2];
+         bool ok[5];
+#pragma unroll
+         for (int m = 0; m < 5; m++) ok[m] = x0 + m - 2 >= xl && x0 + m - 2 <= xh;
+         const bool inner = ok[0] && ok[4];
+         const float2 bd = t == 0 ? __ldg(g.bdc[a] + oa) : make_float2(0.f, 0.f);
+         const bool damp = t == 0 && ok[1] && ok[3] && bd.x != 0.f;
+         DF xs = df_zero(), ys = df_zero(), xa = df_zero(), ya = df_zero(), ds = df_zero();
+#pragma unroll
+         for (int c = 0; c < 3; c++) {
+            DF x[5], y[5];
+#pragma unroll
+            for (int m = 0; m < 5; m++) {
+               const long long q = c * n + p + (m - 2) * sd;
+               x[m] = ok[m] ? df_of(__ldg(A + q)) : df_zero();
+               y[m] = ok[m] ? df_of(__ldg(F + q)) : df_zero();
+            }
+            // edges (p-2+e, p-1+e) and (p-2+e, p+e)
+            DF e1[4], e2[3];
+#pragma unroll
+            for (int e = 0; e < 4; e++) e1[e] = df_mul(df_diff(x[e + 1], x[e]), df_diff(y[e + 1], y[e]));
+#pragma unroll
+            for (int e = 0; e < 3; e++) e2[e] = df_mul(df_diff(x[e + 2], x[e]), df_diff(y[e + 2], y[e]));
+            // E1(p+1) + E1(p-2) + E2(p-1) + 3 [E1(p-1) + E1(p) - (E2(p) + E2(p-2))/4]
+            const DF X = df_add(df_add(e1[3], e1[0]), e2[1]);
+            const DF Y = df_add(df_add(e1[1], e1[2]), df_scale(df_add(e2[2], e2[0]), -0.25f));
+            xs = df_add(xs, X);
+            ys = df_add(ys, Y);
+            if (c == a) {
+               xa = X;
+               ya = Y;
+            }
+            // (DW . f)(p) = f(p-2) - f(p+2) + 8 (f(p+1) - f(p-1))
+            const DF fa = df_add(df_diff(x[0], x[4]), df_scale(df_diff(x[3], x[1]), 8.f));
+            const DF fw = inner ? df_add(df_diff(y[0], y[4]), df_scale(df_diff(y[3], y[1]), 8.f)) : df_zero();
+            fd[c * 3 + a][tid] = make_float2(fa.h, fa.l);
+            fd[9 + c * 3 + a][tid] = make_float2(fw.h, fw.l);
+            if (damp) {  // D2(u - um) D2(b1) along a (y holds u)
+               DF d[3], v[3];
+#pragma unroll
+               for (int m = 0; m < 3; m++) {
+                  const long long q = c * n + p + (m - 1) * sd;
+                  d[m] = df_diff(y[m + 1], df_of(__ldg(g.dum + q)));
+                  v[m] = df_of(__ldg(g.db1 + q));
+               }
+               const DF d2u = df_add(df_add(d[0], d[2]), df_scale(d[1], -2.f));
+               const DF d2b = df_add(df_add(v[0], v[2]), df_scale(v[1], -2.f));
+               ds = df_add(ds, df_mul(d2u, d2b));
+            }
+         }
+         const DF i1 = df_of(__ldg(g.ist[a1] + o1)), i2 = df_of(__ldg(g.ist[a2] + o2));
+         const DF qq = df_scale(df_mul(df_mul(df_of(__ldg(g.st24[a] + oa)), i1), i2), wt);
+         gm = df_add(gm, df_mul(qq, df_add(df_add(xs, xa), df_scale(df_add(ys, ya), 3.f))));
+         gl = df_add(gl, df_mul(qq, df_add(xa, df_scale(ya, 3.f))));
+         if (damp) {
+            const DF cc = df_mul(df_of(__ldg(g.cist[a1] + o1)), df_of(__ldg(g.cist[a2] + o2)));
+            gr = df_add(gr, df_neg(df_mul(df_mul(df_of(bd), cc), ds)));
+         }
+      }
+      // mixed terms, grouped by the axis t3 that neither derivative takes:
+      // lambda from the diagonal first differences, mu from the off-diagonal ones
+#pragma unroll 1
+      for (int t3 = 0; t3 < 3; t3++) {
+         const int a1 = t3 == 2 ? 0 : t3 + 1, a2 = t3 == 0 ? 2 : t3 - 1;
+         auto A_ = [&](int c, int a) { return df_of(fd[c * 3 + a][tid]); };
+         auto W_ = [&](int c, int a) { return df_of(fd[9 + c * 3 + a][tid]); };
+         const DF ml = df_add(df_mul(W_(a2, a2), A_(a1, a1)), df_mul(W_(a1, a1), A_(a2, a2)));
+         const DF mm = df_add(df_mul(W_(a2, a1), A_(a1, a2)), df_mul(W_(a1, a2), A_(a2, a1)));
+         const int ot = t3 == 0 ? off[0] : t3 == 1 ? off[1] : off[2];
+         const DF f = df_scale(df_of(__ldg(g.ist[t3] + ot)), wt);
+         gm = df_add(gm, df_mul(f, mm));
+         gl = df_add(gl, df_mul(f, ml));
+      }
+   }
+   acc_add(g.am, p, gm);
+   acc_add(g.al, p, gl);
+   acc_add(g.ar, p, gr);
+}
+
+// g += scale * acc (FP64), acc = 0
+__global__ void __launch_bounds__(256) grad_flush_kernel(long long n, float2* __restrict__ am,
+                                                         float2* __restrict__ al, float2* __restrict__ ar,
+                                                         const int* __restrict__ emax, int marg_a, int marg_f,
+                                                         double kmu, double* __restrict__ gm,
+                                                         double* __restrict__ gl, double* __restrict__ gr)
+{
+   const double sc = ldexp(1.0, shift_of(emax[0], marg_a) + shift_of(emax[1], marg_f));
+   const double km = kmu * sc;
+   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+        q += (long long)gridDim.x * blockDim.x) {
+      const float2 m = am[q], l = al[q], r = ar[q];
+      gm[q] += km * ((double)m.x + (double)m.y);
+      gl[q] += km * ((double)l.x + (double)l.y);
+      gr[q] += sc * ((double)r.x + (double)r.y);
+      am[q] = al[q] = ar[q] = make_float2(0.f, 0.f);
+   }
+}
+
+int grid_stride_blocks(long long n, int threads)
+{
+   long long b = (n + threads - 1) / threads;
+   if (b > 152 * 16) b = 152 * 16;
+   return (int)(b > 0 ? b : 1);
+}
+
+}  // namespace
+
+int launch_grad_df_profiles(const GradDFProfiles& p, cudaStream_t s)
+{
+   for (int a = 0; a < 3; a++) {
+      grad_profiles_kernel<<<blocks_for(p.n[a], 128), 128, 0, s>>>(p.n[a], p.st[a], p.co[a], p.dc[a], p.beta,
+                                                                   p.st24[a], p.ist[a], p.cist[a], p.bdc[a]);
+      SW4G_TRY(launch_status());
+   }
+   return kOk;
+}
+
+int launch_exp_max(const double* x, long long n, int* out, cudaStream_t s)
+{
+   exp_max_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(x, n, out);
+   return launch_status();
+}
+
+int launch_inj_exp(const Box& b, const double* const st[3], int nrec, const int* ijk, const double* res,
+                   long long rows, int nval, const double* rho, int* out, cudaStream_t s)
+{
+   if (nrec <= 0 || rows <= 0) return kOk;
+   inj_exp_kernel<<<blocks_for(rows * nrec, 128), 128, 0, s>>>(b, st[0], st[1], st[2], nrec, ijk, res, rows,
+                                                               nval, rho, out);
+   return launch_status();
+}
+
+int launch_grad_df_step(const GradDF& g, cudaStream_t s)
+{
+   const Box& b = g.b;
+   const int ni = (int)b.ni, nj = b.je - b.jb + 1, nk = b.ke - b.kb + 1;
+   grad_prep_kernel<<<dim3((ni + 127) / 128, nj, nk), 128, 0, s>>>(g);
+   SW4G_TRY(launch_status());
+   grad_df_kernel<<<dim3((ni + 31) / 32, (nj + 3) / 4, nk), dim3(32, 4), 0, s>>>(g);
+   return launch_status();
+}
+
+int launch_grad_df_flush(const GradDF& g, double kmu, double* gm, double* gl, double* gr, cudaStream_t s)
+{
+   grad_flush_kernel<<<grid_stride_blocks(g.b.npts, 256), 256, 0, s>>>(g.b.npts, g.am, g.al, g.ar, g.emax,
+                                                                      g.marg_a, g.marg_f, kmu, gm, gl, gr);
+   return launch_status();
+}
+
+}  // namespace sw4g

@@ -33,6 +33,8 @@
 //   rho        : -W [mt.(up - 2u + um) + b1.(u+ - up)] (the 1/rho factors and
 //                the forcing) - beta dc D2(u - um) . D2(w W b1) (the damping's
 //                rho dc factors).
+// The FP64 form evaluates these sums in double-float arithmetic on the FP32 pipe
+// (adj_grad.cu); the mixed form in FP32 with the kernels below.
 // Forward levels come from checkpoints every C steps, recomputed one segment
 // at a time with every level and predicted level kept in HBM.
 #include <algorithm>
@@ -63,12 +65,8 @@ __device__ __forceinline__ T sxyz(const Box& b, const ProfT<T>& f, int i, int j,
    return f.st[0][i - b.ib] * f.st[1][j - b.jb] * f.st[2][k - b.kb];
 }
 
-// a[q] - b[q] of two levels: FP64, or double-float (hi at q, lo at q + lo) formed
-// exactly and rounded once to FP32
-__device__ __forceinline__ double lev_diff(const double* a, const double* b, long long q, long long)
-{
-   return a[q] - b[q];
-}
+// a[q] - b[q] of two double-float levels (hi at q, lo at q + lo), formed exactly and
+// rounded once to FP32
 __device__ __forceinline__ float lev_diff(const float* a, const float* b, long long q, long long lo)
 {
    float d, e;
@@ -81,33 +79,6 @@ __device__ __forceinline__ void grid_point(const Box& b, long long p, int& i, in
    i = b.ib + (int)(p % b.ni);
    j = b.jb + (int)((p / b.ni) % (b.je - b.jb + 1));
    k = b.kb + (int)(p / b.nij);
-}
-
-// w1 = up - 2u + um
-__global__ void adj_w1_kernel(long long n3, const double* __restrict__ up, const double* __restrict__ u,
-                              const double* __restrict__ um, double* __restrict__ w1)
-{
-   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n3;
-        q += (long long)gridDim.x * blockDim.x)
-      w1[q] = (up[q] - 2 * u[q]) + um[q];
-}
-
-// v1 = c1 W b1, v2 = c2 W mt (W = 1/(sx sy sz); both zero outside I)
-__global__ void adj_v_kernel(Box b, Prof f, const double* __restrict__ b1,
-                             const double* __restrict__ mt, double c1, double c2,
-                             double* __restrict__ v1, double* __restrict__ v2)
-{
-   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < b.npts;
-        p += (long long)gridDim.x * blockDim.x) {
-      int i, j, k;
-      grid_point(b, p, i, j, k);
-      const double w = 1.0 / sxyz(b, f, i, j, k);
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-         v1[c * b.npts + p] = c1 * w * b1[c * b.npts + p];
-         v2[c * b.npts + p] = c2 * w * mt[c * b.npts + p];
-      }
-   }
 }
 
 // b[receiver point] += W^-1 R res (receivers in order, 3 values each)
@@ -525,7 +496,14 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
    if (st == kOk) st = alloc(&pred, (size_t)seglen * lv);
    if (st == kOk) st = alloc(&work, 9 * lv);  // adjoint work (7) + the forward's final levels (2)
    if (st == kOk) st = alloc(&resd, (size_t)(nsteps + 1) * nval * sizeof(double));
-   if (st == kOk) st = alloc(&adj_edges_, 12 * (size_t)npts_ * sizeof(double));
+   if (st == kOk && mixed_) st = alloc(&adj_edges_, 12 * (size_t)npts_ * sizeof(double));
+   // FP64 form: double-float copies of the step's levels (5), the per-point sums (1),
+   // the 1-D profile pairs and the two exponent maxima (adj_grad.cu)
+   double *dfw = nullptr, *dfp = nullptr, *dfe = nullptr;
+   const int nax[3] = {bd.ie - bd.ib + 1, bd.je - bd.jb + 1, bd.ke - bd.kb + 1};
+   if (st == kOk && !mixed_) st = alloc(&dfw, 6 * lv);
+   if (st == kOk && !mixed_) st = alloc(&dfp, 4 * (size_t)(nax[0] + nax[1] + nax[2]) * sizeof(float2));
+   if (st == kOk && !mixed_) st = alloc(&dfe, sizeof(double));
    double* gr_d = g_rho;
    double* gm_d = g_mu;
    double* gl_d = g_la;
@@ -545,7 +523,6 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       cleanup();
       return st;
    }
-   const int blocks = gs_blocks(npts_, 256);
    Prof pf;
    for (int a = 0; a < 3; a++) {
       pf.dc[a] = dprof_[a];
@@ -579,6 +556,47 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       ms.dt = dt;
    }
    auto F = [](double* x) { return reinterpret_cast<float*>(x); };
+   GradDF gd;
+   GradDFProfiles gp{};
+   int* emax = reinterpret_cast<int*>(dfe);
+   if (!mixed_) {
+      float2* f2 = reinterpret_cast<float2*>(dfw);
+      gd.b = b;
+      gd.db1 = f2;
+      gd.dmt = f2 + n3;
+      gd.dw1 = f2 + 2 * n3;
+      gd.du = f2 + 3 * n3;
+      gd.dum = f2 + 4 * n3;
+      gd.am = f2 + 5 * n3;
+      gd.al = gd.am + npts_;
+      gd.ar = gd.al + npts_;
+      gd.emax = emax;
+      // Each class's bound maps to 2^26..2^28: the largest products (x 1/(s_b s_c) <=
+      // 2^32 in the supergrid layers, x 12, summed) stay below 2^110, and values down
+      // to 2^-131 of the bound keep all 47 bits (FP32's lo word reaches 2^-103).
+      int marg = 4;
+      while ((1LL << (marg - 4)) < (long long)nsteps + 1) marg++;
+      gd.marg_a = marg - 30;  // the adjoint level is at most (steps) x (largest injection)
+      gd.marg_f = 4 - 32;     // w1 = up - 2u + um is at most 4 x the largest level
+      float2* pp = reinterpret_cast<float2*>(dfp);
+      gp.beta = beta;
+      for (int a = 0; a < 3; a++) {
+         gp.n[a] = nax[a];
+         gp.st[a] = dprof_[3 + a];
+         gp.co[a] = dprof_[6 + a];
+         gp.dc[a] = dprof_[a];
+         gp.st24[a] = pp;
+         gp.ist[a] = pp + nax[a];
+         gp.cist[a] = pp + 2 * nax[a];
+         gp.bdc[a] = pp + 3 * nax[a];
+         pp += 4 * nax[a];
+         gd.st24[a] = gp.st24[a];
+         gd.ist[a] = gp.ist[a];
+         gd.cist[a] = gp.cist[a];
+         gd.bdc[a] = gp.bdc[a];
+      }
+   }
+   const double kmu = -(dt * dt / 12) / (144 * g_.h * g_.h);
 
    auto run = [&]() -> int {
       SW4G_TRY(cuda_ok(cudaMemsetAsync(gr_d, 0, npts_ * sizeof(double), stream_)));
@@ -613,6 +631,13 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       }
       *misfit = J;
       SW4G_TRY(cuda_ok(cudaMemcpy(resd, rec.data(), rec.size() * sizeof(double), cudaMemcpyHostToDevice)));
+      if (!mixed_) {  // the adjoint level's shift from its sources; the per-point sums zeroed
+         SW4G_TRY(cuda_ok(cudaMemsetAsync(dfe, 0, sizeof(double), stream_)));
+         const double* stp[3] = {dprof_[3], dprof_[4], dprof_[5]};
+         SW4G_TRY(launch_inj_exp(b, stp, drec_.n, drec_.ijk, resd, nsteps + 1, nval, rho_, emax, stream_));
+         SW4G_TRY(launch_grad_df_profiles(gp, stream_));
+         SW4G_TRY(cuda_ok(cudaMemsetAsync(gd.am, 0, 3 * (size_t)npts_ * sizeof(float2), stream_)));
+      }
 
       double* b1 = work;           // scaled adjoint b = W^-1 R a at n+1
       double* b2 = work + n3;      // at n+2
@@ -663,50 +688,24 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
             status = adjoint_step_mixed(ms, &pf, &pf32, b, n3, u, um, up, un, b1, b2, bn, mt, w1, v1, v2,
                                         gr_d, gm_d, gl_d, dt, beta, saved_n, res, clk, nval);
          } else {
-            adj_w1_kernel<<<gs_blocks(n3, 256), 256, 0, stream_>>>(n3, up, u, um, w1);
-            status = launch_status();
-            if (status == kOk) {  // mt = b1 + dt^2/12 R L(b1): predictor form, um = u
-               fs.corrector = 0;
-               fs.u = b1;
-               fs.um = b1;
-               fs.up = nullptr;
-               fs.out = mt;
-               fs.beta = 0;
-               fs.coef = dt * dt / 12;
-               status = launch_fused_stage(fs, stream_);
-            }
-            if (status == kOk) {
-               adj_v_kernel<<<blocks, 256, 0, stream_>>>(b, pf, b1, mt, dt * dt / 12, dt * dt, v1, v2);
-               status = launch_status();
-            }
-            if (status == kOk) {
-               GradArgs<double> ga;
-               ga.lo = 0;
-               ga.b = b;
-               ga.f = pf;
-               ga.v1 = v1;
-               ga.v2 = v2;
-               ga.rho = rho_;
-               ga.u = u;
-               ga.um = um;
-               ga.up = up;
-               ga.un = un;
-               ga.w1 = w1;
-               ga.gr = gr_d;
-               ga.gm = gm_d;
-               ga.gl = gl_d;
-               ga.c1 = dt * dt / 12;
-               ga.c2 = dt * dt;
-               ga.ih2 = 1 / (g_.h * g_.h);
-               ga.beta = beta;
-               ga.ed = adj_edges_;
-               grad_constants(ga);
-               adj_edge_kernel<double><<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
-               status = launch_status();
-               if (status == kOk) {
-                  adj_gradient_kernel<double><<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
-                  status = launch_status();
-               }
+            // mt = b1 + dt^2/12 R L(b1): predictor form, um = u
+            fs.corrector = 0;
+            fs.u = b1;
+            fs.um = b1;
+            fs.up = nullptr;
+            fs.out = mt;
+            fs.beta = 0;
+            fs.coef = dt * dt / 12;
+            status = launch_fused_stage(fs, stream_);
+            if (status == kOk) {  // the gradient terms of the step (double-float sums)
+               GradDF g = gd;
+               g.b1 = b1;
+               g.mt = mt;
+               g.up = up;
+               g.u = u;
+               g.um = um;
+               g.un = un;
+               status = launch_grad_df_step(g, stream_);
             }
             if (status == kOk) {  // b^n = 2 b1 - b2 + dt^2 R L(mt) - beta R SG(b1 - b2)
                fs.corrector = 2;
@@ -737,7 +736,15 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
             SW4G_TRY(cuda_ok(cudaMemcpyAsync(seg + (size_t)(nn - s0 + 2) * n3, lev_[iu_], lv,
                                              cudaMemcpyDeviceToDevice, stream_)));
          }
+         if (!mixed_) {  // the forward levels' shift: the largest exponent over the segment
+            SW4G_TRY(cuda_ok(cudaMemsetAsync(emax + 1, 0, sizeof(int), stream_)));
+            SW4G_TRY(launch_exp_max(seg, (long long)(s1 - s0 + 2) * (long long)n3, emax + 1, stream_));
+         }
          return kOk;
+      };
+      // the segment's double-float sums into the FP64 gradients
+      auto flush = [&]() -> int {
+         return mixed_ ? kOk : launch_grad_df_flush(gd, kmu, gm_d, gl_d, gr_d, stream_);
       };
       auto rotate = [&]() {
          double* tmp = b2;
@@ -797,7 +804,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
                      SW4G_TRY(adj_step(nn, s0, b1, b2, bn, true));
                      rotate();
                   }
-                  return kOk;
+                  return flush();
                }, &ex);
                if (status == kOk) {
                   agraphs.emplace_back(key, ex);
@@ -812,6 +819,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
                status = adj_step(nn, s0, b1, b2, bn, false);
                rotate();
             }
+            if (status == kOk) status = flush();
             adj_warm = true;
          }
       }
