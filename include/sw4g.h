@@ -299,12 +299,19 @@ int sw4g_ew_step(sw4g_ew* ew, int nsteps, int mode);
  * J = 1/2 sum_{n=0..nsteps} sum_r |rec^n_r - obs^n_r|^2 (obs: (nsteps+1) x nvals,
  * the record layout) and dJ/drho, dJ/dmu, dJ/dlambda at every array point (npts
  * each), by the exact transpose of the step with checkpoints every
- * checkpoint_every steps.  Device memory: (2*ceil(nsteps/C) + 2*C + 11) levels of
- * 3*npts doubles.  Requires Dirichlet or supergrid sides (zero ghost data), 4th-order
- * damping, no topography.  The object ends at the end of the forward run. */
+ * checkpoint_every steps.  Device memory: (2*ceil(nsteps/C) + 2*C + 15) levels of
+ * 3*npts doubles, plus the segments kept from the forward run (below).  Requires
+ * Dirichlet or supergrid sides (zero ghost data), 4th-order damping, no topography.
+ * The object ends at the end of the forward run. */
 int sw4g_ew_gradient(sw4g_ew* ew, int nsteps, int checkpoint_every, const double* observed,
                      int obs_on_device, double* misfit, double* grad_rho, double* grad_mu,
                      double* grad_lambda, int grad_on_device);
+/* The forward run of sw4g_ew_gradient keeps every level of its last segment, and of
+ * as many segments before it as max_bytes allows (2C+2 levels each), so the backward
+ * sweep recomputes only the others from their checkpoints.  max_bytes < 0 (the
+ * default): all free device memory but a reserve of max(4 GiB, 1/32 of the device);
+ * 0: only the last segment. */
+int sw4g_ew_set_gradient_memory(sw4g_ew* ew, long long max_bytes);
 
 /* Topography (replaces the reference's topography + curvilinear grid set-up,
  * src/EW.C:540-720 (deck), 2018-2046 (dimensions), 6164 (generate_grid), 6229

@@ -105,6 +105,7 @@ _SIGS = {
     "sw4g_ew_compute_time_step": ([_VP, C.c_double, C.c_double, _D, _I], C.c_int),
     "sw4g_ew_time": ([_VP], C.c_double),
     "sw4g_ew_set_graphs": ([_VP, C.c_int], C.c_int),
+    "sw4g_ew_set_gradient_memory": ([_VP, C.c_longlong], C.c_int),
     "sw4g_discretize_source_topo": ([_VP, _VP, C.c_int, _D, _VP, C.c_int, _I, _D, _I, _I, _D, _I], C.c_int),
     "sw4g_ew_grid_point_sources": ([_VP, C.c_int, C.c_int, _I, _D, _I], C.c_int),
     "sw4g_ew_set_fields": ([_VP, _VP, _VP, C.c_int], C.c_int),
@@ -310,6 +311,12 @@ class EW:
     def set_graphs(self, on=True):
         """Replay the fused time loop (and the gradient's loops) as CUDA graphs."""
         check(lib().sw4g_ew_set_graphs(self._h, int(bool(on))), "set_graphs")
+
+    def set_gradient_memory(self, max_bytes):
+        """Device memory gradient() may add for segments kept from its forward run
+        (their recompute is skipped): < 0 all free memory but a reserve, 0 none
+        beyond the last segment."""
+        check(lib().sw4g_ew_set_gradient_memory(self._h, int(max_bytes)), "set_gradient_memory")
 
     def compute_time_step(self, cfl, tmax):
         dt = C.c_double()

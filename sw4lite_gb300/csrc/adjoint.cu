@@ -481,7 +481,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
    const size_t n3 = 3 * (size_t)npts_, lv = n3 * sizeof(double);
    const int nseg = (nsteps + ckpt - 1) / ckpt;
    const int seglen = std::min(ckpt, nsteps);
-   const double t0 = t_, dt = dt_;
+   const double dt = dt_;
 
    // device memory: checkpoints, one segment of levels and predicted levels, adjoint work
    std::vector<double*> bufs;
@@ -523,6 +523,37 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       cleanup();
       return st;
    }
+   // Segments kept from the forward run, whose recompute the backward sweep skips:
+   // the last one in seg/pred, and before it as many as the store budget holds
+   // (each 2C + 2 levels; by default the free device memory less a reserve).
+   const size_t segbytes = (size_t)(2 * seglen + 2) * lv;
+   std::vector<double*> xbuf;
+   if (nseg > 1 && grad_store_bytes_ != 0) {
+      size_t freeb = 0, totb = 0;
+      if (cudaMemGetInfo(&freeb, &totb) == cudaSuccess) {
+         const size_t reserve = std::max((size_t)4 << 30, totb / 32);
+         size_t budget = freeb > reserve ? freeb - reserve : 0;
+         if (grad_store_bytes_ > 0) budget = std::min(budget, (size_t)grad_store_bytes_);
+         const int want = (int)std::min<size_t>((size_t)nseg - 1, budget / segbytes);
+         for (int q = 0; q < want; q++) {
+            double* x = nullptr;
+            if (cudaMalloc(&x, segbytes) != cudaSuccess) {
+               cudaGetLastError();
+               break;
+            }
+            bufs.push_back(x);
+            xbuf.push_back(x);
+         }
+      }
+   }
+   const int nkept = 1 + (int)xbuf.size();
+   std::vector<double> tseg(nseg);  // the time at each segment's start in the forward run
+   auto kept = [&](int sg) { return sg >= nseg - nkept; };
+   // buffers of segment sg: levels u^{s0-1..s1} and predicted levels up^{s0..s1-1}
+   auto seg_of = [&](int sg) { return kept(sg) && sg < nseg - 1 ? xbuf[nseg - 2 - sg] : seg; };
+   auto pred_of = [&](int sg) {
+      return kept(sg) && sg < nseg - 1 ? xbuf[nseg - 2 - sg] + (size_t)(seglen + 2) * n3 : pred;
+   };
    Prof pf;
    for (int a = 0; a < 3; a++) {
       pf.dc[a] = dprof_[a];
@@ -608,11 +639,30 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       // forward with checkpoints; receivers record from row 0
       rec_rows_ = 0;
       rec_initial_ = true;
-      for (int nn = 0; nn < nsteps; nn += ckpt) {
-         double* c0 = ck + 2 * (size_t)(nn / ckpt) * n3;
+      for (int sg = 0; sg < nseg; sg++) {
+         const int nn = sg * ckpt, s1 = std::min(nsteps, nn + ckpt);
+         double* c0 = ck + 2 * (size_t)sg * n3;
+         tseg[sg] = t_;  // the recompute restarts from this time, bit for bit
          SW4G_TRY(cuda_ok(cudaMemcpyAsync(c0, lev_[iu_], lv, cudaMemcpyDeviceToDevice, stream_)));
          SW4G_TRY(cuda_ok(cudaMemcpyAsync(c0 + n3, lev_[ium_], lv, cudaMemcpyDeviceToDevice, stream_)));
-         SW4G_TRY(step(std::min(ckpt, nsteps - nn), kModeFused));  // graphed when graphs are on
+         if (!kept(sg)) {
+            SW4G_TRY(step(s1 - nn, kModeFused));  // graphed when graphs are on
+            continue;
+         }
+         // a kept segment: every level and predicted level into its buffers
+         SW4G_TRY(step(0, kModeFused));  // sources uploaded, the initial record row
+         double* sq = seg_of(sg);
+         double* pq = pred_of(sg);
+         SW4G_TRY(cuda_ok(cudaMemcpyAsync(sq, lev_[ium_], lv, cudaMemcpyDeviceToDevice, stream_)));
+         SW4G_TRY(cuda_ok(cudaMemcpyAsync(sq + n3, lev_[iu_], lv, cudaMemcpyDeviceToDevice, stream_)));
+         for (int n = nn; n < s1; n++) {
+            capture_pred_ = pq + (size_t)(n - nn) * n3;
+            const int status = step_fused();
+            capture_pred_ = nullptr;
+            SW4G_TRY(status);
+            SW4G_TRY(cuda_ok(cudaMemcpyAsync(sq + (size_t)(n - nn + 2) * n3, lev_[iu_], lv,
+                                             cudaMemcpyDeviceToDevice, stream_)));
+         }
       }
       const double t_end = t_;
       double* fin = work + 7 * n3;  // u^N, u^{N-1}: the recompute overwrites the levels
@@ -676,11 +726,13 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       drec_.n = 0;  // no recording while segments are recomputed
       // one adjoint step nn of the segment starting at s0 (step nn maps u^nn, u^{nn-1}
       // to u^{nn+1}); with the device clock its residual row is clock[2]
+      double* segp = seg;  // the buffers of the segment being swept
+      double* predp = pred;
       auto adj_step = [&](int nn, int s0, double* b1, double* b2, double* bn, bool clocked) -> int {
-         const double* u = seg + (size_t)(nn - s0 + 1) * n3;
-         const double* um = seg + (size_t)(nn - s0) * n3;
-         const double* up = pred + (size_t)(nn - s0) * n3;
-         const double* un = seg + (size_t)(nn - s0 + 2) * n3;
+         const double* u = segp + (size_t)(nn - s0 + 1) * n3;
+         const double* um = segp + (size_t)(nn - s0) * n3;
+         const double* up = predp + (size_t)(nn - s0) * n3;
+         const double* un = segp + (size_t)(nn - s0 + 2) * n3;
          const double* clk = clocked ? dclock_ : nullptr;
          const double* res = clocked ? resd : resd + (size_t)nn * nval;
          int status = kOk;
@@ -736,11 +788,13 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
             SW4G_TRY(cuda_ok(cudaMemcpyAsync(seg + (size_t)(nn - s0 + 2) * n3, lev_[iu_], lv,
                                              cudaMemcpyDeviceToDevice, stream_)));
          }
-         if (!mixed_) {  // the forward levels' shift: the largest exponent over the segment
-            SW4G_TRY(cuda_ok(cudaMemsetAsync(emax + 1, 0, sizeof(int), stream_)));
-            SW4G_TRY(launch_exp_max(seg, (long long)(s1 - s0 + 2) * (long long)n3, emax + 1, stream_));
-         }
          return kOk;
+      };
+      // the forward levels' shift: the largest exponent over the segment's levels
+      auto seg_scale = [&](int s0, int s1) -> int {
+         if (mixed_) return kOk;
+         SW4G_TRY(cuda_ok(cudaMemsetAsync(emax + 1, 0, sizeof(int), stream_)));
+         return launch_exp_max(segp, (long long)(s1 - s0 + 2) * (long long)n3, emax + 1, stream_);
       };
       // the segment's double-float sums into the FP64 gradients
       auto flush = [&]() -> int {
@@ -757,46 +811,58 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       // of (b1, b2, bn); the first adjoint segment runs directly
       cudaGraphExec_t rgraph = nullptr;
       int r_iu = 0, r_ium = 0;
-      std::vector<std::pair<double*, cudaGraphExec_t>> agraphs;
+      struct AdjGraph {
+         double* b1;
+         double* seg;
+         cudaGraphExec_t exec;
+      };
+      std::vector<AdjGraph> agraphs;
       bool adj_warm = false;
       int status = kOk;
       for (int sg = nseg - 1; sg >= 0 && status == kOk; sg--) {
          const int s0 = sg * ckpt, s1 = std::min(nsteps, s0 + ckpt);
          const bool full = graphs_ && s1 - s0 == ckpt;
-         if (full) {
-            iu_ = 2;
-            ium_ = 3;
-         }
-         double* c0 = ck + 2 * (size_t)sg * n3;
-         status = cuda_ok(cudaMemcpyAsync(lev_[iu_], c0, lv, cudaMemcpyDeviceToDevice, stream_));
-         if (status == kOk)
-            status = cuda_ok(cudaMemcpyAsync(lev_[ium_], c0 + n3, lv, cudaMemcpyDeviceToDevice, stream_));
-         if (status == kOk) status = cuda_ok(cudaMemcpyAsync(seg, c0 + n3, lv, cudaMemcpyDeviceToDevice, stream_));
-         if (status == kOk) status = cuda_ok(cudaMemcpyAsync(seg + n3, c0, lv, cudaMemcpyDeviceToDevice, stream_));
-         t_ = t0 + s0 * dt;
-         if (status == kOk && full) {
-            status = sync_clock();
-            clocked_ = true;
-            if (status == kOk && !rgraph) {
-               status = capture([&]() { return recompute(s0, s1); }, &rgraph);
-               r_iu = iu_;
-               r_ium = ium_;
-               if (status == kOk) status = cuda_ok(cudaGraphLaunch(rgraph, stream_));
-            } else if (status == kOk) {
-               status = cuda_ok(cudaGraphLaunch(rgraph, stream_));
-               iu_ = r_iu;
-               ium_ = r_ium;
+         segp = seg_of(sg);
+         predp = pred_of(sg);
+         if (kept(sg)) {
+            status = seg_scale(s0, s1);
+         } else {
+            if (full) {
+               iu_ = 2;
+               ium_ = 3;
             }
-            clocked_ = false;
-         } else if (status == kOk) {
-            status = recompute(s0, s1);
+            double* c0 = ck + 2 * (size_t)sg * n3;
+            status = cuda_ok(cudaMemcpyAsync(lev_[iu_], c0, lv, cudaMemcpyDeviceToDevice, stream_));
+            if (status == kOk)
+               status = cuda_ok(cudaMemcpyAsync(lev_[ium_], c0 + n3, lv, cudaMemcpyDeviceToDevice, stream_));
+            if (status == kOk) status = cuda_ok(cudaMemcpyAsync(seg, c0 + n3, lv, cudaMemcpyDeviceToDevice, stream_));
+            if (status == kOk) status = cuda_ok(cudaMemcpyAsync(seg + n3, c0, lv, cudaMemcpyDeviceToDevice, stream_));
+            t_ = tseg[sg];
+            if (status == kOk && full) {
+               status = sync_clock();
+               clocked_ = true;
+               if (status == kOk && !rgraph) {
+                  status = capture([&]() { return recompute(s0, s1); }, &rgraph);
+                  r_iu = iu_;
+                  r_ium = ium_;
+                  if (status == kOk) status = cuda_ok(cudaGraphLaunch(rgraph, stream_));
+               } else if (status == kOk) {
+                  status = cuda_ok(cudaGraphLaunch(rgraph, stream_));
+                  iu_ = r_iu;
+                  ium_ = r_ium;
+               }
+               clocked_ = false;
+            } else if (status == kOk) {
+               status = recompute(s0, s1);
+            }
+            if (status == kOk) status = seg_scale(s0, s1);
          }
          if (status != kOk) break;
          if (full && adj_warm) {
             status = sync_clock((double)(s1 - 1));
             cudaGraphExec_t ex = nullptr;
             for (auto& g : agraphs)
-               if (g.first == b1) ex = g.second;
+               if (g.b1 == b1 && g.seg == segp) ex = g.exec;
             if (status == kOk && !ex) {
                double* key = b1;
                status = capture([&]() -> int {
@@ -807,7 +873,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
                   return flush();
                }, &ex);
                if (status == kOk) {
-                  agraphs.emplace_back(key, ex);
+                  agraphs.push_back(AdjGraph{key, segp, ex});
                   status = cuda_ok(cudaGraphLaunch(ex, stream_));
                }
             } else if (status == kOk) {
@@ -825,7 +891,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       }
       if (rgraph || !agraphs.empty()) cudaStreamSynchronize(stream_);
       if (rgraph) cudaGraphExecDestroy(rgraph);
-      for (auto& g : agraphs) cudaGraphExecDestroy(g.second);
+      for (auto& g : agraphs) cudaGraphExecDestroy(g.exec);
       drec_.n = keep_rec ? saved_n : 0;
       if (status != kOk) return status;
       // the object ends where the forward run ended

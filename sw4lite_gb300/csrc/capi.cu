@@ -491,6 +491,12 @@ int sw4g_ew_gradient(sw4g_ew* ew, int nsteps, int checkpoint_every, const double
                              grad_rho, grad_mu, grad_lambda, grad_on_device != 0);
 }
 
+int sw4g_ew_set_gradient_memory(sw4g_ew* ew, long long max_bytes)
+{
+   if (!ew) return SW4G_BAD_ARGUMENT;
+   return ew->impl->set_gradient_memory(max_bytes);
+}
+
 int sw4g_ew_num_grids(const sw4g_ew* ew) { return ew ? ew->impl->num_grids() : -1; }
 
 int sw4g_ew_grid_dims(const sw4g_ew* ew, int grid, int* nx, int* ny, int* nz, long long* npts)

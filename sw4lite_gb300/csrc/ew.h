@@ -110,6 +110,14 @@ class EW {
    // Dirichlet / supergrid sides only.  The object ends after the forward run.
    int gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, double* misfit,
                 double* g_rho, double* g_mu, double* g_la, bool grad_on_device);
+   // Device memory gradient() may add for segments kept from its forward run (whose
+   // recompute the backward sweep then skips): < 0 all free memory but a reserve
+   // (the default), 0 none beyond the last segment, else at most this many bytes.
+   int set_gradient_memory(long long bytes)
+   {
+      grad_store_bytes_ = bytes;
+      return kOk;
+   }
 
    // Grids: 0 the Cartesian grid, 1 the curvilinear grid (with topography).
    int num_grids() const { return cv_ ? 2 : 1; }
@@ -226,6 +234,7 @@ class EW {
    std::unique_ptr<CurvGrid> cv_;
    double* capture_pred_ = nullptr;  // if set, a fused step copies its predicted level here
    double* adj_edges_ = nullptr;     // gradient(): edge products of the adjoint step
+   long long grad_store_bytes_ = -1;  // gradient(): budget for kept segments
 
    double t_ = 0, dt_ = 0;
 

@@ -7,6 +7,8 @@
   adjoint workload (smooth 5% log-normal heterogeneity, one point force, 16
   receivers): the directional derivative along a smooth random direction in
   (rho, mu, lambda) to 1e-6 relative.
+* Segments kept from the forward run (sw4g_ew_set_gradient_memory) instead of
+  recomputed give bit-identical results.
 """
 import numpy as np
 import pytest
@@ -41,8 +43,10 @@ def _ew(case, mat=None, precision=sg.FP64):
     return ew
 
 
-def _gpu_gradient(case, obs, ckpt, precision=sg.FP64):
+def _gpu_gradient(case, obs, ckpt, precision=sg.FP64, memory=None):
     ew = _ew(case, precision=precision)
+    if memory is not None:
+        ew.set_gradient_memory(memory)
     g = [dev(np.zeros(case.npts)) for _ in range(3)]
     J = ew.gradient(case.nsteps, ckpt, dev(obs), *g)
     # the object ends after the forward run
@@ -65,13 +69,15 @@ def _rel(a, b):
     return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
 
-@pytest.mark.parametrize("ckpt", [30, 7, 1])
-def test_gradient_matches_oracle_adjoint(ckpt):
+# memory 0: every segment but the last recomputed from its checkpoint; None: the
+# default budget, which keeps every segment of these small cases
+@pytest.mark.parametrize("ckpt,memory", [(30, None), (7, 0), (7, None), (1, 0)])
+def test_gradient_matches_oracle_adjoint(ckpt, memory):
     c = AdjointCase()
     obs_case = AdjointCase(seed=11)
     obs = obs_case.records(oracle_forward(obs_case)[0][1:])
     J0, gr, gm, gl = oracle_gradient(c, obs)
-    J, (r, m, l), ufin = _gpu_gradient(c, obs, ckpt)
+    J, (r, m, l), ufin = _gpu_gradient(c, obs, ckpt, memory=memory)
     assert J == pytest.approx(J0, rel=1e-12)
     assert _rel(r, gr) <= 1e-9
     assert _rel(m, gm) <= 1e-9
@@ -169,3 +175,21 @@ def test_mixed_gradient_close_to_fp64(ckpt):
     assert J1 == pytest.approx(J0, rel=1e-6)
     for a, b in zip(g1, g0):
         assert _rel(a, b) <= 1e-5, _rel(a, b)
+
+
+@pytest.mark.parametrize("precision", [sg.FP64, sg.MIXED])
+def test_kept_segments_bit_identical(precision):
+    """No extra segments kept, two kept, and all kept: identical misfit and gradients."""
+    c = AdjointCase(nsteps=47)
+    obs_case = AdjointCase(seed=11, nsteps=47)
+    obs = obs_case.records(oracle_forward(obs_case)[0][1:])
+    ckpt = 9  # 5 full segments of 9 steps and one of 2
+    seg_bytes = (2 * ckpt + 2) * 3 * c.npts * 8
+    res = [_gpu_gradient(c, obs, ckpt, precision=precision, memory=m)
+           for m in (0, 2 * seg_bytes + seg_bytes // 2, -1)]
+    for J, g, u in res[1:]:
+        assert J == res[0][0]
+        for x, y in zip(g, res[0][1]):
+            assert np.array_equal(x, y)
+        assert np.array_equal(u, res[0][2])
+    assert max(np.max(np.abs(x)) for x in res[0][1]) > 0

@@ -90,8 +90,8 @@ def test_graphed_topography_steps_bit_identical():
         assert np.array_equal(x, y)
 
 
-@pytest.mark.parametrize("precision", [sg.FP64, sg.MIXED])
-def test_graphed_gradient_bit_identical(precision):
+@pytest.mark.parametrize("precision,memory", [(sg.FP64, 0), (sg.FP64, -1), (sg.MIXED, 0)])
+def test_graphed_gradient_bit_identical(precision, memory):
     c = AdjointCase(nsteps=47)
     obs_case = AdjointCase(seed=11, nsteps=47)
     obs = obs_case.records(oracle_forward(obs_case)[0][1:])
@@ -105,6 +105,7 @@ def test_graphed_gradient_bit_identical(precision):
             ew.add_source(s)
         ew.set_time_step(c.dt, 0.0)
         ew.set_receivers(c.rec, [sg.REC_DISPLACEMENT] * len(c.rec), c.nsteps + 1)
+        ew.set_gradient_memory(memory)  # 0: segments recomputed (graphed), -1: kept
         if graphs:
             ew.set_graphs(True)
         gr = [np.zeros(c.npts) for _ in range(3)]
