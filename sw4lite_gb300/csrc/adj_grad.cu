@@ -72,6 +72,18 @@ __device__ __forceinline__ DF df_mul(DF a, DF b)
    return {p, e};
 }
 
+// a + b without the final renormalisation (the trailing part within a few ulp of
+// the leading one): for sums that feed a product or another sum
+__device__ __forceinline__ DF df_addf(DF a, DF b)
+{
+   float s, e;
+   two_sum(a.h, b.h, s, e);
+   return {s, __fadd_rn(e, __fadd_rn(a.l, b.l))};
+}
+
+// k a for a power of two k (exact)
+__device__ __forceinline__ DF df_pow2(DF a, float k) { return {__fmul_rn(k, a.h), __fmul_rn(k, a.l)}; }
+
 // k a for a small integer k (the rounding of k a.h kept)
 __device__ __forceinline__ DF df_scale(DF a, float k)
 {
@@ -204,9 +216,99 @@ __global__ void __launch_bounds__(128) grad_prep_kernel(GradDF g)
    }
 }
 
-// the mu, lambda and damping rho sums of one point (32 x 4 points per CTA)
-constexpr int kGradThreads = 128;
+constexpr int kGradThreads = 128;  // 32 x 4 points per CTA
 
+// the four edge sums {E1 mu, E1 lambda, E2 mu, E2 lambda} of the forward edges
+// (q, q+1) and (q, q+2) along axis a, summed over the components (mu weight 2 for
+// the component along a, lambda weight for it alone) and the pairs 12 x (mt, u) +
+// (b1, w1).  CHECK: some of q, q+1, q+2 lie outside the array along a (values there
+// count as zero; q may lie below the array).
+template <bool CHECK>
+__device__ __forceinline__ void edges_body(const GradDF& g, long long n, int pq, bool ok0, bool ok1, bool ok2,
+                                           int sd, int a, DF E[4])
+{
+   E[0] = E[1] = E[2] = E[3] = df_zero();
+#pragma unroll
+   for (int t = 0; t < 2; t++) {
+      DF s1 = df_zero(), s2 = df_zero(), a1 = df_zero(), a2 = df_zero();
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+         const float2* __restrict__ A = (t == 0 ? g.dmt : g.db1) + c * n;
+         const float2* __restrict__ F = (t == 0 ? g.du : g.dw1) + c * n;
+         DF x0, x1, x2, y0, y1, y2;
+         if (CHECK) {
+            x0 = ok0 ? df_of(__ldg(A + pq)) : df_zero();
+            y0 = ok0 ? df_of(__ldg(F + pq)) : df_zero();
+            x1 = ok1 ? df_of(__ldg(A + pq + sd)) : df_zero();
+            y1 = ok1 ? df_of(__ldg(F + pq + sd)) : df_zero();
+            x2 = ok2 ? df_of(__ldg(A + pq + 2 * sd)) : df_zero();
+            y2 = ok2 ? df_of(__ldg(F + pq + 2 * sd)) : df_zero();
+         } else {
+            x0 = df_of(__ldg(A + pq));
+            y0 = df_of(__ldg(F + pq));
+            x1 = df_of(__ldg(A + pq + sd));
+            y1 = df_of(__ldg(F + pq + sd));
+            x2 = df_of(__ldg(A + pq + 2 * sd));
+            y2 = df_of(__ldg(F + pq + 2 * sd));
+         }
+         const DF e1 = df_mul(df_diff(x1, x0), df_diff(y1, y0));
+         const DF e2 = df_mul(df_diff(x2, x0), df_diff(y2, y0));
+         s1 = df_add(s1, e1);
+         s2 = df_add(s2, e2);
+         if (c == a) {
+            a1 = e1;
+            a2 = e2;
+         }
+      }
+      const float wt = t == 0 ? 12.f : 1.f;
+      E[0] = df_add(E[0], df_scale(df_addf(s1, a1), wt));
+      E[1] = df_add(E[1], df_scale(a1, wt));
+      E[2] = df_add(E[2], df_scale(df_addf(s2, a2), wt));
+      E[3] = df_add(E[3], df_scale(a2, wt));
+   }
+}
+
+__device__ __forceinline__ void edges_at(const GradDF& g, long long n, int pq, int xq, int xl, int xh, int sd,
+                                         int a, DF E[4])
+{
+   if (xq >= xl && xq + 2 <= xh)
+      edges_body<false>(g, n, pq, true, true, true, sd, a, E);
+   else
+      edges_body<true>(g, n, pq, xq >= xl, xq + 1 >= xl && xq + 1 <= xh, xq + 2 >= xl && xq + 2 <= xh, sd, a,
+                       E);
+}
+
+// the edge sums of every array point: ed[(a*4 + r) * npts + p]
+__global__ void __launch_bounds__(kGradThreads) grad_edge_kernel(GradDF g)
+{
+   const Box& b = g.b;
+   const int i = b.ib + (int)(blockIdx.x * 32 + threadIdx.x), j = b.jb + (int)(blockIdx.y * 4 + threadIdx.y),
+             k = b.kb + (int)blockIdx.z;
+   if (i > b.ie || j > b.je) return;
+   const long long n = b.npts;
+   const int p = (i - b.ib) + (j - b.jb) * (int)b.ni + (k - b.kb) * (int)b.nij;
+#pragma unroll 1
+   for (int a = 0; a < 3; a++) {
+      const int x = a == 0 ? i : a == 1 ? j : k;
+      const int xl = a == 0 ? b.ib : a == 1 ? b.jb : b.kb, xh = a == 0 ? b.ie : a == 1 ? b.je : b.ke;
+      const int sd = a == 0 ? 1 : a == 1 ? (int)b.ni : (int)b.nij;
+      DF E[4];
+      edges_at(g, n, p, x, xl, xh, sd, a, E);
+#pragma unroll
+      for (int r = 0; r < 4; r++) g.ed[(a * 4 + r) * n + p] = make_float2(E[r].h, E[r].l);
+   }
+}
+
+// centred first differences (DW . f)(p) = f(p-2) - f(p+2) + 8 (f(p+1) - f(p-1)) of
+// one component of A and F along an axis (x[m], y[m]: values at p + (m-2) sd)
+__device__ __forceinline__ void first_diffs(const DF x[5], const DF y[5], bool inner, DF& fa, DF& fw)
+{
+   fa = df_addf(df_diff(x[0], x[4]), df_pow2(df_diff(x[3], x[1]), 8.f));
+   fw = inner ? df_addf(df_diff(y[0], y[4]), df_pow2(df_diff(y[3], y[1]), 8.f)) : df_zero();
+}
+
+// the mu, lambda and damping rho sums of one point from the edge sums, the centred
+// first differences and the damping's second differences
 __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
 {
    // centred first differences of the current pair, [slot][thread]: slot c*3 + a for
@@ -218,76 +320,106 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
                       b.kb + (int)blockIdx.z};
    if (pc[0] > b.ie || pc[1] > b.je) return;
    const long long n = b.npts;
-   const long long p = (pc[0] - b.ib) + (pc[1] - b.jb) * b.ni + (pc[2] - b.kb) * b.nij;
    const int off[3] = {pc[0] - b.ib, pc[1] - b.jb, pc[2] - b.kb};
+   const int p = off[0] + off[1] * (int)b.ni + off[2] * (int)b.nij;
    DF gm = df_zero(), gl = df_zero(), gr = df_zero();
+   // same-axis second differences: the seven edges of each axis around p
+#pragma unroll 1
+   for (int a = 0; a < 3; a++) {
+      const int a1 = a == 2 ? 0 : a + 1, a2 = a == 0 ? 2 : a - 1;
+      const int x0 = a == 0 ? pc[0] : a == 1 ? pc[1] : pc[2];
+      const int xl = a == 0 ? b.ib : a == 1 ? b.jb : b.kb, xh = a == 0 ? b.ie : a == 1 ? b.je : b.ke;
+      const int sd = a == 0 ? 1 : a == 1 ? (int)b.ni : (int)b.nij;
+      const int oa = x0 - xl, o1 = a1 == 0 ? off[0] : a1 == 1 ? off[1] : off[2],
+                o2 = a2 == 0 ? off[0] : a2 == 1 ? off[1] : off[2];
+      const float2* __restrict__ ed = g.ed + a * 4 * n;
+      DF E[4][4];  // edges starting at p-2 .. p+1
+      if (x0 - 2 >= xl && x0 + 1 <= xh) {
+#pragma unroll
+         for (int m = 0; m < 4; m++)
+#pragma unroll
+            for (int r = 0; r < 4; r++) E[m][r] = df_of(__ldg(ed + r * n + p + (m - 2) * sd));
+      } else {
+#pragma unroll
+         for (int m = 0; m < 4; m++) {
+            const int x = x0 + m - 2;
+            const int q = p + (m - 2) * sd;
+            if (x > xh) {
+               E[m][0] = E[m][1] = E[m][2] = E[m][3] = df_zero();
+            } else if (x >= xl) {
+#pragma unroll
+               for (int r = 0; r < 4; r++) E[m][r] = df_of(__ldg(ed + r * n + q));
+            } else {  // an edge from below the array (ghost-point gradients)
+               edges_at(g, n, q, x, xl, xh, sd, a, E[m]);
+            }
+         }
+      }
+      // E1(p+1) + E1(p-2) + E2(p-1) + 3 [E1(p-1) + E1(p) - (E2(p) + E2(p-2))/4]
+      DF T[2];
+#pragma unroll
+      for (int r = 0; r < 2; r++) {
+         const DF X = df_addf(df_addf(E[3][r], E[0][r]), E[1][2 + r]);
+         const DF Y = df_addf(df_addf(E[1][r], E[2][r]), df_pow2(df_addf(E[2][2 + r], E[0][2 + r]), -0.25f));
+         T[r] = df_addf(X, df_scale(Y, 3.f));
+      }
+      const DF qq = df_mul(df_mul(df_of(__ldg(g.st24[a] + oa)), df_of(__ldg(g.ist[a1] + o1))),
+                           df_of(__ldg(g.ist[a2] + o2)));
+      gm = df_add(gm, df_mul(qq, T[0]));
+      gl = df_add(gl, df_mul(qq, T[1]));
+   }
    // pair 0: (mt, u) with weight 12 (c2 = 12 c1) and the damping term; pair 1: (b1, w1)
 #pragma unroll 1
    for (int t = 0; t < 2; t++) {
-      const float2* __restrict__ A = t == 0 ? g.dmt : g.db1;
-      const float2* __restrict__ F = t == 0 ? g.du : g.dw1;
       const float wt = t == 0 ? 12.f : 1.f;
 #pragma unroll 1
       for (int a = 0; a < 3; a++) {
          const int a1 = a == 2 ? 0 : a + 1, a2 = a == 0 ? 2 : a - 1;
          const int x0 = a == 0 ? pc[0] : a == 1 ? pc[1] : pc[2];
          const int xl = a == 0 ? b.ib : a == 1 ? b.jb : b.kb, xh = a == 0 ? b.ie : a == 1 ? b.je : b.ke;
-         const long long sd = a == 0 ? 1 : a == 1 ? b.ni : b.nij;
+         const int sd = a == 0 ? 1 : a == 1 ? (int)b.ni : (int)b.nij;
          const int oa = x0 - xl, o1 = a1 == 0 ? off[0] : a1 == 1 ? off[1] : off[2],
                    o2 = a2 == 0 ? off[0] : a2 == 1 ? off[1] : off[2];
-         bool ok[5];
-#pragma unroll
-         for (int m = 0; m < 5; m++) ok[m] = x0 + m - 2 >= xl && x0 + m - 2 <= xh;
-         const bool inner = ok[0] && ok[4];
+         const bool inner = x0 - 2 >= xl && x0 + 2 <= xh;
          const float2 bd = t == 0 ? __ldg(g.bdc[a] + oa) : make_float2(0.f, 0.f);
-         const bool damp = t == 0 && ok[1] && ok[3] && bd.x != 0.f;
-         DF xs = df_zero(), ys = df_zero(), xa = df_zero(), ya = df_zero(), ds = df_zero();
+         const bool damp = t == 0 && x0 - 1 >= xl && x0 + 1 <= xh && bd.x != 0.f;
+         DF ds = df_zero();
 #pragma unroll
          for (int c = 0; c < 3; c++) {
+            const float2* __restrict__ A = (t == 0 ? g.dmt : g.db1) + c * n;
+            const float2* __restrict__ F = (t == 0 ? g.du : g.dw1) + c * n;
             DF x[5], y[5];
+            if (inner) {
 #pragma unroll
-            for (int m = 0; m < 5; m++) {
-               const long long q = c * n + p + (m - 2) * sd;
-               x[m] = ok[m] ? df_of(__ldg(A + q)) : df_zero();
-               y[m] = ok[m] ? df_of(__ldg(F + q)) : df_zero();
+               for (int m = 0; m < 5; m++) {
+                  if (m == 2) continue;
+                  x[m] = df_of(__ldg(A + p + (m - 2) * sd));
+                  y[m] = df_of(__ldg(F + p + (m - 2) * sd));
+               }
+            } else {
+#pragma unroll
+               for (int m = 0; m < 5; m++) {
+                  if (m == 2) continue;
+                  const bool ok = x0 + m - 2 >= xl && x0 + m - 2 <= xh;
+                  x[m] = ok ? df_of(__ldg(A + p + (m - 2) * sd)) : df_zero();
+                  y[m] = ok ? df_of(__ldg(F + p + (m - 2) * sd)) : df_zero();
+               }
             }
-            // edges (p-2+e, p-1+e) and (p-2+e, p+e)
-            DF e1[4], e2[3];
-#pragma unroll
-            for (int e = 0; e < 4; e++) e1[e] = df_mul(df_diff(x[e + 1], x[e]), df_diff(y[e + 1], y[e]));
-#pragma unroll
-            for (int e = 0; e < 3; e++) e2[e] = df_mul(df_diff(x[e + 2], x[e]), df_diff(y[e + 2], y[e]));
-            // E1(p+1) + E1(p-2) + E2(p-1) + 3 [E1(p-1) + E1(p) - (E2(p) + E2(p-2))/4]
-            const DF X = df_add(df_add(e1[3], e1[0]), e2[1]);
-            const DF Y = df_add(df_add(e1[1], e1[2]), df_scale(df_add(e2[2], e2[0]), -0.25f));
-            xs = df_add(xs, X);
-            ys = df_add(ys, Y);
-            if (c == a) {
-               xa = X;
-               ya = Y;
-            }
-            // (DW . f)(p) = f(p-2) - f(p+2) + 8 (f(p+1) - f(p-1))
-            const DF fa = df_add(df_diff(x[0], x[4]), df_scale(df_diff(x[3], x[1]), 8.f));
-            const DF fw = inner ? df_add(df_diff(y[0], y[4]), df_scale(df_diff(y[3], y[1]), 8.f)) : df_zero();
+            DF fa, fw;
+            first_diffs(x, y, inner, fa, fw);
             fd[c * 3 + a][tid] = make_float2(fa.h, fa.l);
             fd[9 + c * 3 + a][tid] = make_float2(fw.h, fw.l);
-            if (damp) {  // D2(u - um) D2(b1) along a (y holds u)
-               DF d[3], v[3];
-#pragma unroll
-               for (int m = 0; m < 3; m++) {
-                  const long long q = c * n + p + (m - 1) * sd;
-                  d[m] = df_diff(y[m + 1], df_of(__ldg(g.dum + q)));
-                  v[m] = df_of(__ldg(g.db1 + q));
-               }
-               const DF d2u = df_add(df_add(d[0], d[2]), df_scale(d[1], -2.f));
-               const DF d2b = df_add(df_add(v[0], v[2]), df_scale(v[1], -2.f));
+            if (damp) {  // D2(u - um) D2(b1) along a (y holds u at p -+ 1)
+               const float2* __restrict__ um = g.dum + c * n;
+               const float2* __restrict__ b1 = g.db1 + c * n;
+               const DF d0 = df_diff(y[1], df_of(__ldg(um + p - sd)));
+               const DF d1 = df_diff(df_of(__ldg(F + p)), df_of(__ldg(um + p)));
+               const DF d2 = df_diff(y[3], df_of(__ldg(um + p + sd)));
+               const DF d2u = df_addf(df_addf(d0, d2), df_pow2(d1, -2.f));
+               const DF d2b = df_addf(df_addf(df_of(__ldg(b1 + p - sd)), df_of(__ldg(b1 + p + sd))),
+                                      df_pow2(df_of(__ldg(b1 + p)), -2.f));
                ds = df_add(ds, df_mul(d2u, d2b));
             }
          }
-         const DF i1 = df_of(__ldg(g.ist[a1] + o1)), i2 = df_of(__ldg(g.ist[a2] + o2));
-         const DF qq = df_scale(df_mul(df_mul(df_of(__ldg(g.st24[a] + oa)), i1), i2), wt);
-         gm = df_add(gm, df_mul(qq, df_add(df_add(xs, xa), df_scale(df_add(ys, ya), 3.f))));
-         gl = df_add(gl, df_mul(qq, df_add(xa, df_scale(ya, 3.f))));
          if (damp) {
             const DF cc = df_mul(df_of(__ldg(g.cist[a1] + o1)), df_of(__ldg(g.cist[a2] + o2)));
             gr = df_add(gr, df_neg(df_mul(df_mul(df_of(bd), cc), ds)));
@@ -300,8 +432,8 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
          const int a1 = t3 == 2 ? 0 : t3 + 1, a2 = t3 == 0 ? 2 : t3 - 1;
          auto A_ = [&](int c, int a) { return df_of(fd[c * 3 + a][tid]); };
          auto W_ = [&](int c, int a) { return df_of(fd[9 + c * 3 + a][tid]); };
-         const DF ml = df_add(df_mul(W_(a2, a2), A_(a1, a1)), df_mul(W_(a1, a1), A_(a2, a2)));
-         const DF mm = df_add(df_mul(W_(a2, a1), A_(a1, a2)), df_mul(W_(a1, a2), A_(a2, a1)));
+         const DF ml = df_addf(df_mul(W_(a2, a2), A_(a1, a1)), df_mul(W_(a1, a1), A_(a2, a2)));
+         const DF mm = df_addf(df_mul(W_(a2, a1), A_(a1, a2)), df_mul(W_(a1, a2), A_(a2, a1)));
          const int ot = t3 == 0 ? off[0] : t3 == 1 ? off[1] : off[2];
          const DF f = df_scale(df_of(__ldg(g.ist[t3] + ot)), wt);
          gm = df_add(gm, df_mul(f, mm));
@@ -372,7 +504,10 @@ int launch_grad_df_step(const GradDF& g, cudaStream_t s)
    const int ni = (int)b.ni, nj = b.je - b.jb + 1, nk = b.ke - b.kb + 1;
    grad_prep_kernel<<<dim3((ni + 127) / 128, nj, nk), 128, 0, s>>>(g);
    SW4G_TRY(launch_status());
-   grad_df_kernel<<<dim3((ni + 31) / 32, (nj + 3) / 4, nk), dim3(32, 4), 0, s>>>(g);
+   const dim3 grid((ni + 31) / 32, (nj + 3) / 4, nk), block(32, 4);
+   grad_edge_kernel<<<grid, block, 0, s>>>(g);
+   SW4G_TRY(launch_status());
+   grad_df_kernel<<<grid, block, 0, s>>>(g);
    return launch_status();
 }
 

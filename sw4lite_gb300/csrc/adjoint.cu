@@ -498,10 +498,10 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
    if (st == kOk) st = alloc(&resd, (size_t)(nsteps + 1) * nval * sizeof(double));
    if (st == kOk && mixed_) st = alloc(&adj_edges_, 12 * (size_t)npts_ * sizeof(double));
    // FP64 form: double-float copies of the step's levels (5), the per-point sums (1),
-   // the 1-D profile pairs and the two exponent maxima (adj_grad.cu)
+   // the edge sums (4), the 1-D profile pairs and the two exponent maxima (adj_grad.cu)
    double *dfw = nullptr, *dfp = nullptr, *dfe = nullptr;
    const int nax[3] = {bd.ie - bd.ib + 1, bd.je - bd.jb + 1, bd.ke - bd.kb + 1};
-   if (st == kOk && !mixed_) st = alloc(&dfw, 6 * lv);
+   if (st == kOk && !mixed_) st = alloc(&dfw, 10 * lv);
    if (st == kOk && !mixed_) st = alloc(&dfp, 4 * (size_t)(nax[0] + nax[1] + nax[2]) * sizeof(float2));
    if (st == kOk && !mixed_) st = alloc(&dfe, sizeof(double));
    double* gr_d = g_rho;
@@ -601,6 +601,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       gd.am = f2 + 5 * n3;
       gd.al = gd.am + npts_;
       gd.ar = gd.al + npts_;
+      gd.ed = f2 + 6 * n3;
       gd.emax = emax;
       // Each class's bound maps to 2^26..2^28: the largest products (x 1/(s_b s_c) <=
       // 2^32 in the supergrid layers, x 12, summed) stay below 2^110, and values down

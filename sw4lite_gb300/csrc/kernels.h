@@ -342,6 +342,7 @@ struct GradDF {
    const float2* cist[3] = {};
    const float2* bdc[3] = {};
    float2 *am = nullptr, *al = nullptr, *ar = nullptr;  // per-point sums (mu, lambda, rho)
+   float2* ed = nullptr;  // edge sums, 12 x npts
    const int* emax = nullptr;
    int marg_a = 0, marg_f = 0;
 };
