@@ -472,9 +472,10 @@ def _lognormal(torch, shape, std, corr, seed):
     return torch.exp(std * g)
 
 
-def _make_c4(sg, torch, cfg, stream, nsteps, homogeneous=False, dt=None):
+def _make_c4(sg, torch, cfg, stream, nsteps, homogeneous=False, dt=None, precision=None):
     n, h = cfg["n"], cfg["h"]
-    g = sg.grid_desc(n, n, n, h, bc=(2,) * 6, sg_gp=cfg["gp"])
+    g = sg.grid_desc(n, n, n, h, bc=(2,) * 6, sg_gp=cfg["gp"],
+                     precision=sg.FP64 if precision is None else precision)
     shape = (n + 4, n + 4, n + 4)
     if homogeneous:
         pr = ps = pv = torch.ones(shape, dtype=torch.float64, device="cuda")
@@ -506,13 +507,17 @@ def _make_c4(sg, torch, cfg, stream, nsteps, homogeneous=False, dt=None):
 def _time_adjoint(args, sg, torch, stream):
     """Forward solve and misfit gradient of the adjoint workload, each timed with
     CUDA events on the EW stream; the ratio is the gradient's cost in forward
-    solves."""
+    solves.  The gradient keeps as many segments of its forward run as the free
+    device memory holds (the rest are recomputed from checkpoints), so the ratio is
+    measured at the workload's full length.  The observed data (records of the same
+    shot in the homogeneous background) come from the FP32-mixed solver: any data
+    serve, and the timed runs are FP64."""
     cfg = c4_config(args.adj_n)
     N, C = args.adj_steps, args.adj_ckpt
     with torch.cuda.stream(stream):
         ew, dt = _make_c4(sg, torch, cfg, stream, N)
         ew.close()
-        ew0, _ = _make_c4(sg, torch, cfg, stream, N, homogeneous=True, dt=dt)
+        ew0, _ = _make_c4(sg, torch, cfg, stream, N, homogeneous=True, dt=dt, precision=sg.MIXED)
         ew0.step(N, sg.MODE_FUSED)
         obs = torch.zeros(ew0.record_shape(), dtype=torch.float64, device="cuda")
         ew0.records(obs)
@@ -590,73 +595,79 @@ def _c5_shot(sg, ew, cfg, s):
                                  kind=sg.GAUSSIAN))
 
 
+def _c5_gradients(sg, torch, cfg, stream, mat, dt, N, C, shots, precisions):
+    """Observed data (FP32-mixed forward in the homogeneous background) for the shots,
+    then for each precision the summed gradient over the shots (FP64 accumulation on
+    the device) with each shot's gradient() timed by CUDA events."""
+    ew0 = _c5_ew(sg, torch, cfg, stream, N, sg.MIXED, _c5_medium(torch, cfg, True), dt)
+    zero = torch.zeros(3 * ew0.npts, dtype=torch.float64, device="cuda")
+    obs = []
+    for s in shots:
+        _c5_shot(sg, ew0, cfg, s)
+        ew0.set_time_step(dt, 0.0)
+        ew0.set_receivers(*_c5_receivers(cfg), N + 1)
+        ew0.set_fields(zero, zero)
+        ew0.step(N, sg.MODE_FUSED)
+        o = torch.zeros(ew0.record_shape(), dtype=torch.float64, device="cuda")
+        ew0.records(o)
+        obs.append(o)
+    ew0.close()
+    out = {}
+    for prec in precisions:
+        ew = _c5_ew(sg, torch, cfg, stream, N, prec, mat, dt)
+        tot = [torch.zeros(ew.npts, dtype=torch.float64, device="cuda") for _ in range(3)]
+        g = [torch.zeros(ew.npts, dtype=torch.float64, device="cuda") for _ in range(3)]
+        ms, J = [], 0.0
+        for s, o in zip(shots, obs):
+            _c5_shot(sg, ew, cfg, s)
+            ew.set_time_step(dt, 0.0)
+            ew.set_fields(zero, zero)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            J += ew.gradient(N, C, o, *g)
+            for q in range(3):
+                tot[q] += g[q]  # FP64 accumulation over shots, on the device
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        ew.close()
+        out[prec] = dict(ms=ms, J=J, tot=tot)
+    return out
+
+
 def _time_multishot(args, sg, torch, stream):
-    """C5: the summed misfit gradient of args.ms_shots shots, FP32-mixed (double-float
+    """C5: the summed misfit gradient over point-force shots, FP32-mixed (double-float
     levels, FP32 stencils and gradient terms) with FP64 accumulation, every time loop
-    replayed as CUDA graphs; per-shot time from CUDA events; error of the sum of the
-    first args.ms_err_shots shots against the FP64 gradient of the same shots."""
+    replayed as CUDA graphs.  Per-shot time from CUDA events on args.ms_shots shots at
+    the workload's full length (args.ms_steps); error of the mixed sum over
+    args.ms_err_shots shots against the FP64 gradients of the same shots, at
+    args.ms_err_steps steps (FP64 gradients of the full length take minutes)."""
     cfg = c5_config(args.adj_n)
     N, C, S = args.ms_steps, args.adj_ckpt, args.ms_shots
     n = cfg["n"]
     with torch.cuda.stream(stream):
         mat = _c5_medium(torch, cfg, False)
         dt = cfg["cfl"] * cfg["h"] / float(torch.sqrt(((4 * mat[1] + mat[2]) / mat[0]).max()))
-        # observed data: each shot in the homogeneous background
-        ew0 = _c5_ew(sg, torch, cfg, stream, N, sg.MIXED, _c5_medium(torch, cfg, True), dt)
-        zero = torch.zeros(3 * ew0.npts, dtype=torch.float64, device="cuda")
-        obs = []
-        for s in range(S):
-            _c5_shot(sg, ew0, cfg, s)
-            ew0.set_time_step(dt, 0.0)
-            ew0.set_receivers(*_c5_receivers(cfg), N + 1)
-            ew0.set_fields(zero, zero)
-            ew0.step(N, sg.MODE_FUSED)
-            o = torch.zeros(ew0.record_shape(), dtype=torch.float64, device="cuda")
-            ew0.records(o)
-            obs.append(o)
-        ew0.close()
-        out = {}
-        for prec, nshots in ((sg.MIXED, S), (sg.FP64, min(args.ms_err_shots, S))):
-            if nshots == 0:
-                continue
-            ew = _c5_ew(sg, torch, cfg, stream, N, prec, mat, dt)
-            tot = [torch.zeros(ew.npts, dtype=torch.float64, device="cuda") for _ in range(3)]
-            part = None
-            g = [torch.zeros(ew.npts, dtype=torch.float64, device="cuda") for _ in range(3)]
-            ms = []
-            J = 0.0
-            for s in range(nshots):
-                _c5_shot(sg, ew, cfg, s)
-                ew.set_time_step(dt, 0.0)
-                ew.set_fields(zero, zero)
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                J += ew.gradient(N, C, obs[s], *g)
-                for q in range(3):
-                    tot[q] += g[q]  # FP64 accumulation over shots, on the device
-                e1.record(stream)
-                torch.cuda.synchronize()
-                ms.append(e0.elapsed_time(e1))
-                if s + 1 == min(args.ms_err_shots, S):
-                    part = [t.clone() for t in tot]
-            ew.close()
-            out[prec] = dict(ms=ms, J=J, tot=tot, part=part)
-        mx = out[sg.MIXED]
-        res = {"workload": f"C5 multi-shot gradient {n}^3, C4 medium, {S} point-force shots, 16 receivers, "
+        mx = _c5_gradients(sg, torch, cfg, stream, mat, dt, N, C, list(range(S)), [sg.MIXED])[sg.MIXED]
+        res = {"workload": f"C5 multi-shot gradient {n}^3, C4 medium, point-force shots, 16 receivers, "
                            f"{N} steps, checkpoints every {C}, FP32-mixed with FP64 accumulation, "
                            "time loops as CUDA graphs",
-               "shots": S, "steps": N, "per_shot_ms": sum(mx["ms"]) / len(mx["ms"]),
-               "total_ms": sum(mx["ms"]), "misfit": mx["J"],
-               "grad_norms": [float(x.norm()) for x in mx["tot"]]}
-        if sg.FP64 in out:
-            f64 = out[sg.FP64]
-            res["fp64_per_shot_ms"] = sum(f64["ms"]) / len(f64["ms"])
+               "shots": S, "of_shots": len(cfg["shots"]), "steps": N,
+               "per_shot_ms": sum(mx["ms"]) / len(mx["ms"]), "total_ms": sum(mx["ms"]),
+               "misfit": mx["J"], "grad_norms": [float(x.norm()) for x in mx["tot"]]}
+        del mx
+        E = min(args.ms_err_shots, len(cfg["shots"]))
+        if E > 0:
+            out = _c5_gradients(sg, torch, cfg, stream, mat, dt, args.ms_err_steps, C, list(range(E)),
+                                [sg.MIXED, sg.FP64])
+            a, b = out[sg.MIXED], out[sg.FP64]
             res["error_vs_fp64"] = {
-                "shots": len(f64["ms"]),
-                "l2_rel": [float((a - b).norm() / b.norm()) for a, b in zip(mx["part"], f64["tot"])],
-                "linf_rel": [float((a - b).abs().max() / b.abs().max()) for a, b in zip(mx["part"], f64["tot"])],
+                "shots": E, "steps": args.ms_err_steps,
+                "mixed_per_shot_ms": sum(a["ms"]) / E, "fp64_per_shot_ms": sum(b["ms"]) / E,
+                "l2_rel": [float((x - y).norm() / y.norm()) for x, y in zip(a["tot"], b["tot"])],
+                "linf_rel": [float((x - y).abs().max() / y.abs().max()) for x, y in zip(a["tot"], b["tot"])],
                 "against": "sum of the FP64 gradients of the same shots (rho, mu, lambda)"}
-        del out
+            del out
         torch.cuda.empty_cache()
     return res
 
@@ -851,11 +862,12 @@ def main():
                     help="steps of the mixed-vs-FP64 error run of the topography workload (0: skip)")
     ap.add_argument("--topo-nz", type=int, default=128, help="z points of both grids together")
     ap.add_argument("--adj-n", type=int, default=256, help="grid of the adjoint workload")
-    ap.add_argument("--adj-steps", type=int, default=200, help="steps of the adjoint workload")
+    ap.add_argument("--adj-steps", type=int, default=2000, help="steps of the adjoint workload")
     ap.add_argument("--adj-ckpt", type=int, default=100, help="checkpoint spacing")
     ap.add_argument("--no-multishot", action="store_true", help="skip the multi-shot gradient workload")
-    ap.add_argument("--ms-shots", type=int, default=16, help="shots of the multi-shot workload")
-    ap.add_argument("--ms-steps", type=int, default=150, help="steps of the multi-shot workload")
+    ap.add_argument("--ms-shots", type=int, default=2, help="timed shots of the multi-shot workload (of 16)")
+    ap.add_argument("--ms-steps", type=int, default=1500, help="steps of the multi-shot workload")
+    ap.add_argument("--ms-err-steps", type=int, default=150, help="steps of the mixed-vs-FP64 gradient check")
     ap.add_argument("--ms-err-shots", type=int, default=2,
                     help="shots whose summed gradient is compared with FP64 (0: skip)")
     ap.add_argument("--only-c2", choices=["fp64", "mixed"], default=None,

@@ -514,11 +514,35 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       gm_d = gtmp + npts_;
       gl_d = gtmp + 2 * npts_;
    }
+   // FP64 form: a segment's adjoint steps run on two streams forked from the object's
+   // stream, the FP64 stages (the critical path) on one of the highest priority and
+   // the double-float gradient terms of each step on one of the lowest, beside the
+   // next stages (they need the step's mt and nothing after it needs them), so their
+   // CTAs take what the stage kernels leave of each SM.  mt is double-buffered and
+   // events order its reuse.
+   cudaStream_t hs = nullptr, gs = nullptr;
+   cudaEvent_t ev_s0 = nullptr, ev_g[2] = {nullptr, nullptr}, ev_join = nullptr, ev_fork = nullptr,
+               ev_back = nullptr;
    auto cleanup = [&]() {
       cudaStreamSynchronize(stream_);
+      if (hs) cudaStreamSynchronize(hs);
+      if (gs) cudaStreamSynchronize(gs);
       for (double* p : bufs) cudaFree(p);
       adj_edges_ = nullptr;
+      if (hs) cudaStreamDestroy(hs);
+      if (gs) cudaStreamDestroy(gs);
+      for (cudaEvent_t e : {ev_s0, ev_g[0], ev_g[1], ev_join, ev_fork, ev_back})
+         if (e) cudaEventDestroy(e);
    };
+   if (st == kOk && !mixed_) {
+      int lo = 0, hi = 0;
+      st = cuda_ok(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+      if (st == kOk) st = cuda_ok(cudaStreamCreateWithPriority(&hs, cudaStreamNonBlocking, hi));
+      if (st == kOk) st = cuda_ok(cudaStreamCreateWithPriority(&gs, cudaStreamNonBlocking, lo));
+      for (cudaEvent_t* e : {&ev_s0, &ev_g[0], &ev_g[1], &ev_join, &ev_fork, &ev_back})
+         if (st == kOk) st = cuda_ok(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+   }
+   cudaStream_t sa = mixed_ ? stream_ : hs;  // the adjoint steps' stages
    if (st != kOk) {
       cleanup();
       return st;
@@ -694,7 +718,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       double* b2 = work + n3;      // at n+2
       double* bn = work + 2 * n3;  // at n
       double* mt = work + 3 * n3;  // b1 + dt^2/12 R L(b1)
-      double* w1 = work + 4 * n3;  // up - 2u + um
+      double* w1 = work + 4 * n3;  // up - 2u + um (mixed form); the FP64 form's second mt slot
       double* v1 = work + 5 * n3;  // dt^2/12 W b1
       double* v2 = work + 6 * n3;  // dt^2 W mt
       SW4G_TRY(cuda_ok(cudaMemsetAsync(work, 0, 7 * lv, stream_)));  // not fin
@@ -729,7 +753,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       // to u^{nn+1}); with the device clock its residual row is clock[2]
       double* segp = seg;  // the buffers of the segment being swept
       double* predp = pred;
-      auto adj_step = [&](int nn, int s0, double* b1, double* b2, double* bn, bool clocked) -> int {
+      auto adj_step = [&](int nn, int s0, double* b1, double* b2, double* bn, bool clocked, bool wait_g) -> int {
          const double* u = segp + (size_t)(nn - s0 + 1) * n3;
          const double* um = segp + (size_t)(nn - s0) * n3;
          const double* up = predp + (size_t)(nn - s0) * n3;
@@ -741,42 +765,48 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
             status = adjoint_step_mixed(ms, &pf, &pf32, b, n3, u, um, up, un, b1, b2, bn, mt, w1, v1, v2,
                                         gr_d, gm_d, gl_d, dt, beta, saved_n, res, clk, nval);
          } else {
-            // mt = b1 + dt^2/12 R L(b1): predictor form, um = u
+            // mt = b1 + dt^2/12 R L(b1): predictor form, um = u; into the slot whose
+            // previous reader, the gradient terms two steps later, has finished
+            double* mtb = (nn & 1) ? w1 : mt;
+            if (wait_g) status = cuda_ok(cudaStreamWaitEvent(sa, ev_g[nn & 1], 0));
             fs.corrector = 0;
             fs.u = b1;
             fs.um = b1;
             fs.up = nullptr;
-            fs.out = mt;
+            fs.out = mtb;
             fs.beta = 0;
             fs.coef = dt * dt / 12;
-            status = launch_fused_stage(fs, stream_);
+            if (status == kOk) status = launch_fused_stage(fs, sa);
+            if (status == kOk) status = cuda_ok(cudaEventRecord(ev_s0, sa));
+            if (status == kOk) status = cuda_ok(cudaStreamWaitEvent(gs, ev_s0, 0));
             if (status == kOk) {  // the gradient terms of the step (double-float sums)
                GradDF g = gd;
                g.b1 = b1;
-               g.mt = mt;
+               g.mt = mtb;
                g.up = up;
                g.u = u;
                g.um = um;
                g.un = un;
-               status = launch_grad_df_step(g, stream_);
+               status = launch_grad_df_step(g, gs);
             }
+            if (status == kOk) status = cuda_ok(cudaEventRecord(ev_g[nn & 1], gs));
             if (status == kOk) {  // b^n = 2 b1 - b2 + dt^2 R L(mt) - beta R SG(b1 - b2)
                fs.corrector = 2;
                fs.u = b1;
                fs.um = b2;
-               fs.up = mt;
+               fs.up = mtb;
                fs.out = bn;
                fs.beta = beta;
                fs.coef = dt * dt;
-               status = launch_fused_stage(fs, stream_);
+               status = launch_fused_stage(fs, sa);
             }
             if (status == kOk) {
-               adj_source_kernel<<<blocks_for(saved_n, 64), 64, 0, stream_>>>(
+               adj_source_kernel<<<blocks_for(saved_n, 64), 64, 0, sa>>>(
                    b, pf, saved_n, drec_.ijk, res, rho_, bn, clk, nval);
                status = launch_status();
             }
          }
-         if (status == kOk && clocked) status = launch_clock_advance(dclock_, 0.0, 0.0, -1.0, stream_);
+         if (status == kOk && clocked) status = launch_clock_advance(dclock_, 0.0, 0.0, -1.0, sa);
          return status;
       };
       // recompute the segment from its checkpoint: seg[q] = u^{s0-1+q}, pred[q] = up^{s0+q}
@@ -799,7 +829,18 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       };
       // the segment's double-float sums into the FP64 gradients
       auto flush = [&]() -> int {
-         return mixed_ ? kOk : launch_grad_df_flush(gd, kmu, gm_d, gl_d, gr_d, stream_);
+         if (mixed_) return kOk;
+         SW4G_TRY(launch_grad_df_flush(gd, kmu, gm_d, gl_d, gr_d, gs));
+         SW4G_TRY(cuda_ok(cudaEventRecord(ev_join, gs)));
+         SW4G_TRY(cuda_ok(cudaStreamWaitEvent(hs, ev_join, 0)));
+         SW4G_TRY(cuda_ok(cudaEventRecord(ev_back, hs)));
+         return cuda_ok(cudaStreamWaitEvent(stream_, ev_back, 0));
+      };
+      // a segment's adjoint steps start after everything before them on the object's stream
+      auto fork = [&]() -> int {
+         if (mixed_) return kOk;
+         SW4G_TRY(cuda_ok(cudaEventRecord(ev_fork, stream_)));
+         return cuda_ok(cudaStreamWaitEvent(hs, ev_fork, 0));
       };
       auto rotate = [&]() {
          double* tmp = b2;
@@ -867,8 +908,9 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
             if (status == kOk && !ex) {
                double* key = b1;
                status = capture([&]() -> int {
+                  SW4G_TRY(fork());
                   for (int nn = s1 - 1; nn >= s0; nn--) {
-                     SW4G_TRY(adj_step(nn, s0, b1, b2, bn, true));
+                     SW4G_TRY(adj_step(nn, s0, b1, b2, bn, true, nn + 2 <= s1 - 1));
                      rotate();
                   }
                   return flush();
@@ -882,8 +924,9 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
                for (int nn = s1 - 1; nn >= s0; nn--) rotate();
             }
          } else {
+            status = fork();
             for (int nn = s1 - 1; nn >= s0 && status == kOk; nn--) {
-               status = adj_step(nn, s0, b1, b2, bn, false);
+               status = adj_step(nn, s0, b1, b2, bn, false, nn + 2 <= s1 - 1);
                rotate();
             }
             if (status == kOk) status = flush();
