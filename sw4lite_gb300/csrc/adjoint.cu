@@ -653,6 +653,31 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       }
    }
    const double kmu = -(dt * dt / 12) / (144 * g_.h * g_.h);
+   // Fused steps n0..n1-1 with the level slots pointing into a segment's buffers, so
+   // each level lands where the adjoint reads it: u^{n+1} in sq[n - n0 + 2], the
+   // predicted level up^n in pq[n - n0] (sq[0], sq[1] hold u^{n0-1}, u^{n0} on
+   // entry).  The object's own level buffers then get the last two levels back.
+   auto steps_into = [&](int n0, int n1, double* sq, double* pq) -> int {
+      double* own[4] = {lev_[0], lev_[1], lev_[2], lev_[3]};
+      lev_[iu_] = sq + n3;
+      lev_[ium_] = sq;
+      int status = kOk;
+      for (int n = n0; n < n1 && status == kOk; n++) {
+         int ip = 0;
+         while (ip == iu_ || ip == ium_) ip++;
+         int iq = ip + 1;
+         while (iq == iu_ || iq == ium_) iq++;
+         lev_[ip] = pq + (size_t)(n - n0) * n3;
+         lev_[iq] = sq + (size_t)(n - n0 + 2) * n3;
+         status = step_fused();
+      }
+      for (int q = 0; q < 4; q++) lev_[q] = own[q];
+      SW4G_TRY(status);
+      SW4G_TRY(cuda_ok(cudaMemcpyAsync(lev_[iu_], sq + (size_t)(n1 - n0 + 1) * n3, lv, cudaMemcpyDeviceToDevice,
+                                       stream_)));
+      return cuda_ok(cudaMemcpyAsync(lev_[ium_], sq + (size_t)(n1 - n0) * n3, lv, cudaMemcpyDeviceToDevice,
+                                     stream_));
+   };
 
    auto run = [&]() -> int {
       SW4G_TRY(cuda_ok(cudaMemsetAsync(gr_d, 0, npts_ * sizeof(double), stream_)));
@@ -680,14 +705,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
          double* pq = pred_of(sg);
          SW4G_TRY(cuda_ok(cudaMemcpyAsync(sq, lev_[ium_], lv, cudaMemcpyDeviceToDevice, stream_)));
          SW4G_TRY(cuda_ok(cudaMemcpyAsync(sq + n3, lev_[iu_], lv, cudaMemcpyDeviceToDevice, stream_)));
-         for (int n = nn; n < s1; n++) {
-            capture_pred_ = pq + (size_t)(n - nn) * n3;
-            const int status = step_fused();
-            capture_pred_ = nullptr;
-            SW4G_TRY(status);
-            SW4G_TRY(cuda_ok(cudaMemcpyAsync(sq + (size_t)(n - nn + 2) * n3, lev_[iu_], lv,
-                                             cudaMemcpyDeviceToDevice, stream_)));
-         }
+         SW4G_TRY(steps_into(nn, s1, sq, pq));
       }
       const double t_end = t_;
       double* fin = work + 7 * n3;  // u^N, u^{N-1}: the recompute overwrites the levels
@@ -810,17 +828,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
          return status;
       };
       // recompute the segment from its checkpoint: seg[q] = u^{s0-1+q}, pred[q] = up^{s0+q}
-      auto recompute = [&](int s0, int s1) -> int {
-         for (int nn = s0; nn < s1; nn++) {
-            capture_pred_ = pred + (size_t)(nn - s0) * n3;
-            const int status = step_fused();
-            capture_pred_ = nullptr;
-            SW4G_TRY(status);
-            SW4G_TRY(cuda_ok(cudaMemcpyAsync(seg + (size_t)(nn - s0 + 2) * n3, lev_[iu_], lv,
-                                             cudaMemcpyDeviceToDevice, stream_)));
-         }
-         return kOk;
-      };
+      auto recompute = [&](int s0, int s1) -> int { return steps_into(s0, s1, seg, pred); };
       // the forward levels' shift: the largest exponent over the segment's levels
       auto seg_scale = [&](int s0, int s1) -> int {
          if (mixed_) return kOk;
@@ -874,10 +882,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
                ium_ = 3;
             }
             double* c0 = ck + 2 * (size_t)sg * n3;
-            status = cuda_ok(cudaMemcpyAsync(lev_[iu_], c0, lv, cudaMemcpyDeviceToDevice, stream_));
-            if (status == kOk)
-               status = cuda_ok(cudaMemcpyAsync(lev_[ium_], c0 + n3, lv, cudaMemcpyDeviceToDevice, stream_));
-            if (status == kOk) status = cuda_ok(cudaMemcpyAsync(seg, c0 + n3, lv, cudaMemcpyDeviceToDevice, stream_));
+            status = cuda_ok(cudaMemcpyAsync(seg, c0 + n3, lv, cudaMemcpyDeviceToDevice, stream_));
             if (status == kOk) status = cuda_ok(cudaMemcpyAsync(seg + n3, c0, lv, cudaMemcpyDeviceToDevice, stream_));
             t_ = tseg[sg];
             if (status == kOk && full) {

@@ -499,7 +499,7 @@ int EW::run_graphed(int nsteps)
    };
    int st = kOk;
    while (nsteps > 0 && st == kOk) {
-      if (nsteps >= kGraphSteps && in_cycle() && !capture_pred_) {
+      if (nsteps >= kGraphSteps && in_cycle()) {
          const int rec = drec_.n > 0 ? 1 : 0;
          cudaGraphExec_t ex = nullptr;
          for (const GraphKey& g : graph_cache_)
@@ -827,9 +827,6 @@ int EW::step_fused()
    while (iq == iu_ || iq == ium_) iq++;
    for (int which = 0; which < 6; which++) {
       SW4G_TRY(piece(which, ip, iq));
-      if (which == 2 && capture_pred_)
-         SW4G_TRY(cuda_ok(cudaMemcpyAsync(capture_pred_, lev_[ip], 3 * (size_t)npts_ * sizeof(double),
-                                          cudaMemcpyDeviceToDevice, stream_)));
       if (!cv_) continue;
       if (which == 0) SW4G_TRY(curv_pred(ip));
       if (which == 2) SW4G_TRY(curv_bc(lev_[ip], cv_->lev[ip]));

@@ -232,7 +232,6 @@ class EW {
    bool rec_initial_ = false;  // the initial-data row is still to be written
 
    std::unique_ptr<CurvGrid> cv_;
-   double* capture_pred_ = nullptr;  // if set, a fused step copies its predicted level here
    double* adj_edges_ = nullptr;     // gradient(): edge products of the adjoint step
    long long grad_store_bytes_ = -1;  // gradient(): budget for kept segments
 
