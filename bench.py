@@ -84,10 +84,10 @@ def measured_peaks():
 # words) and mu, lambda, rho (3), writes the new level (3): 15 FP64 words
 CORR_STAGE_WORDS = 15
 # DRAM bytes per interior point of the corrector stage kernel, from one ncu capture
-# of the 192^3 case (dram__bytes_read.sum + dram__bytes_write.sum = 1.7234e9 B over
+# of the 192^3 case (dram__bytes_read.sum + dram__bytes_write.sum = 2.1268e9 B over
 # 7,077,888 interior points; profiles/fused_stage_c2_192.md); traffic grows with
 # the point count, so a launch moves this many bytes per point at any size
-CORR_STAGE_DRAM_BYTES_PER_PT = 243.49
+CORR_STAGE_DRAM_BYTES_PER_PT = 300.49
 # reference flop counts per interior point (tests/testil/testil.C:271, :299):
 # rhs4sg 666, addsgd4 375, corrector+dpdm ~23 -> corrector stage; predictor ~683
 CORR_STAGE_REF_FLOPS = 666 + 375 + 11 + 12
