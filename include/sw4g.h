@@ -299,7 +299,7 @@ int sw4g_ew_step(sw4g_ew* ew, int nsteps, int mode);
  * J = 1/2 sum_{n=0..nsteps} sum_r |rec^n_r - obs^n_r|^2 (obs: (nsteps+1) x nvals,
  * the record layout) and dJ/drho, dJ/dmu, dJ/dlambda at every array point (npts
  * each), by the exact transpose of the step with checkpoints every
- * checkpoint_every steps.  Device memory: (2*ceil(nsteps/C) + 2*C + 15) levels of
+ * checkpoint_every steps.  Device memory: (2*ceil(nsteps/C) + 2*C + 19) levels of
  * 3*npts doubles, plus the segments kept from the forward run (below).  Requires
  * Dirichlet or supergrid sides (zero ghost data), 4th-order damping, no topography.
  * The object ends at the end of the forward run. */

@@ -28,6 +28,11 @@
 //
 // The cancellations that matter stay in FP64: w1 = (up - 2u) + um and un - up are
 // formed from the FP64 levels before the split.
+//
+// The FP32-mixed form runs the same edge and combine kernels with single FP32 values
+// (number type F1) on its double-float levels rounded to FP32 (w1 and un - up formed
+// exactly from the pairs first), and adds each point's sums to the FP64 gradients
+// every step.
 #include "common.cuh"
 #include "df.cuh"
 #include "kernels.h"
@@ -89,6 +94,44 @@ __device__ __forceinline__ DF df_scale(DF a, float k)
 {
    const float p = __fmul_rn(k, a.h);
    return {p, __fmaf_rn(k, a.l, __fmaf_rn(k, a.h, -p))};
+}
+
+// One FP32 value with the same operations (the mixed form's gradient terms).
+struct F1 {
+   float h;
+};
+__device__ __forceinline__ F1 df_neg(F1 a) { return {-a.h}; }
+__device__ __forceinline__ F1 df_diff(F1 a, F1 b) { return {a.h - b.h}; }
+__device__ __forceinline__ F1 df_add(F1 a, F1 b) { return {a.h + b.h}; }
+__device__ __forceinline__ F1 df_addf(F1 a, F1 b) { return {a.h + b.h}; }
+__device__ __forceinline__ F1 df_mul(F1 a, F1 b) { return {a.h * b.h}; }
+__device__ __forceinline__ F1 df_pow2(F1 a, float k) { return {k * a.h}; }
+__device__ __forceinline__ F1 df_scale(F1 a, float k) { return {k * a.h}; }
+
+// storage and conversions of a number type: S the stored element of the level and
+// edge arrays, of() a stored element, ofp() a profile pair, st() the stored form
+template <class V>
+struct Num;
+template <>
+struct Num<DF> {
+   using S = float2;
+   static __device__ __forceinline__ DF zero() { return {0.f, 0.f}; }
+   static __device__ __forceinline__ DF of(float2 a) { return {a.x, a.y}; }
+   static __device__ __forceinline__ DF ofp(float2 a) { return {a.x, a.y}; }
+   static __device__ __forceinline__ float2 st(DF v) { return make_float2(v.h, v.l); }
+};
+template <>
+struct Num<F1> {
+   using S = float;
+   static __device__ __forceinline__ F1 zero() { return {0.f}; }
+   static __device__ __forceinline__ F1 of(float a) { return {a}; }
+   static __device__ __forceinline__ F1 ofp(float2 a) { return {a.x + a.y}; }
+   static __device__ __forceinline__ float st(F1 v) { return v.h; }
+};
+template <class V>
+__device__ __forceinline__ const typename Num<V>::S* arr(const void* p)
+{
+   return static_cast<const typename Num<V>::S*>(p);
 }
 
 // the shift of a level class: 2^(emax - 1023 + margin) bounds its values
@@ -199,11 +242,11 @@ __global__ void __launch_bounds__(128) grad_prep_kernel(GradDF g)
       const double uq = __ldg(g.u + q), umq = __ldg(g.um + q), upq = __ldg(g.up + q);
       const double w1 = (upq - 2 * uq) + umq;
       const float2 vb = to_df(__ldg(g.b1 + q), ka), vm = to_df(__ldg(g.mt + q), ka), fw = to_df(w1, kf);
-      g.db1[q] = vb;
-      g.dmt[q] = vm;
-      g.dw1[q] = fw;
-      g.du[q] = to_df(uq, kf);
-      g.dum[q] = to_df(umq, kf);
+      static_cast<float2*>(g.db1)[q] = vb;
+      static_cast<float2*>(g.dmt)[q] = vm;
+      static_cast<float2*>(g.dw1)[q] = fw;
+      static_cast<float2*>(g.du)[q] = to_df(uq, kf);
+      static_cast<float2*>(g.dum)[q] = to_df(umq, kf);
       if (in) {
          const float2 d = to_df(__ldg(g.un + q) - upq, kf);
          acc = df_add(acc, df_add(df_mul(df_of(vm), df_of(fw)), df_mul(df_of(vb), df_of(d))));
@@ -212,7 +255,55 @@ __global__ void __launch_bounds__(128) grad_prep_kernel(GradDF g)
    if (in) {
       const DF w = df_mul(df_mul(df_of(g.ist[0][i - b.ib]), df_of(g.ist[1][j - b.jb])),
                           df_of(g.ist[2][k - b.kb]));
-      acc_add(g.ar, p, df_neg(df_mul(w, acc)));
+      acc_add(static_cast<float2*>(g.ar), p, df_neg(df_mul(w, acc)));
+   }
+}
+
+// The mixed form's step: its double-float levels (hi at q, lo at q + g.lo) rounded to
+// FP32 values, w1 = up - 2u + um and un - up formed exactly first; the interior rho
+// terms -W [mt . w1 + b1 . (un - up)] added to the FP64 gradient.
+__device__ __forceinline__ float df_round(const float* x, long long q, long long lo)
+{
+   return __fadd_rn(__ldg(x + q), __ldg(x + q + lo));
+}
+
+__global__ void __launch_bounds__(128) grad_prep_f1_kernel(GradDF g)
+{
+   const Box& b = g.b;
+   const int i = b.ib + blockIdx.x * blockDim.x + threadIdx.x, j = b.jb + blockIdx.y,
+             k = b.kb + blockIdx.z;
+   if (i > b.ie) return;
+   const long long n = b.npts, lo = g.lo;
+   const long long p = (i - b.ib) + (j - b.jb) * b.ni + (k - b.kb) * b.nij;
+   const bool in = i >= b.ib + 2 && i <= b.ie - 2 && j >= b.jb + 2 && j <= b.je - 2 && k >= b.kb + 2 &&
+                   k <= b.ke - 2;
+   float acc = 0.f;
+#pragma unroll
+   for (int c = 0; c < 3; c++) {
+      const long long q = c * n + p;
+      // w1 = up - 2u + um exactly from the pairs, rounded once
+      float s1, e1, s2, e2;
+      two_sum(__ldg(g.lup + q), -2.f * __ldg(g.lu + q), s1, e1);
+      two_sum(s1, __ldg(g.lum + q), s2, e2);
+      const float w1 = s2 + ((e1 + e2) + ((__ldg(g.lup + q + lo) - 2.f * __ldg(g.lu + q + lo)) +
+                                         __ldg(g.lum + q + lo)));
+      const float vb = df_round(g.lb1, q, lo), vm = df_round(g.lmt, q, lo);
+      static_cast<float*>(g.db1)[q] = vb;
+      static_cast<float*>(g.dmt)[q] = vm;
+      static_cast<float*>(g.dw1)[q] = w1;
+      static_cast<float*>(g.du)[q] = df_round(g.lu, q, lo);
+      static_cast<float*>(g.dum)[q] = df_round(g.lum, q, lo);
+      if (in) {  // un - up exactly from the pairs
+         float d, e;
+         two_sum(__ldg(g.lun + q), -__ldg(g.lup + q), d, e);
+         d = d + (e + (__ldg(g.lun + q + lo) - __ldg(g.lup + q + lo)));
+         acc = fmaf(vm, w1, fmaf(vb, d, acc));
+      }
+   }
+   if (in) {
+      const float w = Num<F1>::ofp(g.ist[0][i - b.ib]).h * Num<F1>::ofp(g.ist[1][j - b.jb]).h *
+                      Num<F1>::ofp(g.ist[2][k - b.kb]).h;
+      g.gr64[p] -= (double)(w * acc);
    }
 }
 
@@ -223,36 +314,37 @@ constexpr int kGradThreads = 128;  // 32 x 4 points per CTA
 // the component along a, lambda weight for it alone) and the pairs 12 x (mt, u) +
 // (b1, w1).  CHECK: some of q, q+1, q+2 lie outside the array along a (values there
 // count as zero; q may lie below the array).
-template <bool CHECK>
+template <class V, bool CHECK>
 __device__ __forceinline__ void edges_body(const GradDF& g, long long n, int pq, bool ok0, bool ok1, bool ok2,
-                                           int sd, int a, DF E[4])
+                                           int sd, int a, V E[4])
 {
-   E[0] = E[1] = E[2] = E[3] = df_zero();
+   using N = Num<V>;
+   E[0] = E[1] = E[2] = E[3] = N::zero();
 #pragma unroll
    for (int t = 0; t < 2; t++) {
-      DF s1 = df_zero(), s2 = df_zero(), a1 = df_zero(), a2 = df_zero();
+      V s1 = N::zero(), s2 = N::zero(), a1 = N::zero(), a2 = N::zero();
 #pragma unroll
       for (int c = 0; c < 3; c++) {
-         const float2* __restrict__ A = (t == 0 ? g.dmt : g.db1) + c * n;
-         const float2* __restrict__ F = (t == 0 ? g.du : g.dw1) + c * n;
-         DF x0, x1, x2, y0, y1, y2;
+         const typename N::S* __restrict__ A = arr<V>(t == 0 ? g.dmt : g.db1) + c * n;
+         const typename N::S* __restrict__ F = arr<V>(t == 0 ? g.du : g.dw1) + c * n;
+         V x0, x1, x2, y0, y1, y2;
          if (CHECK) {
-            x0 = ok0 ? df_of(__ldg(A + pq)) : df_zero();
-            y0 = ok0 ? df_of(__ldg(F + pq)) : df_zero();
-            x1 = ok1 ? df_of(__ldg(A + pq + sd)) : df_zero();
-            y1 = ok1 ? df_of(__ldg(F + pq + sd)) : df_zero();
-            x2 = ok2 ? df_of(__ldg(A + pq + 2 * sd)) : df_zero();
-            y2 = ok2 ? df_of(__ldg(F + pq + 2 * sd)) : df_zero();
+            x0 = ok0 ? N::of(__ldg(A + pq)) : N::zero();
+            y0 = ok0 ? N::of(__ldg(F + pq)) : N::zero();
+            x1 = ok1 ? N::of(__ldg(A + pq + sd)) : N::zero();
+            y1 = ok1 ? N::of(__ldg(F + pq + sd)) : N::zero();
+            x2 = ok2 ? N::of(__ldg(A + pq + 2 * sd)) : N::zero();
+            y2 = ok2 ? N::of(__ldg(F + pq + 2 * sd)) : N::zero();
          } else {
-            x0 = df_of(__ldg(A + pq));
-            y0 = df_of(__ldg(F + pq));
-            x1 = df_of(__ldg(A + pq + sd));
-            y1 = df_of(__ldg(F + pq + sd));
-            x2 = df_of(__ldg(A + pq + 2 * sd));
-            y2 = df_of(__ldg(F + pq + 2 * sd));
+            x0 = N::of(__ldg(A + pq));
+            y0 = N::of(__ldg(F + pq));
+            x1 = N::of(__ldg(A + pq + sd));
+            y1 = N::of(__ldg(F + pq + sd));
+            x2 = N::of(__ldg(A + pq + 2 * sd));
+            y2 = N::of(__ldg(F + pq + 2 * sd));
          }
-         const DF e1 = df_mul(df_diff(x1, x0), df_diff(y1, y0));
-         const DF e2 = df_mul(df_diff(x2, x0), df_diff(y2, y0));
+         const V e1 = df_mul(df_diff(x1, x0), df_diff(y1, y0));
+         const V e2 = df_mul(df_diff(x2, x0), df_diff(y2, y0));
          s1 = df_add(s1, e1);
          s2 = df_add(s2, e2);
          if (c == a) {
@@ -268,17 +360,19 @@ __device__ __forceinline__ void edges_body(const GradDF& g, long long n, int pq,
    }
 }
 
+template <class V>
 __device__ __forceinline__ void edges_at(const GradDF& g, long long n, int pq, int xq, int xl, int xh, int sd,
-                                         int a, DF E[4])
+                                         int a, V E[4])
 {
    if (xq >= xl && xq + 2 <= xh)
-      edges_body<false>(g, n, pq, true, true, true, sd, a, E);
+      edges_body<V, false>(g, n, pq, true, true, true, sd, a, E);
    else
-      edges_body<true>(g, n, pq, xq >= xl, xq + 1 >= xl && xq + 1 <= xh, xq + 2 >= xl && xq + 2 <= xh, sd, a,
-                       E);
+      edges_body<V, true>(g, n, pq, xq >= xl, xq + 1 >= xl && xq + 1 <= xh, xq + 2 >= xl && xq + 2 <= xh, sd,
+                          a, E);
 }
 
 // the edge sums of every array point: ed[(a*4 + r) * npts + p]
+template <class V>
 __global__ void __launch_bounds__(kGradThreads) grad_edge_kernel(GradDF g)
 {
    const Box& b = g.b;
@@ -292,28 +386,32 @@ __global__ void __launch_bounds__(kGradThreads) grad_edge_kernel(GradDF g)
       const int x = a == 0 ? i : a == 1 ? j : k;
       const int xl = a == 0 ? b.ib : a == 1 ? b.jb : b.kb, xh = a == 0 ? b.ie : a == 1 ? b.je : b.ke;
       const int sd = a == 0 ? 1 : a == 1 ? (int)b.ni : (int)b.nij;
-      DF E[4];
-      edges_at(g, n, p, x, xl, xh, sd, a, E);
+      V E[4];
+      edges_at<V>(g, n, p, x, xl, xh, sd, a, E);
 #pragma unroll
-      for (int r = 0; r < 4; r++) g.ed[(a * 4 + r) * n + p] = make_float2(E[r].h, E[r].l);
+      for (int r = 0; r < 4; r++)
+         static_cast<typename Num<V>::S*>(g.ed)[(a * 4 + r) * n + p] = Num<V>::st(E[r]);
    }
 }
 
 // centred first differences (DW . f)(p) = f(p-2) - f(p+2) + 8 (f(p+1) - f(p-1)) of
 // one component of A and F along an axis (x[m], y[m]: values at p + (m-2) sd)
-__device__ __forceinline__ void first_diffs(const DF x[5], const DF y[5], bool inner, DF& fa, DF& fw)
+template <class V>
+__device__ __forceinline__ void first_diffs(const V x[5], const V y[5], bool inner, V& fa, V& fw)
 {
    fa = df_addf(df_diff(x[0], x[4]), df_pow2(df_diff(x[3], x[1]), 8.f));
-   fw = inner ? df_addf(df_diff(y[0], y[4]), df_pow2(df_diff(y[3], y[1]), 8.f)) : df_zero();
+   fw = inner ? df_addf(df_diff(y[0], y[4]), df_pow2(df_diff(y[3], y[1]), 8.f)) : Num<V>::zero();
 }
 
 // the mu, lambda and damping rho sums of one point from the edge sums, the centred
 // first differences and the damping's second differences
+template <class V>
 __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
 {
+   using N = Num<V>;
    // centred first differences of the current pair, [slot][thread]: slot c*3 + a for
    // the adjoint level, 9 + c*3 + a for the forward level
-   __shared__ float2 fd[18][kGradThreads];
+   __shared__ typename N::S fd[18][kGradThreads];
    const int tid = threadIdx.y * 32 + threadIdx.x;
    const Box& b = g.b;
    const int pc[3] = {b.ib + (int)(blockIdx.x * 32 + threadIdx.x), b.jb + (int)(blockIdx.y * 4 + threadIdx.y),
@@ -322,7 +420,7 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
    const long long n = b.npts;
    const int off[3] = {pc[0] - b.ib, pc[1] - b.jb, pc[2] - b.kb};
    const int p = off[0] + off[1] * (int)b.ni + off[2] * (int)b.nij;
-   DF gm = df_zero(), gl = df_zero(), gr = df_zero();
+   V gm = N::zero(), gl = N::zero(), gr = N::zero();
    // same-axis second differences: the seven edges of each axis around p
 #pragma unroll 1
    for (int a = 0; a < 3; a++) {
@@ -332,38 +430,38 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
       const int sd = a == 0 ? 1 : a == 1 ? (int)b.ni : (int)b.nij;
       const int oa = x0 - xl, o1 = a1 == 0 ? off[0] : a1 == 1 ? off[1] : off[2],
                 o2 = a2 == 0 ? off[0] : a2 == 1 ? off[1] : off[2];
-      const float2* __restrict__ ed = g.ed + a * 4 * n;
-      DF E[4][4];  // edges starting at p-2 .. p+1
+      const typename N::S* __restrict__ ed = arr<V>(g.ed) + a * 4 * n;
+      V E[4][4];  // edges starting at p-2 .. p+1
       if (x0 - 2 >= xl && x0 + 1 <= xh) {
 #pragma unroll
          for (int m = 0; m < 4; m++)
 #pragma unroll
-            for (int r = 0; r < 4; r++) E[m][r] = df_of(__ldg(ed + r * n + p + (m - 2) * sd));
+            for (int r = 0; r < 4; r++) E[m][r] = N::of(__ldg(ed + r * n + p + (m - 2) * sd));
       } else {
 #pragma unroll
          for (int m = 0; m < 4; m++) {
             const int x = x0 + m - 2;
             const int q = p + (m - 2) * sd;
             if (x > xh) {
-               E[m][0] = E[m][1] = E[m][2] = E[m][3] = df_zero();
+               E[m][0] = E[m][1] = E[m][2] = E[m][3] = N::zero();
             } else if (x >= xl) {
 #pragma unroll
-               for (int r = 0; r < 4; r++) E[m][r] = df_of(__ldg(ed + r * n + q));
+               for (int r = 0; r < 4; r++) E[m][r] = N::of(__ldg(ed + r * n + q));
             } else {  // an edge from below the array (ghost-point gradients)
-               edges_at(g, n, q, x, xl, xh, sd, a, E[m]);
+               edges_at<V>(g, n, q, x, xl, xh, sd, a, E[m]);
             }
          }
       }
       // E1(p+1) + E1(p-2) + E2(p-1) + 3 [E1(p-1) + E1(p) - (E2(p) + E2(p-2))/4]
-      DF T[2];
+      V T[2];
 #pragma unroll
       for (int r = 0; r < 2; r++) {
-         const DF X = df_addf(df_addf(E[3][r], E[0][r]), E[1][2 + r]);
-         const DF Y = df_addf(df_addf(E[1][r], E[2][r]), df_pow2(df_addf(E[2][2 + r], E[0][2 + r]), -0.25f));
+         const V X = df_addf(df_addf(E[3][r], E[0][r]), E[1][2 + r]);
+         const V Y = df_addf(df_addf(E[1][r], E[2][r]), df_pow2(df_addf(E[2][2 + r], E[0][2 + r]), -0.25f));
          T[r] = df_addf(X, df_scale(Y, 3.f));
       }
-      const DF qq = df_mul(df_mul(df_of(__ldg(g.st24[a] + oa)), df_of(__ldg(g.ist[a1] + o1))),
-                           df_of(__ldg(g.ist[a2] + o2)));
+      const V qq = df_mul(df_mul(N::ofp(__ldg(g.st24[a] + oa)), N::ofp(__ldg(g.ist[a1] + o1))),
+                           N::ofp(__ldg(g.ist[a2] + o2)));
       gm = df_add(gm, df_mul(qq, T[0]));
       gl = df_add(gl, df_mul(qq, T[1]));
    }
@@ -382,47 +480,47 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
          const bool inner = x0 - 2 >= xl && x0 + 2 <= xh;
          const float2 bd = t == 0 ? __ldg(g.bdc[a] + oa) : make_float2(0.f, 0.f);
          const bool damp = t == 0 && x0 - 1 >= xl && x0 + 1 <= xh && bd.x != 0.f;
-         DF ds = df_zero();
+         V ds = N::zero();
 #pragma unroll
          for (int c = 0; c < 3; c++) {
-            const float2* __restrict__ A = (t == 0 ? g.dmt : g.db1) + c * n;
-            const float2* __restrict__ F = (t == 0 ? g.du : g.dw1) + c * n;
-            DF x[5], y[5];
+            const typename N::S* __restrict__ A = arr<V>(t == 0 ? g.dmt : g.db1) + c * n;
+            const typename N::S* __restrict__ F = arr<V>(t == 0 ? g.du : g.dw1) + c * n;
+            V x[5], y[5];
             if (inner) {
 #pragma unroll
                for (int m = 0; m < 5; m++) {
                   if (m == 2) continue;
-                  x[m] = df_of(__ldg(A + p + (m - 2) * sd));
-                  y[m] = df_of(__ldg(F + p + (m - 2) * sd));
+                  x[m] = N::of(__ldg(A + p + (m - 2) * sd));
+                  y[m] = N::of(__ldg(F + p + (m - 2) * sd));
                }
             } else {
 #pragma unroll
                for (int m = 0; m < 5; m++) {
                   if (m == 2) continue;
                   const bool ok = x0 + m - 2 >= xl && x0 + m - 2 <= xh;
-                  x[m] = ok ? df_of(__ldg(A + p + (m - 2) * sd)) : df_zero();
-                  y[m] = ok ? df_of(__ldg(F + p + (m - 2) * sd)) : df_zero();
+                  x[m] = ok ? N::of(__ldg(A + p + (m - 2) * sd)) : N::zero();
+                  y[m] = ok ? N::of(__ldg(F + p + (m - 2) * sd)) : N::zero();
                }
             }
-            DF fa, fw;
-            first_diffs(x, y, inner, fa, fw);
-            fd[c * 3 + a][tid] = make_float2(fa.h, fa.l);
-            fd[9 + c * 3 + a][tid] = make_float2(fw.h, fw.l);
+            V fa, fw;
+            first_diffs<V>(x, y, inner, fa, fw);
+            fd[c * 3 + a][tid] = N::st(fa);
+            fd[9 + c * 3 + a][tid] = N::st(fw);
             if (damp) {  // D2(u - um) D2(b1) along a (y holds u at p -+ 1)
-               const float2* __restrict__ um = g.dum + c * n;
-               const float2* __restrict__ b1 = g.db1 + c * n;
-               const DF d0 = df_diff(y[1], df_of(__ldg(um + p - sd)));
-               const DF d1 = df_diff(df_of(__ldg(F + p)), df_of(__ldg(um + p)));
-               const DF d2 = df_diff(y[3], df_of(__ldg(um + p + sd)));
-               const DF d2u = df_addf(df_addf(d0, d2), df_pow2(d1, -2.f));
-               const DF d2b = df_addf(df_addf(df_of(__ldg(b1 + p - sd)), df_of(__ldg(b1 + p + sd))),
-                                      df_pow2(df_of(__ldg(b1 + p)), -2.f));
+               const typename N::S* __restrict__ um = arr<V>(g.dum) + c * n;
+               const typename N::S* __restrict__ b1 = arr<V>(g.db1) + c * n;
+               const V d0 = df_diff(y[1], N::of(__ldg(um + p - sd)));
+               const V d1 = df_diff(N::of(__ldg(F + p)), N::of(__ldg(um + p)));
+               const V d2 = df_diff(y[3], N::of(__ldg(um + p + sd)));
+               const V d2u = df_addf(df_addf(d0, d2), df_pow2(d1, -2.f));
+               const V d2b = df_addf(df_addf(N::of(__ldg(b1 + p - sd)), N::of(__ldg(b1 + p + sd))),
+                                      df_pow2(N::of(__ldg(b1 + p)), -2.f));
                ds = df_add(ds, df_mul(d2u, d2b));
             }
          }
          if (damp) {
-            const DF cc = df_mul(df_of(__ldg(g.cist[a1] + o1)), df_of(__ldg(g.cist[a2] + o2)));
-            gr = df_add(gr, df_neg(df_mul(df_mul(df_of(bd), cc), ds)));
+            const V cc = df_mul(N::ofp(__ldg(g.cist[a1] + o1)), N::ofp(__ldg(g.cist[a2] + o2)));
+            gr = df_add(gr, df_neg(df_mul(df_mul(N::ofp(bd), cc), ds)));
          }
       }
       // mixed terms, grouped by the axis t3 that neither derivative takes:
@@ -430,19 +528,25 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
 #pragma unroll 1
       for (int t3 = 0; t3 < 3; t3++) {
          const int a1 = t3 == 2 ? 0 : t3 + 1, a2 = t3 == 0 ? 2 : t3 - 1;
-         auto A_ = [&](int c, int a) { return df_of(fd[c * 3 + a][tid]); };
-         auto W_ = [&](int c, int a) { return df_of(fd[9 + c * 3 + a][tid]); };
-         const DF ml = df_addf(df_mul(W_(a2, a2), A_(a1, a1)), df_mul(W_(a1, a1), A_(a2, a2)));
-         const DF mm = df_addf(df_mul(W_(a2, a1), A_(a1, a2)), df_mul(W_(a1, a2), A_(a2, a1)));
+         auto A_ = [&](int c, int a) { return N::of(fd[c * 3 + a][tid]); };
+         auto W_ = [&](int c, int a) { return N::of(fd[9 + c * 3 + a][tid]); };
+         const V ml = df_addf(df_mul(W_(a2, a2), A_(a1, a1)), df_mul(W_(a1, a1), A_(a2, a2)));
+         const V mm = df_addf(df_mul(W_(a2, a1), A_(a1, a2)), df_mul(W_(a1, a2), A_(a2, a1)));
          const int ot = t3 == 0 ? off[0] : t3 == 1 ? off[1] : off[2];
-         const DF f = df_scale(df_of(__ldg(g.ist[t3] + ot)), wt);
+         const V f = df_scale(N::ofp(__ldg(g.ist[t3] + ot)), wt);
          gm = df_add(gm, df_mul(f, mm));
          gl = df_add(gl, df_mul(f, ml));
       }
    }
-   acc_add(g.am, p, gm);
-   acc_add(g.al, p, gl);
-   acc_add(g.ar, p, gr);
+   if constexpr (sizeof(V) == sizeof(DF)) {  // per-segment double-float sums
+      acc_add(static_cast<float2*>(g.am), p, gm);
+      acc_add(static_cast<float2*>(g.al), p, gl);
+      acc_add(static_cast<float2*>(g.ar), p, gr);
+   } else {  // the FP64 gradients, every step
+      g.gm64[p] += g.kmu * (double)Num<V>::st(gm);
+      g.gl64[p] += g.kmu * (double)Num<V>::st(gl);
+      g.gr64[p] += (double)Num<V>::st(gr);
+   }
 }
 
 // g += scale * acc (FP64), acc = 0
@@ -505,16 +609,30 @@ int launch_grad_df_step(const GradDF& g, cudaStream_t s)
    grad_prep_kernel<<<dim3((ni + 127) / 128, nj, nk), 128, 0, s>>>(g);
    SW4G_TRY(launch_status());
    const dim3 grid((ni + 31) / 32, (nj + 3) / 4, nk), block(32, 4);
-   grad_edge_kernel<<<grid, block, 0, s>>>(g);
+   grad_edge_kernel<DF><<<grid, block, 0, s>>>(g);
    SW4G_TRY(launch_status());
-   grad_df_kernel<<<grid, block, 0, s>>>(g);
+   grad_df_kernel<DF><<<grid, block, 0, s>>>(g);
+   return launch_status();
+}
+
+int launch_grad_f1_step(const GradDF& g, cudaStream_t s)
+{
+   const Box& b = g.b;
+   const int ni = (int)b.ni, nj = b.je - b.jb + 1, nk = b.ke - b.kb + 1;
+   grad_prep_f1_kernel<<<dim3((ni + 127) / 128, nj, nk), 128, 0, s>>>(g);
+   SW4G_TRY(launch_status());
+   const dim3 grid((ni + 31) / 32, (nj + 3) / 4, nk), block(32, 4);
+   grad_edge_kernel<F1><<<grid, block, 0, s>>>(g);
+   SW4G_TRY(launch_status());
+   grad_df_kernel<F1><<<grid, block, 0, s>>>(g);
    return launch_status();
 }
 
 int launch_grad_df_flush(const GradDF& g, double kmu, double* gm, double* gl, double* gr, cudaStream_t s)
 {
-   grad_flush_kernel<<<grid_stride_blocks(g.b.npts, 256), 256, 0, s>>>(g.b.npts, g.am, g.al, g.ar, g.emax,
-                                                                      g.marg_a, g.marg_f, kmu, gm, gl, gr);
+   grad_flush_kernel<<<grid_stride_blocks(g.b.npts, 256), 256, 0, s>>>(
+       g.b.npts, static_cast<float2*>(g.am), static_cast<float2*>(g.al), static_cast<float2*>(g.ar), g.emax,
+       g.marg_a, g.marg_f, kmu, gm, gl, gr);
    return launch_status();
 }
 

@@ -33,8 +33,8 @@
 //   rho        : -W [mt.(up - 2u + um) + b1.(u+ - up)] (the 1/rho factors and
 //                the forcing) - beta dc D2(u - um) . D2(w W b1) (the damping's
 //                rho dc factors).
-// The FP64 form evaluates these sums in double-float arithmetic on the FP32 pipe
-// (adj_grad.cu); the mixed form in FP32 with the kernels below.
+// These sums run in adj_grad.cu: double-float arithmetic on the FP32 pipe for the
+// FP64 form, FP32 for the mixed form.
 // Forward levels come from checkpoints every C steps, recomputed one segment
 // at a time with every level and predicted level kept in HBM.
 #include <algorithm>
@@ -47,12 +47,6 @@
 namespace sw4g {
 namespace {
 
-__device__ __forceinline__ bool inside(const Box& b, int i, int j, int k)
-{
-   return i >= b.ib + 2 && i <= b.ie - 2 && j >= b.jb + 2 && j <= b.je - 2 && k >= b.kb + 2 &&
-          k <= b.ke - 2;
-}
-
 template <class T>
 struct ProfT {
    const T *dc[3], *st[3], *co[3];
@@ -63,22 +57,6 @@ template <class T>
 __device__ __forceinline__ T sxyz(const Box& b, const ProfT<T>& f, int i, int j, int k)
 {
    return f.st[0][i - b.ib] * f.st[1][j - b.jb] * f.st[2][k - b.kb];
-}
-
-// a[q] - b[q] of two double-float levels (hi at q, lo at q + lo), formed exactly and
-// rounded once to FP32
-__device__ __forceinline__ float lev_diff(const float* a, const float* b, long long q, long long lo)
-{
-   float d, e;
-   two_sum(__ldg(a + q), -__ldg(b + q), d, e);
-   return d + (e + (__ldg(a + q + lo) - __ldg(b + q + lo)));
-}
-
-__device__ __forceinline__ void grid_point(const Box& b, long long p, int& i, int& j, int& k)
-{
-   i = b.ib + (int)(p % b.ni);
-   j = b.jb + (int)((p / b.ni) % (b.je - b.jb + 1));
-   k = b.kb + (int)(p / b.nij);
 }
 
 // b[receiver point] += W^-1 R res (receivers in order, 3 values each)
@@ -96,40 +74,7 @@ __global__ void adj_source_kernel(Box b, Prof f, int nrec, const int* __restrict
    for (int c = 0; c < 3; c++) an[c * b.npts + p] += s * res[3 * r + c];
 }
 
-// The mixed form's helpers over double-float levels (hi at q, lo at q + 3 npts):
-// w1 = up - 2u + um formed exactly and rounded to FP32; v1 = c1 W b1, v2 = c2 W mt in
-// FP32; the adjoint source added to a double-float level in FP64.
-__global__ void adj_w1_df_kernel(long long n3, const float* __restrict__ up, const float* __restrict__ u,
-                                 const float* __restrict__ um, float* __restrict__ w1)
-{
-   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n3;
-        q += (long long)gridDim.x * blockDim.x) {
-      float s1, e1, s2, e2;
-      two_sum(up[q], -2.f * u[q], s1, e1);
-      two_sum(s1, um[q], s2, e2);
-      w1[q] = s2 + ((e1 + e2) + ((up[q + n3] - 2.f * u[q + n3]) + um[q + n3]));
-   }
-}
-
-__global__ void adj_v_df_kernel(Box b, ProfT<float> f, const float* __restrict__ b1,
-                                const float* __restrict__ mt, float c1, float c2,
-                                float* __restrict__ v1, float* __restrict__ v2)
-{
-   const long long lo = 3 * b.npts;
-   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < b.npts;
-        p += (long long)gridDim.x * blockDim.x) {
-      int i, j, k;
-      grid_point(b, p, i, j, k);
-      const float w = 1.f / sxyz(b, f, i, j, k);
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-         const long long q = c * b.npts + p;
-         v1[q] = (c1 * w) * (b1[q] + b1[q + lo]);
-         v2[q] = (c2 * w) * (mt[q] + mt[q + lo]);
-      }
-   }
-}
-
+// the adjoint source added to a double-float level (hi at q, lo at q + 3 npts) in FP64
 __global__ void adj_source_df_kernel(Box b, Prof f, int nrec, const int* __restrict__ ijk,
                                      const double* __restrict__ res, const double* __restrict__ rho,
                                      float* __restrict__ an, const double* __restrict__ clk, int nval)
@@ -145,266 +90,18 @@ __global__ void adj_source_df_kernel(Box b, Prof f, int nrec, const int* __restr
    for (int c = 0; c < 3; c++) a.set(c * b.npts + p, a.get(c * b.npts + p) + s * res[3 * r + c]);
 }
 
-__device__ constexpr double kDW[5] = {1, -8, 0, 8, -1};
-// mixed terms of the operator: (equation, component, outer axis, inner axis, lambda?)
-__device__ constexpr int kMix[12][5] = {{0, 1, 0, 1, 1}, {0, 1, 1, 0, 0}, {0, 2, 0, 2, 1},
-                                        {0, 2, 2, 0, 0}, {1, 0, 0, 1, 0}, {1, 0, 1, 0, 1},
-                                        {1, 2, 1, 2, 1}, {1, 2, 2, 1, 0}, {2, 0, 0, 2, 0},
-                                        {2, 0, 2, 0, 1}, {2, 1, 1, 2, 0}, {2, 1, 2, 1, 1}};
-
-// T = double: FP64 throughout.  T = float (the mixed form): the levels u, um, up, un
-// are double-float (lo = 3 npts further; the stencil terms read the hi halves, the
-// level differences un - up and u - um are formed exactly), the products and sums are
-// FP32 and each point's contribution is accumulated into the FP64 gradients.
-template <class T>
-struct GradArgs {
-   Box b;
-   ProfT<T> f;
-   const T *v1, *v2, *rho, *u, *um, *up, *un, *w1;
-   double* gr;
-   double* gm;
-   double* gl;
-   T c1, c2;  // v1 = c1 W b1 (pair with w1), v2 = c2 W mt (pair with u)
-   T ih2, beta;
-   T k6, k144, ic1, ic2, bc1;  // -ih2/6, -ih2/144, 1/c1, 1/c2, beta/c1 (set by grad_constants)
-   long long lo;  // offset of the levels' lo halves (float only)
-   T* ed;         // edge products, 12 x npts (adj_edge_kernel)
-};
-
-// The forward edges (p, p+1) and (p, p+2) along ax of the second differences'
-// edge form, summed over the two pairs (v1, w1), (v2, u) and the three components
-// with the mu weights (2 for c == ax, else 1) and the lambda weights (c == ax only):
-// e = {EM1, EL1, EM2, EL2}.  Values beyond the array are zero; p may lie one or two
-// points below the array along ax (then only its in-array neighbours are read).
-template <class T>
-__device__ __forceinline__ void edges_at(const GradArgs<T>& g, int ax, const int pc[3], long long p,
-                                         T e[4])
-{
-   const Box& b = g.b;
-   const long long n = b.npts;
-   const long long st = ax == 0 ? 1 : ax == 1 ? b.ni : b.nij;
-   const int lo = ax == 0 ? b.ib : ax == 1 ? b.jb : b.kb, hi = ax == 0 ? b.ie : ax == 1 ? b.je : b.ke;
-   bool ok[3];
-   T sv[3];
-#pragma unroll
-   for (int m = 0; m < 3; m++) {
-      const int x = pc[ax] + m;
-      ok[m] = x >= lo && x <= hi;
-      sv[m] = ok[m] ? g.f.st[ax][x - lo] : T(0);
-   }
-   e[0] = e[1] = e[2] = e[3] = 0;
-#pragma unroll
-   for (int t = 0; t < 2; t++) {
-      const T* vb = t == 0 ? g.v1 : g.v2;
-      const T* wf = t == 0 ? g.w1 : g.u;
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-         T v[3], w[3];
-#pragma unroll
-         for (int m = 0; m < 3; m++) {
-            if (!ok[m]) {
-               v[m] = w[m] = 0;
-               continue;
-            }
-            const long long q = c * n + p + m * st;
-            v[m] = sv[m] * vb[q];
-            w[m] = wf[q];
-         }
-         const T e1 = (v[1] - v[0]) * (w[1] - w[0]), e2 = (v[2] - v[0]) * (w[2] - w[0]);
-         if (c == ax) {
-            e[0] += 2 * e1;
-            e[1] += e1;
-            e[2] += 2 * e2;
-            e[3] += e2;
-         } else {
-            e[0] += e1;
-            e[2] += e2;
-         }
-      }
-   }
-}
-
-template <class T>
-void grad_constants(GradArgs<T>& g)
-{
-   g.k6 = -g.ih2 / T(6);
-   g.k144 = -g.ih2 / T(144);
-   g.ic1 = T(1) / g.c1;
-   g.ic2 = T(1) / g.c2;
-   g.bc1 = g.beta / g.c1;
-}
-
-template <class T>
-__global__ void __launch_bounds__(128) adj_edge_kernel(GradArgs<T> g)
-{
-   const long long n = g.b.npts;
-   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
-        p += (long long)gridDim.x * blockDim.x) {
-      int pc[3];
-      grid_point(g.b, p, pc[0], pc[1], pc[2]);
-#pragma unroll
-      for (int ax = 0; ax < 3; ax++) {
-         T e[4];
-         edges_at(g, ax, pc, p, e);
-#pragma unroll
-         for (int r = 0; r < 4; r++) g.ed[(ax * 4 + r) * n + p] = e[r];
-      }
-   }
-}
-
-// gradient of a1 . u+ at every array point (one thread per point)
-template <class T>
-__global__ void __launch_bounds__(128) adj_gradient_kernel(GradArgs<T> g)
-{
-   const Box& b = g.b;
-   const long long n = b.npts;
-   const long long st[3] = {1, b.ni, b.nij};
-   const int lo[3] = {b.ib, b.jb, b.kb}, hi[3] = {b.ie, b.je, b.ke};
-   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
-        p += (long long)gridDim.x * blockDim.x) {
-      int pc[3];
-      grid_point(b, p, pc[0], pc[1], pc[2]);
-      T gm = 0, gl = 0, gr = 0;
-      // same-axis second differences: the seven edges of each axis around p
-#pragma unroll
-      for (int ax = 0; ax < 3; ax++) {
-         T E[4][4];  // edges starting at p-2 .. p+1: {EM1, EL1, EM2, EL2}
-#pragma unroll
-         for (int m = -2; m <= 1; m++) {
-            const int x = pc[ax] + m;
-            if (x > hi[ax]) {
-               E[m + 2][0] = E[m + 2][1] = E[m + 2][2] = E[m + 2][3] = 0;
-            } else if (x >= lo[ax]) {
-#pragma unroll
-               for (int r = 0; r < 4; r++) E[m + 2][r] = g.ed[(ax * 4 + r) * n + p + m * st[ax]];
-            } else {  // an edge from below the array (ghost-point gradients)
-               int qc[3] = {pc[0], pc[1], pc[2]};
-               qc[ax] = x;
-               edges_at(g, ax, qc, p + m * st[ax], E[m + 2]);
-            }
-         }
-         const T s = g.k6 * g.f.st[ax][pc[ax] - lo[ax]];
-#pragma unroll
-         for (int r = 0; r < 2; r++)  // r = 0: mu, 1: lambda
-         {
-            const T val = E[3][r] + E[0][r] + T(3) * (E[1][r] + E[2][r]) + E[1][2 + r] -
-                          T(0.75) * (E[2][2 + r] + E[0][2 + r]);
-            if (r == 0) gm += s * val;
-            else gl += s * val;
-         }
-      }
-      // mixed terms: -(1/144h^2) s_ai(p) (DW . w_d along ai)(p) (DW . (s_ao v_c) along ao)(p),
-      // each first difference computed once per pair; ws = DW x s along each axis
-      T ws[3][5];
-#pragma unroll
-      for (int a = 0; a < 3; a++)
-#pragma unroll
-         for (int m = -2; m <= 2; m++) {
-            const int x = pc[a] + m;
-            ws[a][m + 2] = (m == 0 || x < lo[a] || x > hi[a]) ? T(0) : T(kDW[m + 2]) * g.f.st[a][x - lo[a]];
-         }
-#pragma unroll
-      for (int t = 0; t < 2; t++) {
-         const T* vb = t == 0 ? g.v1 : g.v2;
-         const T* wf = t == 0 ? g.w1 : g.u;
-         T din[3][3], dout[3][3];
-#pragma unroll
-         for (int a = 0; a < 3; a++) {
-            const bool inner_ok = pc[a] >= lo[a] + 2 && pc[a] <= hi[a] - 2;
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-               T si = 0, so = 0;
-#pragma unroll
-               for (int m = -2; m <= 2; m++) {
-                  if (m == 0) continue;
-                  if (inner_ok) si += T(kDW[m + 2]) * wf[c * n + p + m * st[a]];
-                  const int x = pc[a] + m;
-                  if (x < lo[a] || x > hi[a]) continue;
-                  so += ws[a][m + 2] * vb[c * n + p + m * st[a]];
-               }
-               din[c][a] = si;
-               dout[c][a] = so;
-            }
-         }
-#pragma unroll
-         for (int e = 0; e < 12; e++) {
-            const int c = kMix[e][0], d = kMix[e][1], ao = kMix[e][2], ai = kMix[e][3];
-            if (pc[ai] < lo[ai] + 2 || pc[ai] > hi[ai] - 2) continue;
-            const T gg = g.k144 * g.f.st[ai][pc[ai] - lo[ai]] * din[d][ai] * dout[c][ao];
-            if (kMix[e][4]) gl += gg;
-            else gm += gg;
-         }
-      }
-      // rho: the 1/rho factors and forcing (interior points), and the damping's rho dc
-      if (inside(b, pc[0], pc[1], pc[2])) {
-         // W mt = v2/c2, W b1 = v1/c1
-         T s1 = 0, s2 = 0;
-#pragma unroll
-         for (int c = 0; c < 3; c++) {
-            const long long q = c * n + p;
-            s2 += g.v2[q] * g.w1[q];
-            s1 += g.v1[q] * lev_diff(g.un, g.up, q, g.lo);
-         }
-         gr -= s2 * g.ic2 + s1 * g.ic1;
-      }
-      if (g.beta != 0) {
-         T sgr = 0;
-#pragma unroll
-         for (int ax = 0; ax < 3; ax++) {
-            if (pc[ax] - 1 < lo[ax] || pc[ax] + 1 > hi[ax]) continue;
-            const T dcp = g.f.dc[ax][pc[ax] - lo[ax]];
-            if (dcp == 0) continue;  // the term is exactly zero there
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-               T vv[3], dd[3];
-#pragma unroll
-               for (int m = -1; m <= 1; m++) {
-                  int qc[3] = {pc[0], pc[1], pc[2]};
-                  qc[ax] += m;
-                  const long long q = p + m * st[ax];
-                  dd[m + 1] = lev_diff(g.u, g.um, c * n + q, g.lo);
-                  const int oi = qc[0] - b.ib, oj = qc[1] - b.jb, ok = qc[2] - b.kb;
-                  const T wax = ax == 0   ? g.f.st[0][oi] * g.f.co[1][oj] * g.f.co[2][ok]
-                                     : ax == 1 ? g.f.st[1][oj] * g.f.co[0][oi] * g.f.co[2][ok]
-                                               : g.f.st[2][ok] * g.f.co[0][oi] * g.f.co[1][oj];
-                  vv[m + 1] = wax * g.v1[c * n + q];
-               }
-               sgr += dcp * (dd[2] - 2 * dd[1] + dd[0]) * (vv[2] - 2 * vv[1] + vv[0]);
-            }
-         }
-         gr -= g.bc1 * sgr;  // vv holds c1 W b1
-      }
-      g.gm[p] += (double)gm;
-      g.gl[p] += (double)gl;
-      g.gr[p] += (double)gr;
-   }
-}
-
-int gs_blocks(long long n, int threads)
-{
-   long long b = (n + threads - 1) / threads;
-   if (b > 152 * 32) b = 152 * 32;
-   return (int)(b > 0 ? b : 1);
-}
-
 }  // namespace
 
-// One adjoint step of the mixed form (double-float b, mt and levels; FP32 w1, v1,
-// v2 in the first half of their buffers): the same sequence as the FP64 step.
-int EW::adjoint_step_mixed(const MixedStage& base, const void* pfv, const void* pf32v, const Box& b,
-                           size_t n3, const double* u, const double* um, const double* up,
-                           const double* un, double* b1, double* b2, double* bn, double* mt,
-                           double* w1, double* v1, double* v2, double* gr, double* gm, double* gl,
-                           double dt, double beta, int nrec, const double* res,
-                           const double* clk, int nval)
+// One adjoint step of the mixed form (double-float b, mt and levels): the same
+// sequence as the FP64 step, the gradient terms in FP32 (adj_grad.cu).
+int EW::adjoint_step_mixed(const MixedStage& base, const void* pfv, const GradDF& gbase, const Box& b,
+                           const double* u, const double* um, const double* up, const double* un, double* b1,
+                           double* b2, double* bn, double* mt, double dt, double beta, int nrec,
+                           const double* res, const double* clk, int nval)
 {
    const Prof& pf = *static_cast<const Prof*>(pfv);
-   const ProfT<float>& pf32 = *static_cast<const ProfT<float>*>(pf32v);
    auto F = [](double* x) { return reinterpret_cast<float*>(x); };
    auto CF = [](const double* x) { return reinterpret_cast<const float*>(x); };
-   adj_w1_df_kernel<<<gs_blocks((long long)n3, 256), 256, 0, stream_>>>((long long)n3, CF(up), CF(u),
-                                                                          CF(um), F(w1));
-   SW4G_TRY(launch_status());
    MixedStage ms = base;  // mt = b1 + dt^2/12 R L(b1): predictor form, um = u
    ms.corrector = 0;
    ms.u = CF(b1);
@@ -414,34 +111,14 @@ int EW::adjoint_step_mixed(const MixedStage& base, const void* pfv, const void* 
    ms.beta = 0;
    ms.coef = dt * dt / 12;
    SW4G_TRY(launch_mixed_stage(ms, stream_));
-   adj_v_df_kernel<<<gs_blocks(npts_, 256), 256, 0, stream_>>>(b, pf32, CF(b1), CF(mt), (float)(dt * dt / 12),
-                                                               (float)(dt * dt), F(v1), F(v2));
-   SW4G_TRY(launch_status());
-   GradArgs<float> ga;
-   ga.b = b;
-   ga.f = pf32;
-   ga.v1 = CF(v1);
-   ga.v2 = CF(v2);
-   ga.rho = rho32_;
-   ga.u = CF(u);
-   ga.um = CF(um);
-   ga.up = CF(up);
-   ga.un = CF(un);
-   ga.w1 = CF(w1);
-   ga.gr = gr;
-   ga.gm = gm;
-   ga.gl = gl;
-   ga.c1 = (float)(dt * dt / 12);
-   ga.c2 = (float)(dt * dt);
-   ga.ih2 = (float)(1 / (g_.h * g_.h));
-   ga.beta = (float)beta;
-   ga.lo = 3 * npts_;
-   ga.ed = reinterpret_cast<float*>(adj_edges_);
-   grad_constants(ga);
-   adj_edge_kernel<float><<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
-   SW4G_TRY(launch_status());
-   adj_gradient_kernel<float><<<gs_blocks(npts_, 128), 128, 0, stream_>>>(ga);
-   SW4G_TRY(launch_status());
+   GradDF g = gbase;
+   g.lb1 = CF(b1);
+   g.lmt = CF(mt);
+   g.lup = CF(up);
+   g.lu = CF(u);
+   g.lum = CF(um);
+   g.lun = CF(un);
+   SW4G_TRY(launch_grad_f1_step(g, stream_));
    ms = base;  // b^n = 2 b1 - b2 + dt^2 R L(mt) - beta R SG(b1 - b2): adjoint form
    ms.corrector = 2;
    ms.u = CF(b1);
@@ -494,16 +171,17 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
    int st = alloc(&ck, 2 * (size_t)nseg * lv);
    if (st == kOk) st = alloc(&seg, (size_t)(seglen + 2) * lv);
    if (st == kOk) st = alloc(&pred, (size_t)seglen * lv);
-   if (st == kOk) st = alloc(&work, 9 * lv);  // adjoint work (7) + the forward's final levels (2)
+   if (st == kOk) st = alloc(&work, 7 * lv);  // adjoint work (5) + the forward's final levels (2)
    if (st == kOk) st = alloc(&resd, (size_t)(nsteps + 1) * nval * sizeof(double));
-   if (st == kOk && mixed_) st = alloc(&adj_edges_, 12 * (size_t)npts_ * sizeof(double));
-   // FP64 form: double-float copies of the step's levels (5), the per-point sums (1),
-   // the edge sums (4), the 1-D profile pairs and the two exponent maxima (adj_grad.cu)
+   // the gradient terms (adj_grad.cu): the step's levels in the kernels' number type
+   // (5 levels of pairs, FP64 form, or of floats), the FP64 form's per-point sums (1
+   // level), the edge sums (12 numbers per point), the 1-D profile pairs and the two
+   // exponent maxima
    double *dfw = nullptr, *dfp = nullptr, *dfe = nullptr;
    const int nax[3] = {bd.ie - bd.ib + 1, bd.je - bd.jb + 1, bd.ke - bd.kb + 1};
-   if (st == kOk && !mixed_) st = alloc(&dfw, 10 * lv);
-   if (st == kOk && !mixed_) st = alloc(&dfp, 4 * (size_t)(nax[0] + nax[1] + nax[2]) * sizeof(float2));
-   if (st == kOk && !mixed_) st = alloc(&dfe, sizeof(double));
+   if (st == kOk) st = alloc(&dfw, mixed_ ? 5 * lv : 10 * lv);
+   if (st == kOk) st = alloc(&dfp, 4 * (size_t)(nax[0] + nax[1] + nax[2]) * sizeof(float2));
+   if (st == kOk) st = alloc(&dfe, sizeof(double));
    double* gr_d = g_rho;
    double* gm_d = g_mu;
    double* gl_d = g_la;
@@ -528,7 +206,6 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       if (hs) cudaStreamSynchronize(hs);
       if (gs) cudaStreamSynchronize(gs);
       for (double* p : bufs) cudaFree(p);
-      adj_edges_ = nullptr;
       if (hs) cudaStreamDestroy(hs);
       if (gs) cudaStreamDestroy(gs);
       for (cudaEvent_t e : {ev_s0, ev_g[0], ev_g[1], ev_join, ev_fork, ev_back})
@@ -586,14 +263,8 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
    }
    const double beta = (prof_.used && g_.sg_damping != 0) ? g_.sg_damping : 0.0;
    // the mixed form: double-float levels, FP32 stages and gradient terms
-   ProfT<float> pf32{};
    MixedStage ms;
    if (mixed_) {
-      for (int a = 0; a < 3; a++) {
-         pf32.dc[a] = prof32_[a];
-         pf32.st[a] = prof32_[3 + a];
-         pf32.co[a] = prof32_[6 + a];
-      }
       ms.b = b;
       ms.k1 = 1;
       ms.k2 = g_.nz;
@@ -614,17 +285,31 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
    GradDF gd;
    GradDFProfiles gp{};
    int* emax = reinterpret_cast<int*>(dfe);
-   if (!mixed_) {
+   const double kmu = -(dt * dt / 12) / (144 * g_.h * g_.h);
+   gd.b = b;
+   if (mixed_) {  // FP32 numbers, added to the FP64 gradients every step
+      float* f1 = reinterpret_cast<float*>(dfw);
+      gd.db1 = f1;
+      gd.dmt = f1 + n3;
+      gd.dw1 = f1 + 2 * n3;
+      gd.du = f1 + 3 * n3;
+      gd.dum = f1 + 4 * n3;
+      gd.ed = f1 + 5 * n3;
+      gd.lo = (long long)n3;
+      gd.gm64 = gm_d;
+      gd.gl64 = gl_d;
+      gd.gr64 = gr_d;
+      gd.kmu = kmu;
+   } else {
       float2* f2 = reinterpret_cast<float2*>(dfw);
-      gd.b = b;
       gd.db1 = f2;
       gd.dmt = f2 + n3;
       gd.dw1 = f2 + 2 * n3;
       gd.du = f2 + 3 * n3;
       gd.dum = f2 + 4 * n3;
       gd.am = f2 + 5 * n3;
-      gd.al = gd.am + npts_;
-      gd.ar = gd.al + npts_;
+      gd.al = f2 + 5 * n3 + npts_;
+      gd.ar = f2 + 5 * n3 + 2 * npts_;
       gd.ed = f2 + 6 * n3;
       gd.emax = emax;
       // Each class's bound maps to 2^26..2^28: the largest products (x 1/(s_b s_c) <=
@@ -634,25 +319,24 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       while ((1LL << (marg - 4)) < (long long)nsteps + 1) marg++;
       gd.marg_a = marg - 30;  // the adjoint level is at most (steps) x (largest injection)
       gd.marg_f = 4 - 32;     // w1 = up - 2u + um is at most 4 x the largest level
-      float2* pp = reinterpret_cast<float2*>(dfp);
-      gp.beta = beta;
-      for (int a = 0; a < 3; a++) {
-         gp.n[a] = nax[a];
-         gp.st[a] = dprof_[3 + a];
-         gp.co[a] = dprof_[6 + a];
-         gp.dc[a] = dprof_[a];
-         gp.st24[a] = pp;
-         gp.ist[a] = pp + nax[a];
-         gp.cist[a] = pp + 2 * nax[a];
-         gp.bdc[a] = pp + 3 * nax[a];
-         pp += 4 * nax[a];
-         gd.st24[a] = gp.st24[a];
-         gd.ist[a] = gp.ist[a];
-         gd.cist[a] = gp.cist[a];
-         gd.bdc[a] = gp.bdc[a];
-      }
    }
-   const double kmu = -(dt * dt / 12) / (144 * g_.h * g_.h);
+   float2* pp = reinterpret_cast<float2*>(dfp);
+   gp.beta = beta;
+   for (int a = 0; a < 3; a++) {
+      gp.n[a] = nax[a];
+      gp.st[a] = dprof_[3 + a];
+      gp.co[a] = dprof_[6 + a];
+      gp.dc[a] = dprof_[a];
+      gp.st24[a] = pp;
+      gp.ist[a] = pp + nax[a];
+      gp.cist[a] = pp + 2 * nax[a];
+      gp.bdc[a] = pp + 3 * nax[a];
+      pp += 4 * nax[a];
+      gd.st24[a] = gp.st24[a];
+      gd.ist[a] = gp.ist[a];
+      gd.cist[a] = gp.cist[a];
+      gd.bdc[a] = gp.bdc[a];
+   }
    // Fused steps n0..n1-1 with the level slots pointing into a segment's buffers, so
    // each level lands where the adjoint reads it: u^{n+1} in sq[n - n0 + 2], the
    // predicted level up^n in pq[n - n0] (sq[0], sq[1] hold u^{n0-1}, u^{n0} on
@@ -708,7 +392,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
          SW4G_TRY(steps_into(nn, s1, sq, pq));
       }
       const double t_end = t_;
-      double* fin = work + 7 * n3;  // u^N, u^{N-1}: the recompute overwrites the levels
+      double* fin = work + 5 * n3;  // u^N, u^{N-1}: the recompute overwrites the levels
       SW4G_TRY(cuda_ok(cudaMemcpyAsync(fin, lev_[iu_], lv, cudaMemcpyDeviceToDevice, stream_)));
       SW4G_TRY(cuda_ok(cudaMemcpyAsync(fin + n3, lev_[ium_], lv, cudaMemcpyDeviceToDevice, stream_)));
       // misfit and residuals (host; rows x receivers is small)
@@ -724,11 +408,11 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       }
       *misfit = J;
       SW4G_TRY(cuda_ok(cudaMemcpy(resd, rec.data(), rec.size() * sizeof(double), cudaMemcpyHostToDevice)));
+      SW4G_TRY(launch_grad_df_profiles(gp, stream_));
       if (!mixed_) {  // the adjoint level's shift from its sources; the per-point sums zeroed
          SW4G_TRY(cuda_ok(cudaMemsetAsync(dfe, 0, sizeof(double), stream_)));
          const double* stp[3] = {dprof_[3], dprof_[4], dprof_[5]};
          SW4G_TRY(launch_inj_exp(b, stp, drec_.n, drec_.ijk, resd, nsteps + 1, nval, rho_, emax, stream_));
-         SW4G_TRY(launch_grad_df_profiles(gp, stream_));
          SW4G_TRY(cuda_ok(cudaMemsetAsync(gd.am, 0, 3 * (size_t)npts_ * sizeof(float2), stream_)));
       }
 
@@ -736,10 +420,8 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       double* b2 = work + n3;      // at n+2
       double* bn = work + 2 * n3;  // at n
       double* mt = work + 3 * n3;  // b1 + dt^2/12 R L(b1)
-      double* w1 = work + 4 * n3;  // up - 2u + um (mixed form); the FP64 form's second mt slot
-      double* v1 = work + 5 * n3;  // dt^2/12 W b1
-      double* v2 = work + 6 * n3;  // dt^2 W mt
-      SW4G_TRY(cuda_ok(cudaMemsetAsync(work, 0, 7 * lv, stream_)));  // not fin
+      double* w1 = work + 4 * n3;  // the FP64 form's second mt slot
+      SW4G_TRY(cuda_ok(cudaMemsetAsync(work, 0, 5 * lv, stream_)));  // not fin
       // b^N = W^-1 R g^N
       if (mixed_)
          adj_source_df_kernel<<<blocks_for(drec_.n, 64), 64, 0, stream_>>>(
@@ -780,8 +462,8 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
          const double* res = clocked ? resd : resd + (size_t)nn * nval;
          int status = kOk;
          if (mixed_) {
-            status = adjoint_step_mixed(ms, &pf, &pf32, b, n3, u, um, up, un, b1, b2, bn, mt, w1, v1, v2,
-                                        gr_d, gm_d, gl_d, dt, beta, saved_n, res, clk, nval);
+            status = adjoint_step_mixed(ms, &pf, gd, b, u, um, up, un, b1, b2, bn, mt, dt, beta, saved_n, res,
+                                        clk, nval);
          } else {
             // mt = b1 + dt^2/12 R L(b1): predictor form, um = u; into the slot whose
             // previous reader, the gradient terms two steps later, has finished

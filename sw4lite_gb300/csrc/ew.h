@@ -160,12 +160,10 @@ class EW {
    int piece(int which, int ip, int iq) { return mixed_ ? mixed_piece(which, ip, iq) : fused_piece(which, ip, iq); }
    int ensure_staging();
    int init_topo();
-   int adjoint_step_mixed(const MixedStage& base, const void* pf, const void* pf32, const Box& b,
-                          size_t n3, const double* u, const double* um, const double* up,
-                          const double* un, double* b1, double* b2, double* bn, double* mt,
-                          double* w1, double* v1, double* v2, double* gr, double* gm, double* gl,
-                          double dt, double beta, int nrec, const double* res, const double* clk,
-                          int nval);
+   int adjoint_step_mixed(const MixedStage& base, const void* pf, const GradDF& g, const Box& b,
+                          const double* u, const double* um, const double* up, const double* un, double* b1,
+                          double* b2, double* bn, double* mt, double dt, double beta, int nrec,
+                          const double* res, const double* clk, int nval);
    int curv_pred(int ip);
    int curv_corr(int ip, int iq);
    int curv_bc(double* ucart, double* ucurv);
@@ -232,7 +230,6 @@ class EW {
    bool rec_initial_ = false;  // the initial-data row is still to be written
 
    std::unique_ptr<CurvGrid> cv_;
-   double* adj_edges_ = nullptr;     // gradient(): edge products of the adjoint step
    long long grad_store_bytes_ = -1;  // gradient(): budget for kept segments
 
    double t_ = 0, dt_ = 0;

@@ -329,22 +329,31 @@ long long zcoef_len(const Box& b);
 int launch_zcoef(const Box& b, int nk, bool top, const double* mu, const double* la, double* zc,
                  cudaStream_t s);
 
-// Material gradient of one FP64 adjoint step in double-float arithmetic (adj_grad.cu).
-// Pairs are (hi, lo) float2, 3 components at [c*npts + p]; adjoint levels are scaled
-// by 2^-sA and forward levels by 2^-sF, sA/sF = emax[0/1] - 1023 + marg_a/marg_f.
+// Material gradient of one adjoint step (adj_grad.cu): the FP64 form in double-float
+// arithmetic (pairs (hi, lo) as float2, 3 components at [c*npts + p]; adjoint levels
+// scaled by 2^-sA and forward levels by 2^-sF, sA/sF = emax[0/1] - 1023 +
+// marg_a/marg_f; per-point sums flushed per segment), or the FP32-mixed form in FP32
+// (floats, from the double-float levels lb1 .. lun with lo halves lo further; each
+// step added to gm64, gl64, gr64 with kmu).
 struct GradDF {
    Box b;
    const double *b1 = nullptr, *mt = nullptr, *up = nullptr, *u = nullptr, *um = nullptr,
                 *un = nullptr;
-   float2 *db1 = nullptr, *dmt = nullptr, *dw1 = nullptr, *du = nullptr, *dum = nullptr;
+   const float *lb1 = nullptr, *lmt = nullptr, *lup = nullptr, *lu = nullptr, *lum = nullptr,
+               *lun = nullptr;
+   long long lo = 0;
+   // the step's levels in the kernels' number type: float2 pairs or floats
+   void *db1 = nullptr, *dmt = nullptr, *dw1 = nullptr, *du = nullptr, *dum = nullptr;
    const float2* st24[3] = {};  // 24 st, 1/st, co/st, beta dc per axis
    const float2* ist[3] = {};
    const float2* cist[3] = {};
    const float2* bdc[3] = {};
-   float2 *am = nullptr, *al = nullptr, *ar = nullptr;  // per-point sums (mu, lambda, rho)
-   float2* ed = nullptr;  // edge sums, 12 x npts
+   void *am = nullptr, *al = nullptr, *ar = nullptr;  // per-point sums (mu, lambda, rho), pairs
+   void* ed = nullptr;  // edge sums, 12 x npts
    const int* emax = nullptr;
    int marg_a = 0, marg_f = 0;
+   double *gm64 = nullptr, *gl64 = nullptr, *gr64 = nullptr;  // FP32 form: the gradients
+   double kmu = 0;
 };
 struct GradDFProfiles {
    int n[3];
@@ -357,6 +366,7 @@ int launch_exp_max(const double* x, long long n, int* out, cudaStream_t s);
 int launch_inj_exp(const Box& b, const double* const st[3], int nrec, const int* ijk, const double* res,
                    long long rows, int nval, const double* rho, int* out, cudaStream_t s);
 int launch_grad_df_step(const GradDF& g, cudaStream_t s);
+int launch_grad_f1_step(const GradDF& g, cudaStream_t s);
 // gm += kmu 2^(sA+sF) am, gl likewise, gr += 2^(sA+sF) ar; the sums are zeroed
 int launch_grad_df_flush(const GradDF& g, double kmu, double* gm, double* gl, double* gr, cudaStream_t s);
 
