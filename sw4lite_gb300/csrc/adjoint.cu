@@ -92,46 +92,6 @@ __global__ void adj_source_df_kernel(Box b, Prof f, int nrec, const int* __restr
 
 }  // namespace
 
-// One adjoint step of the mixed form (double-float b, mt and levels): the same
-// sequence as the FP64 step, the gradient terms in FP32 (adj_grad.cu).
-int EW::adjoint_step_mixed(const MixedStage& base, const void* pfv, const GradDF& gbase, const Box& b,
-                           const double* u, const double* um, const double* up, const double* un, double* b1,
-                           double* b2, double* bn, double* mt, double dt, double beta, int nrec,
-                           const double* res, const double* clk, int nval)
-{
-   const Prof& pf = *static_cast<const Prof*>(pfv);
-   auto F = [](double* x) { return reinterpret_cast<float*>(x); };
-   auto CF = [](const double* x) { return reinterpret_cast<const float*>(x); };
-   MixedStage ms = base;  // mt = b1 + dt^2/12 R L(b1): predictor form, um = u
-   ms.corrector = 0;
-   ms.u = CF(b1);
-   ms.um = CF(b1);
-   ms.up = nullptr;
-   ms.out = F(mt);
-   ms.beta = 0;
-   ms.coef = dt * dt / 12;
-   SW4G_TRY(launch_mixed_stage(ms, stream_));
-   GradDF g = gbase;
-   g.lb1 = CF(b1);
-   g.lmt = CF(mt);
-   g.lup = CF(up);
-   g.lu = CF(u);
-   g.lum = CF(um);
-   g.lun = CF(un);
-   SW4G_TRY(launch_grad_f1_step(g, stream_));
-   ms = base;  // b^n = 2 b1 - b2 + dt^2 R L(mt) - beta R SG(b1 - b2): adjoint form
-   ms.corrector = 2;
-   ms.u = CF(b1);
-   ms.um = CF(b2);
-   ms.up = CF(mt);
-   ms.out = F(bn);
-   ms.beta = beta;
-   SW4G_TRY(launch_mixed_stage(ms, stream_));
-   adj_source_df_kernel<<<blocks_for(nrec, 64), 64, 0, stream_>>>(b, pf, nrec, drec_.ijk, res, rho_, F(bn),
-                                                                   clk, nval);
-   return launch_status();
-}
-
 int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, double* misfit,
                  double* g_rho, double* g_mu, double* g_la, bool grad_on_device)
 {
@@ -192,12 +152,11 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       gm_d = gtmp + npts_;
       gl_d = gtmp + 2 * npts_;
    }
-   // FP64 form: a segment's adjoint steps run on two streams forked from the object's
-   // stream, the FP64 stages (the critical path) on one of the highest priority and
-   // the double-float gradient terms of each step on one of the lowest, beside the
-   // next stages (they need the step's mt and nothing after it needs them), so their
-   // CTAs take what the stage kernels leave of each SM.  mt is double-buffered and
-   // events order its reuse.
+   // A segment's adjoint steps run on two streams forked from the object's stream:
+   // the stages (the critical path) on one of the highest priority and the gradient
+   // terms of each step on one of the lowest, beside the next stages (they need the
+   // step's mt and nothing after it needs them), so their CTAs take what the stage
+   // kernels leave of each SM.  mt is double-buffered and events order its reuse.
    cudaStream_t hs = nullptr, gs = nullptr;
    cudaEvent_t ev_s0 = nullptr, ev_g[2] = {nullptr, nullptr}, ev_join = nullptr, ev_fork = nullptr,
                ev_back = nullptr;
@@ -211,7 +170,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       for (cudaEvent_t e : {ev_s0, ev_g[0], ev_g[1], ev_join, ev_fork, ev_back})
          if (e) cudaEventDestroy(e);
    };
-   if (st == kOk && !mixed_) {
+   if (st == kOk) {
       int lo = 0, hi = 0;
       st = cuda_ok(cudaDeviceGetStreamPriorityRange(&lo, &hi));
       if (st == kOk) st = cuda_ok(cudaStreamCreateWithPriority(&hs, cudaStreamNonBlocking, hi));
@@ -219,7 +178,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       for (cudaEvent_t* e : {&ev_s0, &ev_g[0], &ev_g[1], &ev_join, &ev_fork, &ev_back})
          if (st == kOk) st = cuda_ok(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
    }
-   cudaStream_t sa = mixed_ ? stream_ : hs;  // the adjoint steps' stages
+   cudaStream_t sa = hs;  // the adjoint steps' stages
    if (st != kOk) {
       cleanup();
       return st;
@@ -461,9 +420,45 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
          const double* clk = clocked ? dclock_ : nullptr;
          const double* res = clocked ? resd : resd + (size_t)nn * nval;
          int status = kOk;
-         if (mixed_) {
-            status = adjoint_step_mixed(ms, &pf, gd, b, u, um, up, un, b1, b2, bn, mt, dt, beta, saved_n, res,
-                                        clk, nval);
+         if (mixed_) {  // double-float b, mt and levels; FP32 stages and gradient terms
+            auto CF = [](const double* x) { return reinterpret_cast<const float*>(x); };
+            double* mtb = (nn & 1) ? w1 : mt;
+            if (wait_g) status = cuda_ok(cudaStreamWaitEvent(sa, ev_g[nn & 1], 0));
+            MixedStage m = ms;  // mt = b1 + dt^2/12 R L(b1): predictor form, um = u
+            m.corrector = 0;
+            m.u = CF(b1);
+            m.um = CF(b1);
+            m.up = nullptr;
+            m.out = F(mtb);
+            m.beta = 0;
+            m.coef = dt * dt / 12;
+            if (status == kOk) status = launch_mixed_stage(m, sa);
+            if (status == kOk) status = cuda_ok(cudaEventRecord(ev_s0, sa));
+            if (status == kOk) status = cuda_ok(cudaStreamWaitEvent(gs, ev_s0, 0));
+            if (status == kOk) {
+               GradDF g = gd;
+               g.lb1 = CF(b1);
+               g.lmt = CF(mtb);
+               g.lup = CF(up);
+               g.lu = CF(u);
+               g.lum = CF(um);
+               g.lun = CF(un);
+               status = launch_grad_f1_step(g, gs);
+            }
+            if (status == kOk) status = cuda_ok(cudaEventRecord(ev_g[nn & 1], gs));
+            m = ms;  // b^n = 2 b1 - b2 + dt^2 R L(mt) - beta R SG(b1 - b2): adjoint form
+            m.corrector = 2;
+            m.u = CF(b1);
+            m.um = CF(b2);
+            m.up = CF(mtb);
+            m.out = F(bn);
+            m.beta = beta;
+            if (status == kOk) status = launch_mixed_stage(m, sa);
+            if (status == kOk) {
+               adj_source_df_kernel<<<blocks_for(saved_n, 64), 64, 0, sa>>>(b, pf, saved_n, drec_.ijk, res, rho_,
+                                                                            F(bn), clk, nval);
+               status = launch_status();
+            }
          } else {
             // mt = b1 + dt^2/12 R L(b1): predictor form, um = u; into the slot whose
             // previous reader, the gradient terms two steps later, has finished
@@ -519,8 +514,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       };
       // the segment's double-float sums into the FP64 gradients
       auto flush = [&]() -> int {
-         if (mixed_) return kOk;
-         SW4G_TRY(launch_grad_df_flush(gd, kmu, gm_d, gl_d, gr_d, gs));
+         if (!mixed_) SW4G_TRY(launch_grad_df_flush(gd, kmu, gm_d, gl_d, gr_d, gs));
          SW4G_TRY(cuda_ok(cudaEventRecord(ev_join, gs)));
          SW4G_TRY(cuda_ok(cudaStreamWaitEvent(hs, ev_join, 0)));
          SW4G_TRY(cuda_ok(cudaEventRecord(ev_back, hs)));
@@ -528,7 +522,6 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       };
       // a segment's adjoint steps start after everything before them on the object's stream
       auto fork = [&]() -> int {
-         if (mixed_) return kOk;
          SW4G_TRY(cuda_ok(cudaEventRecord(ev_fork, stream_)));
          return cuda_ok(cudaStreamWaitEvent(hs, ev_fork, 0));
       };

@@ -160,10 +160,6 @@ class EW {
    int piece(int which, int ip, int iq) { return mixed_ ? mixed_piece(which, ip, iq) : fused_piece(which, ip, iq); }
    int ensure_staging();
    int init_topo();
-   int adjoint_step_mixed(const MixedStage& base, const void* pf, const GradDF& g, const Box& b,
-                          const double* u, const double* um, const double* up, const double* un, double* b1,
-                          double* b2, double* bn, double* mt, double dt, double beta, int nrec,
-                          const double* res, const double* clk, int nval);
    int curv_pred(int ip);
    int curv_corr(int ip, int iq);
    int curv_bc(double* ucart, double* ucurv);
