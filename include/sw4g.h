@@ -29,7 +29,8 @@ typedef enum {
    SW4G_CUDA_ERROR = 2,
    SW4G_NAN_DETECTED = 3,
    SW4G_NOT_SUPPORTED = 4,
-   SW4G_TIMEOUT = 5
+   SW4G_TIMEOUT = 5,
+   SW4G_IO_ERROR = 6
 } sw4g_status;
 
 /* Library version string. */
@@ -312,6 +313,16 @@ int sw4g_ew_gradient(sw4g_ew* ew, int nsteps, int checkpoint_every, const double
  * default): all free device memory but a reserve of max(4 GiB, 1/32 of the device);
  * 0: only the last segment. */
 int sw4g_ew_set_gradient_memory(sw4g_ew* ew, long long max_bytes);
+
+/* Restart files in the reference's checkpoint format (CheckPoint::write_checkpoint,
+ * src/CheckPoint.C:251-370, and read_checkpoint, :373-470): precision 8, the number of
+ * grids, the current level's time, the cycle, per grid {1, nx, 1, ny, 1, nz}, then per
+ * grid the previous and the current level at the interior points, components
+ * fastest.  Reading checks the grids, sets both levels, fills their ghost points from
+ * the boundary conditions (as src/EW.C:2403-2415) and the time; a restarted run
+ * continues bit for bit.  SW4G_IO_ERROR on a file error. */
+int sw4g_ew_write_checkpoint(sw4g_ew* ew, const char* path, int cycle);
+int sw4g_ew_read_checkpoint(sw4g_ew* ew, const char* path, int* cycle);
 
 /* Topography (replaces the reference's topography + curvilinear grid set-up,
  * src/EW.C:540-720 (deck), 2018-2046 (dimensions), 6164 (generate_grid), 6229

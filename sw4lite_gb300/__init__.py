@@ -106,6 +106,8 @@ _SIGS = {
     "sw4g_ew_time": ([_VP], C.c_double),
     "sw4g_ew_set_graphs": ([_VP, C.c_int], C.c_int),
     "sw4g_ew_set_gradient_memory": ([_VP, C.c_longlong], C.c_int),
+    "sw4g_ew_write_checkpoint": ([_VP, C.c_char_p, C.c_int], C.c_int),
+    "sw4g_ew_read_checkpoint": ([_VP, C.c_char_p, _I], C.c_int),
     "sw4g_discretize_source_topo": ([_VP, _VP, C.c_int, _D, _VP, C.c_int, _I, _D, _I, _I, _D, _I], C.c_int),
     "sw4g_ew_grid_point_sources": ([_VP, C.c_int, C.c_int, _I, _D, _I], C.c_int),
     "sw4g_ew_set_fields": ([_VP, _VP, _VP, C.c_int], C.c_int),
@@ -317,6 +319,16 @@ class EW:
         (their recompute is skipped): < 0 all free memory but a reserve, 0 none
         beyond the last segment."""
         check(lib().sw4g_ew_set_gradient_memory(self._h, int(max_bytes)), "set_gradient_memory")
+
+    def write_checkpoint(self, path, cycle):
+        """Both levels and the time in the reference's restart-file format."""
+        check(lib().sw4g_ew_write_checkpoint(self._h, os.fsencode(path), int(cycle)), "write_checkpoint")
+
+    def read_checkpoint(self, path):
+        """Restart from a file in the reference's format; returns its cycle."""
+        cyc = C.c_int()
+        check(lib().sw4g_ew_read_checkpoint(self._h, os.fsencode(path), C.byref(cyc)), "read_checkpoint")
+        return cyc.value
 
     def compute_time_step(self, cfl, tmax):
         dt = C.c_double()

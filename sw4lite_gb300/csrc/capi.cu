@@ -491,6 +491,18 @@ int sw4g_ew_gradient(sw4g_ew* ew, int nsteps, int checkpoint_every, const double
                              grad_rho, grad_mu, grad_lambda, grad_on_device != 0);
 }
 
+int sw4g_ew_write_checkpoint(sw4g_ew* ew, const char* path, int cycle)
+{
+   if (!ew) return SW4G_BAD_ARGUMENT;
+   return ew->impl->write_checkpoint(path, cycle);
+}
+
+int sw4g_ew_read_checkpoint(sw4g_ew* ew, const char* path, int* cycle)
+{
+   if (!ew) return SW4G_BAD_ARGUMENT;
+   return ew->impl->read_checkpoint(path, cycle);
+}
+
 int sw4g_ew_set_gradient_memory(sw4g_ew* ew, long long max_bytes)
 {
    if (!ew) return SW4G_BAD_ARGUMENT;

@@ -84,6 +84,7 @@ enum Status : int {
    kNanDetected = 3,
    kNotSupported = 4,
    kTimeout = 5,
+   kIoError = 6,
 };
 
 // Returns from the calling function with the status of expr unless it is kOk.

@@ -110,6 +110,10 @@ class EW {
    // Dirichlet / supergrid sides only.  The object ends after the forward run.
    int gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, double* misfit,
                 double* g_rho, double* g_mu, double* g_la, bool grad_on_device);
+   // Restart files in the reference's checkpoint format (checkpoint.cu); read sets
+   // both levels, their ghost points and the time.
+   int write_checkpoint(const char* path, int cycle);
+   int read_checkpoint(const char* path, int* cycle);
    // Device memory gradient() may add for segments kept from its forward run (whose
    // recompute the backward sweep then skips): < 0 all free memory but a reserve
    // (the default), 0 none beyond the last segment, else at most this many bytes.
