@@ -275,6 +275,13 @@ int sw4g_ew_add_grid_point_sources(sw4g_ew* ew, int n, const int* ijk, const dou
                                    const double* freq, const double* t0, const int* kind);
 int sw4g_ew_clear_sources(sw4g_ew* ew);
 int sw4g_ew_num_grid_point_sources(const sw4g_ew* ew);
+/* Where sw4g_ew_add_source computes the grid-point sources (the host loop of
+ * Source::set_grid_point_sources4, src/Source.C:1074-1530): on the host (0, the
+ * default), or on the device (1), one CTA per source for the whole batch before the
+ * next step, grouped by grid point on the device; the same bits either way.  The
+ * device path takes the Cartesian grid alone (SW4G_NOT_SUPPORTED with topography or
+ * with sources from sw4g_ew_add_grid_point_sources). */
+int sw4g_ew_set_source_discretization(sw4g_ew* ew, int on_device);
 int sw4g_ew_set_time_step(sw4g_ew* ew, double dt, double t0);
 /* dt from the CFL number, adjusted to end at tmax (EW::computeDT, src/EW.C:5041) */
 int sw4g_ew_compute_time_step(sw4g_ew* ew, double cfl, double tmax, double* dt, int* nsteps);

@@ -106,6 +106,7 @@ _SIGS = {
     "sw4g_ew_time": ([_VP], C.c_double),
     "sw4g_ew_set_graphs": ([_VP, C.c_int], C.c_int),
     "sw4g_ew_set_gradient_memory": ([_VP, C.c_longlong], C.c_int),
+    "sw4g_ew_set_source_discretization": ([_VP, C.c_int], C.c_int),
     "sw4g_ew_write_checkpoint": ([_VP, C.c_char_p, C.c_int], C.c_int),
     "sw4g_ew_read_checkpoint": ([_VP, C.c_char_p, _I], C.c_int),
     "sw4g_discretize_source_topo": ([_VP, _VP, C.c_int, _D, _VP, C.c_int, _I, _D, _I, _I, _D, _I], C.c_int),
@@ -313,6 +314,12 @@ class EW:
     def set_graphs(self, on=True):
         """Replay the fused time loop (and the gradient's loops) as CUDA graphs."""
         check(lib().sw4g_ew_set_graphs(self._h, int(bool(on))), "set_graphs")
+
+    def set_source_discretization(self, on_device=True):
+        """Compute add_source's grid-point sources on the device (the whole batch,
+        the same bits as the host path); Cartesian grid only."""
+        check(lib().sw4g_ew_set_source_discretization(self._h, int(bool(on_device))),
+              "set_source_discretization")
 
     def set_gradient_memory(self, max_bytes):
         """Device memory gradient() may add for segments kept from its forward run

@@ -25,6 +25,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # which turns a 1-ulp contraction difference into a 1e-12 relative one.
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr", f"-I{INCLUDE}"]
+# Device code that must reproduce host set-up values bit for bit: no FMA contraction
+# there either (the source weights, srcdisc.cu).
+FILE_FLAGS = {"srcdisc.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:
@@ -56,7 +59,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     def compile_one(src: Path) -> Path:
         obj = OUT / (src.name + ".o")
         lang = ["-x", "cu"] if src.suffix == ".cu" else []
-        cmd = [cc, *ARCH, *FLAGS, *lang, "-c", str(src), "-o", str(obj)]
+        cmd = [cc, *ARCH, *FLAGS, *FILE_FLAGS.get(src.name, []), *lang, "-c", str(src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stdout}\n{r.stderr}")

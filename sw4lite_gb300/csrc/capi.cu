@@ -603,6 +603,11 @@ int sw4g_ew_get_records(const sw4g_ew* ew, double* out, int on_device)
    return ew ? ew->impl->get_records(out, on_device != 0) : SW4G_BAD_ARGUMENT;
 }
 
+int sw4g_ew_set_source_discretization(sw4g_ew* ew, int on_device)
+{
+   return ew ? ew->impl->set_source_discretization(on_device != 0) : SW4G_BAD_ARGUMENT;
+}
+
 int sw4g_ew_num_grid_point_sources(const sw4g_ew* ew)
 {
    return ew ? ew->impl->num_grid_point_sources() : -1;

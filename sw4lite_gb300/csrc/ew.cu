@@ -172,6 +172,11 @@ int EW::add_source(const SourceSpec& s)
 {
    if (!ready_) return kBadArgument;
    if (s.kind < 0 || s.kind > 3 || !(s.freq > 0)) return kBadArgument;
+   specs_.push_back(s);
+   if (dev_src_) {  // discretised with the whole batch before the next step
+      src_dirty_ = true;
+      return kOk;
+   }
    if (cv_) {
       // two grids: the source may go to either, or straddle the interface
       const CurvSourceGrid cs = curv_source_grid();
@@ -187,6 +192,8 @@ int EW::add_grid_point_sources(int n, const int* ijk, const double* amp, const d
                                const double* t0, const int* kind)
 {
    if (!ready_ || n < 0 || (n > 0 && (!ijk || !amp || !freq || !t0 || !kind))) return kBadArgument;
+   if (dev_src_) return kNotSupported;
+   raw_src_ += n;
    for (int s = 0; s < n; s++) {
       GridPointSource p;
       p.i = ijk[3 * s];
@@ -209,8 +216,31 @@ int EW::clear_sources()
 {
    hsrc_.clear();
    hsrc_curv_.clear();
+   specs_.clear();
+   raw_src_ = 0;
    src_dirty_ = true;
    return kOk;
+}
+
+int EW::set_source_discretization(bool on_device)
+{
+   if (!ready_) return kBadArgument;
+   if (on_device && (cv_ || raw_src_ > 0)) return kNotSupported;
+   if (on_device == dev_src_) return kOk;
+   dev_src_ = on_device;
+   if (!on_device) {  // the host list from the sources added meanwhile
+      hsrc_.clear();
+      for (const SourceSpec& s : specs_) discretize_source(g_, onesided_, s, hsrc_);
+   }
+   src_dirty_ = true;
+   return kOk;
+}
+
+int EW::num_grid_point_sources() const
+{
+   if (!dev_src_) return (int)hsrc_.size();
+   std::vector<GridPointSource> v;
+   return grid_point_sources(0, &v) == kOk ? (int)v.size() : -1;
 }
 
 namespace {
@@ -271,6 +301,9 @@ int EW::upload_sources()
    drop_graphs();  // the graphs hold the old source list
    if (dsrc_mem_ || dsrc_curv_mem_) SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
    src_dirty_ = false;
+   if (dev_src_)
+      return launch_discretize_sources(g_, onesided_, (int)specs_.size(), specs_.data(), &dsrc_, &dsrc_mem_,
+                                       stream_);
    SW4G_TRY(pack_sources(hsrc_, dsrc_, dsrc_mem_));
    return pack_sources(hsrc_curv_, dsrc_curv_, dsrc_curv_mem_);
 }
@@ -278,7 +311,35 @@ int EW::upload_sources()
 int EW::grid_point_sources(int grid, std::vector<GridPointSource>* out) const
 {
    if (grid < 0 || grid >= num_grids() || !out) return kBadArgument;
-   *out = grid == 0 ? hsrc_ : hsrc_curv_;
+   if (!dev_src_) {
+      *out = grid == 0 ? hsrc_ : hsrc_curv_;
+      return kOk;
+   }
+   // the device list, grouped by grid point; discretised first if it is not yet (a
+   // cache refresh: the object's observable state does not change)
+   EW* self = const_cast<EW*>(this);
+   SW4G_TRY(self->upload_sources());
+   const int ns = dsrc_.nsources;
+   out->assign(ns, GridPointSource{});
+   if (ns == 0) return kOk;
+   std::vector<int> ijk(3 * (size_t)ns), kind(ns);
+   std::vector<double> amp(3 * (size_t)ns), freq(ns), t0(ns);
+   SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
+   SW4G_TRY(cuda_ok(cudaMemcpy(ijk.data(), dsrc_.ijk, ijk.size() * sizeof(int), cudaMemcpyDeviceToHost)));
+   SW4G_TRY(cuda_ok(cudaMemcpy(kind.data(), dsrc_.kind, kind.size() * sizeof(int), cudaMemcpyDeviceToHost)));
+   SW4G_TRY(cuda_ok(cudaMemcpy(amp.data(), dsrc_.amp, amp.size() * sizeof(double), cudaMemcpyDeviceToHost)));
+   SW4G_TRY(cuda_ok(cudaMemcpy(freq.data(), dsrc_.freq, freq.size() * sizeof(double), cudaMemcpyDeviceToHost)));
+   SW4G_TRY(cuda_ok(cudaMemcpy(t0.data(), dsrc_.t0, t0.size() * sizeof(double), cudaMemcpyDeviceToHost)));
+   for (int s = 0; s < ns; s++) {
+      GridPointSource& p = (*out)[s];
+      p.i = ijk[3 * s];
+      p.j = ijk[3 * s + 1];
+      p.k = ijk[3 * s + 2];
+      for (int c = 0; c < 3; c++) p.amp[c] = amp[3 * s + c];
+      p.freq = freq[s];
+      p.t0 = t0[s];
+      p.kind = kind[s];
+   }
    return kOk;
 }
 

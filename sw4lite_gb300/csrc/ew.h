@@ -79,7 +79,11 @@ class EW {
    int add_grid_point_sources(int n, const int* ijk, const double* amp, const double* freq,
                               const double* t0, const int* kind);
    int clear_sources();
-   int num_grid_point_sources() const { return (int)hsrc_.size(); }
+   // Where add_source's grid-point sources are computed: on the host (the default)
+   // or on the device, the whole batch at the next step (srcdisc.cu; the same bits).
+   // The device path takes the Cartesian grid alone and no raw grid-point sources.
+   int set_source_discretization(bool on_device);
+   int num_grid_point_sources() const;
    // the discretised grid-point sources of grid 0 (Cartesian) or 1 (curvilinear)
    int grid_point_sources(int grid, std::vector<GridPointSource>* out) const;
    // Time step: explicit dt, or computed from the CFL number and an end time.
@@ -216,6 +220,9 @@ class EW {
    long long slab_len_ = 0;
 
    std::vector<GridPointSource> hsrc_;
+   std::vector<SourceSpec> specs_;  // the sources added, in order
+   int raw_src_ = 0;                // grid-point sources added directly
+   bool dev_src_ = false;           // discretise on the device
    std::vector<GridPointSource> hsrc_curv_;  // sources of the curvilinear grid
    SourceSet dsrc_curv_{};
    void* dsrc_curv_mem_ = nullptr;

@@ -366,6 +366,13 @@ int launch_exp_max(const double* x, long long n, int* out, cudaStream_t s);
 int launch_inj_exp(const Box& b, const double* const st[3], int nrec, const int* ijk, const double* res,
                    long long rows, int nval, const double* rho, int* out, cudaStream_t s);
 int launch_grad_df_step(const GradDF& g, cudaStream_t s);
+// The grid-point sources of nsrc sources on the Cartesian grid (srcdisc.cu): one
+// device block *mem (freed and replaced) holding the grouped SourceSet.  Synchronises
+// the stream (the point count sizes the forcing launches).
+struct GridSpec;
+struct SourceSpec;
+int launch_discretize_sources(const GridSpec& g, const int onesided[6], int nsrc, const SourceSpec* host_specs,
+                              SourceSet* out, void** mem, cudaStream_t s);
 int launch_grad_f1_step(const GradDF& g, cudaStream_t s);
 // gm += kmu 2^(sA+sF) am, gl likewise, gr += 2^(sA+sF) ar; the sums are zeroed
 int launch_grad_df_flush(const GradDF& g, double kmu, double* gm, double* gl, double* gr, cudaStream_t s);

@@ -1,6 +1,8 @@
 // Host-side set-up for one Cartesian grid; see setup.h.
 #include "setup.h"
 
+#include "source_weights.h"
+
 #include <algorithm>
 #include <cmath>
 #include <tuple>
@@ -158,57 +160,6 @@ double cfl_time_step(const GridSpec& g, const double* rho, const double* mu, con
 
 namespace {
 
-// 6-point delta weights at offsets -2..3 for a source at fractional position a
-// (moments 0..4 exact), src/Source.C:553-584.
-void delta_weights(double a, double w[6])
-{
-   const double a2 = a * a, a3 = a2 * a, a4 = a3 * a, a5 = a4 * a;
-   const double p5 = a5 * (5.0 / 3 - 7.0 / 24 * a - 17 / 12.0 * a2 + 1.125 * a3 - 0.25 * a4);
-   w[0] = 1.0 / 24 * (2 * a - a2 - 2 * a3 - 19 * a4) + p5;
-   w[1] = 1.0 / 6 * (-4 * a + 4 * a2 + a3) + 4 * a4 - 5 * p5;
-   w[2] = 1 - 1.25 * a2 - 97.0 / 12 * a4 + 10 * p5;
-   w[3] = 1.0 / 6 * (4 * a + 4 * a2 - a3 + 49 * a4) - 10 * p5;
-   w[4] = 1.0 / 24 * (-2 * a - a2 + 2 * a3) - 4.125 * a4 + 5 * p5;
-   w[5] = 5.0 / 6 * a4 - p5;
-}
-
-// 6-point delta' weights, src/Source.C:587-619.
-void ddelta_weights(double a, double w[6])
-{
-   const double a2 = a * a, a3 = a2 * a, a4 = a3 * a;
-   const double p5 = a4 * (-25.0 / 12 - 0.75 * a + 59.0 / 12 * a2 - 4 * a3 + a4);
-   w[0] = 1.0 / 12 * (-1 + a + 3 * a2 + 8 * a3) + p5;
-   w[1] = 2.0 / 3 * (1 - 2 * a) - 0.5 * a2 - 3.5 * a3 - 5 * p5;
-   w[2] = 2.5 * a + 22.0 / 3 * a3 + 10 * p5;
-   w[3] = 2.0 / 3 * (-1 - 2 * a) + 0.5 * a2 - 23.0 / 3 * a3 - 10 * p5;
-   w[4] = (1 + a) / 12 - 0.25 * a2 + 4 * a3 + 5 * p5;
-   w[5] = -5.0 / 6 * a3 - p5;
-}
-
-// Five-point variants used next to the free surface when the source lies above
-// the third grid plane (src/Source.C:622-679).
-void delta_weights_low(double a, double w[6])
-{
-   const double a2 = a * a, a3 = a2 * a, a4 = a3 * a;
-   w[0] = (2 * a - a2 - 2 * a3 + a4) / 24;
-   w[1] = (-4 * a + 4 * a2 + a3 - a4) / 6;
-   w[2] = 1 - 1.25 * a2 + 0.25 * a4;
-   w[3] = (4 * a + 4 * a2 - a3 - a4) / 6;
-   w[4] = (-2 * a - a2 + 2 * a3 + a4) / 24;
-   w[5] = 0;
-}
-
-void ddelta_weights_low(double a, double w[6])
-{
-   const double a2 = a * a, a3 = a2 * a;
-   w[0] = (-1 + a + 3 * a2 - 2 * a3) / 12;
-   w[1] = (2 - 4 * a - 1.5 * a2 + 2 * a3) / 3;
-   w[2] = 2.5 * a - a3;
-   w[3] = (-2 - 4 * a + 1.5 * a2 + 2 * a3) / 3;
-   w[4] = (1 + a - 3 * a2 - 2 * a3) / 12;
-   w[5] = 0;
-}
-
 // 8-point interpolation weights at offsets -3..4 and their derivative, for the
 // topography and its tangential derivatives at a source (src/Source.C:682-720; the
 // same polynomials interpolate the topography, src/EW.C:5671-5690).
@@ -298,14 +249,22 @@ void metric_at_source(const CurvSourceGrid& c, double h, double q, double r, dou
 void discretize_source(const GridSpec& g, const int onesided[6], const SourceSpec& s,
                        std::vector<GridPointSource>& out)
 {
-   std::vector<GridPointSource> none;
-   discretize_source_topo(g, onesided, nullptr, s, out, none);
+   CartStencil c;
+   cart_stencil(g, onesided[4] != 0, onesided[5] != 0, s, c);
+   for (int t = 0; t < 216; t++) {
+      GridPointSource p;
+      if (cart_entry(g, c, s, t, p)) out.push_back(p);
+   }
 }
 
 int discretize_source_topo(const GridSpec& g, const int onesided[6], const CurvSourceGrid* cv,
                            const SourceSpec& s, std::vector<GridPointSource>& cart,
                            std::vector<GridPointSource>& curv)
 {
+   if (!cv) {  // one Cartesian grid (source_weights.h, shared with the device path)
+      discretize_source(g, onesided, s, cart);
+      return 0;
+   }
    const double h = g.h;
    const int Ni = g.nx, Nj = g.ny;
    // the grid of the source (src/EW.C:5149-5213): the curvilinear grid at or above
