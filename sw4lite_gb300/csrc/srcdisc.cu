@@ -57,8 +57,8 @@ __global__ void heads_kernel(int n, const unsigned long long* __restrict__ keys,
    if (valid && (q + 1 == n || keys[q + 1] == kNone)) *nvalid = q + 1;
 }
 
-// the SourceSet arrays from the sorted entries (cap = the capacity of each array)
-__global__ void gather_kernel(int n, int cap, const unsigned long long* __restrict__ keys,
+// the SourceSet arrays from the sorted entries
+__global__ void gather_kernel(int n, const unsigned long long* __restrict__ keys,
                               const unsigned* __restrict__ vals, const int* __restrict__ head,
                               const int* __restrict__ pidx, const GridPointSource* __restrict__ ent,
                               int* __restrict__ start, int* __restrict__ ijk, int* __restrict__ kind,
@@ -78,7 +78,6 @@ __global__ void gather_kernel(int n, int cap, const unsigned long long* __restri
    t0[q] = p.t0;
    if (head[q]) start[pidx[q]] = q;
    if (q + 1 == nv) start[pidx[q] + head[q]] = nv;  // start[np] = number of sources
-   (void)cap;
 }
 
 size_t align8(size_t b) { return (b + 7) / 8 * 8; }
@@ -151,8 +150,8 @@ int launch_discretize_sources(const GridSpec& g, const int onesided[6], int nsrc
    }
    if (st == kOk) st = cuda_ok(cub::DeviceScan::ExclusiveSum(at(o_scan), scan_bytes, head, pidx, n, s));
    if (st == kOk) {
-      gather_kernel<<<blocks_for(n, 256), 256, 0, s>>>(n, n, k1, v1, head, pidx, ent, start, ijk, kind, amp,
-                                                       freq, t0, nv);
+      gather_kernel<<<blocks_for(n, 256), 256, 0, s>>>(n, k1, v1, head, pidx, ent, start, ijk, kind, amp, freq,
+                                                       t0, nv);
       st = launch_status();
    }
    // the counts for the forcing launches: sources and grid points
