@@ -58,8 +58,7 @@ __global__ void heads_kernel(int n, const unsigned long long* __restrict__ keys,
 }
 
 // the SourceSet arrays from the sorted entries
-__global__ void gather_kernel(int n, const unsigned long long* __restrict__ keys,
-                              const unsigned* __restrict__ vals, const int* __restrict__ head,
+__global__ void gather_kernel(int n, const unsigned* __restrict__ vals, const int* __restrict__ head,
                               const int* __restrict__ pidx, const GridPointSource* __restrict__ ent,
                               int* __restrict__ start, int* __restrict__ ijk, int* __restrict__ kind,
                               double* __restrict__ amp, double* __restrict__ freq, double* __restrict__ t0,
@@ -150,8 +149,8 @@ int launch_discretize_sources(const GridSpec& g, const int onesided[6], int nsrc
    }
    if (st == kOk) st = cuda_ok(cub::DeviceScan::ExclusiveSum(at(o_scan), scan_bytes, head, pidx, n, s));
    if (st == kOk) {
-      gather_kernel<<<blocks_for(n, 256), 256, 0, s>>>(n, k1, v1, head, pidx, ent, start, ijk, kind, amp, freq,
-                                                       t0, nv);
+      gather_kernel<<<blocks_for(n, 256), 256, 0, s>>>(n, v1, head, pidx, ent, start, ijk, kind, amp, freq, t0,
+                                                       nv);
       st = launch_status();
    }
    // the counts for the forcing launches: sources and grid points
