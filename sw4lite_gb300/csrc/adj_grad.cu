@@ -345,8 +345,8 @@ __device__ __forceinline__ void edges_body(const GradDF& g, long long n, int pq,
          }
          const V e1 = df_mul(df_diff(x1, x0), df_diff(y1, y0));
          const V e2 = df_mul(df_diff(x2, x0), df_diff(y2, y0));
-         s1 = df_add(s1, e1);
-         s2 = df_add(s2, e2);
+         s1 = df_addf(s1, e1);
+         s2 = df_addf(s2, e2);
          if (c == a) {
             a1 = e1;
             a2 = e2;
@@ -462,8 +462,8 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
       }
       const V qq = df_mul(df_mul(N::ofp(__ldg(g.st24[a] + oa)), N::ofp(__ldg(g.ist[a1] + o1))),
                            N::ofp(__ldg(g.ist[a2] + o2)));
-      gm = df_add(gm, df_mul(qq, T[0]));
-      gl = df_add(gl, df_mul(qq, T[1]));
+      gm = df_addf(gm, df_mul(qq, T[0]));
+      gl = df_addf(gl, df_mul(qq, T[1]));
    }
    // pair 0: (mt, u) with weight 12 (c2 = 12 c1) and the damping term; pair 1: (b1, w1)
 #pragma unroll 1
@@ -515,12 +515,12 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
                const V d2u = df_addf(df_addf(d0, d2), df_pow2(d1, -2.f));
                const V d2b = df_addf(df_addf(N::of(__ldg(b1 + p - sd)), N::of(__ldg(b1 + p + sd))),
                                       df_pow2(N::of(__ldg(b1 + p)), -2.f));
-               ds = df_add(ds, df_mul(d2u, d2b));
+               ds = df_addf(ds, df_mul(d2u, d2b));
             }
          }
          if (damp) {
             const V cc = df_mul(N::ofp(__ldg(g.cist[a1] + o1)), N::ofp(__ldg(g.cist[a2] + o2)));
-            gr = df_add(gr, df_neg(df_mul(df_mul(N::ofp(bd), cc), ds)));
+            gr = df_addf(gr, df_neg(df_mul(df_mul(N::ofp(bd), cc), ds)));
          }
       }
       // mixed terms, grouped by the axis t3 that neither derivative takes:
@@ -534,8 +534,8 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
          const V mm = df_addf(df_mul(W_(a2, a1), A_(a1, a2)), df_mul(W_(a1, a2), A_(a2, a1)));
          const int ot = t3 == 0 ? off[0] : t3 == 1 ? off[1] : off[2];
          const V f = df_scale(N::ofp(__ldg(g.ist[t3] + ot)), wt);
-         gm = df_add(gm, df_mul(f, mm));
-         gl = df_add(gl, df_mul(f, ml));
+         gm = df_addf(gm, df_mul(f, mm));
+         gl = df_addf(gl, df_mul(f, ml));
       }
    }
    if constexpr (sizeof(V) == sizeof(DF)) {  // per-segment double-float sums
