@@ -175,34 +175,35 @@ __device__ __forceinline__ void shell_update(const DFField& out, const DFField& 
    out.h[x + out.lo] = ol;
 }
 
+// The two-point shell of the array box around the centred rows: the two k-planes at
+// each end (whole planes), the two j-rows at each end of the other planes, and the two
+// i-points at each end of the remaining rows.  32-bit index arithmetic (the shell has
+// O(N^2) points); on the i-faces four consecutive threads take the four shell points of
+// one row, two adjacent pairs, so a warp's loads touch 16 sectors rather than 32.
 template <class Field>
 __global__ void ghost_shell_kernel(Box b, int corrector, Field out, Field u, Field um, Field up)
 {
-   const long long ni = b.ni, nj = b.je - b.jb + 1, nk = b.ke - b.kb + 1;
-   const long long nA = 4 * ni * nj, nB = 4 * ni * (nk - 4), nC = 4 * (nj - 4) * (nk - 4);
-   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nA + nB + nC;
-        q += (long long)gridDim.x * blockDim.x) {
+   const int ni = (int)b.ni, nj = b.je - b.jb + 1, nk = b.ke - b.kb + 1;
+   const int nA = 4 * ni * nj, nB = 4 * ni * (nk - 4), nC = 4 * (nj - 4) * (nk - 4);
+   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nA + nB + nC; q += gridDim.x * blockDim.x) {
       int i, j, k;
       if (q < nA) {
-         const int s = (int)(q / (ni * nj));
-         const long long r = q % (ni * nj);
+         const int s = q / (ni * nj), r = q - s * ni * nj;
          k = s < 2 ? b.kb + s : b.ke - (3 - s);
-         j = b.jb + (int)(r / ni);
-         i = b.ib + (int)(r % ni);
+         j = b.jb + r / ni;
+         i = b.ib + r % ni;
       } else if (q < nA + nB) {
-         const long long r0 = q - nA;
-         const int s = (int)(r0 / (ni * (nk - 4)));
-         const long long r = r0 % (ni * (nk - 4));
+         const int r0 = q - nA;
+         const int s = r0 / (ni * (nk - 4)), r = r0 - s * ni * (nk - 4);
          j = s < 2 ? b.jb + s : b.je - (3 - s);
-         k = b.kb + 2 + (int)(r / ni);
-         i = b.ib + (int)(r % ni);
+         k = b.kb + 2 + r / ni;
+         i = b.ib + r % ni;
       } else {
-         const long long r0 = q - nA - nB;
-         const int s = (int)(r0 / ((nj - 4) * (nk - 4)));
-         const long long r = r0 % ((nj - 4) * (nk - 4));
+         const int r0 = q - nA - nB;
+         const int s = r0 & 3, r = r0 >> 2;
          i = s < 2 ? b.ib + s : b.ie - (3 - s);
-         k = b.kb + 2 + (int)(r / (nj - 4));
-         j = b.jb + 2 + (int)(r % (nj - 4));
+         k = b.kb + 2 + r / (nj - 4);
+         j = b.jb + 2 + r % (nj - 4);
       }
 #pragma unroll
       for (int c = 0; c < 3; c++) shell_update(out, u, um, up, cidx(b, c, i, j, k), corrector);
@@ -250,6 +251,7 @@ int launch_ghost_shell(const Box& b, int corrector, double* out, const double* u
    const long long ni = b.ni, nj = b.je - b.jb + 1, nk = b.ke - b.kb + 1;
    if (ni < 5 || nj < 5 || nk < 5) return kBadArgument;
    const long long n = 4 * ni * nj + 4 * ni * (nk - 4) + 4 * (nj - 4) * (nk - 4);
+   if (n >= (1LL << 31)) return kNotSupported;  // the kernel indexes the shell in 32 bits
    ghost_shell_kernel<<<stream_grid(n), 256, 0, s>>>(b, corrector, F64Field{out},
                                                      F64Field{const_cast<double*>(u)},
                                                      F64Field{const_cast<double*>(um)},
@@ -263,6 +265,7 @@ int launch_ghost_shell_df(const Box& b, int corrector, float* out, const float* 
    const long long ni = b.ni, nj = b.je - b.jb + 1, nk = b.ke - b.kb + 1;
    if (ni < 5 || nj < 5 || nk < 5) return kBadArgument;
    const long long n = 4 * ni * nj + 4 * ni * (nk - 4) + 4 * (nj - 4) * (nk - 4);
+   if (n >= (1LL << 31)) return kNotSupported;  // the kernel indexes the shell in 32 bits
    const long long lo = 3 * b.npts;
    ghost_shell_kernel<<<stream_grid(n), 256, 0, s>>>(
        b, corrector, DFField{out, lo}, DFField{const_cast<float*>(u), lo},
