@@ -121,37 +121,71 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
    const double dt = dt_;
 
    // device memory: checkpoints, one segment of levels and predicted levels, adjoint work
-   std::vector<double*> bufs;
-   auto alloc = [&](double** p, size_t bytes) {
-      int st = cuda_ok(cudaMalloc(p, bytes));
-      if (st == kOk) bufs.push_back(*p);
-      return st;
-   };
-   double *ck = nullptr, *seg = nullptr, *pred = nullptr, *work = nullptr, *resd = nullptr;
-   int st = alloc(&ck, 2 * (size_t)nseg * lv);
-   if (st == kOk) st = alloc(&seg, (size_t)(seglen + 2) * lv);
-   if (st == kOk) st = alloc(&pred, (size_t)seglen * lv);
-   if (st == kOk) st = alloc(&work, 7 * lv);  // adjoint work (5) + the forward's final levels (2)
-   if (st == kOk) st = alloc(&resd, (size_t)(nsteps + 1) * nval * sizeof(double));
-   // the gradient terms (adj_grad.cu): the step's levels in the kernels' number type
-   // (5 levels of pairs, FP64 form, or of floats), the FP64 form's per-point sums (1
-   // level), the edge sums (12 numbers per point), the 1-D profile pairs and the two
-   // exponent maxima
-   double *dfw = nullptr, *dfp = nullptr, *dfe = nullptr;
+   // (kept from the previous call of the same shape)
+   const size_t segbytes = (size_t)(2 * seglen + 2) * lv;
    const int nax[3] = {bd.ie - bd.ib + 1, bd.je - bd.jb + 1, bd.ke - bd.kb + 1};
-   if (st == kOk) st = alloc(&dfw, mixed_ ? 5 * lv : 10 * lv);
-   if (st == kOk) st = alloc(&dfp, 4 * (size_t)(nax[0] + nax[1] + nax[2]) * sizeof(float2));
-   if (st == kOk) st = alloc(&dfe, sizeof(double));
-   double* gr_d = g_rho;
-   double* gm_d = g_mu;
-   double* gl_d = g_la;
-   double* gtmp = nullptr;
-   if (st == kOk && !grad_on_device) {
-      st = alloc(&gtmp, 3 * (size_t)npts_ * sizeof(double));
-      gr_d = gtmp;
-      gm_d = gtmp + npts_;
-      gl_d = gtmp + 2 * npts_;
+   GradCache& gc = gcache_;
+   int st = kOk;
+   if (!(gc.npts == npts_ && gc.nsteps == nsteps && gc.ckpt == ckpt && gc.nval == nval &&
+         gc.mixed == (int)mixed_ && gc.host_grad == (int)!grad_on_device && gc.budget == grad_store_bytes_)) {
+      drop_grad_cache();
+      auto alloc = [&](double** p, size_t bytes) {
+         int s = cuda_ok(cudaMalloc(p, bytes));
+         if (s == kOk) gc.mem.push_back(*p);
+         return s;
+      };
+      st = alloc(&gc.ck, 2 * (size_t)nseg * lv);
+      if (st == kOk) st = alloc(&gc.seg, (size_t)(seglen + 2) * lv);
+      if (st == kOk) st = alloc(&gc.pred, (size_t)seglen * lv);
+      if (st == kOk) st = alloc(&gc.work, 7 * lv);  // adjoint work (5) + the forward's final levels (2)
+      if (st == kOk) st = alloc(&gc.resd, (size_t)(nsteps + 1) * nval * sizeof(double));
+      // the gradient terms (adj_grad.cu): the step's levels in the kernels' number type
+      // (5 levels of pairs, FP64 form, or of floats), the FP64 form's per-point sums (1
+      // level), the edge sums (12 numbers per point), the 1-D profile pairs, the exponent
+      // maxima (adjoint; forward per segment; the kept segments')
+      if (st == kOk) st = alloc(&gc.dfw, mixed_ ? 5 * lv : 10 * lv);
+      if (st == kOk) st = alloc(&gc.dfp, 4 * (size_t)(nax[0] + nax[1] + nax[2]) * sizeof(float2));
+      if (st == kOk) st = alloc(&gc.dfe, ((size_t)nseg + 2) * sizeof(int) + sizeof(double));
+      if (st == kOk && !grad_on_device) st = alloc(&gc.gtmp, 3 * (size_t)npts_ * sizeof(double));
+      // Segments kept from the forward run, whose recompute the backward sweep skips:
+      // the last one in seg/pred, and before it as many as the store budget holds
+      // (each 2C + 2 levels; by default the free device memory less a reserve).
+      if (st == kOk && nseg > 1 && grad_store_bytes_ != 0) {
+         size_t freeb = 0, totb = 0;
+         if (cudaMemGetInfo(&freeb, &totb) == cudaSuccess) {
+            const size_t reserve = std::max((size_t)4 << 30, totb / 32);
+            size_t budget = freeb > reserve ? freeb - reserve : 0;
+            if (grad_store_bytes_ > 0) budget = std::min(budget, (size_t)grad_store_bytes_);
+            const int want = (int)std::min<size_t>((size_t)nseg - 1, budget / segbytes);
+            for (int q = 0; q < want; q++) {
+               double* x = nullptr;
+               if (cudaMalloc(&x, segbytes) != cudaSuccess) {
+                  cudaGetLastError();
+                  break;
+               }
+               gc.mem.push_back(x);
+               gc.xbuf.push_back(x);
+            }
+         }
+      }
+      if (st != kOk) {
+         drop_grad_cache();
+         return st;
+      }
+      gc.npts = npts_;
+      gc.nsteps = nsteps;
+      gc.ckpt = ckpt;
+      gc.nval = nval;
+      gc.mixed = (int)mixed_;
+      gc.host_grad = (int)!grad_on_device;
+      gc.budget = grad_store_bytes_;
    }
+   double *ck = gc.ck, *seg = gc.seg, *pred = gc.pred, *work = gc.work, *resd = gc.resd, *dfw = gc.dfw,
+          *dfp = gc.dfp, *dfe = gc.dfe;
+   const std::vector<double*>& xbuf = gc.xbuf;
+   double* gr_d = grad_on_device ? g_rho : gc.gtmp;
+   double* gm_d = grad_on_device ? g_mu : gc.gtmp + npts_;
+   double* gl_d = grad_on_device ? g_la : gc.gtmp + 2 * npts_;
    // A segment's adjoint steps run on two streams forked from the object's stream:
    // the stages (the critical path) on one of the highest priority and the gradient
    // terms of each step on one of the lowest, beside the next stages (they need the
@@ -164,7 +198,6 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       cudaStreamSynchronize(stream_);
       if (hs) cudaStreamSynchronize(hs);
       if (gs) cudaStreamSynchronize(gs);
-      for (double* p : bufs) cudaFree(p);
       if (hs) cudaStreamDestroy(hs);
       if (gs) cudaStreamDestroy(gs);
       for (cudaEvent_t e : {ev_s0, ev_g[0], ev_g[1], ev_join, ev_fork, ev_back})
@@ -182,29 +215,6 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
    if (st != kOk) {
       cleanup();
       return st;
-   }
-   // Segments kept from the forward run, whose recompute the backward sweep skips:
-   // the last one in seg/pred, and before it as many as the store budget holds
-   // (each 2C + 2 levels; by default the free device memory less a reserve).
-   const size_t segbytes = (size_t)(2 * seglen + 2) * lv;
-   std::vector<double*> xbuf;
-   if (nseg > 1 && grad_store_bytes_ != 0) {
-      size_t freeb = 0, totb = 0;
-      if (cudaMemGetInfo(&freeb, &totb) == cudaSuccess) {
-         const size_t reserve = std::max((size_t)4 << 30, totb / 32);
-         size_t budget = freeb > reserve ? freeb - reserve : 0;
-         if (grad_store_bytes_ > 0) budget = std::min(budget, (size_t)grad_store_bytes_);
-         const int want = (int)std::min<size_t>((size_t)nseg - 1, budget / segbytes);
-         for (int q = 0; q < want; q++) {
-            double* x = nullptr;
-            if (cudaMalloc(&x, segbytes) != cudaSuccess) {
-               cudaGetLastError();
-               break;
-            }
-            bufs.push_back(x);
-            xbuf.push_back(x);
-         }
-      }
    }
    const int nkept = 1 + (int)xbuf.size();
    std::vector<double> tseg(nseg);  // the time at each segment's start in the forward run
@@ -322,6 +332,17 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
                                      stream_));
    };
 
+   // The forward levels' shift of a segment: the largest exponent over its levels, of
+   // the two it starts from here and of the others from the corrector stages that write
+   // them (stage_emax_, set until the caller's steps end)
+   auto forward_scale = [&](const double* sq, int* slot) -> int {
+      if (mixed_) return kOk;
+      SW4G_TRY(cuda_ok(cudaMemsetAsync(slot, 0, sizeof(int), stream_)));
+      SW4G_TRY(launch_exp_max(sq, 2 * (long long)n3, slot, stream_));
+      stage_emax_ = slot;
+      return kOk;
+   };
+
    auto run = [&]() -> int {
       SW4G_TRY(cuda_ok(cudaMemsetAsync(gr_d, 0, npts_ * sizeof(double), stream_)));
       SW4G_TRY(cuda_ok(cudaMemsetAsync(gm_d, 0, npts_ * sizeof(double), stream_)));
@@ -348,7 +369,10 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
          double* pq = pred_of(sg);
          SW4G_TRY(cuda_ok(cudaMemcpyAsync(sq, lev_[ium_], lv, cudaMemcpyDeviceToDevice, stream_)));
          SW4G_TRY(cuda_ok(cudaMemcpyAsync(sq + n3, lev_[iu_], lv, cudaMemcpyDeviceToDevice, stream_)));
-         SW4G_TRY(steps_into(nn, s1, sq, pq));
+         SW4G_TRY(forward_scale(sq, emax + 2 + (nseg - 1 - sg)));
+         const int status = steps_into(nn, s1, sq, pq);
+         stage_emax_ = nullptr;
+         SW4G_TRY(status);
       }
       const double t_end = t_;
       double* fin = work + 5 * n3;  // u^N, u^{N-1}: the recompute overwrites the levels
@@ -505,12 +529,11 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
          return status;
       };
       // recompute the segment from its checkpoint: seg[q] = u^{s0-1+q}, pred[q] = up^{s0+q}
-      auto recompute = [&](int s0, int s1) -> int { return steps_into(s0, s1, seg, pred); };
-      // the forward levels' shift: the largest exponent over the segment's levels
-      auto seg_scale = [&](int s0, int s1) -> int {
-         if (mixed_) return kOk;
-         SW4G_TRY(cuda_ok(cudaMemsetAsync(emax + 1, 0, sizeof(int), stream_)));
-         return launch_exp_max(segp, (long long)(s1 - s0 + 2) * (long long)n3, emax + 1, stream_);
+      auto recompute = [&](int s0, int s1) -> int {
+         SW4G_TRY(forward_scale(seg, emax + 1));
+         const int status = steps_into(s0, s1, seg, pred);
+         stage_emax_ = nullptr;
+         return status;
       };
       // the segment's double-float sums into the FP64 gradients
       auto flush = [&]() -> int {
@@ -549,8 +572,10 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
          const bool full = graphs_ && s1 - s0 == ckpt;
          segp = seg_of(sg);
          predp = pred_of(sg);
-         if (kept(sg)) {
-            status = seg_scale(s0, s1);
+         if (kept(sg)) {  // its forward levels' shift, from the forward run
+            if (!mixed_)
+               status = cuda_ok(cudaMemcpyAsync(emax + 1, emax + 2 + (nseg - 1 - sg), sizeof(int),
+                                                cudaMemcpyDeviceToDevice, stream_));
          } else {
             if (full) {
                iu_ = 2;
@@ -577,7 +602,6 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
             } else if (status == kOk) {
                status = recompute(s0, s1);
             }
-            if (status == kOk) status = seg_scale(s0, s1);
          }
          if (status != kOk) break;
          if (full && adj_warm) {
@@ -625,6 +649,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       return kOk;
    };
    st = run();
+   stage_emax_ = nullptr;
    if (st == kOk && !grad_on_device) {
       st = cuda_ok(cudaMemcpyAsync(g_rho, gr_d, npts_ * sizeof(double), cudaMemcpyDeviceToHost, stream_));
       if (st == kOk)
@@ -633,7 +658,15 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
          st = cuda_ok(cudaMemcpyAsync(g_la, gl_d, npts_ * sizeof(double), cudaMemcpyDeviceToHost, stream_));
    }
    cleanup();
+   if (st != kOk) drop_grad_cache();
    return st;
+}
+
+void EW::drop_grad_cache()
+{
+   if (!gcache_.mem.empty()) cudaStreamSynchronize(stream_);
+   for (void* p : gcache_.mem) cudaFree(p);
+   gcache_ = GradCache{};
 }
 
 }  // namespace sw4g

@@ -20,6 +20,7 @@ EW::EW(const GridSpec& g, cudaStream_t stream, const TopoSpec* topo) : g_(g), st
 EW::~EW()
 {
    drop_graphs();
+   drop_grad_cache();
    auto f = [](void* p) {
       if (p) cudaFree(p);
    };
@@ -743,6 +744,7 @@ int EW::fused_piece(int piece, int ip, int iq)
          fs.up = up;
          fs.out = out;
          fs.beta = beta4;
+         fs.emax = stage_emax_;
       }
       return launch_fused_stage(fs, stream_);
    }

@@ -121,8 +121,11 @@ class EW {
    // Device memory gradient() may add for segments kept from its forward run (whose
    // recompute the backward sweep then skips): < 0 all free memory but a reserve
    // (the default), 0 none beyond the last segment, else at most this many bytes.
+   // gradient() keeps its device buffers for the next call of the same shape; this
+   // call releases them.
    int set_gradient_memory(long long bytes)
    {
+      drop_grad_cache();
       grad_store_bytes_ = bytes;
       return kOk;
    }
@@ -238,6 +241,18 @@ class EW {
 
    std::unique_ptr<CurvGrid> cv_;
    long long grad_store_bytes_ = -1;  // gradient(): budget for kept segments
+   // gradient()'s device buffers, kept for the next call of the same shape (freeing
+   // ~100 GB takes tens of milliseconds; a multi-shot inversion calls it once per shot)
+   struct GradCache {
+      long long npts = 0, budget = 0;
+      int nsteps = 0, ckpt = 0, nval = 0, mixed = -1, host_grad = -1;
+      std::vector<void*> mem;  // every allocation
+      double *ck = nullptr, *seg = nullptr, *pred = nullptr, *work = nullptr, *resd = nullptr,
+             *dfw = nullptr, *dfp = nullptr, *dfe = nullptr, *gtmp = nullptr;
+      std::vector<double*> xbuf;  // segments kept from the forward run
+   } gcache_;
+   void drop_grad_cache();
+   int* stage_emax_ = nullptr;        // gradient(): exponent maximum of the corrector's levels
 
    double t_ = 0, dt_ = 0;
 

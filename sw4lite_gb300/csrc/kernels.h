@@ -39,6 +39,7 @@ struct FusedStage {
    const double* co[3] = {nullptr, nullptr, nullptr};
    double h = 1, dt = 0, beta = 0;
    double coef = 0;  // > 0: the L(.) coefficient instead of dt^2 (dt^2/12 corrector)
+   int* emax = nullptr;  // corrector: atomicMax of the exponent fields of the level written
 };
 
 // (hi, lo) pairs interleaved: one 8-byte load per coefficient

@@ -63,6 +63,7 @@ struct FusedArgs {
    double cof144;  // 1/(144 h^2)
    double coef;    // dt^2 (predictor) or dt^2/12 (corrector)
    double beta;    // supergrid damping coefficient (corrector)
+   int* emax;      // if set: atomicMax of the FP64 exponent fields written (corrector)
 };
 
 __host__ __device__ constexpr int smem_doubles(int corr)
@@ -201,6 +202,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
       for (int c = 0; c < 3; c++) dq[4][c] = ds[c * PLANE + own];
    }
 
+   int em = 0;  // the largest exponent field written (a.emax)
    for (int k = kbeg; k <= kend; k++) {
       load_plane(k + 2);
       load_material(k);
@@ -399,14 +401,18 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                const long long q = p + c * npts;
-               if (CORR == 1)
-                  a.out[q] = (__ldg(a.up + q) + cr * lu[c]) - birho * sg[c];
-               else
-                  a.out[q] = (2 * __ldg(a.u + q) - __ldg(a.um + q) + cr * lu[c]) - birho * sg[c];
+               const double v = CORR == 1 ? (__ldg(a.up + q) + cr * lu[c]) - birho * sg[c]
+                                          : (2 * __ldg(a.u + q) - __ldg(a.um + q) + cr * lu[c]) - birho * sg[c];
+               a.out[q] = v;
+               em = max(em, (__double2hiint(v) >> 20) & 0x7ff);
             }
          }
       }
       __syncthreads();
+   }
+   if (a.emax) {  // uniform: every thread of a running CTA gets here
+      em = __reduce_max_sync(0xffffffffu, em);
+      if ((threadIdx.x & 31) == 0 && em > 0) atomicMax(a.emax, em);
    }
 }
 
@@ -623,6 +629,7 @@ int launch_fused_stage(const FusedStage& st, cudaStream_t stream)
    a.cof144 = 1.0 / (144 * st.h * st.h);
    a.coef = st.coef > 0 ? st.coef : (st.corrector ? st.dt * st.dt / 12 : st.dt * st.dt);
    a.beta = st.beta;
+   a.emax = st.emax;
    const int ni = b.ie - b.ib - 3, nj = b.je - b.jb - 3, nk = st.k2 - st.k1 + 1;
    const int gx = blocks_for(ni, TX), gy = blocks_for(nj, TY);
    // enough CTAs to fill every SM several times over; a chunk of at least 16 planes

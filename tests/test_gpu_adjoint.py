@@ -193,3 +193,26 @@ def test_kept_segments_bit_identical(precision):
             assert np.array_equal(x, y)
         assert np.array_equal(u, res[0][2])
     assert max(np.max(np.abs(x)) for x in res[0][1]) > 0
+
+
+@pytest.mark.parametrize("precision", [sg.FP64, sg.MIXED])
+def test_repeated_gradients_reuse_buffers(precision):
+    """A second gradient of the same shape on the same object (its buffers kept from
+    the first) and one of another shape (buffers made again) equal fresh objects'."""
+    c = AdjointCase(nsteps=31)
+    obs_case = AdjointCase(seed=12, nsteps=31)
+    obs = obs_case.records(oracle_forward(obs_case)[0][1:])
+    seg_bytes = (2 * 8 + 2) * 3 * c.npts * 8
+    fresh = {k: _gpu_gradient(c, obs, k, precision=precision, memory=seg_bytes) for k in (8, 6)}
+    ew = _ew(c, precision=precision)
+    ew.set_gradient_memory(seg_bytes)
+    zero = dev(np.zeros(3 * c.npts))
+    for k in (8, 8, 6):
+        ew.set_fields(zero, zero)
+        ew.set_time_step(c.dt, 0.0)
+        g = [dev(np.zeros(c.npts)) for _ in range(3)]
+        J = ew.gradient(c.nsteps, k, dev(obs), *g)
+        assert J == fresh[k][0]
+        for x, y in zip(g, fresh[k][1]):
+            assert np.array_equal(host(x), y)
+    ew.close()
