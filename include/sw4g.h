@@ -310,7 +310,9 @@ int sw4g_ew_step(sw4g_ew* ew, int nsteps, int mode);
  * checkpoint_every steps.  Device memory: (2*ceil(nsteps/C) + 2*C + 19) levels of
  * 3*npts doubles, plus the segments kept from the forward run (below).  Requires
  * Dirichlet or supergrid sides (zero ghost data), 4th-order damping, no topography.
- * The object ends at the end of the forward run. */
+ * The object ends at the end of the forward run.  It keeps that device memory for its
+ * next gradient of the same nsteps, checkpoint interval and receivers; a failed call,
+ * sw4g_ew_set_gradient_memory and sw4g_ew_destroy release it. */
 int sw4g_ew_gradient(sw4g_ew* ew, int nsteps, int checkpoint_every, const double* observed,
                      int obs_on_device, double* misfit, double* grad_rho, double* grad_mu,
                      double* grad_lambda, int grad_on_device);
@@ -318,7 +320,7 @@ int sw4g_ew_gradient(sw4g_ew* ew, int nsteps, int checkpoint_every, const double
  * as many segments before it as max_bytes allows (2C+2 levels each), so the backward
  * sweep recomputes only the others from their checkpoints.  max_bytes < 0 (the
  * default): all free device memory but a reserve of max(4 GiB, 1/32 of the device);
- * 0: only the last segment. */
+ * 0: only the last segment.  Releases the device memory kept from an earlier gradient. */
 int sw4g_ew_set_gradient_memory(sw4g_ew* ew, long long max_bytes);
 
 /* Restart files in the reference's checkpoint format (CheckPoint::write_checkpoint,
