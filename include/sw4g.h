@@ -414,6 +414,11 @@ int sw4g_ew_launches_per_step(const sw4g_ew* ew, int mode);
  * rows, ms[3] boundary conditions and forcing.  Synchronises the stream. */
 int sw4g_ew_profile_kernels(sw4g_ew* ew, int nrep, double* ms);
 
+/* Tuning (no reference counterpart): the number of k chunks every stage kernel
+ * splits its planes into, for all objects of the process; 0 restores the automatic
+ * choice (the count that fills the GPU's SMs in whole waves). */
+int sw4g_dev_set_stage_chunks(int chunks);
+
 /* Arithmetic throughput probe (no reference counterpart): FMA chains on every SM
  * in FP64 (precision=64) or FP32 (32); writes TFLOP/s.  Synchronises the stream. */
 int sw4g_fma_peak(int precision, double* tflops, void* stream);

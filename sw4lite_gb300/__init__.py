@@ -130,6 +130,7 @@ _SIGS = {
     "sw4g_ew_get_records": ([_VP, _VP, C.c_int], C.c_int),
     "sw4g_ew_launches_per_step": ([_VP, C.c_int], C.c_int),
     "sw4g_ew_profile_kernels": ([_VP, C.c_int, _D], C.c_int),
+    "sw4g_dev_set_stage_chunks": ([C.c_int], C.c_int),
     "sw4g_fma_peak": ([C.c_int, _D, _VP], C.c_int),
     "sw4g_corr_rows_scratch_len": ([C.c_int] * 4, C.c_longlong),
     "sw4g_pred_rows": ([C.c_int] * 8 + [_VP] * 9 + [C.c_double, C.c_double, _VP], C.c_int),
@@ -483,6 +484,11 @@ def nearest_grid_point(g, x, y, z):
     ijk = (C.c_int * 3)()
     check(lib().sw4g_nearest_grid_point(C.byref(g), x, y, z, ijk), "nearest_grid_point")
     return tuple(ijk)
+
+
+def set_stage_chunks(chunks=0) -> None:
+    """Tuning: k chunks of every stage kernel launch (0: the automatic choice)."""
+    check(lib().sw4g_dev_set_stage_chunks(int(chunks)), "set_stage_chunks")
 
 
 def fma_peak(precision=64, stream=None) -> float:

@@ -221,16 +221,20 @@ __global__ void grad_profiles_kernel(int n, const double* __restrict__ st, const
    bdc[x] = make_float2(h, l);
 }
 
+// The step kernels: one thread per array point, kGradThreads consecutive points of
+// a k plane (rows of i) per CTA, blockIdx.y the plane.
+constexpr int kGradThreads = 128;
+
 // w1 = up - 2u + um; the pairs of b1, mt (adjoint shift) and w1, u, um (forward
 // shift); the rho terms -W [mt . w1 + b1 . (un - up)] of the interior points
-__global__ void __launch_bounds__(128) grad_prep_kernel(GradDF g)
+__global__ void __launch_bounds__(kGradThreads) grad_prep_kernel(GradDF g)
 {
    const Box& b = g.b;
-   const int i = b.ib + blockIdx.x * blockDim.x + threadIdx.x, j = b.jb + blockIdx.y,
-             k = b.kb + blockIdx.z;
-   if (i > b.ie) return;
+   const int t = blockIdx.x * kGradThreads + threadIdx.x;
+   if (t >= (int)b.nij) return;
+   const int i = b.ib + t % (int)b.ni, j = b.jb + t / (int)b.ni, k = b.kb + blockIdx.y;
    const long long n = b.npts;
-   const long long p = (i - b.ib) + (j - b.jb) * b.ni + (k - b.kb) * b.nij;
+   const long long p = t + (k - b.kb) * b.nij;
    const int ka = (896 + shift_of(g.emax[0], g.marg_a)) << 20;
    const int kf = (896 + shift_of(g.emax[1], g.marg_f)) << 20;
    const bool in = i >= b.ib + 2 && i <= b.ie - 2 && j >= b.jb + 2 && j <= b.je - 2 && k >= b.kb + 2 &&
@@ -267,14 +271,14 @@ __device__ __forceinline__ float df_round(const float* x, long long q, long long
    return __fadd_rn(__ldg(x + q), __ldg(x + q + lo));
 }
 
-__global__ void __launch_bounds__(128) grad_prep_f1_kernel(GradDF g)
+__global__ void __launch_bounds__(kGradThreads) grad_prep_f1_kernel(GradDF g)
 {
    const Box& b = g.b;
-   const int i = b.ib + blockIdx.x * blockDim.x + threadIdx.x, j = b.jb + blockIdx.y,
-             k = b.kb + blockIdx.z;
-   if (i > b.ie) return;
+   const int t = blockIdx.x * kGradThreads + threadIdx.x;
+   if (t >= (int)b.nij) return;
+   const int i = b.ib + t % (int)b.ni, j = b.jb + t / (int)b.ni, k = b.kb + blockIdx.y;
    const long long n = b.npts, lo = g.lo;
-   const long long p = (i - b.ib) + (j - b.jb) * b.ni + (k - b.kb) * b.nij;
+   const long long p = t + (k - b.kb) * b.nij;
    const bool in = i >= b.ib + 2 && i <= b.ie - 2 && j >= b.jb + 2 && j <= b.je - 2 && k >= b.kb + 2 &&
                    k <= b.ke - 2;
    float acc = 0.f;
@@ -307,7 +311,6 @@ __global__ void __launch_bounds__(128) grad_prep_f1_kernel(GradDF g)
    }
 }
 
-constexpr int kGradThreads = 128;  // 32 x 4 points per CTA
 
 // the four edge sums {E1 mu, E1 lambda, E2 mu, E2 lambda} of the forward edges
 // (q, q+1) and (q, q+2) along axis a, summed over the components (mu weight 2 for
@@ -376,11 +379,11 @@ template <class V>
 __global__ void __launch_bounds__(kGradThreads) grad_edge_kernel(GradDF g)
 {
    const Box& b = g.b;
-   const int i = b.ib + (int)(blockIdx.x * 32 + threadIdx.x), j = b.jb + (int)(blockIdx.y * 4 + threadIdx.y),
-             k = b.kb + (int)blockIdx.z;
-   if (i > b.ie || j > b.je) return;
+   const int t = blockIdx.x * kGradThreads + threadIdx.x;
+   if (t >= (int)b.nij) return;
+   const int i = b.ib + t % (int)b.ni, j = b.jb + t / (int)b.ni, k = b.kb + (int)blockIdx.y;
    const long long n = b.npts;
-   const int p = (i - b.ib) + (j - b.jb) * (int)b.ni + (k - b.kb) * (int)b.nij;
+   const int p = t + (k - b.kb) * (int)b.nij;
 #pragma unroll 1
    for (int a = 0; a < 3; a++) {
       const int x = a == 0 ? i : a == 1 ? j : k;
@@ -412,11 +415,11 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
    // centred first differences of the current pair, [slot][thread]: slot c*3 + a for
    // the adjoint level, 9 + c*3 + a for the forward level
    __shared__ typename N::S fd[18][kGradThreads];
-   const int tid = threadIdx.y * 32 + threadIdx.x;
+   const int tid = threadIdx.x;
    const Box& b = g.b;
-   const int pc[3] = {b.ib + (int)(blockIdx.x * 32 + threadIdx.x), b.jb + (int)(blockIdx.y * 4 + threadIdx.y),
-                      b.kb + (int)blockIdx.z};
-   if (pc[0] > b.ie || pc[1] > b.je) return;
+   const int t0 = blockIdx.x * kGradThreads + tid;
+   if (t0 >= (int)b.nij) return;
+   const int pc[3] = {b.ib + t0 % (int)b.ni, b.jb + t0 / (int)b.ni, b.kb + (int)blockIdx.y};
    const long long n = b.npts;
    const int off[3] = {pc[0] - b.ib, pc[1] - b.jb, pc[2] - b.kb};
    const int p = off[0] + off[1] * (int)b.ni + off[2] * (int)b.nij;
@@ -605,26 +608,24 @@ int launch_inj_exp(const Box& b, const double* const st[3], int nrec, const int*
 int launch_grad_df_step(const GradDF& g, cudaStream_t s)
 {
    const Box& b = g.b;
-   const int ni = (int)b.ni, nj = b.je - b.jb + 1, nk = b.ke - b.kb + 1;
-   grad_prep_kernel<<<dim3((ni + 127) / 128, nj, nk), 128, 0, s>>>(g);
+   const dim3 grid(blocks_for(b.nij, kGradThreads), b.ke - b.kb + 1);
+   grad_prep_kernel<<<grid, kGradThreads, 0, s>>>(g);
    SW4G_TRY(launch_status());
-   const dim3 grid((ni + 31) / 32, (nj + 3) / 4, nk), block(32, 4);
-   grad_edge_kernel<DF><<<grid, block, 0, s>>>(g);
+   grad_edge_kernel<DF><<<grid, kGradThreads, 0, s>>>(g);
    SW4G_TRY(launch_status());
-   grad_df_kernel<DF><<<grid, block, 0, s>>>(g);
+   grad_df_kernel<DF><<<grid, kGradThreads, 0, s>>>(g);
    return launch_status();
 }
 
 int launch_grad_f1_step(const GradDF& g, cudaStream_t s)
 {
    const Box& b = g.b;
-   const int ni = (int)b.ni, nj = b.je - b.jb + 1, nk = b.ke - b.kb + 1;
-   grad_prep_f1_kernel<<<dim3((ni + 127) / 128, nj, nk), 128, 0, s>>>(g);
+   const dim3 grid(blocks_for(b.nij, kGradThreads), b.ke - b.kb + 1);
+   grad_prep_f1_kernel<<<grid, kGradThreads, 0, s>>>(g);
    SW4G_TRY(launch_status());
-   const dim3 grid((ni + 31) / 32, (nj + 3) / 4, nk), block(32, 4);
-   grad_edge_kernel<F1><<<grid, block, 0, s>>>(g);
+   grad_edge_kernel<F1><<<grid, kGradThreads, 0, s>>>(g);
    SW4G_TRY(launch_status());
-   grad_df_kernel<F1><<<grid, block, 0, s>>>(g);
+   grad_df_kernel<F1><<<grid, kGradThreads, 0, s>>>(g);
    return launch_status();
 }
 

@@ -668,6 +668,13 @@ int sw4g_ew_profile_kernels(sw4g_ew* ew, int nrep, double* ms)
    return ew->impl->profile_kernels(nrep, ms);
 }
 
+int sw4g_dev_set_stage_chunks(int chunks)
+{
+   if (chunks < 0) return SW4G_BAD_ARGUMENT;
+   set_stage_chunks_override(chunks);
+   return SW4G_OK;
+}
+
 int sw4g_fma_peak(int precision, double* tflops, void* stream)
 {
    if (!tflops || (precision != 64 && precision != 32)) return SW4G_BAD_ARGUMENT;

@@ -109,4 +109,16 @@ inline int blocks_for(long long n, int threads)
    return (int)(b > 0 ? b : 1);
 }
 
+// Planes per CTA of a stage kernel that marches along k over cols CTA columns of nk
+// planes, with `resident` CTAs of it on each SM at once.  The launch runs in waves of
+// resident x SMs CTAs and a last wave that fills only part of the GPU leaves the rest
+// idle, so the chunk count minimises waves x (planes per chunk + the ring's warm-up,
+// about two planes' work), with at least min_planes planes per chunk.  A positive
+// stage_chunks_override() (sw4g_dev_set_stage_chunks) replaces the count.
+int stage_kchunk(long long cols, int nk, int resident, int min_planes);
+int stage_chunks_override();
+void set_stage_chunks_override(int chunks);
+// CTAs of `kernel` resident per SM at `threads` threads and `smem` dynamic bytes
+int resident_ctas(const void* kernel, int threads, size_t smem);
+
 }  // namespace sw4g

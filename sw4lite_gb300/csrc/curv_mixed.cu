@@ -462,21 +462,20 @@ int launch_curv_stage_df(const CurvStageDF& st, cudaStream_t s)
    if (nk <= 0) return kOk;
    const int ni = b.ie - b.ib - 3, nj = b.je - b.jb - 3;
    const int gx = blocks_for(ni, TX), gy = blocks_for(nj, TY);
-   int chunks = 1;
-   const long long cols = (long long)gx * gy, want = 152LL * 8;
-   if (cols < want) chunks = (int)std::min<long long>((want + cols - 1) / cols, std::max(1, nk / 12));
-   a.kchunk = (nk + chunks - 1) / chunks;
-   const dim3 grid(gx, gy, (nk + a.kchunk - 1) / a.kchunk), block(TX, TY, 1);
    const size_t smem = mixed_smem_floats(corr) * sizeof(float);
+   const void* kern = corr ? (const void*)curv_mixed_kernel<1> : (const void*)curv_mixed_kernel<0>;
    int dev = 0;
    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return kCudaError;
    static bool attr[2][64] = {};
+   static int resident[2][64] = {};
    if (!attr[corr][dev]) {
-      cudaError_t e = corr ? cudaFuncSetAttribute(curv_mixed_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                           : cudaFuncSetAttribute(curv_mixed_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return kCudaError;
+      if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+         return kCudaError;
+      resident[corr][dev] = resident_ctas(kern, NTHREADS, smem);
       attr[corr][dev] = true;
    }
+   a.kchunk = stage_kchunk((long long)gx * gy, nk, resident[corr][dev], 12);
+   const dim3 grid(gx, gy, (nk + a.kchunk - 1) / a.kchunk), block(TX, TY, 1);
    if (corr) curv_mixed_kernel<1><<<grid, block, smem, s>>>(a);
    else curv_mixed_kernel<0><<<grid, block, smem, s>>>(a);
    return launch_status();

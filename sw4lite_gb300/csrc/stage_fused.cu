@@ -27,6 +27,7 @@
 //      out = 2u - um + coef/rho * L(up) - beta/rho * SG(u - um)
 //    (the stage field read from `up` directly).
 #include <algorithm>
+#include <atomic>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -599,6 +600,53 @@ int launch_uacc_slab_df(const Box& b, int k0, int k1, const float* up, const flo
    return launch_status();
 }
 
+namespace {
+std::atomic<int> g_stage_chunks{0};
+}
+
+int stage_chunks_override() { return g_stage_chunks.load(std::memory_order_relaxed); }
+void set_stage_chunks_override(int chunks) { g_stage_chunks.store(chunks > 0 ? chunks : 0); }
+
+int resident_ctas(const void* kernel, int threads, size_t smem)
+{
+   int n = 0;
+   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess) {
+      cudaGetLastError();
+      return 1;
+   }
+   return n > 0 ? n : 1;
+}
+
+int stage_kchunk(long long cols, int nk, int resident, int min_planes)
+{
+   if (nk < 1) return 1;
+   int sms = 0, dev = 0;
+   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+       sms < 1) {
+      cudaGetLastError();
+      sms = 152;
+   }
+   const long long slots = (long long)sms * std::max(1, resident);
+   const int forced = stage_chunks_override();
+   int chunks = 1;
+   if (forced > 0) {
+      chunks = std::min(forced, nk);
+   } else {
+      const int most = std::max(1, nk / std::max(1, min_planes));
+      double best = 0;
+      for (int c = 1; c <= most; c++) {
+         const int per = (nk + c - 1) / c;
+         const long long ctas = cols * (long long)((nk + per - 1) / per);
+         const double cost = (double)((ctas + slots - 1) / slots) * (per + 2);
+         if (c == 1 || cost < best * 0.999) {
+            best = cost;
+            chunks = c;
+         }
+      }
+   }
+   return (nk + chunks - 1) / chunks;
+}
+
 int launch_fused_stage(const FusedStage& st, cudaStream_t stream)
 {
    if (st.k2 < st.k1) return kOk;
@@ -632,31 +680,25 @@ int launch_fused_stage(const FusedStage& st, cudaStream_t stream)
    a.emax = st.emax;
    const int ni = b.ie - b.ib - 3, nj = b.je - b.jb - 3, nk = st.k2 - st.k1 + 1;
    const int gx = blocks_for(ni, TX), gy = blocks_for(nj, TY);
-   // enough CTAs to fill every SM several times over; a chunk of at least 16 planes
-   // keeps the 4-plane warm-up of the ring small
-   int chunks = 1;
-   const long long cols = (long long)gx * gy;
-   const long long want = 152LL * 8;
-   if (cols < want) chunks = (int)std::min<long long>((want + cols - 1) / cols, std::max(1, nk / 16));
-   if (st.kchunk > 0) chunks = (nk + st.kchunk - 1) / st.kchunk;
-   a.kchunk = (nk + chunks - 1) / chunks;
-   const dim3 grid(gx, gy, (nk + a.kchunk - 1) / a.kchunk), block(TX, TY, 1);
    const int form = st.corrector;  // 0, 1 or 2
    if (form < 0 || form > 2) return kBadArgument;
    const size_t smem = smem_doubles(form) * sizeof(double);
+   const void* kern = form == 0 ? (const void*)fused_stage_kernel<0>
+                      : form == 1 ? (const void*)fused_stage_kernel<1>
+                                  : (const void*)fused_stage_kernel<2>;
    // the opt-in shared-memory size is a per-device function attribute
    int dev = 0;
    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return kCudaError;
    static bool attr_set[3][64] = {};
+   static int resident[3][64] = {};
    if (!attr_set[form][dev]) {
-      cudaError_t e = form == 0
-          ? cudaFuncSetAttribute(fused_stage_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-          : form == 1
-          ? cudaFuncSetAttribute(fused_stage_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-          : cudaFuncSetAttribute(fused_stage_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return kCudaError;
+      if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+         return kCudaError;
+      resident[form][dev] = resident_ctas(kern, NTHREADS, smem);
       attr_set[form][dev] = true;
    }
+   a.kchunk = st.kchunk > 0 ? st.kchunk : stage_kchunk((long long)gx * gy, nk, resident[form][dev], 12);
+   const dim3 grid(gx, gy, (nk + a.kchunk - 1) / a.kchunk), block(TX, TY, 1);
    if (form == 0)
       fused_stage_kernel<0><<<grid, block, smem, stream>>>(a);
    else if (form == 1)

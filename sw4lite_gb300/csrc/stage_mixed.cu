@@ -619,24 +619,22 @@ int launch_mixed_stage(const MixedStage& st, cudaStream_t stream)
    a.beta = (float)st.beta;
    const int ni = b.ie - b.ib - 3, nj = b.je - b.jb - 3, nk = st.k2 - st.k1 + 1;
    const int gx = blocks_for(ni, TX), gy = blocks_for(nj, TY);
-   int chunks = 1;
-   const long long cols = (long long)gx * gy;
-   const long long want = 152LL * 8;
-   if (cols < want) chunks = (int)std::min<long long>((want + cols - 1) / cols, std::max(1, nk / 16));
-   a.kchunk = (nk + chunks - 1) / chunks;
-   const dim3 grid(gx, gy, (nk + a.kchunk - 1) / a.kchunk), block(TX, TY, 1);
    const size_t smem = smem_floats(st.corrector) * sizeof(float);
+   const void* kern = st.corrector == 1   ? (const void*)mixed_stage_kernel<1>
+                      : st.corrector == 2 ? (const void*)mixed_stage_kernel<2>
+                                          : (const void*)mixed_stage_kernel<0>;
    int dev = 0;
    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return kCudaError;
    static bool attr_set[3][64] = {};
+   static int resident[3][64] = {};
    if (!attr_set[st.corrector][dev]) {
-      const cudaError_t e =
-          st.corrector == 1   ? cudaFuncSetAttribute(mixed_stage_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-          : st.corrector == 2 ? cudaFuncSetAttribute(mixed_stage_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                              : cudaFuncSetAttribute(mixed_stage_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return kCudaError;
+      if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+         return kCudaError;
+      resident[st.corrector][dev] = resident_ctas(kern, NTHREADS, smem);
       attr_set[st.corrector][dev] = true;
    }
+   a.kchunk = stage_kchunk((long long)gx * gy, nk, resident[st.corrector][dev], 12);
+   const dim3 grid(gx, gy, (nk + a.kchunk - 1) / a.kchunk), block(TX, TY, 1);
    if (st.corrector == 1)
       mixed_stage_kernel<1><<<grid, block, smem, stream>>>(a);
    else if (st.corrector == 2)
