@@ -113,7 +113,8 @@ inline int blocks_for(long long n, int threads)
 // planes, with `resident` CTAs of it on each SM at once.  The launch runs in waves of
 // resident x SMs CTAs and a last wave that fills only part of the GPU leaves the rest
 // idle, so the chunk count minimises waves x (planes per chunk + the ring's warm-up,
-// about two planes' work), with at least min_planes planes per chunk.  A positive
+// about two planes' work) over the counts that give at least 3.5 waves, with at
+// least min_planes planes per chunk.  A positive
 // stage_chunks_override() (sw4g_dev_set_stage_chunks) replaces the count.
 int stage_kchunk(long long cols, int nk, int resident, int min_planes);
 int stage_chunks_override();

@@ -632,13 +632,17 @@ int stage_kchunk(long long cols, int nk, int resident, int min_planes)
    if (forced > 0) {
       chunks = std::min(forced, nk);
    } else {
+      // among the counts that give at least 3.5 waves (fewer, longer CTAs measured
+      // slower on the topography grids); the most chunks if none does
       const int most = std::max(1, nk / std::max(1, min_planes));
-      double best = 0;
+      double best = -1;
+      chunks = most;
       for (int c = 1; c <= most; c++) {
          const int per = (nk + c - 1) / c;
          const long long ctas = cols * (long long)((nk + per - 1) / per);
+         if (2 * ctas < 7 * slots) continue;
          const double cost = (double)((ctas + slots - 1) / slots) * (per + 2);
-         if (c == 1 || cost < best * 0.999) {
+         if (best < 0 || cost < best * 0.999) {
             best = cost;
             chunks = c;
          }
