@@ -222,8 +222,11 @@ __global__ void grad_profiles_kernel(int n, const double* __restrict__ st, const
 }
 
 // The step kernels: one thread per array point, kGradThreads consecutive points of
-// a k plane (rows of i) per CTA, blockIdx.y the plane.
-constexpr int kGradThreads = 128;
+// a k plane (rows of i) per CTA, blockIdx.y the plane.  They run beside the FP64
+// stage kernels, in the registers those leave free: the predictor-form stage (96
+// registers x 512 threads per SM) leaves 16K, room for three 64-thread CTAs of
+// grad_df_kernel (72 registers) but one of 128 threads.
+constexpr int kGradThreads = 64;
 
 // w1 = up - 2u + um; the pairs of b1, mt (adjoint shift) and w1, u, um (forward
 // shift); the rho terms -W [mt . w1 + b1 . (un - up)] of the interior points
