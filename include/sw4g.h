@@ -403,6 +403,43 @@ int sw4g_ew_set_receivers(sw4g_ew* ew, int n, const int* ijk, const int* mode, i
 int sw4g_ew_record_shape(const sw4g_ew* ew, int* rows, int* nvals);
 /* copies rows x nvals doubles (row-major) to host (on_device=0) or device memory */
 int sw4g_ew_get_records(const sw4g_ew* ew, double* out, int on_device);
+/* Receiver files.  The grid's geographic mapping: the members of EW that
+ * EW::computeGeographicCoord reads (src/EW.C:5794-5816; defaults src/EW.C:192-197). */
+typedef struct {
+   double lon_origin, lat_origin; /* degrees, at x = y = 0 */
+   double az;                     /* grid azimuth, degrees (mGeoAz) */
+   double meters_per_degree;
+   double meters_per_longitude;   /* used when const_meters_per_longitude != 0 */
+   int const_meters_per_longitude;
+} sw4g_geo;
+/* The reference's defaults: lon -118, lat 37, az 0, 111319.5 m per degree,
+ * 87721 m per degree of longitude (not constant). */
+int sw4g_geo_default(sw4g_geo* geo);
+/* longitude and latitude of grid point (x, y); replaces EW::computeGeographicCoord
+ * (src/EW.C:5794) for the spheroidal mapping (no proj4 projection). */
+int sw4g_geographic_coord(const sw4g_geo* geo, double x, double y, double* lon, double* lat);
+/* One receiver's file: what a TimeSeries holds besides its records. */
+typedef struct {
+   const char* station; /* written as "# Station:" (TimeSeries::m_fileName) */
+   double x, y;         /* requested location, m */
+   double gp_x, gp_y;   /* location of the grid point that records, m */
+   int utc[7];          /* year, month, day, hour, minute, second, millisecond */
+   int mode;            /* SW4G_REC_*: the columns */
+   int xyz;             /* 1: grid components; 0: east-west, north-south, up-down */
+   double t_shift, dt;  /* row r is at time t_shift + r dt */
+} sw4g_usgs_station;
+/* Writes `rows` record rows of one receiver in the USGS text format of
+ * TimeSeries::write_usgs_format (src/TimeSeries.C:924-1056), byte for byte: the
+ * header, then per row the time and the mode's values.  rec points at the
+ * receiver's first value of row 0; its values are consecutive and rows are
+ * row_stride doubles apart (the record array of sw4g_ew_get_records on the host:
+ * row_stride = nvals, rec offset by the values of the receivers before it).  With
+ * xyz = 0, displacement and velocity are rotated to east-west, north-south and
+ * up-down as the reference does; for the other modes (curl, strains, gradient) the
+ * reference writes the header alone, and so does this function, returning
+ * SW4G_NOT_SUPPORTED.  SW4G_IO_ERROR if the file cannot be written. */
+int sw4g_write_usgs(const char* path, const sw4g_geo* geo, const sw4g_usgs_station* st,
+                    const double* rec, long long rows, long long row_stride);
 /* boundary conditions of this grid on a caller's 3-component device array */
 int sw4g_ew_enforce_bc(sw4g_ew* ew, double* u);
 /* kernel launches one step enqueues */

@@ -52,6 +52,20 @@ class TopoDesc(C.Structure):
                 ("ly", C.c_double), ("zeta_break", C.c_double), ("order", C.c_int)]
 
 
+class GeoDesc(C.Structure):
+    """sw4g_geo (include/sw4g.h): the grid's geographic mapping."""
+    _fields_ = [("lon_origin", C.c_double), ("lat_origin", C.c_double), ("az", C.c_double),
+                ("meters_per_degree", C.c_double), ("meters_per_longitude", C.c_double),
+                ("const_meters_per_longitude", C.c_int)]
+
+
+class UsgsStation(C.Structure):
+    """sw4g_usgs_station (include/sw4g.h): one receiver file's header fields."""
+    _fields_ = [("station", C.c_char_p), ("x", C.c_double), ("y", C.c_double),
+                ("gp_x", C.c_double), ("gp_y", C.c_double), ("utc", C.c_int * 7),
+                ("mode", C.c_int), ("xyz", C.c_int), ("t_shift", C.c_double), ("dt", C.c_double)]
+
+
 def topo_desc(amp, xc, yc, lx, ly, zeta_break=0.95, order=4) -> TopoDesc:
     t = TopoDesc()
     t.amp, t.xc, t.yc, t.lx, t.ly, t.zeta_break, t.order = amp, xc, yc, lx, ly, zeta_break, order
@@ -65,6 +79,8 @@ FREE, DIRICHLET, SUPERGRID, PERIODIC, INTERFACE = 0, 1, 2, 3, 4
 MODE_PHASES, MODE_FUSED = 0, 1
 # receiver record modes (the reference's TimeSeries::receiverMode numbering)
 REC_DISPLACEMENT, REC_DIV, REC_CURL, REC_STRAINS, REC_VELOCITY, REC_GRADIENT = 0, 1, 2, 3, 4, 5
+# sw4g_status codes
+OK, BAD_ARGUMENT, CUDA_ERROR, NAN_DETECTED, NOT_SUPPORTED, TIMEOUT, IO_ERROR = range(7)
 
 _SIGS = {
     "sw4g_version": ([], C.c_char_p),
@@ -131,6 +147,10 @@ _SIGS = {
     "sw4g_ew_launches_per_step": ([_VP, C.c_int], C.c_int),
     "sw4g_ew_profile_kernels": ([_VP, C.c_int, _D], C.c_int),
     "sw4g_dev_set_stage_chunks": ([C.c_int], C.c_int),
+    "sw4g_geo_default": ([C.POINTER(GeoDesc)], C.c_int),
+    "sw4g_geographic_coord": ([C.POINTER(GeoDesc), C.c_double, C.c_double, _D, _D], C.c_int),
+    "sw4g_write_usgs": ([C.c_char_p, C.POINTER(GeoDesc), C.POINTER(UsgsStation), _D, C.c_longlong,
+                         C.c_longlong], C.c_int),
     "sw4g_fma_peak": ([C.c_int, _D, _VP], C.c_int),
     "sw4g_corr_rows_scratch_len": ([C.c_int] * 4, C.c_longlong),
     "sw4g_pred_rows": ([C.c_int] * 8 + [_VP] * 9 + [C.c_double, C.c_double, _VP], C.c_int),
@@ -484,6 +504,48 @@ def nearest_grid_point(g, x, y, z):
     ijk = (C.c_int * 3)()
     check(lib().sw4g_nearest_grid_point(C.byref(g), x, y, z, ijk), "nearest_grid_point")
     return tuple(ijk)
+
+
+def geo_desc(**kw) -> GeoDesc:
+    """The reference's default geographic mapping (lon -118, lat 37, azimuth 0),
+    with any field replaced by a keyword."""
+    g = GeoDesc()
+    check(lib().sw4g_geo_default(C.byref(g)), "geo_default")
+    for k, v in kw.items():
+        setattr(g, k, v)
+    return g
+
+
+def geographic_coord(geo, x, y):
+    """(longitude, latitude) in degrees of grid point (x, y)."""
+    lon, lat = C.c_double(), C.c_double()
+    check(lib().sw4g_geographic_coord(C.byref(geo), x, y, C.byref(lon), C.byref(lat)), "geographic_coord")
+    return lon.value, lat.value
+
+
+def write_usgs(path, values, *, station, x, y, gp_x, gp_y, dt, mode=REC_DISPLACEMENT, xyz=True,
+               t_shift=0.0, utc=(1970, 1, 1, 0, 0, 0, 0), geo=None):
+    """Writes one receiver's records (rows x values, e.g. its columns of
+    EW.records()) as a USGS text file, byte for byte as the reference does.
+    Returns the status: 0, or NOT_SUPPORTED (header only) for curl, strains and
+    gradient records in geographic components."""
+    import numpy as np
+    v = np.asarray(values, dtype=np.float64)
+    if v.ndim == 1:
+        v = v.reshape(-1, 1)
+    if v.strides[1] != 8:
+        v = np.ascontiguousarray(v)
+    st = UsgsStation()
+    st.station = station.encode()
+    st.x, st.y, st.gp_x, st.gp_y = x, y, gp_x, gp_y
+    st.utc[:] = list(utc)
+    st.mode, st.xyz, st.t_shift, st.dt = mode, int(bool(xyz)), t_shift, dt
+    geo = geo_desc() if geo is None else geo
+    rc = lib().sw4g_write_usgs(str(path).encode(), C.byref(geo), C.byref(st), v.ctypes.data_as(_D),
+                               v.shape[0], v.strides[0] // 8)
+    if rc not in (0, NOT_SUPPORTED):
+        check(rc, "write_usgs")
+    return rc
 
 
 def set_stage_chunks(chunks=0) -> None:

@@ -1,0 +1,78 @@
+#!/usr/bin/env python
+"""Writes the receiver-file fixtures of tests/test_usgs_format.py from the
+reference's own stored outputs (USGS text files written by
+TimeSeries::write_usgs_format, src/TimeSeries.C:924) and the decks that made them.
+
+Each fixture keeps a file's header and either all its record rows (the 64-row
+topography files) or a 48-row window around the largest value; usgs_meta.json
+records the total row count, the window's first row and, from the deck, the grid
+spacing, extent, run time and the receiver's requested location.
+
+    python tests/golden/make_usgs_fixtures.py [REFERENCE_ROOT]
+"""
+import json
+import re
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+# (fixture name, stored output, deck) under the reference's pytest/reference
+FILES = [
+    ("topo_sta01", "topo/curvilinear-output/sta01.txt", "topo/curvilinear.in"),
+    ("topo_sta02", "topo/curvilinear-output/sta02.txt", "topo/curvilinear.in"),
+    ("topo_sta03", "topo/curvilinear-output/sta03.txt", "topo/curvilinear.in"),
+    ("many_blocks_sta01", "topo/many-blocks-out/sta01.txt", "topo/many-blocks.in"),
+    ("loh1_h50_sta10", "loh1/LOH1-h50/sta10.txt", "loh1/LOH.1-h50.in"),
+    ("loh1_h100_sta10", "loh1/LOH1-h100/sta10.txt", "loh1/LOH.1-h100.in"),
+    ("loh2_h50_sta10", "loh2/LOH2-h50/sta10.txt", "loh2/LOH.2-h50.in"),
+    ("loh2_h100_sta10", "loh2/LOH2-h100/sta10.txt", "loh2/LOH.2-h100.in"),
+]
+WINDOW = 48
+
+
+def _tokens(line):
+    return dict(t.split("=", 1) for t in line.split()[1:] if "=" in t)
+
+
+def deck_params(text, station):
+    out = {}
+    for line in text.splitlines():
+        line = line.strip()
+        if line.startswith("grid "):
+            g = _tokens(line)
+            out.update(h=float(g["h"]), x_extent=float(g["x"]), y_extent=float(g["y"]),
+                       z_extent=float(g["z"]))
+        elif line.startswith("time "):
+            out["t"] = float(_tokens(line)["t"])
+        elif line.startswith("rec "):
+            r = _tokens(line)
+            if r.get("file") == station:
+                out.update(x=float(r["x"]), y=float(r["y"]),
+                           z=float(r.get("z", r.get("depth", "0"))))
+    return out
+
+
+def main(root):
+    base = Path(root) / "pytest" / "reference"
+    meta = {}
+    for name, out, deck in FILES:
+        lines = (base / out).read_text().splitlines(keepends=True)
+        head = [l for l in lines if l.startswith("#")]
+        data = lines[len(head):]
+        station = re.search(r"# Station: (\S+)", "".join(head)).group(1)
+        if len(data) <= 2 * WINDOW:
+            start, keep = 0, data
+        else:
+            peak = max(range(len(data)), key=lambda i: max(abs(float(v)) for v in data[i].split()[1:]))
+            start = max(0, min(len(data) - WINDOW, peak - WINDOW // 2))
+            keep = data[start:start + WINDOW]
+        (HERE / f"usgs_{name}.txt").write_text("".join(head + keep))
+        p = deck_params((base / deck).read_text(), station)
+        p.update(rows=len(data), start=start, source=f"pytest/reference/{out}",
+                 deck=f"pytest/reference/{deck}")
+        meta[name] = p
+    (HERE / "usgs_meta.json").write_text(json.dumps(meta, indent=1, sort_keys=True) + "\n")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
