@@ -440,6 +440,29 @@ typedef struct {
  * SW4G_NOT_SUPPORTED.  SW4G_IO_ERROR if the file cannot be written. */
 int sw4g_write_usgs(const char* path, const sw4g_geo* geo, const sw4g_usgs_station* st,
                     const double* rec, long long rows, long long row_stride);
+/* The event a SAC header names (EVLA, EVLO, EVDP, O). */
+typedef struct {
+   double lat, lon;    /* degrees */
+   double depth;       /* m (written in km) */
+   double time_offset; /* s */
+} sw4g_sac_event;
+/* Writes one receiver's records as binary SAC files, one per value of the mode,
+ * named prefix + the reference's suffix (x y z, e n u, xv yv zv, ev nv uv, div,
+ * curlx.., xx yy zz xy xz yz, duxdx..duzdz); replaces the SAC branch of
+ * TimeSeries::writeFile (src/TimeSeries.C:416-822) with write_sac_format (:826) and
+ * its SAC header library (src/sacsubc.C: newhdr, scmxmn, bwsac).  The values are
+ * written as FP32 (the reference's mRecordedFloats), the header holds their
+ * extrema and mean, the time axis (t_shift, dt), the UTC fields with the day of
+ * the year, the station's latitude and longitude, the event, the component's name,
+ * inclination and azimuth, and KSTNM = st->station.  With xyz = 0 displacement,
+ * velocity and curl are rotated as in the USGS writer.  flush_subnormals = 1 writes
+ * samples that round to an FP32 subnormal as signed zeros, as builds with
+ * flush-to-zero arithmetic do (the reference's stored LOH.1 h=100 traces); 0 keeps
+ * IEEE rounding (its stored LOH.2 traces, a default gcc build).  Little-endian
+ * words, as the reference's fwrite of its header struct on x86_64 and aarch64. */
+int sw4g_write_sac(const char* prefix, const sw4g_geo* geo, const sw4g_usgs_station* st,
+                   const sw4g_sac_event* ev, const double* rec, long long rows, long long row_stride,
+                   int flush_subnormals);
 /* boundary conditions of this grid on a caller's 3-component device array */
 int sw4g_ew_enforce_bc(sw4g_ew* ew, double* u);
 /* kernel launches one step enqueues */

@@ -59,6 +59,12 @@ class GeoDesc(C.Structure):
                 ("const_meters_per_longitude", C.c_int)]
 
 
+class SacEvent(C.Structure):
+    """sw4g_sac_event (include/sw4g.h): the event a SAC header names."""
+    _fields_ = [("lat", C.c_double), ("lon", C.c_double), ("depth", C.c_double),
+                ("time_offset", C.c_double)]
+
+
 class UsgsStation(C.Structure):
     """sw4g_usgs_station (include/sw4g.h): one receiver file's header fields."""
     _fields_ = [("station", C.c_char_p), ("x", C.c_double), ("y", C.c_double),
@@ -151,6 +157,8 @@ _SIGS = {
     "sw4g_geographic_coord": ([C.POINTER(GeoDesc), C.c_double, C.c_double, _D, _D], C.c_int),
     "sw4g_write_usgs": ([C.c_char_p, C.POINTER(GeoDesc), C.POINTER(UsgsStation), _D, C.c_longlong,
                          C.c_longlong], C.c_int),
+    "sw4g_write_sac": ([C.c_char_p, C.POINTER(GeoDesc), C.POINTER(UsgsStation), C.POINTER(SacEvent), _D,
+                        C.c_longlong, C.c_longlong, C.c_int], C.c_int),
     "sw4g_fma_peak": ([C.c_int, _D, _VP], C.c_int),
     "sw4g_corr_rows_scratch_len": ([C.c_int] * 4, C.c_longlong),
     "sw4g_pred_rows": ([C.c_int] * 8 + [_VP] * 9 + [C.c_double, C.c_double, _VP], C.c_int),
@@ -529,23 +537,49 @@ def write_usgs(path, values, *, station, x, y, gp_x, gp_y, dt, mode=REC_DISPLACE
     EW.records()) as a USGS text file, byte for byte as the reference does.
     Returns the status: 0, or NOT_SUPPORTED (header only) for curl, strains and
     gradient records in geographic components."""
-    import numpy as np
-    v = np.asarray(values, dtype=np.float64)
-    if v.ndim == 1:
-        v = v.reshape(-1, 1)
-    if v.strides[1] != 8:
-        v = np.ascontiguousarray(v)
-    st = UsgsStation()
-    st.station = station.encode()
-    st.x, st.y, st.gp_x, st.gp_y = x, y, gp_x, gp_y
-    st.utc[:] = list(utc)
-    st.mode, st.xyz, st.t_shift, st.dt = mode, int(bool(xyz)), t_shift, dt
+    v = _rows(values)
+    st = _station(station, x, y, gp_x, gp_y, dt, mode, xyz, t_shift, utc)
     geo = geo_desc() if geo is None else geo
     rc = lib().sw4g_write_usgs(str(path).encode(), C.byref(geo), C.byref(st), v.ctypes.data_as(_D),
                                v.shape[0], v.strides[0] // 8)
     if rc not in (0, NOT_SUPPORTED):
         check(rc, "write_usgs")
     return rc
+
+
+def _station(station, x, y, gp_x, gp_y, dt, mode, xyz, t_shift, utc):
+    st = UsgsStation()
+    st.station = station.encode()
+    st.x, st.y, st.gp_x, st.gp_y = x, y, gp_x, gp_y
+    st.utc[:] = list(utc)
+    st.mode, st.xyz, st.t_shift, st.dt = mode, int(bool(xyz)), t_shift, dt
+    return st
+
+
+def _rows(values):
+    import numpy as np
+    v = np.asarray(values, dtype=np.float64)
+    if v.ndim == 1:
+        v = v.reshape(-1, 1)
+    if v.strides[1] != 8:
+        v = np.ascontiguousarray(v)
+    return v
+
+
+def write_sac(prefix, values, *, station, x, y, dt, mode=REC_DISPLACEMENT, xyz=True, t_shift=0.0,
+              utc=(1970, 1, 1, 0, 0, 0, 0), event=(0.0, 0.0, 0.0, 0.0), geo=None,
+              flush_subnormals=False) -> None:
+    """Writes one receiver's records as binary SAC files prefix + suffix (one per
+    value of the mode), as the reference does.  event = (lat, lon, depth m, origin
+    time offset s); flush_subnormals writes FP32 subnormal samples as signed zeros
+    (a flush-to-zero build of the reference)."""
+    v = _rows(values)
+    st = _station(station, x, y, x, y, dt, mode, xyz, t_shift, utc)
+    ev = SacEvent(*event)
+    geo = geo_desc() if geo is None else geo
+    check(lib().sw4g_write_sac(str(prefix).encode(), C.byref(geo), C.byref(st), C.byref(ev),
+                               v.ctypes.data_as(_D), v.shape[0], v.strides[0] // 8, int(bool(flush_subnormals))),
+          "write_sac")
 
 
 def set_stage_chunks(chunks=0) -> None:

@@ -72,6 +72,40 @@ def main(root):
                  deck=f"pytest/reference/{deck}")
         meta[name] = p
     (HERE / "usgs_meta.json").write_text(json.dumps(meta, indent=1, sort_keys=True) + "\n")
+    sac_fixtures(Path(root) / "tests")
+
+
+# SAC traces stored beside the USGS file of the same run under the reference's
+# tests/ (binary, written by TimeSeries::write_sac_format, src/TimeSeries.C:826):
+# the traces are kept whole, the run's record values (the USGS file's columns) as
+# compressed FP64, and the deck's grid, time, receiver and first source.  The stored
+# headers name the event either as the source (EVLA, EVLO, EVDP, O) or as zeros
+# (the reference source zeroes it before writing, src/TimeSeries.C:430); "event"
+# says which.
+SAC = [("loh1_h100_sta10", "loh1/loh1-h100-sta10", "loh1/LOH.1-h100.in"),
+       ("loh2_h100_sta10", "loh2/loh2-h100-sta10", "loh2/LOH.2-h100.in")]
+
+
+def sac_fixtures(tests):
+    import numpy as np
+    meta = {}
+    for name, run, deck in SAC:
+        text = (tests / run / "sta10.txt").read_text()
+        lines = text.splitlines()
+        head = [l for l in lines if l.startswith("#")]
+        vals = np.array([[float(v) for v in l.split()[1:]] for l in lines[len(head):]])
+        np.savez_compressed(HERE / f"sac_{name}_records.npz", records=vals)
+        for c in "xyz":
+            (HERE / f"sac_{name}.{c}").write_bytes((tests / run / f"sta10.{c}").read_bytes())
+        d = (tests / deck).read_text()
+        p = deck_params(d, "sta10")
+        src = _tokens([l for l in d.splitlines() if l.strip().startswith("source ")][0])
+        evla = np.frombuffer((tests / run / "sta10.x").read_bytes()[35 * 4:36 * 4], dtype="<f4")[0]
+        p.update(date=[l for l in head if l.startswith("# Date:")][0], rows=len(vals),
+                 source_xyz=[float(src["x"]), float(src["y"]), float(src["z"])], source_t0=float(src["t0"]),
+                 event="source" if evla != 0 else "zero", run=f"tests/{run}", deck=f"tests/{deck}")
+        meta[name] = p
+    (HERE / "sac_meta.json").write_text(json.dumps(meta, indent=1, sort_keys=True) + "\n")
 
 
 if __name__ == "__main__":

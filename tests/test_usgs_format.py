@@ -153,3 +153,97 @@ def test_errors(tmp_path):
         sg.write_usgs(tmp_path / "x.txt", np.zeros((2, 3)), mode=9, **st)
     with pytest.raises(sg.Sw4gError, match="status 1"):  # rows closer than the mode's values
         sg.write_usgs(tmp_path / "x.txt", np.zeros((2, 2)), **st)
+
+
+# ---------------------------------------------------------------------------
+# Binary SAC traces (sw4g_write_sac) against the reference's stored traces
+# tests/loh1/loh1-h100-sta10/sta10.[xyz] and tests/loh2/loh2-h100-sta10/sta10.[xyz]
+# (TimeSeries::write_sac_format, src/TimeSeries.C:826, with the SAC header library
+# src/sacsubc.C), given the same run's record values (its USGS file's columns).
+SAC_META = json.loads((GOLDEN / "sac_meta.json").read_text())
+# The two stored runs come from different builds: the LOH.1 traces hold signed zeros
+# where the records round to FP32 subnormals (a flush-to-zero build; 13-15 samples per
+# trace), the LOH.2 traces hold the subnormals themselves (8-9 per trace).
+SAC_FLUSH = {"loh1_h100_sta10": True, "loh2_h100_sta10": False}
+# ... and different longitude origins: +118 for LOH.1, the source's default -118 for
+# LOH.2 (the "Target location" of each run's own USGS file: 118.2594 and -117.7406).
+SAC_LON0 = {"loh1_h100_sta10": 118.0, "loh2_h100_sta10": -118.0}
+
+
+def _utc_of(date_line):
+    return _utc([date_line])
+
+
+@pytest.mark.parametrize("name", sorted(SAC_META))
+def test_sac_writer_reproduces_reference_traces(name, tmp_path):
+    m = SAC_META[name]
+    rec = np.load(GOLDEN / f"sac_{name}_records.npz")["records"]
+    assert rec.shape == (m["rows"], 3)
+    geo = sg.geo_desc(lon_origin=SAC_LON0[name])
+    if m["event"] == "source":
+        sx, sy, sz = m["source_xyz"]
+        lon, lat = sg.geographic_coord(geo, sx, sy)
+        event = (lat, lon, sz, m["source_t0"])
+    else:
+        event = (0.0, 0.0, 0.0, 0.0)
+    sg.write_sac(tmp_path / "sta10.", rec, station="sta10", x=m["x"], y=m["y"], dt=m["t"] / (m["rows"] - 1),
+                 utc=_utc_of(m["date"]), event=event, geo=geo, flush_subnormals=SAC_FLUSH[name])
+    for c in "xyz":
+        mine = (tmp_path / f"sta10.{c}").read_bytes()
+        ref = (GOLDEN / f"sac_{name}.{c}").read_bytes()
+        assert len(mine) == len(ref) == 632 + 4 * m["rows"]
+        assert mine == ref, c
+
+
+def _sac(path):
+    b = Path(path).read_bytes()
+    return (np.frombuffer(b[:280], "<f4"), np.frombuffer(b[280:440], "<i4"),
+            [b[440 + 8 * q:448 + 8 * q].decode() for q in range(24)], np.frombuffer(b[632:], "<f4"))
+
+
+@pytest.mark.parametrize("mode,xyz,files", [
+    (sg.REC_DISPLACEMENT, False, [("e", "EW", 90, 90), ("n", "NS", 90, 0), ("u", "UP", 0, 0)]),
+    (sg.REC_VELOCITY, True, [("xv", "Vx", 90, 30), ("yv", "Vy", 90, 120), ("zv", "Vz", 180, 0)]),
+    (sg.REC_VELOCITY, False, [("ev", "Vew", 90, 90), ("nv", "Vns", 90, 0), ("uv", "Vup", 0, 0)]),
+    (sg.REC_DIV, True, [("div", "Div", 90, 30)]),
+    (sg.REC_CURL, False, [("curlx", "Curlx", 90, 30), ("curly", "Curly", 90, 120), ("curlz", "Curlz", 180, 0)]),
+    (sg.REC_STRAINS, True, [("xx", "Uxx", 90, 30), ("yy", "Uyy", 90, 120), ("zz", "Uzz", 180, 0),
+                            ("xy", "Uxy", 90, 30), ("xz", "Uxz", 90, 30), ("yz", "Uyz", 90, 30)]),
+    (sg.REC_GRADIENT, True, [("duxdx", "DUXDX", 90, 30), ("duxdy", "DUXDY", 90, 30), ("duxdz", "DUXDZ", 90, 30),
+                             ("duydx", "DUYDX", 90, 30), ("duydy", "DUYDY", 90, 120), ("duydz", "DUYDZ", 90, 30),
+                             ("duzdx", "DUZDX", 90, 30), ("duzdy", "DUZDY", 90, 30), ("duzdz", "DUZDZ", 180, 0)]),
+])
+def test_sac_modes(mode, xyz, files, tmp_path):
+    """Every mode's files, names, inclinations and azimuths (src/TimeSeries.C:450-822),
+    grid azimuth 30; geographic displacement, velocity and curl rotated from the FP32
+    values (src/TimeSeries.C:704-713)."""
+    geo = sg.geo_desc(az=30.0)
+    n = len(files)
+    rng = np.random.default_rng(11)
+    v = rng.standard_normal((9, n))
+    x, y = 3000.0, 4000.0
+    sg.write_sac(tmp_path / "r.", v, station="station12345", x=x, y=y, dt=0.25, t_shift=-0.5, mode=mode,
+                 xyz=xyz, utc=(2016, 12, 15, 17, 41, 34, 7), event=(1.0, 2.0, 3000.0, 0.5), geo=geo)
+    f32 = v.astype(np.float32)
+    if not xyz and mode in (sg.REC_DISPLACEMENT, sg.REC_VELOCITY, sg.REC_CURL):
+        _, lat = sg.geographic_coord(geo, x, y)
+        ca, sa = math.cos(math.pi * 30 / 180.0), math.sin(math.pi * 30 / 180.0)
+        d = (x * sa + y * ca) / math.cos(math.pi * lat / 180.0) / geo.meters_per_degree * (math.pi / 180.0) \
+            * math.sin(math.pi * lat / 180.0)
+        tx, ty = sa + d * ca, ca - d * sa
+        nrm = math.sqrt(tx * tx + ty * ty)
+        tx, ty = tx / nrm, ty / nrm
+        u0, u1, u2 = (f32[:, c].astype(np.float64) for c in range(3))
+        f32 = np.stack([(sa * u0 + ca * u1), (ty * u0 - tx * u1), -u2], axis=1).astype(np.float32)
+    for c, (suffix, name, inc, az) in enumerate(files):
+        fh, ih, kh, data = _sac(tmp_path / f"r.{suffix}")
+        assert np.array_equal(data, f32[:, c])
+        assert kh[20] == f"{name:<8}"[:8] and kh[0] == "station1"
+        assert (fh[58], fh[57]) == (np.float32(inc), np.float32(az))
+        assert (fh[0], fh[5], fh[6], fh[7]) == (np.float32(0.25), np.float32(-0.5), np.float32(1.5), np.float32(0.5))
+        assert (fh[1], fh[2]) == (f32[:, c].min(), f32[:, c].max())
+        assert fh[56] == np.float32(f32[:, c].astype(np.float64).sum() / 9)
+        assert (fh[35], fh[36], fh[38]) == (np.float32(1.0), np.float32(2.0), np.float32(3.0))
+        assert list(ih[:10]) == [2016, 350, 17, 41, 34, 7, 6, 0, 0, 9]
+        assert (ih[15], ih[35], ih[36], ih[37], ih[38], ih[39]) == (1, 1, 0, 1, 1, 0)
+        assert kh[1] == "-12345  "
