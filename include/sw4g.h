@@ -478,6 +478,11 @@ int sw4g_ew_profile_kernels(sw4g_ew* ew, int nrep, double* ms);
  * splits its planes into, for all objects of the process; 0 restores the automatic
  * choice (the count that fills the GPU's SMs in whole waves). */
 int sw4g_dev_set_stage_chunks(int chunks);
+/* Tuning (no reference counterpart): the planes per k chunk that the automatic
+ * choice gives a stage kernel of `cols` CTA columns over nk planes with `resident`
+ * CTAs per SM on the current device's SMs (152 when no device answers), at least
+ * min_planes planes per chunk where nk allows.  Host arithmetic only. */
+int sw4g_dev_stage_kchunk(long long cols, int nk, int resident, int min_planes, int* planes);
 
 /* Arithmetic throughput probe (no reference counterpart): FMA chains on every SM
  * in FP64 (precision=64) or FP32 (32); writes TFLOP/s.  Synchronises the stream. */

@@ -153,6 +153,7 @@ _SIGS = {
     "sw4g_ew_launches_per_step": ([_VP, C.c_int], C.c_int),
     "sw4g_ew_profile_kernels": ([_VP, C.c_int, _D], C.c_int),
     "sw4g_dev_set_stage_chunks": ([C.c_int], C.c_int),
+    "sw4g_dev_stage_kchunk": ([C.c_longlong, C.c_int, C.c_int, C.c_int, _I], C.c_int),
     "sw4g_geo_default": ([C.POINTER(GeoDesc)], C.c_int),
     "sw4g_geographic_coord": ([C.POINTER(GeoDesc), C.c_double, C.c_double, _D, _D], C.c_int),
     "sw4g_write_usgs": ([C.c_char_p, C.POINTER(GeoDesc), C.POINTER(UsgsStation), _D, C.c_longlong,
@@ -580,6 +581,13 @@ def write_sac(prefix, values, *, station, x, y, dt, mode=REC_DISPLACEMENT, xyz=T
     check(lib().sw4g_write_sac(str(prefix).encode(), C.byref(geo), C.byref(st), C.byref(ev),
                                v.ctypes.data_as(_D), v.shape[0], v.strides[0] // 8, int(bool(flush_subnormals))),
           "write_sac")
+
+
+def stage_kchunk(cols, nk, resident, min_planes=12) -> int:
+    """Planes per k chunk of the automatic stage launch shape."""
+    p = C.c_int()
+    check(lib().sw4g_dev_stage_kchunk(cols, nk, resident, min_planes, C.byref(p)), "stage_kchunk")
+    return p.value
 
 
 def set_stage_chunks(chunks=0) -> None:

@@ -675,6 +675,13 @@ int sw4g_dev_set_stage_chunks(int chunks)
    return SW4G_OK;
 }
 
+int sw4g_dev_stage_kchunk(long long cols, int nk, int resident, int min_planes, int* planes)
+{
+   if (!planes || cols < 1 || nk < 1 || resident < 1 || min_planes < 1) return SW4G_BAD_ARGUMENT;
+   *planes = stage_kchunk(cols, nk, resident, min_planes);
+   return SW4G_OK;
+}
+
 int sw4g_fma_peak(int precision, double* tflops, void* stream)
 {
    if (!tflops || (precision != 64 && precision != 32)) return SW4G_BAD_ARGUMENT;
