@@ -6,7 +6,7 @@ operator.  Tolerances:
   * level storage round trip (FP64 -> double-float -> FP64): 1e-14 relative;
   * one step from smooth data: 1e-6 relative to the field maximum;
   * 120 steps with sources, free surface and supergrid: relative L2 error
-    <= 1e-5 against the FP64 form (the benchmark spec accuracy bar).
+    <= 1e-5 against the FP64 form (the mixed form's stated accuracy bar).
 """
 import numpy as np
 import pytest
