@@ -247,3 +247,17 @@ def test_sac_modes(mode, xyz, files, tmp_path):
         assert list(ih[:10]) == [2016, 350, 17, 41, 34, 7, 6, 0, 0, 9]
         assert (ih[15], ih[35], ih[36], ih[37], ih[38], ih[39]) == (1, 1, 0, 1, 1, 0)
         assert kh[1] == "-12345  "
+
+
+def test_sac_errors(tmp_path):
+    kw = dict(station="s", x=0.0, y=0.0, dt=0.1)
+    with pytest.raises(sg.Sw4gError, match="status 6"):  # no such directory
+        sg.write_sac(tmp_path / "missing" / "r.", np.zeros((2, 3)), **kw)
+    with pytest.raises(sg.Sw4gError, match="status 1"):  # unknown mode
+        sg.write_sac(tmp_path / "r.", np.zeros((2, 3)), mode=7, **kw)
+    with pytest.raises(sg.Sw4gError, match="status 1"):  # rows closer than the mode's values
+        sg.write_sac(tmp_path / "r.", np.zeros((2, 2)), **kw)
+    # no rows: header-only traces with NPTS 0 and the mean unset
+    sg.write_sac(tmp_path / "e.", np.zeros((0, 1)), mode=sg.REC_DIV, **kw)
+    fh, ih, _, data = _sac(tmp_path / "e.div")
+    assert ih[9] == 0 and fh[56] == np.float32(-12345.0) and data.size == 0
