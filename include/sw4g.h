@@ -11,8 +11,12 @@
  *   - all field pointers are DEVICE pointers owned by the caller unless a
  *     function says otherwise; small tables (wind, bccnd, onesided, sbop) are
  *     host pointers;
- *   - `stream` is a cudaStream_t (NULL = legacy default stream); every call only
- *     enqueues work on it, never synchronises the host and never allocates.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  The
+ *     kernel-level and phase-level calls only enqueue work on it: they never
+ *     synchronise the host and never allocate.  The time-loop object
+ *     (sw4g_ew_*) allocates its device state when it is created and when a
+ *     call sizes it (receivers, sources, the gradient's checkpoint and segment
+ *     buffers); the calls that synchronise or allocate say so.
  * Every function returns an sw4g_status (0 = success); none aborts or exits,
  * where the reference would CHECK_ERROR -> exit(0) or MPI_Abort.
  */
@@ -196,9 +200,11 @@ int sw4g_corr_rows(int ifirst, int ilast, int jfirst, int jlast, int kfirst, int
  * planes return SW4G_BAD_ARGUMENT without device work.  All calls on a device
  * share the array, so calls that overlap on the GPU race; serialise them on
  * one stream.  Every scratch element the call reads it writes first, so the
- * array carries no state between calls.  The first call on each device looks up
- * the array's address (cudaGetSymbolAddress) with that device current; make it
- * before capturing a stream into a CUDA graph. */
+ * array carries no state between calls.  Every call looks up the array's
+ * address (cudaGetSymbolAddress) with the current device, so a device reset
+ * between calls does no harm; the first call on a device also loads the
+ * library's device code there, so make it before capturing a stream into a
+ * CUDA graph. */
 int sw4g_corr_rows_noalloc(int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
                            int nz, int side, double* out, const double* up, const double* u,
                            const double* um, const double* mu, const double* lambda,
@@ -299,6 +305,27 @@ int sw4g_ew_get_fields(const sw4g_ew* ew, double* u, double* um, int on_device);
 double* sw4g_ew_field(const sw4g_ew* ew, int which);
 /* advance nsteps time steps */
 int sw4g_ew_step(sw4g_ew* ew, int nsteps, int mode);
+/* Non-finite check of the time loop; replaces the reference's checkfornan option
+ * (src/EW.C:1333) with EW::check_for_nan_GPU / check_nan_dev (src/EW_cuda.C:652,
+ * src/device-routines.C:8279) after the phases of timesteploop (src/EW.C:2544-2759).
+ * every > 0: after every `every`-th step, and after the last step of each
+ * sw4g_ew_step call, the new level of every grid is scanned on the device for NaN
+ * and infinite values; sw4g_ew_step then synchronises the stream and returns
+ * SW4G_NAN_DETECTED after the first checked step that holds one, with the object at
+ * that step (the reference prints and goes on).  every = 0 (the default) turns the
+ * check off; the time loop then never synchronises. */
+int sw4g_ew_set_nan_check(sw4g_ew* ew, int every);
+/* The last detection: grid (0 Cartesian, 1 curvilinear, -1 none), the first offending
+ * entry in storage order as component c (0-based) and point (i, j, k) in the grid's
+ * 1-based bounds, the number of non-finite entries, and the time of that level. */
+int sw4g_ew_nan_report(const sw4g_ew* ew, int* grid, int* c, int* i, int* j, int* k,
+                       long long* count, double* t);
+/* Synchronises the object's stream and returns SW4G_TIMEOUT if one of its kernels
+ * gave up a bounded wait since the last call (the FP32-mixed tensor-copy stage
+ * kernels wait at most one second for each plane's data; their CTAs then stop and
+ * the level they write is incomplete), else SW4G_OK.  sw4g_ew_step with the
+ * non-finite check on and sw4g_ew_gradient in the FP32-mixed form report it too. */
+int sw4g_ew_status(sw4g_ew* ew);
 
 /* Discrete adjoint (no reference counterpart: sw4lite computes source-parameter
  * gradients only, src/GridPointSource.C:659-760).  Runs nsteps fused FP64 steps
@@ -467,27 +494,6 @@ int sw4g_write_sac(const char* prefix, const sw4g_geo* geo, const sw4g_usgs_stat
 int sw4g_ew_enforce_bc(sw4g_ew* ew, double* u);
 /* kernel launches one step enqueues */
 int sw4g_ew_launches_per_step(const sw4g_ew* ew, int mode);
-/* Per-kernel device time of a fused step (CUDA events on the EW stream), each
- * piece launched nrep times on the current levels without advancing time; the
- * counterpart of the reference's phase timers (src/EW.C:2863-2873, reporttiming):
- * ms[0] predictor stage kernel, ms[1] corrector stage kernel, ms[2] one-sided
- * rows, ms[3] boundary conditions and forcing.  Synchronises the stream. */
-int sw4g_ew_profile_kernels(sw4g_ew* ew, int nrep, double* ms);
-
-/* Tuning (no reference counterpart): the number of k chunks every stage kernel
- * splits its planes into, for all objects of the process; 0 restores the automatic
- * choice (the count that fills the GPU's SMs in whole waves). */
-int sw4g_dev_set_stage_chunks(int chunks);
-/* Tuning (no reference counterpart): the planes per k chunk that the automatic
- * choice gives a stage kernel of `cols` CTA columns over nk planes with `resident`
- * CTAs per SM on the current device's SMs (152 when no device answers), at least
- * min_planes planes per chunk where nk allows.  Host arithmetic only. */
-int sw4g_dev_stage_kchunk(long long cols, int nk, int resident, int min_planes, int* planes);
-
-/* Arithmetic throughput probe (no reference counterpart): FMA chains on every SM
- * in FP64 (precision=64) or FP32 (32); writes TFLOP/s.  Synchronises the stream. */
-int sw4g_fma_peak(int precision, double* tflops, void* stream);
-
 #ifdef __cplusplus
 }
 #endif

@@ -36,6 +36,15 @@ def _ip(a):
     return a, a.ctypes.data_as(_I)
 
 
+def reference_src():
+    """The reference's source directory as the oracle recipe resolves it
+    (SW4_REFERENCE_SRC, else the recipe's default), or None where it is absent."""
+    r = subprocess.run(["make", "-s", "-C", str(HERE), "print-ref-src"], capture_output=True,
+                       text=True)
+    path = r.stdout.strip() if r.returncode == 0 else ""
+    return path if path and os.path.isdir(path) else None
+
+
 def build(ref: bool = False) -> None:
     """Build liboracle.so (and the reference kernels when asked and possible)."""
     target = "ref" if ref else "all"

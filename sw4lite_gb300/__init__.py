@@ -17,6 +17,7 @@ from pathlib import Path
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libsw4g.so"
 HEADER = _PKG.parent / "include" / "sw4g.h"
+DEV_HEADER = _PKG.parent / "include" / "sw4g_dev.h"
 
 _lib = None
 
@@ -27,6 +28,15 @@ _VP = C.c_void_p
 
 class Sw4gError(RuntimeError):
     pass
+
+
+class NonFiniteError(Sw4gError):
+    """A step's new level held NaN or infinite values (SW4G_NAN_DETECTED); .report is
+    the object's nan_report() dict."""
+
+    def __init__(self, msg, report):
+        super().__init__(msg)
+        self.report = report
 
 
 class GridDesc(C.Structure):
@@ -137,6 +147,9 @@ _SIGS = {
     "sw4g_ew_get_fields": ([_VP, _VP, _VP, C.c_int], C.c_int),
     "sw4g_ew_field": ([_VP, C.c_int], _VP),
     "sw4g_ew_step": ([_VP, C.c_int, C.c_int], C.c_int),
+    "sw4g_ew_set_nan_check": ([_VP, C.c_int], C.c_int),
+    "sw4g_ew_nan_report": ([_VP, _I, _I, _I, _I, _I, C.POINTER(C.c_longlong), _D], C.c_int),
+    "sw4g_ew_status": ([_VP], C.c_int),
     "sw4g_ew_enforce_bc": ([_VP, _VP], C.c_int),
     "sw4g_rhs4sgcurv": ([C.c_int] * 7 + [_I] + [_VP] * 8 + [_VP], C.c_int),
     "sw4g_metric": ([C.c_int] * 7 + [C.c_double, _VP, _VP, _VP, _VP], C.c_int),
@@ -153,6 +166,7 @@ _SIGS = {
     "sw4g_ew_launches_per_step": ([_VP, C.c_int], C.c_int),
     "sw4g_ew_profile_kernels": ([_VP, C.c_int, _D], C.c_int),
     "sw4g_dev_set_stage_chunks": ([C.c_int], C.c_int),
+    "sw4g_dev_set_mixed_tma": ([C.c_int], C.c_int),
     "sw4g_dev_stage_kchunk": ([C.c_longlong, C.c_int, C.c_int, C.c_int, _I], C.c_int),
     "sw4g_geo_default": ([C.POINTER(GeoDesc)], C.c_int),
     "sw4g_geographic_coord": ([C.POINTER(GeoDesc), C.c_double, C.c_double, _D, _D], C.c_int),
@@ -160,7 +174,6 @@ _SIGS = {
                          C.c_longlong], C.c_int),
     "sw4g_write_sac": ([C.c_char_p, C.POINTER(GeoDesc), C.POINTER(UsgsStation), C.POINTER(SacEvent), _D,
                         C.c_longlong, C.c_longlong, C.c_int], C.c_int),
-    "sw4g_fma_peak": ([C.c_int, _D, _VP], C.c_int),
     "sw4g_corr_rows_scratch_len": ([C.c_int] * 4, C.c_longlong),
     "sw4g_pred_rows": ([C.c_int] * 8 + [_VP] * 9 + [C.c_double, C.c_double, _VP], C.c_int),
     "sw4g_corr_rows": ([C.c_int] * 8 + [_VP] * 16 + [C.c_double] * 3 + [_VP, C.c_longlong, _VP],
@@ -197,9 +210,10 @@ def check(status: int, what: str = "") -> None:
 
 
 def header_functions() -> list[str]:
-    """Names of every function the C ABI header declares."""
+    """Names of every function the C ABI headers declare (the drop-in header and
+    the developer header)."""
     import re
-    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text() + DEV_HEADER.read_text(), flags=re.S)
     return sorted(set(re.findall(r"\b(sw4g_[a-z0-9_]+)\s*\(", text)))
 
 
@@ -211,6 +225,7 @@ def stencil_coefficients():
 
 
 FP64, MIXED = 0, 1
+OK, BAD_ARGUMENT, CUDA_ERROR, NAN_DETECTED, NOT_SUPPORTED, TIMEOUT, IO_ERROR = range(7)
 
 
 def grid_desc(nx, ny, nz, h, bc=(SUPERGRID,) * 4 + (FREE, SUPERGRID), zmin=0.0, sg_gp=20,
@@ -393,7 +408,29 @@ class EW:
         return lib().sw4g_ew_field(self._h, which)
 
     def step(self, nsteps=1, mode=MODE_FUSED):
-        check(lib().sw4g_ew_step(self._h, nsteps, mode), "step")
+        st = lib().sw4g_ew_step(self._h, nsteps, mode)
+        if st == NAN_DETECTED:
+            r = self.nan_report()
+            raise NonFiniteError(f"step: {r['count']} non-finite values on grid {r['grid']}, first "
+                                 f"at component {r['c']} point {r['ijk']} (t = {r['t']})", r)
+        check(st, "step")
+
+    def set_nan_check(self, every=1):
+        """Scan the new level for NaN/Inf every `every` steps (0: off)."""
+        check(lib().sw4g_ew_set_nan_check(self._h, int(every)), "set_nan_check")
+
+    def nan_report(self) -> dict:
+        v = [C.c_int() for _ in range(5)]
+        cnt, t = C.c_longlong(), C.c_double()
+        check(lib().sw4g_ew_nan_report(self._h, *[C.byref(x) for x in v], C.byref(cnt), C.byref(t)),
+              "nan_report")
+        return {"grid": v[0].value, "c": v[1].value, "ijk": (v[2].value, v[3].value, v[4].value),
+                "count": cnt.value, "t": t.value}
+
+    def status(self) -> int:
+        """Synchronises the object's stream; SW4G status of its bounded waits (0 or
+        TIMEOUT)."""
+        return lib().sw4g_ew_status(self._h)
 
     def enforce_bc(self, u):
         with self._ordered(u):
@@ -595,8 +632,7 @@ def set_stage_chunks(chunks=0) -> None:
     check(lib().sw4g_dev_set_stage_chunks(int(chunks)), "set_stage_chunks")
 
 
-def fma_peak(precision=64, stream=None) -> float:
-    """Measured FMA throughput of this GPU in TFLOP/s (FP64 or FP32)."""
-    t = C.c_double()
-    check(lib().sw4g_fma_peak(precision, C.byref(t), _stream_ptr(stream)), "fma_peak")
-    return t.value
+def set_mixed_tma(on=True) -> None:
+    """Comparison switch: FP32-mixed stages on the tensor-copy kernels (default) or
+    on the synchronous kernels."""
+    check(lib().sw4g_dev_set_mixed_tma(1 if on else 0), "set_mixed_tma")

@@ -249,6 +249,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       }
       ms.h = g_.h;
       ms.dt = dt;
+      ms.status = reinterpret_cast<int*>(dstat_);
    }
    auto F = [](double* x) { return reinterpret_cast<float*>(x); };
    GradDF gd;
@@ -657,6 +658,8 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       if (st == kOk)
          st = cuda_ok(cudaMemcpyAsync(g_la, gl_d, npts_ * sizeof(double), cudaMemcpyDeviceToHost, stream_));
    }
+   // the mixed form's tensor-copy stages report a wait that gave up in the status block
+   if (st == kOk && mixed_) st = status();
    cleanup();
    if (st != kOk) drop_grad_cache();
    return st;

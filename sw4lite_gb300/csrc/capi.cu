@@ -283,7 +283,7 @@ int sw4g_bcfortsg(int soa, int ib, int ie, int jb, int je, int kb, int ke, const
 long long sw4g_corr_rows_scratch_len(int ifirst, int ilast, int jfirst, int jlast)
 {
    if (ilast < ifirst || jlast < jfirst) return 0;
-   return 3LL * 10 * (ilast - ifirst + 1) * (long long)(jlast - jfirst + 1);
+   return 3LL * 10 * ((long long)ilast - ifirst + 1) * ((long long)jlast - jfirst + 1);
 }
 
 namespace {
@@ -651,6 +651,31 @@ int sw4g_ew_step(sw4g_ew* ew, int nsteps, int mode)
    return ew ? ew->impl->step(nsteps, mode) : SW4G_BAD_ARGUMENT;
 }
 
+int sw4g_ew_set_nan_check(sw4g_ew* ew, int every)
+{
+   return ew ? ew->impl->set_nan_check(every) : SW4G_BAD_ARGUMENT;
+}
+
+int sw4g_ew_nan_report(const sw4g_ew* ew, int* grid, int* c, int* i, int* j, int* k,
+                       long long* count, double* t)
+{
+   if (!ew || !grid || !c || !i || !j || !k || !count || !t) return SW4G_BAD_ARGUMENT;
+   const sw4g::EW::NanReport& r = ew->impl->nan_report();
+   *grid = r.grid;
+   *c = r.c;
+   *i = r.i;
+   *j = r.j;
+   *k = r.k;
+   *count = r.count;
+   *t = r.t;
+   return SW4G_OK;
+}
+
+int sw4g_ew_status(sw4g_ew* ew)
+{
+   return ew ? ew->impl->status() : SW4G_BAD_ARGUMENT;
+}
+
 int sw4g_ew_enforce_bc(sw4g_ew* ew, double* u)
 {
    if (!ew || !u) return SW4G_BAD_ARGUMENT;
@@ -675,17 +700,18 @@ int sw4g_dev_set_stage_chunks(int chunks)
    return SW4G_OK;
 }
 
+int sw4g_dev_set_mixed_tma(int on)
+{
+   if (on != 0 && on != 1) return SW4G_BAD_ARGUMENT;
+   set_mixed_tma(on);
+   return SW4G_OK;
+}
+
 int sw4g_dev_stage_kchunk(long long cols, int nk, int resident, int min_planes, int* planes)
 {
    if (!planes || cols < 1 || nk < 1 || resident < 1 || min_planes < 1) return SW4G_BAD_ARGUMENT;
    *planes = stage_kchunk(cols, nk, resident, min_planes);
    return SW4G_OK;
-}
-
-int sw4g_fma_peak(int precision, double* tflops, void* stream)
-{
-   if (!tflops || (precision != 64 && precision != 32)) return SW4G_BAD_ARGUMENT;
-   return fma_peak(precision, tflops, as_stream(stream));
 }
 
 }  // extern "C"

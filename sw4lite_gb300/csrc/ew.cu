@@ -25,6 +25,7 @@ EW::~EW()
       if (p) cudaFree(p);
    };
    f(dclock_);
+   f(dstat_);
    f(rho_);
    f(mu_);
    f(la_);
@@ -81,6 +82,11 @@ int EW::init()
    prof_ = supergrid_profiles(g_);
 
    const size_t n = (size_t)npts_;
+   SW4G_TRY(cuda_ok(cudaMalloc(&dstat_, 4 * sizeof(unsigned long long))));
+   {
+      const unsigned long long init[4] = {0, 0, ~0ull, 0};
+      SW4G_TRY(cuda_ok(cudaMemcpy(dstat_, init, sizeof init, cudaMemcpyHostToDevice)));
+   }
    SW4G_TRY(cuda_ok(cudaMalloc(&rho_, n * sizeof(double))));
    SW4G_TRY(cuda_ok(cudaMalloc(&mu_, n * sizeof(double))));
    SW4G_TRY(cuda_ok(cudaMalloc(&la_, n * sizeof(double))));
@@ -479,9 +485,81 @@ int EW::step(int nsteps, int mode)
       SW4G_TRY(record(lev_[iu_], lev_[ium_], 1));
       rec_initial_ = false;
    }
-   if (mode == kModeFused && graphs_) return run_graphed(nsteps);
-   for (int n = 0; n < nsteps; n++) SW4G_TRY(mode == kModePhases ? step_phases() : step_fused());
+   auto advance = [&](int k) -> int {
+      if (mode == kModeFused && graphs_) return run_graphed(k);
+      for (int n = 0; n < k; n++) SW4G_TRY(mode == kModePhases ? step_phases() : step_fused());
+      return kOk;
+   };
+   if (nan_every_ <= 0) return advance(nsteps);
+   for (int done = 0; done < nsteps;) {
+      const int k = std::min(nan_every_, nsteps - done);
+      SW4G_TRY(advance(k));
+      done += k;
+      SW4G_TRY(scan_levels());
+   }
    return kOk;
+}
+
+int EW::set_nan_check(int every)
+{
+   if (!ready_ || every < 0) return kBadArgument;
+   nan_every_ = every;
+   nan_ = NanReport{};
+   return kOk;
+}
+
+int EW::read_status(unsigned long long out[4])
+{
+   SW4G_TRY(cuda_ok(cudaMemcpyAsync(out, dstat_, 4 * sizeof(unsigned long long),
+                                    cudaMemcpyDeviceToHost, stream_)));
+   return cuda_ok(cudaStreamSynchronize(stream_));
+}
+
+int EW::status()
+{
+   if (!ready_) return kBadArgument;
+   unsigned long long h[4];
+   SW4G_TRY(read_status(h));
+   if (h[0] & (1ull << kTimeout)) {
+      const unsigned long long zero = 0;
+      SW4G_TRY(cuda_ok(cudaMemcpy(dstat_, &zero, sizeof zero, cudaMemcpyHostToDevice)));
+      return kTimeout;
+   }
+   return kOk;
+}
+
+// Scans the current level of every grid (the level the last step wrote) for NaN and
+// infinite values and reads the verdict: kNanDetected with nan_ filled in, kTimeout
+// if a kernel's bounded wait gave up, else kOk.
+int EW::scan_levels()
+{
+   const unsigned long long reset[2] = {0, ~0ull};
+   SW4G_TRY(cuda_ok(cudaMemcpyAsync(dstat_ + 1, reset, sizeof reset, cudaMemcpyHostToDevice, stream_)));
+   const long long n0 = (mixed_ ? 6 : 3) * npts_;
+   SW4G_TRY(launch_nonfinite_scan(lev_[iu_], n0, mixed_, 0, dstat_, stream_));
+   if (cv_) {
+      const long long n1 = (mixed_ ? 6 : 3) * cv_->npts;
+      SW4G_TRY(launch_nonfinite_scan(cv_->lev[iu_], n1, mixed_, 1, dstat_, stream_));
+   }
+   unsigned long long h[4];
+   SW4G_TRY(read_status(h));  // also orders the reset's host buffer before this frame ends
+   if (h[0] & (1ull << kTimeout)) return kTimeout;
+   if (h[1] == 0) return kOk;
+   const int grid = (int)(h[2] >> kScanGridShift);
+   long long off = (long long)(h[2] & ((1ull << kScanGridShift) - 1));
+   const Bounds& b = grid == 0 ? b_ : cv_->b;
+   const long long np = b.npts();
+   off %= 3 * np;  // the mixed form's lo half holds the same points
+   const long long ni = b.ie - b.ib + 1, nij = ni * (b.je - b.jb + 1);
+   const long long p = off % np;
+   nan_.grid = grid;
+   nan_.c = (int)(off / np);
+   nan_.i = b.ib + (int)(p % ni);
+   nan_.j = b.jb + (int)((p / ni) % (b.je - b.jb + 1));
+   nan_.k = b.kb + (int)(p / nij);
+   nan_.count = (long long)h[1];
+   nan_.t = t_;
+   return kNanDetected;
 }
 
 int EW::record(double* up, double* um, int initial)
@@ -823,6 +901,7 @@ int EW::mixed_piece(int piece, int ip, int iq)
       ms.dt = dt;
       ms.u = u;
       ms.um = um;
+      ms.status = reinterpret_cast<int*>(dstat_);
       if (piece == 0) {
          ms.corrector = 0;
          ms.out = up;

@@ -99,6 +99,21 @@ class EW {
    double* field_um() const { return lev_[ium_]; }
 
    int step(int nsteps, int mode);
+   // Non-finite check of the time loop (the reference's checkfornan, src/EW.C:1333,
+   // 2544-2759): every `every` steps (and after the last step of a step() call) the
+   // new level of every grid is scanned; step() then synchronises and returns
+   // kNanDetected after the first checked step that holds a NaN or an infinity, with
+   // the object at that step.  0 turns the check off (the default).
+   int set_nan_check(int every);
+   struct NanReport {
+      int grid = -1, c = 0, i = 0, j = 0, k = 0;
+      long long count = 0;
+      double t = 0;
+   };
+   const NanReport& nan_report() const { return nan_; }
+   // Synchronises the object's stream and returns kTimeout if a kernel's bounded wait
+   // gave up since the last call (clearing the flag), else kOk.
+   int status();
    // CUDA graphs for the fused time loop: when on, step() replays captured chunks of
    // kGraphSteps steps (a multiple of the level rotation's period 3) and gradient()
    // replays its forward chunks, recompute segments and adjoint segments; the forcing
@@ -163,6 +178,8 @@ class EW {
 
  private:
    int upload_sources();
+   int scan_levels();                 // non-finite scans of the current levels, then the verdict
+   int read_status(unsigned long long out[4]);
    int record(double* up, double* um, int initial);
    int step_phases();
    int step_fused();
@@ -255,6 +272,9 @@ class EW {
    int* stage_emax_ = nullptr;        // gradient(): exponent maximum of the corrector's levels
 
    double t_ = 0, dt_ = 0;
+   unsigned long long* dstat_ = nullptr;  // status block (kernels.h): flags, count, first offset
+   int nan_every_ = 0;
+   NanReport nan_{};
 
    bool graphs_ = false, clocked_ = false, warm_ = false;
    double* dclock_ = nullptr;  // [0] forcing time, [1] record row, [2] adjoint residual row

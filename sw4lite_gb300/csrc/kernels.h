@@ -69,6 +69,9 @@ struct MixedStage {
    // corrector 0 predictor, 1 corrector, 2 adjoint form (stage_mixed.cu); coef != 0
    // replaces the stage's dt^2 (predictor, adjoint) or dt^2/12 (corrector)
    double coef = 0;
+   // device status word: the tensor-copy kernels or in 1 << kTimeout when an
+   // mbarrier wait gives up (may be null)
+   int* status = nullptr;
 };
 
 // Device-resident grid-point sources grouped by grid point: the sources of point
@@ -277,9 +280,22 @@ int launch_force_update_f32(int soa, int ib, int ie, int jb, int je, int kb, int
                             const double* rho, const SourceSet& src, double t, int tt,
                             double coef, cudaStream_t s);
 
-int fma_peak(int precision, double* tflops, cudaStream_t s);
-
 int launch_mixed_stage(const MixedStage& st, cudaStream_t stream);
+// Status block of an EW object (device, 4 words): [0] flags (bit kTimeout: an
+// mbarrier wait gave up), [1] non-finite values found by the scans, [2] the
+// smallest offending storage offset, tagged with its grid above kScanGridShift.
+constexpr int kScanGridShift = 48;
+// Counts non-finite entries of x[0..n) (double, or float when is_float) into block.
+int launch_nonfinite_scan(const void* x, long long n, bool is_float, int grid,
+                          unsigned long long* block, cudaStream_t s);
+
+// The predictor and corrector forms fed by tensor copies (stage_mixed_tma.cu), where
+// the strides and addresses allow them; launch_mixed_stage picks this path by itself.
+bool mixed_stage_tma_ok(const MixedStage& st);
+int launch_mixed_stage_tma(const MixedStage& st, cudaStream_t stream);
+// 0 keeps launch_mixed_stage on the synchronous kernels (for comparisons), 1 the default
+void set_mixed_tma(int on);
+int mixed_tma_enabled();
 int launch_df_from_f64(long long n, const double* x, float* h, float* l, cudaStream_t s);
 // FP64 -> interleaved (hi, lo) FP32 pairs
 int launch_df2_from_f64(long long n, const double* x, float2* hl, cudaStream_t s);

@@ -19,10 +19,11 @@
 //    results; serialise them on one stream.  Every element the kernels read is
 //    written earlier in the same call, so the array keeps the previous call's
 //    contents without harm and nothing needs clearing;
-//  * the first call on each device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current; make that first call before
-//    capturing a stream into a CUDA graph.
-#include <mutex>
+//  * every call looks up the array's device address on the current device
+//    (cudaGetSymbolAddress, a host-side table lookup) instead of caching it, so
+//    an address never outlives a cudaDeviceReset or a re-created primary
+//    context; the first call on a device also loads the library's device code
+//    there, so make that first call before capturing a stream into a CUDA graph.
 
 #include "../../include/sw4g.h"
 #include "kernels.h"
@@ -37,24 +38,14 @@ constexpr long long kMaxScratchDoubles = 8LL << 20;  // 64 MiB of doubles
 // cudaGetSymbolAddress below.
 static __device__ __align__(256) double g_corr_rows_scratch[kMaxScratchDoubles];
 
-constexpr int kMaxDevices = 64;
-double* g_scratch_address[kMaxDevices] = {};
-std::mutex g_scratch_mutex;
-
-// Device address of the scratch array on the current device (set up once per device).
+// Device address of the scratch array on the current device, looked up afresh
+// with that device current.
 int scratch_address(double** out)
 {
-   int dev = 0;
-   if (cudaGetDevice(&dev) != cudaSuccess) return kCudaError;
-   if (dev < 0 || dev >= kMaxDevices) return kBadArgument;
-   std::lock_guard<std::mutex> lock(g_scratch_mutex);
-   if (!g_scratch_address[dev]) {
-      void* p = nullptr;
-      const cudaError_t e = cudaGetSymbolAddress(&p, g_corr_rows_scratch);
-      if (e != cudaSuccess || p == nullptr) return kCudaError;
-      g_scratch_address[dev] = static_cast<double*>(p);
-   }
-   *out = g_scratch_address[dev];
+   void* p = nullptr;
+   const cudaError_t e = cudaGetSymbolAddress(&p, g_corr_rows_scratch);
+   if (e != cudaSuccess || p == nullptr) return kCudaError;
+   *out = static_cast<double*>(p);
    return kOk;
 }
 

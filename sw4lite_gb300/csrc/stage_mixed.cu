@@ -26,6 +26,7 @@
 // to step.  One-sided rows, the free-surface ghost solve and forcing stay in
 // FP64 (rhs4_direct.cu, bc.cu, forcing.cu).
 #include <algorithm>
+#include <atomic>
 
 #include "common.cuh"
 #include "df.cuh"
@@ -584,9 +585,17 @@ int launch_to_f32(long long n, const double* x, float* y, cudaStream_t s)
    return launch_status();
 }
 
+namespace {
+std::atomic<int> g_mixed_tma{1};
+}
+
+void set_mixed_tma(int on) { g_mixed_tma.store(on ? 1 : 0); }
+int mixed_tma_enabled() { return g_mixed_tma.load(); }
+
 int launch_mixed_stage(const MixedStage& st, cudaStream_t stream)
 {
    if (st.k2 < st.k1) return kOk;
+   if (g_mixed_tma.load() && mixed_stage_tma_ok(st)) return launch_mixed_stage_tma(st, stream);
    const Box& b = st.b;
    MixedArgs a;
    a.ib = b.ib; a.ie = b.ie; a.jb = b.jb; a.je = b.je; a.kb = b.kb; a.ke = b.ke;

@@ -109,4 +109,12 @@ def sac_fixtures(tests):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) > 1:
+        main(sys.argv[1])
+    else:
+        sys.path.insert(0, str(HERE.parent.parent))
+        from oracle import oracle as O
+        src = O.reference_src()
+        if src is None:
+            sys.exit("reference tree not found: pass its root or set SW4_REFERENCE_SRC")
+        main(str(Path(src).parent))

@@ -6,21 +6,16 @@ tests skip elsewhere.  Tolerances: FP64 results agree to 1e-13 relative to the
 largest output magnitude (summation order differs); table lookups and copies
 agree bit for bit.
 """
-import os
-
 import numpy as np
 import pytest
 
 from oracle import oracle as O
 from tests.fields import Grid, rel_err
 
-REF_SRC = os.environ.get("SW4_REFERENCE_SRC", "/root/reference/src")
-
-
 @pytest.fixture(scope="module", autouse=True)
 def _ref_lib():
     if not O.ref_available():
-        if not os.path.isdir(REF_SRC):
+        if O.reference_src() is None:
             pytest.skip("reference sources not present; oracle pinned by tests/golden instead")
         O.build(ref=True)
     O.lib()
