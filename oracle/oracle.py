@@ -408,3 +408,142 @@ def solerr3(bounds, h, zmin, uex, u, x0, y0, z0, radius, region):
 
 def set_threads(n: int) -> None:
     os.environ["OMP_NUM_THREADS"] = str(n)
+
+
+# --------------------------------------------------------------------------
+# Source discretisation and a whole Cartesian problem, built from plain values
+# (no product types), for the parity tests and the CPU baseline.
+# --------------------------------------------------------------------------
+def source_weights(which, a):
+    """The 6 weights of a source at fractional position a: which 0 delta, 1 delta',
+    2 and 3 their five-point free-surface variants (sw4_oracle_src.c)."""
+    w = np.zeros(6)
+    lib().sw4o_source_weights(C.c_int(which), C.c_double(a), _dp(w))
+    return w
+
+
+def discretize_source(nx, ny, nz, h, zmin, top_onesided, bot_onesided, x, y, z, *, force=None,
+                      moment=None, cap=512):
+    """Grid-point sources of one point force or moment tensor (m: xx xy xz yy yz zz) on
+    a Cartesian grid: (ijk int32 [3n], amp [3n]) in the reference's emission order."""
+    ijk = np.zeros(3 * cap, dtype=np.int32)
+    amp = np.zeros(3 * cap)
+    f = np.asarray(force if force is not None else (0.0, 0.0, 0.0), dtype=np.float64)
+    m = np.asarray(moment if moment is not None else (0.0,) * 6, dtype=np.float64)
+    n = lib().sw4o_discretize_source(
+        C.c_int(nx), C.c_int(ny), C.c_int(nz), C.c_double(h), C.c_double(zmin),
+        C.c_int(int(top_onesided)), C.c_int(int(bot_onesided)), C.c_double(x), C.c_double(y),
+        C.c_double(z), C.c_int(int(moment is not None)), _dp(f), _dp(m), C.c_int(cap),
+        ijk.ctypes.data_as(_I), _dp(amp))
+    if n < 0:
+        raise ValueError("more grid-point sources than cap")
+    return ijk[:3 * n].copy(), amp[:3 * n].copy()
+
+
+class PointSource:
+    """A point force (force=(fx, fy, fz)) or moment tensor (moment=(xx, xy, xz, yy, yz,
+    zz)) at (x, y, z) with time function `kind` (0 Gaussian, 1 C6SmoothBump, 3
+    VerySmoothBump), frequency and offset."""
+
+    def __init__(self, x, y, z, *, force=None, moment=None, freq=1.0, t0=0.0, kind=0):
+        self.x, self.y, self.z = x, y, z
+        self.force, self.moment = force, moment
+        self.freq, self.t0, self.kind = freq, t0, kind
+
+
+class CartProblem:
+    """sw4o_problem of one Cartesian grid: nx, ny, nz interior points with 2 ghost
+    points per side, bc[6] (0 free surface, 1 Dirichlet, 2 supergrid, 3 periodic),
+    supergrid width sg_gp points with damping sg_damping and order sg_order, the
+    material over the whole array, dt, and PointSource sources discretised here."""
+
+    def __init__(self, nx, ny, nz, h, bc, rho, mu, la, dt, sources=(), *, zmin=0.0, sg_gp=20,
+                 sg_damping=0.02, sg_order=4):
+        self.nx, self.ny, self.nz, self.h, self.zmin = nx, ny, nz, h, zmin
+        self.bounds = (-1, nx + 2, -1, ny + 2, -1, nz + 2)
+        self.keep = [rho, mu, la]
+        bc = list(bc)
+        used = 2 in bc
+        prof = []
+        for ax, n, b0, b1 in [(0, nx, bc[0], bc[1]), (1, ny, bc[2], bc[3]), (2, nz, bc[4], bc[5])]:
+            if used:
+                x0 = zmin if ax == 2 else 0.0
+                p = supergrid_profile(-1, n + 2, h, x0, b0 == 2, b1 == 2, 0.0, x0 + (n - 1) * h,
+                                      sg_gp * h)
+            else:
+                p = (np.zeros(n + 4), np.ones(n + 4), np.ones(n + 4))
+            prof.append(p)
+        self.prof = prof
+        self.keep += [a for p in prof for a in p]
+        wind, _ = boundary_windows(self.bounds, (nx, ny, nz), bc)
+        P = Problem()
+        P.ib, P.ie, P.jb, P.je, P.kb, P.ke = self.bounds
+        P.nx, P.ny, P.nz = nx, ny, nz
+        P.h, P.dt = h, dt
+        for s in range(6):
+            P.bccnd[s] = bc[s]
+        P.onesided[4] = int(bc[4] == 0)
+        P.onesided[5] = int(bc[5] == 0)
+        for q in range(36):
+            P.wind[q] = int(wind[q])
+        P.sg_beta = sg_damping if used else 0.0
+        P.sg_order = sg_order
+        P.rho, P.mu, P.la = _dp(rho), _dp(mu), _dp(la)
+        P.dcx, P.strx, P.cox = [_dp(a) for a in prof[0]]
+        P.dcy, P.stry, P.coy = [_dp(a) for a in prof[1]]
+        P.dcz, P.strz, P.coz = [_dp(a) for a in prof[2]]
+        self.P = P
+        ijk, amp, freq, t0, kind = [], [], [], [], []
+        for src in sources:
+            a, b = discretize_source(nx, ny, nz, h, zmin, bc[4] == 0, bc[5] == 0, src.x, src.y, src.z,
+                                     force=src.force, moment=src.moment)
+            n = len(a) // 3
+            ijk.append(a)
+            amp.append(b)
+            freq += [src.freq] * n
+            t0 += [src.t0] * n
+            kind += [src.kind] * n
+        self.set_grid_point_sources(np.concatenate(ijk) if ijk else np.zeros(0),
+                                    np.concatenate(amp) if amp else np.zeros(0), freq, t0, kind)
+        self.npts = (nx + 4) * (ny + 4) * (nz + 4)
+
+    def set_grid_point_sources(self, ijk, amp, freq, t0, kind):
+        """Grid-point sources (flat ijk and amp, 3 per source) of this problem."""
+        self.src = (np.ascontiguousarray(ijk, dtype=np.int32).reshape(-1),
+                    np.ascontiguousarray(amp, dtype=np.float64).reshape(-1),
+                    np.asarray(freq, dtype=np.float64), np.asarray(t0, dtype=np.float64),
+                    np.asarray(kind, dtype=np.int32))
+        self.keep += list(self.src)
+        P = self.P
+        P.nsrc = len(self.src[2])
+        P.src_ijk = self.src[0].ctypes.data_as(_I)
+        P.src_amp = self.src[1].ctypes.data_as(_D)
+        P.src_freq = self.src[2].ctypes.data_as(_D)
+        P.src_t0 = self.src[3].ctypes.data_as(_D)
+        P.src_kind = self.src[4].ctypes.data_as(_I)
+
+    def run(self, u, um, t0, nsteps, which="oracle", receivers=None):
+        """nsteps steps from (u, um) (which: "oracle" the restatement, "ref" the
+        reference's kernels); with receivers [(ijk, mode), ...] also returns the record
+        rows (initial data, then one row per step)."""
+        n3 = 3 * self.npts
+        u, um = u.copy(), um.copy()
+        up, lu, f, uacc = (np.zeros(n3) for _ in range(4))
+        t = t0
+        dims = (self.nx, self.ny, self.nz)
+
+        def row(a, b, initial):
+            return np.concatenate([record(m, ijk, a, b, self.P.dt, self.h, dims, initial)
+                                   for ijk, m in receivers])
+
+        rows = [row(u, um, True)] if receivers else []
+        for _ in range(nsteps):
+            step(self.P, 1, t, up, u, um, lu, f, uacc, which=which)
+            if receivers:
+                rows.append(row(up, um, False))
+            um, u, up = u, up, um
+            t += self.P.dt
+        if receivers:
+            return u, um, np.array(rows)
+        return u, um
+

@@ -213,6 +213,16 @@ void sw4o_solerr3(int ib, int ie, int jb, int je, int kb, int ke, double h, doub
                   double radius, int imin, int imax, int jmin, int jmax, int kmin, int kmax,
                   double* li, double* l2, double* xli);
 
+/* Source discretisation on a Cartesian grid (sw4_oracle_src.c; restates the
+ * Cartesian branch of Source::set_grid_point_sources4, src/Source.C:1074-1930, and
+ * the weights of src/Source.C:553-679).  which: 0 delta, 1 delta', 2 and 3 their
+ * five-point free-surface variants.  Returns the number of grid-point sources
+ * written (ijk[3n] 1-based, amp[3n]), or -1 if more than cap. */
+void sw4o_source_weights(int which, double a, double w[6]);
+int sw4o_discretize_source(int nx, int ny, int nz, double h, double zmin, int top_onesided,
+                           int bot_onesided, double x, double y, double z, int is_moment,
+                           const double f[3], const double m[6], int cap, int* ijk, double* amp);
+
 #ifdef __cplusplus
 }
 #endif

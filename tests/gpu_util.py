@@ -64,6 +64,7 @@ def smooth_fields(nx, ny, nz, seed, scale=1e-3):
 
 
 def discretize(grid, src):
+    """The library's host discretisation of one source (the product's set-up path)."""
     cap = 4096
     ijk = np.zeros(3 * cap, dtype=np.int32)
     amp = np.zeros(3 * cap)
@@ -75,99 +76,32 @@ def discretize(grid, src):
     return ijk[:3 * n].copy(), amp[:3 * n].copy()
 
 
-class OracleProblem:
-    """The oracle's sw4o_problem for a grid, with the same material, profiles and
-    grid-point sources as a GPU EW object."""
+def oracle_source(src):
+    """An sw4g_source descriptor as the oracle's PointSource."""
+    if src.moment:
+        return O.PointSource(src.x, src.y, src.z, moment=(src.mxx, src.mxy, src.mxz, src.myy,
+                                                          src.myz, src.mzz),
+                             freq=src.freq, t0=src.t0, kind=src.kind)
+    return O.PointSource(src.x, src.y, src.z, force=(src.fx, src.fy, src.fz), freq=src.freq,
+                         t0=src.t0, kind=src.kind)
+
+
+def oracle_discretize(grid, src):
+    """The oracle's discretisation of one source on a grid descriptor's grid."""
+    p = oracle_source(src)
+    return O.discretize_source(grid.nx, grid.ny, grid.nz, grid.h, grid.zmin, grid.bc[4] == 0,
+                               grid.bc[5] == 0, p.x, p.y, p.z, force=p.force, moment=p.moment)
+
+
+class OracleProblem(O.CartProblem):
+    """The oracle's problem for a GPU grid descriptor: the same material, supergrid
+    profiles and sources, with the sources discretised by the oracle itself."""
 
     def __init__(self, grid, rho, mu, la, dt, sources=()):
+        super().__init__(grid.nx, grid.ny, grid.nz, grid.h, [grid.bc[s] for s in range(6)], rho, mu,
+                         la, dt, [oracle_source(s) for s in sources], zmin=grid.zmin,
+                         sg_gp=grid.sg_gp, sg_damping=grid.sg_damping, sg_order=grid.sg_order)
         self.g = grid
-        nx, ny, nz = grid.nx, grid.ny, grid.nz
-        self.bounds = (-1, nx + 2, -1, ny + 2, -1, nz + 2)
-        self.keep = [rho, mu, la]
-        bc = [grid.bc[s] for s in range(6)]
-        used = 2 in bc
-        prof = []
-        for ax, n, b0, b1 in [(0, nx, bc[0], bc[1]), (1, ny, bc[2], bc[3]), (2, nz, bc[4], bc[5])]:
-            if used:
-                xmax = (grid.zmin if ax == 2 else 0.0) + (n - 1) * grid.h
-                p = O.supergrid_profile(-1, n + 2, grid.h, grid.zmin if ax == 2 else 0.0, b0 == 2,
-                                        b1 == 2, 0.0, xmax, grid.sg_gp * grid.h)
-            else:
-                p = (np.zeros(n + 4), np.ones(n + 4), np.ones(n + 4))
-            prof.append(p)
-        self.prof = prof
-        self.keep += [a for p in prof for a in p]
-        wind, _ = O.boundary_windows(self.bounds, (nx, ny, nz), bc)
-        P = O.Problem()
-        P.ib, P.ie, P.jb, P.je, P.kb, P.ke = self.bounds
-        P.nx, P.ny, P.nz = nx, ny, nz
-        P.h, P.dt = grid.h, dt
-        for s in range(6):
-            P.bccnd[s] = bc[s]
-        P.onesided[4] = int(bc[4] == 0)
-        P.onesided[5] = int(bc[5] == 0)
-        for q in range(36):
-            P.wind[q] = int(wind[q])
-        P.sg_beta = grid.sg_damping if used else 0.0
-        P.sg_order = grid.sg_order
-        dp = O._dp
-        P.rho, P.mu, P.la = dp(rho), dp(mu), dp(la)
-        P.dcx, P.strx, P.cox = [dp(a) for a in prof[0]]
-        P.dcy, P.stry, P.coy = [dp(a) for a in prof[1]]
-        P.dcz, P.strz, P.coz = [dp(a) for a in prof[2]]
-        self.P = P
-        ijk, amp, freq, t0, kind = [], [], [], [], []
-        for src in sources:
-            a, b = discretize(grid, src)
-            n = len(a) // 3
-            ijk.append(a)
-            amp.append(b)
-            freq += [src.freq] * n
-            t0 += [src.t0] * n
-            kind += [src.kind] * n
-        self.set_grid_point_sources(np.concatenate(ijk) if ijk else np.zeros(0),
-                                    np.concatenate(amp) if amp else np.zeros(0), freq, t0, kind)
-        self.npts = (nx + 4) * (ny + 4) * (nz + 4)
-
-    def set_grid_point_sources(self, ijk, amp, freq, t0, kind):
-        """Grid-point sources (flat ijk and amp, 3 per source) of this problem."""
-        self.src = (np.ascontiguousarray(ijk, dtype=np.int32).reshape(-1),
-                    np.ascontiguousarray(amp, dtype=np.float64).reshape(-1),
-                    np.asarray(freq, dtype=np.float64), np.asarray(t0, dtype=np.float64),
-                    np.asarray(kind, dtype=np.int32))
-        self.keep += list(self.src)
-        P = self.P
-        P.nsrc = len(self.src[2])
-        P.src_ijk = self.src[0].ctypes.data_as(O._I)
-        P.src_amp = self.src[1].ctypes.data_as(O._D)
-        P.src_freq = self.src[2].ctypes.data_as(O._D)
-        P.src_t0 = self.src[3].ctypes.data_as(O._D)
-        P.src_kind = self.src[4].ctypes.data_as(O._I)
-
-    def run(self, u, um, t0, nsteps, which="oracle", receivers=None):
-        """nsteps oracle steps from (u, um); with receivers [(ijk, mode), ...] also
-        returns the record rows (initial data, then one row per step)."""
-        n3 = 3 * self.npts
-        u, um = u.copy(), um.copy()
-        up, lu, f, uacc = (np.zeros(n3) for _ in range(4))
-        t = t0
-        g = self.g
-        dims = (g.nx, g.ny, g.nz)
-
-        def row(a, b, initial):
-            return np.concatenate([O.record(m, ijk, a, b, self.P.dt, g.h, dims, initial)
-                                   for ijk, m in receivers])
-
-        rows = [row(u, um, True)] if receivers else []
-        for _ in range(nsteps):
-            O.step(self.P, 1, t, up, u, um, lu, f, uacc, which=which)
-            if receivers:
-                rows.append(row(up, um, False))
-            um, u, up = u, up, um
-            t += self.P.dt
-        if receivers:
-            return u, um, np.array(rows)
-        return u, um
 
 
 def solution_mask(grid):
