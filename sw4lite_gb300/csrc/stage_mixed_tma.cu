@@ -47,7 +47,7 @@ constexpr int TX = 32, TY = 8, HALO = 2;
 constexpr int PX = TX + 2 * HALO;  // 36
 constexpr int PY = TY + 2 * HALO;  // 12
 constexpr int PLANE = PX * PY;     // 432
-constexpr int NTHREADS = TX * TY * 3;  // one thread per (point, component)
+constexpr int NTHREADS = TX * TY;
 constexpr int OWNP = PX * TY;      // 288: own rows of a tile with the x halo (columns 0..35)
 
 constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s per mbarrier wait
@@ -222,11 +222,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
    const uint32_t barM0 = barF + 8;
    volatile int* abort_flag = reinterpret_cast<volatile int*>(smb + L::bar + 24);
 
-   // thread = (point tx, ty of the 32 x 8 tile, component c); a warp holds one row of
-   // 32 points of one component, so every branch on c is warp-uniform
-   const int tx = threadIdx.x, ty = threadIdx.y, c = threadIdx.z;
-   const int tid = tx + TX * (ty + TY * c);
-   const int lane = tid & 31, warp = tid >> 5;
+   const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + TX * ty;
    const int i0 = a.ib + 2 + blockIdx.x * TX;
    const int j0 = a.jb + 2 + blockIdx.y * TY;
    const int kbeg = a.k1 + blockIdx.z * a.kchunk;
@@ -236,7 +232,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
    const bool active = (i <= a.ie - 2) && (j <= a.je - 2);
    const int own = (ty + HALO) * PX + (tx + HALO);  // own point in a halo tile
    const int ownr = ty * PX + (tx + HALO);          // own point in an own-rows tile
-   const int oc = c * PLANE;                        // own component in a staged plane
    const long long npts = a.npts, lo = 3 * a.npts;
    // tensor coordinates of the CTA's tiles
    const int xt = blockIdx.x * TX;      // first column (i0 - 2) of the halo tile
@@ -247,58 +242,37 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       return (long long)(gi - a.ib) + a.ni * (gj - a.jb) + a.nij * (long long)(gk - a.kb);
    };
 
-   // ---- producer: the lanes of warp 0 each issue one tensor copy ----
-   // F(mf): stage fields of plane mf and the own mu, lambda pairs; M(mm): the
-   // once-per-plane inputs of plane mm.  A plane index below kbeg - 2 skips the group.
-   auto issue = [&](int mf, int mm) {
-      if (warp != 0) return;
-      const bool doF = mf >= kbeg - 2, doM = mm >= kbeg;
-      const uint32_t barM = barM0 + 8 * (mm & 1);
-      if (lane == 0) {
-         fence_async_shared();
-         if (doF) mbar_expect_tx(barF, L::f_tx);
-         if (doM) mbar_expect_tx(barM, M::tx_bytes);
+   // ---- producers (thread 0) ----
+   auto issue_F = [&](int m) {  // stage fields of plane m and the own mu, lambda pairs
+      const int z = m - a.kb;
+      const uint32_t slot = smem_u32(smb + L::f + (CORR ? 0 : mod6(m) * kLevHaloB));
+      mbar_expect_tx(barF, L::f_tx);
+      if (CORR) {
+         for (int q = 0; q < 3; q++) tma4(slot + q * kLevHaloB, &tm.lev_halo[q], xt, yh, z, 0, barF);
+      } else {
+         tma4(slot, &tm.lev_halo[0], xt, yh, z, 0, barF);
       }
-      __syncwarp();
-      constexpr int nF = CORR ? 5 : 3;
-      int op = lane;
-      if (op < nF) {
-         if (!doF) return;
-         const int z = mf - a.kb;
-         const uint32_t slot = smem_u32(smb + L::f + (CORR ? 0 : mod6(mf) * kLevHaloB));
-         const uint32_t fo = smem_u32(smb + L::fown);
-         if (op < nF - 2)
-            tma4(slot + op * kLevHaloB, &tm.lev_halo[op], xt, yh, z, 0, barF);
-         else if (op == nF - 2)
-            tma3(fo, &tm.mu_own, 2 * xt, yo, z, barF);
-         else
-            tma3(fo + kPairOwnB, &tm.la_own, 2 * xt, yo, z, barF);
-         return;
+      const uint32_t fo = smem_u32(smb + L::fown);
+      tma3(fo, &tm.mu_own, 2 * xt, yo, z, barF);
+      tma3(fo + kPairOwnB, &tm.la_own, 2 * xt, yo, z, barF);
+   };
+   auto issue_M = [&](int m) {  // once-per-plane inputs of plane m
+      const int z = m - a.kb;
+      const uint32_t bar = barM0 + 8 * (m & 1);
+      const uint32_t s = smem_u32(smb + ((m & 1) ? L::m1 : L::m0));
+      mbar_expect_tx(bar, M::tx_bytes);
+      tma3(s + M::mu, &tm.mu_halo, 2 * xt, yh, z, bar);
+      tma3(s + M::la, &tm.la_halo, 2 * xt, yh, z, bar);
+      if (CORR) tma3(s + M::rho, &tm.rho_halo, xt, yh, z, bar);
+      tma4(s + M::own, &tm.lev_own, xt, yo, z, 0, bar);
+      tma3(s + M::ir, &tm.ir_own, 2 * xt, yo, z, bar);
+      for (int q = 0; q < 4; q++) {
+         tma3(s + M::wx + q * kPairOwnB, &tm.wx[q], 2 * xt, yo, z, bar);
+         tma3(s + M::wy + q * kWyB, &tm.wy[q], 2 * xt, yo, z, bar);
       }
-      op -= nF;
-      if (!doM) return;
-      const int z = mm - a.kb;
-      const uint32_t s = smem_u32(smb + ((mm & 1) ? L::m1 : L::m0));
-      if (!CORR && op >= 2) op++;  // the predictor reads no rho
-      switch (op) {
-         case 0: tma3(s + M::mu, &tm.mu_halo, 2 * xt, yh, z, barM); break;
-         case 1: tma3(s + M::la, &tm.la_halo, 2 * xt, yh, z, barM); break;
-         case 2: tma3(s + M::rho, &tm.rho_halo, xt, yh, z, barM); break;
-         case 3: tma4(s + M::own, &tm.lev_own, xt, yo, z, 0, barM); break;
-         case 4: tma3(s + M::ir, &tm.ir_own, 2 * xt, yo, z, barM); break;
-         case 5: case 6: case 7: case 8:
-            tma3(s + M::wx + (op - 5) * kPairOwnB, &tm.wx[op - 5], 2 * xt, yo, z, barM);
-            break;
-         case 9: case 10: case 11: case 12:
-            tma3(s + M::wy + (op - 9) * kWyB, &tm.wy[op - 9], 2 * xt, yo, z, barM);
-            break;
-         case 13: case 14:
-            tma3(s + M::wz1 + (op - 13) * kWz1B, &tm.wz1[op - 13], 2 * xt, yo, z, barM);
-            break;
-         case 15: case 16:
-            tma3(s + M::wz2 + (op - 15) * kWz2B, &tm.wz2[op - 15], 2 * xt, yo, z, barM);
-            break;
-         default: break;
+      for (int t = 0; t < 2; t++) {
+         tma3(s + M::wz1 + t * kWz1B, &tm.wz1[t], 2 * xt, yo, z, bar);
+         tma3(s + M::wz2 + t * kWz2B, &tm.wz2[t], 2 * xt, yo, z, bar);
       }
    };
 
@@ -339,23 +313,26 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       return reinterpret_cast<float*>(smb + L::dd) + mod3(kk) * 3 * PLANE;
    };
 
-   // corrector: raw (up, u, um) slot -> rounded up - 2u + um and u - um, per
-   // (halo point, component)
+   // corrector: raw (up, u, um) slot -> rounded up - 2u + um and u - um
    auto transform = [&](int kk) {
       const float* raw = reinterpret_cast<const float*>(smb + L::f);
       float* vs = reinterpret_cast<float*>(smb + L::vh) + mod5(kk) * 3 * PLANE;
       float* ds = dd_plane(kk);
-      for (int q = tid; q < 3 * PLANE; q += NTHREADS) {
-         const float uph = raw[q], upl = raw[q + 3 * PLANE];
-         const float uh = raw[q + 6 * PLANE], ul = raw[q + 9 * PLANE];
-         const float mh = raw[q + 12 * PLANE], ml = raw[q + 15 * PLANE];
-         float s1, e1, s2, e2;
-         two_sum(uph, -2.f * uh, s1, e1);
-         two_sum(s1, mh, s2, e2);
-         vs[q] = s2 + ((e1 + e2) + ((upl - 2.f * ul) + ml));
-         float d1_, f1;
-         two_sum(uh, -mh, d1_, f1);
-         ds[q] = d1_ + (f1 + (ul - ml));
+      for (int idx = tid; idx < PLANE; idx += NTHREADS) {
+#pragma unroll
+         for (int c = 0; c < 3; c++) {
+            const int q = c * PLANE + idx;
+            const float uph = raw[q], upl = raw[q + 3 * PLANE];
+            const float uh = raw[q + 6 * PLANE], ul = raw[q + 9 * PLANE];
+            const float mh = raw[q + 12 * PLANE], ml = raw[q + 15 * PLANE];
+            float s1, e1, s2, e2;
+            two_sum(uph, -2.f * uh, s1, e1);
+            two_sum(s1, mh, s2, e2);
+            vs[q] = s2 + ((e1 + e2) + ((upl - 2.f * ul) + ml));
+            float d1, f1;
+            two_sum(uh, -mh, d1, f1);
+            ds[q] = d1 + (f1 + (ul - ml));
+         }
       }
    };
 
@@ -375,39 +352,38 @@ __global__ void __launch_bounds__(NTHREADS, 1)
    const float syj = active ? __ldg(a.sy + (j - a.jb)) : 0.f;
 
    // own mu, lambda pairs of plane kk from the F area (read before the next F issue)
-   float omh = 0.f, oml = 0.f;
+   float omh = 0.f, oml = 0.f, olh = 0.f, oll = 0.f;
    auto read_own_material = [&]() {
       const float* fo = reinterpret_cast<const float*>(smb + L::fown);
-      // components 0, 1 use mu, component 2 lambda
-      const int base = (c == 2 ? OWNP * 2 : 0) + 2 * ownr;
-      omh = fo[base];
-      oml = fo[base + 1];
+      omh = fo[2 * ownr];
+      oml = fo[2 * ownr + 1];
+      olh = fo[OWNP * 2 + 2 * ownr];
+      oll = fo[OWNP * 2 + 2 * ownr + 1];
    };
 
-   // the z-flux of this thread's component at the own point of plane kk
-   auto compute_gz = [&](int kk) -> float {
+   auto compute_gz = [&](int kk, float g[3]) {
       const float* vh = vh_plane(kk);
       const float* vl = CORR ? vh : vl_plane(kk);
       const float *hu = vh, *hv = vh + PLANE, *hw = vh + 2 * PLANE;
       const float *lu_ = vl, *lv = vl + PLANE, *lw = vl + 2 * PLANE;
-      float x;
-      if (c == 0) {
-         x = sxi * d1(hw, lw, own - 2, hw, lw, own - 1, hw, lw, own + 1, hw, lw, own + 2);
-      } else if (c == 1) {
-         x = syj * d1(hw, lw, own - 2 * PX, hw, lw, own - PX, hw, lw, own + PX, hw, lw, own + 2 * PX);
-      } else {
-         const float dxu = d1(hu, lu_, own - 2, hu, lu_, own - 1, hu, lu_, own + 1, hu, lu_, own + 2);
-         const float dyv = d1(hv, lv, own - 2 * PX, hv, lv, own - PX, hv, lv, own + PX, hv, lv, own + 2 * PX);
-         x = sxi * dxu + syj * dyv;
-      }
-      return fmaf(omh, x, oml * x);
+      const float dxw = d1(hw, lw, own - 2, hw, lw, own - 1, hw, lw, own + 1, hw, lw, own + 2);
+      const float dyw = d1(hw, lw, own - 2 * PX, hw, lw, own - PX, hw, lw, own + PX, hw, lw, own + 2 * PX);
+      const float dxu = d1(hu, lu_, own - 2, hu, lu_, own - 1, hu, lu_, own + 1, hu, lu_, own + 2);
+      const float dyv = d1(hv, lv, own - 2 * PX, hv, lv, own - PX, hv, lv, own + PX, hv, lv, own + 2 * PX);
+      const float x0 = sxi * dxw, x1 = syj * dyw, x2 = sxi * dxu + syj * dyv;
+      g[0] = fmaf(omh, x0, oml * x0);
+      g[1] = fmaf(omh, x1, oml * x1);
+      g[2] = fmaf(olh, x2, oll * x2);
    };
 
-   float gz[5], dq[5];
+   float gz[5][3], dq[5][3];
    const int kfin = kend + 2;  // last plane the stencil reads
 
    // ---- prologue: planes kbeg-2 .. kbeg+1 into the rings, M(kbeg) in flight ----
-   issue(kbeg - 2, kbeg);
+   if (tid == 0) {
+      issue_M(kbeg);
+      issue_F(kbeg - 2);
+   }
 #pragma unroll
    for (int q = 1; q <= 4; q++) {  // slots 1..4 hold planes kbeg-2..kbeg+1
       const int kk = kbeg - 3 + q;
@@ -416,9 +392,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       read_own_material();
       __syncthreads();
       if (*abort_flag) return;
-      issue(kk + 1, kbeg - 1);
-      if (active) gz[q] = compute_gz(kk);
-      if (CORR) dq[q] = dd_plane(kk)[oc + own];
+      if (tid == 0) {
+         fence_async_shared();
+         issue_F(kk + 1);
+      }
+      if (active) compute_gz(kk, gz[q]);
+      if (CORR) {
+         const float* dd = dd_plane(kk);
+#pragma unroll
+         for (int c = 0; c < 3; c++) dq[q][c] = dd[c * PLANE + own];
+      }
    }
 
    for (int k = kbeg; k <= kend; k++) {
@@ -428,14 +411,25 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       read_own_material();
       __syncthreads();  // (A)
       if (*abort_flag) return;
-      issue(k + 3 <= kfin ? k + 3 : kbeg - 3, k + 1 <= kend ? k + 1 : kbeg - 1);
+      if (tid == 0) {
+         fence_async_shared();
+         if (k + 3 <= kfin) issue_F(k + 3);
+         if (k + 1 <= kend) issue_M(k + 1);
+      }
 #pragma unroll
       for (int q = 0; q < 4; q++) {
-         gz[q] = gz[q + 1];
-         if (CORR) dq[q] = dq[q + 1];
+#pragma unroll
+         for (int c = 0; c < 3; c++) {
+            gz[q][c] = gz[q + 1][c];
+            if (CORR) dq[q][c] = dq[q + 1][c];
+         }
       }
-      if (active) gz[4] = compute_gz(k + 2);
-      if (CORR) dq[4] = dd_plane(k + 2)[oc + own];
+      if (active) compute_gz(k + 2, gz[4]);
+      if (CORR) {
+         const float* dd = dd_plane(k + 2);
+#pragma unroll
+         for (int c = 0; c < 3; c++) dq[4][c] = dd[c * PLANE + own];
+      }
       wait_M(k);
       const unsigned char* ms = smb + ((k & 1) ? L::m1 : L::m0);
       const float* MU2 = reinterpret_cast<const float*>(ms + M::mu);
@@ -452,130 +446,146 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const float* l0 = CORR ? h0 : vl_plane(k);
       const float* lp1 = CORR ? hp1 : vl_plane(k + 1);
       const float* lp2 = CORR ? hp2 : vl_plane(k + 2);
-      auto dz = [&](int cc, int s) {
-         const int o = cc * PLANE;
+      auto dz = [&](int c, int s) {
+         const int o = c * PLANE;
          return d1(hm2 + o, lm2 + o, s, hm1 + o, lm1 + o, s, hp1 + o, lp1 + o, s, hp2 + o, lp2 + o, s);
       };
 
-      // x-outer products over 36 x 8 (items 0..287), y-outer products over 32 x 12
-      // (items 288..671), one item per thread
-      for (int idx = tid; idx < TY * PX + PY * TX; idx += NTHREADS) {
+      // x-outer products over 36 x 8, y-outer products over 32 x 12
+      for (int idx = tid; idx < TY * PX; idx += NTHREADS) {
+         const int li = idx % PX, ljr = idx / PX;
+         const int s = (ljr + HALO) * PX + li;
+         const int gi = i0 - HALO + li, gj = j0 + ljr;
          float g0 = 0.f, g1 = 0.f, g2 = 0.f;
-         const float *hu = h0, *hv = h0 + PLANE, *lu_ = l0, *lv = l0 + PLANE;
-         if (idx < TY * PX) {
-            const int li = idx % PX, ljr = idx / PX;
-            const int s = (ljr + HALO) * PX + li;
-            const int gi = i0 - HALO + li, gj = j0 + ljr;
-            if (gi <= a.ie && gj <= a.je) {
-               const float syy = __ldg(a.sy + (gj - a.jb));
-               const float dyv = d1(hv, lv, s - 2 * PX, hv, lv, s - PX, hv, lv, s + PX, hv, lv, s + 2 * PX);
-               const float dyu = d1(hu, lu_, s - 2 * PX, hu, lu_, s - PX, hu, lu_, s + PX, hu, lu_, s + 2 * PX);
-               const float dzw = dz(2, s), dzu = dz(0, s);
-               const float mh = MU2[2 * s], ml = MU2[2 * s + 1], lh = LA2[2 * s], ll = LA2[2 * s + 1];
-               const float x0 = syy * dyv + szk * dzw, x1 = syy * dyu, x2 = szk * dzu;
-               g0 = fmaf(lh, x0, ll * x0);
-               g1 = fmaf(mh, x1, ml * x1);
-               g2 = fmaf(mh, x2, ml * x2);
-            }
-            GX[idx] = g0;
-            GX[TY * PX + idx] = g1;
-            GX[2 * TY * PX + idx] = g2;
-         } else {
-            const int iy = idx - TY * PX;
-            const int lic = iy % TX, lj = iy / TX;
-            const int s = lj * PX + lic + HALO;
-            const int gi = i0 + lic, gj = j0 - HALO + lj;
-            if (gi <= a.ie && gj <= a.je) {
-               const float sxx = __ldg(a.sx + (gi - a.ib));
-               const float dxv = d1(hv, lv, s - 2, hv, lv, s - 1, hv, lv, s + 1, hv, lv, s + 2);
-               const float dxu = d1(hu, lu_, s - 2, hu, lu_, s - 1, hu, lu_, s + 1, hu, lu_, s + 2);
-               const float dzw = dz(2, s), dzv = dz(1, s);
-               const float mh = MU2[2 * s], ml = MU2[2 * s + 1], lh = LA2[2 * s], ll = LA2[2 * s + 1];
-               const float x0 = sxx * dxv, x1 = sxx * dxu + szk * dzw, x2 = szk * dzv;
-               g0 = fmaf(mh, x0, ml * x0);
-               g1 = fmaf(lh, x1, ll * x1);
-               g2 = fmaf(mh, x2, ml * x2);
-            }
-            GY[iy] = g0;
-            GY[PY * TX + iy] = g1;
-            GY[2 * PY * TX + iy] = g2;
+         if (gi <= a.ie && gj <= a.je) {
+            const float syy = __ldg(a.sy + (gj - a.jb));
+            const float *hu = h0, *hv = h0 + PLANE, *lu_ = l0, *lv = l0 + PLANE;
+            const float dyv = d1(hv, lv, s - 2 * PX, hv, lv, s - PX, hv, lv, s + PX, hv, lv, s + 2 * PX);
+            const float dyu = d1(hu, lu_, s - 2 * PX, hu, lu_, s - PX, hu, lu_, s + PX, hu, lu_, s + 2 * PX);
+            const float dzw = dz(2, s), dzu = dz(0, s);
+            const float mh = MU2[2 * s], ml = MU2[2 * s + 1], lh = LA2[2 * s], ll = LA2[2 * s + 1];
+            const float x0 = syy * dyv + szk * dzw, x1 = syy * dyu, x2 = szk * dzu;
+            g0 = fmaf(lh, x0, ll * x0);
+            g1 = fmaf(mh, x1, ml * x1);
+            g2 = fmaf(mh, x2, ml * x2);
          }
+         GX[idx] = g0;
+         GX[TY * PX + idx] = g1;
+         GX[2 * TY * PX + idx] = g2;
+      }
+      for (int idx = tid; idx < PY * TX; idx += NTHREADS) {
+         const int lic = idx % TX, lj = idx / TX;
+         const int s = lj * PX + lic + HALO;
+         const int gi = i0 + lic, gj = j0 - HALO + lj;
+         float g0 = 0.f, g1 = 0.f, g2 = 0.f;
+         if (gi <= a.ie && gj <= a.je) {
+            const float sxx = __ldg(a.sx + (gi - a.ib));
+            const float *hu = h0, *hv = h0 + PLANE, *lu_ = l0, *lv = l0 + PLANE;
+            const float dxv = d1(hv, lv, s - 2, hv, lv, s - 1, hv, lv, s + 1, hv, lv, s + 2);
+            const float dxu = d1(hu, lu_, s - 2, hu, lu_, s - 1, hu, lu_, s + 1, hu, lu_, s + 2);
+            const float dzw = dz(2, s), dzv = dz(1, s);
+            const float mh = MU2[2 * s], ml = MU2[2 * s + 1], lh = LA2[2 * s], ll = LA2[2 * s + 1];
+            const float x0 = sxx * dxv, x1 = sxx * dxu + szk * dzw, x2 = szk * dzv;
+            g0 = fmaf(mh, x0, ml * x0);
+            g1 = fmaf(lh, x1, ll * x1);
+            g2 = fmaf(mh, x2, ml * x2);
+         }
+         GY[idx] = g0;
+         GY[PY * TX + idx] = g1;
+         GY[2 * PY * TX + idx] = g2;
       }
       __syncthreads();  // (B)
       if (*abort_flag) return;
 
       if (active) {
          const long long p = gidx(i, j, k);
+         // W1(q), W2(q), W2(q+1), W1(q+2) per axis and coefficient type, as (hi, lo)
          const float2* wxs = reinterpret_cast<const float2*>(ms + M::wx);
          const float2* wys = reinterpret_cast<const float2*>(ms + M::wy);
          const float2* wz1 = reinterpret_cast<const float2*>(ms + M::wz1);
          const float2* wz2 = reinterpret_cast<const float2*>(ms + M::wz2);
-         // second difference along one axis with the (hi, lo) weights W1(q), W2(q),
-         // W2(q+1), W1(q+2) of coefficient type t = (c == axis)
-         auto wsum = [&](float2 w0, float2 w1, float2 w2, float2 w3, float dm2, float dm1, float dp1,
-                         float dp2) {
-            const float sh = fmaf(w0.x, dm2, fmaf(w1.x, dm1, fmaf(w2.x, dp1, w3.x * dp2)));
-            const float sl = fmaf(w0.y, dm2, fmaf(w1.y, dm1, fmaf(w2.y, dp1, w3.y * dp2)));
+         float wth[3][2][4], wtl[3][2][4];
+#pragma unroll
+         for (int t = 0; t < 2; t++) {
+            const float2* x1 = wxs + (2 * t) * OWNP;      // W1 of the x axis
+            const float2* x2 = wxs + (2 * t + 1) * OWNP;  // W2
+            const float2 q0 = x1[ownr], q1 = x2[ownr], q2 = x2[ownr + 1], q3 = x1[ownr + 2];
+            const float2* y1 = wys + (2 * t) * (kWyB / 8);
+            const float2* y2 = wys + (2 * t + 1) * (kWyB / 8);
+            const float2 r0 = y1[ownr], r1 = y2[ownr], r2 = y2[ownr + PX], r3 = y1[ownr + 2 * PX];
+            const float2* z1 = wz1 + t * (kWz1B / 8);
+            const float2* z2 = wz2 + t * (kWz2B / 8);
+            const float2 s0 = z1[ownr], s1 = z2[ownr], s2 = z2[ownr + OWNP], s3 = z1[ownr + 2 * OWNP];
+            wth[0][t][0] = q0.x; wth[0][t][1] = q1.x; wth[0][t][2] = q2.x; wth[0][t][3] = q3.x;
+            wtl[0][t][0] = q0.y; wtl[0][t][1] = q1.y; wtl[0][t][2] = q2.y; wtl[0][t][3] = q3.y;
+            wth[1][t][0] = r0.x; wth[1][t][1] = r1.x; wth[1][t][2] = r2.x; wth[1][t][3] = r3.x;
+            wtl[1][t][0] = r0.y; wtl[1][t][1] = r1.y; wtl[1][t][2] = r2.y; wtl[1][t][3] = r3.y;
+            wth[2][t][0] = s0.x; wth[2][t][1] = s1.x; wth[2][t][2] = s2.x; wth[2][t][3] = s3.x;
+            wtl[2][t][0] = s0.y; wtl[2][t][1] = s1.y; wtl[2][t][2] = s2.y; wtl[2][t][3] = s3.y;
+         }
+         auto wsum = [&](int ax, int t, float dm2, float dm1, float dp1, float dp2) {
+            const float* hh = wth[ax][t];
+            const float* ll = wtl[ax][t];
+            const float sh = fmaf(hh[0], dm2, fmaf(hh[1], dm1, fmaf(hh[2], dp1, hh[3] * dp2)));
+            const float sl = fmaf(ll[0], dm2, fmaf(ll[1], dm1, fmaf(ll[2], dp1, ll[3] * dp2)));
             return sh + sl;
          };
-         const int tx_ = c == 0 ? 1 : 0, ty_ = c == 1 ? 1 : 0, tz_ = c == 2 ? 1 : 0;
-         const float* ch = h0 + oc;
-         const float* cl = l0 + oc;
-         const float2* x1 = wxs + (2 * tx_) * OWNP;      // W1 of the x axis
-         const float2* x2 = wxs + (2 * tx_ + 1) * OWNP;  // W2
-         const float sxx = wsum(x1[ownr], x2[ownr], x2[ownr + 1], x1[ownr + 2],
-                                diff(ch, cl, own - 2, own), diff(ch, cl, own - 1, own),
-                                diff(ch, cl, own + 1, own), diff(ch, cl, own + 2, own));
-         const float2* y1 = wys + (2 * ty_) * (kWyB / 8);
-         const float2* y2 = wys + (2 * ty_ + 1) * (kWyB / 8);
-         const float syy = wsum(y1[ownr], y2[ownr], y2[ownr + PX], y1[ownr + 2 * PX],
-                                diff(ch, cl, own - 2 * PX, own), diff(ch, cl, own - PX, own),
-                                diff(ch, cl, own + PX, own), diff(ch, cl, own + 2 * PX, own));
-         float dzm2, dzm1, dzp1, dzp2;
-         if (CORR == 1) {
-            dzm2 = hm2[oc + own] - ch[own];
-            dzm1 = hm1[oc + own] - ch[own];
-            dzp1 = hp1[oc + own] - ch[own];
-            dzp2 = hp2[oc + own] - ch[own];
-         } else {
-            dzm2 = (hm2[oc + own] - ch[own]) + (lm2[oc + own] - cl[own]);
-            dzm1 = (hm1[oc + own] - ch[own]) + (lm1[oc + own] - cl[own]);
-            dzp1 = (hp1[oc + own] - ch[own]) + (lp1[oc + own] - cl[own]);
-            dzp2 = (hp2[oc + own] - ch[own]) + (lp2[oc + own] - cl[own]);
+         float xs[3];
+#pragma unroll
+         for (int c = 0; c < 3; c++) {
+            const float* ch = h0 + c * PLANE;
+            const float* cl = l0 + c * PLANE;
+            const int o = c * PLANE;
+            const float sxx = wsum(0, c == 0, diff(ch, cl, own - 2, own), diff(ch, cl, own - 1, own),
+                                   diff(ch, cl, own + 1, own), diff(ch, cl, own + 2, own));
+            const float syy = wsum(1, c == 1, diff(ch, cl, own - 2 * PX, own),
+                                   diff(ch, cl, own - PX, own), diff(ch, cl, own + PX, own),
+                                   diff(ch, cl, own + 2 * PX, own));
+            float dzm2, dzm1, dzp1, dzp2;
+            if (CORR == 1) {
+               dzm2 = hm2[o + own] - ch[own];
+               dzm1 = hm1[o + own] - ch[own];
+               dzp1 = hp1[o + own] - ch[own];
+               dzp2 = hp2[o + own] - ch[own];
+            } else {
+               dzm2 = (hm2[o + own] - ch[own]) + (lm2[o + own] - cl[own]);
+               dzm1 = (hm1[o + own] - ch[own]) + (lm1[o + own] - cl[own]);
+               dzp1 = (hp1[o + own] - ch[own]) + (lp1[o + own] - cl[own]);
+               dzp2 = (hp2[o + own] - ch[own]) + (lp2[o + own] - cl[own]);
+            }
+            const float szz = wsum(2, c == 2, dzm2, dzm1, dzp1, dzp2);
+            const float* gxp = GX + c * TY * PX + ty * PX + tx;
+            const float* gyp = GY + c * PY * TX + ty * TX + tx;
+            const float cx = (gxp[0] - gxp[4]) + 8.f * (gxp[3] - gxp[1]);
+            const float cy = (gyp[0] - gyp[4 * TX]) + 8.f * (gyp[3 * TX] - gyp[TX]);
+            const float cz = (gz[0][c] - gz[4][c]) + 8.f * (gz[3][c] - gz[1][c]);
+            const float sd = sxi * sxx + syj * syy + szk * szz;
+            xs[c] = (16.f * sd + 8.f * sd) + (sxi * cx + syj * cy + szk * cz);
          }
-         const float2* z1 = wz1 + tz_ * (kWz1B / 8);
-         const float2* z2 = wz2 + tz_ * (kWz2B / 8);
-         const float szz = wsum(z1[ownr], z2[ownr], z2[ownr + OWNP], z1[ownr + 2 * OWNP], dzm2, dzm1,
-                                dzp1, dzp2);
-         const float* gxp = GX + c * TY * PX + ty * PX + tx;
-         const float* gyp = GY + c * PY * TX + ty * TX + tx;
-         const float cx = (gxp[0] - gxp[4]) + 8.f * (gxp[3] - gxp[1]);
-         const float cy = (gyp[0] - gyp[4 * TX]) + 8.f * (gyp[3 * TX] - gyp[TX]);
-         const float cz = (gz[0] - gz[4]) + 8.f * (gz[3] - gz[1]);
-         // 144 h^2 L u = 24 * (second differences) + (mixed differences)
-         const float sd = sxi * sxx + syj * syy + szk * szz;
-         const float xs = (16.f * sd + 8.f * sd) + (sxi * cx + syj * cy + szk * cz);
-         // per-point scale K/rho as a (hi, lo) pair: ph + pl = (Kh + Kl) * (irh + irl)
          const float2 ir = reinterpret_cast<const float2*>(ms + M::ir)[ownr];
          const float irh = ir.x, irl = ir.y;
          const float ph = a.Kh * irh;
          const float pl = fmaf(a.Kh, irh, -ph) + fmaf(a.Kh, irl, a.Kl * irh);
-         const float scaled = fmaf(xs, ph, xs * pl);
+         auto scaled = [&](float x) { return fmaf(x, ph, x * pl); };
          const float* ownlev = reinterpret_cast<const float*>(ms + M::own);  // [6][8][36]
-         const long long q = p + c * npts;
-         float oh, ol;
          if (!CORR) {
-            const float uh = ch[own], ul = cl[own];
-            const float mh = ownlev[c * OWNP + ownr], ml = ownlev[(c + 3) * OWNP + ownr];
-            float s_, e, t, e2;
-            two_sum(2.f * uh, -mh, s_, e);
-            two_sum(s_, scaled, t, e2);
-            fast_two_sum(t, (e + e2) + (2.f * ul - ml), oh, ol);
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+               const long long q = p + c * npts;
+               const float uh = h0[c * PLANE + own], ul = l0[c * PLANE + own];
+               const float mh = ownlev[c * OWNP + ownr], ml = ownlev[(c + 3) * OWNP + ownr];
+               float s, e, t, e2, oh, ol;
+               two_sum(2.f * uh, -mh, s, e);
+               two_sum(s, scaled(xs[c]), t, e2);
+               fast_two_sum(t, (e + e2) + (2.f * ul - ml), oh, ol);
+               a.out[q] = oh;
+               a.out[q + lo] = ol;
+            }
          } else {
             const float* RH = reinterpret_cast<const float*>(ms + M::rho);
-            float sg = 0.f;
+            float sg[3] = {0.f, 0.f, 0.f};
             if (a.beta != 0.f) {
-               const float* d = dd_plane(k) + oc + own;
+               const float* dd = dd_plane(k);
                const float cxi = __ldg(a.co[0] + (i - a.ib)), cyj = __ldg(a.co[1] + (j - a.jb)),
                            czk = __ldg(a.co[2] + (k - a.kb));
                const float dx0 = __ldg(a.dc[0] + (i - 1 - a.ib)), dx1 = __ldg(a.dc[0] + (i - a.ib)),
@@ -583,17 +593,25 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                if (dx0 != 0.f || dx1 != 0.f || dx2 != 0.f) {
                   const float e0 = RH[own - 1] * dx0, e1 = RH[own] * dx1, e2 = RH[own + 1] * dx2;
                   const float w = sxi * cyj * czk;
-                  sg += w * (e2 * (d[2] - 2.f * d[1] + d[0]) - 2.f * e1 * (d[1] - 2.f * d[0] + d[-1]) +
-                             e0 * (d[0] - 2.f * d[-1] + d[-2]));
+#pragma unroll
+                  for (int c = 0; c < 3; c++) {
+                     const float* d = dd + c * PLANE + own;
+                     sg[c] += w * (e2 * (d[2] - 2.f * d[1] + d[0]) - 2.f * e1 * (d[1] - 2.f * d[0] + d[-1]) +
+                                   e0 * (d[0] - 2.f * d[-1] + d[-2]));
+                  }
                }
                const float dy0 = __ldg(a.dc[1] + (j - 1 - a.jb)), dy1 = __ldg(a.dc[1] + (j - a.jb)),
                            dy2 = __ldg(a.dc[1] + (j + 1 - a.jb));
                if (dy0 != 0.f || dy1 != 0.f || dy2 != 0.f) {
                   const float e0 = RH[own - PX] * dy0, e1 = RH[own] * dy1, e2 = RH[own + PX] * dy2;
                   const float w = syj * cxi * czk;
-                  sg += w * (e2 * (d[2 * PX] - 2.f * d[PX] + d[0]) -
-                             2.f * e1 * (d[PX] - 2.f * d[0] + d[-PX]) +
-                             e0 * (d[0] - 2.f * d[-PX] + d[-2 * PX]));
+#pragma unroll
+                  for (int c = 0; c < 3; c++) {
+                     const float* d = dd + c * PLANE + own;
+                     sg[c] += w * (e2 * (d[2 * PX] - 2.f * d[PX] + d[0]) -
+                                   2.f * e1 * (d[PX] - 2.f * d[0] + d[-PX]) +
+                                   e0 * (d[0] - 2.f * d[-PX] + d[-2 * PX]));
+                  }
                }
                const float dz0 = __ldg(a.dc[2] + (k - 1 - a.kb)), dz1 = __ldg(a.dc[2] + (k - a.kb)),
                            dz2 = __ldg(a.dc[2] + (k + 1 - a.kb));
@@ -601,18 +619,25 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                   const float e0 = __ldg(a.rho + p - a.nij) * dz0, e1 = RH[own] * dz1,
                               e2 = __ldg(a.rho + p + a.nij) * dz2;
                   const float w = szk * cxi * cyj;
-                  sg += w * (e2 * (dq[4] - 2.f * dq[3] + dq[2]) - 2.f * e1 * (dq[3] - 2.f * dq[2] + dq[1]) +
-                             e0 * (dq[2] - 2.f * dq[1] + dq[0]));
+#pragma unroll
+                  for (int c = 0; c < 3; c++)
+                     sg[c] += w * (e2 * (dq[4][c] - 2.f * dq[3][c] + dq[2][c]) -
+                                   2.f * e1 * (dq[3][c] - 2.f * dq[2][c] + dq[1][c]) +
+                                   e0 * (dq[2][c] - 2.f * dq[1][c] + dq[0][c]));
                }
             }
             const float birho = a.beta * irh;
-            const float uph = ownlev[c * OWNP + ownr], upl = ownlev[(c + 3) * OWNP + ownr];
-            float t, e;
-            two_sum(uph, scaled - birho * sg, t, e);
-            fast_two_sum(t, e + upl, oh, ol);
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+               const long long q = p + c * npts;
+               const float uph = ownlev[c * OWNP + ownr], upl = ownlev[(c + 3) * OWNP + ownr];
+               float t, e, oh, ol;
+               two_sum(uph, scaled(xs[c]) - birho * sg[c], t, e);
+               fast_two_sum(t, e + upl, oh, ol);
+               a.out[q] = oh;
+               a.out[q + lo] = ol;
+            }
          }
-         a.out[q] = oh;
-         a.out[q + lo] = ol;
       }
       __syncthreads();  // (C): GX/GY, M stage k and the oldest ring slot are free
    }
@@ -809,7 +834,7 @@ int launch_mixed_stage_tma(const MixedStage& st, cudaStream_t stream)
       }
    }
    a.kchunk = stage_kchunk((long long)gx * gy, nk, resident[corr][dev], 12);
-   const dim3 grid(gx, gy, (nk + a.kchunk - 1) / a.kchunk), block(TX, TY, 3);
+   const dim3 grid(gx, gy, (nk + a.kchunk - 1) / a.kchunk), block(TX, TY, 1);
    if (corr)
       mixed_stage_tma_kernel<1><<<grid, block, smem, stream>>>(tm, a);
    else

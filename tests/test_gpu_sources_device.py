@@ -3,12 +3,15 @@ loop of Source::set_grid_point_sources4, src/Source.C:1074-1530) against the hos
 path: the same grid-point sources bit for bit (grouped by grid point, in the host's
 order within a point) and the same fields after a run, for a batch of point forces
 and moment tensors that reaches the free surface (five-point weights, SBP
-normalisation), the side clamps and overlapping stencils."""
+normalisation), the side clamps and overlapping stencils; and the device list
+against the oracle's own discretisation (oracle/sw4_oracle_src.c), summed per grid
+point, to 1e-14 of the largest amplitude (1e-12 for stencils clamped next to a side,
+where the double evaluation of the published polynomials loses about two digits)."""
 import numpy as np
 import pytest
 
 import sw4lite_gb300 as sg
-from tests.gpu_util import dev, host, smooth_fields, smooth_material
+from tests.gpu_util import dev, host, oracle_discretize, smooth_fields, smooth_material
 
 pytestmark = pytest.mark.gpu
 
@@ -82,6 +85,46 @@ def test_device_sources_match_host_bit_for_bit():
         out.append(host(r))
         ew.close()
     assert np.array_equal(out[0], out[1])
+
+
+def _per_point(ijk, amp):
+    d = {}
+    for q in range(len(ijk) // 3):
+        key = tuple(int(v) for v in ijk[3 * q:3 * q + 3])
+        d[key] = d.get(key, np.zeros(3)) + amp[3 * q:3 * q + 3]
+    return d
+
+
+def _clamped(s):
+    cells = [int(np.floor(s.x / H + 1)), int(np.floor(s.y / H + 1)), int(np.floor(s.z / H + 1))]
+    return any(c <= 2 or c >= n - 2 for c, n in zip(cells, (NX, NY, NZ)))
+
+
+def _device_vs_oracle(srcs):
+    ew = _ew(True, srcs)
+    g = ew.grid
+    got = _per_point(*[a.reshape(-1) for a in ew.grid_point_sources()])
+    ew.close()
+    want = {}
+    for s in srcs:
+        for key, v in _per_point(*oracle_discretize(g, s)).items():
+            want[key] = want.get(key, np.zeros(3)) + v
+    scale = max(np.abs(v).max() for v in want.values())
+    err = max(np.abs(got.get(k, np.zeros(3)) - want.get(k, np.zeros(3))).max()
+              for k in set(got) | set(want))
+    big = lambda d: {k for k, v in d.items() if np.abs(v).max() > 1e-12 * scale}
+    return err / scale, big(got) == big(want)
+
+
+def test_device_sources_match_the_oracle():
+    srcs = _sources()
+    err, same = _device_vs_oracle(srcs)
+    assert err <= (1e-12 if any(_clamped(s) for s in srcs) else 1e-14), err
+    assert same
+    # the sources whose stencils are not clamped next to a side meet the tight bound
+    err, same = _device_vs_oracle([s for s in srcs if not _clamped(s)])
+    assert err <= 1e-14, err
+    assert same
 
 
 def test_switching_back_to_the_host_rebuilds_its_list():
