@@ -83,18 +83,25 @@ def measured_peaks():
 # algorithmic bytes per interior point of one corrector stage: reads Up, U, Um (9
 # words) and mu, lambda, rho (3), writes the new level (3): 15 FP64 words
 CORR_STAGE_WORDS = 15
-# DRAM bytes per interior point of the corrector stage kernel, from one ncu capture
-# of the 192^3 case (dram__bytes_read.sum + dram__bytes_write.sum = 2.1268e9 B over
-# 7,077,888 interior points; profiles/fused_stage_c2_192.md); traffic grows with
-# the point count, so a launch moves this many bytes per point at any size
-CORR_STAGE_DRAM_BYTES_PER_PT = 300.49
-# reference flop counts per interior point (tests/testil/testil.C:271, :299):
-# rhs4sg 666, addsgd4 375, corrector+dpdm ~23 -> corrector stage; predictor ~683
-CORR_STAGE_REF_FLOPS = 666 + 375 + 11 + 12
+# DRAM bytes per interior point of the FP64 corrector stage kernel, from one ncu
+# capture of the 192^3 case (dram__bytes_read.sum + dram__bytes_write.sum = 2.1133e9 B
+# over 7,077,888 interior points); traffic grows with the point count, so a launch
+# moves this many bytes per point at any size
+CORR_STAGE_DRAM_BYTES_PER_PT = 298.6
+# FP64-pipe warp instructions per interior point of the FP64 stage kernels on the
+# 512^3 workload (smsp__inst_executed_pipe_fp64.sum, one single-pass ncu capture of
+# the full-size run: 896,543,168 and 715,560,960 over 512^3 points).  The pipe issues
+# 2 FP64 thread instructions per clock per SM, i.e. one warp instruction per 16 clocks.
+FP64_WARP_INST_PER_PT = {"corr": 896543168 / 512 ** 3, "pred": 715560960 / 512 ** 3}
+FP64_THREAD_INST_PER_CLK_PER_SM = 2
 # mixed form, corrector stage: reads Up, U, Um as double-float pairs (9 x 8 B), mu,
-# lambda, rho in FP32 (3 x 4 B), writes the new level (3 x 8 B)
+# lambda, rho in FP32 (3 x 4 B), writes the new level (3 x 8 B): the compulsory bytes
+# of an all-FP32-coefficient stage
 MIXED_CORR_STAGE_BYTES = 9 * 8 + 3 * 4 + 3 * 8
-STEP_REF_FLOPS = 1747
+# DRAM bytes per interior point the tensor-copy corrector stage moves (ncu, 256^3:
+# 3.445e9 read + 0.394e9 written over 256^3 points): the levels, the (hi, lo)
+# coefficient pairs of mu, lambda, 1/rho and the twelve weight arrays
+MIXED_CORR_STAGE_DRAM_BYTES_PER_PT = 228.8
 
 
 class ClockSampler:
@@ -182,65 +189,63 @@ def max_over_ranks(x, world):
 
 
 # --------------------------------------------------------------------------
-# CPU baseline: the oracle time step on a bounded sample of the workload
+# CPU baseline: the reference's CPU step on the host cores, on the same workload.
+# Built from oracle/ alone (no product code): the reference's own kernels
+# (oracle/_ref, compiled from the reference sources where they are present) or
+# else the oracle's restatement of them, both OpenMP over every host core.
 # --------------------------------------------------------------------------
-def cpu_sample(n=96, steps=1, min_seconds=0.0, max_steps=40):
-    """Time CPU time steps of the C2 workload restricted to an n^3 grid: `steps`
-    steps, continued until at least `min_seconds` have elapsed (at most max_steps)."""
+def cpu_rate(n, steps, warmup=1, which=None):
+    """Grid-point-steps/s of `steps` CPU time steps of the C2 workload at n^3 after
+    `warmup` untimed ones, on the reference's kernels where they were built here
+    (which="ref") or else on the oracle restatement ("oracle"); returns (rate,
+    seconds, kind, cores)."""
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
     from oracle import oracle as O
-    import sw4lite_gb300 as sg
-    from tests.gpu_util import OracleProblem
     O.lib()
+    if which is None:
+        which = "ref" if O.ref_available() else "oracle"
     cfg = c2_config(n)
-    cfg["sg_gp"] = min(cfg["sg_gp"], n // 4)
-    cfg["src"].update(x=(n - 1) * cfg["h"] / 2, y=(n - 1) * cfg["h"] / 2, z=min(2000.0, n * cfg["h"] / 3))
-    g = sg.grid_desc(n, n, n, cfg["h"], bc=cfg["bc"], sg_gp=cfg["sg_gp"], sg_damping=cfg["sg_damping"])
     rho, mu, la = layered_material(cfg)
-    src = sg.source_desc(**{k: cfg["src"][k] for k in ("x", "y", "z")}, moment=cfg["src"]["moment"],
-                         freq=cfg["src"]["freq"], t0=cfg["src"]["t0"], kind=sg.GAUSSIAN)
-    dt = cfl_dt(cfg)
-    prob = OracleProblem(g, rho, mu, la, dt, [src])
-    npts3 = 3 * prob.npts
-    u = np.zeros(npts3)
-    um = np.zeros(npts3)
-    up, lu, f, uacc = (np.zeros(npts3) for _ in range(4))
-    # one untimed step warms the OpenMP pool and the pages
-    O.step(prob.P, 1, 0.0, up, u, um, lu, f, uacc)
-    t0 = time.perf_counter()
-    t = cfg["src"]["t0"]
-    done = 0
-    while done < steps or (time.perf_counter() - t0 < min_seconds and done < max_steps):
-        O.step(prob.P, 1, t, up, u, um, lu, f, uacc)
+    sc = cfg["src"]
+    src = O.PointSource(sc["x"], sc["y"], sc["z"], moment=sc["moment"], freq=sc["freq"], t0=sc["t0"],
+                        kind=0)  # Gaussian
+    prob = O.CartProblem(n, n, n, cfg["h"], cfg["bc"], rho, mu, la, cfl_dt(cfg), [src],
+                         sg_gp=cfg["sg_gp"], sg_damping=cfg["sg_damping"])
+    n3 = 3 * prob.npts
+    u, um, up, lu, f, uacc = (np.zeros(n3) for _ in range(6))
+    t = 0.0
+    for _ in range(warmup):
+        O.step(prob.P, 1, t, up, u, um, lu, f, uacc, which=which)
         um, u, up = u, up, um
-        t += dt
-        done += 1
+        t += prob.P.dt
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        O.step(prob.P, 1, t, up, u, um, lu, f, uacc, which=which)
+        um, u, up = u, up, um
+        t += prob.P.dt
     el = time.perf_counter() - t0
-    return n ** 3 * done / el, el, n, done
+    kind = "reference" if which == "ref" else "port"
+    return n ** 3 * steps / el, el, kind, int(os.environ["OMP_NUM_THREADS"])
 
 
 def run_reference(args, rank, world):
-    """Reference arm: the reference's CPU step on the host cores."""
+    """Reference arm: the reference's CPU step on the host cores, same workload."""
     if rank != 0:
         return 0
-    ncores = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(ncores))
-    n = args.cpu_n
-    samples = []
-    for s in range(args.warmup + args.steps):
-        rate, el, _, _ = cpu_sample(n=n, steps=1)
-        if s >= args.warmup:
-            samples.append((rate, el))
-    rate = len(samples) * n ** 3 / sum(e for _, e in samples)
+    n = args.n
+    rate, el, kind, cores = cpu_rate(n, args.steps, args.warmup)
+    src = ("the reference's own kernels (oracle/_ref)" if kind == "reference"
+           else "the oracle restatement of the reference kernels")
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * n ** 3 / rate, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"C2 layer-over-halfspace, FP64 time step, sampled on {n}^3 "
-                               "(h=50, same material, boundaries and source)", "grid": [n, n, n]},
-        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]),
-                         "kind": "port",
-                         "sample": f"{args.steps} time steps of a {n}^3 grid of the workload"},
+        "config": {"workload": f"C2 layer-over-halfspace {n}^3 h=50, FP64 time step (CPU)",
+                   "grid": [n, n, n]},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": f"{args.steps} time steps of the {n}^3 workload after "
+                                   f"{args.warmup} untimed ({el:.1f} s; {src}, OpenMP)"},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -595,10 +600,8 @@ def _c5_shot(sg, ew, cfg, s):
                                  kind=sg.GAUSSIAN))
 
 
-def _c5_gradients(sg, torch, cfg, stream, mat, dt, N, C, shots, precisions):
-    """Observed data (FP32-mixed forward in the homogeneous background) for the shots,
-    then for each precision the summed gradient over the shots (FP64 accumulation on
-    the device) with each shot's gradient() timed by CUDA events."""
+def _c5_observed(sg, torch, cfg, stream, N, shots, dt):
+    """Observed data of the shots: FP32-mixed forward runs in the homogeneous background."""
     ew0 = _c5_ew(sg, torch, cfg, stream, N, sg.MIXED, _c5_medium(torch, cfg, True), dt)
     zero = torch.zeros(3 * ew0.npts, dtype=torch.float64, device="cuda")
     obs = []
@@ -612,62 +615,79 @@ def _c5_gradients(sg, torch, cfg, stream, mat, dt, N, C, shots, precisions):
         ew0.records(o)
         obs.append(o)
     ew0.close()
-    out = {}
-    for prec in precisions:
-        ew = _c5_ew(sg, torch, cfg, stream, N, prec, mat, dt)
-        tot = [torch.zeros(ew.npts, dtype=torch.float64, device="cuda") for _ in range(3)]
-        g = [torch.zeros(ew.npts, dtype=torch.float64, device="cuda") for _ in range(3)]
-        ms, J = [], 0.0
-        for s, o in zip(shots, obs):
-            _c5_shot(sg, ew, cfg, s)
-            ew.set_time_step(dt, 0.0)
-            ew.set_fields(zero, zero)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            J += ew.gradient(N, C, o, *g)
-            for q in range(3):
-                tot[q] += g[q]  # FP64 accumulation over shots, on the device
-            e1.record(stream)
-            torch.cuda.synchronize()
-            ms.append(e0.elapsed_time(e1))
-        ew.close()
-        out[prec] = dict(ms=ms, J=J, tot=tot)
-    return out
+    return obs
+
+
+def _c5_gradients(sg, torch, cfg, stream, mat, dt, N, C, shots, obs, prec, keep_after=0):
+    """The summed gradient over the shots in one precision (FP64 accumulation on the
+    device), each shot's gradient() timed by CUDA events; with keep_after = E > 0 also
+    a copy of the sum after the first E shots."""
+    ew = _c5_ew(sg, torch, cfg, stream, N, prec, mat, dt)
+    zero = torch.zeros(3 * ew.npts, dtype=torch.float64, device="cuda")
+    tot = [torch.zeros(ew.npts, dtype=torch.float64, device="cuda") for _ in range(3)]
+    g = [torch.zeros(ew.npts, dtype=torch.float64, device="cuda") for _ in range(3)]
+    ms, J, part = [], 0.0, None
+    for n, (s, o) in enumerate(zip(shots, obs)):
+        _c5_shot(sg, ew, cfg, s)
+        ew.set_time_step(dt, 0.0)
+        ew.set_fields(zero, zero)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        J += ew.gradient(N, C, o, *g)
+        for q in range(3):
+            tot[q] += g[q]  # FP64 accumulation over shots, on the device
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        if n + 1 == keep_after:
+            part = [x.clone() for x in tot]
+    ew.close()
+    return dict(ms=ms, J=J, tot=tot, part=part)
 
 
 def _time_multishot(args, sg, torch, stream):
     """C5: the summed misfit gradient over point-force shots, FP32-mixed (double-float
     levels, FP32 stencils and gradient terms) with FP64 accumulation, every time loop
     replayed as CUDA graphs.  Per-shot time from CUDA events on args.ms_shots shots at
-    the workload's full length (args.ms_steps); error of the mixed sum over
-    args.ms_err_shots shots against the FP64 gradients of the same shots, at
-    args.ms_err_steps steps (FP64 gradients of the full length take minutes)."""
+    the workload's length (args.ms_steps); the error of the mixed sum over the first
+    args.ms_err_shots shots against the FP64 gradients of the same shots at
+    args.ms_err_steps steps (the timed run's partial sum when the lengths agree)."""
     cfg = c5_config(args.adj_n)
     N, C, S = args.ms_steps, args.adj_ckpt, args.ms_shots
+    E = min(args.ms_err_shots, len(cfg["shots"]))
     n = cfg["n"]
     with torch.cuda.stream(stream):
         mat = _c5_medium(torch, cfg, False)
         dt = cfg["cfl"] * cfg["h"] / float(torch.sqrt(((4 * mat[1] + mat[2]) / mat[0]).max()))
-        mx = _c5_gradients(sg, torch, cfg, stream, mat, dt, N, C, list(range(S)), [sg.MIXED])[sg.MIXED]
+        shots = list(range(S))
+        obs = _c5_observed(sg, torch, cfg, stream, N, shots, dt)
+        reuse = E > 0 and E <= S and args.ms_err_steps == N
+        mx = _c5_gradients(sg, torch, cfg, stream, mat, dt, N, C, shots, obs, sg.MIXED,
+                           keep_after=E if reuse else 0)
         res = {"workload": f"C5 multi-shot gradient {n}^3, C4 medium, point-force shots, 16 receivers, "
                            f"{N} steps, checkpoints every {C}, FP32-mixed with FP64 accumulation, "
                            "time loops as CUDA graphs",
                "shots": S, "of_shots": len(cfg["shots"]), "steps": N,
                "per_shot_ms": sum(mx["ms"]) / len(mx["ms"]), "total_ms": sum(mx["ms"]),
                "misfit": mx["J"], "grad_norms": [float(x.norm()) for x in mx["tot"]]}
-        del mx
-        E = min(args.ms_err_shots, len(cfg["shots"]))
         if E > 0:
-            out = _c5_gradients(sg, torch, cfg, stream, mat, dt, args.ms_err_steps, C, list(range(E)),
-                                [sg.MIXED, sg.FP64])
-            a, b = out[sg.MIXED], out[sg.FP64]
+            M = args.ms_err_steps
+            if reuse:
+                a_tot, a_ms = mx["part"], sum(mx["ms"][:E]) / E
+                eobs = obs[:E]
+            else:
+                eobs = _c5_observed(sg, torch, cfg, stream, M, list(range(E)), dt)
+                a = _c5_gradients(sg, torch, cfg, stream, mat, dt, M, C, list(range(E)), eobs, sg.MIXED)
+                a_tot, a_ms = a["tot"], sum(a["ms"]) / E
+            del mx, obs
+            b = _c5_gradients(sg, torch, cfg, stream, mat, dt, M, C, list(range(E)), eobs, sg.FP64)
             res["error_vs_fp64"] = {
-                "shots": E, "steps": args.ms_err_steps,
-                "mixed_per_shot_ms": sum(a["ms"]) / E, "fp64_per_shot_ms": sum(b["ms"]) / E,
-                "l2_rel": [float((x - y).norm() / y.norm()) for x, y in zip(a["tot"], b["tot"])],
-                "linf_rel": [float((x - y).abs().max() / y.abs().max()) for x, y in zip(a["tot"], b["tot"])],
+                "shots": E, "steps": M,
+                "mixed_per_shot_ms": a_ms, "fp64_per_shot_ms": sum(b["ms"]) / E,
+                "l2_rel": [float((x - y).norm() / y.norm()) for x, y in zip(a_tot, b["tot"])],
+                "linf_rel": [float((x - y).abs().max() / y.abs().max()) for x, y in zip(a_tot, b["tot"])],
                 "against": "sum of the FP64 gradients of the same shots (rho, mu, lambda)"}
-            del out
+            del b
         torch.cuda.empty_cache()
     return res
 
@@ -695,11 +715,10 @@ def c2_receivers(cfg, n, nrec=8):
 
 def _mixed_l2_error(args, sg, torch, stream):
     """The mixed form against the FP64 form over args.err_steps steps of the
-    workload at args.err_n^3: relative L2 difference of the surface receivers'
-    displacement traces (all receivers, components and steps), and of the whole
-    field at the end, relative both to the field then and to its largest norm
-    during the run (the supergrid absorbs the waves, so the field at the end is
-    a small remainder of the peak)."""
+    workload at args.err_n^3: relative L2 and Linf difference of the surface
+    receivers' displacement traces (all receivers, components and steps), and the
+    absolute L2 norms of the whole-field difference at the end beside the FP64
+    field's own norm at the end and at its peak."""
     n = args.err_n
     cfg = c2_config(n)
     rec_xyz = c2_receivers(cfg, n)
@@ -727,10 +746,14 @@ def _mixed_l2_error(args, sg, torch, stream):
     a, b = res
     ta, tb = traces
     d = float(torch.linalg.norm(b - a))
+    # the workload's measure is the receiver traces; the whole field is reported as
+    # absolute L2 norms (the difference at the end, the FP64 field at the end and at
+    # its largest during the run), since the supergrid has absorbed most of the wave
+    # energy by the end and a ratio to the remainder says little
     return {"receivers_l2_rel": float(np.linalg.norm(tb - ta) / np.linalg.norm(ta)),
             "receivers_linf_rel": float(np.abs(tb - ta).max() / np.abs(ta).max()),
-            "field_l2_rel_end": d / float(torch.linalg.norm(a)),
-            "field_l2_rel_peak": d / peak,
+            "field_diff_l2_end": d, "field_l2_end": float(torch.linalg.norm(a)),
+            "field_l2_peak": peak,
             "receivers": {"n": len(rec_xyz), "seed": RECEIVER_SEED, "z": 0.0,
                           "mode": "displacement"},
             "grid": [n, n, n], "steps": args.err_steps, "t_end": args.err_steps * cfl_dt(cfg)}
@@ -777,11 +800,19 @@ def run_ours(args, rank, world):
     peak_hbm, peak_kind = measured_peaks()
     corr_bytes = CORR_STAGE_WORDS * 8 * npts_int
     achieved = corr_bytes / (corr_ms * 1e-3) / 1e9
-    fp64_peak = sg.fma_peak(64, stream=stream)
-    fp64_equiv = CORR_STAGE_REF_FLOPS * npts_int / (corr_ms * 1e-3) / 1e12
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    mhz = fp64["clocks"]["sm_mhz"] or 2070.0
+    fp64_peak = FP64_THREAD_INST_PER_CLK_PER_SM * nsm * mhz * 1e6 / 1e9
+    fp64_rate = 32 * FP64_WARP_INST_PER_PT["corr"] * npts_int / (corr_ms * 1e-3) / 1e9
+    pred_ms = fp64["kernel_ms"]["pred_stage"]
+    fp64_rate_pred = 32 * FP64_WARP_INST_PER_PT["pred"] * npts_int / (pred_ms * 1e-3) / 1e9
     if mixed is not None:
         mixed["roofline"]["peak"] = peak_hbm
         mixed["roofline"]["frac"] = mixed["roofline"]["achieved"] / peak_hbm
+        mb = MIXED_CORR_STAGE_DRAM_BYTES_PER_PT * npts_int / (cm * 1e-3) / 1e9
+        mixed["roofline"].update({"dram_bytes_per_pt": MIXED_CORR_STAGE_DRAM_BYTES_PER_PT,
+                                  "dram_achieved": mb, "dram_frac": mb / peak_hbm,
+                                  "peak_source": peak_kind, "launch_ms": cm})
 
     topo = None if args.no_topo else _time_topo(args, sg, torch, stream, world)
     topo_mixed = None
@@ -796,13 +827,10 @@ def run_ours(args, rank, world):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        ncores = os.cpu_count() or 1
-        os.environ.setdefault("OMP_NUM_THREADS", str(ncores))
-        rate, el, cn, done = cpu_sample(n=args.cpu_n, steps=1, min_seconds=args.cpu_seconds)
-        cpu = {"value": rate, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]),
-               "kind": "port",
-               "sample": f"{done} time steps of a {cn}^3 grid of the workload ({el:.1f} s; oracle "
-                         "restatement of the reference kernels, OpenMP)"}
+        rate, el, kind, cores = cpu_rate(args.n, args.cpu_steps, 1)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": kind,
+               "sample": f"{args.cpu_steps} time steps of the {args.n}^3 workload after 1 untimed "
+                         f"({el:.1f} s; the reference arm's timing function, OpenMP)"}
 
     if rank == 0:
         line = {
@@ -814,18 +842,22 @@ def run_ours(args, rank, world):
                        "grid": [n, n, n], "mode": args.mode, "dt": cfl_dt(c2_config(n)),
                        "l2": "inputs larger than L2 (3.3 GB per field), no flush",
                        "parallelism": "replicas" if world > 1 else "single"},
-            "roofline": {"bound": "hbm", "kernel": "fused corrector stage", "achieved": achieved,
-                         "peak": peak_hbm, "unit": "GB/s", "frac": achieved / peak_hbm,
-                         "traffic": CORR_STAGE_DRAM_BYTES_PER_PT * npts_int,
-                         "traffic_source": "ncu capture at 192^3 scaled per point",
-                         "peak_source": peak_kind,
-                         "algorithmic_bytes_per_launch": corr_bytes, "launch_ms": corr_ms},
-            "fp64_pipe": {"kernel": "fused corrector stage",
-                          "reference_equivalent_tflops": fp64_equiv,
-                          "measured_fma_peak_tflops": fp64_peak,
-                          "frac": fp64_equiv / fp64_peak,
-                          "basis": f"{CORR_STAGE_REF_FLOPS} reference flops per point "
-                                   "(rhs4sg 666 + addsgd4 375 + update 23)"},
+            "roofline": {
+                "bound": "fp64", "kernel": "fused corrector stage (fused_stage_kernel<1>)",
+                "achieved": fp64_rate, "peak": fp64_peak, "unit": "G FP64 thread-instructions/s",
+                "frac": fp64_rate / fp64_peak,
+                "traffic": CORR_STAGE_DRAM_BYTES_PER_PT * npts_int,
+                "basis": f"{32 * FP64_WARP_INST_PER_PT['corr']:.2f} FP64-pipe thread instructions "
+                         "per interior point (ncu smsp__inst_executed_pipe_fp64 x 32 at 512^3) x points "
+                         f"/ launch_ms; peak = {FP64_THREAD_INST_PER_CLK_PER_SM} per clock per SM x "
+                         f"{nsm} SMs x the median sampled SM clock ({mhz:.0f} MHz)",
+                "launch_ms": corr_ms,
+                "predictor": {"achieved": fp64_rate_pred, "frac": fp64_rate_pred / fp64_peak,
+                              "launch_ms": pred_ms},
+                "hbm": {"achieved": achieved, "peak": peak_hbm, "unit": "GB/s",
+                        "frac": achieved / peak_hbm, "peak_source": peak_kind,
+                        "algorithmic_bytes_per_launch": corr_bytes,
+                        "traffic_source": "ncu capture at 192^3 scaled per point"}},
             "kernel_ms": fp64["kernel_ms"],
             "clocks": fp64["clocks"],
             "e2e": fp64.get("e2e"),
@@ -849,9 +881,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--mode", choices=["fused", "phases"], default="fused")
     ap.add_argument("--n", type=int, default=512, help="grid points per axis")
-    ap.add_argument("--cpu-n", type=int, default=256, help="CPU sample grid points per axis")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0,
-                    help="minimum CPU work of the baseline sample")
+    ap.add_argument("--cpu-steps", type=int, default=4,
+                    help="timed CPU steps of the in-line CPU baseline (same workload as the GPU)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the FP32-mixed form")
@@ -865,9 +896,9 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=2000, help="steps of the adjoint workload")
     ap.add_argument("--adj-ckpt", type=int, default=100, help="checkpoint spacing")
     ap.add_argument("--no-multishot", action="store_true", help="skip the multi-shot gradient workload")
-    ap.add_argument("--ms-shots", type=int, default=2, help="timed shots of the multi-shot workload (of 16)")
+    ap.add_argument("--ms-shots", type=int, default=16, help="timed shots of the multi-shot workload (of 16)")
     ap.add_argument("--ms-steps", type=int, default=1500, help="steps of the multi-shot workload")
-    ap.add_argument("--ms-err-steps", type=int, default=150, help="steps of the mixed-vs-FP64 gradient check")
+    ap.add_argument("--ms-err-steps", type=int, default=1500, help="steps of the mixed-vs-FP64 gradient check")
     ap.add_argument("--ms-err-shots", type=int, default=2,
                     help="shots whose summed gradient is compared with FP64 (0: skip)")
     ap.add_argument("--only-c2", choices=["fp64", "mixed"], default=None,
@@ -875,7 +906,7 @@ def main():
     ap.add_argument("--only-topo", choices=["fp64", "mixed"], default=None,
                     help="time only the topography workload in that form (for profiling)")
     ap.add_argument("--no-err", action="store_true", help="skip the mixed-vs-FP64 error run")
-    ap.add_argument("--err-n", type=int, default=256, help="grid of the mixed-vs-FP64 error run")
+    ap.add_argument("--err-n", type=int, default=512, help="grid of the mixed-vs-FP64 error run")
     ap.add_argument("--err-steps", type=int, default=1000, help="steps of the error run")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
