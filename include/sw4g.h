@@ -360,6 +360,54 @@ int sw4g_ew_set_gradient_memory(sw4g_ew* ew, long long max_bytes);
 int sw4g_ew_write_checkpoint(sw4g_ew* ew, const char* path, int cycle);
 int sw4g_ew_read_checkpoint(sw4g_ew* ew, const char* path, int* cycle);
 
+/* ---------------------------------------------------------------------------
+ * Domain decomposition: subdomains and halo exchange
+ * ------------------------------------------------------------------------- */
+
+/* Elements (doubles) of one side's halo of a 3-component FP64 field along axis 0 (x)
+ * or 1 (y): the 2 planes next to the side over the full extent of the other two
+ * axes, ghosts included; -1 for bad bounds.  With sw4g_halo_pack / _unpack, replaces
+ * the reference's halo packing (EW::pack_HaloArrayCU_X/Y and unpack_HaloArrayCU_X/Y,
+ * src/EW_cuda.C:1515-1698) for one side: pack copies the two interior planes next
+ * to side (0 low, 1 high) into buf, unpack copies buf into that side's two ghost
+ * planes (the neighbour's interior planes across the shared side). */
+long long sw4g_halo_len(int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast, int axis);
+int sw4g_halo_pack(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                   int axis, int side, const double* u, double* buf, void* stream);
+int sw4g_halo_unpack(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                     int axis, int side, const double* buf, double* u, void* stream);
+
+/* The EW object of the subdomain of the global grid g whose interior points are
+ * i0..i1 x j0..j1 (1-based, global; all nz planes), on the current device: the
+ * reference's per-rank grid of its 2-D (i, j) decomposition (src/EW.C:1921-1949).
+ * Sides shared with a neighbour get no boundary closure (bProcessor); the supergrid
+ * profiles are the global grid's, and sources are discretised on the global grid
+ * and kept on this subdomain's interior points, so the subdomains of a grid
+ * reproduce the undivided run.  Material, levels and receivers are the
+ * subdomain's own arrays (nx = i1-i0+1, ny = j1-j0+1, 2 ghost points per side, the
+ * ghost planes at shared sides holding the neighbours' values).  Periodic axes
+ * cannot be divided (SW4G_NOT_SUPPORTED). */
+int sw4g_ew_create_subdomain(const sw4g_grid* g, int i0, int i1, int j0, int j1, void* stream,
+                             sw4g_ew** out);
+/* One fused step of a subdomain in three parts; after part 0 and after part 1 the
+ * caller exchanges the halos of the level the part left (the reference's exchange
+ * points after the predictor and after the corrector, src/EW.C:2596-2616,
+ * 2728-2744): x sides first, then y sides.  Parts run in the order 0, 1, 2. */
+int sw4g_ew_step_part(sw4g_ew* ew, int part);
+/* Bytes of one side's halo along axis in the object's level format (FP64 or the
+ * FP32-mixed form's double-float pairs); pack / unpack that side of the level to
+ * exchange to / from a device buffer of that size on the object's stream. */
+long long sw4g_ew_halo_bytes(const sw4g_ew* ew, int axis);
+int sw4g_ew_halo_pack(sw4g_ew* ew, int axis, int side, void* buf);
+int sw4g_ew_halo_unpack(sw4g_ew* ew, int axis, int side, const void* buf);
+/* nsteps steps of n subdomains in lockstep inside one process, with the halo
+ * exchanges between them: neighbors[4 s + q] is the subdomain across side q (x-low,
+ * x-high, y-low, y-high) of subdomain s, or -1 for a physical side.  The subdomains
+ * may sit on different GPUs: halos travel by device-to-device copies into the
+ * receiving GPU's own memory, ordered by events on the objects' streams (the
+ * reference's MPI Sendrecv of packed halos, src/EW_cuda.C:1699-1900). */
+int sw4g_ew_step_group(sw4g_ew* const* subs, int n, const int* neighbors, int nsteps);
+
 /* Topography (replaces the reference's topography + curvilinear grid set-up,
  * src/EW.C:540-720 (deck), 2018-2046 (dimensions), 6164 (generate_grid), 6229
  * (setup_metric), and the curvilinear grid's share of every phase of the time

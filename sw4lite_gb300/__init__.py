@@ -116,6 +116,16 @@ _SIGS = {
     "sw4g_discretize_source": ([C.POINTER(GridDesc), C.POINTER(SourceDesc), C.c_int, _I, _D, _I],
                                C.c_int),
     "sw4g_ew_create": ([C.POINTER(GridDesc), _VP, C.POINTER(_VP)], C.c_int),
+    "sw4g_ew_create_subdomain": ([C.POINTER(GridDesc), C.c_int, C.c_int, C.c_int, C.c_int, _VP,
+                                  C.POINTER(_VP)], C.c_int),
+    "sw4g_ew_step_part": ([_VP, C.c_int], C.c_int),
+    "sw4g_ew_halo_bytes": ([_VP, C.c_int], C.c_longlong),
+    "sw4g_ew_halo_pack": ([_VP, C.c_int, C.c_int, _VP], C.c_int),
+    "sw4g_ew_halo_unpack": ([_VP, C.c_int, C.c_int, _VP], C.c_int),
+    "sw4g_ew_step_group": ([C.POINTER(_VP), C.c_int, _I, C.c_int], C.c_int),
+    "sw4g_halo_len": ([C.c_int] * 6 + [C.c_int], C.c_longlong),
+    "sw4g_halo_pack": ([C.c_int] * 9 + [_VP, _VP, _VP], C.c_int),
+    "sw4g_halo_unpack": ([C.c_int] * 9 + [_VP, _VP, _VP], C.c_int),
     "sw4g_ew_create_topo": ([C.POINTER(GridDesc), C.POINTER(TopoDesc), _VP, C.POINTER(_VP)],
                             C.c_int),
     "sw4g_ew_num_grids": ([_VP], C.c_int),
@@ -269,18 +279,45 @@ def _stream_ptr(stream) -> int | None:
 class EW:
     """One Cartesian grid's time loop on the GPU (sw4g_ew_* in include/sw4g.h)."""
 
-    def __init__(self, grid: GridDesc, stream=None, topo: TopoDesc = None):
-        self.grid = grid
+    def __init__(self, grid: GridDesc, stream=None, topo: TopoDesc = None, subdomain=None):
+        """subdomain=(i0, i1, j0, j1): the object of that block of interior points of the
+        global grid `grid` (sw4g_ew_create_subdomain); self.grid is then the local grid."""
         self._stream = _stream_ptr(stream)
         h = _VP()
-        if topo is None:
+        if subdomain is not None:
+            i0, i1, j0, j1 = subdomain
+            check(lib().sw4g_ew_create_subdomain(C.byref(grid), i0, i1, j0, j1, self._stream,
+                                                 C.byref(h)), "sw4g_ew_create_subdomain")
+            loc = GridDesc.from_buffer_copy(grid)
+            loc.nx, loc.ny = i1 - i0 + 1, j1 - j0 + 1
+            grid = loc
+            self.subdomain = tuple(subdomain)
+        elif topo is None:
             check(lib().sw4g_ew_create(C.byref(grid), self._stream, C.byref(h)), "sw4g_ew_create")
         else:
             check(lib().sw4g_ew_create_topo(C.byref(grid), C.byref(topo), self._stream,
                                             C.byref(h)), "sw4g_ew_create_topo")
+        self.grid = grid
         self._h = h
         self.npts = lib().sw4g_ew_npts(h)
         self.shape = (grid.nz + 4, grid.ny + 4, grid.nx + 4)
+
+    # --- subdomains of a decomposed grid ---
+    def step_part(self, part):
+        check(lib().sw4g_ew_step_part(self._h, part), "step_part")
+
+    def halo_bytes(self, axis) -> int:
+        return lib().sw4g_ew_halo_bytes(self._h, axis)
+
+    def halo_pack(self, axis, side, buf):
+        """Pack side (0 low, 1 high) along axis of the level to exchange into buf (a
+        device tensor of halo_bytes(axis) bytes)."""
+        with self._ordered(buf):
+            check(lib().sw4g_ew_halo_pack(self._h, axis, side, _ptr(buf)), "halo_pack")
+
+    def halo_unpack(self, axis, side, buf):
+        with self._ordered(buf):
+            check(lib().sw4g_ew_halo_unpack(self._h, axis, side, _ptr(buf)), "halo_unpack")
 
     @contextlib.contextmanager
     def _ordered(self, *arrays):
@@ -636,3 +673,13 @@ def set_mixed_tma(on=True) -> None:
     """Comparison switch: FP32-mixed stages on the tensor-copy kernels (default) or
     on the synchronous kernels."""
     check(lib().sw4g_dev_set_mixed_tma(1 if on else 0), "set_mixed_tma")
+
+
+def step_group(subs, neighbors, nsteps):
+    """nsteps lockstep steps of subdomain EW objects with their halo exchanges;
+    neighbors[s] = (x-low, x-high, y-low, y-high) indices into subs or -1."""
+    n = len(subs)
+    hs = (_VP * n)(*[e._h for e in subs])
+    nb = (C.c_int * (4 * n))(*[int(x) for row in neighbors for x in row])
+    check(lib().sw4g_ew_step_group(hs, n, nb, nsteps), "step_group")
+

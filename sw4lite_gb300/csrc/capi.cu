@@ -454,6 +454,96 @@ int sw4g_ew_create(const sw4g_grid* g, void* stream, sw4g_ew** out)
    return SW4G_OK;
 }
 
+int sw4g_ew_create_subdomain(const sw4g_grid* global, int i0, int i1, int j0, int j1, void* stream,
+                             sw4g_ew** out)
+{
+   if (!global || !out) return SW4G_BAD_ARGUMENT;
+   *out = nullptr;
+   const GridSpec gs = to_spec(global);
+   if (i0 < 1 || j0 < 1 || i1 > gs.nx || j1 > gs.ny || i1 < i0 || j1 < j0) return SW4G_BAD_ARGUMENT;
+   GridSpec ls = gs;
+   ls.nx = i1 - i0 + 1;
+   ls.ny = j1 - j0 + 1;
+   const bool edge[4] = {i0 == 1, i1 == gs.nx, j0 == 1, j1 == gs.ny};
+   for (int q = 0; q < 4; q++) {
+      if (edge[q]) continue;
+      // a periodic axis would need its wrap-around exchanged too
+      if (gs.bc[q] == kPeriodic) return SW4G_NOT_SUPPORTED;
+      ls.bc[q] = kProcessor;
+   }
+   EW* e = new (std::nothrow) EW(ls, as_stream(stream));
+   if (!e) return SW4G_BAD_ARGUMENT;
+   int st = e->set_subdomain(gs, i0 - 1, j0 - 1);
+   if (st == SW4G_OK) st = e->init();
+   if (st != SW4G_OK) {
+      delete e;
+      return st;
+   }
+   sw4g_ew* h = new (std::nothrow) sw4g_ew{e};
+   if (!h) {
+      delete e;
+      return SW4G_BAD_ARGUMENT;
+   }
+   *out = h;
+   return SW4G_OK;
+}
+
+int sw4g_ew_step_part(sw4g_ew* ew, int part)
+{
+   return ew ? ew->impl->step_part(part) : SW4G_BAD_ARGUMENT;
+}
+
+long long sw4g_ew_halo_bytes(const sw4g_ew* ew, int axis)
+{
+   if (!ew || (axis != 0 && axis != 1) || !ew->impl->is_subdomain()) return -1;
+   return ew->impl->halo_bytes(axis);
+}
+
+int sw4g_ew_halo_pack(sw4g_ew* ew, int axis, int side, void* buf)
+{
+   return ew ? ew->impl->halo_pack(axis, side, buf) : SW4G_BAD_ARGUMENT;
+}
+
+int sw4g_ew_halo_unpack(sw4g_ew* ew, int axis, int side, const void* buf)
+{
+   return ew ? ew->impl->halo_unpack(axis, side, buf) : SW4G_BAD_ARGUMENT;
+}
+
+int sw4g_ew_step_group(sw4g_ew* const* subs, int n, const int* neighbors, int nsteps)
+{
+   if (!subs || n < 1 || n > 4096 || !neighbors) return SW4G_BAD_ARGUMENT;
+   std::vector<EW*> v(n);
+   for (int s = 0; s < n; s++) {
+      if (!subs[s]) return SW4G_BAD_ARGUMENT;
+      v[s] = subs[s]->impl;
+   }
+   return step_group(v.data(), n, neighbors, nsteps);
+}
+
+long long sw4g_halo_len(int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast, int axis)
+{
+   if (!bounds_ok(ifirst, ilast, jfirst, jlast, kfirst, klast) || (axis != 0 && axis != 1)) return -1;
+   return halo_len(make_box(1, ifirst, ilast, jfirst, jlast, kfirst, klast), axis, 3);
+}
+
+int sw4g_halo_pack(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                   int axis, int side, const double* u, double* buf, void* stream)
+{
+   if (!bounds_ok(ifirst, ilast, jfirst, jlast, kfirst, klast) || !u || !buf) return SW4G_BAD_ARGUMENT;
+   if (ilast - ifirst < 7 || jlast - jfirst < 7) return SW4G_BAD_ARGUMENT;
+   return launch_halo_copy(make_box(soa, ifirst, ilast, jfirst, jlast, kfirst, klast), axis, side, true,
+                           false, 3, const_cast<double*>(u), buf, as_stream(stream));
+}
+
+int sw4g_halo_unpack(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                     int axis, int side, const double* buf, double* u, void* stream)
+{
+   if (!bounds_ok(ifirst, ilast, jfirst, jlast, kfirst, klast) || !u || !buf) return SW4G_BAD_ARGUMENT;
+   if (ilast - ifirst < 7 || jlast - jfirst < 7) return SW4G_BAD_ARGUMENT;
+   return launch_halo_copy(make_box(soa, ifirst, ilast, jfirst, jlast, kfirst, klast), axis, side, false,
+                           false, 3, u, const_cast<double*>(buf), as_stream(stream));
+}
+
 int sw4g_ew_create_topo(const sw4g_grid* g, const sw4g_topography* t, void* stream, sw4g_ew** out)
 {
    if (!g || !t || !out) return SW4G_BAD_ARGUMENT;

@@ -26,6 +26,7 @@ EW::~EW()
    };
    f(dclock_);
    f(dstat_);
+   for (auto* p : xbuf_) f(p);
    f(rho_);
    f(mu_);
    f(la_);
@@ -63,6 +64,7 @@ int EW::init()
          if (t != kInterface) return kBadArgument;  // the top is the curvilinear grid
          continue;
       }
+      if (t == kProcessor && sub_ && s < 4) continue;  // a side shared with a neighbour
       if (!(t == kStressFree || t == kDirichlet || t == kSuperGrid || t == kPeriodic)) return kBadArgument;
       if (t == kStressFree && s < 4) return kNotSupported;
    }
@@ -79,9 +81,14 @@ int EW::init()
    onesided_flags(g_, onesided_);
    double acof[384], ghcof[6], bope[48];
    sbp_coefficients(acof, ghcof, bope, sbop_);
-   prof_ = supergrid_profiles(g_);
+   prof_ = sub_ ? subdomain_profiles(global_, g_, ioff_, joff_) : supergrid_profiles(g_);
 
    const size_t n = (size_t)npts_;
+   SW4G_TRY(cuda_ok(cudaGetDevice(&dev_)));
+   if (sub_) {
+      const size_t hb = (size_t)std::max(halo_bytes(0), halo_bytes(1));
+      for (auto*& p : xbuf_) SW4G_TRY(cuda_ok(cudaMalloc(&p, hb)));
+   }
    SW4G_TRY(cuda_ok(cudaMalloc(&dstat_, 4 * sizeof(unsigned long long))));
    {
       const unsigned long long init[4] = {0, 0, ~0ull, 0};
@@ -189,9 +196,37 @@ int EW::add_source(const SourceSpec& s)
       const CurvSourceGrid cs = curv_source_grid();
       if (discretize_source_topo(g_, onesided_, &cs, s, hsrc_, hsrc_curv_) != 0) return kBadArgument;
    } else {
-      discretize_source(g_, onesided_, s, hsrc_);
+      discretize_into(s, hsrc_);
    }
    src_dirty_ = true;
+   return kOk;
+}
+
+void EW::discretize_into(const SourceSpec& s, std::vector<GridPointSource>& out) const
+{
+   if (!sub_) {
+      discretize_source(g_, onesided_, s, out);
+      return;
+   }
+   // the global grid's grid-point sources, in the reference's order, on this
+   // subdomain's interior points (src/Source.C: interior_point_in_proc)
+   std::vector<GridPointSource> all;
+   discretize_source(global_, onesided_, s, all);
+   for (GridPointSource p : all) {
+      p.i -= ioff_;
+      p.j -= joff_;
+      if (p.i >= 1 && p.i <= g_.nx && p.j >= 1 && p.j <= g_.ny) out.push_back(p);
+   }
+}
+
+int EW::set_subdomain(const GridSpec& global, int ioff, int joff)
+{
+   if (ready_) return kBadArgument;
+   if (ioff < 0 || joff < 0 || ioff + g_.nx > global.nx || joff + g_.ny > global.ny) return kBadArgument;
+   global_ = global;
+   ioff_ = ioff;
+   joff_ = joff;
+   sub_ = true;
    return kOk;
 }
 
@@ -232,12 +267,12 @@ int EW::clear_sources()
 int EW::set_source_discretization(bool on_device)
 {
    if (!ready_) return kBadArgument;
-   if (on_device && (cv_ || raw_src_ > 0)) return kNotSupported;
+   if (on_device && (cv_ || raw_src_ > 0 || sub_)) return kNotSupported;
    if (on_device == dev_src_) return kOk;
    dev_src_ = on_device;
    if (!on_device) {  // the host list from the sources added meanwhile
       hsrc_.clear();
-      for (const SourceSpec& s : specs_) discretize_source(g_, onesided_, s, hsrc_);
+      for (const SourceSpec& s : specs_) discretize_into(s, hsrc_);
    }
    src_dirty_ = true;
    return kOk;
@@ -475,6 +510,7 @@ int EW::ensure_phase_arrays()
 int EW::step(int nsteps, int mode)
 {
    if (!ready_ || !material_ || !(dt_ > 0) || nsteps < 0) return kBadArgument;
+   if (sub_) return kNotSupported;  // a subdomain steps by step_part with halo exchanges
    if (cv_ && !cv_->material) return kBadArgument;
    if (mode != kModePhases && mode != kModeFused) return kBadArgument;
    if (mixed_ && mode == kModePhases) return kNotSupported;
@@ -835,10 +871,11 @@ int EW::fused_piece(int piece, int ip, int iq)
                                        zc_[side], stream_, rscr_));
       return kOk;
    }
-   if (piece == 2) {
-      SW4G_TRY(launch_force_update(1, bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, up, rho_, dsrc_, t_, 0,
-                                   dt2, stream_, clocked_ ? dclock_ : nullptr));
-      return enforce_bc(up);
+   if (piece == 2 || piece == kForcePred || piece == kBcPred) {
+      if (piece != kBcPred)
+         SW4G_TRY(launch_force_update(1, bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, up, rho_, dsrc_, t_,
+                                      0, dt2, stream_, clocked_ ? dclock_ : nullptr));
+      return piece == kForcePred ? kOk : enforce_bc(up);
    }
    if (piece == 4) {
       SW4G_TRY(launch_ghost_shell(b, 1, out, u, um, up, stream_));
@@ -858,10 +895,11 @@ int EW::fused_piece(int piece, int ip, int iq)
                                 stream_));
       return kOk;
    }
-   if (piece == 5) {
-      SW4G_TRY(launch_force_update(1, bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, out, rho_, dsrc_, t_, 1,
-                                   dt2 * dt2 / 12, stream_, clocked_ ? dclock_ : nullptr));
-      return enforce_bc(out);
+   if (piece == 5 || piece == kForceCorr || piece == kBcCorr) {
+      if (piece != kBcCorr)
+         SW4G_TRY(launch_force_update(1, bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, out, rho_, dsrc_, t_,
+                                      1, dt2 * dt2 / 12, stream_, clocked_ ? dclock_ : nullptr));
+      return piece == kForceCorr ? kOk : enforce_bc(out);
    }
    return kBadArgument;
 }
@@ -929,9 +967,11 @@ int EW::mixed_piece(int piece, int ip, int iq)
       }
       return kOk;
    }
-   if (piece == 2) {
-      SW4G_TRY(launch_force_update_df(bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, up, rho_, dsrc_, t_,
-                                      0, dt2, stream_, clocked_ ? dclock_ : nullptr));
+   if (piece == 2 || piece == kForcePred || piece == kBcPred) {
+      if (piece != kBcPred)
+         SW4G_TRY(launch_force_update_df(bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, up, rho_, dsrc_, t_,
+                                         0, dt2, stream_, clocked_ ? dclock_ : nullptr));
+      if (piece == kForcePred) return kOk;
       return launch_bcfortsg_df(bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, wind_, g_.nx, g_.ny, g_.nz,
                                 up, g_.h, g_.bc, sbop_, mu_, la_, dprof_[3], dprof_[4], stream_);
    }
@@ -952,9 +992,11 @@ int EW::mixed_piece(int piece, int ip, int iq)
       }
       return kOk;
    }
-   if (piece == 5) {
-      SW4G_TRY(launch_force_update_df(bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, out, rho_, dsrc_, t_,
-                                      1, dt2 * dt2 / 12, stream_, clocked_ ? dclock_ : nullptr));
+   if (piece == 5 || piece == kForceCorr || piece == kBcCorr) {
+      if (piece != kBcCorr)
+         SW4G_TRY(launch_force_update_df(bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, out, rho_, dsrc_, t_,
+                                         1, dt2 * dt2 / 12, stream_, clocked_ ? dclock_ : nullptr));
+      if (piece == kForceCorr) return kOk;
       return launch_bcfortsg_df(bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, wind_, g_.nx, g_.ny, g_.nz,
                                 out, g_.h, g_.bc, sbop_, mu_, la_, dprof_[3], dprof_[4], stream_);
    }
@@ -980,6 +1022,42 @@ int EW::step_fused()
    ium_ = iu_;
    iu_ = iq;
    t_ += dt_;
+   return kOk;
+}
+
+int EW::step_part(int part)
+{
+   if (!sub_ || part != part_) return kBadArgument;
+   if (part == 0) {
+      if (!ready_ || !material_ || !(dt_ > 0) || graphs_) return kBadArgument;
+      if (drec_.n > 0 && rec_rows_ + (rec_initial_ ? 1 : 0) + 1 > rec_cap_) return kBadArgument;
+      SW4G_TRY(upload_sources());
+      if (drec_.n > 0 && rec_initial_) {
+         SW4G_TRY(record(lev_[iu_], lev_[ium_], 1));
+         rec_initial_ = false;
+      }
+      int ip = 0;
+      while (ip == iu_ || ip == ium_) ip++;
+      int iq = ip + 1;
+      while (iq == iu_ || iq == ium_) iq++;
+      split_ip_ = ip;
+      split_iq_ = iq;
+      SW4G_TRY(piece(0, ip, iq));
+      SW4G_TRY(piece(1, ip, iq));
+      SW4G_TRY(piece(kForcePred, ip, iq));
+   } else if (part == 1) {
+      SW4G_TRY(piece(kBcPred, split_ip_, split_iq_));
+      SW4G_TRY(piece(3, split_ip_, split_iq_));
+      SW4G_TRY(piece(4, split_ip_, split_iq_));
+      SW4G_TRY(piece(kForceCorr, split_ip_, split_iq_));
+   } else {
+      SW4G_TRY(piece(kBcCorr, split_ip_, split_iq_));
+      if (drec_.n > 0) SW4G_TRY(record(lev_[split_iq_], lev_[ium_], 0));
+      ium_ = iu_;
+      iu_ = split_iq_;
+      t_ += dt_;
+   }
+   part_ = (part + 1) % 3;
    return kOk;
 }
 

@@ -66,6 +66,10 @@ class EW {
    EW(const EW&) = delete;
    EW& operator=(const EW&) = delete;
 
+   // Makes this object the subdomain of `global` whose interior points are the global
+   // points i = ioff + 1 .. ioff + nx, j = joff + 1 .. joff + ny of this object's grid
+   // (sides shared with a neighbour are kProcessor).  Call before init().
+   int set_subdomain(const GridSpec& global, int ioff, int joff);
    int init();  // allocates device memory; returns a Status
    const GridSpec& grid() const { return g_; }
    const Bounds& bounds() const { return b_; }
@@ -99,6 +103,27 @@ class EW {
    double* field_um() const { return lev_[ium_]; }
 
    int step(int nsteps, int mode);
+   // A subdomain's fused step in three parts, with a halo exchange of the level the
+   // part leaves after parts 0 and 1 (the reference's exchange points after the
+   // predictor and after the corrector, src/EW.C:2596-2616, 2728-2744): part 0 the
+   // predictor stage, its one-sided rows and forcing; part 1 the predictor's boundary
+   // closures, the corrector stage, rows, damping and forcing; part 2 the corrector's
+   // boundary closures, receivers, level rotation and time.  Parts run in order.
+   int step_part(int part);
+   bool is_subdomain() const { return sub_; }
+   int device() const { return dev_; }
+   // bytes of one side's halo along axis (0 x, 1 y) in the level's storage format
+   long long halo_bytes(int axis) const;
+   // pack the two interior planes next to side (0 low, 1 high) of the level to
+   // exchange into buf, or unpack buf into that side's two ghost planes (halo.cu)
+   int halo_pack(int axis, int side, void* buf) { return halo_copy(axis, side, true, buf); }
+   int halo_unpack(int axis, int side, const void* buf)
+   {
+      return halo_copy(axis, side, false, const_cast<void*>(buf));
+   }
+   // the object's own exchange buffers (device memory of its GPU), halo_bytes each
+   void* send_buffer(int axis, int side) const { return xbuf_[2 * axis + side]; }
+   void* recv_buffer(int axis, int side) const { return xbuf_[4 + 2 * axis + side]; }
    // Non-finite check of the time loop (the reference's checkfornan, src/EW.C:1333,
    // 2544-2759): every `every` steps (and after the last step of a step() call) the
    // new level of every grid is scanned; step() then synchronises and returns
@@ -178,6 +203,10 @@ class EW {
 
  private:
    int upload_sources();
+   int halo_copy(int axis, int side, bool pack, void* buf);
+   // discretise one source into hsrc_ (on the global grid for a subdomain, keeping
+   // the entries on this subdomain's interior points)
+   void discretize_into(const SourceSpec& s, std::vector<GridPointSource>& out) const;
    int scan_levels();                 // non-finite scans of the current levels, then the verdict
    int read_status(unsigned long long out[4]);
    int record(double* up, double* um, int initial);
@@ -186,6 +215,8 @@ class EW {
    int fused_piece(int piece, int ip, int iq);
    int mixed_piece(int piece, int ip, int iq);
    int piece(int which, int ip, int iq) { return mixed_ ? mixed_piece(which, ip, iq) : fused_piece(which, ip, iq); }
+   // pieces 2 and 5 split at a subdomain's exchange points: forcing, then closures
+   static constexpr int kForcePred = 6, kBcPred = 7, kForceCorr = 8, kBcCorr = 9;
    int ensure_staging();
    int init_topo();
    int curv_pred(int ip);
@@ -272,6 +303,12 @@ class EW {
    int* stage_emax_ = nullptr;        // gradient(): exponent maximum of the corrector's levels
 
    double t_ = 0, dt_ = 0;
+   // subdomain of a decomposed grid
+   bool sub_ = false;
+   GridSpec global_{};
+   int ioff_ = 0, joff_ = 0, dev_ = 0;
+   int part_ = 0, split_ip_ = 0, split_iq_ = 0;  // step_part state
+   void* xbuf_[8] = {};                           // send (4) and receive (4) halo buffers
    unsigned long long* dstat_ = nullptr;  // status block (kernels.h): flags, count, first offset
    int nan_every_ = 0;
    NanReport nan_{};
@@ -284,5 +321,10 @@ class EW {
    };
    std::vector<GraphKey> graph_cache_;
 };
+
+// Steps subdomain objects in lockstep with halo exchanges between them (halo.cu);
+// nb[4 s + q] is the neighbour of subdomain s across side q (x-low, x-high, y-low,
+// y-high) or -1.
+int step_group(EW* const* subs, int n, const int* nb, int nsteps);
 
 }  // namespace sw4g

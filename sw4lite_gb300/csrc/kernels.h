@@ -281,6 +281,15 @@ int launch_force_update_f32(int soa, int ib, int ie, int jb, int je, int kb, int
                             double coef, cudaStream_t s);
 
 int launch_mixed_stage(const MixedStage& st, cudaStream_t stream);
+// Halo planes of a decomposed grid (halo.cu): the first of the two planes a side
+// sends (pack: the interior planes next to it) or receives (the ghost planes), the
+// elements of one side's halo, and the pack / unpack of those planes of a field of
+// ncomp components of float or double.
+int halo_first_plane(const Box& b, int axis, int side, bool pack);
+long long halo_len(const Box& b, int axis, int ncomp);
+int launch_halo_copy(const Box& b, int axis, int side, bool pack, bool is_float, int ncomp,
+                     void* field, void* buf, cudaStream_t s);
+
 // Status block of an EW object (device, 4 words): [0] flags (bit kTimeout: an
 // mbarrier wait gave up), [1] non-finite values found by the scans, [2] the
 // smallest offending storage offset, tagged with its grid above kScanGridShift.

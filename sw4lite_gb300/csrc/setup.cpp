@@ -107,6 +107,21 @@ SupergridProfiles supergrid_profiles(const GridSpec& g)
    return p;
 }
 
+SupergridProfiles subdomain_profiles(const GridSpec& global, const GridSpec& local, int ioff,
+                                     int joff)
+{
+   const SupergridProfiles gp = supergrid_profiles(global);
+   SupergridProfiles p;
+   p.used = gp.used;
+   const int off[3] = {ioff, joff, 0}, n[3] = {local.nx + 4, local.ny + 4, local.nz + 4};
+   for (int ax = 0; ax < 3; ax++) {
+      p.dc[ax].assign(gp.dc[ax].begin() + off[ax], gp.dc[ax].begin() + off[ax] + n[ax]);
+      p.str[ax].assign(gp.str[ax].begin() + off[ax], gp.str[ax].begin() + off[ax] + n[ax]);
+      p.co[ax].assign(gp.co[ax].begin() + off[ax], gp.co[ax].begin() + off[ax] + n[ax]);
+   }
+   return p;
+}
+
 void boundary_windows(const GridSpec& g, int wind[36], int npts[6])
 {
    const Bounds b = grid_bounds(g);

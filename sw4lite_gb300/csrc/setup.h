@@ -17,6 +17,7 @@ enum Bc : int {
    kSuperGrid = 2,
    kPeriodic = 3,
    kInterface = 4,  // bCCInterface: the top of a Cartesian grid below a curvilinear grid
+   kProcessor = 7,  // bProcessor: a side shared with a neighbouring subdomain (halo exchange)
    kNone = 8
 };
 
@@ -46,6 +47,10 @@ struct SupergridProfiles {
    bool used = false;
 };
 SupergridProfiles supergrid_profiles(const GridSpec& g);
+// The profiles of a subdomain: the global grid's profiles at the subdomain's array
+// indices (local i = global i - ioff, local j = global j - joff).
+SupergridProfiles subdomain_profiles(const GridSpec& global, const GridSpec& local, int ioff,
+                                     int joff);
 
 // Boundary windows and point counts per side (src/EW.C:3347-3444) and the
 // one-sided flags of the top/bottom sides (src/EW.C:4863-4868).
