@@ -147,6 +147,13 @@ int sw4g_addsgd4cfort(int soa, int ifirst, int ilast, int jfirst, int jlast, int
                       const double* dcx, const double* dcy, const double* strx, const double* stry,
                       const double* jac, const double* cox, const double* coy, double beta,
                       void* stream);
+/* 6th-order supergrid damping in x and y on a curvilinear grid; replaces
+ * EW::addsgd6cfort / addsgd6cfort_indrev (src/ew-cfromfort.C:1241, :1405). */
+int sw4g_addsgd6cfort(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                      double* up, const double* u, const double* um, const double* rho,
+                      const double* dcx, const double* dcy, const double* strx, const double* stry,
+                      const double* jac, const double* cox, const double* coy, double beta,
+                      void* stream);
 
 /* dt = cfl / sqrt(max over the grid of -lambda_min(A)/(4 rho)), the curvilinear
  * limit of EW::computeDT (src/EW.C:5066-5125).  The reference gets lambda_min from

@@ -185,8 +185,11 @@ def freesurfcurvisg(soa, bounds, nz, side, u, mu, la, met, sbop, forcing, strx, 
 
 
 def addsgd4c(soa, bounds, up, u, um, rho, dcx, dcy, strx, stry, jac, cox, coy, beta,
-             which="oracle"):
-    fn = ref().sw4ref_addsgd4c if which == "ref" else lib().sw4o_addsgd4c
+             which="oracle", order=4):
+    if order == 6:
+        fn = ref().sw4ref_addsgd6c if which == "ref" else lib().sw4o_addsgd6c
+    else:
+        fn = ref().sw4ref_addsgd4c if which == "ref" else lib().sw4o_addsgd4c
     fn(C.c_int(soa), *[C.c_int(b) for b in bounds], _dp(up), _dp(u), _dp(um), _dp(rho), _dp(dcx),
        _dp(dcy), _dp(strx), _dp(stry), _dp(jac), _dp(cox), _dp(coy), C.c_double(beta))
 

@@ -138,6 +138,20 @@ void sw4ref_addsgd4c(int soa, int ifirst, int ilast, int jfirst, int jlast, int 
                        strx, stry, jac, cox, coy, beta);
 }
 
+void sw4ref_addsgd6c(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst,
+                     int klast, double* up, double* u, double* um, double* rho, double* dcx,
+                     double* dcy, double* strx, double* stry, double* jac, double* cox,
+                     double* coy, double beta)
+{
+   EW* ew = kernel_host(soa);
+   if (soa)
+      ew->addsgd6cfort_indrev(ifirst, ilast, jfirst, jlast, kfirst, klast, up, u, um, rho, dcx,
+                              dcy, strx, stry, jac, cox, coy, beta);
+   else
+      ew->addsgd6cfort(ifirst, ilast, jfirst, jlast, kfirst, klast, up, u, um, rho, dcx, dcy,
+                       strx, stry, jac, cox, coy, beta);
+}
+
 void sw4ref_bcfortsg(int soa, int ib, int ie, int jb, int je, int kb, int ke, int* wind, int nx,
                      int ny, int nz, double* u, double h, const int* bccnd_int, double* sbop,
                      double* mu, double* la, double t, double* bf1, double* bf2, double* bf3,
@@ -367,7 +381,14 @@ void sw4ref_step_topo(const sw4o_problem* p, const sw4o_curv* cv, double t, doub
    ew->corrfort(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, lu, f, D(p->rho), dt * dt * dt * dt);
    ew->corrfort(cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cup, clu, cf, D(cv->rho),
                 dt * dt * dt * dt);
-   if (p->sg_beta != 0) {
+   if (p->sg_beta != 0 && p->sg_order == 6) {
+      ew->addsgd6fort_indrev(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, D(u), D(um), D(p->rho),
+                             D(p->dcx), D(p->dcy), D(p->dcz), D(p->strx), D(p->stry), D(p->strz),
+                             D(p->cox), D(p->coy), D(p->coz), p->sg_beta);
+      ew->addsgd6cfort_indrev(cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cup, D(cu), D(cum),
+                              D(cv->rho), D(cv->dcx), D(cv->dcy), D(cv->strx), D(cv->stry),
+                              D(cv->jac), D(cv->cox), D(cv->coy), p->sg_beta);
+   } else if (p->sg_beta != 0) {
       ew->addsgd4fort_indrev(p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, D(u), D(um), D(p->rho),
                              D(p->dcx), D(p->dcy), D(p->dcz), D(p->strx), D(p->stry), D(p->strz),
                              D(p->cox), D(p->coy), D(p->coz), p->sg_beta);

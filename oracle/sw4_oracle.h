@@ -130,6 +130,12 @@ void sw4o_freesurfcurvisg(int soa, int ib, int ie, int jb, int je, int kb, int k
                           double* u, const double* mu, const double* la, const double* met,
                           const double* sbop, const double* forcing, const double* strx,
                           const double* stry);
+/* Sixth-order curvilinear supergrid damping (EW::addsgd6cfort(_indrev),
+ * ew-cfromfort.C:1241, :1405). */
+void sw4o_addsgd6c(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
+                   const double* u, const double* um, const double* rho, const double* dcx,
+                   const double* dcy, const double* strx, const double* stry, const double* jac,
+                   const double* cox, const double* coy, double beta);
 /* Curvilinear supergrid damping (EW::addsgd4cfort_indrev, ew-cfromfort.C:1323). */
 void sw4o_addsgd4c(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
                    const double* u, const double* um, const double* rho, const double* dcx,

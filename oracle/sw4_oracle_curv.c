@@ -490,6 +490,56 @@ void sw4o_addsgd4c(int soa, int ib, int ie, int jb, int je, int kb, int ke, doub
 }
 
 /* ------------------------------------------------------------------------ */
+/* Sixth-order supergrid damping on a curvilinear grid (EW::addsgd6cfort and  */
+/* _indrev, ew-cfromfort.C:1241-1322, :1405): x and y only; along each axis    */
+/* the sum over the four half points of +-(1, 3) x (e_a + e_b) x the third     */
+/* difference of u - um across them, e = rho dc J; the whole times             */
+/* beta / (2 rho J), over the points 3 away from every array edge.             */
+/* ------------------------------------------------------------------------ */
+void sw4o_addsgd6c(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* up,
+                   const double* u, const double* um, const double* rho, const double* dcx,
+                   const double* dcy, const double* strx, const double* stry, const double* jac,
+                   const double* cox, const double* coy, double beta)
+{
+   if (beta == 0) return;
+   const cbox b = make_cbox(soa, ib, ie, jb, je, kb, ke);
+   /* half point m + 1/2 for m = -2..1: sign and weight, and the offsets of the third
+      difference (u(m+2) - 3u(m+1) + 3u(m) - u(m-1)) */
+   static const double wgt[4] = {-1, 3, -3, 1};
+#pragma omp parallel for collapse(2)
+   for (int k = kb + 3; k <= ke - 3; k++)
+      for (int j = jb + 3; j <= je - 3; j++)
+         for (int i = ib + 3; i <= ie - 3; i++) {
+            const long p = P(&b, i, j, k);
+            const double birhoj = 0.5 * beta / (rho[p] * jac[p]);
+            for (int c = 0; c < 3; c++) {
+               const long o = c * b.cs;
+               double acc = 0;
+               for (int ax = 0; ax < 2; ax++) {
+                  const long st = ax == 0 ? 1 : b.ni;
+                  const double* dc = ax == 0 ? dcx : dcy;
+                  const int q = ax == 0 ? i - ib : j - jb;
+                  const double w = ax == 0 ? strx[i - ib] * coy[j - jb] : stry[j - jb] * cox[i - ib];
+                  double s = 0;
+                  for (int m = -2; m <= 1; m++) {
+                     const long pa = p + m * st, pb = p + (m + 1) * st;
+                     const double e = rho[pb] * dc[q + m + 1] * jac[pb] + rho[pa] * dc[q + m] * jac[pa];
+                     double d3 = 0;
+                     for (int t = -1; t <= 2; t++) {
+                        static const double c3[4] = {-1, 3, -3, 1};
+                        const long pt = o + b.ps * (p + (m + t) * st);
+                        d3 += c3[t + 1] * (u[pt] - um[pt]);
+                     }
+                     s += wgt[m + 2] * e * d3;
+                  }
+                  acc += w * s;
+               }
+               up[o + b.ps * p] += birhoj * acc;
+            }
+         }
+}
+
+/* ------------------------------------------------------------------------ */
 /* Time step limit of a curvilinear grid (EW::computeDT, EW.C:5066-5125): the  */
 /* largest -lambda_min(A)/(4 rho) over the grid, A the symmetric 3x3 matrix    */
 /* built from the metric and material; dt = cfl / sqrt(max).  The reference     */
@@ -616,10 +666,17 @@ void sw4o_step_topo(const sw4o_problem* p, const sw4o_curv* cv, double t, double
    sw4o_corrfort(1, cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cup, clu, cf, cv->rho,
                  dt * dt * dt * dt);
    if (p->sg_beta != 0) {
-      sw4o_addsgd4(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, u, um, p->rho, p->dcx, p->dcy,
-                   p->dcz, p->strx, p->stry, p->strz, p->cox, p->coy, p->coz, p->sg_beta);
-      sw4o_addsgd4c(1, cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cup, cu, cum, cv->rho, cv->dcx,
-                    cv->dcy, cv->strx, cv->stry, cv->jac, cv->cox, cv->coy, p->sg_beta);
+      if (p->sg_order == 6) {
+         sw4o_addsgd6(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, u, um, p->rho, p->dcx, p->dcy,
+                      p->dcz, p->strx, p->stry, p->strz, p->cox, p->coy, p->coz, p->sg_beta);
+         sw4o_addsgd6c(1, cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cup, cu, cum, cv->rho,
+                       cv->dcx, cv->dcy, cv->strx, cv->stry, cv->jac, cv->cox, cv->coy, p->sg_beta);
+      } else {
+         sw4o_addsgd4(1, p->ib, p->ie, p->jb, p->je, p->kb, p->ke, up, u, um, p->rho, p->dcx, p->dcy,
+                      p->dcz, p->strx, p->stry, p->strz, p->cox, p->coy, p->coz, p->sg_beta);
+         sw4o_addsgd4c(1, cv->ib, cv->ie, cv->jb, cv->je, cv->kb, cv->ke, cup, cu, cum, cv->rho,
+                       cv->dcx, cv->dcy, cv->strx, cv->stry, cv->jac, cv->cox, cv->coy, p->sg_beta);
+      }
    }
    topo_bc(p, cv, sbop, up, cup);
 }

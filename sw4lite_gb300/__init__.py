@@ -167,6 +167,7 @@ _SIGS = {
                                 + [_VP, _VP], C.c_int),
     "sw4g_freesurfcurvisg": ([C.c_int] * 9 + [_VP] * 4 + [_D] + [_VP] * 3 + [_VP], C.c_int),
     "sw4g_addsgd4cfort": ([C.c_int] * 7 + [_VP] * 11 + [C.c_double, _VP], C.c_int),
+    "sw4g_addsgd6cfort": ([C.c_int] * 7 + [_VP] * 11 + [C.c_double, _VP], C.c_int),
     "sw4g_curvilinear_time_step": ([C.c_int] * 7 + [_VP] * 5 + [C.c_double, _D, _VP], C.c_int),
     "sw4g_nearest_grid_point": ([C.POINTER(GridDesc), C.c_double, C.c_double, C.c_double, _I],
                                 C.c_int),

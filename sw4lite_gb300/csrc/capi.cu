@@ -183,6 +183,19 @@ int sw4g_addsgd4cfort(int soa, int ifirst, int ilast, int jfirst, int jlast, int
                           dcy, strx, stry, jac, cox, coy, beta, as_stream(stream));
 }
 
+int sw4g_addsgd6cfort(int soa, int ifirst, int ilast, int jfirst, int jlast, int kfirst, int klast,
+                      double* up, const double* u, const double* um, const double* rho,
+                      const double* dcx, const double* dcy, const double* strx, const double* stry,
+                      const double* jac, const double* cox, const double* coy, double beta,
+                      void* stream)
+{
+   if (!up || !u || !um || !rho || !dcx || !dcy || !strx || !stry || !jac || !cox || !coy ||
+       !bounds_ok(ifirst, ilast, jfirst, jlast, kfirst, klast))
+      return SW4G_BAD_ARGUMENT;
+   return launch_addsgd6c(make_box(soa, ifirst, ilast, jfirst, jlast, kfirst, klast), up, u, um, rho,
+                          dcx, dcy, strx, stry, jac, cox, coy, beta, as_stream(stream));
+}
+
 int sw4g_curvilinear_time_step(int soa, int ib, int ie, int jb, int je, int kb, int ke,
                                const double* rho, const double* mu, const double* lambda,
                                const double* met, const double* jac, double cfl, double* dt,

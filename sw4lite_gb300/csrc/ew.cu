@@ -68,11 +68,9 @@ int EW::init()
       if (!(t == kStressFree || t == kDirichlet || t == kSuperGrid || t == kPeriodic)) return kBadArgument;
       if (t == kStressFree && s < 4) return kNotSupported;
    }
-   if (cv_ && g_.sg_order != 4) return kNotSupported;
    if (g_.sg_order != 4 && g_.sg_order != 6) return kBadArgument;
    if (g_.precision != 0 && g_.precision != 1) return kBadArgument;
    mixed_ = g_.precision == 1;
-   if (mixed_ && g_.sg_order != 4) return kNotSupported;
    if ((g_.bc[4] == kStressFree && g_.nz < 14) || (g_.bc[5] == kStressFree && g_.nz < 14))
       return kBadArgument;  // the one-sided rows need 8 interior planes on each such side
    b_ = grid_bounds(g_);
@@ -948,7 +946,7 @@ int EW::mixed_piece(int piece, int ip, int iq)
          ms.corrector = 1;
          ms.up = up;
          ms.out = out;
-         ms.beta = beta;
+         ms.beta = g_.sg_order == 4 ? beta : 0.0;  // 6th order: a separate pass in piece 4
       }
       return launch_mixed_stage(ms, stream_);
    }
@@ -976,6 +974,7 @@ int EW::mixed_piece(int piece, int ip, int iq)
                                 up, g_.h, g_.bc, sbop_, mu_, la_, dprof_[3], dprof_[4], stream_);
    }
    if (piece == 4) {
+      const double beta4 = g_.sg_order == 4 ? beta : 0.0;
       SW4G_TRY(launch_ghost_shell_df(b, 1, out, u, um, up, stream_));
       for (int side = 0; side < 2; side++) {
          if (!onesided_[4 + side]) continue;
@@ -983,12 +982,18 @@ int EW::mixed_piece(int piece, int ip, int iq)
          double* slab = slab_ + side * slab_len_;
          double* dslab = slab_ + (2 + side) * slab_len_;  // u - um for the damping
          SW4G_TRY(launch_uacc_slab_df(b, k0, k1, up, u, um, slab, stream_));
-         if (beta != 0) SW4G_TRY(launch_df_slab(b, k0, k1, u, um, dslab, stream_));
+         if (beta4 != 0) SW4G_TRY(launch_df_slab(b, k0, k1, u, um, dslab, stream_));
          Box sb = make_box(1, bd.ib, bd.ie, bd.jb, bd.je, k0, k1);
          SW4G_TRY(launch_stage_rows_df(1, side == 0, b, nz, slab, nullptr, sb, mu_, la_, g_.h, st[0],
-                                       st[1], st[2], u, um, up, out, rho_, irho_, dt2 / 12, beta,
-                                       dc, st, co, zc_[side], stream_, beta != 0 ? dslab : nullptr,
+                                       st[1], st[2], u, um, up, out, rho_, irho_, dt2 / 12, beta4,
+                                       dc, st, co, zc_[side], stream_, beta4 != 0 ? dslab : nullptr,
                                        rscr_));
+      }
+      if (beta != 0 && g_.sg_order == 6) {
+         const float* dc32[3] = {prof32_[0], prof32_[1], prof32_[2]};
+         const float* st32[3] = {prof32_[3], prof32_[4], prof32_[5]};
+         const float* co32[3] = {prof32_[6], prof32_[7], prof32_[8]};
+         SW4G_TRY(launch_addsgd6_df(3, b, out, u, um, rho32_, dc32, st32, co32, beta, stream_));
       }
       return kOk;
    }

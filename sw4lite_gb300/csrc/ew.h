@@ -48,6 +48,8 @@ struct CurvGrid {
    double* topscr = nullptr;  // work array of the SBP top rows, 36 doubles per column
    std::vector<double> hjac;  // host copy of the Jacobian (source discretisation)
    CurvCoefDF cd{};
+   float* rhoj32 = nullptr;  // rho J in FP32: the mixed form's 6th-order damping
+   bool rhoj32_ok = false;
    bool material = false;
    ~CurvGrid();
 };

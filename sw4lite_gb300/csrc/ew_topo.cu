@@ -29,6 +29,7 @@ CurvGrid::~CurvGrid()
    f(z);
    f(met);
    f(jac);
+   f(rhoj32);
    f(rho);
    f(mu);
    f(la);
@@ -186,6 +187,7 @@ int EW::set_material_grid(int grid, const double* rho, const double* mu, const d
    }
    SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
    cv_->material = true;
+   cv_->rhoj32_ok = false;  // rho J of the mixed form's 6th-order damping, on next use
    return kOk;
 }
 
@@ -329,10 +331,12 @@ int EW::curv_corr(int ip, int iq)
    CurvGrid& c = *cv_;
    const Bounds& b = c.b;
    const double dt = dt_;
+   const double beta = (prof_.used && g_.sg_damping != 0) ? g_.sg_damping : 0.0;
+   const double beta4 = g_.sg_order == 4 ? beta : 0.0;  // 6th order: a separate pass
+   const Box cbox = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke);
    if (mixed_) {
       if (ip == iq) return kNotSupported;
-      const double beta = (prof_.used && g_.sg_damping != 0) ? g_.sg_damping : 0.0;
-      CurvStageDF st = curv_stage_args_df(c, dprof_, prof32_, dt, beta);
+      CurvStageDF st = curv_stage_args_df(c, dprof_, prof32_, dt, beta4);
       st.corrector = 1;
       st.up = df(c.lev[ip]);
       st.u = df(c.lev[iu_]);
@@ -341,6 +345,21 @@ int EW::curv_corr(int ip, int iq)
       st.work1 = c.uacc;
       st.work2 = c.lu;
       SW4G_TRY(launch_curv_stage_df(st, stream_));
+      if (beta != 0 && g_.sg_order == 6) {
+         if (!c.rhoj32) {
+            SW4G_TRY(cuda_ok(cudaMalloc(&c.rhoj32, c.npts * sizeof(float))));
+            c.rhoj32_ok = false;
+         }
+         if (!c.rhoj32_ok) {
+            SW4G_TRY(launch_rho_jac_f32(c.npts, c.rho, c.jac, c.rhoj32, stream_));
+            c.rhoj32_ok = true;
+         }
+         const float* dc32[3] = {prof32_[0], prof32_[1], nullptr};
+         const float* st32[3] = {prof32_[3], prof32_[4], nullptr};
+         const float* co32[3] = {prof32_[6], prof32_[7], nullptr};
+         SW4G_TRY(launch_addsgd6_df(2, cbox, df(c.lev[iq]), df(c.lev[iu_]), df(c.lev[ium_]), c.rhoj32,
+                                    dc32, st32, co32, beta, stream_));
+      }
       return curv_force(c.lev[iq], 1, dt * dt * dt * dt / 12);
    }
    if (ip != iq) {
@@ -348,8 +367,7 @@ int EW::curv_corr(int ip, int iq)
       // up - 2u + um from a slab of planes kb..8
       const Box full = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke);
       SW4G_TRY(launch_uacc_slab(full, b.kb, 8, c.lev[ip], c.lev[iu_], c.lev[ium_], c.uacc, stream_));
-      const double beta = (prof_.used && g_.sg_damping != 0) ? g_.sg_damping : 0.0;
-      CurvStage st = curv_stage_args(c, dprof_, dt, beta);
+      CurvStage st = curv_stage_args(c, dprof_, dt, beta4);
       st.corrector = 1;
       st.up = c.lev[ip];
       st.u = c.lev[iu_];
@@ -358,6 +376,9 @@ int EW::curv_corr(int ip, int iq)
       st.f = c.uacc;
       st.fbox = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, 8);
       SW4G_TRY(launch_curv_stage(st, stream_));
+      if (beta != 0 && g_.sg_order == 6)
+         SW4G_TRY(launch_addsgd6c(cbox, c.lev[iq], c.lev[iu_], c.lev[ium_], c.rho, dprof_[0], dprof_[1],
+                                  dprof_[3], dprof_[4], c.jac, dprof_[6], dprof_[7], beta, stream_));
       return curv_force(c.lev[iq], 1, dt * dt * dt * dt / 12);
    }
    // phase order (in place): the reference's kernel sequence
@@ -369,7 +390,10 @@ int EW::curv_corr(int ip, int iq)
    SW4G_TRY(launch_corrfort(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, up, c.lu, c.fzero, c.rho,
                             dt * dt * dt * dt, stream_));
    SW4G_TRY(curv_force(up, 1, dt * dt * dt * dt / 12));
-   if (prof_.used && g_.sg_damping != 0)
+   if (beta != 0 && g_.sg_order == 6)
+      SW4G_TRY(launch_addsgd6c(cbox, up, u, um, c.rho, dprof_[0], dprof_[1], dprof_[3], dprof_[4],
+                               c.jac, dprof_[6], dprof_[7], beta, stream_));
+   else if (beta != 0)
       SW4G_TRY(launch_addsgd4c(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke, up, u, um, c.rho, dprof_[0],
                                dprof_[1], dprof_[3], dprof_[4], c.jac, dprof_[6], dprof_[7],
                                g_.sg_damping, stream_));

@@ -281,6 +281,18 @@ int launch_force_update_f32(int soa, int ib, int ie, int jb, int je, int kb, int
                             double coef, cudaStream_t s);
 
 int launch_mixed_stage(const MixedStage& st, cudaStream_t stream);
+// Sixth-order supergrid damping (damping6.cu): curvilinear FP64 (addsgd6cfort), and
+// on double-float levels in FP32 arithmetic for the mixed form, naxes 3 (Cartesian,
+// e = rho) or 2 (curvilinear, e = rho J); rho J as FP32 for the latter.
+int launch_addsgd6c(const Box& b, double* up, const double* u, const double* um, const double* rho,
+                    const double* dcx, const double* dcy, const double* strx, const double* stry,
+                    const double* jac, const double* cox, const double* coy, double beta,
+                    cudaStream_t s);
+int launch_addsgd6_df(int naxes, const Box& b, float* out, const float* u, const float* um,
+                      const float* e, const float* const dc[3], const float* const st[3],
+                      const float* const co[3], double beta, cudaStream_t s);
+int launch_rho_jac_f32(long long n, const double* rho, const double* jac, float* e, cudaStream_t s);
+
 // Halo planes of a decomposed grid (halo.cu): the first of the two planes a side
 // sends (pack: the interior planes next to it) or receives (the ghost planes), the
 // elements of one side's halo, and the pack / unpack of those planes of a field of

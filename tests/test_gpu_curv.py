@@ -109,7 +109,8 @@ def test_freesurfcurvisg_matches_oracle(soa):
 
 
 @pytest.mark.parametrize("soa", [1, 0])
-def test_addsgd4c_matches_oracle(soa):
+@pytest.mark.parametrize("order", [4, 6])
+def test_addsgd4c_matches_oracle(soa, order):
     nx, ny, nz = 17, 14, 11
     b, _, z, met, jac = _setup(nx, ny, nz)
     u, mu, la, rho, sx, sy = _fields(nx, ny, nz, seed=5)
@@ -118,12 +119,12 @@ def test_addsgd4c_matches_oracle(soa):
     dcx, dcy = rng.random(nx + 4) * 0.1, rng.random(ny + 4) * 0.1
     cox, coy = 0.5 + rng.random(nx + 4), 0.5 + rng.random(ny + 4)
     ref = up0.copy()
-    O.addsgd4c(1, b, ref, u, um, rho, dcx, dcy, sx, sy, jac, cox, coy, 0.02)
+    O.addsgd4c(1, b, ref, u, um, rho, dcx, dcy, sx, sy, jac, cox, coy, 0.02, order=order)
     cv = (lambda a: a) if soa else (lambda a: _to_aos(a, 3))
     upd = dev(cv(up0))
     keep = [dev(a) for a in (cv(u), cv(um), rho, dcx, dcy, sx, sy, jac, cox, coy)]
-    sg.check(sg.lib().sw4g_addsgd4cfort(soa, *b, upd.data_ptr(), *[k.data_ptr() for k in keep],
-                                        0.02, None), "addsgd4c")
+    fn = sg.lib().sw4g_addsgd6cfort if order == 6 else sg.lib().sw4g_addsgd4cfort
+    sg.check(fn(soa, *b, upd.data_ptr(), *[k.data_ptr() for k in keep], 0.02, None), "addsgd c")
     got = host(upd) if soa else _from_aos(host(upd), 3)
     assert _rel(got - up0, ref - up0) <= 1e-13
 

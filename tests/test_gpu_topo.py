@@ -26,17 +26,19 @@ def _lib():
     O.lib()
 
 
-def _case(bc_bottom=2):
+def _case(bc_bottom=2, sg_order=4):
     nx, ny, ncart, h = 30, 28, 22, 0.1
     src = [sg.source_desc(0.5 * nx * h, 0.45 * ny * h, 1.0 + 0.5 * ncart * h * 0.5,
                           force=(1.0, -0.5, 0.3), freq=8.0, t0=0.1, kind=sg.GAUSSIAN),
            sg.source_desc(0.4 * nx * h, 0.55 * ny * h, 1.0 + 0.3 * ncart * h,
                           moment=(1.0, 0.2, -0.3, 0.7, 0.1, -0.5), freq=6.0, kind=sg.C6SMOOTHBUMP)]
     return TopoCase(nx, ny, ncart, h, zmax_topo=1.0, amp=0.2, xc=1.4, yc=1.3, lx=0.6, ly=0.5,
-                    gp=5, sources=src, bc_bottom=bc_bottom)
+                    gp=5, sources=src, bc_bottom=bc_bottom, sg_order=sg_order)
 
 
-def _long_case():
+def _long_case(sg_order=4):
+    if sg_order == 6:
+        return _long_case6()
     # runs of more than a few steps need supergrid layers of at least ~15 points:
     # the damping coefficient PsiDamp/phi reaches 1/epsL = 1e4 at the boundary, and
     # thinner layers (5-10 points) grow without bound in the reference formulation
@@ -48,6 +50,19 @@ def _long_case():
                     gp=15, sources=src)
 
 
+def _long_case6():
+    # 6th-order damping with the reference's default coefficient for that order,
+    # 0.005 (src/EW.C:1307-1310), on 20-point layers: with 15-point layers and this
+    # topography the reference's own two-grid step (the oracle, pinned to the
+    # reference's kernels) grows without bound within 100 steps, and the GPU run
+    # reproduces that growth
+    nx, ny, ncart, h = 60, 56, 36, 0.1
+    src = [sg.source_desc(0.5 * nx * h, 0.45 * ny * h, 1.0 + 0.3 * ncart * h, force=(1.0, -0.5, 0.3),
+                          freq=8.0, t0=0.1, kind=sg.GAUSSIAN)]
+    return TopoCase(nx, ny, ncart, h, zmax_topo=1.0, amp=0.2, xc=3.0, yc=2.8, lx=0.6, ly=0.5,
+                    gp=20, sources=src, sg_order=6, damping=0.005)
+
+
 def _rel(a, b):
     return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
@@ -57,7 +72,8 @@ def _gpu(case, fields, dt, nsteps, mode, precision=sg.FP64):
     g = case.grid
     if precision != sg.FP64:
         g = sg.grid_desc(case.nx, case.ny, case.ncart, case.h, bc=case.bc, zmin=case.zmax_topo,
-                         sg_gp=g.sg_gp, sg_damping=g.sg_damping, precision=precision)
+                         sg_gp=g.sg_gp, sg_damping=g.sg_damping, sg_order=g.sg_order,
+                         precision=precision)
     ew = sg.EW(g, topo=t)
     assert ew.num_grids == 2
     nx, ny, nz, n = ew.grid_dims(1)
@@ -88,9 +104,9 @@ def test_grid_set_up_matches_oracle():
 
 
 @pytest.mark.parametrize("mode", [sg.MODE_FUSED, sg.MODE_PHASES])
-@pytest.mark.parametrize("bc_bottom", [2, 0])
-def test_topo_steps_match_oracle(mode, bc_bottom):
-    c = _case(bc_bottom)
+@pytest.mark.parametrize("bc_bottom,sg_order", [(2, 4), (0, 4), (2, 6)])
+def test_topo_steps_match_oracle(mode, bc_bottom, sg_order):
+    c = _case(bc_bottom, sg_order)
     dt = c.time_step(1.3)
     fields = smooth_topo_fields(c, seed=6)
     ref = c.oracle(dt).run(*fields, 0.0, 6)
@@ -131,9 +147,21 @@ def test_mixed_topo_level_round_trip():
         assert _rel(a, b) <= 1e-14
 
 
+@pytest.mark.parametrize("sg_order", [4, 6])
 @pytest.mark.parametrize("nsteps,tol", [(1, 1e-6), (120, 1e-5)])
-def test_mixed_topo_close_to_fp64(nsteps, tol):
-    c = _case() if nsteps == 1 else _long_case()
+def test_mixed_topo_close_to_fp64(nsteps, tol, sg_order):
+    # 6th order on thick layers: over thin (5-point) layers neighbouring stretching
+    # values differ by orders of magnitude and the damping terms, large there, carry
+    # the FP32 rounding of u - um above the form's 1e-6 per step
+    c = _case() if nsteps == 1 and sg_order == 4 else _long_case(sg_order)
+    if sg_order == 6 and nsteps > 40:
+        # With topography the reference's 6th-order damping has a slowly growing mode
+        # on the Cartesian grid: in the FP64 oracle (pinned to the reference's kernels)
+        # a 1e-8 perturbation of this case's initial levels grows to 5e-7 by step 60
+        # and 1.5e-2 by step 120, against 2e-9 with 4th-order damping.  FP32 rounding
+        # seeds that mode 1e8 times above FP64 rounding, so the comparison stops at
+        # 40 steps, before the mode dominates.
+        nsteps = 40
     dt = c.time_step(1.3)
     fields = smooth_topo_fields(c, seed=6)
     a, _ = _gpu(c, fields, dt, nsteps, sg.MODE_FUSED)

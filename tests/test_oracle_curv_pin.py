@@ -130,8 +130,9 @@ def test_freesurfcurvisg_matches_reference(soa):
     assert _rel(res[0], res[1]) <= 1e-13
 
 
+@pytest.mark.parametrize("order", [4, 6])
 @pytest.mark.parametrize("soa", [1, 0])
-def test_addsgd4c_matches_reference(soa):
+def test_addsgd4c_matches_reference(soa, order):
     nx, ny, nz = 13, 14, 11
     b, z = _hill(nx, ny, nz)
     n = z.size
@@ -147,11 +148,12 @@ def test_addsgd4c_matches_reference(soa):
     for which in ("oracle", "ref"):
         if soa:
             up = up0.copy()
-            O.addsgd4c(1, b, up, u, um, rho, dcx, dcy, sx, sy, jac, cox, coy, 0.02, which=which)
+            O.addsgd4c(1, b, up, u, um, rho, dcx, dcy, sx, sy, jac, cox, coy, 0.02, which=which,
+                       order=order)
         else:
             up = _to_aos(up0, 3)
             O.addsgd4c(0, b, up, _to_aos(u, 3), _to_aos(um, 3), rho, dcx, dcy, sx, sy, jac, cox,
-                       coy, 0.02, which=which)
+                       coy, 0.02, which=which, order=order)
             up = _from_aos(up, 3)
         res.append(up - up0)
     assert np.max(np.abs(res[1])) > 0

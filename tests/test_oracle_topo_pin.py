@@ -15,12 +15,12 @@ from tests.topo_util import TopoCase, smooth_topo_fields
 pytestmark = pytest.mark.skipif(not O.ref_available(), reason="reference kernels not built here")
 
 
-def _case():
+def _case(sg_order=4):
     nx, ny, ncart, h = 26, 24, 20, 0.1
     src = [sg.source_desc(0.5 * nx * h, 0.45 * ny * h, 1.0 + 0.6 * ncart * h * 0.5,
                           force=(1.0, -0.5, 0.3), freq=8.0, t0=0.1, kind=sg.GAUSSIAN)]
     return TopoCase(nx, ny, ncart, h, zmax_topo=1.0, amp=0.2, xc=1.3, yc=1.2, lx=0.6, ly=0.5,
-                    gp=5, sources=src)
+                    gp=5, sources=src, sg_order=sg_order)
 
 
 def _rel(a, b):
@@ -35,8 +35,9 @@ def test_topo_case_dimensions():
     assert np.allclose(z[2], c.zs)                  # top plane on the topography
 
 
-def test_topo_step_matches_reference_kernels():
-    c = _case()
+@pytest.mark.parametrize("sg_order", [4, 6])
+def test_topo_step_matches_reference_kernels(sg_order):
+    c = _case(sg_order)
     dt = c.time_step(1.3)
     assert 0 < dt < 0.1
     fields = smooth_topo_fields(c, seed=4)

@@ -19,7 +19,8 @@ INTERFACE = 4
 
 class TopoCase:
     def __init__(self, nx, ny, ncart, h, zmax_topo, amp, xc, yc, lx, ly, vs0=1.0, grad=0.5,
-                 rho=1.0, gp=6, damping=0.02, sources=(), bc_sides=(2, 2, 2, 2), bc_bottom=2):
+                 rho=1.0, gp=6, damping=0.02, sources=(), bc_sides=(2, 2, 2, 2), bc_bottom=2,
+                 sg_order=4, precision=0):
         self.nx, self.ny, self.ncart, self.h = nx, ny, ncart, h
         self.zmax_topo = zmax_topo
         self.hill = dict(amp=amp, xc=xc, yc=yc, lx=lx, ly=ly)
@@ -33,7 +34,7 @@ class TopoCase:
         bc = tuple(bc_sides) + (INTERFACE, bc_bottom)
         self.bc = bc
         self.grid = sg.grid_desc(nx, ny, ncart, h, bc=bc, zmin=zmax_topo, sg_gp=gp,
-                                 sg_damping=damping)
+                                 sg_damping=damping, sg_order=sg_order, precision=precision)
         self.cbounds = (-1, nx + 2, -1, ny + 2, -1, nc + 2)
         self.z = O.gaussian_hill_z(self.cbounds, nc, h, zmax_topo, amp, xc, yc, lx, ly)
         n = self.z.size
