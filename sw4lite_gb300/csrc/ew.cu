@@ -6,6 +6,7 @@
 #include <cstring>
 
 #include "sbp.h"
+#include "source_weights.h"
 
 namespace sw4g {
 
@@ -184,18 +185,26 @@ int EW::add_source(const SourceSpec& s)
 {
    if (!ready_) return kBadArgument;
    if (s.kind < 0 || s.kind > 3 || !(s.freq > 0)) return kBadArgument;
-   specs_.push_back(s);
    if (dev_src_) {  // discretised with the whole batch before the next step
+      if (cv_) {
+         // the same refusals as the host path: above the topography, or where the
+         // grid mapping cannot be inverted (the stencil needs no Jacobian)
+         const CurvSourceGrid cs = curv_source_grid(false);
+         TopoStencil st;
+         if (topo_stencil(g_, onesided_, cs, s, st) != 0) return kBadArgument;
+      }
+      specs_.push_back(s);
       src_dirty_ = true;
       return kOk;
    }
    if (cv_) {
       // two grids: the source may go to either, or straddle the interface
-      const CurvSourceGrid cs = curv_source_grid();
+      const CurvSourceGrid cs = curv_source_grid(false);
       if (discretize_source_topo(g_, onesided_, &cs, s, hsrc_, hsrc_curv_) != 0) return kBadArgument;
    } else {
       discretize_into(s, hsrc_);
    }
+   specs_.push_back(s);
    src_dirty_ = true;
    return kOk;
 }
@@ -265,12 +274,19 @@ int EW::clear_sources()
 int EW::set_source_discretization(bool on_device)
 {
    if (!ready_) return kBadArgument;
-   if (on_device && (cv_ || raw_src_ > 0 || sub_)) return kNotSupported;
+   if (on_device && (raw_src_ > 0 || sub_)) return kNotSupported;
    if (on_device == dev_src_) return kOk;
    dev_src_ = on_device;
-   if (!on_device) {  // the host list from the sources added meanwhile
+   if (!on_device) {  // the host lists from the sources added meanwhile
       hsrc_.clear();
-      for (const SourceSpec& s : specs_) discretize_into(s, hsrc_);
+      hsrc_curv_.clear();
+      const CurvSourceGrid cs = cv_ ? curv_source_grid(false) : CurvSourceGrid{};
+      for (const SourceSpec& s : specs_) {
+         if (cv_)
+            discretize_source_topo(g_, onesided_, &cs, s, hsrc_, hsrc_curv_);
+         else
+            discretize_into(s, hsrc_);
+      }
    }
    src_dirty_ = true;
    return kOk;
@@ -341,6 +357,10 @@ int EW::upload_sources()
    drop_graphs();  // the graphs hold the old source list
    if (dsrc_mem_ || dsrc_curv_mem_) SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
    src_dirty_ = false;
+   if (dev_src_ && cv_)
+      return launch_discretize_sources_topo(g_, onesided_, curv_source_grid(true), (int)specs_.size(),
+                                            specs_.data(), &dsrc_, &dsrc_mem_, &dsrc_curv_, &dsrc_curv_mem_,
+                                            stream_);
    if (dev_src_)
       return launch_discretize_sources(g_, onesided_, (int)specs_.size(), specs_.data(), &dsrc_, &dsrc_mem_,
                                        stream_);
@@ -359,17 +379,18 @@ int EW::grid_point_sources(int grid, std::vector<GridPointSource>* out) const
    // cache refresh: the object's observable state does not change)
    EW* self = const_cast<EW*>(this);
    SW4G_TRY(self->upload_sources());
-   const int ns = dsrc_.nsources;
+   const SourceSet& ds = grid == 0 ? dsrc_ : dsrc_curv_;
+   const int ns = ds.nsources;
    out->assign(ns, GridPointSource{});
    if (ns == 0) return kOk;
    std::vector<int> ijk(3 * (size_t)ns), kind(ns);
    std::vector<double> amp(3 * (size_t)ns), freq(ns), t0(ns);
    SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
-   SW4G_TRY(cuda_ok(cudaMemcpy(ijk.data(), dsrc_.ijk, ijk.size() * sizeof(int), cudaMemcpyDeviceToHost)));
-   SW4G_TRY(cuda_ok(cudaMemcpy(kind.data(), dsrc_.kind, kind.size() * sizeof(int), cudaMemcpyDeviceToHost)));
-   SW4G_TRY(cuda_ok(cudaMemcpy(amp.data(), dsrc_.amp, amp.size() * sizeof(double), cudaMemcpyDeviceToHost)));
-   SW4G_TRY(cuda_ok(cudaMemcpy(freq.data(), dsrc_.freq, freq.size() * sizeof(double), cudaMemcpyDeviceToHost)));
-   SW4G_TRY(cuda_ok(cudaMemcpy(t0.data(), dsrc_.t0, t0.size() * sizeof(double), cudaMemcpyDeviceToHost)));
+   SW4G_TRY(cuda_ok(cudaMemcpy(ijk.data(), ds.ijk, ijk.size() * sizeof(int), cudaMemcpyDeviceToHost)));
+   SW4G_TRY(cuda_ok(cudaMemcpy(kind.data(), ds.kind, kind.size() * sizeof(int), cudaMemcpyDeviceToHost)));
+   SW4G_TRY(cuda_ok(cudaMemcpy(amp.data(), ds.amp, amp.size() * sizeof(double), cudaMemcpyDeviceToHost)));
+   SW4G_TRY(cuda_ok(cudaMemcpy(freq.data(), ds.freq, freq.size() * sizeof(double), cudaMemcpyDeviceToHost)));
+   SW4G_TRY(cuda_ok(cudaMemcpy(t0.data(), ds.t0, t0.size() * sizeof(double), cudaMemcpyDeviceToHost)));
    for (int s = 0; s < ns; s++) {
       GridPointSource& p = (*out)[s];
       p.i = ijk[3 * s];

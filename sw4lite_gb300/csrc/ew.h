@@ -227,7 +227,7 @@ class EW {
    int curv_time_step(double cfl, double* dt);
    int curv_launches(int mode) const;
    int curv_force(double* lev, int tt, double coef);
-   CurvSourceGrid curv_source_grid() const;
+   CurvSourceGrid curv_source_grid(bool device) const;
    int ensure_phase_arrays();
    // graphs
    int sync_clock(double res_row = 0);

@@ -116,7 +116,8 @@ int EW::init_topo()
    return cuda_ok(cudaMemcpy(c.hjac.data(), c.jac, n * sizeof(double), cudaMemcpyDeviceToHost));
 }
 
-CurvSourceGrid EW::curv_source_grid() const
+// device: the Jacobian in device memory (the device discretisation), else its host copy
+CurvSourceGrid EW::curv_source_grid(bool device) const
 {
    const CurvGrid& c = *cv_;
    CurvSourceGrid cs;
@@ -129,7 +130,7 @@ CurvSourceGrid EW::curv_source_grid() const
    cs.ly = c.topo.ly;
    cs.zeta_break = c.topo.zeta_break;
    cs.order = c.topo.order;
-   cs.jac = c.hjac.data();
+   cs.jac = device ? c.jac : c.hjac.data();
    cs.ib = c.b.ib;
    cs.jb = c.b.jb;
    cs.kb = c.b.kb;

@@ -409,8 +409,13 @@ int launch_grad_df_step(const GradDF& g, cudaStream_t s);
 // the stream (the point count sizes the forcing launches).
 struct GridSpec;
 struct SourceSpec;
+struct CurvSourceGrid;
 int launch_discretize_sources(const GridSpec& g, const int onesided[6], int nsrc, const SourceSpec* host_specs,
                               SourceSet* out, void** mem, cudaStream_t s);
+// Two grids: the Cartesian and curvilinear grid-point sources (cv.jac in device memory).
+int launch_discretize_sources_topo(const GridSpec& g, const int onesided[6], const CurvSourceGrid& cv,
+                                   int nsrc, const SourceSpec* host_specs, SourceSet* cart, void** cart_mem,
+                                   SourceSet* curv, void** curv_mem, cudaStream_t s);
 int launch_grad_f1_step(const GradDF& g, cudaStream_t s);
 // gm += kmu 2^(sA+sF) am, gl likewise, gr += 2^(sA+sF) ar; the sums are zeroed
 int launch_grad_df_flush(const GradDF& g, double kmu, double* gm, double* gl, double* gr, cudaStream_t s);

@@ -7,6 +7,14 @@
 #include <cmath>
 #include <vector>
 
+#ifndef SW4G_HD
+#ifdef __CUDACC__
+#define SW4G_HD __host__ __device__
+#else
+#define SW4G_HD
+#endif
+#endif
+
 namespace sw4g {
 
 // Boundary condition kinds, numbered as the reference's boundaryConditionType
@@ -97,11 +105,16 @@ struct CurvSourceGrid {
    const double* jac = nullptr;
    int ib = 0, jb = 0, kb = 0;
    long long ni = 0, nij = 0;
-   double elevation(double x, double y) const
+   // jac: the Jacobian over the curvilinear array, in host memory for the host path and
+   // in device memory for the device path
+   SW4G_HD double elevation(double x, double y) const
    {
-      return amp * std::exp(-((x - xc) / lx) * ((x - xc) / lx) - ((y - yc) / ly) * ((y - yc) / ly));
+      return amp * ::exp(-((x - xc) / lx) * ((x - xc) / lx) - ((y - yc) / ly) * ((y - yc) / ly));
    }
-   double J(int i, int j, int k) const { return jac[(i - ib) + ni * (j - jb) + nij * (long long)(k - kb)]; }
+   SW4G_HD double J(int i, int j, int k) const
+   {
+      return jac[(i - ib) + ni * (j - jb) + nij * (long long)(k - kb)];
+   }
 };
 
 // Two-grid source discretisation (src/Source.C:1074-1990 with the curvilinear

@@ -149,9 +149,3 @@ def test_device_path_refusals():
     with pytest.raises(sg.Sw4gError):
         ew.add_grid_point_sources([3, 4, 5], [1.0, 0.0, 0.0], [5.0], [0.0], [sg.GAUSSIAN])
     ew.close()
-    from tests.test_gpu_topo import _long_case
-    c = _long_case()
-    ew = sg.EW(c.grid, topo=sg.topo_desc(**c.hill))
-    with pytest.raises(sg.Sw4gError):  # the curvilinear sources are discretised on the host
-        ew.set_source_discretization(True)
-    ew.close()
