@@ -306,6 +306,16 @@ def apply_lt(bounds, nz, y, mu, la, h, strx, stry, strz):
     return lt
 
 
+def apply_lt_fs(bounds, nxyz, onesided, y, mu, la, h, strx, stry, strz):
+    """L^T y = D L (D^-1 y) on the interior with free-surface z sides, D = H W (H the
+    SBP norm weights next to those sides)."""
+    lt = np.zeros_like(y)
+    os_arr, os_p = _ip(onesided)
+    lib().sw4o_apply_lt_fs(*[C.c_int(b) for b in bounds], *[C.c_int(n) for n in nxyz], os_p, _dp(y),
+                           _dp(mu), _dp(la), C.c_double(h), _dp(strx), _dp(stry), _dp(strz), _dp(lt))
+    return lt
+
+
 def sg_adjoint(bounds, y, rho, dc, st, co):
     """SG^T (y / rho) on the interior."""
     z = np.zeros_like(y)
@@ -318,6 +328,14 @@ def coef_gradient(bounds, v, w, h, st, gmu, gla):
     """gmu, gla += gradient of v . L(w) with respect to mu, lambda."""
     lib().sw4o_coef_gradient(*[C.c_int(b) for b in bounds], _dp(v), _dp(w), C.c_double(h),
                              *[_dp(a) for a in st], _dp(gmu), _dp(gla))
+
+
+def coef_gradient_fs(bounds, nz, onesided, v, w, h, st, gmu, gla):
+    """gmu, gla += gradient of v . L(w) with free-surface z sides (one-sided rows and
+    the ghost plane from the traction condition)."""
+    os_arr, os_p = _ip(onesided)
+    lib().sw4o_coef_gradient_fs(*[C.c_int(b) for b in bounds], C.c_int(nz), os_p, _dp(v), _dp(w),
+                                C.c_double(h), *[_dp(a) for a in st], _dp(gmu), _dp(gla))
 
 
 def sg_rho_gradient(bounds, a1, d, rho, dc, st, co, beta, grho):

@@ -188,6 +188,14 @@ void sw4o_sg_adjoint(int ib, int ie, int jb, int je, int kb, int ke, const doubl
 void sw4o_coef_gradient(int ib, int ie, int jb, int je, int kb, int ke, const double* v,
                         const double* w, double h, const double* strx, const double* stry,
                         const double* strz, double* gmu, double* gla);
+/* Free-surface z sides (onesided[4], onesided[5]): G(v, w) including the one-sided
+ * rows, and L^T y = D L D^-1 y with D = H W (H the SBP norm weights). */
+void sw4o_coef_gradient_fs(int ib, int ie, int jb, int je, int kb, int ke, int nz, const int onesided[6],
+                           const double* v, const double* w, double h, const double* strx,
+                           const double* stry, const double* strz, double* gmu, double* gla);
+void sw4o_apply_lt_fs(int ib, int ie, int jb, int je, int kb, int ke, int nx, int ny, int nz,
+                      const int onesided[6], const double* y, const double* mu, const double* la,
+                      double h, const double* strx, const double* stry, const double* strz, double* lt);
 void sw4o_sg_rho_gradient(int ib, int ie, int jb, int je, int kb, int ke, const double* a1,
                           const double* d, const double* rho, const double* dcx, const double* dcy,
                           const double* dcz, const double* strx, const double* stry,

@@ -5,7 +5,8 @@
  * gradients only, src/GridPointSource.C:659); these functions restate the exact
  * transpose of the oracle's own step (sw4o_step) for grids whose ghost points
  * are zero after every boundary pass (Dirichlet / supergrid sides with zero
- * boundary data, no free surface), so the state is the interior points I.
+ * boundary data) or, on the z sides, set by the free-surface condition from the
+ * interior (src/ew-cfromfort.C:415-476), so the state is the interior points I.
  *
  * Step (on I, R = diag(1/rho)):
  *   up = 2u - um + dt^2 R L(u) + dt^2 R F
@@ -22,6 +23,15 @@
  *   mu, lambda: G(R a1 dt^2/12, up - 2u + um) + G(R m dt^2, u), G(v, w) the
  *   coefficient gradient of v . L(w);
  *   rho: -(1/rho)[m.(up - 2u + um) + a1.(u+ - up)] - beta dSG/drho terms.
+ * Free surface on a z side: L is the operator with the one-sided SBP rows
+ * (src/rhs4sg_rev.C:349-856) applied after the ghost plane is solved from the
+ * traction condition.  D L is symmetric for D = H W, H the SBP norm weights
+ * (17/48, 59/48, 43/48, 49/48 on the four planes next to the side, 1 elsewhere),
+ * provided the z stretching is 1 on the rows next to the side (the reference does
+ * not apply it there; with no supergrid layer on a free-surface side it is 1), so
+ * L^T = D L D^-1.  L stays linear in (mu, lambda): the ghost plane enters the first
+ * row only through ghcof (2mu + lambda) w_ghost (mu u_ghost), and the traction
+ * condition makes that product linear in the material of the boundary point.
  */
 #ifndef _GNU_SOURCE
 #define _GNU_SOURCE
@@ -143,9 +153,11 @@ void sw4o_sg_adjoint(int ib, int ie, int jb, int je, int kb, int ke, const doubl
  * point, added into gmu, gla.  v zero outside I; w zero at ghost points. */
 static const double DW[5] = {1, -8, 0, 8, -1};
 
-void sw4o_coef_gradient(int ib, int ie, int jb, int je, int kb, int ke, const double* v,
-                        const double* w, double h, const double* strx, const double* stry,
-                        const double* strz, double* gmu, double* gla)
+/* The centred rows' part of G(v, w); the z-involving terms skip the rows k <= zlo
+ * and k >= zhi (the one-sided rows next to a free surface). */
+static void coef_gradient_central(int ib, int ie, int jb, int je, int kb, int ke, const double* v,
+                                  const double* w, double h, const double* strx, const double* stry,
+                                  const double* strz, int zlo, int zhi, double* gmu, double* gla)
 {
    const abox b = mk(ib, ie, jb, je, kb, ke);
    const double* sp[3] = {strx, stry, strz};
@@ -168,6 +180,7 @@ void sw4o_coef_gradient(int ib, int ie, int jb, int je, int kb, int ke, const do
                   int qc[3] = {i, j, k};
                   qc[ax] -= n;
                   if (!interior(&b, qc[0], qc[1], qc[2])) continue;
+                  if (ax == 2 && (qc[2] <= zlo || qc[2] >= zhi)) continue;
                   const long q = IX(&b, qc[0], qc[1], qc[2]);
                   const long st = ax == 0 ? 1 : ax == 1 ? b.ni : b.nij;
                   for (int c = 0; c < 3; c++) {
@@ -197,6 +210,7 @@ void sw4o_coef_gradient(int ib, int ie, int jb, int je, int kb, int ke, const do
             for (int t = 0; t < 12; t++) {
                const int c = mix[t][0], d = mix[t][1], ao = mix[t][2], ai = mix[t][3];
                if (pc[ai] < lo[ai] + 2 || pc[ai] > hi[ai] - 2) continue;
+               if (ai == 2 && (k <= zlo || k >= zhi)) continue; /* rows in this plane */
                double inner = 0, outer = 0;
                for (int m = -2; m <= 2; m++) {
                   if (m == 0) continue;
@@ -206,6 +220,7 @@ void sw4o_coef_gradient(int ib, int ie, int jb, int je, int kb, int ke, const do
                   int o[3] = {i, j, k};
                   o[ao] += m;
                   if (o[ao] < lo[ao] || o[ao] > hi[ao] || !interior(&b, o[0], o[1], o[2])) continue;
+                  if (ao == 2 && (o[2] <= zlo || o[2] >= zhi)) continue;
                   outer += DW[m + 2] * sp[ao][o[ao] - lo[ao]] * v[c * b.npts + IX(&b, o[0], o[1], o[2])];
                }
                const double g = -c144 * sp[ai][pc[ai] - lo[ai]] * inner * outer;
@@ -215,6 +230,175 @@ void sw4o_coef_gradient(int ib, int ie, int jb, int je, int kb, int ke, const do
             gmu[p] += gm;
             gla[p] += gl;
          }
+}
+
+void sw4o_coef_gradient(int ib, int ie, int jb, int je, int kb, int ke, const double* v,
+                        const double* w, double h, const double* strx, const double* stry,
+                        const double* strz, double* gmu, double* gla)
+{
+   coef_gradient_central(ib, ie, jb, je, kb, ke, v, w, h, strx, stry, strz, kb - 10, ke + 10, gmu, gla);
+}
+
+/* The z-involving terms of the six one-sided rows next to a free-surface z side
+ * (top: rows 1..6, bottom: nz-5..nz), differentiated term by term
+ * (src/rhs4sg_rev.C:349-600 top, :602-856 bottom; the ghost plane from the
+ * traction condition, src/ew-cfromfort.C:415-476):
+ *   zz   sum_q (sum_m acof(k,q,m) coef(m)) f(q) + ghcof coef(bnd) f(ghost);
+ *   dz_of_inner  s_a Dz(coef D_a f) / 12,  outer_of_dz  s_a D_a(coef Dz f) / 12,
+ * Dz the one-sided bope rows, D_a the centred DW stencil along x or y. */
+static void coef_gradient_rows(const abox* b, int nz, int top, const double* v, const double* w, double h,
+                               const double* strx, const double* stry, double* gmu, double* gla)
+{
+   double acof[384], ghcof[6], bope[48], sbop[5];
+   sw4o_stencil_coefficients(acof, ghcof, bope, sbop);
+   const double cof = 1.0 / (h * h), d4a = 2.0 / 3.0, d4b = -1.0 / 12.0;
+   const int kl = top ? 1 : -1, kbnd = top ? 1 : nz, kgh = top ? 0 : nz + 1;
+   const long n = b->npts;
+#define W_(c, i, j, k) w[(c) * n + IX(b, i, j, k)]
+   for (int kk = 1; kk <= 6; kk++) {
+      const int k = top ? kk : nz - kk + 1;
+      int kq[8];
+      double wz[8];
+      for (int q = 1; q <= 8; q++) {
+         kq[q - 1] = top ? q : nz - q + 1;
+         wz[q - 1] = top ? bope[(kk - 1) + 6 * (q - 1)] : -bope[(kk - 1) + 6 * (q - 1)];
+      }
+      for (int j = b->jb + 2; j <= b->je - 2; j++)
+         for (int i = b->ib + 2; i <= b->ie - 2; i++) {
+            const long r = IX(b, i, j, k);
+            const double V[3] = {v[r], v[n + r], v[2 * n + r]};
+            if (V[0] == 0 && V[1] == 0 && V[2] == 0) continue;
+            const double sx = strx[i - b->ib], sy = stry[j - b->jb];
+            /* zz rows: coefficient mu (components 0, 1) or 2mu + lambda (component 2) */
+            for (int m = 1; m <= 8; m++) {
+               double t[3] = {0, 0, 0};
+               for (int q = 1; q <= 8; q++) {
+                  const double a = acof[(kk - 1) + 6 * (q - 1) + 48 * (m - 1)];
+                  if (a == 0) continue;
+                  for (int c = 0; c < 3; c++) t[c] += a * W_(c, i, j, kq[q - 1]);
+               }
+               const long pm = IX(b, i, j, kq[m - 1]);
+               gmu[pm] += cof * (V[0] * t[0] + V[1] * t[1] + 2 * V[2] * t[2]);
+               gla[pm] += cof * V[2] * t[2];
+            }
+            if (ghcof[kk - 1] != 0) {
+               /* ghost plane: u, v ghosts do not depend on the material; (2mu + la) w_gh =
+                * -[(2mu + la) Sw + kl la (ux + vy)] / sbop0 */
+               const double gh = ghcof[kk - 1];
+               double S[3] = {0, 0, 0};
+               for (int q = 1; q <= 4; q++)
+                  for (int c = 0; c < 3; c++) S[c] += sbop[q] * W_(c, i, j, k + kl * (q - 1));
+               const double wx = sx * (d4a * (W_(2, i + 1, j, k) - W_(2, i - 1, j, k)) +
+                                       d4b * (W_(2, i + 2, j, k) - W_(2, i - 2, j, k)));
+               const double wy = sy * (d4a * (W_(2, i, j + 1, k) - W_(2, i, j - 1, k)) +
+                                       d4b * (W_(2, i, j + 2, k) - W_(2, i, j - 2, k)));
+               const double ux = sx * (d4a * (W_(0, i + 1, j, k) - W_(0, i - 1, j, k)) +
+                                       d4b * (W_(0, i + 2, j, k) - W_(0, i - 2, j, k)));
+               const double vy = sy * (d4a * (W_(1, i, j + 1, k) - W_(1, i, j - 1, k)) +
+                                       d4b * (W_(1, i, j + 2, k) - W_(1, i, j - 2, k)));
+               const double ugh = (-S[0] - kl * wx) / sbop[0], vgh = (-S[1] - kl * wy) / sbop[0];
+               const long pb = IX(b, i, j, kbnd);
+               (void)kgh;
+               gmu[pb] += cof * gh * (V[0] * ugh + V[1] * vgh - 2 * V[2] * S[2] / sbop[0]);
+               gla[pb] += cof * gh * V[2] * (-(S[2] + kl * (ux + vy)) / sbop[0]);
+            }
+            /* dz_of_inner: s_a Dz(coef D_a f) / 12 */
+            for (int q = 1; q <= 8; q++) {
+               if (wz[q - 1] == 0) continue;
+               const int kk2 = kq[q - 1];
+               double dx[3], dy[3];
+               for (int c = 0; c < 3; c++) {
+                  dx[c] = dy[c] = 0;
+                  for (int e = -2; e <= 2; e++) {
+                     dx[c] += DW[e + 2] * W_(c, i + e, j, kk2);
+                     dy[c] += DW[e + 2] * W_(c, i, j + e, kk2);
+                  }
+               }
+               const long pq = IX(b, i, j, kk2);
+               const double f = cof * wz[q - 1] / 12;
+               gmu[pq] += f * (V[0] * sx * dx[2] + V[1] * sy * dy[2]);
+               gla[pq] += f * V[2] * (sx * dx[0] + sy * dy[1]);
+            }
+            /* outer_of_dz: s_a D_a(coef Dz f) / 12 with the coefficient at the row's
+             * neighbours along a */
+            for (int e = -2; e <= 2; e++) {
+               if (e == 0) continue;
+               double zx[3] = {0, 0, 0}, zy[3] = {0, 0, 0};
+               for (int q = 1; q <= 8; q++)
+                  for (int c = 0; c < 3; c++) {
+                     zx[c] += wz[q - 1] * W_(c, i + e, j, kq[q - 1]);
+                     zy[c] += wz[q - 1] * W_(c, i, j + e, kq[q - 1]);
+                  }
+               const double f = cof * DW[e + 2] / 12;
+               const long px = IX(b, i + e, j, k), py = IX(b, i, j + e, k);
+               gla[px] += f * V[0] * sx * zx[2];
+               gla[py] += f * V[1] * sy * zy[2];
+               gmu[px] += f * V[2] * sx * zx[0];
+               gmu[py] += f * V[2] * sy * zy[1];
+            }
+         }
+   }
+#undef W_
+}
+
+/* G(v, w) with free-surface z sides (onesided[4], onesided[5]): the centred rows'
+ * terms (z-involving ones without the one-sided rows) plus the one-sided rows'. */
+void sw4o_coef_gradient_fs(int ib, int ie, int jb, int je, int kb, int ke, int nz, const int onesided[6],
+                           const double* v, const double* w, double h, const double* strx,
+                           const double* stry, const double* strz, double* gmu, double* gla)
+{
+   const abox b = mk(ib, ie, jb, je, kb, ke);
+   const int zlo = onesided[4] ? 6 : kb - 10, zhi = onesided[5] ? nz - 5 : ke + 10;
+   coef_gradient_central(ib, ie, jb, je, kb, ke, v, w, h, strx, stry, strz, zlo, zhi, gmu, gla);
+   if (onesided[4]) coef_gradient_rows(&b, nz, 1, v, w, h, strx, stry, gmu, gla);
+   if (onesided[5]) coef_gradient_rows(&b, nz, 0, v, w, h, strx, stry, gmu, gla);
+}
+
+/* The SBP norm weight of plane k next to free-surface z sides (1 elsewhere). */
+static double norm_h(int k, int nz, const int onesided[6])
+{
+   static const double om[4] = {17.0 / 48, 59.0 / 48, 43.0 / 48, 49.0 / 48};
+   if (onesided[4] && k >= 1 && k <= 4) return om[k - 1];
+   if (onesided[5] && k <= nz && k >= nz - 3) return om[nz - k];
+   return 1;
+}
+
+/* lt = L^T y = D L (D^-1 y) on I with free-surface z sides, D = H W: the ghost
+ * planes of D^-1 y from the traction condition (the lateral sides' ghosts zero). */
+void sw4o_apply_lt_fs(int ib, int ie, int jb, int je, int kb, int ke, int nx, int ny, int nz,
+                      const int onesided[6], const double* y, const double* mu, const double* la,
+                      double h, const double* strx, const double* stry, const double* strz, double* lt)
+{
+   double acof[384], ghcof[6], bope[48], sbop[5];
+   sw4o_stencil_coefficients(acof, ghcof, bope, sbop);
+   const abox b = mk(ib, ie, jb, je, kb, ke);
+   double* wy = (double*)calloc(3 * b.npts, sizeof(double));
+   for (int k = kb; k <= ke; k++)
+      for (int j = jb; j <= je; j++)
+         for (int i = ib; i <= ie; i++) {
+            if (!interior(&b, i, j, k)) continue;
+            const long p = IX(&b, i, j, k);
+            const double iw = strx[i - ib] * stry[j - jb] * strz[k - kb] / norm_h(k, nz, onesided);
+            for (int c = 0; c < 3; c++) wy[c * b.npts + p] = iw * y[c * b.npts + p];
+         }
+   const int bccnd[6] = {1, 1, 1, 1, onesided[4] ? 0 : 1, onesided[5] ? 0 : 1};
+   int wind[36], npts[6];
+   sw4o_boundary_windows(ib, ie, jb, je, kb, ke, nx, ny, nz, bccnd, wind, npts);
+   double* const bf[6] = {NULL, NULL, NULL, NULL, NULL, NULL};
+   sw4o_bcfortsg(1, ib, ie, jb, je, kb, ke, wind, nx, ny, nz, wy, h, bccnd, sbop, mu, la, bf, strx, stry);
+   memset(lt, 0, 3 * b.npts * sizeof(double));
+   sw4o_rhs4sg(1, ib, ie, jb, je, kb, ke, nz, onesided, acof, bope, ghcof, lt, wy, mu, la, h, strx, stry,
+               strz);
+   for (int k = kb; k <= ke; k++)
+      for (int j = jb; j <= je; j++)
+         for (int i = ib; i <= ie; i++) {
+            const long p = IX(&b, i, j, k);
+            const double w = interior(&b, i, j, k)
+                                 ? norm_h(k, nz, onesided) / (strx[i - ib] * stry[j - jb] * strz[k - kb])
+                                 : 0;
+            for (int c = 0; c < 3; c++) lt[c * b.npts + p] *= w;
+         }
+   free(wy);
 }
 
 /* rho gradient of the damping term: -beta * (R a1) . dSG(d)/drho at every point,

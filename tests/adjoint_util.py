@@ -1,6 +1,7 @@
-"""Test support for the discrete adjoint: a small all-supergrid problem with a
-smooth heterogeneous medium, receivers at grid points, the oracle's forward run
-(every level and predicted level kept) and the oracle's adjoint sweep.
+"""Test support for the discrete adjoint: a small supergrid problem (optionally with
+free-surface z sides) with a smooth heterogeneous medium, receivers at grid points,
+the oracle's forward run (every level and predicted level kept) and the oracle's
+adjoint sweep.
 
 Misfit J = 1/2 sum over steps n = 0..N and receivers r of |u^n(x_r) - d^n_r|^2
 (displacement at the receiver grid points).
@@ -25,7 +26,7 @@ def smooth_random(shape, seed, corr=4.0, amp=0.05):
 
 class AdjointCase:
     def __init__(self, shape=(20, 18, 22), h=0.1, gp=5, seed=3, nsteps=30, nrec=6,
-                 vp=1.8, vs=1.0, rho=1.5, bc=(2,) * 6):
+                 vp=1.8, vs=1.0, rho=1.5, bc=(2,) * 6, rec_k=None):
         self.nx, self.ny, self.nz = shape
         nx, ny, nz = shape
         self.h = h
@@ -44,6 +45,9 @@ class AdjointCase:
         rng = np.random.default_rng(seed + 10)
         self.rec = [(int(rng.integers(gp + 2, nx - gp)), int(rng.integers(gp + 2, ny - gp)),
                      int(rng.integers(gp + 2, nz - gp))) for _ in range(nrec)]
+        if rec_k is not None:  # receivers on a plane (e.g. the free surface, k = 1)
+            self.rec = [(i, j, rec_k) for i, j, _ in self.rec]
+        self.onesided = (0, 0, 0, 0, int(bc[4] == 0), int(bc[5] == 0))
         self.npts = (nx + 4) * (ny + 4) * (nz + 4)
 
     def rec_index(self):
@@ -106,14 +110,28 @@ def oracle_gradient(case: AdjointCase, obs):
     gr, gm, gl = np.zeros(n), np.zeros(n), np.zeros(n)
     a2 = np.zeros(n3)
     a1 = g_of(N)
+    fs = any(case.onesided)
+    dims = (case.nx, case.ny, case.nz)
+
+    def lt(y):
+        if fs:
+            return O.apply_lt_fs(bounds, dims, case.onesided, y, mu, la, case.h, *st)
+        return O.apply_lt(bounds, case.nz, y, mu, la, case.h, *st)
+
+    def cg(v, w):
+        if fs:
+            O.coef_gradient_fs(bounds, case.nz, case.onesided, v, w, case.h, st, gm, gl)
+        else:
+            O.coef_gradient(bounds, v, w, case.h, st, gm, gl)
+
     for step in range(N - 1, -1, -1):
         u, um, up, unew = levels[step + 1], levels[step], preds[step], levels[step + 2]
-        s = O.apply_lt(bounds, case.nz, a1 * R3, mu, la, case.h, *st)
+        s = lt(a1 * R3)
         m = a1 + dt * dt / 12 * s
-        t = O.apply_lt(bounds, case.nz, m * R3, mu, la, case.h, *st)
+        t = lt(m * R3)
         w1 = up - 2 * u + um
-        O.coef_gradient(bounds, a1 * R3 * (dt * dt / 12), w1, case.h, st, gm, gl)
-        O.coef_gradient(bounds, m * R3 * (dt * dt), u, case.h, st, gm, gl)
+        cg(a1 * R3 * (dt * dt / 12), w1)
+        cg(m * R3 * (dt * dt), u)
         gr -= ((m * w1 + a1 * (unew - up)).reshape(3, -1).sum(0)) / rho
         O.sg_rho_gradient(bounds, a1, u - um, rho, dc, st, co, beta, gr)
         an = g_of(step) + 2 * m + dt * dt * t - dt * dt / 6 * s - a2 - beta * O.sg_adjoint(

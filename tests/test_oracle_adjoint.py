@@ -10,6 +10,11 @@ only), so the adjoint is checked by its defining identities:
   * the whole gradient against central finite differences of the misfit along a
     smooth random direction in (rho, mu, lambda), to 1e-6 relative (the bar the
     adjoint is held to on the GPU).
+With free-surface z sides (one-sided SBP rows, ghost plane from the traction
+condition) the same identities: L^T = D L D^-1 (D = H W, H the SBP norm weights)
+by dot products to 1e-13, the coefficient gradient including the one-sided rows by
+Euler's identity and single-entry perturbations, and the gradient against finite
+differences with receivers on the free surface.
 """
 import numpy as np
 import pytest
@@ -122,6 +127,83 @@ def test_oracle_gradient_matches_finite_differences(which):
     dm = [dirs[q] * c.mat[q] if q in keep else np.zeros(c.npts) for q in range(3)]
     pred = float(gr @ dm[0] + gm @ dm[1] + gl @ dm[2])
     eps = 1e-5  # central difference: truncation ~eps^2, rounding ~1e-16/eps
+    Jp = misfit(c, oracle_forward(c, [c.mat[q] + eps * dm[q] for q in range(3)])[0], obs)
+    Jm = misfit(c, oracle_forward(c, [c.mat[q] - eps * dm[q] for q in range(3)])[0], obs)
+    fd = (Jp - Jm) / (2 * eps)
+    assert abs(pred) > 0
+    assert abs(fd - pred) <= 1e-6 * abs(pred), (fd, pred)
+
+
+# ---- free-surface z sides ----
+
+def _fs_case(bc, shape=(14, 13, 24)):
+    # the z stretching is 1 on the ten planes next to a free-surface side (no layer there)
+    return AdjointCase(shape=shape, bc=bc)
+
+
+def _lfs(c, x, mu, la, st):
+    """L x with the free-surface ghost planes solved from x (interior of x only)."""
+    bccnd = np.array([1, 1, 1, 1, 0 if c.onesided[4] else 1, 0 if c.onesided[5] else 1], dtype=np.int32)
+    wind, _ = O.boundary_windows(_bounds(c), (c.nx, c.ny, c.nz), bccnd)
+    _, _, _, sbop = O.stencil_coefficients()
+    u = np.where(_interior_mask(c), x, 0.0)
+    O.bcfortsg(1, _bounds(c), wind, (c.nx, c.ny, c.nz), u, c.h, bccnd, sbop, mu, la, [None] * 6, *st[:2])
+    out = np.zeros_like(u)
+    O.rhs4sg(1, _bounds(c), c.nz, c.onesided, out, u, mu, la, c.h, *st)
+    out[~_interior_mask(c)] = 0
+    return out, u
+
+
+@pytest.mark.parametrize("bc", [(2, 2, 2, 2, 0, 2), (2, 2, 2, 2, 2, 0), (2, 2, 2, 2, 0, 0)])
+def test_lt_fs_dot_product(bc):
+    c = _fs_case(bc)
+    _, st, _ = _profiles(c)
+    x, y = _rand_interior(c, 21), _rand_interior(c, 22)
+    lhs = float(_lfs(c, x, c.mat[1], c.mat[2], st)[0] @ y)
+    rhs = float(x @ O.apply_lt_fs(_bounds(c), (c.nx, c.ny, c.nz), c.onesided, y, c.mat[1], c.mat[2], c.h,
+                                  *st))
+    assert abs(lhs - rhs) <= 1e-13 * abs(lhs)
+
+
+@pytest.mark.parametrize("bc", [(2, 2, 2, 2, 0, 2), (2, 2, 2, 2, 2, 0)])
+def test_coef_gradient_fs_identities(bc):
+    c = _fs_case(bc)
+    _, st, _ = _profiles(c)
+    v, w = _rand_interior(c, 23), _rand_interior(c, 24)
+    mu, la = c.mat[1], c.mat[2]
+    n = c.npts
+    full, wg = _lfs(c, w, mu, la, st)
+    full = float(v @ full)
+    gm, gl = np.zeros(n), np.zeros(n)
+    O.coef_gradient_fs(_bounds(c), c.nz, c.onesided, v, wg, c.h, st, gm, gl)
+    # v . L(w) is linear in (mu, lambda), the ghost plane included
+    assert abs(float(mu @ gm + la @ gl) - full) <= 1e-12 * abs(full)
+    # single entries, by linearity, on the planes next to the free surface and elsewhere
+    nk, nj, ni = c.nz + 4, c.ny + 4, c.nx + 4
+    side_k = [1, 2, 3, 4, 5, 6, 7, 8] if c.onesided[4] else [c.nz - q for q in range(8)]
+    pts = [int(np.ravel_multi_index((k + 1, 6, 5), (nk, nj, ni))) for k in side_k]
+    pts += np.random.default_rng(25).integers(0, n, size=8).tolist()
+    for p in pts:
+        for which in (0, 1):
+            m2, l2 = mu.copy(), la.copy()
+            (m2 if which == 0 else l2)[p] += 1.0
+            d = float(v @ _lfs(c, w, m2, l2, st)[0]) - full
+            g = (gm if which == 0 else gl)[p]
+            assert abs(d - g) <= 1e-12 * abs(full), (p, which, d, g)
+
+
+@pytest.mark.parametrize("which", ["mu", "la", "all"])
+def test_oracle_gradient_fs_matches_finite_differences(which):
+    c = AdjointCase(shape=(16, 15, 24), bc=(2, 2, 2, 2, 0, 2), rec_k=1)
+    obs_case = AdjointCase(shape=(16, 15, 24), bc=(2, 2, 2, 2, 0, 2), rec_k=1, seed=11)
+    obs = obs_case.records(oracle_forward(obs_case)[0][1:])
+    J, gr, gm, gl = oracle_gradient(c, obs)
+    shape = (c.nz + 4, c.ny + 4, c.nx + 4)
+    dirs = [smooth_random(shape, 50 + q, corr=3.0, amp=0.3).reshape(-1) - 1.0 for q in range(3)]
+    keep = {"mu": (1,), "la": (2,), "all": (0, 1, 2)}[which]
+    dm = [dirs[q] * c.mat[q] if q in keep else np.zeros(c.npts) for q in range(3)]
+    pred = float(gr @ dm[0] + gm @ dm[1] + gl @ dm[2])
+    eps = 1e-5
     Jp = misfit(c, oracle_forward(c, [c.mat[q] + eps * dm[q] for q in range(3)])[0], obs)
     Jm = misfit(c, oracle_forward(c, [c.mat[q] - eps * dm[q] for q in range(3)])[0], obs)
     fd = (Jp - Jm) / (2 * eps)
