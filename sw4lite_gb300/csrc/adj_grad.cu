@@ -29,6 +29,16 @@
 // The cancellations that matter stay in FP64: w1 = (up - 2u) + um and un - up are
 // formed from the FP64 levels before the split.
 //
+// Free-surface z sides: the state vector's norm gains the SBP weights H (17/48,
+// 59/48, 43/48, 49/48 on the four planes next to the side), so the adjoint variable
+// is b = (H W)^-1 R a and every term above carries H at its row.  The terms along x
+// and y stay in their plane, so H joins the z profile factors (1/s_z, co_z/s_z).  The
+// z-involving terms of the six one-sided rows next to the side differ from the centred
+// form: the edge and combine kernels treat the adjoint values on those rows as zero for
+// them (planes k <= zlo, k >= zhi), and grad_rows_kernel adds those rows' terms,
+// differentiated term by term from the one-sided operator and the ghost plane's
+// traction condition (src/rhs4sg_rev.C:349-856, src/ew-cfromfort.C:415-476), in FP64.
+//
 // The FP32-mixed form runs the same edge and combine kernels with single FP32 values
 // (number type F1) on its double-float levels rounded to FP32 (w1 and un - up formed
 // exactly from the pairs first), and adds each point's sums to the FP64 gradients
@@ -36,6 +46,7 @@
 #include "common.cuh"
 #include "df.cuh"
 #include "kernels.h"
+#include "sbp.h"
 
 namespace sw4g {
 namespace {
@@ -186,7 +197,8 @@ __global__ void __launch_bounds__(256) exp_max_kernel(const double* __restrict__
 __global__ void inj_exp_kernel(Box b, const double* __restrict__ s0, const double* __restrict__ s1,
                                const double* __restrict__ s2, int nrec, const int* __restrict__ ijk,
                                const double* __restrict__ res, long long rows, int nval,
-                               const double* __restrict__ rho, int* __restrict__ out)
+                               const double* __restrict__ rho, const double* __restrict__ hz,
+                               int* __restrict__ out)
 {
    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
    int m = 0;
@@ -194,7 +206,7 @@ __global__ void inj_exp_kernel(Box b, const double* __restrict__ s0, const doubl
       const int r = (int)(t % nrec);
       const long long row = t / nrec;
       const int i = ijk[3 * r], j = ijk[3 * r + 1], k = ijk[3 * r + 2];
-      const double s = s0[i - b.ib] * s1[j - b.jb] * s2[k - b.kb] / rho[pidx(b, i, j, k)];
+      const double s = s0[i - b.ib] * s1[j - b.jb] * s2[k - b.kb] / (rho[pidx(b, i, j, k)] * (hz ? hz[k - b.kb] : 1.0));
       for (int c = 0; c < 3; c++)
          m = max(m, (__double2hiint(fabs(s * res[row * nval + 3 * r + c])) >> 20) & 0x7ff);
    }
@@ -203,19 +215,21 @@ __global__ void inj_exp_kernel(Box b, const double* __restrict__ s0, const doubl
 }
 
 // per axis: 24 st, 1/st, co/st, beta dc as pairs
+// (hz: the SBP norm weights of the z planes next to free-surface sides, for axis 2)
 __global__ void grad_profiles_kernel(int n, const double* __restrict__ st, const double* __restrict__ co,
                                      const double* __restrict__ dc, double beta, float2* __restrict__ st24,
                                      float2* __restrict__ ist, float2* __restrict__ cist,
-                                     float2* __restrict__ bdc)
+                                     float2* __restrict__ bdc, const double* __restrict__ hz)
 {
    const int x = blockIdx.x * blockDim.x + threadIdx.x;
    if (x >= n) return;
+   const double hw = hz ? hz[x] : 1.0;
    float h, l;
    df_split(24 * st[x], h, l);
    st24[x] = make_float2(h, l);
-   df_split(1 / st[x], h, l);
+   df_split(hw / st[x], h, l);
    ist[x] = make_float2(h, l);
-   df_split(co[x] / st[x], h, l);
+   df_split(hw * co[x] / st[x], h, l);
    cist[x] = make_float2(h, l);
    df_split(beta * dc[x], h, l);
    bdc[x] = make_float2(h, l);
@@ -248,7 +262,11 @@ __global__ void __launch_bounds__(kGradThreads) grad_prep_kernel(GradDF g)
       const long long q = c * n + p;
       const double uq = __ldg(g.u + q), umq = __ldg(g.um + q), upq = __ldg(g.up + q);
       const double w1 = (upq - 2 * uq) + umq;
-      const float2 vb = to_df(__ldg(g.b1 + q), ka), vm = to_df(__ldg(g.mt + q), ka), fw = to_df(w1, kf);
+      // the adjoint is a vector on the interior: zero on the ghost points (a free
+      // surface's ghost plane of b1 and mt holds the traction condition's values)
+      const float2 vb = in ? to_df(__ldg(g.b1 + q), ka) : make_float2(0.f, 0.f);
+      const float2 vm = in ? to_df(__ldg(g.mt + q), ka) : make_float2(0.f, 0.f);
+      const float2 fw = to_df(w1, kf);
       static_cast<float2*>(g.db1)[q] = vb;
       static_cast<float2*>(g.dmt)[q] = vm;
       static_cast<float2*>(g.dw1)[q] = fw;
@@ -294,7 +312,7 @@ __global__ void __launch_bounds__(kGradThreads) grad_prep_f1_kernel(GradDF g)
       two_sum(s1, __ldg(g.lum + q), s2, e2);
       const float w1 = s2 + ((e1 + e2) + ((__ldg(g.lup + q + lo) - 2.f * __ldg(g.lu + q + lo)) +
                                          __ldg(g.lum + q + lo)));
-      const float vb = df_round(g.lb1, q, lo), vm = df_round(g.lmt, q, lo);
+      const float vb = in ? df_round(g.lb1, q, lo) : 0.f, vm = in ? df_round(g.lmt, q, lo) : 0.f;
       static_cast<float*>(g.db1)[q] = vb;
       static_cast<float*>(g.dmt)[q] = vm;
       static_cast<float*>(g.dw1)[q] = w1;
@@ -322,7 +340,7 @@ __global__ void __launch_bounds__(kGradThreads) grad_prep_f1_kernel(GradDF g)
 // count as zero; q may lie below the array).
 template <class V, bool CHECK>
 __device__ __forceinline__ void edges_body(const GradDF& g, long long n, int pq, bool ok0, bool ok1, bool ok2,
-                                           int sd, int a, V E[4])
+                                           bool ma0, bool ma1, bool ma2, int sd, int a, V E[4])
 {
    using N = Num<V>;
    E[0] = E[1] = E[2] = E[3] = N::zero();
@@ -335,11 +353,11 @@ __device__ __forceinline__ void edges_body(const GradDF& g, long long n, int pq,
          const typename N::S* __restrict__ F = arr<V>(t == 0 ? g.du : g.dw1) + c * n;
          V x0, x1, x2, y0, y1, y2;
          if (CHECK) {
-            x0 = ok0 ? N::of(__ldg(A + pq)) : N::zero();
+            x0 = ok0 && ma0 ? N::of(__ldg(A + pq)) : N::zero();
             y0 = ok0 ? N::of(__ldg(F + pq)) : N::zero();
-            x1 = ok1 ? N::of(__ldg(A + pq + sd)) : N::zero();
+            x1 = ok1 && ma1 ? N::of(__ldg(A + pq + sd)) : N::zero();
             y1 = ok1 ? N::of(__ldg(F + pq + sd)) : N::zero();
-            x2 = ok2 ? N::of(__ldg(A + pq + 2 * sd)) : N::zero();
+            x2 = ok2 && ma2 ? N::of(__ldg(A + pq + 2 * sd)) : N::zero();
             y2 = ok2 ? N::of(__ldg(F + pq + 2 * sd)) : N::zero();
          } else {
             x0 = N::of(__ldg(A + pq));
@@ -366,15 +384,19 @@ __device__ __forceinline__ void edges_body(const GradDF& g, long long n, int pq,
    }
 }
 
+// the adjoint value of plane k enters the z-involving terms (not a one-sided row)
+__device__ __forceinline__ bool zrow(const GradDF& g, int k) { return k > g.zlo && k < g.zhi; }
+
 template <class V>
 __device__ __forceinline__ void edges_at(const GradDF& g, long long n, int pq, int xq, int xl, int xh, int sd,
                                          int a, V E[4])
 {
-   if (xq >= xl && xq + 2 <= xh)
-      edges_body<V, false>(g, n, pq, true, true, true, sd, a, E);
+   const bool m0 = a != 2 || zrow(g, xq), m1 = a != 2 || zrow(g, xq + 1), m2 = a != 2 || zrow(g, xq + 2);
+   if (xq >= xl && xq + 2 <= xh && m0 && m1 && m2)
+      edges_body<V, false>(g, n, pq, true, true, true, true, true, true, sd, a, E);
    else
-      edges_body<V, true>(g, n, pq, xq >= xl, xq + 1 >= xl && xq + 1 <= xh, xq + 2 >= xl && xq + 2 <= xh, sd,
-                          a, E);
+      edges_body<V, true>(g, n, pq, xq >= xl, xq + 1 >= xl && xq + 1 <= xh, xq + 2 >= xl && xq + 2 <= xh, m0,
+                          m1, m2, sd, a, E);
 }
 
 // the edge sums of every array point: ed[(a*4 + r) * npts + p]
@@ -508,6 +530,11 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
                   y[m] = ok ? N::of(__ldg(F + p + (m - 2) * sd)) : N::zero();
                }
             }
+            if (a == 2 && (x0 - 2 <= g.zlo || x0 + 2 >= g.zhi)) {
+#pragma unroll
+               for (int m = 0; m < 5; m++)
+                  if (m != 2 && !zrow(g, x0 + m - 2)) x[m] = N::zero();
+            }
             V fa, fw;
             first_diffs<V>(x, y, inner, fa, fw);
             fd[c * 3 + a][tid] = N::st(fa);
@@ -534,7 +561,10 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
 #pragma unroll 1
       for (int t3 = 0; t3 < 3; t3++) {
          const int a1 = t3 == 2 ? 0 : t3 + 1, a2 = t3 == 0 ? 2 : t3 - 1;
-         auto A_ = [&](int c, int a) { return N::of(fd[c * 3 + a][tid]); };
+         // the terms with a z derivative skip the one-sided rows' adjoint values: the
+         // in-plane first differences of a one-sided row's plane drop out of them
+         const bool zoff = t3 != 2 && !zrow(g, pc[2]);
+         auto A_ = [&](int c, int a) { return zoff && a != 2 ? N::zero() : N::of(fd[c * 3 + a][tid]); };
          auto W_ = [&](int c, int a) { return N::of(fd[9 + c * 3 + a][tid]); };
          const V ml = df_addf(df_mul(W_(a2, a2), A_(a1, a1)), df_mul(W_(a1, a1), A_(a2, a2)));
          const V mm = df_addf(df_mul(W_(a2, a1), A_(a1, a2)), df_mul(W_(a1, a2), A_(a2, a1)));
@@ -553,6 +583,195 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
       g.gl64[p] += g.kmu * (double)Num<V>::st(gl);
       g.gr64[p] += (double)Num<V>::st(gr);
    }
+}
+
+// ---- the one-sided rows next to a free-surface z side ----
+__constant__ double kr_acof[384];  // acof[(k-1) + 6 (q-1) + 48 (m-1)]
+__constant__ double kr_bope[48];   // bope[(k-1) + 6 (q-1)]
+__constant__ double kr_sbop[5];
+__constant__ double kr_gh;         // ghcof of row 1 (the other rows' are zero)
+
+constexpr int kRowThreads = 64;
+
+template <bool DF>
+__device__ __forceinline__ double rlvl(const GradRows& g, const double* d, const float* f, long long q)
+{
+   if (DF) return (double)__ldg(f + q) + (double)__ldg(f + q + g.lo);
+   return __ldg(d + q);
+}
+
+// One thread per interior column (i, j).  Rows kk = 1..6 from the side (plane kq(kk)),
+// the material planes kq(1..8); term by term (the FP64 checker restates the same):
+//   zz   sum_q (sum_m acof(kk,q,m) coef(m)) w(q) + ghcof coef(bnd) w(ghost), coef mu
+//        (components 0, 1) or 2mu + lambda (component 2); the ghost plane through the
+//        traction condition: u, v ghosts free of the material, (2mu + la) w_ghost =
+//        -[(2mu + la) Sw + kl la (ux + vy)] / sbop0;
+//   dz_of_inner  s_a Dz(coef D_a w) / 12 (coef on the column, planes kq(q));
+//   outer_of_dz  s_a D_a(coef Dz w) / 12 (coef at the rows' neighbours along a, gathered
+//        here from the rows that reach this column).
+template <bool DF>
+__global__ void __launch_bounds__(kRowThreads) grad_rows_kernel(GradRows g)
+{
+   const Box& b = g.b;
+   const int nic = b.ie - b.ib - 3, njc = b.je - b.jb - 3;
+   const int t = blockIdx.x * kRowThreads + threadIdx.x;
+   if (t >= nic * njc) return;
+   const int i = b.ib + 2 + t % nic, j = b.jb + 2 + t / nic;
+   const bool top = g.top != 0;
+   const int kl = top ? 1 : -1;
+   const long long n = b.npts;
+   const double cof = 1 / (g.h * g.h), DW[5] = {1, -8, 0, 8, -1};
+   const double d4a = 2.0 / 3.0, d4b = -1.0 / 12.0;
+   auto kq = [&](int q) { return top ? q : g.nz - q + 1; };  // q = 1..8
+   auto wz = [&](int kk, int q) {
+      const double v = kr_bope[(kk - 1) + 6 * (q - 1)];
+      return top ? v : -v;
+   };
+   auto Wf = [&](int P, int c, int ii, int jj, int kk) -> double {
+      const long long q = c * n + pidx(b, ii, jj, kk);
+      if (P == 1) return rlvl<DF>(g, g.u, g.lu, q);
+      return (rlvl<DF>(g, g.up, g.lup, q) - 2 * rlvl<DF>(g, g.u, g.lu, q)) + rlvl<DF>(g, g.um, g.lum, q);
+   };
+   auto Va = [&](int P, int c, int ii, int jj, int kk) -> double {
+      if (ii < b.ib + 2 || ii > b.ie - 2 || jj < b.jb + 2 || jj > b.je - 2) return 0.0;
+      const long long q = c * n + pidx(b, ii, jj, kk);
+      const double x = P == 0 ? rlvl<DF>(g, g.b1, g.lb1, q) : rlvl<DF>(g, g.mt, g.lmt, q);
+      const double s = __ldg(g.sx + ii - b.ib) * __ldg(g.sy + jj - b.jb) * __ldg(g.sz + kk - b.kb);
+      return (P == 0 ? g.c1 : g.c2) * __ldg(g.hz + kk - b.kb) * x / s;
+   };
+   const double sxi = __ldg(g.sx + i - b.ib), syj = __ldg(g.sy + j - b.jb);
+   double gmc[8], glc[8];
+#pragma unroll
+   for (int m = 0; m < 8; m++) gmc[m] = glc[m] = 0;
+#pragma unroll 1
+   for (int P = 0; P < 2; P++) {
+      // zz rows, one component at a time
+#pragma unroll 1
+      for (int c = 0; c < 3; c++) {
+         double Vk[6], wq[8];
+#pragma unroll
+         for (int kk = 0; kk < 6; kk++) Vk[kk] = Va(P, c, i, j, kq(kk + 1));
+#pragma unroll
+         for (int q = 0; q < 8; q++) wq[q] = Wf(P, c, i, j, kq(q + 1));
+#pragma unroll
+         for (int m = 0; m < 8; m++) {
+            double tm = 0;
+#pragma unroll
+            for (int kk = 0; kk < 6; kk++) {
+               double y = 0;
+#pragma unroll
+               for (int q = 0; q < 8; q++) y = fma(kr_acof[kk + 6 * q + 48 * m], wq[q], y);
+               tm = fma(Vk[kk], y, tm);
+            }
+            gmc[m] += cof * (c == 2 ? 2 * tm : tm);
+            if (c == 2) glc[m] += cof * tm;
+         }
+      }
+      // the ghost plane (row 1)
+      {
+         const int k = kq(1);
+         double S[3] = {0, 0, 0};
+#pragma unroll
+         for (int q = 1; q <= 4; q++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) S[c] += kr_sbop[q] * Wf(P, c, i, j, k + kl * (q - 1));
+         auto dxy = [&](int c, int ax) {
+            const int di = ax == 0, dj = ax == 1;
+            return (ax == 0 ? sxi : syj) *
+                   (d4a * (Wf(P, c, i + di, j + dj, k) - Wf(P, c, i - di, j - dj, k)) +
+                    d4b * (Wf(P, c, i + 2 * di, j + 2 * dj, k) - Wf(P, c, i - 2 * di, j - 2 * dj, k)));
+         };
+         const double wx = dxy(2, 0), wy = dxy(2, 1), ux = dxy(0, 0), vy = dxy(1, 1);
+         const double s0 = kr_sbop[0];
+         const double ugh = (-S[0] - kl * wx) / s0, vgh = (-S[1] - kl * wy) / s0;
+         const double V0 = Va(P, 0, i, j, k), V1 = Va(P, 1, i, j, k), V2 = Va(P, 2, i, j, k);
+         gmc[0] += cof * kr_gh * (V0 * ugh + V1 * vgh - 2 * V2 * S[2] / s0);
+         glc[0] += cof * kr_gh * V2 * (-(S[2] + kl * (ux + vy)) / s0);
+      }
+      // dz_of_inner: this column's rows, the coefficient on planes kq(q)
+      {
+         double Bv[3][8];
+#pragma unroll
+         for (int c = 0; c < 3; c++)
+#pragma unroll
+            for (int q = 0; q < 8; q++) Bv[c][q] = 0;
+#pragma unroll 1
+         for (int kk = 1; kk <= 6; kk++) {
+            const int k = kq(kk);
+            const double V0 = Va(P, 0, i, j, k), V1 = Va(P, 1, i, j, k), V2 = Va(P, 2, i, j, k);
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+               const double w = wz(kk, q + 1);
+               Bv[0][q] = fma(w, V0, Bv[0][q]);
+               Bv[1][q] = fma(w, V1, Bv[1][q]);
+               Bv[2][q] = fma(w, V2, Bv[2][q]);
+            }
+         }
+#pragma unroll 1
+         for (int q = 0; q < 8; q++) {
+            const int k = kq(q + 1);
+            double dx0 = 0, dx2 = 0, dy1 = 0, dy2 = 0;
+#pragma unroll
+            for (int e = -2; e <= 2; e++) {
+               if (e == 0) continue;
+               dx0 += DW[e + 2] * Wf(P, 0, i + e, j, k);
+               dx2 += DW[e + 2] * Wf(P, 2, i + e, j, k);
+               dy1 += DW[e + 2] * Wf(P, 1, i, j + e, k);
+               dy2 += DW[e + 2] * Wf(P, 2, i, j + e, k);
+            }
+            gmc[q] += cof / 12 * (Bv[0][q] * sxi * dx2 + Bv[1][q] * syj * dy2);
+            glc[q] += cof / 12 * Bv[2][q] * (sxi * dx0 + syj * dy1);
+         }
+      }
+      // outer_of_dz: the rows along x and y whose outer difference reaches this column
+#pragma unroll 1
+      for (int kk = 1; kk <= 6; kk++) {
+         const int k = kq(kk);
+         double dz[3] = {0, 0, 0};
+#pragma unroll
+         for (int q = 1; q <= 8; q++) {
+            const double w = wz(kk, q);
+#pragma unroll
+            for (int c = 0; c < 3; c++) dz[c] = fma(w, Wf(P, c, i, j, kq(q)), dz[c]);
+         }
+         double tx0 = 0, ty1 = 0, tx2 = 0, ty2 = 0;
+#pragma unroll
+         for (int e = -2; e <= 2; e++) {
+            if (e == 0) continue;
+            const double sxe = __ldg(g.sx + i - e - b.ib), sye = __ldg(g.sy + j - e - b.jb);
+            tx0 += DW[e + 2] * sxe * Va(P, 0, i - e, j, k);
+            tx2 += DW[e + 2] * sxe * Va(P, 2, i - e, j, k);
+            ty1 += DW[e + 2] * sye * Va(P, 1, i, j - e, k);
+            ty2 += DW[e + 2] * sye * Va(P, 2, i, j - e, k);
+         }
+         glc[kk - 1] += cof / 12 * dz[2] * (tx0 + ty1);
+         gmc[kk - 1] += cof / 12 * (dz[0] * tx2 + dz[1] * ty2);
+      }
+   }
+#pragma unroll
+   for (int m = 0; m < 8; m++) {
+      const long long p = pidx(b, i, j, kq(m + 1));
+      g.gm[p] += gmc[m];
+      g.gl[p] += glc[m];
+   }
+}
+
+bool g_row_tables[64] = {false};
+
+int upload_row_tables()
+{
+   int dev = 0;
+   if (cudaGetDevice(&dev) != cudaSuccess) return kCudaError;
+   if (dev < 0 || dev >= 64) return kBadArgument;
+   if (g_row_tables[dev]) return kOk;
+   double acof[384], ghcof[6], bope[48], sbop[5];
+   sbp_coefficients(acof, ghcof, bope, sbop);
+   if (cudaMemcpyToSymbol(kr_acof, acof, sizeof(acof)) != cudaSuccess) return kCudaError;
+   if (cudaMemcpyToSymbol(kr_bope, bope, sizeof(bope)) != cudaSuccess) return kCudaError;
+   if (cudaMemcpyToSymbol(kr_sbop, sbop, sizeof(sbop)) != cudaSuccess) return kCudaError;
+   if (cudaMemcpyToSymbol(kr_gh, &ghcof[0], sizeof(double)) != cudaSuccess) return kCudaError;
+   g_row_tables[dev] = true;
+   return kOk;
 }
 
 // g += scale * acc (FP64), acc = 0
@@ -587,7 +806,8 @@ int launch_grad_df_profiles(const GradDFProfiles& p, cudaStream_t s)
 {
    for (int a = 0; a < 3; a++) {
       grad_profiles_kernel<<<blocks_for(p.n[a], 128), 128, 0, s>>>(p.n[a], p.st[a], p.co[a], p.dc[a], p.beta,
-                                                                   p.st24[a], p.ist[a], p.cist[a], p.bdc[a]);
+                                                                   p.st24[a], p.ist[a], p.cist[a], p.bdc[a],
+                                                                   a == 2 ? p.hz : nullptr);
       SW4G_TRY(launch_status());
    }
    return kOk;
@@ -600,11 +820,11 @@ int launch_exp_max(const double* x, long long n, int* out, cudaStream_t s)
 }
 
 int launch_inj_exp(const Box& b, const double* const st[3], int nrec, const int* ijk, const double* res,
-                   long long rows, int nval, const double* rho, int* out, cudaStream_t s)
+                   long long rows, int nval, const double* rho, const double* hz, int* out, cudaStream_t s)
 {
    if (nrec <= 0 || rows <= 0) return kOk;
    inj_exp_kernel<<<blocks_for(rows * nrec, 128), 128, 0, s>>>(b, st[0], st[1], st[2], nrec, ijk, res, rows,
-                                                               nval, rho, out);
+                                                               nval, rho, hz, out);
    return launch_status();
 }
 
@@ -629,6 +849,20 @@ int launch_grad_f1_step(const GradDF& g, cudaStream_t s)
    grad_edge_kernel<F1><<<grid, kGradThreads, 0, s>>>(g);
    SW4G_TRY(launch_status());
    grad_df_kernel<F1><<<grid, kGradThreads, 0, s>>>(g);
+   return launch_status();
+}
+
+int launch_grad_rows(const GradRows& g, cudaStream_t s)
+{
+   SW4G_TRY(upload_row_tables());
+   const Box& b = g.b;
+   const long long cols = (long long)(b.ie - b.ib - 3) * (b.je - b.jb - 3);
+   if (cols <= 0) return kOk;
+   const int nb = (int)((cols + kRowThreads - 1) / kRowThreads);
+   if (g.lb1)
+      grad_rows_kernel<true><<<nb, kRowThreads, 0, s>>>(g);
+   else
+      grad_rows_kernel<false><<<nb, kRowThreads, 0, s>>>(g);
    return launch_status();
 }
 

@@ -35,9 +35,18 @@
 //                rho dc factors).
 // These sums run in adj_grad.cu: double-float arithmetic on the FP32 pipe for the
 // FP64 form, FP32 for the mixed form.
+// Free-surface z sides (the ghost plane solved from the interior by the traction
+// condition, one-sided SBP rows): D L is symmetric for D = H W, H the SBP norm weights
+// (17/48, 59/48, 43/48, 49/48 on the four planes next to the side), so the scaled
+// adjoint is b = (H W)^-1 R a and the recursion keeps the forward's form, with the
+// forward's one-sided rows (and an adjoint form of them) and free-surface ghost plane
+// applied to b and mt.  This needs the z stretching to be 1 and the z damping zero on
+// the planes next to the side (no supergrid layer there), which the call checks.  The
+// gradient terms of the one-sided rows come from grad_rows (adj_grad.cu).
 // Forward levels come from checkpoints every C steps, recomputed one segment
 // at a time with every level and predicted level kept in HBM.
 #include <algorithm>
+#include <tuple>
 #include <cmath>
 #include <vector>
 
@@ -59,35 +68,59 @@ __device__ __forceinline__ T sxyz(const Box& b, const ProfT<T>& f, int i, int j,
    return f.st[0][i - b.ib] * f.st[1][j - b.jb] * f.st[2][k - b.kb];
 }
 
-// b[receiver point] += W^-1 R res (receivers in order, 3 values each)
-__global__ void adj_source_kernel(Box b, Prof f, int nrec, const int* __restrict__ ijk,
-                                  const double* __restrict__ res, const double* __restrict__ rho,
-                                  double* __restrict__ an, const double* __restrict__ clk, int nval)
+// Receivers grouped by grid point: point u holds receivers rg.idx[rg.start[u] ..
+// rg.start[u+1]) in increasing order (several receivers may share a point; one thread
+// per point adds their residuals, in order, so the sum does not depend on scheduling).
+struct RecGroups {
+   int n = 0;  // points
+   const int* start = nullptr;
+   const int* idx = nullptr;
+};
+
+// residual sum of point u's receivers, component c, and the point's (i, j, k)
+__device__ __forceinline__ double group_res(const RecGroups& rg, int u, const int* __restrict__ ijk,
+                                            const double* __restrict__ res, int c)
 {
-   const int r = blockIdx.x * blockDim.x + threadIdx.x;
-   if (r >= nrec) return;
+   double acc = 0;
+   for (int q = rg.start[u]; q < rg.start[u + 1]; q++) acc += res[3 * rg.idx[q] + c];
+   return acc;
+}
+
+// b[receiver point] += (H W)^-1 R res (3 values per receiver; hz the SBP norm weights
+// H of the z planes)
+__global__ void adj_source_kernel(Box b, Prof f, RecGroups rg, const int* __restrict__ ijk,
+                                  const double* __restrict__ res, const double* __restrict__ rho,
+                                  const double* __restrict__ hz, double* __restrict__ an,
+                                  const double* __restrict__ clk, int nval)
+{
+   const int u = blockIdx.x * blockDim.x + threadIdx.x;
+   if (u >= rg.n) return;
    if (clk) res += (long long)clk[2] * nval;  // the residual row from the device clock
+   const int r = rg.idx[rg.start[u]];
    const int i = ijk[3 * r], j = ijk[3 * r + 1], k = ijk[3 * r + 2];
    const long long p = pidx(b, i, j, k);
-   const double s = sxyz(b, f, i, j, k) / rho[p];
+   const double s = sxyz(b, f, i, j, k) / (rho[p] * hz[k - b.kb]);
 #pragma unroll
-   for (int c = 0; c < 3; c++) an[c * b.npts + p] += s * res[3 * r + c];
+   for (int c = 0; c < 3; c++) an[c * b.npts + p] += s * group_res(rg, u, ijk, res, c);
 }
 
 // the adjoint source added to a double-float level (hi at q, lo at q + 3 npts) in FP64
-__global__ void adj_source_df_kernel(Box b, Prof f, int nrec, const int* __restrict__ ijk,
+__global__ void adj_source_df_kernel(Box b, Prof f, RecGroups rg, const int* __restrict__ ijk,
                                      const double* __restrict__ res, const double* __restrict__ rho,
-                                     float* __restrict__ an, const double* __restrict__ clk, int nval)
+                                     const double* __restrict__ hz, float* __restrict__ an,
+                                     const double* __restrict__ clk, int nval)
 {
-   const int r = blockIdx.x * blockDim.x + threadIdx.x;
-   if (r >= nrec) return;
+   const int u = blockIdx.x * blockDim.x + threadIdx.x;
+   if (u >= rg.n) return;
    if (clk) res += (long long)clk[2] * nval;
+   const int r = rg.idx[rg.start[u]];
    const int i = ijk[3 * r], j = ijk[3 * r + 1], k = ijk[3 * r + 2];
    const long long p = pidx(b, i, j, k);
-   const double s = sxyz(b, f, i, j, k) / rho[p];
+   const double s = sxyz(b, f, i, j, k) / (rho[p] * hz[k - b.kb]);
    const DFField a{an, 3 * b.npts};
 #pragma unroll
-   for (int c = 0; c < 3; c++) a.set(c * b.npts + p, a.get(c * b.npts + p) + s * res[3 * r + c]);
+   for (int c = 0; c < 3; c++)
+      a.set(c * b.npts + p, a.get(c * b.npts + p) + s * group_res(rg, u, ijk, res, c));
 }
 
 }  // namespace
@@ -100,13 +133,44 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       return kBadArgument;
    if (cv_ || g_.sg_order != 4) return kNotSupported;
    for (int s = 0; s < 6; s++)
-      if (g_.bc[s] != kDirichlet && g_.bc[s] != kSuperGrid) return kNotSupported;
+      if (g_.bc[s] != kDirichlet && g_.bc[s] != kSuperGrid && !(s >= 4 && g_.bc[s] == kStressFree))
+         return kNotSupported;
+   // free-surface z sides: the symmetry D L = (D L)^T needs the z stretching 1 and the
+   // z damping 0 on the ten planes next to the side (true without a layer there)
+   const bool fs_top = onesided_[4] != 0, fs_bot = onesided_[5] != 0;
+   if (fs_top || fs_bot) {
+      const std::vector<double>& sz = prof_.str[2];
+      const std::vector<double>& dz = prof_.dc[2];
+      for (int k = b_.kb; k <= b_.ke; k++) {
+         const bool near = (fs_top && k <= 10) || (fs_bot && k >= g_.nz - 9);
+         const size_t q = (size_t)(k - b_.kb);
+         if (near && ((q < sz.size() && sz[q] != 1.0) || (q < dz.size() && dz[q] != 0.0))) return kNotSupported;
+      }
+      if (g_.nz < 22) return kNotSupported;  // one-sided rows and centred rows apart
+   }
    if (drec_.n == 0) return kBadArgument;
+   // receivers grouped by grid point for the adjoint sources (start | idx)
+   std::vector<int> rgroup;
+   int ngroups = 0;
    {
-      std::vector<int> modes(drec_.n);
+      std::vector<int> modes(drec_.n), ijk(3 * (size_t)drec_.n);
       SW4G_TRY(cuda_ok(cudaMemcpy(modes.data(), drec_.mode, drec_.n * sizeof(int), cudaMemcpyDeviceToHost)));
       for (int m : modes)
          if (m != kRecDisplacement) return kNotSupported;
+      SW4G_TRY(cuda_ok(cudaMemcpy(ijk.data(), drec_.ijk, ijk.size() * sizeof(int), cudaMemcpyDeviceToHost)));
+      std::vector<int> ord(drec_.n);
+      for (int r = 0; r < drec_.n; r++) ord[r] = r;
+      auto key = [&](int r) {
+         return std::make_tuple(ijk[3 * r + 2], ijk[3 * r + 1], ijk[3 * r]);
+      };
+      std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return key(x) < key(y); });
+      std::vector<int> start;
+      for (int q = 0; q < drec_.n; q++)
+         if (q == 0 || key(ord[q]) != key(ord[q - 1])) start.push_back(q);
+      ngroups = (int)start.size();
+      start.push_back(drec_.n);
+      rgroup = start;
+      rgroup.insert(rgroup.end(), ord.begin(), ord.end());
    }
    const int nval = rec_nvals_;
    // the records of this run: the initial row and one per step, from row 0
@@ -146,6 +210,8 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       if (st == kOk) st = alloc(&gc.dfw, mixed_ ? 5 * lv : 10 * lv);
       if (st == kOk) st = alloc(&gc.dfp, 4 * (size_t)(nax[0] + nax[1] + nax[2]) * sizeof(float2));
       if (st == kOk) st = alloc(&gc.dfe, ((size_t)nseg + 2) * sizeof(int) + sizeof(double));
+      if (st == kOk) st = alloc(&gc.hz, (size_t)nax[2] * sizeof(double));
+      if (st == kOk) st = alloc(&gc.rgrp, (2 * (size_t)nval / 3 + 1) * sizeof(int));
       if (st == kOk && !grad_on_device) st = alloc(&gc.gtmp, 3 * (size_t)npts_ * sizeof(double));
       // Segments kept from the forward run, whose recompute the backward sweep skips:
       // the last one in seg/pred, and before it as many as the store budget holds
@@ -181,7 +247,22 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       gc.budget = grad_store_bytes_;
    }
    double *ck = gc.ck, *seg = gc.seg, *pred = gc.pred, *work = gc.work, *resd = gc.resd, *dfw = gc.dfw,
-          *dfp = gc.dfp, *dfe = gc.dfe;
+          *dfp = gc.dfp, *dfe = gc.dfe, *hz = gc.hz;
+   {  // the SBP norm weights of the z planes: 1 but next to free-surface sides
+      static const double om[4] = {17.0 / 48, 59.0 / 48, 43.0 / 48, 49.0 / 48};
+      std::vector<double> hh(nax[2], 1.0);
+      for (int k = bd.kb; k <= bd.ke; k++) {
+         if (fs_top && k >= 1 && k <= 4) hh[k - bd.kb] = om[k - 1];
+         if (fs_bot && k <= g_.nz && k >= g_.nz - 3) hh[k - bd.kb] = om[g_.nz - k];
+      }
+      if (st == kOk) st = cuda_ok(cudaMemcpy(hz, hh.data(), hh.size() * sizeof(double), cudaMemcpyHostToDevice));
+      if (st == kOk)
+         st = cuda_ok(cudaMemcpy(gc.rgrp, rgroup.data(), rgroup.size() * sizeof(int), cudaMemcpyHostToDevice));
+   }
+   RecGroups rg;
+   rg.n = ngroups;
+   rg.start = reinterpret_cast<const int*>(gc.rgrp);
+   rg.idx = rg.start + ngroups + 1;
    const std::vector<double*>& xbuf = gc.xbuf;
    double* gr_d = grad_on_device ? g_rho : gc.gtmp;
    double* gm_d = grad_on_device ? g_mu : gc.gtmp + npts_;
@@ -250,6 +331,8 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       ms.h = g_.h;
       ms.dt = dt;
       ms.status = reinterpret_cast<int*>(dstat_);
+      ms.k1 = fs_top ? 7 : 1;
+      ms.k2 = fs_bot ? g_.nz - 6 : g_.nz;
    }
    auto F = [](double* x) { return reinterpret_cast<float*>(x); };
    GradDF gd;
@@ -290,8 +373,24 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       gd.marg_a = marg - 30;  // the adjoint level is at most (steps) x (largest injection)
       gd.marg_f = 4 - 32;     // w1 = up - 2u + um is at most 4 x the largest level
    }
+   if (fs_top) gd.zlo = 6;
+   if (fs_bot) gd.zhi = g_.nz - 5;
+   GradRows gw;  // the one-sided rows' gradient terms
+   gw.b = b;
+   gw.nz = g_.nz;
+   gw.sx = dprof_[3];
+   gw.sy = dprof_[4];
+   gw.sz = dprof_[5];
+   gw.hz = hz;
+   gw.c1 = dt * dt / 12;
+   gw.c2 = dt * dt;
+   gw.h = g_.h;
+   gw.gm = gm_d;
+   gw.gl = gl_d;
+   gw.lo = (long long)n3;
    float2* pp = reinterpret_cast<float2*>(dfp);
    gp.beta = beta;
+   gp.hz = hz;
    for (int a = 0; a < 3; a++) {
       gp.n[a] = nax[a];
       gp.st[a] = dprof_[3 + a];
@@ -396,7 +495,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       if (!mixed_) {  // the adjoint level's shift from its sources; the per-point sums zeroed
          SW4G_TRY(cuda_ok(cudaMemsetAsync(dfe, 0, sizeof(double), stream_)));
          const double* stp[3] = {dprof_[3], dprof_[4], dprof_[5]};
-         SW4G_TRY(launch_inj_exp(b, stp, drec_.n, drec_.ijk, resd, nsteps + 1, nval, rho_, emax, stream_));
+         SW4G_TRY(launch_inj_exp(b, stp, drec_.n, drec_.ijk, resd, nsteps + 1, nval, rho_, hz, emax, stream_));
          SW4G_TRY(cuda_ok(cudaMemsetAsync(gd.am, 0, 3 * (size_t)npts_ * sizeof(float2), stream_)));
       }
 
@@ -406,18 +505,49 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       double* mt = work + 3 * n3;  // b1 + dt^2/12 R L(b1)
       double* w1 = work + 4 * n3;  // the FP64 form's second mt slot
       SW4G_TRY(cuda_ok(cudaMemsetAsync(work, 0, 5 * lv, stream_)));  // not fin
-      // b^N = W^-1 R g^N
+      // b^N = (H W)^-1 R g^N
       if (mixed_)
-         adj_source_df_kernel<<<blocks_for(drec_.n, 64), 64, 0, stream_>>>(
-             b, pf, drec_.n, drec_.ijk, resd + (size_t)nsteps * nval, rho_, F(b1), nullptr, nval);
+         adj_source_df_kernel<<<blocks_for(rg.n, 64), 64, 0, stream_>>>(
+             b, pf, rg, drec_.ijk, resd + (size_t)nsteps * nval, rho_, hz, F(b1), nullptr, nval);
       else
-         adj_source_kernel<<<blocks_for(drec_.n, 64), 64, 0, stream_>>>(
-             b, pf, drec_.n, drec_.ijk, resd + (size_t)nsteps * nval, rho_, b1, nullptr, nval);
+         adj_source_kernel<<<blocks_for(rg.n, 64), 64, 0, stream_>>>(
+             b, pf, rg, drec_.ijk, resd + (size_t)nsteps * nval, rho_, hz, b1, nullptr, nval);
       SW4G_TRY(launch_status());
+      // the free-surface ghost planes of an adjoint level
+      auto fs_ghosts = [&](double* x, cudaStream_t s) -> int {
+         for (int side = 4; side <= 5; side++)
+            if (onesided_[side])
+               SW4G_TRY(launch_free_surface_ghosts(b, g_.nz, side, mixed_, x, mu_, la_, dprof_[3], dprof_[4],
+                                                   g_.h, sbop_, s));
+         return kOk;
+      };
+      // the one-sided rows of an adjoint stage: corrector 0 (mt = u + coef R L(field),
+      // u = um = field) or 2 (out = 2u - um + coef R L(field) - beta R SG(u - um))
+      const double* dcp[3] = {dprof_[0], dprof_[1], dprof_[2]};
+      const double* stp3[3] = {dprof_[3], dprof_[4], dprof_[5]};
+      const double* cop[3] = {dprof_[6], dprof_[7], dprof_[8]};
+      auto adj_rows = [&](int form, const double* field, const double* u, const double* um, double* out,
+                          double coef, double bt, cudaStream_t s) -> int {
+         for (int side = 0; side < 2; side++) {
+            if (!onesided_[4 + side]) continue;
+            if (mixed_) {
+               auto CF = [](const double* x) { return reinterpret_cast<const float*>(x); };
+               SW4G_TRY(launch_stage_rows_df(form, side == 0, b, g_.nz, nullptr, CF(field), b, mu_, la_, g_.h,
+                                             stp3[0], stp3[1], stp3[2], CF(u), CF(um), nullptr, F(out), rho_,
+                                             irho_, coef, bt, dcp, stp3, cop, zc_[side], s));
+            } else {
+               SW4G_TRY(launch_stage_rows(form, side == 0, b, g_.nz, field, b, mu_, la_, g_.h, stp3[0], stp3[1],
+                                          stp3[2], u, um, nullptr, out, rho_, irho_, coef, bt, dcp, stp3, cop,
+                                          zc_[side], s));
+            }
+         }
+         return kOk;
+      };
+      SW4G_TRY(fs_ghosts(b1, stream_));
       FusedStage fs;
       fs.b = b;
-      fs.k1 = 1;
-      fs.k2 = g_.nz;
+      fs.k1 = fs_top ? 7 : 1;
+      fs.k2 = fs_bot ? g_.nz - 6 : g_.nz;
       fs.mu = mu_;
       fs.la = la_;
       fs.rho = rho_;
@@ -458,6 +588,8 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
             m.beta = 0;
             m.coef = dt * dt / 12;
             if (status == kOk) status = launch_mixed_stage(m, sa);
+            if (status == kOk) status = adj_rows(0, b1, b1, b1, mtb, dt * dt / 12, 0.0, sa);
+            if (status == kOk) status = fs_ghosts(mtb, sa);
             if (status == kOk) status = cuda_ok(cudaEventRecord(ev_s0, sa));
             if (status == kOk) status = cuda_ok(cudaStreamWaitEvent(gs, ev_s0, 0));
             if (status == kOk) {
@@ -470,6 +602,17 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
                g.lun = CF(un);
                status = launch_grad_f1_step(g, gs);
             }
+            for (int side = 0; side < 2 && status == kOk; side++) {
+               if (!onesided_[4 + side]) continue;
+               GradRows r = gw;
+               r.top = side == 0;
+               r.lb1 = CF(b1);
+               r.lmt = CF(mtb);
+               r.lup = CF(up);
+               r.lu = CF(u);
+               r.lum = CF(um);
+               status = launch_grad_rows(r, gs);
+            }
             if (status == kOk) status = cuda_ok(cudaEventRecord(ev_g[nn & 1], gs));
             m = ms;  // b^n = 2 b1 - b2 + dt^2 R L(mt) - beta R SG(b1 - b2): adjoint form
             m.corrector = 2;
@@ -479,11 +622,13 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
             m.out = F(bn);
             m.beta = beta;
             if (status == kOk) status = launch_mixed_stage(m, sa);
+            if (status == kOk) status = adj_rows(2, mtb, b1, b2, bn, dt * dt, beta, sa);
             if (status == kOk) {
-               adj_source_df_kernel<<<blocks_for(saved_n, 64), 64, 0, sa>>>(b, pf, saved_n, drec_.ijk, res, rho_,
-                                                                            F(bn), clk, nval);
+               adj_source_df_kernel<<<blocks_for(rg.n, 64), 64, 0, sa>>>(b, pf, rg, drec_.ijk, res, rho_, hz,
+                                                                         F(bn), clk, nval);
                status = launch_status();
             }
+            if (status == kOk) status = fs_ghosts(bn, sa);
          } else {
             // mt = b1 + dt^2/12 R L(b1): predictor form, um = u; into the slot whose
             // previous reader, the gradient terms two steps later, has finished
@@ -497,6 +642,8 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
             fs.beta = 0;
             fs.coef = dt * dt / 12;
             if (status == kOk) status = launch_fused_stage(fs, sa);
+            if (status == kOk) status = adj_rows(0, b1, b1, b1, mtb, dt * dt / 12, 0.0, sa);
+            if (status == kOk) status = fs_ghosts(mtb, sa);
             if (status == kOk) status = cuda_ok(cudaEventRecord(ev_s0, sa));
             if (status == kOk) status = cuda_ok(cudaStreamWaitEvent(gs, ev_s0, 0));
             if (status == kOk) {  // the gradient terms of the step (double-float sums)
@@ -509,6 +656,17 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
                g.un = un;
                status = launch_grad_df_step(g, gs);
             }
+            for (int side = 0; side < 2 && status == kOk; side++) {
+               if (!onesided_[4 + side]) continue;
+               GradRows r = gw;
+               r.top = side == 0;
+               r.b1 = b1;
+               r.mt = mtb;
+               r.up = up;
+               r.u = u;
+               r.um = um;
+               status = launch_grad_rows(r, gs);
+            }
             if (status == kOk) status = cuda_ok(cudaEventRecord(ev_g[nn & 1], gs));
             if (status == kOk) {  // b^n = 2 b1 - b2 + dt^2 R L(mt) - beta R SG(b1 - b2)
                fs.corrector = 2;
@@ -520,11 +678,13 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
                fs.coef = dt * dt;
                status = launch_fused_stage(fs, sa);
             }
+            if (status == kOk) status = adj_rows(2, mtb, b1, b2, bn, dt * dt, beta, sa);
             if (status == kOk) {
-               adj_source_kernel<<<blocks_for(saved_n, 64), 64, 0, sa>>>(
-                   b, pf, saved_n, drec_.ijk, res, rho_, bn, clk, nval);
+               adj_source_kernel<<<blocks_for(rg.n, 64), 64, 0, sa>>>(b, pf, rg, drec_.ijk, res, rho_, hz, bn,
+                                                                     clk, nval);
                status = launch_status();
             }
+            if (status == kOk) status = fs_ghosts(bn, sa);
          }
          if (status == kOk && clocked) status = launch_clock_advance(dclock_, 0.0, 0.0, -1.0, sa);
          return status;

@@ -144,6 +144,26 @@ int bc_sides(int soa, int ib, int ie, int jb, int je, int kb, int ke, const int 
    return launch_status();
 }
 
+// The ghost plane of one free-surface z side (side 4 top, 5 bottom) from the
+// homogeneous traction condition, on an FP64 level or a double-float level (df).
+int launch_free_surface_ghosts(const Box& b, int nz, int side, bool df, void* u, const double* mu,
+                               const double* la, const double* strx, const double* stry, double h,
+                               const double sbop[5], cudaStream_t s)
+{
+   if ((side != 4 && side != 5) || !u) return kBadArgument;
+   FreeSurf fs;
+   for (int q = 0; q < 5; q++) fs.sbop[q] = sbop[q];
+   const int k = side == 4 ? 1 : nz, kl = side == 4 ? 1 : -1;
+   const dim3 block(32, 8), grid(blocks_for(b.ie - b.ib - 3, 32), blocks_for(b.je - b.jb - 3, 8));
+   if (df)
+      free_surface_kernel<<<grid, block, 0, s>>>(b, DFField{static_cast<float*>(u), 3 * b.npts}, mu, la,
+                                                 nullptr, strx, stry, h, k, kl, fs);
+   else
+      free_surface_kernel<<<grid, block, 0, s>>>(b, F64Field{static_cast<double*>(u)}, mu, la, nullptr, strx,
+                                                 stry, h, k, kl, fs);
+   return launch_status();
+}
+
 int launch_bcfortsg(int soa, int ib, int ie, int jb, int je, int kb, int ke, const int wind[36],
                     int nx, int ny, int nz, double* u, double h, const int bccnd[6],
                     const double sbop[5], const double* mu, const double* la,

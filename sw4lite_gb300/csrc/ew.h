@@ -298,7 +298,8 @@ class EW {
       int nsteps = 0, ckpt = 0, nval = 0, mixed = -1, host_grad = -1;
       std::vector<void*> mem;  // every allocation
       double *ck = nullptr, *seg = nullptr, *pred = nullptr, *work = nullptr, *resd = nullptr,
-             *dfw = nullptr, *dfp = nullptr, *dfe = nullptr, *gtmp = nullptr;
+             *dfw = nullptr, *dfp = nullptr, *dfe = nullptr, *gtmp = nullptr, *hz = nullptr,
+             *rgrp = nullptr;  // rgrp: receivers grouped by grid point (ints)
       std::vector<double*> xbuf;  // segments kept from the forward run
    } gcache_;
    void drop_grad_cache();

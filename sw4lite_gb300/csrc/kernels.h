@@ -267,6 +267,12 @@ int launch_bcfortsg(int soa, int ib, int ie, int jb, int je, int kb, int ke, con
                     const double* const bforce[6], const double* strx, const double* stry,
                     cudaStream_t s);
 
+// The ghost plane of one free-surface z side (4 top, 5 bottom) from the homogeneous
+// traction condition, on an FP64 level or a double-float level (df).
+int launch_free_surface_ghosts(const Box& b, int nz, int side, bool df, void* u, const double* mu,
+                               const double* la, const double* strx, const double* stry, double h,
+                               const double sbop[5], cudaStream_t s);
+
 int launch_force_dense(int soa, int ib, int ie, int jb, int je, int kb, int ke, double* f,
                        const SourceSet& src, double t, int tt, cudaStream_t s);
 // clk (optional): the device clock of a captured time loop, [0] the forcing time,
@@ -392,17 +398,36 @@ struct GradDF {
    int marg_a = 0, marg_f = 0;
    double *gm64 = nullptr, *gl64 = nullptr, *gr64 = nullptr;  // FP32 form: the gradients
    double kmu = 0;
+   // free-surface z sides: the one-sided rows' planes k <= zlo, k >= zhi, whose adjoint
+   // values the z-involving terms skip (grad_rows covers them)
+   int zlo = -(1 << 29), zhi = 1 << 29;
 };
+// The z-involving gradient terms of the six one-sided rows next to a free-surface z
+// side (top: rows 1..6, bottom: nz-5..nz), FP64, added to the FP64 gradients gm, gl:
+// pairs (c1 H W b1, up - 2u + um) and (c2 H W mt, u); levels FP64 or, with the lb1..lum
+// pointers, double-float (hi at q, lo at q + lo).
+struct GradRows {
+   Box b;
+   int nz = 0, top = 1;
+   const double *b1 = nullptr, *mt = nullptr, *up = nullptr, *u = nullptr, *um = nullptr;
+   const float *lb1 = nullptr, *lmt = nullptr, *lup = nullptr, *lu = nullptr, *lum = nullptr;
+   long long lo = 0;
+   const double *sx = nullptr, *sy = nullptr, *sz = nullptr, *hz = nullptr;
+   double c1 = 0, c2 = 0, h = 0;
+   double *gm = nullptr, *gl = nullptr;
+};
+int launch_grad_rows(const GradRows& g, cudaStream_t s);
 struct GradDFProfiles {
    int n[3];
    const double *st[3], *co[3], *dc[3];
    double beta;
    float2 *st24[3], *ist[3], *cist[3], *bdc[3];
+   const double* hz = nullptr;  // SBP norm weights of the z planes (free-surface sides)
 };
 int launch_grad_df_profiles(const GradDFProfiles& p, cudaStream_t s);
 int launch_exp_max(const double* x, long long n, int* out, cudaStream_t s);
 int launch_inj_exp(const Box& b, const double* const st[3], int nrec, const int* ijk, const double* res,
-                   long long rows, int nval, const double* rho, int* out, cudaStream_t s);
+                   long long rows, int nval, const double* rho, const double* hz, int* out, cudaStream_t s);
 int launch_grad_df_step(const GradDF& g, cudaStream_t s);
 // The grid-point sources of nsrc sources on the Cartesian grid (srcdisc.cu): one
 // device block *mem (freed and replaced) holding the grouped SourceSet.  Synchronises

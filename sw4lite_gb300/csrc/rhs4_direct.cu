@@ -327,6 +327,8 @@ __global__ void __launch_bounds__(256) rhs4_bndry_kernel(OpArgs a)
 // Fused update on the one-sided rows (SoA fields):
 //   predictor  out = 2u - um + dt^2/rho * L(u)
 //   corrector  out = up + dt^2/12/rho * L(up - 2u + um) - beta/rho * SG(u - um)
+//   adjoint    out = 2u - um + coef/rho * L(field) - beta/rho * SG(u - um)  (corrector 2,
+//              the adjoint step's second stage)
 // where the corrector's field (up - 2u + um) comes from a scratch slab (box a.bu)
 // and SG is the 4th-order supergrid damping of src/ew-cfromfort.C:952-1057.
 struct RowUpdate {
@@ -414,12 +416,11 @@ __global__ void __launch_bounds__(256, 2) stage_rows_kernel(OpArgs a, RowUpdate 
       const long long q = cidx(a.b, c, i, j, k);
       const double lu = a.cof * r[c];
       double v;
-      if (!w.corrector) {
+      if (w.corrector != 1)
          v = 2 * lvl<DF>(w.u, w.udf, q, w.lo) - lvl<DF>(w.um, w.umdf, q, w.lo) + cr * lu;
-      } else {
+      else
          v = lvl<DF>(w.up, w.updf, q, w.lo) + cr * lu;
-         if (w.beta != 0) v -= birho * sg4_point<DF>(a.b, w, c, i, j, k);
-      }
+      if (w.corrector != 0 && w.beta != 0) v -= birho * sg4_point<DF>(a.b, w, c, i, j, k);
       if (DF) {
          const float hh = __double2float_rn(v);
          w.outdf[q] = hh;

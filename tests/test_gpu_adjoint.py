@@ -9,6 +9,10 @@
   (rho, mu, lambda) to 1e-6 relative.
 * Segments kept from the forward run (sw4g_ew_set_gradient_memory) instead of
   recomputed give bit-identical results.
+* Free-surface z sides (one-sided SBP rows, ghost plane from the traction
+  condition) with receivers on the free surface: the same bars against the
+  oracle's free-surface adjoint (top, bottom, both) and against finite differences
+  at 48^3; the FP32-mixed form against the FP64 gradient.
 """
 import numpy as np
 import pytest
@@ -86,6 +90,23 @@ def test_gradient_matches_oracle_adjoint(ckpt, memory):
     assert _rel(ufin, levels[-1]) <= 1e-12
 
 
+@pytest.mark.parametrize("precision", [sg.FP64, sg.MIXED])
+def test_gradient_receivers_sharing_a_point(precision):
+    # three receivers on one grid point and two on another: their adjoint sources add
+    # up at the point (a race between receivers of one point would drop some)
+    c = AdjointCase()
+    c.rec = c.rec + [c.rec[0], c.rec[0], c.rec[2]]
+    obs_case = AdjointCase(seed=11)
+    obs_case.rec = c.rec
+    obs = obs_case.records(oracle_forward(obs_case)[0][1:])
+    J0, gr, gm, gl = oracle_gradient(c, obs)
+    J, g, _ = _gpu_gradient(c, obs, 10, precision=precision)
+    tol = 1e-9 if precision == sg.FP64 else 1e-5
+    assert J == pytest.approx(J0, rel=1e-12 if precision == sg.FP64 else 1e-6)
+    for a, b in zip(g, (gr, gm, gl)):
+        assert _rel(a, b) <= tol
+
+
 def test_gradient_matches_finite_differences_48():
     # the finite-difference copy of the adjoint workload: 48^3, 5% log-normal
     # heterogeneity with correlation length 10h (here 10 points), 16 receivers
@@ -116,10 +137,14 @@ def test_gradient_rejects_unsupported_set_ups():
     c = AdjointCase(shape=(16, 16, 16), nsteps=4)
     obs = np.zeros((5, 3 * len(c.rec)))
     g = [np.zeros(c.npts) for _ in range(3)]
-    free = sg.grid_desc(16, 16, 16, c.h, bc=(2, 2, 2, 2, 0, 2), sg_gp=5)
-    for grid, code in ((free, "not supported"),):
+    # a free surface whose one-sided rows meet the other side's rows (nz < 22), and
+    # one whose z supergrid layer reaches the ten planes next to it
+    thin = sg.grid_desc(16, 16, 16, c.h, bc=(2, 2, 2, 2, 0, 2), sg_gp=5)
+    layered = sg.grid_desc(40, 40, 24, c.h, bc=(2, 2, 2, 2, 0, 2), sg_gp=16)
+    for grid in (thin, layered):
+        npts = (grid.nx + 4) * (grid.ny + 4) * (grid.nz + 4)
         ew = sg.EW(grid)
-        ew.set_material(*[dev(a) for a in c.mat])
+        ew.set_material(*[dev(np.full(npts, v)) for v in (1.0, 1.0, 1.0)])
         ew.set_time_step(c.dt)
         ew.set_receivers(c.rec, [sg.REC_DISPLACEMENT] * len(c.rec), 5)
         with pytest.raises(sg.Sw4gError):
@@ -216,3 +241,61 @@ def test_repeated_gradients_reuse_buffers(precision):
         for x, y in zip(g, fresh[k][1]):
             assert np.array_equal(host(x), y)
     ew.close()
+
+
+# ---- free-surface z sides ----
+
+FS_CASES = [((2, 2, 2, 2, 0, 2), 1), ((2, 2, 2, 2, 2, 0), 24), ((2, 2, 2, 2, 0, 0), 1)]
+
+
+@pytest.mark.parametrize("bc,rec_k", FS_CASES)
+@pytest.mark.parametrize("ckpt,memory", [(30, None), (7, 0)])
+def test_fs_gradient_matches_oracle_adjoint(bc, rec_k, ckpt, memory):
+    kw = dict(shape=(16, 15, 24), bc=bc, rec_k=rec_k)
+    c = AdjointCase(**kw)
+    obs_case = AdjointCase(seed=11, **kw)
+    obs = obs_case.records(oracle_forward(obs_case)[0][1:])
+    J0, gr, gm, gl = oracle_gradient(c, obs)
+    J, (r, m, l), ufin = _gpu_gradient(c, obs, ckpt, memory=memory)
+    assert J == pytest.approx(J0, rel=1e-12)
+    assert _rel(r, gr) <= 1e-9
+    assert _rel(m, gm) <= 1e-9
+    assert _rel(l, gl) <= 1e-9
+
+
+def test_fs_gradient_matches_finite_differences_48():
+    # the 48^3 copy of the adjoint workload with a free surface on top and the 16
+    # receivers on it (supergrid on the other five sides)
+    kw = dict(shape=(48, 48, 48), h=0.05, gp=10, nsteps=160, nrec=16, vp=1.732, vs=1.0, rho=1.0,
+              bc=(2, 2, 2, 2, 0, 2), rec_k=1)
+    c = AdjointCase(seed=21, **kw)
+    obs_case = AdjointCase(seed=22, **kw)
+    obs_case.rec = c.rec
+    ew = _ew(obs_case)
+    ew.step(obs_case.nsteps, sg.MODE_FUSED)
+    obs = ew.records()
+    ew.close()
+    J, (gr, gm, gl), _ = _gpu_gradient(c, obs, 40)
+    shape = (c.nz + 4, c.ny + 4, c.nx + 4)
+    dirs = [smooth_random(shape, 70 + q, corr=5.0, amp=0.3).reshape(-1) - 1.0 for q in range(3)]
+    dm = [dirs[q] * c.mat[q] for q in range(3)]
+    pred = float(gr @ dm[0] + gm @ dm[1] + gl @ dm[2])
+    eps = 1e-5
+    Jp = _gpu_misfit(c, obs, [c.mat[q] + eps * dm[q] for q in range(3)])
+    Jm = _gpu_misfit(c, obs, [c.mat[q] - eps * dm[q] for q in range(3)])
+    fd = (Jp - Jm) / (2 * eps)
+    assert J > 0 and abs(pred) > 0
+    assert abs(fd - pred) <= 1e-6 * abs(pred), (fd, pred)
+
+
+@pytest.mark.parametrize("bc,rec_k", FS_CASES[:2])
+def test_fs_mixed_gradient_close_to_fp64(bc, rec_k):
+    kw = dict(shape=(16, 15, 24), bc=bc, rec_k=rec_k, nsteps=40)
+    c = AdjointCase(**kw)
+    obs_case = AdjointCase(seed=11, **kw)
+    obs = obs_case.records(oracle_forward(obs_case)[0][1:])
+    J0, g0, _ = _gpu_gradient(c, obs, 10)
+    J1, g1, _ = _gpu_gradient(c, obs, 10, precision=sg.MIXED)
+    assert J1 == pytest.approx(J0, rel=1e-6)
+    for a, b in zip(g1, g0):
+        assert _rel(a, b) <= 1e-5, _rel(a, b)
