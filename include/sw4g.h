@@ -289,11 +289,11 @@ int sw4g_ew_add_grid_point_sources(sw4g_ew* ew, int n, const int* ijk, const dou
 int sw4g_ew_clear_sources(sw4g_ew* ew);
 int sw4g_ew_num_grid_point_sources(const sw4g_ew* ew);
 /* Where sw4g_ew_add_source computes the grid-point sources (the host loop of
- * Source::set_grid_point_sources4, src/Source.C:1074-1530): on the host (0, the
+ * Source::set_grid_point_sources4, src/Source.C:1074-1990): on the host (0, the
  * default), or on the device (1), one CTA per source for the whole batch before the
- * next step, grouped by grid point on the device; the same bits either way.  The
- * device path takes the Cartesian grid alone (SW4G_NOT_SUPPORTED with topography or
- * with sources from sw4g_ew_add_grid_point_sources). */
+ * next step, grouped by grid point on the device; the same bits either way on a
+ * Cartesian grid, the last bits of exp/pow with topography.  SW4G_NOT_SUPPORTED with
+ * sources from sw4g_ew_add_grid_point_sources or on a subdomain. */
 int sw4g_ew_set_source_discretization(sw4g_ew* ew, int on_device);
 int sw4g_ew_set_time_step(sw4g_ew* ew, double dt, double t0);
 /* dt from the CFL number, adjusted to end at tmax (EW::computeDT, src/EW.C:5041) */
@@ -343,7 +343,9 @@ int sw4g_ew_status(sw4g_ew* ew);
  * each), by the exact transpose of the step with checkpoints every
  * checkpoint_every steps.  Device memory: (2*ceil(nsteps/C) + 2*C + 19) levels of
  * 3*npts doubles, plus the segments kept from the forward run (below).  Requires
- * Dirichlet or supergrid sides (zero ghost data), 4th-order damping, no topography.
+ * Dirichlet or supergrid sides (zero ghost data) or free-surface z sides (with the z
+ * stretching 1 and no z damping on the ten planes next to them, nz >= 22), 4th-order
+ * damping, no topography.  Receivers may share a grid point.
  * The object ends at the end of the forward run.  It keeps that device memory for its
  * next gradient of the same nsteps, checkpoint interval and receivers; a failed call,
  * sw4g_ew_set_gradient_memory and sw4g_ew_destroy release it. */
