@@ -29,6 +29,10 @@ int sw4g_dev_set_stage_chunks(int chunks);
  * predictor and corrector stages on the tensor-copy kernels wherever the array
  * strides allow, 0 on the synchronous kernels; for all objects of the process. */
 int sw4g_dev_set_mixed_tma(int on);
+/* Comparison switch (no reference counterpart): 1 (the default) runs the one-sided
+ * rows next to a free surface on a second stream beside each fused stage kernel, 0
+ * after it on the object's stream; for all objects of the process. */
+int sw4g_dev_set_rows_overlap(int on);
 /* Tuning (no reference counterpart): the planes per k chunk that the automatic
  * choice gives a stage kernel of `cols` CTA columns over nk planes with `resident`
  * CTAs per SM on the current device's SMs (152 when no device answers), at least

@@ -810,6 +810,13 @@ int sw4g_dev_set_mixed_tma(int on)
    return SW4G_OK;
 }
 
+int sw4g_dev_set_rows_overlap(int on)
+{
+   if (on != 0 && on != 1) return SW4G_BAD_ARGUMENT;
+   set_rows_overlap(on);
+   return SW4G_OK;
+}
+
 int sw4g_dev_stage_kchunk(long long cols, int nk, int resident, int min_planes, int* planes)
 {
    if (!planes || cols < 1 || nk < 1 || resident < 1 || min_planes < 1) return SW4G_BAD_ARGUMENT;

@@ -22,6 +22,12 @@ EW::~EW()
 {
    drop_graphs();
    drop_grad_cache();
+   if (side_) {
+      cudaStreamSynchronize(side_);
+      cudaStreamDestroy(side_);
+   }
+   if (ev_fork_) cudaEventDestroy(ev_fork_);
+   if (ev_join_) cudaEventDestroy(ev_join_);
    auto f = [](void* p) {
       if (p) cudaFree(p);
    };
@@ -145,6 +151,8 @@ int EW::init()
    SW4G_TRY(upload_sbp_tables_direct());
    if (cv_) SW4G_TRY(init_topo());
    SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
+   // the rows' second stream, made here rather than inside a graph capture
+   if (onesided_[4] || onesided_[5]) SW4G_TRY(side_stream());
    ready_ = true;
    return kOk;
 }
@@ -1029,14 +1037,46 @@ int EW::mixed_piece(int piece, int ip, int iq)
    return kBadArgument;
 }
 
+int EW::side_stream()
+{
+   if (side_) return kOk;
+   SW4G_TRY(cuda_ok(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking)));
+   SW4G_TRY(cuda_ok(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming)));
+   return cuda_ok(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming));
+}
+
 int EW::step_fused()
 {
    int ip = 0;
    while (ip == iu_ || ip == ium_) ip++;
    int iq = ip + 1;
    while (iq == iu_ || iq == ium_) iq++;
+   // The one-sided rows (pieces 1, 4) write planes 1..6 / nz-5..nz and the ghost
+   // shell, the stage kernels (0, 3) the planes between, both from the same inputs:
+   // the rows run beside the stage on a second stream (the stage launched first, so
+   // its CTAs are dispatched ahead; a rows CTA fits beside one on each SM), joined
+   // before the forcing and boundary pieces.  Not with 6th-order damping, whose pass
+   // in piece 4 covers every plane.
+   const bool beta6 = g_.sg_order == 6 && prof_.used && g_.sg_damping != 0;
+   const bool beside = rows_overlap_enabled() && (onesided_[4] || onesided_[5]) && !beta6;
    for (int which = 0; which < 6; which++) {
-      SW4G_TRY(piece(which, ip, iq));
+      if (beside && (which == 1 || which == 4)) continue;
+      if (beside && (which == 0 || which == 3)) {
+         // fork point before the stage, stage first, then the rows, then the join
+         SW4G_TRY(side_stream());
+         SW4G_TRY(cuda_ok(cudaEventRecord(ev_fork_, stream_)));
+         SW4G_TRY(piece(which, ip, iq));
+         SW4G_TRY(cuda_ok(cudaStreamWaitEvent(side_, ev_fork_, 0)));
+         cudaStream_t own = stream_;
+         stream_ = side_;
+         const int st = piece(which + 1, ip, iq);
+         stream_ = own;
+         SW4G_TRY(st);
+         SW4G_TRY(cuda_ok(cudaEventRecord(ev_join_, side_)));
+         SW4G_TRY(cuda_ok(cudaStreamWaitEvent(stream_, ev_join_, 0)));
+      } else {
+         SW4G_TRY(piece(which, ip, iq));
+      }
       if (!cv_) continue;
       if (which == 0) SW4G_TRY(curv_pred(ip));
       if (which == 2) SW4G_TRY(curv_bc(lev_[ip], cv_->lev[ip]));

@@ -317,6 +317,11 @@ class EW {
    NanReport nan_{};
 
    bool graphs_ = false, clocked_ = false, warm_ = false;
+   // the one-sided rows beside the stage kernels: a second stream forked from and
+   // joined to stream_ by events (made on first use)
+   cudaStream_t side_ = nullptr;
+   cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
+   int side_stream();
    double* dclock_ = nullptr;  // [0] forcing time, [1] record row, [2] adjoint residual row
    struct GraphKey {
       int iu, ium, rec;

@@ -323,6 +323,10 @@ int launch_mixed_stage_tma(const MixedStage& st, cudaStream_t stream);
 // 0 keeps launch_mixed_stage on the synchronous kernels (for comparisons), 1 the default
 void set_mixed_tma(int on);
 int mixed_tma_enabled();
+// 1 (the default): the one-sided rows of a stage run on a second stream beside the
+// stage kernel; 0: after it, on the object's stream
+void set_rows_overlap(int on);
+int rows_overlap_enabled();
 int launch_df_from_f64(long long n, const double* x, float* h, float* l, cudaStream_t s);
 // FP64 -> interleaved (hi, lo) FP32 pairs
 int launch_df2_from_f64(long long n, const double* x, float2* hl, cudaStream_t s);

@@ -591,6 +591,9 @@ std::atomic<int> g_mixed_tma{1};
 
 void set_mixed_tma(int on) { g_mixed_tma.store(on ? 1 : 0); }
 int mixed_tma_enabled() { return g_mixed_tma.load(); }
+std::atomic<int> g_rows_overlap{1};
+void set_rows_overlap(int on) { g_rows_overlap.store(on ? 1 : 0); }
+int rows_overlap_enabled() { return g_rows_overlap.load(); }
 
 int launch_mixed_stage(const MixedStage& st, cudaStream_t stream)
 {

@@ -192,10 +192,11 @@ def test_coef_gradient_fs_identities(bc):
             assert abs(d - g) <= 1e-12 * abs(full), (p, which, d, g)
 
 
-@pytest.mark.parametrize("which", ["mu", "la", "all"])
-def test_oracle_gradient_fs_matches_finite_differences(which):
-    c = AdjointCase(shape=(16, 15, 24), bc=(2, 2, 2, 2, 0, 2), rec_k=1)
-    obs_case = AdjointCase(shape=(16, 15, 24), bc=(2, 2, 2, 2, 0, 2), rec_k=1, seed=11)
+@pytest.mark.parametrize("which,bc,rec_k", [("mu", (2, 2, 2, 2, 0, 2), 1), ("la", (2, 2, 2, 2, 0, 2), 1),
+                                            ("all", (2, 2, 2, 2, 0, 2), 1), ("all", (2, 2, 2, 2, 2, 0), 24)])
+def test_oracle_gradient_fs_matches_finite_differences(which, bc, rec_k):
+    c = AdjointCase(shape=(16, 15, 24), bc=bc, rec_k=rec_k)
+    obs_case = AdjointCase(shape=(16, 15, 24), bc=bc, rec_k=rec_k, seed=11)
     obs = obs_case.records(oracle_forward(obs_case)[0][1:])
     J, gr, gm, gl = oracle_gradient(c, obs)
     shape = (c.nz + 4, c.ny + 4, c.nx + 4)
