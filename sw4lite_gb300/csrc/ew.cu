@@ -895,7 +895,7 @@ int EW::fused_piece(int piece, int ip, int iq)
          if (onesided_[4 + side])
             SW4G_TRY(launch_stage_rows(0, side == 0, b, nz, u, b, mu_, la_, g_.h, st[0], st[1], st[2],
                                        u, um, nullptr, up, rho_, irho_, dt2, 0.0, dc, st, co,
-                                       zc_[side], stream_, rscr_));
+                                       zc_[side], stream_, rscr_, rows_ctas_));
       return kOk;
    }
    if (piece == 2 || piece == kForcePred || piece == kBcPred) {
@@ -914,7 +914,7 @@ int EW::fused_piece(int piece, int ip, int iq)
          Box sb = make_box(1, bd.ib, bd.ie, bd.jb, bd.je, k0, k1);
          SW4G_TRY(launch_stage_rows(1, side == 0, b, nz, slab, sb, mu_, la_, g_.h, st[0], st[1],
                                     st[2], u, um, up, out, rho_, irho_, dt2 / 12, beta4, dc, st, co,
-                                    zc_[side], stream_, rscr_));
+                                    zc_[side], stream_, rscr_, rows_ctas_));
       }
       if (beta != 0 && g_.sg_order == 6)
          SW4G_TRY(launch_addsgd(6, 1, bd.ib, bd.ie, bd.jb, bd.je, bd.kb, bd.ke, out, u, um, rho_,
@@ -990,7 +990,7 @@ int EW::mixed_piece(int piece, int ip, int iq)
          Box sb = make_box(1, bd.ib, bd.ie, bd.jb, bd.je, k0, k1);
          SW4G_TRY(launch_stage_rows_df(0, side == 0, b, nz, slab, nullptr, sb, mu_, la_, g_.h, st[0],
                                        st[1], st[2], u, um, nullptr, up, rho_, irho_, dt2, 0.0, dc,
-                                       st, co, zc_[side], stream_, nullptr, rscr_));
+                                       st, co, zc_[side], stream_, nullptr, rscr_, rows_ctas_));
       }
       return kOk;
    }
@@ -1016,7 +1016,7 @@ int EW::mixed_piece(int piece, int ip, int iq)
          SW4G_TRY(launch_stage_rows_df(1, side == 0, b, nz, slab, nullptr, sb, mu_, la_, g_.h, st[0],
                                        st[1], st[2], u, um, up, out, rho_, irho_, dt2 / 12, beta4,
                                        dc, st, co, zc_[side], stream_, beta4 != 0 ? dslab : nullptr,
-                                       rscr_));
+                                       rscr_, rows_ctas_));
       }
       if (beta != 0 && g_.sg_order == 6) {
          const float* dc32[3] = {prof32_[0], prof32_[1], prof32_[2]};
@@ -1040,7 +1040,15 @@ int EW::mixed_piece(int piece, int ip, int iq)
 int EW::side_stream()
 {
    if (side_) return kOk;
-   SW4G_TRY(cuda_ok(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking)));
+   int dev = 0, lo = 0, hi = 0;
+   SW4G_TRY(cuda_ok(cudaGetDevice(&dev)));
+   SW4G_TRY(cuda_ok(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev)));
+   // FP32-mixed form: the highest priority, so that the rows' persistent CTAs take
+   // their place on every SM beside the (FP32, issue-bound) stage kernel's as soon as
+   // they are launched.  FP64 form: the stage kernels and the rows both load the FP64
+   // pipe, and the rows' own full grid at the default priority measured best.
+   SW4G_TRY(cuda_ok(cudaDeviceGetStreamPriorityRange(&lo, &hi)));
+   SW4G_TRY(cuda_ok(cudaStreamCreateWithPriority(&side_, cudaStreamNonBlocking, mixed_ ? hi : lo)));
    SW4G_TRY(cuda_ok(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming)));
    return cuda_ok(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming));
 }
@@ -1053,10 +1061,10 @@ int EW::step_fused()
    while (iq == iu_ || iq == ium_) iq++;
    // The one-sided rows (pieces 1, 4) write planes 1..6 / nz-5..nz and the ghost
    // shell, the stage kernels (0, 3) the planes between, both from the same inputs:
-   // the rows run beside the stage on a second stream (the stage launched first, so
-   // its CTAs are dispatched ahead; a rows CTA fits beside one on each SM), joined
-   // before the forcing and boundary pieces.  Not with 6th-order damping, whose pass
-   // in piece 4 covers every plane.
+   // the rows run beside the stage on a second stream, joined before the forcing and
+   // boundary pieces; in the FP32-mixed form as a persistent grid of one CTA per SM (a
+   // rows CTA fits beside a stage CTA on each SM) on a higher-priority stream.  Not
+   // with 6th-order damping, whose pass in piece 4 covers every plane.
    const bool beta6 = g_.sg_order == 6 && prof_.used && g_.sg_damping != 0;
    const bool beside = rows_overlap_enabled() && (onesided_[4] || onesided_[5]) && !beta6;
    for (int which = 0; which < 6; which++) {
@@ -1069,7 +1077,9 @@ int EW::step_fused()
          SW4G_TRY(cuda_ok(cudaStreamWaitEvent(side_, ev_fork_, 0)));
          cudaStream_t own = stream_;
          stream_ = side_;
+         rows_ctas_ = mixed_ ? sms_ : 0;
          const int st = piece(which + 1, ip, iq);
+         rows_ctas_ = 0;
          stream_ = own;
          SW4G_TRY(st);
          SW4G_TRY(cuda_ok(cudaEventRecord(ev_join_, side_)));

@@ -321,6 +321,8 @@ class EW {
    // joined to stream_ by events (made on first use)
    cudaStream_t side_ = nullptr;
    cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
+   int sms_ = 0;        // the device's SM count
+   int rows_ctas_ = 0;  // > 0 while the rows run beside a stage: a persistent grid
    int side_stream();
    double* dclock_ = nullptr;  // [0] forcing time, [1] record row, [2] adjoint residual row
    struct GraphKey {

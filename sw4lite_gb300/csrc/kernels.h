@@ -356,7 +356,7 @@ int launch_stage_rows_df(int corrector, bool top, const Box& b, int nz, const do
                          float* out, const double* rho, const double* irho, double coef,
                          double beta, const double* const dc[3], const double* const st[3],
                          const double* const co[3], const double* zc, cudaStream_t stream,
-                         const double* dd = nullptr, double* rscr = nullptr);
+                         const double* dd = nullptr, double* rscr = nullptr, int ctas = 0);
 
 int launch_weights(const Box& b, const double* mu, const double* la, const double* sx,
                    const double* sy, const double* sz, double h, WeightPtrs w, cudaStream_t s);
@@ -371,8 +371,9 @@ int launch_stage_rows(int corrector, bool top, const Box& b, int nk, const doubl
                       const double* rho, const double* irho, double coef, double beta,
                       const double* const dc[3], const double* const st[3],
                       const double* const co[3], const double* zc, cudaStream_t stream,
-                      double* rscr = nullptr);
-// rscr (optional): work array of 42 x (columns of b) doubles for the rows' per-column terms
+                      double* rscr = nullptr, int ctas = 0);
+// rscr (optional): work array of 42 x (columns of b) doubles for the rows' per-column terms;
+// ctas > 0: a persistent grid of that many CTAs strides over the rows' blocks
 long long zcoef_len(const Box& b);
 int launch_zcoef(const Box& b, int nk, bool top, const double* mu, const double* la, double* zc,
                  cudaStream_t s);

@@ -399,34 +399,42 @@ __device__ __forceinline__ double sg4_point(const Box& b, const RowUpdate& w, in
 
 // DF: the levels (and, when the stage field is not an FP64 slab, the field) are
 // double-float pairs; FDF: the stage field is double-float.
+// DF: the levels (and, when the stage field is not an FP64 slab, the field) are
+// double-float pairs; FDF: the stage field is double-float.  The gx x gy x 6 blocks
+// of 32 x 8 points are strided over by the grid (one CTA per block, or fewer CTAs,
+// each taking several: a persistent grid beside a stage kernel).
 template <bool TOP, bool DF, bool FDF, bool PRE>
-__global__ void __launch_bounds__(256, 2) stage_rows_kernel(OpArgs a, RowUpdate w)
+__global__ void __launch_bounds__(256, 2) stage_rows_kernel(OpArgs a, RowUpdate w, int gx, int gy)
 {
-   const int i = a.b.ib + 2 + blockIdx.x * blockDim.x + threadIdx.x;
-   const int j = a.b.jb + 2 + blockIdx.y * blockDim.y + threadIdx.y;
-   if (i > a.b.ie - 2 || j > a.b.je - 2) return;
-   const int k = TOP ? 1 + (int)blockIdx.z : a.nk - 5 + (int)blockIdx.z;
-   double r[3];
-   lu_bndry_point<TOP, FDF, PRE>(a, i, j, k, r);
-   const long long p = pidx(a.b, i, j, k);
-   const double ir = w.irho ? __ldg(w.irho + p) : 1.0 / __ldg(w.rho + p);
-   const double cr = w.coef * ir;
-   const double birho = w.beta * ir;
-   for (int c = 0; c < 3; c++) {
-      const long long q = cidx(a.b, c, i, j, k);
-      const double lu = a.cof * r[c];
-      double v;
-      if (w.corrector != 1)
-         v = 2 * lvl<DF>(w.u, w.udf, q, w.lo) - lvl<DF>(w.um, w.umdf, q, w.lo) + cr * lu;
-      else
-         v = lvl<DF>(w.up, w.updf, q, w.lo) + cr * lu;
-      if (w.corrector != 0 && w.beta != 0) v -= birho * sg4_point<DF>(a.b, w, c, i, j, k);
-      if (DF) {
-         const float hh = __double2float_rn(v);
-         w.outdf[q] = hh;
-         w.outdf[q + w.lo] = __double2float_rn(v - (double)hh);
-      } else {
-         w.out[q] = v;
+   const int nvb = gx * gy * 6;
+   for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+      const int i = a.b.ib + 2 + (vb % gx) * blockDim.x + threadIdx.x;
+      const int j = a.b.jb + 2 + ((vb / gx) % gy) * blockDim.y + threadIdx.y;
+      if (i > a.b.ie - 2 || j > a.b.je - 2) continue;
+      const int bz = vb / (gx * gy);
+      const int k = TOP ? 1 + bz : a.nk - 5 + bz;
+      double r[3];
+      lu_bndry_point<TOP, FDF, PRE>(a, i, j, k, r);
+      const long long p = pidx(a.b, i, j, k);
+      const double ir = w.irho ? __ldg(w.irho + p) : 1.0 / __ldg(w.rho + p);
+      const double cr = w.coef * ir;
+      const double birho = w.beta * ir;
+      for (int c = 0; c < 3; c++) {
+         const long long q = cidx(a.b, c, i, j, k);
+         const double lu = a.cof * r[c];
+         double v;
+         if (w.corrector != 1)
+            v = 2 * lvl<DF>(w.u, w.udf, q, w.lo) - lvl<DF>(w.um, w.umdf, q, w.lo) + cr * lu;
+         else
+            v = lvl<DF>(w.up, w.updf, q, w.lo) + cr * lu;
+         if (w.corrector != 0 && w.beta != 0) v -= birho * sg4_point<DF>(a.b, w, c, i, j, k);
+         if (DF) {
+            const float hh = __double2float_rn(v);
+            w.outdf[q] = hh;
+            w.outdf[q + w.lo] = __double2float_rn(v - (double)hh);
+         } else {
+            w.out[q] = v;
+         }
       }
    }
 }
@@ -499,7 +507,7 @@ int launch_stage_rows(int corrector, bool top, const Box& b, int nk, const doubl
                       const double* rho, const double* irho, double coef, double beta,
                       const double* const dc[3], const double* const st[3],
                       const double* const co[3], const double* zc, cudaStream_t stream,
-                      double* rscr)
+                      double* rscr, int ctas)
 {
    int status = upload_sbp_tables_direct();
    if (status != kOk) return status;
@@ -539,11 +547,12 @@ int launch_stage_rows(int corrector, bool top, const Box& b, int nk, const doubl
    }
    const int ni = b.ie - b.ib - 3, nj = b.je - b.jb - 3;
    if (ni <= 0 || nj <= 0) return kOk;
-   const dim3 block(32, 8, 1), grid(blocks_for(ni, 32), blocks_for(nj, 8), 6);
+   const int gx = blocks_for(ni, 32), gy = blocks_for(nj, 8);
+   const dim3 block(32, 8, 1), grid(ctas > 0 ? std::min(ctas, gx * gy * 6) : gx * gy * 6);
    if (rscr) {  // the per-column terms once, then the rows read them
       a.dzc = rscr;
       a.roc = rscr + 18 * b.nij;
-      const int nb = (int)std::min<long long>((b.nij + 127) / 128, 152LL * 16);
+      const int nb = ctas > 0 ? ctas : (int)std::min<long long>((b.nij + 127) / 128, 152LL * 16);
       if (top) rows_pre_kernel<true><<<nb, 128, 0, stream>>>(a, rscr, rscr + 18 * b.nij);
       else rows_pre_kernel<false><<<nb, 128, 0, stream>>>(a, rscr, rscr + 18 * b.nij);
       const int st = launch_status();
@@ -551,11 +560,11 @@ int launch_stage_rows(int corrector, bool top, const Box& b, int nk, const doubl
    }
    const bool pre = rscr != nullptr;
    if (top) {
-      if (pre) stage_rows_kernel<true, false, false, true><<<grid, block, 0, stream>>>(a, w);
-      else stage_rows_kernel<true, false, false, false><<<grid, block, 0, stream>>>(a, w);
+      if (pre) stage_rows_kernel<true, false, false, true><<<grid, block, 0, stream>>>(a, w, gx, gy);
+      else stage_rows_kernel<true, false, false, false><<<grid, block, 0, stream>>>(a, w, gx, gy);
    } else {
-      if (pre) stage_rows_kernel<false, false, false, true><<<grid, block, 0, stream>>>(a, w);
-      else stage_rows_kernel<false, false, false, false><<<grid, block, 0, stream>>>(a, w);
+      if (pre) stage_rows_kernel<false, false, false, true><<<grid, block, 0, stream>>>(a, w, gx, gy);
+      else stage_rows_kernel<false, false, false, false><<<grid, block, 0, stream>>>(a, w, gx, gy);
    }
    return launch_status();
 }
@@ -567,7 +576,7 @@ int launch_stage_rows_df(int corrector, bool top, const Box& b, int nz, const do
                          float* out, const double* rho, const double* irho, double coef,
                          double beta, const double* const dc[3], const double* const st[3],
                          const double* const co[3], const double* zc, cudaStream_t stream,
-                         const double* dd, double* rscr)
+                         const double* dd, double* rscr, int ctas)
 {
    int status = upload_sbp_tables_direct();
    if (status != kOk) return status;
@@ -608,11 +617,12 @@ int launch_stage_rows_df(int corrector, bool top, const Box& b, int nz, const do
    }
    const int ni = b.ie - b.ib - 3, nj = b.je - b.jb - 3;
    if (ni <= 0 || nj <= 0) return kOk;
-   const dim3 block(32, 8, 1), grid(blocks_for(ni, 32), blocks_for(nj, 8), 6);
+   const int gx = blocks_for(ni, 32), gy = blocks_for(nj, 8);
+   const dim3 block(32, 8, 1), grid(ctas > 0 ? std::min(ctas, gx * gy * 6) : gx * gy * 6);
    if (rscr) {  // the per-column terms once, then the rows read them
       a.dzc = rscr;
       a.roc = rscr + 18 * b.nij;
-      const int nb = (int)std::min<long long>((b.nij + 127) / 128, 152LL * 16);
+      const int nb = ctas > 0 ? ctas : (int)std::min<long long>((b.nij + 127) / 128, 152LL * 16);
       if (top) rows_pre_kernel<true><<<nb, 128, 0, stream>>>(a, rscr, rscr + 18 * b.nij);
       else rows_pre_kernel<false><<<nb, 128, 0, stream>>>(a, rscr, rscr + 18 * b.nij);
       const int st = launch_status();
@@ -620,13 +630,13 @@ int launch_stage_rows_df(int corrector, bool top, const Box& b, int nz, const do
    }
    const bool fdf = field_df != nullptr;
    if (top) {
-      if (fdf) stage_rows_kernel<true, true, true, false><<<grid, block, 0, stream>>>(a, w);
-      else if (rscr) stage_rows_kernel<true, true, false, true><<<grid, block, 0, stream>>>(a, w);
-      else stage_rows_kernel<true, true, false, false><<<grid, block, 0, stream>>>(a, w);
+      if (fdf) stage_rows_kernel<true, true, true, false><<<grid, block, 0, stream>>>(a, w, gx, gy);
+      else if (rscr) stage_rows_kernel<true, true, false, true><<<grid, block, 0, stream>>>(a, w, gx, gy);
+      else stage_rows_kernel<true, true, false, false><<<grid, block, 0, stream>>>(a, w, gx, gy);
    } else {
-      if (fdf) stage_rows_kernel<false, true, true, false><<<grid, block, 0, stream>>>(a, w);
-      else if (rscr) stage_rows_kernel<false, true, false, true><<<grid, block, 0, stream>>>(a, w);
-      else stage_rows_kernel<false, true, false, false><<<grid, block, 0, stream>>>(a, w);
+      if (fdf) stage_rows_kernel<false, true, true, false><<<grid, block, 0, stream>>>(a, w, gx, gy);
+      else if (rscr) stage_rows_kernel<false, true, false, true><<<grid, block, 0, stream>>>(a, w, gx, gy);
+      else stage_rows_kernel<false, true, false, false><<<grid, block, 0, stream>>>(a, w, gx, gy);
    }
    return launch_status();
 }
