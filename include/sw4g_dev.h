@@ -33,6 +33,11 @@ int sw4g_dev_set_mixed_tma(int on);
  * rows next to a free surface on a second stream beside each fused stage kernel, 0
  * after it on the object's stream; for all objects of the process. */
 int sw4g_dev_set_rows_overlap(int on);
+/* Comparison switch (no reference counterpart): 1 (the default) lets sw4g_ew_gradient
+ * recompute the next segment beside the current segment's adjoint steps (without CUDA
+ * graphs, with two or more segments kept), 0 runs them one after the other; for all
+ * objects of the process.  Results are the same bits either way. */
+int sw4g_dev_set_adjoint_pipeline(int on);
 /* Tuning (no reference counterpart): the planes per k chunk that the automatic
  * choice gives a stage kernel of `cols` CTA columns over nk planes with `resident`
  * CTAs per SM on the current device's SMs (152 when no device answers), at least

@@ -179,6 +179,7 @@ _SIGS = {
     "sw4g_dev_set_stage_chunks": ([C.c_int], C.c_int),
     "sw4g_dev_set_mixed_tma": ([C.c_int], C.c_int),
     "sw4g_dev_set_rows_overlap": ([C.c_int], C.c_int),
+    "sw4g_dev_set_adjoint_pipeline": ([C.c_int], C.c_int),
     "sw4g_dev_stage_kchunk": ([C.c_longlong, C.c_int, C.c_int, C.c_int, _I], C.c_int),
     "sw4g_geo_default": ([C.POINTER(GeoDesc)], C.c_int),
     "sw4g_geographic_coord": ([C.POINTER(GeoDesc), C.c_double, C.c_double, _D, _D], C.c_int),
@@ -669,6 +670,12 @@ def stage_kchunk(cols, nk, resident, min_planes=12) -> int:
 def set_stage_chunks(chunks=0) -> None:
     """Tuning: k chunks of every stage kernel launch (0: the automatic choice)."""
     check(lib().sw4g_dev_set_stage_chunks(int(chunks)), "set_stage_chunks")
+
+
+def set_adjoint_pipeline(on=True) -> None:
+    """Comparison switch: the gradient's backward sweep recomputes the next segment
+    beside the current one's adjoint steps (default) or after them."""
+    check(lib().sw4g_dev_set_adjoint_pipeline(1 if on else 0), "set_adjoint_pipeline")
 
 
 def set_rows_overlap(on=True) -> None:

@@ -728,7 +728,82 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
       std::vector<AdjGraph> agraphs;
       bool adj_warm = false;
       int status = kOk;
-      for (int sg = nseg - 1; sg >= 0 && status == kOk; sg--) {
+      // Without graphs and with two or more kept segments, the backward sweep is
+      // pipelined: each segment buffer freed by a finished sweep receives the recompute
+      // of the next segment to recompute, on its own stream beside the next sweep (the
+      // recompute's FP64 stages then share the GPU with the sweep's, and the gradient
+      // terms find room beside the predictor-form stages of both).  The same kernels on
+      // the same data in the same order per stream: results are bit-identical.
+      const bool pipelined = !graphs_ && nkept >= 2 && nseg > nkept && adjoint_pipeline_enabled();
+      if (pipelined) {
+         struct Buf {
+            double* sq;
+            double* pq;
+         };
+         std::vector<Buf> bufof(nseg, Buf{nullptr, nullptr});
+         for (int sg = nseg - nkept; sg < nseg; sg++) bufof[sg] = Buf{seg_of(sg), pred_of(sg)};
+         std::vector<cudaEvent_t> ready(nseg, nullptr), swept(nseg, nullptr);
+         cudaStream_t rcs = nullptr;
+         int lo_pr = 0, hi_pr = 0;
+         status = cuda_ok(cudaDeviceGetStreamPriorityRange(&lo_pr, &hi_pr));
+         if (status == kOk) status = cuda_ok(cudaStreamCreateWithPriority(&rcs, cudaStreamNonBlocking, lo_pr));
+         for (int sg = 0; sg < nseg && status == kOk; sg++) {
+            status = cuda_ok(cudaEventCreateWithFlags(&ready[sg], cudaEventDisableTiming));
+            if (status == kOk) status = cuda_ok(cudaEventCreateWithFlags(&swept[sg], cudaEventDisableTiming));
+         }
+         // recompute segment r into buffer bf on rcs (the object's stream swapped for the
+         // enqueue), after the sweep that last used bf
+         auto recompute_into = [&](int r, Buf bf, cudaEvent_t after) -> int {
+            const int r0 = r * ckpt, r1 = std::min(nsteps, r0 + ckpt);
+            SW4G_TRY(cuda_ok(cudaStreamWaitEvent(rcs, after, 0)));
+            cudaStream_t own = stream_;
+            stream_ = rcs;
+            int st2 = kOk;
+            const double* c0 = ck + 2 * (size_t)r * n3;
+            st2 = cuda_ok(cudaMemcpyAsync(bf.sq, c0 + n3, lv, cudaMemcpyDeviceToDevice, stream_));
+            if (st2 == kOk) st2 = cuda_ok(cudaMemcpyAsync(bf.sq + n3, c0, lv, cudaMemcpyDeviceToDevice, stream_));
+            t_ = tseg[r];
+            if (st2 == kOk) st2 = forward_scale(bf.sq, emax + 2 + (nseg - 1 - r));
+            if (st2 == kOk) st2 = steps_into(r0, r1, bf.sq, bf.pq);
+            stage_emax_ = nullptr;
+            if (st2 == kOk) st2 = cuda_ok(cudaEventRecord(ready[r], stream_));
+            stream_ = own;
+            return st2;
+         };
+         int next_rc = nseg - nkept - 1;
+         for (int sg = nseg - 1; sg >= 0 && status == kOk; sg--) {
+            const int s0 = sg * ckpt, s1 = std::min(nsteps, s0 + ckpt);
+            segp = bufof[sg].sq;
+            predp = bufof[sg].pq;
+            status = fork();
+            if (status == kOk && !kept(sg)) status = cuda_ok(cudaStreamWaitEvent(hs, ready[sg], 0));
+            // the forward levels' shift of this segment, from its own slot
+            if (status == kOk && !mixed_)
+               status = cuda_ok(cudaMemcpyAsync(emax + 1, emax + 2 + (nseg - 1 - sg), sizeof(int),
+                                                cudaMemcpyDeviceToDevice, hs));
+            for (int nn = s1 - 1; nn >= s0 && status == kOk; nn--) {
+               status = adj_step(nn, s0, b1, b2, bn, false, nn + 2 <= s1 - 1);
+               rotate();
+            }
+            if (status == kOk) status = flush();
+            if (status == kOk) status = cuda_ok(cudaEventRecord(swept[sg], hs));
+            if (status == kOk && next_rc >= 0) {
+               bufof[next_rc] = bufof[sg];
+               status = recompute_into(next_rc, bufof[sg], swept[sg]);
+               next_rc--;
+            }
+         }
+         if (rcs) {
+            cudaStreamSynchronize(rcs);
+            cudaStreamDestroy(rcs);
+         }
+         cudaStreamSynchronize(hs);
+         for (int sg = 0; sg < nseg; sg++) {
+            if (ready[sg]) cudaEventDestroy(ready[sg]);
+            if (swept[sg]) cudaEventDestroy(swept[sg]);
+         }
+      }
+      for (int sg = nseg - 1; sg >= 0 && status == kOk && !pipelined; sg--) {
          const int s0 = sg * ckpt, s1 = std::min(nsteps, s0 + ckpt);
          const bool full = graphs_ && s1 - s0 == ckpt;
          segp = seg_of(sg);

@@ -810,6 +810,13 @@ int sw4g_dev_set_mixed_tma(int on)
    return SW4G_OK;
 }
 
+int sw4g_dev_set_adjoint_pipeline(int on)
+{
+   if (on != 0 && on != 1) return SW4G_BAD_ARGUMENT;
+   set_adjoint_pipeline(on);
+   return SW4G_OK;
+}
+
 int sw4g_dev_set_rows_overlap(int on)
 {
    if (on != 0 && on != 1) return SW4G_BAD_ARGUMENT;

@@ -327,6 +327,10 @@ int mixed_tma_enabled();
 // stage kernel; 0: after it, on the object's stream
 void set_rows_overlap(int on);
 int rows_overlap_enabled();
+// 1 (the default): the gradient's backward sweep recomputes the next segment beside
+// the current segment's adjoint steps where two or more segments are kept; 0: after it
+void set_adjoint_pipeline(int on);
+int adjoint_pipeline_enabled();
 int launch_df_from_f64(long long n, const double* x, float* h, float* l, cudaStream_t s);
 // FP64 -> interleaved (hi, lo) FP32 pairs
 int launch_df2_from_f64(long long n, const double* x, float2* hl, cudaStream_t s);

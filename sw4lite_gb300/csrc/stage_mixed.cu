@@ -592,6 +592,9 @@ std::atomic<int> g_mixed_tma{1};
 void set_mixed_tma(int on) { g_mixed_tma.store(on ? 1 : 0); }
 int mixed_tma_enabled() { return g_mixed_tma.load(); }
 std::atomic<int> g_rows_overlap{1};
+std::atomic<int> g_adj_pipe{1};
+void set_adjoint_pipeline(int on) { g_adj_pipe.store(on ? 1 : 0); }
+int adjoint_pipeline_enabled() { return g_adj_pipe.load(); }
 void set_rows_overlap(int on) { g_rows_overlap.store(on ? 1 : 0); }
 int rows_overlap_enabled() { return g_rows_overlap.load(); }
 
