@@ -338,6 +338,21 @@ def coef_gradient_fs(bounds, nz, onesided, v, w, h, st, gmu, gla):
                                 C.c_double(h), *[_dp(a) for a in st], _dp(gmu), _dp(gla))
 
 
+def sg6_adjoint(bounds, y, rho, dc, st, co):
+    """SG6^T (y / rho) on the interior (sixth-order damping)."""
+    z = np.zeros_like(y)
+    lib().sw4o_sg6_adjoint(*[C.c_int(b) for b in bounds], _dp(y), _dp(rho), *[_dp(a) for a in dc],
+                           *[_dp(a) for a in st], *[_dp(a) for a in co], _dp(z))
+    return z
+
+
+def sg6_rho_gradient(bounds, a1, d, rho, dc, st, co, beta, grho):
+    """grho += -beta * d/drho [(R a1) . SG6(d)] at fixed R (sixth-order damping)."""
+    lib().sw4o_sg6_rho_gradient(*[C.c_int(b) for b in bounds], _dp(a1), _dp(d), _dp(rho),
+                                *[_dp(a) for a in dc], *[_dp(a) for a in st], *[_dp(a) for a in co],
+                                C.c_double(beta), _dp(grho))
+
+
 def sg_rho_gradient(bounds, a1, d, rho, dc, st, co, beta, grho):
     """grho += -beta * d/drho [(R a1) . SG(d)] at fixed R."""
     lib().sw4o_sg_rho_gradient(*[C.c_int(b) for b in bounds], _dp(a1), _dp(d), _dp(rho),

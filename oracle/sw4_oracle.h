@@ -196,6 +196,16 @@ void sw4o_coef_gradient_fs(int ib, int ie, int jb, int je, int kb, int ke, int n
 void sw4o_apply_lt_fs(int ib, int ie, int jb, int je, int kb, int ke, int nx, int ny, int nz,
                       const int onesided[6], const double* y, const double* mu, const double* la,
                       double h, const double* strx, const double* stry, const double* strz, double* lt);
+/* Sixth-order damping: z = SG6^T (y / rho) on I, and its rho gradient term. */
+void sw4o_sg6_adjoint(int ib, int ie, int jb, int je, int kb, int ke, const double* y,
+                      const double* rho, const double* dcx, const double* dcy, const double* dcz,
+                      const double* strx, const double* stry, const double* strz, const double* cox,
+                      const double* coy, const double* coz, double* z);
+void sw4o_sg6_rho_gradient(int ib, int ie, int jb, int je, int kb, int ke, const double* a1,
+                           const double* d, const double* rho, const double* dcx, const double* dcy,
+                           const double* dcz, const double* strx, const double* stry,
+                           const double* strz, const double* cox, const double* coy,
+                           const double* coz, double beta, double* grho);
 void sw4o_sg_rho_gradient(int ib, int ie, int jb, int je, int kb, int ke, const double* a1,
                           const double* d, const double* rho, const double* dcx, const double* dcy,
                           const double* dcz, const double* strx, const double* stry,

@@ -149,6 +149,116 @@ void sw4o_sg_adjoint(int ib, int ie, int jb, int je, int kb, int ke, const doubl
          }
 }
 
+/* Sixth-order damping (sw4o_addsgd6, src/ew-cfromfort.C:1059-1158), applied at the
+ * points three away from every array edge (the set Q) from u - um anywhere:
+ *   SG6 d = 1/2 P_Q sum_ax diag(w_ax) D3^T E~ D3 d,
+ * D3 the third difference at the half points, E~(q+1/2) = E(q) + E(q+1), E = rho dc.
+ * Its transpose on I applies the same stencil at every point of I to a vector that
+ * is zero outside Q:  SG6^T y = 1/2 P_I sum_ax D3^T E~ D3 P_Q (w_ax y).
+ * T(v, h) below is the third difference of v at the half point h = q + 1/2. */
+static inline int in_q(const abox* b, int i, int j, int k)
+{
+   return i >= b->ib + 3 && i <= b->ie - 3 && j >= b->jb + 3 && j <= b->je - 3 && k >= b->kb + 3 &&
+          k <= b->ke - 3;
+}
+
+/* z = SG6^T (y / rho) on I (zero elsewhere). */
+void sw4o_sg6_adjoint(int ib, int ie, int jb, int je, int kb, int ke, const double* y,
+                      const double* rho, const double* dcx, const double* dcy, const double* dcz,
+                      const double* strx, const double* stry, const double* strz, const double* cox,
+                      const double* coy, const double* coz, double* z)
+{
+   const abox b = mk(ib, ie, jb, je, kb, ke);
+   const double* dcs[3] = {dcx, dcy, dcz};
+   const int lo[3] = {ib, jb, kb};
+   memset(z, 0, 3 * b.npts * sizeof(double));
+   static const double sm[4] = {-1, 3, -3, 1}; /* s_m of the half points p-3/2 .. p+3/2 */
+#pragma omp parallel for collapse(2)
+   for (int k = kb + 2; k <= ke - 2; k++)
+      for (int j = jb + 2; j <= je - 2; j++)
+         for (int i = ib + 2; i <= ie - 2; i++) {
+            const long p = IX(&b, i, j, k);
+            const int pc[3] = {i, j, k};
+            for (int c = 0; c < 3; c++) {
+               double tot = 0;
+               for (int ax = 0; ax < 3; ax++) {
+                  double v[7], e[5];
+                  for (int m = -3; m <= 3; m++) {
+                     int q[3] = {i, j, k};
+                     q[ax] += m;
+                     v[m + 3] = 0;
+                     if (!in_q(&b, q[0], q[1], q[2])) continue;
+                     double w[3];
+                     sg_w(&b, q[0], q[1], q[2], strx, stry, strz, cox, coy, coz, w);
+                     const long qi = IX(&b, q[0], q[1], q[2]);
+                     v[m + 3] = w[ax] * y[c * b.npts + qi] / rho[qi];
+                  }
+                  for (int m = -2; m <= 2; m++) {
+                     int q[3] = {i, j, k};
+                     q[ax] += m;
+                     e[m + 2] = rho[IX(&b, q[0], q[1], q[2])] * dcs[ax][pc[ax] + m - lo[ax]];
+                  }
+                  double s = 0;
+                  for (int m = -2; m <= 1; m++) {
+                     const double t3 = v[m + 5] - 3 * v[m + 4] + 3 * v[m + 3] - v[m + 2];
+                     s += sm[m + 2] * (e[m + 3] + e[m + 2]) * t3;
+                  }
+                  tot += s;
+               }
+               z[c * b.npts + p] = -0.5 * tot;
+            }
+         }
+}
+
+/* rho gradient of the sixth-order damping term: -beta (R a1) . dSG6(d)/drho at fixed
+ * R, added into grho: -beta/2 sum_ax dc(q) [T(v, q-1/2) T(d, q-1/2) + T(v, q+1/2)
+ * T(d, q+1/2)], v = P_Q w_ax a1 / rho along the axis. */
+void sw4o_sg6_rho_gradient(int ib, int ie, int jb, int je, int kb, int ke, const double* a1,
+                           const double* d, const double* rho, const double* dcx, const double* dcy,
+                           const double* dcz, const double* strx, const double* stry,
+                           const double* strz, const double* cox, const double* coy,
+                           const double* coz, double beta, double* grho)
+{
+   const abox b = mk(ib, ie, jb, je, kb, ke);
+   const double* dcs[3] = {dcx, dcy, dcz};
+   const int lo[3] = {ib, jb, kb}, hi[3] = {ie, je, ke};
+#pragma omp parallel for collapse(2)
+   for (int k = kb; k <= ke; k++)
+      for (int j = jb; j <= je; j++)
+         for (int i = ib; i <= ie; i++) {
+            const int pc[3] = {i, j, k};
+            double g = 0;
+            for (int ax = 0; ax < 3; ax++) {
+               const double dcq = dcs[ax][pc[ax] - lo[ax]];
+               if (dcq == 0) continue;
+               for (int c = 0; c < 3; c++) {
+                  /* values at q-2 .. q+2 along the axis */
+                  double vv[5], dd[5];
+                  for (int m = -2; m <= 2; m++) {
+                     int q[3] = {i, j, k};
+                     q[ax] += m;
+                     vv[m + 2] = dd[m + 2] = 0;
+                     if (q[ax] < lo[ax] || q[ax] > hi[ax]) continue;
+                     const long qi = IX(&b, q[0], q[1], q[2]);
+                     dd[m + 2] = d[c * b.npts + qi];
+                     if (in_q(&b, q[0], q[1], q[2])) {
+                        double w[3];
+                        sg_w(&b, q[0], q[1], q[2], strx, stry, strz, cox, coy, coz, w);
+                        vv[m + 2] = w[ax] * a1[c * b.npts + qi] / rho[qi];
+                     }
+                  }
+                  /* third differences at q-1/2 (points q-2..q+1) and q+1/2 (q-1..q+2) */
+                  const double tvm = vv[3] - 3 * vv[2] + 3 * vv[1] - vv[0];
+                  const double tdm = dd[3] - 3 * dd[2] + 3 * dd[1] - dd[0];
+                  const double tvp = vv[4] - 3 * vv[3] + 3 * vv[2] - vv[1];
+                  const double tdp = dd[4] - 3 * dd[3] + 3 * dd[2] - dd[1];
+                  g += dcq * (tvm * tdm + tvp * tdp);
+               }
+            }
+            grho[IX(&b, i, j, k)] -= 0.5 * beta * g;
+         }
+}
+
 /* G(v, w): gradient of v . L(w) with respect to mu and lambda at every array
  * point, added into gmu, gla.  v zero outside I; w zero at ghost points. */
 static const double DW[5] = {1, -8, 0, 8, -1};

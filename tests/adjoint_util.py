@@ -26,11 +26,11 @@ def smooth_random(shape, seed, corr=4.0, amp=0.05):
 
 class AdjointCase:
     def __init__(self, shape=(20, 18, 22), h=0.1, gp=5, seed=3, nsteps=30, nrec=6,
-                 vp=1.8, vs=1.0, rho=1.5, bc=(2,) * 6, rec_k=None):
+                 vp=1.8, vs=1.0, rho=1.5, bc=(2,) * 6, rec_k=None, sg_order=4, damping=0.02):
         self.nx, self.ny, self.nz = shape
         nx, ny, nz = shape
         self.h = h
-        self.grid = sg.grid_desc(nx, ny, nz, h, bc=bc, sg_gp=gp, sg_damping=0.02)
+        self.grid = sg.grid_desc(nx, ny, nz, h, bc=bc, sg_gp=gp, sg_damping=damping, sg_order=sg_order)
         arr = (nz + 4, ny + 4, nx + 4)
         r = rho * smooth_random(arr, seed)
         cs = vs * smooth_random(arr, seed + 1)
@@ -133,8 +133,9 @@ def oracle_gradient(case: AdjointCase, obs):
         cg(a1 * R3 * (dt * dt / 12), w1)
         cg(m * R3 * (dt * dt), u)
         gr -= ((m * w1 + a1 * (unew - up)).reshape(3, -1).sum(0)) / rho
-        O.sg_rho_gradient(bounds, a1, u - um, rho, dc, st, co, beta, gr)
-        an = g_of(step) + 2 * m + dt * dt * t - dt * dt / 6 * s - a2 - beta * O.sg_adjoint(
-            bounds, a1 - a2, rho, dc, st, co)
+        six = case.grid.sg_order == 6
+        (O.sg6_rho_gradient if six else O.sg_rho_gradient)(bounds, a1, u - um, rho, dc, st, co, beta, gr)
+        an = g_of(step) + 2 * m + dt * dt * t - dt * dt / 6 * s - a2 - beta * (
+            O.sg6_adjoint if six else O.sg_adjoint)(bounds, a1 - a2, rho, dc, st, co)
         a2, a1 = a1, an
     return J, gr, gm, gl

@@ -210,3 +210,53 @@ def test_oracle_gradient_fs_matches_finite_differences(which, bc, rec_k):
     fd = (Jp - Jm) / (2 * eps)
     assert abs(pred) > 0
     assert abs(fd - pred) <= 1e-6 * abs(pred), (fd, pred)
+
+
+# ---- sixth-order damping ----
+
+def test_sg6_adjoint_dot_product():
+    c = AdjointCase(sg_order=6, damping=0.005)
+    dc, st, co = _profiles(c)
+    rho = c.mat[0]
+    x, y = _rand_interior(c, 31), _rand_interior(c, 32)
+    up = np.zeros_like(x)
+    # sw4o_addsgd6: up += beta/(2 rho) (...) = -beta R SG6(u - um), on the points three
+    # away from the array edges
+    O.addsgd(6, 1, _bounds(c), up, x, np.zeros_like(x), rho, dc, st, co, 1.0)
+    lhs = -float(up @ y)                                          # <R SG6 x, y>
+    rhs = float(x @ O.sg6_adjoint(_bounds(c), y, rho, dc, st, co))  # <x, SG6^T R y>
+    assert abs(lhs - rhs) <= 1e-13 * abs(lhs)
+    assert np.max(np.abs(np.array(dc[0]))) > 0  # damping layers are present
+
+
+def test_sg6_rho_gradient_identity():
+    c = AdjointCase(shape=(14, 13, 15), sg_order=6, damping=0.005)
+    dc, st, co = _profiles(c)
+    rho = c.mat[0]
+    a1, d = _rand_interior(c, 33), _rand_interior(c, 34)
+    g = np.zeros(c.npts)
+    O.sg6_rho_gradient(_bounds(c), a1, d, rho, dc, st, co, 0.005, g)
+    up = np.zeros_like(d)
+    O.addsgd(6, 1, _bounds(c), up, d, np.zeros_like(d), rho, dc, st, co, 0.005)
+    # -beta (R a1).SG6(d) is linear in rho through E = rho dc at fixed R
+    assert float(rho @ g) == pytest.approx(float(a1 @ up), rel=1e-12)
+
+
+@pytest.mark.parametrize("which", ["rho", "all"])
+def test_oracle_gradient_sg6_matches_finite_differences(which):
+    kw = dict(sg_order=6, damping=0.005)
+    c = AdjointCase(**kw)
+    obs_case = AdjointCase(seed=11, **kw)
+    obs = obs_case.records(oracle_forward(obs_case)[0][1:])
+    J, gr, gm, gl = oracle_gradient(c, obs)
+    shape = (c.nz + 4, c.ny + 4, c.nx + 4)
+    dirs = [smooth_random(shape, 90 + q, corr=3.0, amp=0.3).reshape(-1) - 1.0 for q in range(3)]
+    keep = {"rho": (0,), "all": (0, 1, 2)}[which]
+    dm = [dirs[q] * c.mat[q] if q in keep else np.zeros(c.npts) for q in range(3)]
+    pred = float(gr @ dm[0] + gm @ dm[1] + gl @ dm[2])
+    eps = 1e-5
+    Jp = misfit(c, oracle_forward(c, [c.mat[q] + eps * dm[q] for q in range(3)])[0], obs)
+    Jm = misfit(c, oracle_forward(c, [c.mat[q] - eps * dm[q] for q in range(3)])[0], obs)
+    fd = (Jp - Jm) / (2 * eps)
+    assert abs(pred) > 0
+    assert abs(fd - pred) <= 1e-6 * abs(pred), (fd, pred)
