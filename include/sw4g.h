@@ -344,8 +344,8 @@ int sw4g_ew_status(sw4g_ew* ew);
  * checkpoint_every steps.  Device memory: (2*ceil(nsteps/C) + 2*C + 19) levels of
  * 3*npts doubles, plus the segments kept from the forward run (below).  Requires
  * Dirichlet or supergrid sides (zero ghost data) or free-surface z sides (with the z
- * stretching 1 and no z damping on the ten planes next to them, nz >= 22), 4th-order
- * damping, no topography.  Receivers may share a grid point.
+ * stretching 1 and no z damping on the ten planes next to them, nz >= 22), 4th- or
+ * 6th-order damping, no topography.  Receivers may share a grid point.
  * The object ends at the end of the forward run.  It keeps that device memory for its
  * next gradient of the same nsteps, checkpoint interval and receivers; a failed call,
  * sw4g_ew_set_gradient_memory and sw4g_ew_destroy release it. */

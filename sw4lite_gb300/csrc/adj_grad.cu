@@ -507,7 +507,13 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
                    o2 = a2 == 0 ? off[0] : a2 == 1 ? off[1] : off[2];
          const bool inner = x0 - 2 >= xl && x0 + 2 <= xh;
          const float2 bd = t == 0 ? __ldg(g.bdc[a] + oa) : make_float2(0.f, 0.f);
-         const bool damp = t == 0 && x0 - 1 >= xl && x0 + 1 <= xh && bd.x != 0.f;
+         const bool damp = t == 0 && !g.sg6 && x0 - 1 >= xl && x0 + 1 <= xh && bd.x != 0.f;
+         // sixth order: b1 is taken as zero outside the points three from every edge
+         // (the damping's rows), so the other two coordinates must lie there
+         const bool damp6 = t == 0 && g.sg6 && bd.x != 0.f && off[a1] >= 3 &&
+                            (a1 == 0 ? b.ie - b.ib : a1 == 1 ? b.je - b.jb : b.ke - b.kb) - off[a1] >= 3 &&
+                            off[a2] >= 3 &&
+                            (a2 == 0 ? b.ie - b.ib : a2 == 1 ? b.je - b.jb : b.ke - b.kb) - off[a2] >= 3;
          V ds = N::zero();
 #pragma unroll
          for (int c = 0; c < 3; c++) {
@@ -550,10 +556,27 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
                                       df_pow2(N::of(__ldg(b1 + p)), -2.f));
                ds = df_addf(ds, df_mul(d2u, d2b));
             }
+            if (damp6) {  // T(b1) T(u - um) at the half points x0 -+ 1/2
+               const typename N::S* __restrict__ um = arr<V>(g.dum) + c * n;
+               const typename N::S* __restrict__ b1 = arr<V>(g.db1) + c * n;
+               V bb[5], dd[5];
+#pragma unroll
+               for (int m = 0; m < 5; m++) {
+                  const int xm = x0 + m - 2;
+                  const long long q = p + (long long)(m - 2) * sd;
+                  const bool in = xm >= xl && xm <= xh;
+                  dd[m] = in ? df_diff(N::of(__ldg(F + q)), N::of(__ldg(um + q))) : N::zero();
+                  bb[m] = xm >= xl + 3 && xm <= xh - 3 ? N::of(__ldg(b1 + q)) : N::zero();
+               }
+               // T = (a3 - a0) + 3 (a1 - a2) over four consecutive values a0..a3
+               auto T3 = [](const V* v) { return df_addf(df_diff(v[3], v[0]), df_scale(df_diff(v[1], v[2]), 3.f)); };
+               ds = df_addf(ds, df_addf(df_mul(T3(bb), T3(dd)), df_mul(T3(bb + 1), T3(dd + 1))));
+            }
          }
-         if (damp) {
+         if (damp || damp6) {
             const V cc = df_mul(N::ofp(__ldg(g.cist[a1] + o1)), N::ofp(__ldg(g.cist[a2] + o2)));
-            gr = df_addf(gr, df_neg(df_mul(df_mul(N::ofp(bd), cc), ds)));
+            const V term = df_mul(df_mul(N::ofp(bd), cc), ds);
+            gr = df_addf(gr, df_neg(damp6 ? df_pow2(term, 0.5f) : term));
          }
       }
       // mixed terms, grouped by the axis t3 that neither derivative takes:

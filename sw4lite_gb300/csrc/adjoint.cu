@@ -131,7 +131,7 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
    if (!ready_ || !material_ || !(dt_ > 0) || nsteps < 1 || ckpt < 1 || !obs || !misfit || !g_rho ||
        !g_mu || !g_la)
       return kBadArgument;
-   if (cv_ || g_.sg_order != 4) return kNotSupported;
+   if (cv_ || (g_.sg_order != 4 && g_.sg_order != 6)) return kNotSupported;
    for (int s = 0; s < 6; s++)
       if (g_.bc[s] != kDirichlet && g_.bc[s] != kSuperGrid && !(s >= 4 && g_.bc[s] == kStressFree))
          return kNotSupported;
@@ -375,6 +375,12 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
    }
    if (fs_top) gd.zlo = 6;
    if (fs_bot) gd.zhi = g_.nz - 5;
+   gd.sg6 = g_.sg_order == 6;
+   // sixth order: the stages carry no damping; the transposed damping pass follows
+   const double beta4 = g_.sg_order == 4 ? beta : 0.0, beta6 = g_.sg_order == 6 ? beta : 0.0;
+   const double* dcp6[3] = {dprof_[0], dprof_[1], dprof_[2]};
+   const double* stp6[3] = {dprof_[3], dprof_[4], dprof_[5]};
+   const double* cop6[3] = {dprof_[6], dprof_[7], dprof_[8]};
    GradRows gw;  // the one-sided rows' gradient terms
    gw.b = b;
    gw.nz = g_.nz;
@@ -620,9 +626,15 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
             m.um = CF(b2);
             m.up = CF(mtb);
             m.out = F(bn);
-            m.beta = beta;
+            m.beta = beta4;
             if (status == kOk) status = launch_mixed_stage(m, sa);
-            if (status == kOk) status = adj_rows(2, mtb, b1, b2, bn, dt * dt, beta, sa);
+            if (status == kOk) status = adj_rows(2, mtb, b1, b2, bn, dt * dt, beta4, sa);
+            if (status == kOk && beta6 != 0) {
+               const float* dc32[3] = {prof32_[0], prof32_[1], prof32_[2]};
+               const float* st32[3] = {prof32_[3], prof32_[4], prof32_[5]};
+               const float* co32[3] = {prof32_[6], prof32_[7], prof32_[8]};
+               status = launch_addsgd6_df(3, b, F(bn), CF(b1), CF(b2), rho32_, dc32, st32, co32, beta6, sa, 1);
+            }
             if (status == kOk) {
                adj_source_df_kernel<<<blocks_for(rg.n, 64), 64, 0, sa>>>(b, pf, rg, drec_.ijk, res, rho_, hz,
                                                                          F(bn), clk, nval);
@@ -674,11 +686,13 @@ int EW::gradient(int nsteps, int ckpt, const double* obs, bool obs_on_device, do
                fs.um = b2;
                fs.up = mtb;
                fs.out = bn;
-               fs.beta = beta;
+               fs.beta = beta4;
                fs.coef = dt * dt;
                status = launch_fused_stage(fs, sa);
             }
-            if (status == kOk) status = adj_rows(2, mtb, b1, b2, bn, dt * dt, beta, sa);
+            if (status == kOk) status = adj_rows(2, mtb, b1, b2, bn, dt * dt, beta4, sa);
+            if (status == kOk && beta6 != 0)
+               status = launch_addsgd6_adj(b, bn, b1, b2, rho_, dcp6, stp6, cop6, beta6, sa);
             if (status == kOk) {
                adj_source_kernel<<<blocks_for(rg.n, 64), 64, 0, sa>>>(b, pf, rg, drec_.ijk, res, rho_, hz, bn,
                                                                      clk, nval);

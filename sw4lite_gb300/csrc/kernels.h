@@ -296,7 +296,14 @@ int launch_addsgd6c(const Box& b, double* up, const double* u, const double* um,
                     cudaStream_t s);
 int launch_addsgd6_df(int naxes, const Box& b, float* out, const float* u, const float* um,
                       const float* e, const float* const dc[3], const float* const st[3],
-                      const float* const co[3], double beta, cudaStream_t s);
+                      const float* const co[3], double beta, cudaStream_t s, int adj = 0);
+// The transpose of the Cartesian sixth-order damping on the interior points (the
+// adjoint's scaled recursion): every point two from the array edges, u - um taken as
+// zero outside the points three from every edge; FP64.  The double-float form is
+// launch_addsgd6_df with adj = 1.
+int launch_addsgd6_adj(const Box& b, double* up, const double* u, const double* um, const double* rho,
+                       const double* const dc[3], const double* const st[3], const double* const co[3],
+                       double beta, cudaStream_t s);
 int launch_rho_jac_f32(long long n, const double* rho, const double* jac, float* e, cudaStream_t s);
 
 // Halo planes of a decomposed grid (halo.cu): the first of the two planes a side
@@ -410,6 +417,7 @@ struct GradDF {
    // free-surface z sides: the one-sided rows' planes k <= zlo, k >= zhi, whose adjoint
    // values the z-involving terms skip (grad_rows covers them)
    int zlo = -(1 << 29), zhi = 1 << 29;
+   int sg6 = 0;  // sixth-order damping: its rho term from third differences at half points
 };
 // The z-involving gradient terms of the six one-sided rows next to a free-surface z
 // side (top: rows 1..6, bottom: nz-5..nz), FP64, added to the FP64 gradients gm, gl:

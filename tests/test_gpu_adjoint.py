@@ -37,7 +37,8 @@ def _ew(case, mat=None, precision=sg.FP64):
     g = case.grid
     if precision != sg.FP64:
         g = sg.grid_desc(case.nx, case.ny, case.nz, case.h, bc=[g.bc[s] for s in range(6)],
-                         sg_gp=g.sg_gp, sg_damping=g.sg_damping, precision=precision)
+                         sg_gp=g.sg_gp, sg_damping=g.sg_damping, sg_order=g.sg_order,
+                         precision=precision)
     ew = sg.EW(g)
     ew.set_material(*[dev(a) for a in mat])
     for s in case.sources:
@@ -296,6 +297,39 @@ def test_fs_mixed_gradient_close_to_fp64(bc, rec_k):
     obs = obs_case.records(oracle_forward(obs_case)[0][1:])
     J0, g0, _ = _gpu_gradient(c, obs, 10)
     J1, g1, _ = _gpu_gradient(c, obs, 10, precision=sg.MIXED)
+    assert J1 == pytest.approx(J0, rel=1e-6)
+    for a, b in zip(g1, g0):
+        assert _rel(a, b) <= 1e-5, _rel(a, b)
+
+
+# ---- sixth-order supergrid damping ----
+# 12 steps: with these 5-point layers the sixth-order scheme has a mode that grows
+# without bound after a few tens of steps (the reference formulation too).
+
+@pytest.mark.parametrize("bc,rec_k,shape", [((2,) * 6, None, (20, 18, 22)),
+                                            ((2, 2, 2, 2, 0, 2), 1, (16, 15, 24))])
+@pytest.mark.parametrize("ckpt,memory", [(12, None), (5, 0)])
+def test_sg6_gradient_matches_oracle_adjoint(bc, rec_k, shape, ckpt, memory):
+    kw = dict(shape=shape, bc=bc, rec_k=rec_k, sg_order=6, damping=0.005, nsteps=12)
+    c = AdjointCase(**kw)
+    obs_case = AdjointCase(seed=11, **kw)
+    obs = obs_case.records(oracle_forward(obs_case)[0][1:])
+    J0, gr, gm, gl = oracle_gradient(c, obs)
+    J, (r, m, l), _ = _gpu_gradient(c, obs, ckpt, memory=memory)
+    assert J == pytest.approx(J0, rel=1e-12)
+    assert _rel(r, gr) <= 1e-9
+    assert _rel(m, gm) <= 1e-9
+    assert _rel(l, gl) <= 1e-9
+
+
+def test_sg6_mixed_gradient_close_to_fp64():
+    kw = dict(sg_order=6, damping=0.005, nsteps=12)
+    c = AdjointCase(**kw)
+    obs_case = AdjointCase(seed=11, **kw)
+    obs = obs_case.records(oracle_forward(obs_case)[0][1:])
+    J0, g0, _ = _gpu_gradient(c, obs, 4)
+    J1, g1, _ = _gpu_gradient(c, obs, 4, precision=sg.MIXED)
+    assert np.all(np.isfinite(g0[2])) and J0 < 10  # the physical solution, not the growing mode
     assert J1 == pytest.approx(J0, rel=1e-6)
     for a, b in zip(g1, g0):
         assert _rel(a, b) <= 1e-5, _rel(a, b)

@@ -213,9 +213,13 @@ def test_oracle_gradient_fs_matches_finite_differences(which, bc, rec_k):
 
 
 # ---- sixth-order damping ----
+# The small cases' 5-point supergrid layers with sixth-order damping let a mode grow
+# without bound after a few tens of steps (the reference formulation does the same);
+# the runs below stop at 12 steps, while the solution is still the physical one.
+SG6 = dict(sg_order=6, damping=0.005, nsteps=12)
 
 def test_sg6_adjoint_dot_product():
-    c = AdjointCase(sg_order=6, damping=0.005)
+    c = AdjointCase(**SG6)
     dc, st, co = _profiles(c)
     rho = c.mat[0]
     x, y = _rand_interior(c, 31), _rand_interior(c, 32)
@@ -230,7 +234,7 @@ def test_sg6_adjoint_dot_product():
 
 
 def test_sg6_rho_gradient_identity():
-    c = AdjointCase(shape=(14, 13, 15), sg_order=6, damping=0.005)
+    c = AdjointCase(shape=(14, 13, 15), **SG6)
     dc, st, co = _profiles(c)
     rho = c.mat[0]
     a1, d = _rand_interior(c, 33), _rand_interior(c, 34)
@@ -244,7 +248,7 @@ def test_sg6_rho_gradient_identity():
 
 @pytest.mark.parametrize("which", ["rho", "all"])
 def test_oracle_gradient_sg6_matches_finite_differences(which):
-    kw = dict(sg_order=6, damping=0.005)
+    kw = dict(SG6)
     c = AdjointCase(**kw)
     obs_case = AdjointCase(seed=11, **kw)
     obs = obs_case.records(oracle_forward(obs_case)[0][1:])
