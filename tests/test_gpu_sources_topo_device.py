@@ -165,3 +165,36 @@ def test_device_path_keeps_the_host_refusals():
     ew.add_source(sg.source_desc(1.0, 1.0, 0.5, force=(1.0, 0, 0)))  # in the curvilinear grid
     assert len(ew.grid_point_sources(1)[0]) > 0 and len(ew.grid_point_sources(0)[0]) == 0
     ew.close()
+
+
+def test_mixed_run_with_device_lists_matches_host_lists():
+    """The FP32-mixed two-grid loop forces with the same source sets: a run with the
+    device lists against a run with the host lists, to 1e-12 of the field maximum (the
+    lists themselves differ at most in the last bits of exp/pow)."""
+    c = _case()
+    srcs = _sources(c, seed=4, n=8)
+    dt = c.time_step(1.3)
+    fields = smooth_topo_fields(c, seed=5)
+    g = sg.grid_desc(c.nx, c.ny, c.ncart, c.h, bc=c.bc, zmin=c.zmax_topo, sg_gp=c.grid.sg_gp,
+                     sg_damping=c.grid.sg_damping, precision=sg.MIXED)
+    out = []
+    for on_device in (False, True):
+        ew = sg.EW(g, topo=sg.topo_desc(**c.hill))
+        ew.set_material(*[dev(a) for a in c.cart_mat])
+        ew.set_material_grid(1, *[dev(a) for a in c.curv_mat])
+        if on_device:
+            ew.set_source_discretization(True)
+        for s in srcs:
+            ew.add_source(s)
+        ew.set_time_step(dt, 0.0)
+        ew.set_fields(dev(fields[0]), dev(fields[1]))
+        ew.set_fields_grid(1, dev(fields[2]), dev(fields[3]))
+        ew.step(10, sg.MODE_FUSED)
+        r = [dev(np.zeros_like(f)) for f in fields[::2]]
+        ew.get_fields(r[0], None)
+        ew.get_fields_grid(1, r[1], None)
+        out.append([host(x) for x in r])
+        ew.close()
+    for x, y in zip(*out):
+        assert np.all(np.isfinite(x))
+        assert np.max(np.abs(x - y)) <= 1e-12 * np.max(np.abs(y))
