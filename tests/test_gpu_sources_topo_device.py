@@ -168,9 +168,10 @@ def test_device_path_keeps_the_host_refusals():
 
 
 def test_mixed_run_with_device_lists_matches_host_lists():
-    """The FP32-mixed two-grid loop forces with the same source sets: a run with the
-    device lists against a run with the host lists, to 1e-12 of the field maximum (the
-    lists themselves differ at most in the last bits of exp/pow)."""
+    """The FP32-mixed two-grid loop with the device lists against the host lists.  The
+    lists differ at most in the last bits of exp/pow, but such a difference can flip
+    an FP32 rounding in the stencil, so the runs agree to the mixed form's own
+    scale: 1e-7 of the field maximum after 10 steps."""
     c = _case()
     srcs = _sources(c, seed=4, n=8)
     dt = c.time_step(1.3)
@@ -197,4 +198,4 @@ def test_mixed_run_with_device_lists_matches_host_lists():
         ew.close()
     for x, y in zip(*out):
         assert np.all(np.isfinite(x))
-        assert np.max(np.abs(x - y)) <= 1e-12 * np.max(np.abs(y))
+        assert np.max(np.abs(x - y)) <= 1e-7 * np.max(np.abs(y))
