@@ -420,25 +420,28 @@ int curv_coef_df_setup(long long npts, const CurvCoef& c, float* store, CurvCoef
    return launch_status();
 }
 
-int launch_curv_stage_df(const CurvStageDF& st, cudaStream_t s)
+int launch_curv_stage_df(const CurvStageDF& st, cudaStream_t s, int part, int ctas)
 {
    const Box& b = st.b;
    const int corr = st.corrector;
    if (!st.work1 || (corr && !st.work2)) return kBadArgument;
-   // FP64 slabs of the top rows' stage field (and u - um) over planes kb..8
-   CurvStageDF t = st;
-   t.fbox = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, 8);
-   t.f = st.work1;
-   if (corr) {
-      SW4G_TRY(launch_uacc_slab_df(b, b.kb, 8, st.up, st.u, st.um, st.work1, s));
-      SW4G_TRY(launch_df_slab(b, b.kb, 8, st.u, st.um, st.work2, s));
-      t.dd = st.work2;
-   } else {
-      SW4G_TRY(launch_df_slab(b, b.kb, 8, st.u, nullptr, st.work1, s));
+   if (part != 2) {
+      // FP64 slabs of the top rows' stage field (and u - um) over planes kb..8
+      CurvStageDF t = st;
+      t.fbox = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, 8);
+      t.f = st.work1;
+      if (corr) {
+         SW4G_TRY(launch_uacc_slab_df(b, b.kb, 8, st.up, st.u, st.um, st.work1, s));
+         SW4G_TRY(launch_df_slab(b, b.kb, 8, st.u, st.um, st.work2, s));
+         t.dd = st.work2;
+      } else {
+         SW4G_TRY(launch_df_slab(b, b.kb, 8, st.u, nullptr, st.work1, s));
+      }
+      // the ghost shell, then the SBP top rows k = 1..6 in FP64
+      SW4G_TRY(launch_ghost_shell_df(b, corr, st.out, st.u, st.um, st.up, s));
+      SW4G_TRY(launch_curv_top_df(t, s, ctas));
    }
-   // the ghost shell, then the SBP top rows k = 1..6 in FP64
-   SW4G_TRY(launch_ghost_shell_df(b, corr, st.out, st.u, st.um, st.up, s));
-   SW4G_TRY(launch_curv_top_df(t, s));
+   if (part == 1) return kOk;
    MArgs a;
    a.b = b;
    a.u = st.u;

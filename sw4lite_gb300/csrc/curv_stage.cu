@@ -584,14 +584,10 @@ __global__ void __launch_bounds__(128) curv_top_pre_kernel(Box b, Box fb, SF f, 
 // coefficients, with the stage update (and the corrector's x/y damping) fused.
 // FP64 throughout; the levels are FP64 or double-float (RD, WR).
 template <int CORR, class RD, class WR, class SF>
-__global__ void __launch_bounds__(128) curv_top_kernel(TopArgs<RD, WR, SF> a)
+__device__ __forceinline__ void curv_top_point(const TopArgs<RD, WR, SF>& a, int i, int j, int k)
 {
    const Box& b = a.b;
    const Box& fb = a.fb;
-   const int i = b.ib + 2 + blockIdx.x * blockDim.x + threadIdx.x;
-   const int j = b.jb + 2 + blockIdx.y * blockDim.y + threadIdx.y;
-   const int k = 1 + blockIdx.z;
-   if (i > b.ie - 2 || j > b.je - 2) return;
    const long long n = b.npts, ncol = b.nij;
    const long long p = pidx(b, i, j, k), col = pidx(b, i, j, b.kb);
    auto F = [&](int c, int ii, int jj, int kk) { return a.f.get(c * fb.npts + pidx(fb, ii, jj, kk)); };
@@ -737,6 +733,20 @@ __global__ void __launch_bounds__(128) curv_top_kernel(TopArgs<RD, WR, SF> a)
    }
 }
 
+// The gx x gy x 6 blocks of 32 x 4 points, strided over by the grid (one CTA per
+// block, or a persistent grid beside the stage kernels).
+template <int CORR, class RD, class WR, class SF>
+__global__ void __launch_bounds__(128) curv_top_kernel(TopArgs<RD, WR, SF> a, int gx, int gy)
+{
+   const int nvb = gx * gy * 6;
+   for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+      const int i = a.b.ib + 2 + (vb % gx) * blockDim.x + threadIdx.x;
+      const int j = a.b.jb + 2 + ((vb / gx) % gy) * blockDim.y + threadIdx.y;
+      if (i > a.b.ie - 2 || j > a.b.je - 2) continue;
+      curv_top_point<CORR>(a, i, j, 1 + vb / (gx * gy));
+   }
+}
+
 int gsb(long long n, int threads = 256)
 {
    long long b = (n + threads - 1) / threads;
@@ -745,7 +755,8 @@ int gsb(long long n, int threads = 256)
 }
 
 template <int CORR, class RD, class WR, class SF, class ST>
-int launch_top(const ST& st, RD u, RD um, RD up, WR out, SF f, cudaStream_t s, const double* dd = nullptr)
+int launch_top(const ST& st, RD u, RD um, RD up, WR out, SF f, cudaStream_t s, const double* dd = nullptr,
+               int ctas = 0)
 {
    const Box& b = st.b;
    TopArgs<RD, WR, SF> t;
@@ -770,12 +781,13 @@ int launch_top(const ST& st, RD u, RD um, RD up, WR out, SF f, cudaStream_t s, c
    t.coef = CORR ? st.dt * st.dt / 12 : st.dt * st.dt;
    t.beta = st.beta;
    if (!st.scratch) return kBadArgument;
-   curv_top_pre_kernel<<<gsb(b.nij, 128), 128, 0, s>>>(b, st.fbox, f, st.cc, st.sx, st.sy, st.scratch,
-                                                       st.scratch + 18 * b.nij);
+   curv_top_pre_kernel<<<ctas > 0 ? ctas : gsb(b.nij, 128), 128, 0, s>>>(b, st.fbox, f, st.cc, st.sx, st.sy,
+                                                                         st.scratch, st.scratch + 18 * b.nij);
    SW4G_TRY(launch_status());
    const int ni = b.ie - b.ib - 3, nj = b.je - b.jb - 3;
-   const dim3 blk(32, 4), g((ni + 31) / 32, (nj + 3) / 4, 6);
-   curv_top_kernel<CORR><<<g, blk, 0, s>>>(t);
+   const int gx = (ni + 31) / 32, gy = (nj + 3) / 4;
+   const dim3 blk(32, 4), g(ctas > 0 ? std::min(ctas, gx * gy * 6) : gx * gy * 6);
+   curv_top_kernel<CORR><<<g, blk, 0, s>>>(t, gx, gy);
    return launch_status();
 }
 
@@ -805,7 +817,7 @@ int curv_coef_setup(const Box& b, const double* mu, const double* la, const doub
    return launch_status();
 }
 
-int launch_curv_top_df(const CurvStageDF& st, cudaStream_t s)
+int launch_curv_top_df(const CurvStageDF& st, cudaStream_t s, int ctas)
 {
    // the stage field (and the corrector's u - um) come as FP64 slabs over planes
    // kb..8: converting each double-float value once there keeps the float-to-double
@@ -814,12 +826,12 @@ int launch_curv_top_df(const CurvStageDF& st, cudaStream_t s)
    if (!st.f) return kBadArgument;
    if (st.corrector)
       return launch_top<1>(st, RdDF{st.u, lo}, RdDF{st.um, lo}, RdDF{st.up, lo}, DFField{st.out, lo},
-                           RdF64{st.f}, s, st.dd);
+                           RdF64{st.f}, s, st.dd, ctas);
    return launch_top<0>(st, RdDF{st.u, lo}, RdDF{st.um, lo}, RdDF{nullptr, lo}, DFField{st.out, lo},
-                        RdF64{st.f}, s);
+                        RdF64{st.f}, s, nullptr, ctas);
 }
 
-int launch_curv_stage(const CurvStage& st, cudaStream_t s)
+int launch_curv_stage(const CurvStage& st, cudaStream_t s, int part, int ctas)
 {
    const Box& b = st.b;
    StageArgs a;
@@ -838,15 +850,20 @@ int launch_curv_stage(const CurvStage& st, cudaStream_t s)
    a.beta = st.beta;
    const int corr = st.corrector;
    a.coef = corr ? st.dt * st.dt / 12 : st.dt * st.dt;
-   // the ghost shell
-   if (corr) curv_shell_kernel<1><<<gsb(b.npts), 256, 0, s>>>(b, st.nz, st.u, st.um, st.up, st.out);
-   else curv_shell_kernel<0><<<gsb(b.npts), 256, 0, s>>>(b, st.nz, st.u, st.um, st.up, st.out);
-   SW4G_TRY(launch_status());
-   // the SBP top rows k = 1..6
-   if (corr)
-      SW4G_TRY(launch_top<1>(st, RdF64{st.u}, RdF64{st.um}, RdF64{st.up}, F64Field{st.out}, RdF64{st.f}, s));
-   else
-      SW4G_TRY(launch_top<0>(st, RdF64{st.u}, RdF64{st.um}, RdF64{nullptr}, F64Field{st.out}, RdF64{st.f}, s));
+   if (part != 2) {
+      // the ghost shell
+      if (corr) curv_shell_kernel<1><<<gsb(b.npts), 256, 0, s>>>(b, st.nz, st.u, st.um, st.up, st.out);
+      else curv_shell_kernel<0><<<gsb(b.npts), 256, 0, s>>>(b, st.nz, st.u, st.um, st.up, st.out);
+      SW4G_TRY(launch_status());
+      // the SBP top rows k = 1..6
+      if (corr)
+         SW4G_TRY(launch_top<1>(st, RdF64{st.u}, RdF64{st.um}, RdF64{st.up}, F64Field{st.out}, RdF64{st.f}, s,
+                                nullptr, ctas));
+      else
+         SW4G_TRY(launch_top<0>(st, RdF64{st.u}, RdF64{st.um}, RdF64{nullptr}, F64Field{st.out}, RdF64{st.f}, s,
+                                nullptr, ctas));
+   }
+   if (part == 1) return kOk;
    a.coef = corr ? st.dt * st.dt / 12 : st.dt * st.dt;
    a.k1 = 7;
    a.k2 = st.nz;

@@ -152,7 +152,7 @@ int EW::init()
    if (cv_) SW4G_TRY(init_topo());
    SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
    // the rows' second stream, made here rather than inside a graph capture
-   if (onesided_[4] || onesided_[5]) SW4G_TRY(side_stream());
+   if (onesided_[4] || onesided_[5] || cv_) SW4G_TRY(side_stream());
    ready_ = true;
    return kOk;
 }
@@ -1067,30 +1067,38 @@ int EW::step_fused()
    // with 6th-order damping, whose pass in piece 4 covers every plane.
    const bool beta6 = g_.sg_order == 6 && prof_.used && g_.sg_damping != 0;
    const bool beside = rows_overlap_enabled() && (onesided_[4] || onesided_[5]) && !beta6;
+   // With topography the curvilinear grid's top rows (its free surface, FP64) run
+   // beside both grids' stage kernels in the same way, forked at the start of each
+   // stage; its 6th-order damping pass and forcing follow the join.
+   const bool cbeside = rows_overlap_enabled() && cv_ != nullptr;
    for (int which = 0; which < 6; which++) {
       if (beside && (which == 1 || which == 4)) continue;
-      if (beside && (which == 0 || which == 3)) {
-         // fork point before the stage, stage first, then the rows, then the join
+      if ((beside || cbeside) && (which == 0 || which == 3)) {
+         // fork point before the stages, stages first, then the rows, then the join
          SW4G_TRY(side_stream());
          SW4G_TRY(cuda_ok(cudaEventRecord(ev_fork_, stream_)));
          SW4G_TRY(piece(which, ip, iq));
+         if (cbeside) SW4G_TRY(which == 0 ? curv_pred_part(ip, 2, stream_, 0) : curv_corr_part(ip, iq, 2, stream_, 0));
          SW4G_TRY(cuda_ok(cudaStreamWaitEvent(side_, ev_fork_, 0)));
          cudaStream_t own = stream_;
          stream_ = side_;
          rows_ctas_ = mixed_ ? sms_ : 0;
-         const int st = piece(which + 1, ip, iq);
+         int st = beside ? piece(which + 1, ip, iq) : kOk;
+         if (st == kOk && cbeside)
+            st = which == 0 ? curv_pred_part(ip, 1, side_, rows_ctas_) : curv_corr_part(ip, iq, 1, side_, rows_ctas_);
          rows_ctas_ = 0;
          stream_ = own;
          SW4G_TRY(st);
          SW4G_TRY(cuda_ok(cudaEventRecord(ev_join_, side_)));
          SW4G_TRY(cuda_ok(cudaStreamWaitEvent(stream_, ev_join_, 0)));
+         if (cbeside) SW4G_TRY(which == 0 ? curv_pred_part(ip, 3, stream_, 0) : curv_corr_part(ip, iq, 3, stream_, 0));
       } else {
          SW4G_TRY(piece(which, ip, iq));
       }
       if (!cv_) continue;
-      if (which == 0) SW4G_TRY(curv_pred(ip));
+      if (which == 0 && !cbeside) SW4G_TRY(curv_pred(ip));
       if (which == 2) SW4G_TRY(curv_bc(lev_[ip], cv_->lev[ip]));
-      if (which == 3) SW4G_TRY(curv_corr(ip, iq));
+      if (which == 3 && !cbeside) SW4G_TRY(curv_corr(ip, iq));
       if (which == 5) SW4G_TRY(curv_bc(lev_[iq], cv_->lev[iq]));
    }
    if (drec_.n > 0) SW4G_TRY(record(lev_[iq], lev_[ium_], 0));

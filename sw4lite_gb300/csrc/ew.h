@@ -324,6 +324,8 @@ class EW {
    int sms_ = 0;        // the device's SM count
    int rows_ctas_ = 0;  // > 0 while the rows run beside a stage: a persistent grid
    int side_stream();
+   int curv_pred_part(int ip, int part, cudaStream_t s, int ctas);
+   int curv_corr_part(int ip, int iq, int part, cudaStream_t s, int ctas);
    double* dclock_ = nullptr;  // [0] forcing time, [1] record row, [2] adjoint residual row
    struct GraphKey {
       int iu, ium, rec;

@@ -300,34 +300,44 @@ CurvStageDF curv_stage_args_df(const CurvGrid& c, double* const dprof[9], float*
 float* df(double* p) { return reinterpret_cast<float*>(p); }
 }  // namespace
 
-int EW::curv_pred(int ip)
+int EW::curv_pred(int ip) { return curv_pred_part(ip, 0, stream_, 0); }
+
+// The curvilinear predictor in parts: 1 the ghost shell and the SBP top rows (on
+// stream s, as a persistent grid of ctas CTAs when ctas > 0), 2 the stage kernel of
+// rows 7..nz, 3 the forcing after both; 0 all three on the object's stream.
+int EW::curv_pred_part(int ip, int part, cudaStream_t s, int ctas)
 {
+   CurvGrid& c = *cv_;
+   if (part == 3) return curv_force(c.lev[ip], 0, dt_ * dt_);
+   const int lp = part == 0 ? 0 : part;  // the launcher's part
    if (mixed_) {
-      CurvGrid& c = *cv_;
       CurvStageDF st = curv_stage_args_df(c, dprof_, prof32_, dt_, 0.0);
       st.corrector = 0;
       st.u = df(c.lev[iu_]);
       st.um = df(c.lev[ium_]);
       st.out = df(c.lev[ip]);
       st.work1 = c.uacc;
-      SW4G_TRY(launch_curv_stage_df(st, stream_));
-      return curv_force(c.lev[ip], 0, dt_ * dt_);
+      SW4G_TRY(launch_curv_stage_df(st, part == 1 ? s : stream_, lp, ctas));
+   } else {
+      // fused: the stage kernel (rows 7..nz), the top-row kernel (rows 1..6) and the
+      // ghost shell
+      CurvStage st = curv_stage_args(c, dprof_, dt_, 0.0);
+      st.corrector = 0;
+      st.u = c.lev[iu_];
+      st.um = c.lev[ium_];
+      st.out = c.lev[ip];
+      st.f = c.lev[iu_];
+      st.fbox = st.b;
+      SW4G_TRY(launch_curv_stage(st, part == 1 ? s : stream_, lp, ctas));
    }
-   // fused: the stage kernel (rows 7..nz), the top-row kernel (rows 1..6) and the
-   // ghost shell
-   CurvGrid& c = *cv_;
-   CurvStage st = curv_stage_args(c, dprof_, dt_, 0.0);
-   st.corrector = 0;
-   st.u = c.lev[iu_];
-   st.um = c.lev[ium_];
-   st.out = c.lev[ip];
-   st.f = c.lev[iu_];
-   st.fbox = st.b;
-   SW4G_TRY(launch_curv_stage(st, stream_));
-   return curv_force(c.lev[ip], 0, dt_ * dt_);
+   return part == 0 ? curv_force(c.lev[ip], 0, dt_ * dt_) : kOk;
 }
 
-int EW::curv_corr(int ip, int iq)
+int EW::curv_corr(int ip, int iq) { return curv_corr_part(ip, iq, 0, stream_, 0); }
+
+// The curvilinear corrector in parts as the predictor's (the parts apply to the
+// fused form, ip != iq; part 3: the 6th-order damping pass and the forcing).
+int EW::curv_corr_part(int ip, int iq, int part, cudaStream_t s, int ctas)
 {
    CurvGrid& c = *cv_;
    const Bounds& b = c.b;
@@ -337,15 +347,18 @@ int EW::curv_corr(int ip, int iq)
    const Box cbox = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke);
    if (mixed_) {
       if (ip == iq) return kNotSupported;
-      CurvStageDF st = curv_stage_args_df(c, dprof_, prof32_, dt, beta4);
-      st.corrector = 1;
-      st.up = df(c.lev[ip]);
-      st.u = df(c.lev[iu_]);
-      st.um = df(c.lev[ium_]);
-      st.out = df(c.lev[iq]);
-      st.work1 = c.uacc;
-      st.work2 = c.lu;
-      SW4G_TRY(launch_curv_stage_df(st, stream_));
+      if (part != 3) {
+         CurvStageDF st = curv_stage_args_df(c, dprof_, prof32_, dt, beta4);
+         st.corrector = 1;
+         st.up = df(c.lev[ip]);
+         st.u = df(c.lev[iu_]);
+         st.um = df(c.lev[ium_]);
+         st.out = df(c.lev[iq]);
+         st.work1 = c.uacc;
+         st.work2 = c.lu;
+         SW4G_TRY(launch_curv_stage_df(st, part == 1 ? s : stream_, part, ctas));
+         if (part != 0) return kOk;
+      }
       if (beta != 0 && g_.sg_order == 6) {
          if (!c.rhoj32) {
             SW4G_TRY(cuda_ok(cudaMalloc(&c.rhoj32, c.npts * sizeof(float))));
@@ -366,17 +379,23 @@ int EW::curv_corr(int ip, int iq)
    if (ip != iq) {
       // fused: the corrector reads level ip and writes level iq; the top rows read
       // up - 2u + um from a slab of planes kb..8
-      const Box full = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke);
-      SW4G_TRY(launch_uacc_slab(full, b.kb, 8, c.lev[ip], c.lev[iu_], c.lev[ium_], c.uacc, stream_));
-      CurvStage st = curv_stage_args(c, dprof_, dt, beta4);
-      st.corrector = 1;
-      st.up = c.lev[ip];
-      st.u = c.lev[iu_];
-      st.um = c.lev[ium_];
-      st.out = c.lev[iq];
-      st.f = c.uacc;
-      st.fbox = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, 8);
-      SW4G_TRY(launch_curv_stage(st, stream_));
+      if (part != 3) {
+         cudaStream_t rs = part == 1 ? s : stream_;
+         if (part != 2) {
+            const Box full = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, b.ke);
+            SW4G_TRY(launch_uacc_slab(full, b.kb, 8, c.lev[ip], c.lev[iu_], c.lev[ium_], c.uacc, rs));
+         }
+         CurvStage st = curv_stage_args(c, dprof_, dt, beta4);
+         st.corrector = 1;
+         st.up = c.lev[ip];
+         st.u = c.lev[iu_];
+         st.um = c.lev[ium_];
+         st.out = c.lev[iq];
+         st.f = c.uacc;
+         st.fbox = make_box(1, b.ib, b.ie, b.jb, b.je, b.kb, 8);
+         SW4G_TRY(launch_curv_stage(st, rs, part, ctas));
+         if (part != 0) return kOk;
+      }
       if (beta != 0 && g_.sg_order == 6)
          SW4G_TRY(launch_addsgd6c(cbox, c.lev[iq], c.lev[iu_], c.lev[ium_], c.rho, dprof_[0], dprof_[1],
                                   dprof_[3], dprof_[4], c.jac, dprof_[6], dprof_[7], beta, stream_));

@@ -163,7 +163,10 @@ struct CurvStage {
    double* scratch = nullptr;
    double dt = 0, beta = 0;
 };
-int launch_curv_stage(const CurvStage& st, cudaStream_t s);
+// part 0: the whole stage; 1: the ghost shell and the SBP top rows k = 1..6 alone (with
+// ctas > 0 the top rows as a persistent grid of that many CTAs); 2: the stage kernel
+// of rows 7..nz alone.  Parts 1 and 2 write disjoint points from the same inputs.
+int launch_curv_stage(const CurvStage& st, cudaStream_t s, int part = 0, int ctas = 0);
 
 // The curvilinear coefficients of the FP32-mixed stage as (hi, lo) FP32 pairs:
 // products 0..7 as CurvCoef::prod, 8 = (2mu+la) m2 m1, 9 = (2mu+la) m3 m1; the
@@ -206,8 +209,8 @@ struct CurvStageDF {
    double* scratch = nullptr;
    double dt = 0, beta = 0;
 };
-int launch_curv_stage_df(const CurvStageDF& st, cudaStream_t s);
-int launch_curv_top_df(const CurvStageDF& st, cudaStream_t s);
+int launch_curv_stage_df(const CurvStageDF& st, cudaStream_t s, int part = 0, int ctas = 0);
+int launch_curv_top_df(const CurvStageDF& st, cudaStream_t s, int ctas = 0);
 int launch_freesurfcurvisg_df(const CurvSpec& s, int nz, int side, const double* sbop, float* uh,
                               cudaStream_t st);
 int launch_cart_topo_df(const Box& cart, const Box& curv, int nzc, float* ucart, float* ucurv,

@@ -92,3 +92,44 @@ def test_rows_beside_the_stage_match_rows_after_it(precision, graphs):
     sg.set_rows_overlap(True)
     assert np.array_equal(out[0], out[1])
     assert np.max(np.abs(out[0])) > 0
+
+
+@pytest.mark.parametrize("precision", [sg.FP64, sg.MIXED])
+@pytest.mark.parametrize("graphs", [False, True])
+def test_curvilinear_rows_beside_the_stages_match(precision, graphs):
+    """With topography the curvilinear grid's top rows run on a second stream beside
+    both grids' stage kernels: the levels of both grids after a run are bit-identical
+    to running every piece in order on the object's stream."""
+    import torch
+    from tests.gpu_util import dev, host
+    from tests.topo_util import TopoCase, smooth_topo_fields
+    c = TopoCase(30, 28, 22, 0.1, zmax_topo=1.0, amp=0.2, xc=1.4, yc=1.3, lx=0.6, ly=0.5, gp=5,
+                 sources=[sg.source_desc(1.5, 1.4, 0.6, force=(1.0, -0.5, 0.3), freq=8.0, t0=0.1)],
+                 precision=precision)
+    dt = c.time_step(1.3)
+    fields = smooth_topo_fields(c, seed=7)
+    out = []
+    for on in (True, False):
+        sg.set_rows_overlap(on)
+        s = torch.cuda.Stream()
+        ew = sg.EW(c.grid, stream=s, topo=sg.topo_desc(**c.hill))
+        ew.set_material(*[dev(a) for a in c.cart_mat])
+        ew.set_material_grid(1, *[dev(a) for a in c.curv_mat])
+        for src in c.sources:
+            ew.add_source(src)
+        ew.set_time_step(dt, 0.0)
+        ew.set_fields(dev(fields[0]), dev(fields[1]))
+        ew.set_fields_grid(1, dev(fields[2]), dev(fields[3]))
+        if graphs:
+            ew.set_graphs(True)
+        ew.step(6, sg.MODE_FUSED)
+        r = [dev(np.zeros_like(f)) for f in fields[::2]]
+        ew.get_fields(r[0], None)
+        ew.get_fields_grid(1, r[1], None)
+        torch.cuda.synchronize()
+        out.append([host(x) for x in r])
+        ew.close()
+    sg.set_rows_overlap(True)
+    for x, y in zip(*out):
+        assert np.array_equal(x, y)
+        assert np.max(np.abs(x)) > 0
