@@ -433,7 +433,9 @@ __device__ __forceinline__ void first_diffs(const V x[5], const V y[5], bool inn
 
 // the mu, lambda and damping rho sums of one point from the edge sums, the centred
 // first differences and the damping's second differences
-template <class V>
+// SG6: sixth-order damping's rho term; ZM: free-surface sides (the one-sided rows'
+// masks).  Both are template parameters so the common case carries neither.
+template <class V, bool SG6, bool ZM>
 __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
 {
    using N = Num<V>;
@@ -507,10 +509,10 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
                    o2 = a2 == 0 ? off[0] : a2 == 1 ? off[1] : off[2];
          const bool inner = x0 - 2 >= xl && x0 + 2 <= xh;
          const float2 bd = t == 0 ? __ldg(g.bdc[a] + oa) : make_float2(0.f, 0.f);
-         const bool damp = t == 0 && !g.sg6 && x0 - 1 >= xl && x0 + 1 <= xh && bd.x != 0.f;
+         const bool damp = t == 0 && !SG6 && x0 - 1 >= xl && x0 + 1 <= xh && bd.x != 0.f;
          // sixth order: b1 is taken as zero outside the points three from every edge
          // (the damping's rows), so the other two coordinates must lie there
-         const bool damp6 = t == 0 && g.sg6 && bd.x != 0.f && off[a1] >= 3 &&
+         const bool damp6 = SG6 && t == 0 && bd.x != 0.f && off[a1] >= 3 &&
                             (a1 == 0 ? b.ie - b.ib : a1 == 1 ? b.je - b.jb : b.ke - b.kb) - off[a1] >= 3 &&
                             off[a2] >= 3 &&
                             (a2 == 0 ? b.ie - b.ib : a2 == 1 ? b.je - b.jb : b.ke - b.kb) - off[a2] >= 3;
@@ -536,7 +538,7 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
                   y[m] = ok ? N::of(__ldg(F + p + (m - 2) * sd)) : N::zero();
                }
             }
-            if (a == 2 && (x0 - 2 <= g.zlo || x0 + 2 >= g.zhi)) {
+            if (ZM && a == 2 && (x0 - 2 <= g.zlo || x0 + 2 >= g.zhi)) {
 #pragma unroll
                for (int m = 0; m < 5; m++)
                   if (m != 2 && !zrow(g, x0 + m - 2)) x[m] = N::zero();
@@ -556,7 +558,7 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
                                       df_pow2(N::of(__ldg(b1 + p)), -2.f));
                ds = df_addf(ds, df_mul(d2u, d2b));
             }
-            if (damp6) {  // T(b1) T(u - um) at the half points x0 -+ 1/2
+            if (SG6 && damp6) {  // T(b1) T(u - um) at the half points x0 -+ 1/2
                const typename N::S* __restrict__ um = arr<V>(g.dum) + c * n;
                const typename N::S* __restrict__ b1 = arr<V>(g.db1) + c * n;
                V bb[5], dd[5];
@@ -586,7 +588,7 @@ __global__ void __launch_bounds__(kGradThreads) grad_df_kernel(GradDF g)
          const int a1 = t3 == 2 ? 0 : t3 + 1, a2 = t3 == 0 ? 2 : t3 - 1;
          // the terms with a z derivative skip the one-sided rows' adjoint values: the
          // in-plane first differences of a one-sided row's plane drop out of them
-         const bool zoff = t3 != 2 && !zrow(g, pc[2]);
+         const bool zoff = ZM && t3 != 2 && !zrow(g, pc[2]);
          auto A_ = [&](int c, int a) { return zoff && a != 2 ? N::zero() : N::of(fd[c * 3 + a][tid]); };
          auto W_ = [&](int c, int a) { return N::of(fd[9 + c * 3 + a][tid]); };
          const V ml = df_addf(df_mul(W_(a2, a2), A_(a1, a1)), df_mul(W_(a1, a1), A_(a2, a2)));
@@ -816,6 +818,16 @@ __global__ void __launch_bounds__(256) grad_flush_kernel(long long n, float2* __
    }
 }
 
+template <class V>
+void launch_df_kernel(const GradDF& g, dim3 grid, cudaStream_t s)
+{
+   const bool zm = g.zlo > -(1 << 28) || g.zhi < (1 << 28);
+   if (g.sg6 && zm) grad_df_kernel<V, true, true><<<grid, kGradThreads, 0, s>>>(g);
+   else if (g.sg6) grad_df_kernel<V, true, false><<<grid, kGradThreads, 0, s>>>(g);
+   else if (zm) grad_df_kernel<V, false, true><<<grid, kGradThreads, 0, s>>>(g);
+   else grad_df_kernel<V, false, false><<<grid, kGradThreads, 0, s>>>(g);
+}
+
 int grid_stride_blocks(long long n, int threads)
 {
    long long b = (n + threads - 1) / threads;
@@ -859,7 +871,7 @@ int launch_grad_df_step(const GradDF& g, cudaStream_t s)
    SW4G_TRY(launch_status());
    grad_edge_kernel<DF><<<grid, kGradThreads, 0, s>>>(g);
    SW4G_TRY(launch_status());
-   grad_df_kernel<DF><<<grid, kGradThreads, 0, s>>>(g);
+   launch_df_kernel<DF>(g, grid, s);
    return launch_status();
 }
 
@@ -871,7 +883,7 @@ int launch_grad_f1_step(const GradDF& g, cudaStream_t s)
    SW4G_TRY(launch_status());
    grad_edge_kernel<F1><<<grid, kGradThreads, 0, s>>>(g);
    SW4G_TRY(launch_status());
-   grad_df_kernel<F1><<<grid, kGradThreads, 0, s>>>(g);
+   launch_df_kernel<F1>(g, grid, s);
    return launch_status();
 }
 
