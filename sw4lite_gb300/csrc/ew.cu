@@ -592,7 +592,7 @@ int EW::status()
 }
 
 // Scans the current level of every grid (the level the last step wrote) for NaN and
-// infinite values and reads the verdict: kNanDetected with nan_ filled in, kTimeout
+// infinite values and reads the outcome: kNanDetected with nan_ filled in, kTimeout
 // if a kernel's bounded wait gave up, else kOk.
 int EW::scan_levels()
 {

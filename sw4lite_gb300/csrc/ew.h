@@ -209,7 +209,7 @@ class EW {
    // discretise one source into hsrc_ (on the global grid for a subdomain, keeping
    // the entries on this subdomain's interior points)
    void discretize_into(const SourceSpec& s, std::vector<GridPointSource>& out) const;
-   int scan_levels();                 // non-finite scans of the current levels, then the verdict
+   int scan_levels();                 // non-finite scans of the current levels, then the outcome
    int read_status(unsigned long long out[4]);
    int record(double* up, double* um, int initial);
    int step_phases();
