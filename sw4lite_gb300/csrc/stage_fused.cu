@@ -156,6 +156,57 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
       }
    };
 
+   // Predictor: the next plane and the next material plane are loaded into registers
+   // before the current plane's arithmetic and stored after it, so their global-load
+   // latency overlaps the arithmetic (the corrector's three levels would not fit in
+   // the registers its 2 CTAs per SM leave).
+   constexpr int kPre = (PLANE + NTHREADS - 1) / NTHREADS;  // values per thread
+   double pv[kPre][3], pm[kPre][2];
+   auto prefetch_plane = [&](int kk) {
+#pragma unroll
+      for (int r = 0; r < kPre; r++) {
+         const int idx = tid + r * NTHREADS;
+         const int li = idx % PX, lj = idx / PX;
+         const int gi = i0 - HALO + li, gj = j0 - HALO + lj;
+         const bool ok = idx < PLANE && gi <= a.ie && gj <= a.je;
+         const long long p = ok ? gidx(gi, gj, kk) : 0;
+#pragma unroll
+         for (int c = 0; c < 3; c++) pv[r][c] = ok ? __ldg(a.u + p + c * npts) : 0.0;
+      }
+   };
+   auto store_plane = [&](int kk) {
+      double* vs = V + mod5(kk) * 3 * PLANE;
+#pragma unroll
+      for (int r = 0; r < kPre; r++) {
+         const int idx = tid + r * NTHREADS;
+         if (idx < PLANE)
+#pragma unroll
+            for (int c = 0; c < 3; c++) vs[c * PLANE + idx] = pv[r][c];
+      }
+   };
+   auto prefetch_material = [&](int kk) {
+#pragma unroll
+      for (int r = 0; r < kPre; r++) {
+         const int idx = tid + r * NTHREADS;
+         const int li = idx % PX, lj = idx / PX;
+         const int gi = i0 - HALO + li, gj = j0 - HALO + lj;
+         const bool ok = idx < PLANE && gi <= a.ie && gj <= a.je;
+         const long long p = ok ? gidx(gi, gj, kk) : 0;
+         pm[r][0] = ok ? __ldg(a.mu + p) : 0.0;
+         pm[r][1] = ok ? __ldg(a.la + p) : 0.0;
+      }
+   };
+   auto store_material = [&]() {
+#pragma unroll
+      for (int r = 0; r < kPre; r++) {
+         const int idx = tid + r * NTHREADS;
+         if (idx < PLANE) {
+            MU[idx] = pm[r][0];
+            LA[idx] = pm[r][1];
+         }
+      }
+   };
+
    // Own-column stretching factors
    const double sxi = active ? __ldg(a.sx + (i - a.ib)) : 0.0;
    const double syj = active ? __ldg(a.sy + (j - a.jb)) : 0.0;
@@ -204,10 +255,24 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
    }
 
    int em = 0;  // the largest exponent field written (a.emax)
+   if (CORR == 0) {
+      prefetch_plane(kbeg + 2);
+      prefetch_material(kbeg);
+   }
    for (int k = kbeg; k <= kend; k++) {
-      load_plane(k + 2);
-      load_material(k);
+      if (CORR == 0) {
+         store_plane(k + 2);
+         store_material();
+      } else {
+         load_plane(k + 2);
+         load_material(k);
+      }
       __syncthreads();
+      // planes up to kend + 2 are read (kend + 2 <= the last array plane)
+      if (CORR == 0 && k < kend) {
+         prefetch_plane(k + 3);
+         prefetch_material(k + 1);
+      }
 
       // shift the register queues and append plane k+2
 #pragma unroll
