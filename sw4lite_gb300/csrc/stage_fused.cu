@@ -156,12 +156,13 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
       }
    };
 
-   // Predictor: the next plane and the next material plane are loaded into registers
-   // before the current plane's arithmetic and stored after it, so their global-load
-   // latency overlaps the arithmetic (the corrector's three levels would not fit in
-   // the registers its 2 CTAs per SM leave).
+   // The next plane (the stage field, and the corrector's u - um) and the next material
+   // plane are loaded into registers before the current plane's arithmetic and stored
+   // at the start of the next iteration, so their global-load latency overlaps the
+   // arithmetic.  The corrector and adjoint forms spill a little to fit this in the
+   // 128 registers of 2 CTAs per SM; measured a small net gain.
    constexpr int kPre = (PLANE + NTHREADS - 1) / NTHREADS;  // values per thread
-   double pv[kPre][3], pm[kPre][2];
+   double pv[kPre][3], pm[kPre][2], pd[kPre][3];
    auto prefetch_plane = [&](int kk) {
 #pragma unroll
       for (int r = 0; r < kPre; r++) {
@@ -171,17 +172,30 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
          const bool ok = idx < PLANE && gi <= a.ie && gj <= a.je;
          const long long p = ok ? gidx(gi, gj, kk) : 0;
 #pragma unroll
-         for (int c = 0; c < 3; c++) pv[r][c] = ok ? __ldg(a.u + p + c * npts) : 0.0;
+         for (int c = 0; c < 3; c++) {
+            if (CORR == 0) {
+               pv[r][c] = ok ? __ldg(a.u + p + c * npts) : 0.0;
+            } else {
+               const double uu = ok ? __ldg(a.u + p + c * npts) : 0.0, uum = ok ? __ldg(a.um + p + c * npts) : 0.0;
+               const double upp = ok ? __ldg(a.up + p + c * npts) : 0.0;
+               pv[r][c] = CORR == 1 ? (upp - 2 * uu) + uum : upp;
+               pd[r][c] = uu - uum;
+            }
+         }
       }
    };
    auto store_plane = [&](int kk) {
       double* vs = V + mod5(kk) * 3 * PLANE;
+      double* ds = Dd + mod3(kk) * 3 * PLANE;
 #pragma unroll
       for (int r = 0; r < kPre; r++) {
          const int idx = tid + r * NTHREADS;
          if (idx < PLANE)
 #pragma unroll
-            for (int c = 0; c < 3; c++) vs[c * PLANE + idx] = pv[r][c];
+            for (int c = 0; c < 3; c++) {
+               vs[c * PLANE + idx] = pv[r][c];
+               if (CORR) ds[c * PLANE + idx] = pd[r][c];
+            }
       }
    };
    auto prefetch_material = [&](int kk) {
@@ -196,6 +210,17 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
          pm[r][1] = ok ? __ldg(a.la + p) : 0.0;
       }
    };
+   double prh[kPre];
+   auto prefetch_rho = [&](int kk) {
+#pragma unroll
+      for (int r = 0; r < kPre; r++) {
+         const int idx = tid + r * NTHREADS;
+         const int li = idx % PX, lj = idx / PX;
+         const int gi = i0 - HALO + li, gj = j0 - HALO + lj;
+         const bool ok = idx < PLANE && gi <= a.ie && gj <= a.je;
+         prh[r] = ok ? __ldg(a.rho + gidx(gi, gj, kk)) : 0.0;
+      }
+   };
    auto store_material = [&]() {
 #pragma unroll
       for (int r = 0; r < kPre; r++) {
@@ -203,6 +228,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
          if (idx < PLANE) {
             MU[idx] = pm[r][0];
             LA[idx] = pm[r][1];
+            if (CORR) RH[idx] = prh[r];
          }
       }
    };
@@ -255,23 +281,18 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
    }
 
    int em = 0;  // the largest exponent field written (a.emax)
-   if (CORR == 0) {
-      prefetch_plane(kbeg + 2);
-      prefetch_material(kbeg);
-   }
+   prefetch_plane(kbeg + 2);
+   prefetch_material(kbeg);
+   if (CORR) prefetch_rho(kbeg);
    for (int k = kbeg; k <= kend; k++) {
-      if (CORR == 0) {
-         store_plane(k + 2);
-         store_material();
-      } else {
-         load_plane(k + 2);
-         load_material(k);
-      }
+      store_plane(k + 2);
+      store_material();
       __syncthreads();
       // planes up to kend + 2 are read (kend + 2 <= the last array plane)
-      if (CORR == 0 && k < kend) {
+      if (k < kend) {
          prefetch_plane(k + 3);
          prefetch_material(k + 1);
+         if (CORR) prefetch_rho(k + 1);
       }
 
       // shift the register queues and append plane k+2
