@@ -483,6 +483,26 @@ int sw4g_nearest_grid_point(const sw4g_grid* g, double x, double y, double z, in
  * receiver order.  A step that would overflow the array returns SW4G_BAD_ARGUMENT
  * before doing anything.  n = 0 removes the receivers. */
 int sw4g_ew_set_receivers(sw4g_ew* ew, int n, const int* ijk, const int* mode, int capacity);
+/* As sw4g_ew_set_receivers, each receiver on grid grid[r]: 0 the Cartesian grid, 1 the
+ * curvilinear grid of an object with topography (grid may be NULL: all on grid 0).
+ * On the curvilinear grid the derivative modes use the metric at the receiver's
+ * point as the reference's curvilinear branches of EW::extractRecordData
+ * (src/EW.C:5882-6068). */
+int sw4g_ew_set_receivers_grid(sw4g_ew* ew, int n, const int* ijk, const int* mode, const int* grid,
+                               int capacity);
+/* The grid point (ijk, 1-based) and grid of a receiver at (x, y, z) on this object's
+ * grids: EW::computeNearestGridPoint (src/EW.C:5149-5213) with TimeSeries' placement on
+ * the curvilinear grid (src/TimeSeries.C:139-168, :307-329): (i, j) nearest, a point
+ * half-way going to the lower index; below the interface (z > zmin) the Cartesian k;
+ * at or above it the curvilinear k = round(s) of the inverted grid mapping, limited to
+ * 1..nz, or 1 where the mapping cannot be inverted.  SW4G_BAD_ARGUMENT above the
+ * topography (allowance 1e-9) or outside the grids; SW4G_NOT_SUPPORTED on a
+ * subdomain object. */
+int sw4g_ew_nearest_grid_point(const sw4g_ew* ew, double x, double y, double z, int* ijk, int* grid);
+/* z of the topography surface at (x, y), 0 without topography: a receiver or source
+ * given by its depth below the surface lies at z = depth + this (the reference's
+ * topodepth, src/TimeSeries.C:145-150; EW::find_topo_zcoord_owner, src/EW.C:6311). */
+int sw4g_ew_topography_z(const sw4g_ew* ew, double x, double y, double* z);
 /* rows written so far and values per row */
 int sw4g_ew_record_shape(const sw4g_ew* ew, int* rows, int* nvals);
 /* copies rows x nvals doubles (row-major) to host (on_device=0) or device memory */

@@ -172,6 +172,9 @@ _SIGS = {
     "sw4g_nearest_grid_point": ([C.POINTER(GridDesc), C.c_double, C.c_double, C.c_double, _I],
                                 C.c_int),
     "sw4g_ew_set_receivers": ([_VP, C.c_int, _I, _I, C.c_int], C.c_int),
+    "sw4g_ew_set_receivers_grid": ([_VP, C.c_int, _I, _I, _I, C.c_int], C.c_int),
+    "sw4g_ew_nearest_grid_point": ([_VP, C.c_double, C.c_double, C.c_double, _I, _I], C.c_int),
+    "sw4g_ew_topography_z": ([_VP, C.c_double, C.c_double, C.POINTER(C.c_double)], C.c_int),
     "sw4g_ew_record_shape": ([_VP, _I, _I], C.c_int),
     "sw4g_ew_get_records": ([_VP, _VP, C.c_int], C.c_int),
     "sw4g_ew_launches_per_step": ([_VP, C.c_int], C.c_int),
@@ -528,17 +531,39 @@ class EW:
             check(lib().sw4g_ew_curvilinear_arrays(self._h, p(z), p(met), p(jac), on_dev),
                   "curvilinear_arrays")
 
-    def set_receivers(self, ijk, modes, capacity):
+    def set_receivers(self, ijk, modes, capacity, grids=None):
         """Receivers at 1-based grid points ijk (n x 3) with record modes (REC_*);
-        room for `capacity` record rows (initial data + one per step)."""
+        room for `capacity` record rows (initial data + one per step).  grids: per
+        receiver 0 (Cartesian, the default) or 1 (the curvilinear grid)."""
         import numpy as np
         ijk = np.ascontiguousarray(np.asarray(ijk, dtype=np.int32).reshape(-1, 3))
         modes = np.ascontiguousarray(np.asarray(modes, dtype=np.int32).reshape(-1))
         n = len(modes)
         if ijk.shape[0] != n:
             raise Sw4gError("set_receivers: one mode per receiver")
-        check(lib().sw4g_ew_set_receivers(self._h, n, ijk.ctypes.data_as(_I),
-                                          modes.ctypes.data_as(_I), capacity), "set_receivers")
+        if grids is None:
+            check(lib().sw4g_ew_set_receivers(self._h, n, ijk.ctypes.data_as(_I),
+                                              modes.ctypes.data_as(_I), capacity), "set_receivers")
+            return
+        grids = np.ascontiguousarray(np.asarray(grids, dtype=np.int32).reshape(-1))
+        if len(grids) != n:
+            raise Sw4gError("set_receivers: one grid per receiver")
+        check(lib().sw4g_ew_set_receivers_grid(self._h, n, ijk.ctypes.data_as(_I),
+                                               modes.ctypes.data_as(_I), grids.ctypes.data_as(_I),
+                                               capacity), "set_receivers")
+
+    def nearest_grid_point(self, x, y, z):
+        """((i, j, k), grid) of the grid point nearest to (x, y, z) on this object's
+        grids (grid 1: the curvilinear grid)."""
+        ijk, g = (C.c_int * 3)(), C.c_int()
+        check(lib().sw4g_ew_nearest_grid_point(self._h, x, y, z, ijk, C.byref(g)), "nearest_grid_point")
+        return tuple(ijk), g.value
+
+    def topography_z(self, x, y):
+        """z of the topography surface at (x, y) (0 without topography)."""
+        z = C.c_double()
+        check(lib().sw4g_ew_topography_z(self._h, x, y, C.byref(z)), "topography_z")
+        return z.value
 
     def record_shape(self):
         rows, nvals = C.c_int(), C.c_int()

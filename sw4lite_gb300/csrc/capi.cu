@@ -696,6 +696,24 @@ int sw4g_ew_set_receivers(sw4g_ew* ew, int n, const int* ijk, const int* mode, i
    return ew ? ew->impl->set_receivers(n, ijk, mode, capacity) : SW4G_BAD_ARGUMENT;
 }
 
+int sw4g_ew_set_receivers_grid(sw4g_ew* ew, int n, const int* ijk, const int* mode, const int* grid,
+                               int capacity)
+{
+   return ew ? ew->impl->set_receivers(n, ijk, mode, capacity, grid) : SW4G_BAD_ARGUMENT;
+}
+
+int sw4g_ew_nearest_grid_point(const sw4g_ew* ew, double x, double y, double z, int* ijk, int* grid)
+{
+   return ew ? ew->impl->nearest_grid_point(x, y, z, ijk, grid) : SW4G_BAD_ARGUMENT;
+}
+
+int sw4g_ew_topography_z(const sw4g_ew* ew, double x, double y, double* z)
+{
+   if (!ew || !z) return SW4G_BAD_ARGUMENT;
+   *z = ew->impl->topography_z(x, y);
+   return SW4G_OK;
+}
+
 int sw4g_ew_record_shape(const sw4g_ew* ew, int* rows, int* nvals)
 {
    return ew ? ew->impl->record_shape(rows, nvals) : SW4G_BAD_ARGUMENT;

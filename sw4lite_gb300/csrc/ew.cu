@@ -545,7 +545,7 @@ int EW::step(int nsteps, int mode)
    SW4G_TRY(upload_sources());
    if (mode == kModePhases) SW4G_TRY(ensure_phase_arrays());
    if (drec_.n > 0 && rec_initial_) {
-      SW4G_TRY(record(lev_[iu_], lev_[ium_], 1));
+      SW4G_TRY(record(iu_, ium_, 1));
       rec_initial_ = false;
    }
    auto advance = [&](int k) -> int {
@@ -625,19 +625,28 @@ int EW::scan_levels()
    return kNanDetected;
 }
 
-int EW::record(double* up, double* um, int initial)
+int EW::record(int iup, int ium, int initial)
 {
    // with the device clock the kernel takes its row from clock[1]
    const double* clk = clocked_ ? dclock_ : nullptr;
    double* row = clk ? records_ : records_ + (size_t)rec_rows_ * rec_nvals_;
+   RecCurv rc;
+   if (rec_curv_) {
+      const Bounds& cb = cv_->b;
+      rc.b = make_box(1, cb.ib, cb.ie, cb.jb, cb.je, cb.kb, cb.ke);
+      rc.up = cv_->lev[iup];
+      rc.um = cv_->lev[ium];
+      rc.met = cv_->met;
+      rc.jac = cv_->jac;
+   }
+   const Box b = make_box(1, b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke);
    if (mixed_)
-      SW4G_TRY(launch_record_df(make_box(1, b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke),
-                                reinterpret_cast<const float*>(up),
-                                reinterpret_cast<const float*>(um), drec_, row, dt_, g_.h, initial,
-                                stream_, clk, rec_nvals_));
+      SW4G_TRY(launch_record_df(b, reinterpret_cast<const float*>(lev_[iup]),
+                                reinterpret_cast<const float*>(lev_[ium]), drec_, row, dt_, g_.h, initial,
+                                stream_, clk, rec_nvals_, rec_curv_ ? &rc : nullptr));
    else
-      SW4G_TRY(launch_record(make_box(1, b_.ib, b_.ie, b_.jb, b_.je, b_.kb, b_.ke), up, um, drec_,
-                             row, dt_, g_.h, initial, stream_, clk, rec_nvals_));
+      SW4G_TRY(launch_record(b, lev_[iup], lev_[ium], drec_, row, dt_, g_.h, initial, stream_, clk, rec_nvals_,
+                             rec_curv_ ? &rc : nullptr));
    rec_rows_++;
    return kOk;
 }
@@ -734,26 +743,32 @@ int EW::run_graphed(int nsteps)
    return st;
 }
 
-int EW::set_receivers(int n, const int* ijk, const int* mode, int capacity)
+int EW::set_receivers(int n, const int* ijk, const int* mode, int capacity, const int* grid)
 {
    if (!ready_ || n < 0 || (n > 0 && (!ijk || !mode || capacity < 1))) return kBadArgument;
    drop_graphs();  // the graphs hold the old receiver set
-   std::vector<int> host(5 * (size_t)n);
+   std::vector<int> host(6 * (size_t)n);
    int nvals = 0;
+   bool curv = false;
    for (int r = 0; r < n; r++) {
       const int i = ijk[3 * r], j = ijk[3 * r + 1], k = ijk[3 * r + 2];
+      const int g = grid ? grid[r] : 0;
+      if (g != 0 && !(g == 1 && cv_)) return kBadArgument;
+      const Bounds& bb = g == 1 ? cv_->b : b_;
       const int nv = receiver_values(mode[r]);
       if (nv == 0) return kBadArgument;
       // the value itself needs (i,j,k) in the array; the differences need its neighbours
       const int m = (mode[r] == kRecDisplacement || mode[r] == kRecVelocity) ? 0 : 1;
-      if (i - m < b_.ib || i + m > b_.ie || j - m < b_.jb || j + m > b_.je || k - m < b_.kb ||
-          k + m > b_.ke)
+      if (i - m < bb.ib || i + m > bb.ie || j - m < bb.jb || j + m > bb.je || k - m < bb.kb ||
+          k + m > bb.ke)
          return kBadArgument;
       host[3 * r] = i;
       host[3 * r + 1] = j;
       host[3 * r + 2] = k;
       host[3 * n + r] = mode[r];
       host[4 * n + r] = nvals;
+      host[5 * n + r] = g;
+      curv = curv || g == 1;
       nvals += nv;
    }
    if (drec_mem_ || records_) SW4G_TRY(cuda_ok(cudaStreamSynchronize(stream_)));
@@ -764,6 +779,7 @@ int EW::set_receivers(int n, const int* ijk, const int* mode, int capacity)
    drec_ = ReceiverSet{};
    rec_cap_ = rec_rows_ = rec_nvals_ = 0;
    rec_initial_ = false;
+   rec_curv_ = false;
    if (n == 0) return kOk;
    SW4G_TRY(cuda_ok(cudaMalloc(&drec_mem_, host.size() * sizeof(int))));
    SW4G_TRY(cuda_ok(cudaMemcpy(drec_mem_, host.data(), host.size() * sizeof(int),
@@ -775,9 +791,11 @@ int EW::set_receivers(int n, const int* ijk, const int* mode, int capacity)
    drec_.ijk = d;
    drec_.mode = d + 3 * n;
    drec_.off = d + 4 * n;
+   drec_.grid = curv ? d + 5 * n : nullptr;
    rec_cap_ = capacity;
    rec_nvals_ = nvals;
    rec_initial_ = true;
+   rec_curv_ = curv;
    return kOk;
 }
 
@@ -831,7 +849,7 @@ int EW::step_phases()
    if (cv_) SW4G_TRY(curv_corr(ip, ip));
    SW4G_TRY(enforce_bc(up));
    if (cv_) SW4G_TRY(curv_bc(up, cv_->lev[ip]));
-   if (drec_.n > 0) SW4G_TRY(record(up, um, 0));
+   if (drec_.n > 0) SW4G_TRY(record(ip, ium_, 0));
    ium_ = iu_;
    iu_ = ip;
    t_ += dt;
@@ -1101,7 +1119,7 @@ int EW::step_fused()
       if (which == 3 && !cbeside) SW4G_TRY(curv_corr(ip, iq));
       if (which == 5) SW4G_TRY(curv_bc(lev_[iq], cv_->lev[iq]));
    }
-   if (drec_.n > 0) SW4G_TRY(record(lev_[iq], lev_[ium_], 0));
+   if (drec_.n > 0) SW4G_TRY(record(iq, ium_, 0));
    if (clocked_) SW4G_TRY(launch_clock_advance(dclock_, dt_, drec_.n > 0 ? 1.0 : 0.0, 0.0, stream_));
    ium_ = iu_;
    iu_ = iq;
@@ -1117,7 +1135,7 @@ int EW::step_part(int part)
       if (drec_.n > 0 && rec_rows_ + (rec_initial_ ? 1 : 0) + 1 > rec_cap_) return kBadArgument;
       SW4G_TRY(upload_sources());
       if (drec_.n > 0 && rec_initial_) {
-         SW4G_TRY(record(lev_[iu_], lev_[ium_], 1));
+         SW4G_TRY(record(iu_, ium_, 1));
          rec_initial_ = false;
       }
       int ip = 0;
@@ -1136,7 +1154,7 @@ int EW::step_part(int part)
       SW4G_TRY(piece(kForceCorr, split_ip_, split_iq_));
    } else {
       SW4G_TRY(piece(kBcCorr, split_ip_, split_iq_));
-      if (drec_.n > 0) SW4G_TRY(record(lev_[split_iq_], lev_[ium_], 0));
+      if (drec_.n > 0) SW4G_TRY(record(split_iq_, ium_, 0));
       ium_ = iu_;
       iu_ = split_iq_;
       t_ += dt_;

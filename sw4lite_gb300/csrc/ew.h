@@ -186,8 +186,19 @@ class EW {
    // step appends one row of values (all receivers, in order) to a device record
    // array of `capacity` rows; the first row holds the initial data and is written
    // by the first step after this call.  A step that would overflow the array is
-   // refused before it starts.
-   int set_receivers(int n, const int* ijk, const int* mode, int capacity);
+   // refused before it starts.  grid[n] (may be null: all on grid 0) puts a receiver
+   // on the Cartesian grid (0) or the curvilinear grid (1, with topography).
+   int set_receivers(int n, const int* ijk, const int* mode, int capacity, const int* grid = nullptr);
+   // The grid point and grid of a receiver at (x, y, z) (EW::computeNearestGridPoint,
+   // src/EW.C:5149-5213, with TimeSeries' placement on the curvilinear grid,
+   // src/TimeSeries.C:139-168 and :307-329): nearest (i, j); below the interface the
+   // Cartesian k, at or above it k = round(s) of the inverted grid mapping, limited
+   // to 1..nz (the surface if the mapping cannot be inverted).  kBadArgument for a
+   // point above the topography or outside the grids.
+   int nearest_grid_point(double x, double y, double z, int ijk[3], int* grid) const;
+   // z of the topography surface at (x, y) (EW::find_topo_zcoord_owner,
+   // src/EW.C:6311, with the analytic Gaussian hill); 0 without topography
+   double topography_z(double x, double y) const;
    int record_shape(int* rows, int* nvals) const;
    int get_records(double* out, bool on_device) const;
    // Boundary conditions on an arbitrary 3-component device array of this grid.
@@ -211,7 +222,7 @@ class EW {
    void discretize_into(const SourceSpec& s, std::vector<GridPointSource>& out) const;
    int scan_levels();                 // non-finite scans of the current levels, then the outcome
    int read_status(unsigned long long out[4]);
-   int record(double* up, double* um, int initial);
+   int record(int iup, int ium, int initial);  // levels by index (both grids)
    int step_phases();
    int step_fused();
    int fused_piece(int piece, int ip, int iq);
@@ -288,6 +299,7 @@ class EW {
    double* records_ = nullptr;
    int rec_cap_ = 0, rec_rows_ = 0, rec_nvals_ = 0;
    bool rec_initial_ = false;  // the initial-data row is still to be written
+   bool rec_curv_ = false;     // a receiver lies on the curvilinear grid
 
    std::unique_ptr<CurvGrid> cv_;
    long long grad_store_bytes_ = -1;  // gradient(): budget for kept segments

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "ew.h"
+#include "source_weights.h"
 
 namespace sw4g {
 
@@ -137,6 +138,45 @@ CurvSourceGrid EW::curv_source_grid(bool device) const
    cs.ni = c.b.ie - c.b.ib + 1;
    cs.nij = cs.ni * (c.b.je - c.b.jb + 1);
    return cs;
+}
+
+double EW::topography_z(double x, double y) const
+{
+   return cv_ ? -curv_source_grid(false).elevation(x, y) : 0.0;
+}
+
+int EW::nearest_grid_point(double x, double y, double z, int ijk[3], int* grid) const
+{
+   if (!ijk || !grid) return kBadArgument;
+   if (sub_) return kNotSupported;  // global indices: ask the whole grid's object
+   // nearest (i, j); a point exactly half-way goes to the lower index
+   const double h = g_.h;
+   int i = (int)std::floor(x / h) + 1;
+   if (x - ((i - 0.5) * h) > 0.) i++;
+   int j = (int)std::floor(y / h) + 1;
+   if (y - ((j - 0.5) * h) > 0.) j++;
+   if (i < 1 || i > g_.nx || j < 1 || j > g_.ny) return kBadArgument;
+   ijk[0] = i;
+   ijk[1] = j;
+   if (!cv_ || z > g_.zmin) {  // the Cartesian grid
+      int k = (int)std::floor((z - g_.zmin) / h) + 1;
+      if (z - (g_.zmin + (k - 0.5) * h) > 0.) k++;
+      if (k < 1 || k > g_.nz) return kBadArgument;
+      ijk[2] = k;
+      *grid = 0;
+      return kOk;
+   }
+   // the curvilinear grid: refused above the topography (with the reference's 1e-9
+   // allowance); k from the inverted mapping, the surface where it cannot be inverted
+   const CurvSourceGrid cs = curv_source_grid(false);
+   if (z < -cs.elevation(x, y) - 1e-9) return kBadArgument;
+   int k = 1;
+   double s = 1;
+   if (invert_curvilinear_s(cs, h, x / h + 1, y / h + 1, z, &s))
+      k = std::min(std::max((int)std::lround(s), 1), cv_->nz);
+   ijk[2] = k;
+   *grid = 1;
+   return kOk;
 }
 
 // Grid-point sources of the curvilinear grid into one of its levels (the reference

@@ -107,6 +107,17 @@ struct ReceiverSet {
    const int* ijk = nullptr;   // 3*n
    const int* mode = nullptr;  // n
    const int* off = nullptr;   // n
+   const int* grid = nullptr;  // n: 0 Cartesian, 1 curvilinear; null: all Cartesian
+};
+
+// The curvilinear grid's arrays for receivers on it: its box, the two levels (FP64,
+// or (hi, lo) FP32 pairs in the mixed form), the metric (4 x npts) and Jacobian.
+struct RecCurv {
+   Box b{};
+   const void* up = nullptr;
+   const void* um = nullptr;
+   const double* met = nullptr;
+   const double* jac = nullptr;
 };
 
 // A curvilinear grid's arrays for the curvilinear kernels (curv.cu): 3-component
@@ -233,12 +244,13 @@ int launch_curv_eig(int soa, long long n, const double* rho, const double* mu, c
                     cudaStream_t st);
 
 int receiver_values(int mode);  // values one receiver records per step (0: bad mode)
+// cv: the curvilinear grid's arrays when a receiver lies on it (else null)
 int launch_record(const Box& b, const double* up, const double* um, const ReceiverSet& r,
                   double* row, double dt, double h, int initial, cudaStream_t s,
-                  const double* clk = nullptr, int nvals = 0);
+                  const double* clk = nullptr, int nvals = 0, const RecCurv* cv = nullptr);
 int launch_record_df(const Box& b, const float* up, const float* um, const ReceiverSet& r,
                      double* row, double dt, double h, int initial, cudaStream_t s,
-                  const double* clk = nullptr, int nvals = 0);
+                     const double* clk = nullptr, int nvals = 0, const RecCurv* cv = nullptr);
 
 int upload_sbp_tables_direct();
 
