@@ -6,7 +6,8 @@ TimeSeries::write_usgs_format, src/TimeSeries.C:924) and the decks that made the
 Each fixture keeps a file's header and either all its record rows (the 64-row
 topography files) or a 48-row window around the largest value; usgs_meta.json
 records the total row count, the window's first row and, from the deck, the grid
-spacing, extent, run time and the receiver's requested location.
+spacing, extent, run time and the receiver's requested location.  The LOH.2 deck's
+3200 point sources (its finite fault) go into loh2_h100_sources.npz.
 
     python tests/golden/make_usgs_fixtures.py [REFERENCE_ROOT]
 """
@@ -73,6 +74,26 @@ def main(root):
         meta[name] = p
     (HERE / "usgs_meta.json").write_text(json.dumps(meta, indent=1, sort_keys=True) + "\n")
     sac_fixtures(Path(root) / "tests")
+    source_list(base / "loh2" / "LOH.2-h100.in", HERE / "loh2_h100_sources.npz")
+
+
+def source_list(deck, out):
+    """The point sources of a deck (one `source` line each) as arrays: x, y, z, t0,
+    freq, m0 and the six moment components (mxx, mxy, mxz, myy, myz, mzz; a component
+    the line does not name is 0).  LOH.2's finite fault is 3200 such lines."""
+    import numpy as np
+    comps = ("Mxx", "Mxy", "Mxz", "Myy", "Myz", "Mzz")
+    rows = []
+    for line in deck.read_text().splitlines():
+        if not line.strip().startswith("source "):
+            continue
+        t = _tokens(line.strip())
+        assert t.get("type") == "Gaussian", line
+        rows.append([float(t["x"]), float(t["y"]), float(t["z"]), float(t["t0"]), float(t["freq"]),
+                     float(t.get("m0", "1"))] + [float(t.get(c, "0")) for c in comps])
+    a = np.array(rows)
+    np.savez_compressed(out, x=a[:, 0], y=a[:, 1], z=a[:, 2], t0=a[:, 3], freq=a[:, 4], m0=a[:, 5],
+                        moment=a[:, 6:])
 
 
 # SAC traces stored beside the USGS file of the same run under the reference's
