@@ -105,6 +105,28 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
       return (long long)(gi - a.ib) + a.ni * (gj - a.jb) + a.nij * (long long)(gk - a.kb);
    };
 
+   // Damping (corrector and adjoint forms): an axis' term at a point is computed where
+   // that axis' profile dc is nonzero at one of the point's three neighbours along the
+   // axis; elsewhere it is exactly zero.  The x and y tests hold for the whole column;
+   // need_d (uniform over the CTA) says whether any point of the CTA's columns and
+   // planes has a term, and the damping field u - um is only formed where it does.
+   bool dampx = false, dampy = false, need_d = false;
+   if (CORR) {
+      bool any = false;
+      if (a.beta != 0) {
+         if (active) {
+            dampx = nonzero_bits(__ldg(a.dc[0] + (i - 1 - a.ib))) || nonzero_bits(__ldg(a.dc[0] + (i - a.ib))) ||
+                    nonzero_bits(__ldg(a.dc[0] + (i + 1 - a.ib)));
+            dampy = nonzero_bits(__ldg(a.dc[1] + (j - 1 - a.jb))) || nonzero_bits(__ldg(a.dc[1] + (j - a.jb))) ||
+                    nonzero_bits(__ldg(a.dc[1] + (j + 1 - a.jb)));
+         }
+         any = dampx || dampy;
+         for (int kk = kbeg - 1 + tid; kk <= kend + 1; kk += NTHREADS)
+            any = any || nonzero_bits(__ldg(a.dc[2] + (kk - a.kb)));
+      }
+      need_d = __syncthreads_or(any) != 0;
+   }
+
    // Stage plane kk (with halo) of the stage field, and for the corrector the
    // damping field u - um.  Points beyond the array edge are never read by an
    // active column and are zero-filled.
@@ -124,17 +146,17 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
                } else if (CORR == 1) {
                   const double uu = __ldg(a.u + p + c * npts), uum = __ldg(a.um + p + c * npts);
                   v[c] = (__ldg(a.up + p + c * npts) - 2 * uu) + uum;
-                  d[c] = uu - uum;
+                  if (need_d) d[c] = uu - uum;
                } else {
                   v[c] = __ldg(a.up + p + c * npts);
-                  d[c] = __ldg(a.u + p + c * npts) - __ldg(a.um + p + c * npts);
+                  if (need_d) d[c] = __ldg(a.u + p + c * npts) - __ldg(a.um + p + c * npts);
                }
             }
          }
 #pragma unroll
          for (int c = 0; c < 3; c++) {
             vs[c * PLANE + idx] = v[c];
-            if (CORR) ds[c * PLANE + idx] = d[c];
+            if (CORR && need_d) ds[c * PLANE + idx] = d[c];
          }
       }
    };
@@ -164,22 +186,43 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
    constexpr int kPre = (PLANE + NTHREADS - 1) / NTHREADS;  // values per thread
    double pv[kPre][3], pm[kPre][2], pd[kPre][3];
    auto prefetch_plane = [&](int kk) {
+      if (CORR == 0 || need_d) {
 #pragma unroll
-      for (int r = 0; r < kPre; r++) {
-         const int idx = tid + r * NTHREADS;
-         const int li = idx % PX, lj = idx / PX;
-         const int gi = i0 - HALO + li, gj = j0 - HALO + lj;
-         const bool ok = idx < PLANE && gi <= a.ie && gj <= a.je;
-         const long long p = ok ? gidx(gi, gj, kk) : 0;
+         for (int r = 0; r < kPre; r++) {
+            const int idx = tid + r * NTHREADS;
+            const int li = idx % PX, lj = idx / PX;
+            const int gi = i0 - HALO + li, gj = j0 - HALO + lj;
+            const bool ok = idx < PLANE && gi <= a.ie && gj <= a.je;
+            const long long p = ok ? gidx(gi, gj, kk) : 0;
 #pragma unroll
-         for (int c = 0; c < 3; c++) {
-            if (CORR == 0) {
-               pv[r][c] = ok ? __ldg(a.u + p + c * npts) : 0.0;
-            } else {
-               const double uu = ok ? __ldg(a.u + p + c * npts) : 0.0, uum = ok ? __ldg(a.um + p + c * npts) : 0.0;
+            for (int c = 0; c < 3; c++) {
+               if (CORR == 0) {
+                  pv[r][c] = ok ? __ldg(a.u + p + c * npts) : 0.0;
+               } else {
+                  const double uu = ok ? __ldg(a.u + p + c * npts) : 0.0, uum = ok ? __ldg(a.um + p + c * npts) : 0.0;
+                  const double upp = ok ? __ldg(a.up + p + c * npts) : 0.0;
+                  pv[r][c] = CORR == 1 ? (upp - 2 * uu) + uum : upp;
+                  pd[r][c] = uu - uum;
+               }
+            }
+         }
+      } else {  // no damping in this CTA: the stage field alone
+#pragma unroll
+         for (int r = 0; r < kPre; r++) {
+            const int idx = tid + r * NTHREADS;
+            const int li = idx % PX, lj = idx / PX;
+            const int gi = i0 - HALO + li, gj = j0 - HALO + lj;
+            const bool ok = idx < PLANE && gi <= a.ie && gj <= a.je;
+            const long long p = ok ? gidx(gi, gj, kk) : 0;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
                const double upp = ok ? __ldg(a.up + p + c * npts) : 0.0;
-               pv[r][c] = CORR == 1 ? (upp - 2 * uu) + uum : upp;
-               pd[r][c] = uu - uum;
+               if (CORR == 1) {
+                  const double uu = ok ? __ldg(a.u + p + c * npts) : 0.0, uum = ok ? __ldg(a.um + p + c * npts) : 0.0;
+                  pv[r][c] = (upp - 2 * uu) + uum;
+               } else {
+                  pv[r][c] = upp;
+               }
             }
          }
       }
@@ -194,7 +237,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                vs[c * PLANE + idx] = pv[r][c];
-               if (CORR) ds[c * PLANE + idx] = pd[r][c];
+               if (CORR && need_d) ds[c * PLANE + idx] = pd[r][c];
             }
       }
    };
@@ -264,7 +307,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
    for (int kk = kbeg - 2; kk <= kbeg; kk++) {
       const int q = kk - kbeg + 3;  // 1..3
       if (active) compute_gz(kk, gz[q]);
-      if (CORR) {
+      if (CORR && need_d) {
          const double* ds = Dd + mod3(kk) * 3 * PLANE;
 #pragma unroll
          for (int c = 0; c < 3; c++) dq[q][c] = ds[c * PLANE + own];
@@ -274,7 +317,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
    load_plane(kbeg + 1);
    __syncthreads();
    if (active) compute_gz(kbeg + 1, gz[4]);
-   if (CORR) {
+   if (CORR && need_d) {
       const double* ds = Dd + mod3(kbeg + 1) * 3 * PLANE;
 #pragma unroll
       for (int c = 0; c < 3; c++) dq[4][c] = ds[c * PLANE + own];
@@ -304,7 +347,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
             if (CORR) dq[q][c] = dq[q + 1][c];
          }
       if (active) compute_gz(k + 2, gz[4]);
-      if (CORR) {
+      if (CORR && need_d) {
          const double* ds = Dd + mod3(k + 2) * 3 * PLANE;
 #pragma unroll
          for (int c = 0; c < 3; c++) dq[4][c] = ds[c * PLANE + own];
@@ -436,15 +479,19 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
             }
          } else {
             double sg[3] = {0, 0, 0};
-            if (a.beta != 0) {
+            // z: dc at k-1..k+1 (uniform over the CTA); x, y: the column's flags
+            const bool dampz = need_d && (nonzero_bits(__ldg(a.dc[2] + (k - 1 - a.kb))) ||
+                                          nonzero_bits(__ldg(a.dc[2] + (k - a.kb))) ||
+                                          nonzero_bits(__ldg(a.dc[2] + (k + 1 - a.kb))));
+            if (dampx || dampy || dampz) {
                const double* ds = Dd + mod3(k) * 3 * PLANE;
                const double cxi = __ldg(a.co[0] + (i - a.ib));
                const double cyj = __ldg(a.co[1] + (j - a.jb));
                const double czk = __ldg(a.co[2] + (k - a.kb));
                // x: e = rho*dc at i-1..i+1 (skipped where dc vanishes: the term is exactly 0)
-               const double dx0 = __ldg(a.dc[0] + (i - 1 - a.ib)), dx1 = __ldg(a.dc[0] + (i - a.ib)),
-                            dx2 = __ldg(a.dc[0] + (i + 1 - a.ib));
-               if (dx0 != 0 || dx1 != 0 || dx2 != 0) {
+               if (dampx) {
+                  const double dx0 = __ldg(a.dc[0] + (i - 1 - a.ib)), dx1 = __ldg(a.dc[0] + (i - a.ib)),
+                               dx2 = __ldg(a.dc[0] + (i + 1 - a.ib));
                   const double e0 = RH[own - 1] * dx0, e1 = RH[own] * dx1, e2 = RH[own + 1] * dx2;
                   const double wx = sxi * cyj * czk;
 #pragma unroll
@@ -455,9 +502,9 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
                      sg[c] += wx * s;
                   }
                }
-               const double dy0 = __ldg(a.dc[1] + (j - 1 - a.jb)), dy1 = __ldg(a.dc[1] + (j - a.jb)),
-                            dy2 = __ldg(a.dc[1] + (j + 1 - a.jb));
-               if (dy0 != 0 || dy1 != 0 || dy2 != 0) {
+               if (dampy) {
+                  const double dy0 = __ldg(a.dc[1] + (j - 1 - a.jb)), dy1 = __ldg(a.dc[1] + (j - a.jb)),
+                               dy2 = __ldg(a.dc[1] + (j + 1 - a.jb));
                   const double e0 = RH[own - PX] * dy0, e1 = RH[own] * dy1, e2 = RH[own + PX] * dy2;
                   const double wy = syj * cxi * czk;
 #pragma unroll
@@ -469,9 +516,9 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
                      sg[c] += wy * s;
                   }
                }
-               const double dz0 = __ldg(a.dc[2] + (k - 1 - a.kb)), dz1 = __ldg(a.dc[2] + (k - a.kb)),
-                            dz2 = __ldg(a.dc[2] + (k + 1 - a.kb));
-               if (dz0 != 0 || dz1 != 0 || dz2 != 0) {
+               if (dampz) {
+                  const double dz0 = __ldg(a.dc[2] + (k - 1 - a.kb)), dz1 = __ldg(a.dc[2] + (k - a.kb)),
+                               dz2 = __ldg(a.dc[2] + (k + 1 - a.kb));
                   const double e0 = __ldg(a.rho + p - a.nij) * dz0, e1 = RH[own] * dz1,
                                e2 = __ldg(a.rho + p + a.nij) * dz2;
                   const double wz = szk * cxi * cyj;

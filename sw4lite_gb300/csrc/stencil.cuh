@@ -31,4 +31,12 @@ __device__ __forceinline__ R d1c(R fm2, R fm1, R fp1, R fp2)
    return (fm2 - fp2) + R(8) * (fp1 - fm1);
 }
 
+// x != 0.0 for every double x (true for NaN, false for -0.0), tested on the bit pattern
+// by the integer pipe: FP64-pipe-bound kernels keep their FP64 issue slots for the
+// arithmetic.
+__device__ __forceinline__ bool nonzero_bits(double x)
+{
+   return (__double_as_longlong(x) & 0x7fffffffffffffffLL) != 0;
+}
+
 }  // namespace sw4g
