@@ -6,6 +6,7 @@ Usage: python -m sw4lite_gb300.builder [--force]
 from __future__ import annotations
 
 import concurrent.futures as cf
+import fcntl
 import os
 import shutil
 import subprocess
@@ -54,6 +55,16 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if not force and not _stale(LIB, deps):
         return LIB
     OUT.mkdir(exist_ok=True)
+    # Several processes (parallel test workers, a test and a benchmark) may find the
+    # library stale at once: one builds, the others wait and then find it current.
+    with open(OUT / "build.lock", "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        if not force and not _stale(LIB, deps):
+            return LIB
+        return _build_locked(srcs, verbose)
+
+
+def _build_locked(srcs, verbose: bool) -> Path:
     cc = nvcc()
 
     def compile_one(src: Path) -> Path:

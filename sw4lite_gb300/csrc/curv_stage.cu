@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) curv_stage_kernel(StageArgs a)
                const double cxi = __ldg(a.cox + (i - b.ib)), cyj = __ldg(a.coy + (j - b.jb));
                const double dx0 = __ldg(a.dcx + (i - 1 - b.ib)), dx1 = __ldg(a.dcx + (i - b.ib)),
                             dx2 = __ldg(a.dcx + (i + 1 - b.ib));
-               if (dx0 != 0 || dx1 != 0 || dx2 != 0) {
+               if (nonzero_bits(dx0) || nonzero_bits(dx1) || nonzero_bits(dx2)) {  // integer pipe
                   const double e0 = RJ[own - 1] * dx0, e1 = RJ[own] * dx1, e2 = RJ[own + 1] * dx2;
 #pragma unroll
                   for (int c = 0; c < 3; c++) {
@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) curv_stage_kernel(StageArgs a)
                }
                const double dy0 = __ldg(a.dcy + (j - 1 - b.jb)), dy1 = __ldg(a.dcy + (j - b.jb)),
                             dy2 = __ldg(a.dcy + (j + 1 - b.jb));
-               if (dy0 != 0 || dy1 != 0 || dy2 != 0) {
+               if (nonzero_bits(dy0) || nonzero_bits(dy1) || nonzero_bits(dy2)) {
                   const double e0 = RJ[own - PX] * dy0, e1 = RJ[own] * dy1, e2 = RJ[own + PX] * dy2;
 #pragma unroll
                   for (int c = 0; c < 3; c++) {
