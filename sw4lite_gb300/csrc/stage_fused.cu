@@ -28,6 +28,7 @@
 //    (the stage field read from `up` directly).
 #include <algorithm>
 #include <atomic>
+#include <type_traits>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -77,6 +78,19 @@ __host__ __device__ constexpr int smem_doubles(int corr)
 
 __device__ __forceinline__ int mod5(int k) { return ((k % 5) + 5) % 5; }
 __device__ __forceinline__ int mod3(int k) { return ((k % 3) + 3) % 3; }
+
+// The centred first difference (fm2 - fp2) + 8 (fp1 - fm1) with its roundings
+// spelled out, so that every copy of the code that forms it rounds alike.
+__device__ __forceinline__ double d1r(double fm2, double fm1, double fp1, double fp2)
+{
+   return __fma_rn(8.0, __dsub_rn(fp1, fm1), __dsub_rn(fm2, fp2));
+}
+
+// x == 1.0 exactly, from the bit pattern (no FP64 instruction).
+__device__ __forceinline__ bool is_one(double x)
+{
+   return __double_as_longlong(x) == 0x3ff0000000000000LL;
+}
 
 template <int CORR>
 __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
@@ -280,6 +294,20 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
    const double sxi = active ? __ldg(a.sx + (i - a.ib)) : 0.0;
    const double syj = active ? __ldg(a.sy + (j - a.jb)) : 0.0;
 
+   // Away from the supergrid layers the stretching is exactly 1.  xu (yu): every
+   // active column (row) of the CTA has s_x = 1 (s_y = 1); zu, per plane, s_z = 1.
+   // Where they hold, the mixed-derivative products skip their multiplications by
+   // the stretching.  Both forms round alike (x * 1 = x, fma(1, a, b) = a + b), so
+   // the result does not depend on which form a CTA takes.
+   bool xu, yu;
+   {
+      bool okx = true, oky = true;
+      if (tid < TX && i0 + tid <= a.ie - 2) okx = is_one(__ldg(a.sx + (i0 + tid - a.ib)));
+      if (tid < TY && j0 + tid <= a.je - 2) oky = is_one(__ldg(a.sy + (j0 + tid - a.jb)));
+      xu = __syncthreads_and(okx) != 0;
+      yu = __syncthreads_and(oky) != 0;
+   }
+
    // z-outer products G_z at plane kk for the own column: components for
    // (mu w_x)_z, (mu w_y)_z and (lambda (u_x, v_y))_z.
    auto compute_gz = [&](int kk, double g[3]) {
@@ -287,15 +315,21 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
       const double* vu = vs;
       const double* vv = vs + PLANE;
       const double* vw = vs + 2 * PLANE;
-      const double dxw = d1c(vw[own - 2], vw[own - 1], vw[own + 1], vw[own + 2]);
-      const double dyw = d1c(vw[own - 2 * PX], vw[own - PX], vw[own + PX], vw[own + 2 * PX]);
-      const double dxu = d1c(vu[own - 2], vu[own - 1], vu[own + 1], vu[own + 2]);
-      const double dyv = d1c(vv[own - 2 * PX], vv[own - PX], vv[own + PX], vv[own + 2 * PX]);
+      const double dxw = d1r(vw[own - 2], vw[own - 1], vw[own + 1], vw[own + 2]);
+      const double dyw = d1r(vw[own - 2 * PX], vw[own - PX], vw[own + PX], vw[own + 2 * PX]);
+      const double dxu = d1r(vu[own - 2], vu[own - 1], vu[own + 1], vu[own + 2]);
+      const double dyv = d1r(vv[own - 2 * PX], vv[own - PX], vv[own + PX], vv[own + 2 * PX]);
       const long long p = gidx(i, j, kk);
       const double m = __ldg(a.mu + p), l = __ldg(a.la + p);
-      g[0] = m * sxi * dxw;
-      g[1] = m * syj * dyw;
-      g[2] = l * (sxi * dxu + syj * dyv);
+      if (xu && yu) {
+         g[0] = __dmul_rn(m, dxw);
+         g[1] = __dmul_rn(m, dyw);
+         g[2] = __dmul_rn(l, __dadd_rn(dxu, dyv));
+      } else {
+         g[0] = __dmul_rn(__dmul_rn(m, sxi), dxw);
+         g[1] = __dmul_rn(__dmul_rn(m, syj), dyw);
+         g[2] = __dmul_rn(l, __fma_rn(sxi, dxu, __dmul_rn(syj, dyv)));
+      }
    };
 
    double gz[5][3];   // G_z at planes k-2..k+2
@@ -354,62 +388,91 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
       }
 
       const double szk = __ldg(a.sz + (k - a.kb));
+      const bool zu = is_one(szk);
       const double* vm2 = V + mod5(k - 2) * 3 * PLANE;
       const double* vm1 = V + mod5(k - 1) * 3 * PLANE;
       const double* v0 = V + mod5(k) * 3 * PLANE;
       const double* vp1 = V + mod5(k + 1) * 3 * PLANE;
       const double* vp2 = V + mod5(k + 2) * 3 * PLANE;
       auto dz = [&](int c, int idx) {
-         return d1c(vm2[c * PLANE + idx], vm1[c * PLANE + idx], vp1[c * PLANE + idx],
+         return d1r(vm2[c * PLANE + idx], vm1[c * PLANE + idx], vp1[c * PLANE + idx],
                     vp2[c * PLANE + idx]);
       };
 
       // x-outer products over the x-extended rows (all 36 columns, own 8 rows):
       //   G_x = { la (s_y v_y + s_z w_z),  mu s_y u_y,  mu s_z u_z }
-      for (int idx = tid; idx < TY * PX; idx += NTHREADS) {
-         const int li = idx % PX, ljr = idx / PX;
-         const int s = (ljr + HALO) * PX + li;
-         const int gi = i0 - HALO + li, gj = j0 + ljr;
-         double g0 = 0, g1 = 0, g2 = 0;
-         if (gi <= a.ie && gj <= a.je) {
-            const double syy = __ldg(a.sy + (gj - a.jb));
-            const double* vu = v0;
-            const double* vv = v0 + PLANE;
-            const double dyv = d1c(vv[s - 2 * PX], vv[s - PX], vv[s + PX], vv[s + 2 * PX]);
-            const double dyu = d1c(vu[s - 2 * PX], vu[s - PX], vu[s + PX], vu[s + 2 * PX]);
-            const double dzw = dz(2, s), dzu = dz(0, s);
-            const double m = MU[s], l = LA[s];
-            g0 = l * (syy * dyv + szk * dzw);
-            g1 = m * syy * dyu;
-            g2 = m * szk * dzu;
+      // (unit: s_y = s_z = 1 on the rows whose products are used)
+      auto gx_products = [&](auto unit) {
+         constexpr bool U = decltype(unit)::value;
+         for (int idx = tid; idx < TY * PX; idx += NTHREADS) {
+            const int li = idx % PX, ljr = idx / PX;
+            const int s = (ljr + HALO) * PX + li;
+            const int gi = i0 - HALO + li, gj = j0 + ljr;
+            double g0 = 0, g1 = 0, g2 = 0;
+            if (gi <= a.ie && gj <= a.je) {
+               const double* vu = v0;
+               const double* vv = v0 + PLANE;
+               const double dyv = d1r(vv[s - 2 * PX], vv[s - PX], vv[s + PX], vv[s + 2 * PX]);
+               const double dyu = d1r(vu[s - 2 * PX], vu[s - PX], vu[s + PX], vu[s + 2 * PX]);
+               const double dzw = dz(2, s), dzu = dz(0, s);
+               const double m = MU[s], l = LA[s];
+               if (U) {
+                  g0 = __dmul_rn(l, __dadd_rn(dyv, dzw));
+                  g1 = __dmul_rn(m, dyu);
+                  g2 = __dmul_rn(m, dzu);
+               } else {
+                  const double syy = __ldg(a.sy + (gj - a.jb));
+                  g0 = __dmul_rn(l, __fma_rn(syy, dyv, __dmul_rn(szk, dzw)));
+                  g1 = __dmul_rn(__dmul_rn(m, syy), dyu);
+                  g2 = __dmul_rn(__dmul_rn(m, szk), dzu);
+               }
+            }
+            GX[0 * TY * PX + idx] = g0;
+            GX[1 * TY * PX + idx] = g1;
+            GX[2 * TY * PX + idx] = g2;
          }
-         GX[0 * TY * PX + idx] = g0;
-         GX[1 * TY * PX + idx] = g1;
-         GX[2 * TY * PX + idx] = g2;
-      }
+      };
       // y-outer products over the y-extended columns (own 32 columns, all 12 rows):
       //   G_y = { mu s_x v_x,  la (s_x u_x + s_z w_z),  mu s_z v_z }
-      for (int idx = tid; idx < PY * TX; idx += NTHREADS) {
-         const int lic = idx % TX, lj = idx / TX;
-         const int s = lj * PX + lic + HALO;
-         const int gi = i0 + lic, gj = j0 - HALO + lj;
-         double g0 = 0, g1 = 0, g2 = 0;
-         if (gi <= a.ie && gj <= a.je) {
-            const double sxx = __ldg(a.sx + (gi - a.ib));
-            const double* vu = v0;
-            const double* vv = v0 + PLANE;
-            const double dxv = d1c(vv[s - 2], vv[s - 1], vv[s + 1], vv[s + 2]);
-            const double dxu = d1c(vu[s - 2], vu[s - 1], vu[s + 1], vu[s + 2]);
-            const double dzw = dz(2, s), dzv = dz(1, s);
-            const double m = MU[s], l = LA[s];
-            g0 = m * sxx * dxv;
-            g1 = l * (sxx * dxu + szk * dzw);
-            g2 = m * szk * dzv;
+      // (unit: s_x = s_z = 1 on the columns whose products are used)
+      auto gy_products = [&](auto unit) {
+         constexpr bool U = decltype(unit)::value;
+         for (int idx = tid; idx < PY * TX; idx += NTHREADS) {
+            const int lic = idx % TX, lj = idx / TX;
+            const int s = lj * PX + lic + HALO;
+            const int gi = i0 + lic, gj = j0 - HALO + lj;
+            double g0 = 0, g1 = 0, g2 = 0;
+            if (gi <= a.ie && gj <= a.je) {
+               const double* vu = v0;
+               const double* vv = v0 + PLANE;
+               const double dxv = d1r(vv[s - 2], vv[s - 1], vv[s + 1], vv[s + 2]);
+               const double dxu = d1r(vu[s - 2], vu[s - 1], vu[s + 1], vu[s + 2]);
+               const double dzw = dz(2, s), dzv = dz(1, s);
+               const double m = MU[s], l = LA[s];
+               if (U) {
+                  g0 = __dmul_rn(m, dxv);
+                  g1 = __dmul_rn(l, __dadd_rn(dxu, dzw));
+                  g2 = __dmul_rn(m, dzv);
+               } else {
+                  const double sxx = __ldg(a.sx + (gi - a.ib));
+                  g0 = __dmul_rn(__dmul_rn(m, sxx), dxv);
+                  g1 = __dmul_rn(l, __fma_rn(sxx, dxu, __dmul_rn(szk, dzw)));
+                  g2 = __dmul_rn(__dmul_rn(m, szk), dzv);
+               }
+            }
+            GY[0 * PY * TX + idx] = g0;
+            GY[1 * PY * TX + idx] = g1;
+            GY[2 * PY * TX + idx] = g2;
          }
-         GY[0 * PY * TX + idx] = g0;
-         GY[1 * PY * TX + idx] = g1;
-         GY[2 * PY * TX + idx] = g2;
-      }
+      };
+      if (yu && zu)
+         gx_products(std::true_type{});
+      else
+         gx_products(std::false_type{});
+      if (xu && zu)
+         gy_products(std::true_type{});
+      else
+         gy_products(std::false_type{});
       __syncthreads();
 
       if (active) {
@@ -459,15 +522,24 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
                }
             }
             // mixed terms: outer differences of the staged products
+            auto mixed_terms = [&](auto unit) {
+               constexpr bool U = decltype(unit)::value;
 #pragma unroll
-            for (int c = 0; c < 3; c++) {
-               const double* gx = GX + c * TY * PX + ty * PX + tx;  // li = tx .. tx+4
-               const double* gy = GY + c * PY * TX + ty * TX + tx;  // lj = ty .. ty+4
-               const double cx = d1c(gx[0], gx[1], gx[3], gx[4]);
-               const double cy = d1c(gy[0], gy[TX], gy[3 * TX], gy[4 * TX]);
-               const double cz = d1c(gz[0][c], gz[1][c], gz[3][c], gz[4][c]);
-               lu[c] = acc[c] + a.cof144 * (sxi * cx + syj * cy + szk * cz);
-            }
+               for (int c = 0; c < 3; c++) {
+                  const double* gx = GX + c * TY * PX + ty * PX + tx;  // li = tx .. tx+4
+                  const double* gy = GY + c * PY * TX + ty * TX + tx;  // lj = ty .. ty+4
+                  const double cx = d1r(gx[0], gx[1], gx[3], gx[4]);
+                  const double cy = d1r(gy[0], gy[TX], gy[3 * TX], gy[4 * TX]);
+                  const double cz = d1r(gz[0][c], gz[1][c], gz[3][c], gz[4][c]);
+                  const double t = U ? __dadd_rn(cx, __dadd_rn(cy, cz))
+                                     : __fma_rn(sxi, cx, __fma_rn(syj, cy, __dmul_rn(szk, cz)));
+                  lu[c] = __fma_rn(a.cof144, t, acc[c]);
+               }
+            };
+            if (xu && yu && zu)
+               mixed_terms(std::true_type{});
+            else
+               mixed_terms(std::false_type{});
          }
          const double ir = __ldg(a.irho + p);
          const double cr = a.coef * ir;
