@@ -89,10 +89,10 @@ CORR_STAGE_WORDS = 15
 # moves this many bytes per point at any size
 CORR_STAGE_DRAM_BYTES_PER_PT = 298.6
 # FP64-pipe warp instructions per interior point of the FP64 stage kernels on the
-# 512^3 workload (smsp__inst_executed_pipe_fp64.sum, one single-pass ncu capture of
-# the full-size run: 830,809,640 and 696,971,264 over 512^3 points).  The pipe issues
+# 512^3 workload (smsp__inst_executed_pipe_fp64.sum, single-pass ncu captures of the
+# full-size run: corrector 830,809,640 and predictor 671,186,048 over 512^3 points).  The pipe issues
 # 2 FP64 thread instructions per clock per SM, i.e. one warp instruction per 16 clocks.
-FP64_WARP_INST_PER_PT = {"corr": 830809640 / 512 ** 3, "pred": 696971264 / 512 ** 3}
+FP64_WARP_INST_PER_PT = {"corr": 830809640 / 512 ** 3, "pred": 671186048 / 512 ** 3}
 FP64_THREAD_INST_PER_CLK_PER_SM = 2
 # mixed form, corrector stage: reads Up, U, Um as double-float pairs (9 x 8 B), mu,
 # lambda, rho in FP32 (3 x 4 B), writes the new level (3 x 8 B): the compulsory bytes

@@ -482,6 +482,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
          {
             const long long off[3] = {1, a.ni, a.nij};
             const double sc[3] = {sxi, syj, szk};
+            const bool one[3] = {is_one(sxi), is_one(syj), zu};
             double acc[3] = {0, 0, 0};
 #pragma unroll
             for (int ax = 0; ax < 3; ax++) {
@@ -497,29 +498,45 @@ __global__ void __launch_bounds__(NTHREADS, 2) fused_stage_kernel(FusedArgs a)
                   wt[t][3] = __ldg(w1 + p + 2 * o);
                   wt[t][4] = __ldg(a.ws[ax * 2 + t] + p);
                }
+               auto second_differences = [&](auto unit) {
+                  constexpr bool U = decltype(unit)::value;
 #pragma unroll
-               for (int c = 0; c < 3; c++) {
-                  double f[5];
-                  if (ax == 0) {
+                  for (int c = 0; c < 3; c++) {
+                     double f[5];
+                     if (ax == 0) {
 #pragma unroll
-                     for (int m = -2; m <= 2; m++) f[m + 2] = v0[c * PLANE + own + m];
-                  } else if (ax == 1) {
+                        for (int m = -2; m <= 2; m++) f[m + 2] = v0[c * PLANE + own + m];
+                     } else if (ax == 1) {
 #pragma unroll
-                     for (int m = -2; m <= 2; m++) f[m + 2] = v0[c * PLANE + own + m * PX];
-                  } else {
-                     f[0] = vm2[c * PLANE + own];
-                     f[1] = vm1[c * PLANE + own];
-                     f[2] = v0[c * PLANE + own];
-                     f[3] = vp1[c * PLANE + own];
-                     f[4] = vp2[c * PLANE + own];
+                        for (int m = -2; m <= 2; m++) f[m + 2] = v0[c * PLANE + own + m * PX];
+                     } else {
+                        f[0] = vm2[c * PLANE + own];
+                        f[1] = vm1[c * PLANE + own];
+                        f[2] = v0[c * PLANE + own];
+                        f[3] = vp1[c * PLANE + own];
+                        f[4] = vp2[c * PLANE + own];
+                     }
+                     // sum_m W_m (f_m - f_0) as sum_m W_m f_m - (sum_m W_m) f_0: five FMAs
+                     // instead of four subtractions and four products
+                     const double* wv = wt[ax == c ? 1 : 0];
+                     if (U) {  // s = 1: the terms join the running sum, one FMA fewer
+                        acc[c] = __fma_rn(-wv[4], f[2], __fma_rn(wv[3], f[4], __fma_rn(wv[2], f[3],
+                                 __fma_rn(wv[1], f[1], __fma_rn(wv[0], f[0], acc[c])))));
+                     } else {
+                        const double s = fma(-wv[4], f[2], fma(wv[3], f[4], fma(wv[2], f[3],
+                                                                              fma(wv[1], f[1], wv[0] * f[0]))));
+                        acc[c] += sc[ax] * s;
+                     }
                   }
-                  // sum_m W_m (f_m - f_0) as sum_m W_m f_m - (sum_m W_m) f_0: five FMAs
-                  // instead of four subtractions and four products
-                  const double* wv = wt[ax == c ? 1 : 0];
-                  const double s = fma(-wv[4], f[2], fma(wv[3], f[4], fma(wv[2], f[3],
-                                                                        fma(wv[1], f[1], wv[0] * f[0]))));
-                  acc[c] += sc[ax] * s;
-               }
+               };
+               // per point (not per CTA: the two forms round differently), so a point's
+               // result does not depend on the tiling; predictor form only: the corrector
+               // and adjoint forms sit at the register cap, where the second code path
+               // costs more in spills than the FMA it saves
+               if (CORR == 0 && one[ax])
+                  second_differences(std::true_type{});
+               else
+                  second_differences(std::false_type{});
             }
             // mixed terms: outer differences of the staged products
             auto mixed_terms = [&](auto unit) {
